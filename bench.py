@@ -1,0 +1,268 @@
+"""Benchmark: H-matrix product throughput on one GB300 (and N replicas).
+
+Workload (BASELINE configuration 2 geometry): N = 100 000 points uniform on
+the unit sphere (seeded), Laplace single-layer kernel 1/(4 pi r) with a zero
+diagonal, eta = 10, epsilon = 1e-6, partialACA, minclustersize 10; one
+N(0,1) right-hand side per product.  The H-matrix is assembled on the GPU
+(device generator + batched device partialACA); a "step" is one product
+y = H x (mvprod_global_to_global), permutations included.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Prints one JSON line.  `value` is the device-resident throughput (x and y in
+HBM); `e2e` is the same product through the C ABI from pinned host memory,
+host<->device copies inside the timed region.  `--impl reference` times the
+CPU restatement of htool's product (oracle/) on all host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H-matvec/s and % HBM roofline at rel err ≤1e-6, mixed vs plain FP64; ACA secs"
+UNIT = "H-matvec/s"
+WORKLOAD = dict(workload="laplace_sphere", n=100000, kernel="1/(4 pi r), 0 on the diagonal", eta=10.0, epsilon=1e-6, minclustersize=10, compressor="partialACA", mu=1)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--n", type=int, default=WORKLOAD["n"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits", "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [c.strip() for c in r]
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n, reps=10):
+    """The CPU restatement of htool's product (oracle/htool_oracle.c) on all
+    host cores, same workload; its assembly is not timed."""
+    from htool_gb300 import geometry as G
+    from oracle.oracle import Oracle, build_port
+
+    build_port()
+    O = Oracle("port")
+    threads = os.cpu_count() or 1
+    O.set_num_threads(threads)
+    pts = G.sphere(n, seed=1)
+    t = O.cluster(pts)
+    t0 = time.perf_counter()
+    H = O.hmatrix(t, t, pts, pts, 1, WORKLOAD["epsilon"], WORKLOAD["eta"])
+    build_s = time.perf_counter() - t0
+    x = G.rhs(n, 1, seed=2)
+    sec = H.time_mvprod(x, 1, reps)
+    return {"value": 1.0 / sec, "unit": UNIT, "cores": threads, "kind": "port", "sample": "%d products (median) of the N=%d Laplace-sphere H-matrix after one warm-up; assembly %.2f s not timed" % (reps, n, build_s), "build_seconds": build_s}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cb = cpu_baseline(args.n, reps=max(args.steps, 3))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere)", "config": dict(WORKLOAD, n=args.n),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "aca_seconds": cb["build_seconds"]}
+    print(json.dumps(line), flush=True)
+
+
+def sampled_dense_error(pts, x, y, nrows=1000, seed=3):
+    """||y - A x|| / ||A x|| over nrows sampled rows of the dense kernel matrix."""
+    rows = np.random.default_rng(seed).choice(pts.shape[0], nrows, replace=False)
+    ref = np.empty(nrows)
+    for a in range(0, nrows, 50):
+        r = rows[a:a + 50]
+        d = np.sqrt(((pts[r, None, :] - pts[None, :, :]) ** 2).sum(-1))
+        with np.errstate(divide="ignore"):
+            k = np.where(d == 0, 0.0, 1.0 / (4 * np.pi * d))
+        ref[a:a + 50] = k @ x
+    return float(np.linalg.norm(y[rows] - ref) / np.linalg.norm(ref))
+
+
+def run_gpu(args):
+    import torch
+
+    import htool_gb300 as H
+    from htool_gb300 import geometry as G
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    n = args.n
+    pts = G.sphere(n, seed=1)
+    t = H.Cluster().build(n, pts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hm = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).build(H.LAPLACE, pts)
+    aca_seconds = time.perf_counter() - t0
+    info = hm.get_infos()
+
+    x = G.rhs(n, 1, seed=2)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty(n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    for _ in range(args.warmup):
+        hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
+    e1.record(stream)
+    barrier()
+    ms_total = e0.elapsed_time(e1)
+    launches_per_step = hm.last_launches()
+    # per-launch breakdown (same stream, events between launches)
+    phase_ms = hm.profile(1, max(3, args.steps // 2))
+    clk = clocks.stop()
+    if world > 1:
+        tt = torch.tensor([ms_total], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    ms_step = ms_total / args.steps
+    value = world * args.steps / (ms_total / 1e3)
+
+    # end to end through the C ABI: pinned host x -> device -> product -> host y
+    xh = torch.from_numpy(x).pin_memory()
+    yh = torch.empty(n, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
+    barrier()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
+    e2e_s = time.perf_counter() - w0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    y = yh.numpy().copy()
+    err = sampled_dense_error(pts, x, y)
+    peak, peak_kind = measured_peaks()
+    lr, dn = hm.get_leaves()
+    b_v = 8 * int(np.sum(lr[:, 4].astype(np.int64) * lr[:, 3]))
+    b_u = 8 * int(np.sum(lr[:, 4].astype(np.int64) * lr[:, 2]))
+    b_d = 8 * int(np.sum(dn[:, 2].astype(np.int64) * dn[:, 3]))
+    prod_bytes = hm.product_bytes(1)
+    # dominant kernel and its algorithmic bytes per launch
+    k1, k2 = phase_ms[1], phase_ms[2]
+    if k2 >= k1:
+        dom, dom_ms, dom_bytes = "phase2_kernel (U-side + dense + scatter)", k2, b_u + b_d + 12 * n
+    else:
+        dom, dom_ms, dom_bytes = "phase1_kernel (V-side)", k1, b_v
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)",
+        "config": dict(WORKLOAD, n=n, precision="fp64", parallelism="replicas" if world > 1 else "single", l2="inputs larger than L2: %.2f GB of factors per product" % (prod_bytes / 1e9)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "kernel": dom, "peak_source": peak_kind},
+        "whole_product": {"bytes": prod_bytes, "GB_per_s": prod_bytes / (ms_step / 1e3) / 1e9, "frac_of_hbm_peak": prod_bytes / (ms_step / 1e3) / 1e9 / peak, "phase_ms": {"gather": phase_ms[0], "phase1": phase_ms[1], "phase2": phase_ms[2], "total": phase_ms[3]}},
+        "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk,
+        "rel_err_vs_dense_1000_rows": err, "aca_seconds": aca_seconds,
+        "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},
+    }
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(n)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_aca_seconds"] = cb["build_seconds"]
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

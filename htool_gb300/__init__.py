@@ -1,0 +1,285 @@
+"""htool_gb300: htool's H-matrix hot path on GB300 (sm_103a).
+
+Python front-end over the C ABI of libhtgpu (include/htgpu.h).  The class and
+method names follow htool's C++ API so code written against htool reads the
+same:
+
+    t = Cluster(); t.set_minclustersize(10); t.build(N, x)          # cluster.hpp:57
+    H = HMatrix(t, t, epsilon=1e-6, eta=10.0)                        # hmatrix.hpp:115
+    H.build(LAPLACE, x, x)                                           # hmatrix.hpp:286
+    y = H.mvprod_global_to_global(v, mu=1)                           # hmatrix.hpp:1074
+
+Everything runs on the GPU through libhtgpu.so; there is no CPU path.  The
+library is built in-tree by htool_gb300/build.py (or __graft_entry__.build());
+importing this package without it raises ImportError.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libhtgpu.so")
+
+INV_R_EPS = 0  # 1 / (1e-5 + r)
+LAPLACE = 1  # 1 / (4 pi r), 0 on the diagonal
+KERNELS = {"inv_r_eps": INV_R_EPS, "laplace": LAPLACE}
+
+HOST_PTRS = 1
+CLUSTER_NUMBERING = 2
+
+_ERRORS = {1: ValueError, 2: NotImplementedError, 3: RuntimeError, 4: MemoryError, 5: RuntimeError}
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libhtgpu.so is not built (run htool_gb300/build.py): " + LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp, i, d, u = C.c_void_p, C.c_int, C.c_double, C.c_uint
+    sig = {
+        "htgpu_last_error": (C.c_char_p, []),
+        "htgpu_version": (i, [vp, vp]),
+        "htgpu_cluster_build": (i, [i, vp, i, i, vp]),
+        "htgpu_cluster_destroy": (i, [vp]),
+        "htgpu_cluster_info": (i, [vp, vp, vp, vp, vp]),
+        "htgpu_cluster_get_perm": (i, [vp, vp]),
+        "htgpu_cluster_get_nodes": (i, [vp, vp, vp]),
+        "htgpu_block_tasks": (i, [vp, vp, d, vp, vp]),
+        "htgpu_hmatrix_create": (i, [vp, vp, d, d, i, vp]),
+        "htgpu_hmatrix_destroy": (i, [vp]),
+        "htgpu_hmatrix_set_maxblocksize": (i, [vp, u]),
+        "htgpu_hmatrix_set_mintargetdepth": (i, [vp, u]),
+        "htgpu_hmatrix_set_minsourcedepth": (i, [vp, u]),
+        "htgpu_hmatrix_build": (i, [vp, i, d, vp, vp]),
+        "htgpu_hmatrix_set_leaves": (i, [vp, i, vp, vp, i, vp, vp]),
+        "htgpu_hmatrix_mvprod": (i, [vp, vp, vp, i, u, vp]),
+        "htgpu_hmatrix_sizes": (i, [vp, vp, vp, vp, vp]),
+        "htgpu_hmatrix_get_leaves": (i, [vp, vp, vp]),
+        "htgpu_hmatrix_get_factors": (i, [vp, vp, vp]),
+        "htgpu_hmatrix_infos": (i, [vp, vp, vp]),
+        "htgpu_hmatrix_product_bytes": (i, [vp, i, vp]),
+        "htgpu_hmatrix_last_launches": (i, [vp, vp]),
+        "htgpu_hmatrix_profile": (i, [vp, i, i, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+lib = _load()
+
+
+def _check(status):
+    if status != 0:
+        msg = lib.htgpu_last_error().decode()
+        raise _ERRORS.get(status, RuntimeError)(msg)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def exported_symbols():
+    """The entry points declared in include/htgpu.h, as exported by the library."""
+    import re
+
+    hdr = os.path.join(os.path.dirname(_HERE), "include", "htgpu.h")
+    names = re.findall(r"\b(htgpu_[a-z_0-9]+)\s*\(", open(hdr).read())
+    return sorted(set(names))
+
+
+class Cluster:
+    """Cluster<PCA<SplittingTypes::GeometricSplitting>> (cluster.hpp:14-584), one rank."""
+
+    def __init__(self, space_dim=3):
+        if space_dim != 3:
+            raise NotImplementedError("[Htool error] only three-dimensional points are supported")
+        self.minclustersize = 10
+        self.h = None
+
+    def set_minclustersize(self, m):
+        if m == 0:
+            raise ValueError("[Htool error] MinClusterSize parameter cannot be zero")
+        self.minclustersize = int(m)
+
+    def build(self, nb_pt, x, nb_sons=-1):
+        self.points = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        if self.points.shape[0] != nb_pt:
+            raise ValueError("[Htool error] point array does not hold nb_pt points")
+        h = C.c_void_p()
+        _check(lib.htgpu_cluster_build(nb_pt, _ptr(self.points), self.minclustersize, nb_sons, C.byref(h)))
+        self._free()
+        self.h = h
+        return self
+
+    def _info(self):
+        n, nn, mn, mx = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib.htgpu_cluster_info(self.h, C.byref(n), C.byref(nn), C.byref(mn), C.byref(mx)))
+        return n.value, nn.value, mn.value, mx.value
+
+    def get_size(self):
+        return self._info()[0]
+
+    def get_min_depth(self):
+        return self._info()[2]
+
+    def get_max_depth(self):
+        return self._info()[3]
+
+    def get_perm(self):
+        p = np.empty(self.get_size(), np.int32)
+        _check(lib.htgpu_cluster_get_perm(self.h, _ptr(p)))
+        return p
+
+    def get_nodes(self):
+        """Pre-order nodes: (int[nn,6] depth, rank, offset, size, nb_sons, counter;
+        float64[nn,4] rad, ctr)."""
+        nn = self._info()[1]
+        ni = np.empty((nn, 6), np.int32)
+        nd = np.empty((nn, 4), np.float64)
+        _check(lib.htgpu_cluster_get_nodes(self.h, _ptr(ni), _ptr(nd)))
+        return ni, nd
+
+    def _free(self):
+        if self.h:
+            lib.htgpu_cluster_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self._free()
+        except Exception:
+            pass
+
+
+def block_tasks(t, s, eta):
+    """Block::build('N') local tasks (blocks.hpp:237-278): int[n,5] =
+    t.offset, t.size, s.offset, s.size, admissible."""
+    n = C.c_int()
+    _check(lib.htgpu_block_tasks(t.h, s.h, eta, C.byref(n), None))
+    out = np.empty((n.value, 5), np.int32)
+    _check(lib.htgpu_block_tasks(t.h, s.h, eta, C.byref(n), _ptr(out)))
+    return out
+
+
+class HMatrix:
+    """HMatrix<double> (hmatrix.hpp:44-270) with partialACA compression,
+    stored and applied on the GPU."""
+
+    def __init__(self, cluster_tree_t, cluster_tree_s, epsilon=1e-6, eta=10.0, symmetry="N", UPLO="N", device=0):
+        if symmetry != "N" or UPLO != "N":
+            raise NotImplementedError("[Htool error] only non-symmetric storage ('N', 'N') is supported")
+        self.t, self.s = cluster_tree_t, cluster_tree_s
+        h = C.c_void_p()
+        _check(lib.htgpu_hmatrix_create(cluster_tree_t.h, cluster_tree_s.h, float(epsilon), float(eta), int(device), C.byref(h)))
+        self.h = h
+        self.epsilon, self.eta = epsilon, eta
+
+    def set_maxblocksize(self, v):
+        _check(lib.htgpu_hmatrix_set_maxblocksize(self.h, int(v)))
+
+    def set_mintargetdepth(self, v):
+        _check(lib.htgpu_hmatrix_set_mintargetdepth(self.h, int(v)))
+
+    def set_minsourcedepth(self, v):
+        _check(lib.htgpu_hmatrix_set_minsourcedepth(self.h, int(v)))
+
+    def build(self, kernel, xt, xs=None, kernel_param=0.0):
+        """HMatrix::build(generator, xt, xs) with a device generator
+        (LAPLACE or INV_R_EPS, or their names)."""
+        kid = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+        xt = np.ascontiguousarray(xt, dtype=np.float64)
+        xs = xt if xs is None else np.ascontiguousarray(xs, dtype=np.float64)
+        _check(lib.htgpu_hmatrix_build(self.h, kid, float(kernel_param), _ptr(xt), _ptr(xs)))
+        return self
+
+    def set_leaves(self, lr_desc, uv, dense_desc, dense):
+        lr_desc = np.ascontiguousarray(lr_desc, dtype=np.int32)
+        dense_desc = np.ascontiguousarray(dense_desc, dtype=np.int32)
+        uv = np.ascontiguousarray(uv, dtype=np.float64)
+        dense = np.ascontiguousarray(dense, dtype=np.float64)
+        _check(lib.htgpu_hmatrix_set_leaves(self.h, lr_desc.shape[0], _ptr(lr_desc), _ptr(uv), dense_desc.shape[0], _ptr(dense_desc), _ptr(dense)))
+        return self
+
+    def sizes(self):
+        nr, nc, nl, nd = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib.htgpu_hmatrix_sizes(self.h, C.byref(nr), C.byref(nc), C.byref(nl), C.byref(nd)))
+        return nr.value, nc.value, nl.value, nd.value
+
+    def nb_rows(self):
+        return self.sizes()[0]
+
+    def nb_cols(self):
+        return self.sizes()[1]
+
+    def get_nlrmat(self):
+        return self.sizes()[2]
+
+    def get_ndmat(self):
+        return self.sizes()[3]
+
+    def get_leaves(self):
+        _, _, nl, nd = self.sizes()
+        lr = np.empty((nl, 5), np.int32)
+        dn = np.empty((nd, 4), np.int32)
+        _check(lib.htgpu_hmatrix_get_leaves(self.h, _ptr(lr), _ptr(dn)))
+        return lr, dn
+
+    def get_factors(self):
+        lr, dn = self.get_leaves()
+        nuv = int(np.sum(lr[:, 4].astype(np.int64) * (lr[:, 2] + lr[:, 3])))
+        nd = int(np.sum(dn[:, 2].astype(np.int64) * dn[:, 3]))
+        uv = np.empty(max(nuv, 1))
+        dd = np.empty(max(nd, 1))
+        _check(lib.htgpu_hmatrix_get_factors(self.h, _ptr(uv), _ptr(dd)))
+        return lr, dn, uv[:nuv], dd[:nd]
+
+    def get_infos(self):
+        n = C.c_int(0)
+        _check(lib.htgpu_hmatrix_infos(self.h, None, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        _check(lib.htgpu_hmatrix_infos(self.h, buf, C.byref(n)))
+        return dict(l.split("=", 1) for l in buf.value.decode().splitlines() if "=" in l)
+
+    def product_bytes(self, mu=1):
+        b = C.c_longlong()
+        _check(lib.htgpu_hmatrix_product_bytes(self.h, mu, C.byref(b)))
+        return b.value
+
+    def last_launches(self):
+        n = C.c_int()
+        _check(lib.htgpu_hmatrix_last_launches(self.h, C.byref(n)))
+        return n.value
+
+    def profile(self, mu=1, reps=10):
+        """Average ms per product: (gather, phase 1, phase 2, total)."""
+        ms = np.zeros(4, np.float32)
+        _check(lib.htgpu_hmatrix_profile(self.h, mu, reps, _ptr(ms)))
+        return tuple(float(v) for v in ms)
+
+    def mvprod_global_to_global(self, x, mu=1):
+        """Host arrays in and out (column-major, mu right-hand sides)."""
+        nr, nc, _, _ = self.sizes()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.size != nc * mu:
+            raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nc * mu))
+        y = np.empty(nr * mu, np.float64)
+        _check(lib.htgpu_hmatrix_mvprod(self.h, _ptr(x), _ptr(y), mu, HOST_PTRS, None))
+        return y
+
+    def mvprod_ptr(self, x_ptr, y_ptr, mu=1, flags=0, stream=None):
+        """Device (or, with HOST_PTRS, host) pointers; stream-ordered."""
+        _check(lib.htgpu_hmatrix_mvprod(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), mu, flags, C.c_void_p(stream) if stream else None))
+
+    def __matmul__(self, x):
+        return self.mvprod_global_to_global(x, 1)
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib.htgpu_hmatrix_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

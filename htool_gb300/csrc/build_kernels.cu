@@ -1,0 +1,350 @@
+// Assembly kernels: device kernel generators, batched partialACA, dense-leaf
+// fill and factor packing.
+//
+// This translation unit is compiled with -fmad=false: every multiply-add
+// below that htool computes as a separate product and sum stays separate,
+// and the ones htool computes with BLAS axpy are written as explicit fma().
+// With IEEE division and square root this makes every generator entry and
+// every ACA row/column residual bit-identical to htool's CPU arithmetic
+// (partialACA.hpp:83-113); only the Frobenius estimator's dot products are
+// summed in a different (tree) order.
+#include "kernels.hpp"
+
+#include <cstdio>
+
+namespace htgpu {
+
+namespace {
+
+constexpr double kFourPi = 4.0 * 3.14159265358979323846;
+
+// distance with htool's summation order: ((0 + d0^2) + d1^2) + d2^2
+__device__ __forceinline__ double dist3(const double *a, const double *b) {
+    double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+    double s  = 0.;
+    s         = s + d0 * d0;
+    s         = s + d1 * d1;
+    s         = s + d2 * d2;
+    return sqrt(s);
+}
+
+// real kernels (ids 0 and 1)
+__device__ __forceinline__ double kernel_entry(const KernelDesc &kd, const double *a, const double *b) {
+    double r = dist3(a, b);
+    if (kd.id == 0)
+        return 1. / (1e-5 + r);
+    if (r == 0.)
+        return 0.;
+    return 1. / (kFourPi * r);
+}
+
+// (ov, oi) beats (v, idx) for the pivot search: an empty candidate (index
+// < 0) never wins and always loses; a NaN magnitude loses to any number
+__device__ __forceinline__ bool better_max(double ov, int oi, double v, int idx) {
+    if (oi < 0)
+        return false;
+    if (idx < 0)
+        return true;
+    if (ov != ov)
+        return v != v && oi > idx;
+    if (v != v)
+        return true;
+    return ov > v || (ov == v && oi > idx);
+}
+
+template <int NT>
+struct BlockReduce {
+    // argmax over (value, index): larger value wins, ties go to the larger
+    // index -- the "last maximum" of htool's sequential pivot loops
+    __device__ static void argmax(double &v, int &idx, double *sv, int *si) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double ov = __shfl_down_sync(0xffffffffu, v, o);
+            int oi    = __shfl_down_sync(0xffffffffu, idx, o);
+            if (better_max(ov, oi, v, idx)) {
+                v   = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            sv[warp] = v;
+            si[warp] = idx;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < NT / 32; w++)
+                if (better_max(sv[w], si[w], sv[0], si[0])) {
+                    sv[0] = sv[w];
+                    si[0] = si[w];
+                }
+        }
+        __syncthreads();
+        v   = sv[0];
+        idx = si[0];
+        __syncthreads();
+    }
+    // argmin, ties to the smaller index (htool's first-row choice)
+    __device__ static void argmin(double &v, int &idx, double *sv, int *si) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double ov = __shfl_down_sync(0xffffffffu, v, o);
+            int oi    = __shfl_down_sync(0xffffffffu, idx, o);
+            if (ov < v || (ov == v && oi < idx)) {
+                v   = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            sv[warp] = v;
+            si[warp] = idx;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < NT / 32; w++)
+                if (sv[w] < sv[0] || (sv[w] == sv[0] && si[w] < si[0])) {
+                    sv[0] = sv[w];
+                    si[0] = si[w];
+                }
+        }
+        __syncthreads();
+        v   = sv[0];
+        idx = si[0];
+        __syncthreads();
+    }
+};
+
+constexpr int kAcaThreads = 128;
+constexpr int kDotChunk   = 32; // estimator dot products reduced per pass
+
+// One CTA per block.  Scratch columns: U_s[:, k] (length M) and Vt_s[:, k]
+// (length N) hold the k-th cross c_k and r_k of partialACA.
+__global__ void __launch_bounds__(kAcaThreads) partial_aca_kernel(const AcaBlock *__restrict__ blocks, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t,
+                                                                   const int *__restrict__ perm_s, KernelDesc kd, double eps, double *__restrict__ scratch, unsigned char *__restrict__ flags,
+                                                                   int *__restrict__ rank_out) {
+    constexpr int NT = kAcaThreads;
+    __shared__ double sv[NT / 32];
+    __shared__ int si[NT / 32];
+    __shared__ double sdot[NT / 32][kDotChunk];
+    __shared__ double sres[kDotChunk];
+    __shared__ double sacc[3]; // |c.c||r.r|, sum_p (vv_p.r)(uu_p.c), pending (vv_p.r)
+
+    const AcaBlock B = blocks[blockIdx.x];
+    const int M = B.M, N = B.N, tid = threadIdx.x;
+    const int *rows = perm_t + B.row_off;
+    const int *cols = perm_s + B.col_off;
+    double *U       = scratch + B.u_off;
+    double *Vt      = scratch + B.v_off;
+    unsigned char *vrow = flags + B.flag_off;
+    unsigned char *vcol = vrow + M;
+
+    for (int i = tid; i < M + N; i += NT)
+        vrow[i] = 0;
+
+    // first pivot row: the point closest to the target centre (first minimum)
+    double best = 1e300;
+    int I       = 0x7fffffff;
+    for (int i = tid; i < M; i += NT) {
+        const double *p = xt + 3 * (size_t)rows[i];
+        double s        = 0.;
+        for (int d = 0; d < 3; d++)
+            s = s + (p[d] - B.ctr[d]) * (p[d] - B.ctr[d]);
+        double ad = sqrt(s);
+        if (ad < best) {
+            best = ad;
+            I    = i;
+        }
+    }
+    BlockReduce<NT>::argmin(best, I, sv, si);
+    if (!(best < 1e30))
+        I = 0; // htool starts from dist = 1e30 and row 0
+
+    // q * (M + N) > M * N evaluated with 32-bit int products, as upstream
+    const int MN32 = (int)((unsigned)M * (unsigned)N);
+    int q          = 0;
+    double frob = 0., aux = 0.;
+    while (true) {
+        if (!(q == 0 || sqrt(aux / frob) > eps))
+            break;
+        q += 1;
+        if ((int)((unsigned)q * (unsigned)(M + N)) > MN32) {
+            q = -1;
+            break;
+        }
+        if (q > B.cap) {
+            q = -2;
+            break;
+        }
+        const int k = q - 1;
+        // ---- row I of the residual -> Vt_s[:, k]
+        const double *pI = xt + 3 * (size_t)rows[I];
+        double piv       = -1.;
+        int J            = -1;
+        for (int j = tid; j < N; j += NT) {
+            double v = kernel_entry(kd, pI, xs + 3 * (size_t)cols[j]);
+            for (int p = 0; p < k; p++)
+                v = fma(-U[I + (size_t)M * p], Vt[j + (size_t)N * p], v);
+            Vt[j + (size_t)N * k] = v;
+            if (!vcol[j]) {
+                double a = fabs(v);
+                if (!(a < piv)) {
+                    piv = a;
+                    J   = j;
+                }
+            }
+        }
+        BlockReduce<NT>::argmax(piv, J, sv, si);
+        if (J < 0) { // no admissible pivot column (only with non-finite entries)
+            q = q - 1 == 0 ? -1 : q - 1;
+            break;
+        }
+        if (tid == 0)
+            vrow[I] = 1;
+        __syncthreads();
+        const double rJ = Vt[J + (size_t)N * k];
+        if (fabs(rJ) > 1e-15) {
+            const double gamma = 1. / rJ;
+            // ---- column J of the residual, scaled -> U_s[:, k]
+            const double *pJ = xs + 3 * (size_t)cols[J];
+            double piv2      = -1.;
+            int I2           = -1;
+            for (int i = tid; i < M; i += NT) {
+                double v = kernel_entry(kd, xt + 3 * (size_t)rows[i], pJ);
+                for (int p = 0; p < k; p++)
+                    v = fma(-Vt[J + (size_t)N * p], U[i + (size_t)M * p], v);
+                v                    = v * gamma;
+                U[i + (size_t)M * k] = v;
+                if (!vrow[i]) {
+                    double a = fabs(v);
+                    if (!(a < piv2)) {
+                        piv2 = a;
+                        I2   = i;
+                    }
+                }
+            }
+            BlockReduce<NT>::argmax(piv2, I2, sv, si);
+            if (I2 < 0) { // no pivot row left (only with non-finite entries)
+                break;
+            }
+            if (tid == 0)
+                vcol[J] = 1;
+            // ---- Frobenius estimator (partialACA.hpp:127-141), in chunks of
+            // 32 dot products: c.c, r.r, then (vv_p . r), (uu_p . c) for p < k
+            const int nd = 2 + 2 * k;
+            const int lane = tid & 31, warp = tid >> 5;
+            if (tid == 0)
+                sacc[1] = 0.;
+            for (int d0 = 0; d0 < nd; d0 += kDotChunk) {
+                const int dn = min(kDotChunk, nd - d0);
+                for (int dd = 0; dd < dn; dd++) {
+                    const int d = d0 + dd;
+                    double s    = 0.;
+                    if (d == 0) {
+                        for (int i = tid; i < M; i += NT) {
+                            double c = U[i + (size_t)M * k];
+                            s        = s + c * c;
+                        }
+                    } else if (d == 1) {
+                        for (int j = tid; j < N; j += NT) {
+                            double r = Vt[j + (size_t)N * k];
+                            s        = s + r * r;
+                        }
+                    } else if (d & 1) { // (vv_p . r), p = (d - 3) / 2
+                        int p = (d - 2) >> 1;
+                        for (int j = tid; j < N; j += NT)
+                            s = s + Vt[j + (size_t)N * p] * Vt[j + (size_t)N * k];
+                    } else { // (uu_p . c), p = (d - 2) / 2
+                        int p = (d - 2) >> 1;
+                        for (int i = tid; i < M; i += NT)
+                            s = s + U[i + (size_t)M * p] * U[i + (size_t)M * k];
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+                        s = s + __shfl_down_sync(0xffffffffu, s, o);
+                    if (lane == 0)
+                        sdot[warp][dd] = s;
+                }
+                __syncthreads();
+                if (tid < dn) {
+                    double s = 0.;
+                    for (int w = 0; w < NT / 32; w++)
+                        s = s + sdot[w][tid];
+                    sres[tid] = s;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    for (int dd = 0; dd < dn; dd++) {
+                        const int d = d0 + dd;
+                        if (d == 0)
+                            sacc[0] = fabs(sres[dd]);
+                        else if (d == 1)
+                            sacc[0] = sacc[0] * fabs(sres[dd]);
+                        else if (d & 1) // (vv_p . r) times the pending (uu_p . c)
+                            sacc[1] = sacc[1] + sres[dd] * sacc[2];
+                        else
+                            sacc[2] = sres[dd];
+                    }
+                }
+                __syncthreads();
+            }
+            aux       = sacc[0];
+            double fa = sacc[1];
+            frob = frob + (aux + 2 * fa);
+            I    = I2;
+            __syncthreads();
+        } else {
+            q -= 1;
+            if (q == 0)
+                q = -1;
+            break;
+        }
+    }
+    if (tid == 0)
+        rank_out[blockIdx.x] = q;
+}
+
+__global__ void pack_factors_kernel(const PackItem *__restrict__ items, const double *__restrict__ scratch, double *__restrict__ arena) {
+    const PackItem it = items[blockIdx.x];
+    const long long nu = (long long)it.M * it.r, nv = (long long)it.N * it.r;
+    for (long long e = threadIdx.x; e < nu; e += blockDim.x)
+        arena[it.dst_u + e] = scratch[it.src_u + e];
+    for (long long e = threadIdx.x; e < nv; e += blockDim.x)
+        arena[it.dst_v + e] = scratch[it.src_v + e];
+}
+
+__global__ void dense_fill_kernel(const DenseLeaf *__restrict__ leaves, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t, const int *__restrict__ perm_s,
+                                  KernelDesc kd, double *__restrict__ arena) {
+    const DenseLeaf L = leaves[blockIdx.x];
+    const int mn      = L.m * L.n;
+    for (int e = threadIdx.x; e < mn; e += blockDim.x) {
+        int i = e % L.m, j = e / L.m;
+        arena[L.d_off + e] = kernel_entry(kd, xt + 3 * (size_t)perm_t[L.oi + i], xs + 3 * (size_t)perm_s[L.oj + j]);
+    }
+}
+
+} // namespace
+
+void launch_partial_aca(const AcaBlock *blocks, int nblocks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double eps, double *scratch, unsigned char *flags,
+                        int *rank_out, cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    partial_aca_kernel<<<nblocks, kAcaThreads, 0, st>>>(blocks, xt, xs, perm_t, perm_s, kd, eps, scratch, flags, rank_out);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_pack_factors(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st) {
+    if (nitems <= 0)
+        return;
+    pack_factors_kernel<<<nitems, 128, 0, st>>>(items, scratch, arena);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_dense_fill(const DenseLeaf *leaves, int nleaves, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st) {
+    if (nleaves <= 0)
+        return;
+    dense_fill_kernel<<<nleaves, 128, 0, st>>>(leaves, xt, xs, perm_t, perm_s, kd, arena);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+} // namespace htgpu

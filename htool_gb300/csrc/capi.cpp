@@ -1,0 +1,279 @@
+// extern "C" entry points of libhtgpu (declared in include/htgpu.h).
+// Every call catches C++ exceptions and turns them into a status code plus
+// a thread-local message.
+#include "../../include/htgpu.h"
+#include "hmatrix.hpp"
+
+#include <cstring>
+#include <new>
+
+struct htgpu_cluster_s {
+    std::shared_ptr<htgpu::ClusterTree> tree;
+};
+
+struct htgpu_hmatrix_s {
+    std::unique_ptr<htgpu::HMatrix> h;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F f) {
+    try {
+        f();
+        return HTGPU_OK;
+    } catch (const htgpu::Error &e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_last_error = "[Htool error] host allocation failed";
+        return HTGPU_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        g_last_error = std::string("[Htool error] ") + e.what();
+        return HTGPU_ERR_INTERNAL;
+    }
+}
+
+void need(const void *p, const char *what) { htgpu::require(p != nullptr, std::string(what) + " is null"); }
+} // namespace
+
+extern "C" {
+
+const char *htgpu_last_error(void) { return g_last_error.c_str(); }
+
+int htgpu_version(int *major, int *minor) {
+    return guarded([&] {
+        need(major, "major");
+        need(minor, "minor");
+        *major = 0;
+        *minor = 1;
+    });
+}
+
+int htgpu_cluster_build(int n, const double *xyz, int minclustersize, int nb_sons, htgpu_cluster *out) {
+    return guarded([&] {
+        need(xyz, "xyz");
+        need(out, "out");
+        htgpu::require(n >= 2, "a cluster tree needs at least two points");
+        auto *c = new htgpu_cluster_s;
+        c->tree = std::make_shared<htgpu::ClusterTree>(htgpu::build_cluster_tree(n, xyz, minclustersize, nb_sons));
+        *out    = c;
+    });
+}
+
+int htgpu_cluster_destroy(htgpu_cluster c) {
+    return guarded([&] { delete c; });
+}
+
+int htgpu_cluster_info(htgpu_cluster c, int *n, int *nnodes, int *min_depth, int *max_depth) {
+    return guarded([&] {
+        need(c, "cluster");
+        if (n)
+            *n = c->tree->n;
+        if (nnodes)
+            *nnodes = (int)c->tree->nodes.size();
+        if (min_depth)
+            *min_depth = c->tree->min_depth;
+        if (max_depth)
+            *max_depth = c->tree->max_depth;
+    });
+}
+
+int htgpu_cluster_get_perm(htgpu_cluster c, int *perm) {
+    return guarded([&] {
+        need(c, "cluster");
+        need(perm, "perm");
+        std::memcpy(perm, c->tree->perm.data(), sizeof(int) * c->tree->perm.size());
+    });
+}
+
+int htgpu_cluster_get_nodes(htgpu_cluster c, int *node_i, double *node_d) {
+    return guarded([&] {
+        need(c, "cluster");
+        need(node_i, "node_i");
+        need(node_d, "node_d");
+        int k = 0;
+        for (int v : c->tree->preorder()) {
+            const auto &nd    = c->tree->nodes[v];
+            node_i[6 * k + 0] = nd.depth;
+            node_i[6 * k + 1] = nd.rank;
+            node_i[6 * k + 2] = nd.offset;
+            node_i[6 * k + 3] = nd.size;
+            node_i[6 * k + 4] = nd.nb_sons;
+            node_i[6 * k + 5] = nd.counter;
+            node_d[4 * k + 0] = nd.rad;
+            for (int d = 0; d < 3; d++)
+                node_d[4 * k + 1 + d] = nd.ctr[d];
+            k++;
+        }
+    });
+}
+
+int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks, int *out) {
+    return guarded([&] {
+        need(t, "target cluster");
+        need(s, "source cluster");
+        need(ntasks, "ntasks");
+        htgpu::BlockTreeParams p;
+        p.eta      = eta;
+        auto tasks = htgpu::build_local_tasks(*t->tree, *s->tree, p);
+        *ntasks    = (int)tasks.size();
+        if (out)
+            for (std::size_t b = 0; b < tasks.size(); b++) {
+                const auto &tn = t->tree->nodes[tasks[b].t];
+                const auto &sn = s->tree->nodes[tasks[b].s];
+                out[5 * b + 0] = tn.offset;
+                out[5 * b + 1] = tn.size;
+                out[5 * b + 2] = sn.offset;
+                out[5 * b + 3] = sn.size;
+                out[5 * b + 4] = tasks[b].adm ? 1 : 0;
+            }
+    });
+}
+
+int htgpu_hmatrix_create(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out) {
+    return guarded([&] {
+        need(t, "target cluster");
+        need(s, "source cluster");
+        need(out, "out");
+        auto *h = new htgpu_hmatrix_s;
+        try {
+            h->h.reset(new htgpu::HMatrix(t->tree, s->tree, epsilon, eta, device));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int htgpu_hmatrix_destroy(htgpu_hmatrix h) {
+    return guarded([&] { delete h; });
+}
+
+int htgpu_hmatrix_set_maxblocksize(htgpu_hmatrix h, unsigned int v) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        htgpu::require(v > 0, "MaxBlockSize parameter cannot be zero");
+        h->h->bp.maxblocksize = v;
+    });
+}
+int htgpu_hmatrix_set_mintargetdepth(htgpu_hmatrix h, unsigned int v) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->bp.mintargetdepth = (int)v;
+    });
+}
+int htgpu_hmatrix_set_minsourcedepth(htgpu_hmatrix h, unsigned int v) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->bp.minsourcedepth = (int)v;
+    });
+}
+
+int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt, const double *xs) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(xt, "xt");
+        need(xs, "xs");
+        htgpu::KernelDesc kd;
+        kd.id    = kernel_id;
+        kd.param = kernel_param;
+        h->h->build(kd, xt, xs);
+    });
+}
+
+int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const double *uv, int ndense, const int *d_desc, const double *dense) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        htgpu::require(nlr >= 0 && ndense >= 0, "negative leaf count");
+        if (nlr) {
+            need(lr_desc, "lr_desc");
+            need(uv, "uv");
+        }
+        if (ndense) {
+            need(d_desc, "d_desc");
+            need(dense, "dense");
+        }
+        h->h->set_leaves(nlr, lr_desc, uv, ndense, d_desc, dense);
+    });
+}
+
+int htgpu_hmatrix_mvprod(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->mvprod(in, out, mu, (flags & HTGPU_HOST_PTRS) != 0, (flags & HTGPU_CLUSTER_NUMBERING) != 0, (cudaStream_t)stream);
+    });
+}
+
+int htgpu_hmatrix_sizes(htgpu_hmatrix h, int *nr, int *nc, int *nlr, int *ndense) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        if (nr)
+            *nr = h->h->nb_rows();
+        if (nc)
+            *nc = h->h->nb_cols();
+        if (nlr)
+            *nlr = h->h->n_lowrank();
+        if (ndense)
+            *ndense = h->h->n_dense();
+    });
+}
+
+int htgpu_hmatrix_get_leaves(htgpu_hmatrix h, int *lr_desc, int *d_desc) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(lr_desc, "lr_desc");
+        need(d_desc, "d_desc");
+        h->h->leaf_descriptors(lr_desc, d_desc);
+    });
+}
+
+int htgpu_hmatrix_get_factors(htgpu_hmatrix h, double *uv, double *dense) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->export_factors(uv, dense);
+    });
+}
+
+int htgpu_hmatrix_infos(htgpu_hmatrix h, char *buf, int *len) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(len, "len");
+        std::string s;
+        for (auto &kv : h->h->infos())
+            s += kv.first + "=" + kv.second + "\n";
+        const int need_len = (int)s.size() + 1;
+        if (buf && *len >= need_len)
+            std::memcpy(buf, s.c_str(), need_len);
+        *len = need_len;
+    });
+}
+
+int htgpu_hmatrix_product_bytes(htgpu_hmatrix h, int mu, long long *bytes) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(bytes, "bytes");
+        *bytes = h->h->product_bytes(mu);
+    });
+}
+
+int htgpu_hmatrix_last_launches(htgpu_hmatrix h, int *launches) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(launches, "launches");
+        *launches = h->h->last_launch_count();
+    });
+}
+
+int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(ms, "ms");
+        htgpu::require(reps > 0 && mu > 0, "reps and mu must be positive");
+        h->h->profile(mu, reps, ms);
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,141 @@
+// Internal declarations shared by the host (C++) and device (CUDA) parts of
+// libhtgpu.  Nothing here crosses the C ABI; include/htgpu.h is the boundary.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace htgpu {
+
+// ---------------------------------------------------------------------------
+// errors: every C entry point catches these and returns a status code
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define HTGPU_CUDA(call)                                                                             \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            throw ::htgpu::Error(3, std::string("[Htool error] CUDA: ") + cudaGetErrorString(e_) + \
+                                        " at " __FILE__ ":" + std::to_string(__LINE__));             \
+    } while (0)
+
+inline void require(bool ok, const std::string &msg, int code = 1) {
+    if (!ok)
+        throw Error(code, "[Htool error] " + msg);
+}
+
+// ---------------------------------------------------------------------------
+// cluster tree (host).  Same algorithm as htool's Cluster<PCA<Geometric>>.
+// ---------------------------------------------------------------------------
+struct ClusterNode {
+    int depth = 0, rank = 0, offset = 0, size = 0, counter = 0;
+    int nb_sons = 0, first_son = -1, parent = -1;
+    double rad = 0, ctr[3] = {0, 0, 0};
+};
+
+struct ClusterTree {
+    int n = 0;
+    int minclustersize = 10;
+    std::vector<int> perm;
+    std::vector<ClusterNode> nodes; // construction order; sons contiguous
+    int min_depth = -1, max_depth = 0;
+    std::vector<int> preorder() const;
+};
+
+ClusterTree build_cluster_tree(int n, const double *xyz, int minclustersize, int nb_sons);
+
+// ---------------------------------------------------------------------------
+// block tree (host).  Same algorithm as htool's Block::build (UPLO 'N').
+// ---------------------------------------------------------------------------
+struct BlockTask {
+    int t, s;
+    bool adm;
+};
+
+struct BlockTreeParams {
+    double eta = 10;
+    int mintargetdepth = 0, minsourcedepth = 0;
+    std::size_t maxblocksize = 1000000;
+};
+
+bool admissible(const ClusterNode &t, const ClusterNode &s, double eta);
+std::vector<BlockTask> build_local_tasks(const ClusterTree &T, const ClusterTree &S, const BlockTreeParams &p);
+
+// ---------------------------------------------------------------------------
+// device-side descriptors (plain structs, identical layout on host/device)
+// ---------------------------------------------------------------------------
+// kernel ids: 0 = 1/(1e-5 + r); 1 = 1/(4 pi r), 0 at r == 0;
+//             2 = exp(i k r)/(4 pi r), 0 at r == 0 (complex)
+struct KernelDesc {
+    int id = 1;
+    double param = 0; // wavenumber for id 2
+};
+
+struct LrLeaf { // low-rank leaf: y[oi:oi+m] += U (Vt^T x[oj:oj+n])
+    int oi, oj, m, n, r;
+    int nch;            // phase-1 column chunks
+    long long u_off;    // U: m x r, column-major, ld = m   (elements)
+    long long v_off;    // Vt: n x r, column-major, ld = n  (elements)
+    long long a_off;    // first slot of the phase-1 sums Vt^T x: slots [nch][r], mu values each
+};
+
+struct DenseLeaf {
+    int oi, oj, m, n;
+    long long d_off; // m x n, column-major
+};
+
+struct P1Item { // one warp: rows j0 .. j0+jlen of Vt for one leaf
+    int leaf, chunk, j0, jlen;
+};
+
+struct P2Item { // one warp: target rows row0 .. row0+h, contributions [cbeg, cend)
+    int row0, h, cbeg, cend;
+};
+
+struct P2Contrib { // leaf >= 0: low-rank leaf; leaf < 0: dense leaf ~leaf
+    int leaf, rowoff;
+};
+
+// ---------------------------------------------------------------------------
+// device memory helper
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    std::size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(std::size_t count) {
+        release();
+        if (count) {
+            HTGPU_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+            n = count;
+        }
+    }
+    void upload(const T *h, std::size_t count, cudaStream_t st) {
+        if (count > n)
+            alloc(count);
+        if (count)
+            HTGPU_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
+    void upload(const std::vector<T> &v, cudaStream_t st) { upload(v.data(), v.size(), st); }
+};
+
+} // namespace htgpu

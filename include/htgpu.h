@@ -1,0 +1,152 @@
+/*
+ * htgpu.h -- C ABI of libhtgpu, the GB300 (sm_103a) implementation of htool's
+ * H-matrix hot path: cluster/block trees, device partialACA assembly and the
+ * H-matrix product over all leaves.
+ *
+ * Every function returns HTGPU_OK (0) or an error code; htgpu_last_error()
+ * gives the message of the calling thread's last failure (messages keep
+ * htool's "[Htool error] ..." prefix).  No C++ exception crosses this
+ * boundary.  Handles are not thread-safe: one thread per handle at a time,
+ * like htool's HMatrix, whose products mutate its `infos` map
+ * (include/htool/types/hmatrix.hpp:87).
+ *
+ * Each declaration names the upstream htool 0.8.1 interface it replaces
+ * (paths relative to the htool source tree).
+ */
+#ifndef HTGPU_H
+#define HTGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HTGPU_OK 0
+#define HTGPU_ERR_INVALID 1     /* invalid argument (std::invalid_argument upstream) */
+#define HTGPU_ERR_UNSUPPORTED 2 /* valid htool input this library does not handle */
+#define HTGPU_ERR_CUDA 3        /* CUDA runtime error */
+#define HTGPU_ERR_NOMEM 4       /* host allocation failure */
+#define HTGPU_ERR_INTERNAL 5    /* inconsistent device result (a bug) */
+
+/* flags of the product entry points */
+#define HTGPU_HOST_PTRS 1u         /* in/out are host memory; the call is synchronous */
+#define HTGPU_CLUSTER_NUMBERING 2u /* in/out are in cluster (permuted) order: no permutation */
+
+/* built-in device generators (the device-generator variant of
+ * VirtualGenerator<T>::copy_submatrix, include/htool/types/virtual_generator.hpp:22) */
+#define HTGPU_KERNEL_INV_R_EPS 0 /* 1 / (1e-5 + |x - y|) */
+#define HTGPU_KERNEL_LAPLACE 1   /* 1 / (4 pi |x - y|), 0 where x == y */
+
+typedef struct htgpu_cluster_s *htgpu_cluster;
+typedef struct htgpu_hmatrix_s *htgpu_hmatrix;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *htgpu_last_error(void);
+
+/* Library version (htool_gb300 major.minor). */
+int htgpu_version(int *major, int *minor);
+
+/* ---------------------------------------------------------------------------
+ * Cluster trees
+ * -------------------------------------------------------------------------*/
+
+/* Replaces Cluster<PCA<SplittingTypes::GeometricSplitting>>::build(nb_pt, x, nb_sons)
+ * (include/htool/clustering/cluster.hpp:94-97, 57-92; pca.hpp:15-128) after
+ * set_minclustersize (cluster.hpp:334), on one MPI rank.  xyz: n points, xyz
+ * interleaved.  nb_sons: 2 or -1 (automatic = 2).  The tree, permutation,
+ * centres and radii are bit-identical to htool's. */
+int htgpu_cluster_build(int n, const double *xyz, int minclustersize, int nb_sons, htgpu_cluster *out);
+int htgpu_cluster_destroy(htgpu_cluster c);
+
+/* Sizes: number of points, number of nodes, get_min_depth/get_max_depth
+ * (cluster.hpp:277-278). */
+int htgpu_cluster_info(htgpu_cluster c, int *n, int *nnodes, int *min_depth, int *max_depth);
+
+/* get_perm (cluster.hpp:279): perm[n]. */
+int htgpu_cluster_get_perm(htgpu_cluster c, int *perm);
+
+/* Every node in pre-order (sons in order): node_i[6 * k ...] = depth, rank,
+ * offset, size, nb_sons, counter; node_d[4 * k ...] = rad, ctr[0..2]
+ * (VirtualCluster getters, include/htool/clustering/virtual_cluster.hpp:28-40). */
+int htgpu_cluster_get_nodes(htgpu_cluster c, int *node_i, double *node_d);
+
+/* Block::build(UPLO = 'N') local task list (include/htool/blocks/blocks.hpp:237-278):
+ * call with out = NULL to get *ntasks, then with room for 5 * ntasks ints:
+ * t.offset, t.size, s.offset, s.size, admissible. */
+int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks, int *out);
+
+/* ---------------------------------------------------------------------------
+ * H-matrices (double precision, non-symmetric storage)
+ * -------------------------------------------------------------------------*/
+
+/* Replaces HMatrix<double>(cluster_tree_t, cluster_tree_s, epsilon, eta, 'N', 'N')
+ * (include/htool/types/hmatrix.hpp:115-122) followed by
+ * set_compression(std::make_shared<partialACA<double>>()) (hmatrix.hpp:220).
+ * The matrix lives on CUDA device `device`. */
+int htgpu_hmatrix_create(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out);
+int htgpu_hmatrix_destroy(htgpu_hmatrix h);
+
+/* set_maxblocksize / set_mintargetdepth / set_minsourcedepth (hmatrix.hpp:213-215). */
+int htgpu_hmatrix_set_maxblocksize(htgpu_hmatrix h, unsigned int maxblocksize);
+int htgpu_hmatrix_set_mintargetdepth(htgpu_hmatrix h, unsigned int depth);
+int htgpu_hmatrix_set_minsourcedepth(htgpu_hmatrix h, unsigned int depth);
+
+/* Replaces HMatrix<double>::build(mat, xt, xs) (hmatrix.hpp:286-341) where
+ * mat is a built-in device generator (HTGPU_KERNEL_*) evaluated on the GPU;
+ * every admissible block is compressed by device partialACA
+ * (include/htool/lrmat/partialACA.hpp:39-171), batched across blocks, with
+ * htool's rejection and recursion rules (hmatrix.hpp:504-607).  xt / xs are
+ * the host point arrays used to build the cluster trees. */
+int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt, const double *xs);
+
+/* Adopt leaves built elsewhere, e.g. exported from an htool HMatrix through
+ * get_MyFarFieldMats / get_MyNearFieldMats (hmatrix.hpp:193-198) and
+ * LowRankMatrix::get_U / get_V (include/htool/lrmat/lrmat.hpp:65-66).
+ * lr_desc[5 * b ...] = offset_i, offset_j, m, n, rank (cluster numbering);
+ * uv = for each low-rank leaf in order, U (m x rank, column-major) then
+ * V (rank x n, column-major); d_desc[4 * b ...] = offset_i, offset_j, m, n;
+ * dense = each dense leaf m x n column-major.  Host memory; copied. */
+int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const double *uv, int ndense, const int *d_desc, const double *dense);
+
+/* Replaces HMatrix<double>::mvprod_global_to_global(in, out, mu)
+ * (hmatrix.hpp:1074-1182): out = H in for mu right-hand sides stored
+ * column-major (in: nb_cols x mu, out: nb_rows x mu), in user numbering
+ * unless HTGPU_CLUSTER_NUMBERING.  With HTGPU_HOST_PTRS the pointers are host
+ * memory and the call returns when out is written; otherwise they are device
+ * pointers and the call is ordered on `stream` (a cudaStream_t; NULL = the
+ * handle's own stream) and returns at once. */
+int htgpu_hmatrix_mvprod(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream);
+
+/* nb_rows / nb_cols, get_nlrmat / get_ndmat (hmatrix.hpp:173-187). */
+int htgpu_hmatrix_sizes(htgpu_hmatrix h, int *nr, int *nc, int *nlr, int *ndense);
+
+/* Leaf descriptors (same layout as htgpu_hmatrix_set_leaves), sorted by
+ * (offset_i, offset_j) like HMatrix's MyComputedBlocks (hmatrix.hpp:494-500). */
+int htgpu_hmatrix_get_leaves(htgpu_hmatrix h, int *lr_desc, int *d_desc);
+
+/* Factors and dense blocks in htool's layouts (see htgpu_hmatrix_set_leaves). */
+int htgpu_hmatrix_get_factors(htgpu_hmatrix h, double *uv, double *dense);
+
+/* get_infos (hmatrix.hpp:223, keys of ComputeInfos, :739-841) plus the GPU
+ * assembly counters, as "key=value\n" lines.  Returns the needed size in
+ * *len when buf is NULL or too small. */
+int htgpu_hmatrix_infos(htgpu_hmatrix h, char *buf, int *len);
+
+/* Bytes of one FP64 product: stored factors and dense blocks, plus the
+ * input/output vectors and the two permutations for mu right-hand sides. */
+int htgpu_hmatrix_product_bytes(htgpu_hmatrix h, int mu, long long *bytes);
+
+/* Number of this library's kernels the last product launched. */
+int htgpu_hmatrix_last_launches(htgpu_hmatrix h, int *launches);
+
+/* Timing breakdown of `reps` products with mu right-hand sides on the
+ * handle's stream (device-resident input), measured with CUDA events between
+ * the launches: ms[0] gather, ms[1] low-rank V-side (phase 1), ms[2]
+ * U-side + dense + scatter (phase 2), ms[3] whole product; averages per
+ * product.  The counterpart of the timing htool accumulates in its infos map
+ * (nb_mat_vec_prod / total_time_mat_vec_prod, hmatrix.hpp:1180-1181). */
+int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

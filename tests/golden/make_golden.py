@@ -1,0 +1,109 @@
+"""Generate the golden fixtures in this directory from upstream htool.
+
+Runs the upstream htool headers compiled by oracle/refbuild (the reference
+implementation itself, not a restatement) on seeded inputs and stores what
+they produce:
+
+* cluster trees (permutation, per-node depth/rank/offset/size/sons/counter,
+  radius and centre bits) -- Cluster<PCAGeometricClustering>::build;
+* the sorted local block-tree task list -- Block::build;
+* the H-matrix leaf lists (offsets, sizes, ranks), a SHA-256 of the
+  low-rank factors and dense blocks, and the product y = H x for seeded
+  right-hand sides -- HMatrix<double>::build + mvprod_global_to_global;
+* single-block partialACA results on htool's own test geometry
+  (tests/functional_tests/lrmat/test_lrmat_partialACA.cpp:21-67).
+
+Usage (needs the upstream sources, i.e. only in the build container):
+    make -C oracle/refbuild REF=/root/reference/include
+    python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
+from htool_gb300 import geometry as G  # noqa: E402
+from oracle.oracle import Oracle  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def hmatrix_case(R, name, xt, xs, kernel, eps, eta, mus=(1, 3)):
+    ct = R.cluster(xt)
+    cs = ct if xs is xt else R.cluster(xs)
+    perm_t, ni_t, nd_t = ct.export()
+    perm_s, ni_s, nd_s = cs.export()
+    tasks = R.block_tasks(ct, cs, eta)
+    H = R.hmatrix(ct, cs, xt, xs, kernel, eps, eta)
+    lr, dn, uv, dd = H.factors()
+    data = dict(xt=xt, xs=xs, perm_t=perm_t, nodes_i_t=ni_t, nodes_d_t=nd_t, perm_s=perm_s, nodes_i_s=ni_s, nodes_d_s=nd_s, tasks=tasks, lr=lr, dense=dn)
+    for mu in mus:
+        x = G.rhs(xs.shape[0], mu, seed=2)
+        data["x_mu%d" % mu] = x
+        data["y_mu%d" % mu] = H.mvprod(x, mu)
+    infos = R.infos(H)
+    meta = dict(kernel=kernel, eps=eps, eta=eta, minclustersize=10, nb_sons=2, sha_uv=sha(uv), sha_dense=sha(dd), infos=infos, depths_t=ct.depths(), depths_s=cs.depths())
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
+    with open(os.path.join(OUT, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print(name, "leaves", lr.shape[0], dn.shape[0], "ranks", lr[:, 4].min() if len(lr) else None, lr[:, 4].max() if len(lr) else None)
+
+
+def aca_case(R):
+    """test_lrmat_partialACA.cpp: 500 x 100 disks at distances 15..40, srand(1)
+    before each pair, fixed rank 10 and adaptive eps = 1e-4."""
+    out = {}
+    for dist in (15, 20, 30, 40):
+        xt = G.disk_glibc(500, 0.0, srand_seed=1)
+        xs = G.disk_glibc(100, float(dist))
+        ct, cs = R.cluster(xt), R.cluster(xs)
+        res = {}
+        for reqrank in (10, -1):
+            U = np.zeros(500 * 64)
+            V = np.zeros(64 * 100)
+            ss = np.zeros(1)
+            r = R._L.ref_lrmat_partialACA(ct.h, cs.h, 500, xt.ctypes.data, 100, xs.ctypes.data, 1, reqrank, 1e-4, 64, U.ctypes.data, V.ctypes.data, ss.ctypes.data)
+            res["rank_%d" % reqrank] = int(r)
+            res["space_saving_%d" % reqrank] = float(ss[0])
+            res["sha_uv_%d" % reqrank] = sha(np.concatenate([U[: 500 * r], V[: r * 100]]))
+            out["U_%d_%d" % (dist, reqrank)] = U[: 500 * r].reshape(r, 500).T.copy()
+            out["V_%d_%d" % (dist, reqrank)] = V[: r * 100].reshape(100, r).T.copy()
+        out["xt_%d" % dist] = xt
+        out["xs_%d" % dist] = xs
+        out["meta_%d" % dist] = np.frombuffer(json.dumps(res).encode(), np.uint8)
+        print("aca dist", dist, res["rank_10"], res["rank_-1"], res["space_saving_-1"])
+    np.savez_compressed(os.path.join(OUT, "aca_disks.npz"), **out)
+
+
+def main():
+    R = Oracle("reference")
+    R.set_num_threads(1)
+    # BASELINE configuration 1: cylinder, 1/(1e-5 + r), eta 10, eps 1e-6
+    cyl = G.cylinder(4000, seed=1)
+    hmatrix_case(R, "cyl4000_k0", cyl, cyl, 0, 1e-6, 10.0)
+    # Laplace sphere (the configuration-2 geometry at a fixture-sized N)
+    sph = G.sphere(6000, seed=1)
+    hmatrix_case(R, "sphere6000_k1", sph, sph, 1, 1e-6, 10.0)
+    # htool's product test geometry: two glibc-rand disks, 2000 x 1000,
+    # eps 1e-3, eta 10 (test_virtual_hmat_product.hpp:30-90) at the test's
+    # own distance 3 (a single low-rank leaf) and at distance 0.5, where
+    # the block tree has structure
+    for tag, dz in (("d3", 3.0), ("d05", 0.5)):
+        t = G.disk_glibc(2000, 1.0, srand_seed=1)
+        s = G.disk_glibc(1000, 1.0 + dz)
+        hmatrix_case(R, "disks2000x1000_%s_k1" % tag, t, s, 1, 1e-3, 10.0)
+    aca_case(R)
+
+
+if __name__ == "__main__":
+    main()

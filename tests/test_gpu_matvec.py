@@ -1,0 +1,153 @@
+"""GPU product and assembly parity through the C ABI (libhtgpu).
+
+* Leaves built by the CPU oracle (bit-identical to upstream htool's, pinned
+  by test_oracle_golden.py) are loaded into the GPU task table; the GPU
+  product must match the oracle's product within 1e-12 relative (FP64).
+* The GPU's own assembly (device generator + batched device partialACA)
+  must give the same leaf partition and ranks as htool, factors equal to
+  the oracle's up to rounding of the stopping estimator, and the same
+  product within 1e-12.
+"""
+import numpy as np
+import pytest
+
+import htool_gb300 as H
+from htool_gb300 import geometry as G
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+CASES = ["cyl4000_k0", "sphere6000_k1", "disks2000x1000_d3_k1", "disks2000x1000_d05_k1"]
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def gpu_from_oracle(port, xt, xs, kernel, eps, eta):
+    ot, os_ = port.cluster(xt), port.cluster(xs)
+    OH = port.hmatrix(ot, os_, xt, xs, kernel, eps, eta)
+    lr, dn, uv, dd = OH.factors()
+    t = H.Cluster().build(xt.shape[0], xt)
+    s = H.Cluster().build(xs.shape[0], xs)
+    GH = H.HMatrix(t, s, eps, eta).set_leaves(lr, uv, dn, dd)
+    return OH, GH
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_uploaded_leaves_product(port, golden, name):
+    g, meta = golden(name)
+    OH, GH = gpu_from_oracle(port, g["xt"], g["xs"], meta["kernel"], meta["eps"], meta["eta"])
+    for mu in (1, 3):
+        y = GH.mvprod_global_to_global(g["x_mu%d" % mu], mu)
+        assert rel(y, g["y_mu%d" % mu]) < FP64_TOL  # upstream htool's own product
+    nc = g["xs"].shape[0]
+    for mu in (2, 5, 8, 11, 16):
+        x = G.rhs(nc, mu, seed=10 + mu)
+        assert rel(GH.mvprod_global_to_global(x, mu), OH.mvprod(x, mu)) < FP64_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_device_build_matches_reference(port, golden, name):
+    g, meta = golden(name)
+    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    s = H.Cluster().build(g["xs"].shape[0], g["xs"])
+    GH = H.HMatrix(t, s, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"], g["xs"])
+    lr, dn = GH.get_leaves()
+    assert np.array_equal(lr, g["lr"])  # same partition and ranks as htool
+    assert np.array_equal(dn, g["dense"])
+    info = GH.get_infos()
+    for key in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_min", "Dense_block_size_max", "Low_rank_block_size_max"):
+        assert info[key] == meta["infos"][key], key
+    for key in ("Compression_ratio", "Space_saving", "Rank_mean"):
+        assert abs(float(info[key]) - float(meta["infos"][key])) <= 1e-5 * abs(float(meta["infos"][key])), key
+    for mu in (1, 3):
+        assert rel(GH.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < FP64_TOL
+    # factors against the oracle's (bit-identical to upstream's)
+    ot, os_ = port.cluster(g["xt"]), port.cluster(g["xs"])
+    OH = port.hmatrix(ot, os_, g["xt"], g["xs"], meta["kernel"], meta["eps"], meta["eta"])
+    _, _, uv_o, dd_o = OH.factors()
+    _, _, uv_g, dd_g = GH.get_factors()
+    assert np.array_equal(dd_g, dd_o)  # generator entries are bit-exact
+    assert np.max(np.abs(uv_g - uv_o)) <= 1e-12 * np.max(np.abs(uv_o))
+
+
+def test_device_pointers_and_stream():
+    torch = pytest.importorskip("torch")
+    pts = G.sphere(5000, seed=5)
+    t = H.Cluster().build(5000, pts)
+    GH = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+    for mu in (1, 4):
+        x = G.rhs(5000, mu, seed=7)
+        ref = GH.mvprod_global_to_global(x, mu)
+        xd = torch.from_numpy(x).cuda()
+        yd = torch.empty(5000 * mu, dtype=torch.float64, device="cuda")
+        st = torch.cuda.current_stream()
+        GH.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), mu, 0, st.cuda_stream)
+        st.synchronize()
+        assert np.array_equal(yd.cpu().numpy(), ref)  # deterministic: bitwise equal
+
+
+def test_cluster_numbering_flag():
+    torch = pytest.importorskip("torch")
+    pts = G.cylinder(3000, seed=2)
+    t = H.Cluster().build(3000, pts)
+    GH = H.HMatrix(t, t, 1e-6, 10.0).build(H.INV_R_EPS, pts)
+    x = G.rhs(3000)
+    y = GH.mvprod_global_to_global(x)
+    perm = t.get_perm()
+    xd = torch.from_numpy(np.ascontiguousarray(x[perm])).cuda()
+    yd = torch.empty(3000, dtype=torch.float64, device="cuda")
+    GH.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, H.CLUSTER_NUMBERING, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(yd.cpu().numpy(), y[perm])
+
+
+def test_product_is_deterministic_and_linear():
+    pts = G.sphere(8000, seed=9)
+    t = H.Cluster().build(8000, pts)
+    GH = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+    a, b = G.rhs(8000, seed=1), G.rhs(8000, seed=2)
+    ya, yb = GH @ a, GH @ b
+    assert np.array_equal(GH @ a, ya)
+    yab = GH @ (2.0 * a - 3.0 * b)
+    assert rel(yab, 2.0 * ya - 3.0 * yb) < 1e-14
+
+
+@pytest.mark.parametrize("n", [12, 40, 333])
+def test_tiny_problems(port, n):
+    pts = G.sphere(n, seed=n)
+    OH, GH = gpu_from_oracle(port, pts, pts, 1, 1e-6, 10.0)
+    x = G.rhs(n)
+    assert rel(GH @ x, OH.mvprod(x)) < FP64_TOL
+    t = H.Cluster().build(n, pts)
+    GB = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+    assert rel(GB @ x, OH.mvprod(x)) < FP64_TOL
+
+
+def test_dense_reference_error():
+    """htool's product test (test_virtual_hmat_product.hpp:214-219):
+    ||A x - H x|| / ||A x|| < epsilon against the full dense matrix."""
+    pts = G.cylinder(3000, seed=1)
+    t = H.Cluster().build(3000, pts)
+    GH = H.HMatrix(t, t, 1e-6, 10.0).build(H.INV_R_EPS, pts)
+    x = G.rhs(3000)
+    d = np.sqrt(((pts[:, None, :] - pts[None, :, :]) ** 2).sum(-1))
+    yd = (1.0 / (1e-5 + d)) @ x
+    assert rel(GH @ x, yd) < 1e-6
+
+
+def test_bad_arguments():
+    pts = G.sphere(500)
+    t = H.Cluster().build(500, pts)
+    GH = H.HMatrix(t, t, 1e-6, 10.0)
+    with pytest.raises(NotImplementedError):
+        GH.build(7, pts)
+    GH.build(H.LAPLACE, pts)
+    with pytest.raises(ValueError):
+        GH.mvprod_global_to_global(np.zeros(499))
+    lr, dn, uv, dd = GH.get_factors()
+    bad = lr.copy()
+    bad[0, 2] = 10 ** 6
+    with pytest.raises(ValueError, match="out of range"):
+        H.HMatrix(t, t, 1e-6, 10.0).set_leaves(bad, uv, dn, dd)
