@@ -35,8 +35,8 @@ WORKLOAD = dict(workload="laplace_sphere", n=100000, kernel="1/(4 pi r), 0 on th
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -175,14 +175,15 @@ def run_gpu(args):
     x = G.rhs(n, 1, seed=2)
     xd = torch.from_numpy(x).cuda()
     yd = torch.empty(n, dtype=torch.float64, device="cuda")
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
 
-    for _ in range(args.warmup):
-        hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
-    barrier()
     clocks = Clocks(local)
     clocks.start()
+    time.sleep(0.5)  # let the sampler start before the timed region
+    for _ in range(args.warmup):
+        hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)

@@ -270,8 +270,15 @@ class HMatrix:
         return y
 
     def mvprod_ptr(self, x_ptr, y_ptr, mu=1, flags=0, stream=None):
-        """Device (or, with HOST_PTRS, host) pointers; stream-ordered."""
-        _check(lib.htgpu_hmatrix_mvprod(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), mu, flags, C.c_void_p(stream) if stream else None))
+        """Device (or, with HOST_PTRS, host) pointers; ordered on `stream`
+        (a cudaStream_t as an int).  None selects the handle's own stream;
+        0, the legacy default stream (what torch reports for its default
+        stream), is passed on as cudaStreamLegacy."""
+        if stream is None:
+            sarg = None
+        else:
+            sarg = C.c_void_p(1 if int(stream) == 0 else int(stream))
+        _check(lib.htgpu_hmatrix_mvprod(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), mu, flags, sarg))
 
     def __matmul__(self, x):
         return self.mvprod_global_to_global(x, 1)

@@ -7,12 +7,13 @@ to htool_gb300/_build; translation units are compiled in parallel.
 """
 import concurrent.futures
 import os
+import platform
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", platform.machine())
 LIB = os.path.join(HERE, "libhtgpu.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
@@ -56,12 +57,14 @@ def build(verbose=False, jobs=None):
     srcs = _sources()
     with concurrent.futures.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
+    stamp = os.path.join(BUILD, "lib.stamp")
+    if os.path.exists(LIB) and os.path.exists(stamp) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
     cmd = ["g++", "-shared", "-o", LIB] + objs + ["-L" + os.path.join(CUDA, "lib64"), "-lcudart_static", "-ldl", "-lrt", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stderr))
+    open(stamp, "w").write(platform.machine())
     return LIB
 
 

@@ -32,7 +32,7 @@ int max_profitable_rank(int M, int N) {
     return mn / (M + N);
 }
 
-constexpr int kPhase1Chunk = 2048; // source rows per phase-1 warp
+constexpr int kPhase1Chunk = 256;  // source rows per phase-1 warp (tile)
 constexpr int kRowChunk    = 32;   // target rows per phase-2 warp
 constexpr int kDefaultCap  = 48;   // initial ACA scratch columns per block
 
@@ -41,6 +41,9 @@ std::string num(double v) {
     os << v;
     return os.str();
 }
+
+// integer-typed infos (htool's NbrToStr on size_t / int prints every digit)
+std::string inum(long long v) { return std::to_string(v); }
 
 } // namespace
 
@@ -652,21 +655,21 @@ std::map<std::string, std::string> HMatrix::infos() const {
     for (auto &D : dn_h)
         compressed += (double)D.m * (double)D.n;
     const double uncompressed = (double)((long)nr) * nc;
-    m["Source_size"]              = num(nc);
-    m["Target_size"]              = num(nr);
+    m["Source_size"]              = inum(nc);
+    m["Target_size"]              = inum(nr);
     m["Dimension"]                = "1";
-    m["Dense_block_size_max"]     = num((double)dmax);
+    m["Dense_block_size_max"]     = inum((long long)dmax);
     m["Dense_block_size_mean"]    = num(dmean);
-    m["Dense_block_size_min"]     = num((double)(nd ? dmin : 0));
-    m["Low_rank_block_size_max"]  = num((double)lmax);
+    m["Dense_block_size_min"]     = inum((long long)(nd ? dmin : 0));
+    m["Low_rank_block_size_max"]  = inum((long long)lmax);
     m["Low_rank_block_size_mean"] = num(lmean);
-    m["Low_rank_block_size_min"]  = num((double)(nl ? lmin : 0));
-    m["Rank_max"]                 = num((double)rmax);
+    m["Low_rank_block_size_min"]  = inum((long long)(nl ? lmin : 0));
+    m["Rank_max"]                 = inum((long long)rmax);
     m["Rank_mean"]                = num(rmean);
-    m["Rank_min"]                 = num((double)(nl ? rmin : 0));
-    m["Number_of_lrmat"]          = num(nl);
-    m["Number_of_dmat"]           = num(nd);
-    m["Number_of_false_positive"] = num(st_.false_positive);
+    m["Rank_min"]                 = inum((long long)(nl ? rmin : 0));
+    m["Number_of_lrmat"]          = inum(nl);
+    m["Number_of_dmat"]           = inum(nd);
+    m["Number_of_false_positive"] = inum(st_.false_positive);
     m["Compression_ratio"]        = num(uncompressed / compressed);
     m["Space_saving"]             = num(1 - compressed / uncompressed);
     m["Eta"]                      = num(eta_);
@@ -679,24 +682,24 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["MaxClusterDepthTarget"]    = num(T->max_depth);
     m["MinClusterDepthSource"]    = num(S->min_depth);
     m["MaxClusterDepthSource"]    = num(S->max_depth);
-    m["MaxBlockSize"]             = num((double)bp.maxblocksize);
+    m["MaxBlockSize"]             = inum((long long)bp.maxblocksize);
     m["Block_tree_max"]           = num(st_.block_tree_seconds);
     m["Block_tree_mean"]          = num(st_.block_tree_seconds);
     m["Blocks_max"]               = num(st_.build_seconds - st_.block_tree_seconds);
     m["Blocks_mean"]              = num(st_.build_seconds - st_.block_tree_seconds);
     m["Number_of_MPI_tasks"]      = "1";
-    m["Local_size_max"]           = num(nr);
+    m["Local_size_max"]           = inum(nr);
     m["Local_size_mean"]          = num(nr);
-    m["Local_size_min"]           = num(nr);
+    m["Local_size_min"]           = inum(nr);
     m["GPU_aca_rounds"]           = num(st_.aca_rounds);
-    m["GPU_aca_blocks"]           = num((double)st_.aca_blocks);
+    m["GPU_aca_blocks"]           = inum(st_.aca_blocks);
     m["GPU_aca_overflow_reruns"]  = num(st_.overflow_reruns);
     m["GPU_aca_seconds"]          = num(st_.aca_seconds);
     m["GPU_build_seconds"]        = num(st_.build_seconds);
-    m["GPU_stored_bytes"]         = num((double)stored_bytes());
-    m["GPU_phase1_items"]         = num((double)p1_h.size());
-    m["GPU_phase2_items"]         = num((double)p2_h.size());
-    m["GPU_phase2_contributions"] = num((double)c_h.size());
+    m["GPU_stored_bytes"]         = inum(stored_bytes());
+    m["GPU_phase1_items"]         = inum((long long)p1_h.size());
+    m["GPU_phase2_items"]         = inum((long long)p2_h.size());
+    m["GPU_phase2_contributions"] = inum((long long)c_h.size());
     return m;
 }
 

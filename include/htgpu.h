@@ -113,7 +113,8 @@ int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const
  * unless HTGPU_CLUSTER_NUMBERING.  With HTGPU_HOST_PTRS the pointers are host
  * memory and the call returns when out is written; otherwise they are device
  * pointers and the call is ordered on `stream` (a cudaStream_t; NULL = the
- * handle's own stream) and returns at once. */
+ * handle's own stream; cudaStreamLegacy / cudaStreamPerThread select the
+ * default streams) and returns at once. */
 int htgpu_hmatrix_mvprod(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream);
 
 /* nb_rows / nb_cols, get_nlrmat / get_ndmat (hmatrix.hpp:173-187). */

@@ -29,12 +29,19 @@ _d = C.c_double
 
 
 def build_port(force=False):
-    """Compile oracle/htool_oracle.c into oracle/liboracle.so."""
+    """Compile oracle/htool_oracle.c into oracle/liboracle.so (rebuilt when
+    the source is newer or the library was built on another architecture)."""
+    import platform
+
     src = os.path.join(HERE, "htool_oracle.c")
-    if not force and os.path.exists(PORT_SO) and os.path.getmtime(PORT_SO) >= os.path.getmtime(src):
+    stamp = PORT_SO + ".arch"
+    fresh = os.path.exists(PORT_SO) and os.path.getmtime(PORT_SO) >= os.path.getmtime(src)
+    same_arch = os.path.exists(stamp) and open(stamp).read() == platform.machine()
+    if not force and fresh and same_arch:
         return PORT_SO
     cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", PORT_SO, "-lm"]
     subprocess.check_call(cmd)
+    open(stamp, "w").write(platform.machine())
     return PORT_SO
 
 
@@ -134,8 +141,7 @@ class Oracle:
     def __init__(self, kind="port"):
         self.kind = kind
         if kind == "port":
-            if not os.path.exists(PORT_SO):
-                build_port()
+            build_port()
             L = C.CDLL(PORT_SO)
             p = "orc_"
             self._L = L
