@@ -276,4 +276,12 @@ int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms) {
     });
 }
 
+int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out, int mu, void *stream) {
+    return guarded([&] {
+        if (h == nullptr)
+            throw htgpu::Error(HTGPU_ERR_INVALID, "[Htool error] hmatrix is null");
+        h->h->mvprod_noalloc(in, out, mu, (cudaStream_t)stream);
+    });
+}
+
 } // extern "C"

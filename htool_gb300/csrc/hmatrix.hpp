@@ -33,6 +33,10 @@ class HMatrix {
     void mvprod(const double *in, double *out, int mu, bool host_ptrs, bool cluster_numbering, cudaStream_t st);
     // per-launch timing of reps products (ms[0..3]: gather, phase 1, phase 2, total)
     void profile(int mu, int reps, float *ms);
+    // the product with device pointers whose working memory is a fixed array
+    // of the library (noalloc.cu); allocates nothing
+    void mvprod_noalloc(const double *in, double *out, int mu, cudaStream_t st);
+    std::size_t noalloc_scratch_need(int mu) const;
 
     int nb_rows() const { return nr; }
     int nb_cols() const { return nc; }

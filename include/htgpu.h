@@ -147,6 +147,25 @@ int htgpu_hmatrix_last_launches(htgpu_hmatrix h, int *launches);
  * (nb_mat_vec_prod / total_time_mat_vec_prod, hmatrix.hpp:1180-1181). */
 int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
 
+/* No counterpart in the reference.  The product of htgpu_hmatrix_mvprod for
+ * device pointers, but allocation-free: it never calls cudaMalloc, cudaFree
+ * or any other allocating routine, for callers that cannot let a library
+ * allocate device memory mid-run -- e.g. a process whose framework has
+ * already reserved the GPU's memory for its own pool, or a solver driving
+ * the product from a hot loop.  Its working memory is one fixed 16 MiB
+ * array per device inside the library (2^21 doubles, held by every GPU that
+ * loads the library until the process exits); a product needs
+ * nb_cols * mu (rounded up to 32) + (phase-1 partial sums) * mu doubles, and
+ * larger requests fail with HTGPU_ERR_INVALID.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current, so make it before any stream capture.  Every call shares
+ * the one array, whose contents persist between calls: calls that may
+ * overlap on the GPU (different streams, or different handles on one
+ * device) race with each other and must be serialised by the caller.
+ * in/out: device memory, column-major, user numbering; ordered on `stream`
+ * (NULL = the handle's own stream). */
+int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out, int mu, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
