@@ -60,6 +60,10 @@ def _load():
         "htgpu_hmatrix_product_bytes": (i, [vp, i, vp]),
         "htgpu_hmatrix_last_launches": (i, [vp, vp]),
         "htgpu_hmatrix_profile": (i, [vp, i, i, vp]),
+        "htgpu_hmatrix_set_fp64_split": (i, [vp, i, i]),
+        "htgpu_hmatrix_get_fp64_split": (i, [vp, vp, vp]),
+        "htgpu_hmatrix_autotune": (i, [vp, i, i, vp]),
+        "htgpu_hmatrix_mvprod_noalloc": (i, [vp, vp, vp, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -258,6 +262,20 @@ class HMatrix:
         ms = np.zeros(4, np.float32)
         _check(lib.htgpu_hmatrix_profile(self.h, mu, reps, _ptr(ms)))
         return tuple(float(v) for v in ms)
+
+    def set_fp64_split(self, phase1_dfma_permille, phase2_dfma_warps):
+        _check(lib.htgpu_hmatrix_set_fp64_split(self.h, int(phase1_dfma_permille), int(phase2_dfma_warps)))
+
+    def get_fp64_split(self):
+        a, b = C.c_int(), C.c_int()
+        _check(lib.htgpu_hmatrix_get_fp64_split(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def autotune(self, mu=1, reps=5):
+        """Pick the fastest FP64 split for this H-matrix; returns ms/product."""
+        ms = C.c_float()
+        _check(lib.htgpu_hmatrix_autotune(self.h, int(mu), int(reps), C.byref(ms)))
+        return ms.value
 
     def mvprod_global_to_global(self, x, mu=1):
         """Host arrays in and out (column-major, mu right-hand sides)."""

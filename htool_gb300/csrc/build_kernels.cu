@@ -313,13 +313,13 @@ __global__ void pack_factors_kernel(const PackItem *__restrict__ items, const do
         arena[it.dst_v + e] = scratch[it.src_v + e];
 }
 
-__global__ void dense_fill_kernel(const DenseLeaf *__restrict__ leaves, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t, const int *__restrict__ perm_s,
+__global__ void dense_fill_kernel(const DenseChunk *__restrict__ chunks, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t, const int *__restrict__ perm_s,
                                   KernelDesc kd, double *__restrict__ arena) {
-    const DenseLeaf L = leaves[blockIdx.x];
-    const int mn      = L.m * L.n;
-    for (int e = threadIdx.x; e < mn; e += blockDim.x) {
-        int i = e % L.m, j = e / L.m;
-        arena[L.d_off + e] = kernel_entry(kd, xt + 3 * (size_t)perm_t[L.oi + i], xs + 3 * (size_t)perm_s[L.oj + j]);
+    const DenseChunk C = chunks[blockIdx.x];
+    const int hn       = C.h * C.n;
+    for (int e = threadIdx.x; e < hn; e += blockDim.x) {
+        int i = e % C.h, j = e / C.h;
+        arena[C.dst + e] = kernel_entry(kd, xt + 3 * (size_t)perm_t[C.row0 + i], xs + 3 * (size_t)perm_s[C.oj + j]);
     }
 }
 
@@ -340,10 +340,10 @@ void launch_pack_factors(const PackItem *items, int nitems, const double *scratc
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_dense_fill(const DenseLeaf *leaves, int nleaves, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st) {
-    if (nleaves <= 0)
+void launch_dense_fill(const DenseChunk *chunks, int nchunks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st) {
+    if (nchunks <= 0)
         return;
-    dense_fill_kernel<<<nleaves, 128, 0, st>>>(leaves, xt, xs, perm_t, perm_s, kd, arena);
+    dense_fill_kernel<<<nchunks, 128, 0, st>>>(chunks, xt, xs, perm_t, perm_s, kd, arena);
     HTGPU_CUDA(cudaGetLastError());
 }
 

@@ -276,6 +276,30 @@ int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms) {
     });
 }
 
+int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int p1, int n64) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_fp64_split(p1, n64);
+    });
+}
+
+int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *p1, int *n64) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(p1, "phase1_dfma_permille");
+        need(n64, "phase2_dfma_warps");
+        h->h->get_fp64_split(p1, n64);
+    });
+}
+
+int htgpu_hmatrix_autotune(htgpu_hmatrix h, int mu, int reps, float *best_ms) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        htgpu::require(mu > 0 && reps > 0, "mu and reps must be positive");
+        h->h->autotune_fp64(mu, reps, best_ms);
+    });
+}
+
 int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out, int mu, void *stream) {
     return guarded([&] {
         if (h == nullptr)

@@ -35,6 +35,7 @@ int max_profitable_rank(int M, int N) {
 constexpr int kPhase1Chunk = 256;  // source rows per phase-1 warp (tile)
 constexpr int kRowChunk    = 32;   // target rows per phase-2 warp
 constexpr int kDefaultCap  = 48;   // initial ACA scratch columns per block
+constexpr int kP2WarpsHost = 4;    // warps per phase-2 CTA (matvec_kernels.cu)
 
 std::string num(double v) {
     std::ostringstream os;
@@ -56,6 +57,9 @@ HMatrix::HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const Clu
     nc     = S->n;
     HTGPU_CUDA(cudaSetDevice(device_));
     HTGPU_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    HTGPU_CUDA(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
+    HTGPU_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    HTGPU_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
     perm_t.upload(T->perm, stream_);
     perm_s.upload(S->perm, stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
@@ -63,6 +67,12 @@ HMatrix::HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const Clu
 
 HMatrix::~HMatrix() {
     cudaSetDevice(device_);
+    if (fork_)
+        cudaEventDestroy(fork_);
+    if (join_)
+        cudaEventDestroy(join_);
+    if (aux_)
+        cudaStreamDestroy(aux_);
     if (stream_)
         cudaStreamDestroy(stream_);
 }
@@ -286,8 +296,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
         return S->nodes[reqs[a.req].s].offset < S->nodes[reqs[b.req].s].offset;
     });
     lr_h.clear();
-    long long total = 0;
-    std::vector<std::vector<PackItem>> per_round(round_bufs.size());
+    std::vector<LeafSrc> lr_src;
     for (auto &a : acc) {
         const ClusterNode &tn = T->nodes[reqs[a.req].t], &sn = S->nodes[reqs[a.req].s];
         LrLeaf L;
@@ -297,34 +306,10 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
         L.n     = sn.size;
         L.r     = a.r;
         L.nch   = 0;
-        L.u_off = total;
-        L.v_off = total + (long long)L.m * L.r;
         L.a_off = 0;
-        total += (long long)L.r * (L.m + L.n);
         lr_h.push_back(L);
-        PackItem it;
-        it.src_u = a.u;
-        it.src_v = a.v;
-        it.dst_u = L.u_off;
-        it.dst_v = L.v_off;
-        it.M     = L.m;
-        it.N     = L.n;
-        it.r     = L.r;
-        it.pad   = 0;
-        per_round[a.round].push_back(it);
+        lr_src.push_back({a.round, a.u, a.v});
     }
-    fac.alloc(std::max<long long>(total, 1));
-    for (std::size_t rd = 0; rd < round_bufs.size(); rd++) {
-        if (per_round[rd].empty())
-            continue;
-        DevBuf<PackItem> ditems;
-        ditems.upload(per_round[rd], stream_);
-        launch_pack_factors(ditems.p, (int)per_round[rd].size(), round_bufs[rd]->p, fac.p, stream_);
-        HTGPU_CUDA(cudaStreamSynchronize(stream_));
-        round_bufs[rd].reset();
-    }
-
-    // ---- dense leaves
     std::sort(dense_ts.begin(), dense_ts.end(), [&](const std::pair<int, int> &a, const std::pair<int, int> &b) {
         int ia = T->nodes[a.first].offset, ib = T->nodes[b.first].offset;
         if (ia != ib)
@@ -332,22 +317,12 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
         return S->nodes[a.second].offset < S->nodes[b.second].offset;
     });
     dn_h.clear();
-    long long dtot = 0;
-    for (auto &d : dense_ts) {
-        DenseLeaf L;
-        L.oi    = T->nodes[d.first].offset;
-        L.oj    = S->nodes[d.second].offset;
-        L.m     = T->nodes[d.first].size;
-        L.n     = S->nodes[d.second].size;
-        L.d_off = dtot;
-        dtot += (long long)L.m * L.n;
-        dn_h.push_back(L);
-    }
-    dense.alloc(std::max<long long>(dtot, 1));
-    dn_d.upload(dn_h, stream_);
-    launch_dense_fill(dn_d.p, (int)dn_h.size(), dxt.p, dxs.p, perm_t.p, perm_s.p, kd, dense.p, stream_);
-    HTGPU_CUDA(cudaStreamSynchronize(stream_));
-    plan();
+    for (auto &d : dense_ts)
+        dn_h.push_back({T->nodes[d.first].offset, S->nodes[d.second].offset, T->nodes[d.first].size, S->nodes[d.second].size});
+    std::vector<const double *> bufs;
+    for (auto &b : round_bufs)
+        bufs.push_back(b->p);
+    finalize(bufs, lr_src, nullptr, &kd, dxt.p, dxs.p);
     st_.build_seconds = now() - t0;
 }
 
@@ -355,6 +330,7 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
     HTGPU_CUDA(cudaSetDevice(device_));
     lr_h.clear();
     dn_h.clear();
+    std::vector<LeafSrc> lr_src, dn_src;
     long long total = 0;
     for (int b = 0; b < nlr; b++) {
         LrLeaf L;
@@ -365,25 +341,11 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
         L.r  = lr_desc[5 * b + 4];
         require(L.oi >= 0 && L.m > 0 && L.oi + L.m <= nr && L.oj >= 0 && L.n > 0 && L.oj + L.n <= nc && L.r >= 0, "low-rank leaf " + std::to_string(b) + " is out of range");
         L.nch   = 0;
-        L.u_off = total;
-        L.v_off = total + (long long)L.m * L.r;
         L.a_off = 0;
+        lr_src.push_back({0, total, total + (long long)L.m * L.r});
         total += (long long)L.r * (L.m + L.n);
         lr_h.push_back(L);
     }
-    // reference layout -> device layout: U as is, V (r x n) -> Vt (n x r)
-    std::vector<double> host(std::max<long long>(total, 1));
-    long long src = 0;
-    for (auto &L : lr_h) {
-        std::copy(uv + src, uv + src + (long long)L.m * L.r, host.begin() + L.u_off);
-        src += (long long)L.m * L.r;
-        for (int j = 0; j < L.n; j++)
-            for (int k = 0; k < L.r; k++)
-                host[L.v_off + j + (long long)L.n * k] = uv[src + k + (long long)L.r * j];
-        src += (long long)L.n * L.r;
-    }
-    fac.upload(host, stream_);
-    long long dtot = 0;
     for (int b = 0; b < nd; b++) {
         DenseLeaf L;
         L.oi = d_desc[4 * b];
@@ -391,24 +353,51 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
         L.m  = d_desc[4 * b + 2];
         L.n  = d_desc[4 * b + 3];
         require(L.oi >= 0 && L.m > 0 && L.oi + L.m <= nr && L.oj >= 0 && L.n > 0 && L.oj + L.n <= nc, "dense leaf " + std::to_string(b) + " is out of range");
-        L.d_off = dtot;
-        dtot += (long long)L.m * L.n;
+        dn_src.push_back({0, total, 0});
+        total += (long long)L.m * L.n;
         dn_h.push_back(L);
     }
-    dense.upload(dn, dtot, stream_);
-    if (dtot == 0)
-        dense.alloc(1);
+    // one staging buffer in the simple layout: U as given, V (r x n) -> Vt
+    // (n x r), dense as given
+    std::vector<double> host(std::max<long long>(total, 1));
+    long long src = 0;
+    for (std::size_t l = 0; l < lr_h.size(); l++) {
+        const LrLeaf &L = lr_h[l];
+        std::copy(uv + src, uv + src + (long long)L.m * L.r, host.begin() + lr_src[l].su);
+        src += (long long)L.m * L.r;
+        for (int j = 0; j < L.n; j++)
+            for (int k = 0; k < L.r; k++)
+                host[lr_src[l].sv + j + (long long)L.n * k] = uv[src + k + (long long)L.r * j];
+        src += (long long)L.n * L.r;
+    }
+    long long dsrc = 0;
+    for (std::size_t d = 0; d < dn_h.size(); d++) {
+        const long long e = (long long)dn_h[d].m * dn_h[d].n;
+        std::copy(dn + dsrc, dn + dsrc + e, host.begin() + dn_src[d].su);
+        dsrc += e;
+    }
+    DevBuf<double> staging;
+    staging.upload(host, stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
     st_ = BuildStats();
-    plan();
+    finalize({staging.p}, lr_src, &dn_src, nullptr, nullptr, nullptr);
 }
 
-// Work decomposition of the product.
-//  phase 1: one item per (low-rank leaf, chunk of <= kPhase1Chunk source rows)
-//  phase 2: target rows are cut into "atoms" at every leaf row boundary, so
-//           each leaf covers whole atoms; atoms are cut into chunks of
-//           <= kRowChunk rows, one warp each, listing every covering leaf.
-void HMatrix::plan() {
+// Final layout and work decomposition.
+//  target rows are cut into "atoms" at every leaf row boundary (so each leaf
+//  covers whole atoms), atoms into chunks of <= kRowChunk rows: one phase-2
+//  item each, listing every covering leaf in a fixed order (dense, then
+//  low-rank, each in (offset_i, offset_j) order);
+//  every low-rank leaf's source rows are cut into tiles of <= kPhase1Chunk
+//  rows: one phase-1 item each.
+//  The arena holds all phase-1 tiles (item order), then all phase-2 blocks
+//  (item order), each block 16-byte aligned.
+void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs) {
+    auto even = [](long long v) { return (v + 1) & ~1LL; };
+    long long off = 0;
+    std::vector<std::vector<BlockCopy>> copies(bufs.size());
+    std::vector<DenseChunk> fills;
+    // phase-1 tiles
     p1_h.clear();
     a_slots = 0;
     for (int l = 0; l < (int)lr_h.size(); l++) {
@@ -421,8 +410,16 @@ void HMatrix::plan() {
         L.a_off = a_slots;
         a_slots += (long long)L.nch * L.r;
         for (int ch = 0; ch < L.nch; ch++) {
-            int j0 = ch * kPhase1Chunk;
-            p1_h.push_back({l, ch, j0, std::min(kPhase1Chunk, L.n - j0)});
+            P1Item it;
+            it.j0    = ch * kPhase1Chunk;
+            it.jlen  = std::min(kPhase1Chunk, L.n - it.j0);
+            it.leaf  = l;
+            it.chunk = ch;
+            it.pad   = 0;
+            it.off   = off;
+            p1_h.push_back(it);
+            copies[lr_src[l].buf].push_back({lr_src[l].sv + it.j0, off, it.jlen, L.r, L.n, 0});
+            off += even((long long)it.jlen * L.r);
         }
     }
     // atoms
@@ -441,8 +438,6 @@ void HMatrix::plan() {
     const int natoms = (int)cuts.size() - 1;
     auto atom_of     = [&](int row) { return (int)(std::lower_bound(cuts.begin(), cuts.end(), row) - cuts.begin()); };
     std::vector<int> cnt(natoms + 1, 0);
-    // contributions in a fixed order: dense leaves first, then low-rank,
-    // each in (offset_i, offset_j) order
     struct Span {
         int leaf, a0, a1;
     };
@@ -456,36 +451,87 @@ void HMatrix::plan() {
         for (int a = sp.a0; a < sp.a1; a++)
             cnt[a + 1]++;
     std::partial_sum(cnt.begin(), cnt.end(), cnt.begin());
-    std::vector<P2Contrib> by_atom(cnt[natoms]);
+    std::vector<int> by_atom(cnt[natoms]);
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (auto &sp : spans) {
-        const int oi = sp.leaf >= 0 ? lr_h[sp.leaf].oi : dn_h[~sp.leaf].oi;
+    for (auto &sp : spans)
         for (int a = sp.a0; a < sp.a1; a++)
-            by_atom[fill[a]++] = {sp.leaf, cuts[a] - oi};
-    }
+            by_atom[fill[a]++] = sp.leaf;
     p2_h.clear();
     c_h.clear();
+    c_leaf.clear();
     for (int a = 0; a < natoms; a++) {
         for (int r0 = cuts[a]; r0 < cuts[a + 1]; r0 += kRowChunk) {
             P2Item it;
             it.row0 = r0;
             it.h    = std::min(kRowChunk, cuts[a + 1] - r0);
             it.cbeg = (int)c_h.size();
-            for (int c = cnt[a]; c < cnt[a + 1]; c++)
-                c_h.push_back({by_atom[c].leaf, by_atom[c].rowoff + (r0 - cuts[a])});
+            for (int c = cnt[a]; c < cnt[a + 1]; c++) {
+                const int leaf = by_atom[c];
+                P2Contrib pc;
+                pc.off = off;
+                if (leaf >= 0) {
+                    const LrLeaf &L = lr_h[leaf];
+                    pc.w            = L.r;
+                    pc.aux          = (int)L.a_off; // phase-1 slot of the coefficients
+                    copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + (r0 - L.oi), off, it.h, L.r, L.m, 0});
+                } else {
+                    const DenseLeaf &D = dn_h[~leaf];
+                    pc.w               = D.n;
+                    pc.aux             = ~D.oj;
+                    if (dn_src)
+                        copies[(*dn_src)[~leaf].buf].push_back({(*dn_src)[~leaf].su + (r0 - D.oi), off, it.h, D.n, D.m, 0});
+                    else
+                        fills.push_back({off, r0, it.h, D.oj, D.n});
+                }
+                off += even((long long)it.h * pc.w);
+                c_h.push_back(pc);
+                c_leaf.push_back(leaf);
+            }
             it.cend = (int)c_h.size();
             p2_h.push_back(it);
         }
     }
+    arena_len = off;
+    fac.alloc(std::max<long long>(off, 2));
+    HTGPU_CUDA(cudaMemsetAsync(fac.p, 0, sizeof(double) * (std::size_t)std::max<long long>(off, 2), stream_));
+    for (std::size_t b = 0; b < bufs.size(); b++) {
+        if (copies[b].empty())
+            continue;
+        DevBuf<BlockCopy> dcp;
+        dcp.upload(copies[b], stream_);
+        launch_block_copy(dcp.p, (int)copies[b].size(), bufs[b], fac.p, stream_);
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    }
+    if (!fills.empty()) {
+        DevBuf<DenseChunk> dfl;
+        dfl.upload(fills, stream_);
+        launch_dense_fill(dfl.p, (int)fills.size(), dxt, dxs, perm_t.p, perm_s.p, *kd, fac.p, stream_);
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    }
+    multi_h.clear();
+    for (int l = 0; l < (int)lr_h.size(); l++)
+        if (lr_h[l].nch > 1)
+            multi_h.push_back(l);
+    multi_d.upload(multi_h, stream_);
+    if (multi_h.empty())
+        multi_d.alloc(1);
+    // emulation range check: every stored entry below 2^60 in magnitude
+    {
+        DevBuf<int> e;
+        e.alloc(1);
+        int ef = 0;
+        launch_xexp(fac.p, off, e.p, stream_);
+        HTGPU_CUDA(cudaMemcpyAsync(&ef, e.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+        emu_ok_ = ef < 1023 + 60;
+    }
+    assign_phase1_modes();
+    upload_phase1_lists();
     lr_d.upload(lr_h, stream_);
-    dn_d.upload(dn_h, stream_);
-    p1_d.upload(p1_h, stream_);
     p2_d.upload(p2_h, stream_);
     c_d.upload(c_h, stream_);
     if (lr_h.empty())
         lr_d.alloc(1);
-    if (dn_h.empty())
-        dn_d.alloc(1);
     if (c_h.empty())
         c_d.alloc(1);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
@@ -496,6 +542,8 @@ void HMatrix::ensure_work(int mu) {
     if (mu <= mu_cap)
         return;
     xp.alloc((std::size_t)nc * mu + 1);
+    xs.alloc((std::size_t)nc * mu + 1);
+    xexp.alloc(1);
     A.alloc((std::size_t)std::max<long long>(a_slots, 1) * mu);
     xstage.alloc((std::size_t)nc * mu);
     ystage.alloc((std::size_t)nr * mu);
@@ -516,25 +564,126 @@ void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, bool
         x = xstage.p;
         y = ystage.p;
     }
-    launches_ = 0;
-    launch_gather(x, nc, cluster_numbering ? nullptr : perm_s.p, nc, mu, xp.p, st);
-    launches_++;
-    int groups = 0;
-    for (int c0 = 0; c0 < mu;) {
-        int left = mu - c0;
-        c0 += left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
-        groups++;
-    }
-    if (!p1_h.empty()) {
-        launch_phase1(p1_d.p, (int)p1_h.size(), lr_d.p, fac.p, xp.p, mu, A.p, st);
-        launches_ += groups;
-    }
-    launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, dn_d.p, fac.p, dense.p, A.p, xp.p, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
-    launches_ += groups;
+    launch_product(x, y, mu, cluster_numbering, st);
     if (host_ptrs) {
         HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * (std::size_t)nr * mu, cudaMemcpyDeviceToHost, st));
         HTGPU_CUDA(cudaStreamSynchronize(st));
     }
+}
+
+// phase-1 tiles on the FP64 pipe: among tiles of at least 128 rows (full
+// lanes), by error diffusion so that DFMA tiles carry p1_permille_ / 1000 of
+// all phase-1 elements and are spread through the launch
+void HMatrix::assign_phase1_modes() {
+    const double target = emu_ok_ ? p1_permille_ / 1000.0 : 1.0;
+    long long seen = 0, dfma = 0;
+    for (auto &it : p1_h) {
+        it.chunk &= ~kEmuBit;
+        const long long e = (long long)it.jlen * lr_h[it.leaf].r;
+        seen += e;
+        const bool use_dfma = !emu_ok_ || target >= 1.0 || (it.jlen >= 128 && (double)dfma < target * (double)seen);
+        if (use_dfma)
+            dfma += e;
+        else
+            it.chunk |= kEmuBit;
+    }
+}
+
+void HMatrix::upload_phase1_lists() {
+    std::vector<P1Item> a, b;
+    for (auto &it : p1_h)
+        ((it.chunk & kEmuBit) ? b : a).push_back(it);
+    n_p1_dfma_ = (int)a.size();
+    n_p1_emu_  = (int)b.size();
+    p1_d.upload(a, stream_);
+    p1e_d.upload(b, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HMatrix::set_fp64_split(int p1, int n64) {
+    require(p1 >= 0 && p1 <= 1000 && n64 >= 0 && n64 <= 4, "FP64 split: phase-1 share in [0, 1000], phase-2 warps in [0, 4]");
+    p1_permille_ = p1;
+    p2_n64_      = n64;
+    assign_phase1_modes();
+    upload_phase1_lists();
+}
+
+void HMatrix::get_fp64_split(int *p1, int *n64) const {
+    *p1  = emu_ok_ ? p1_permille_ : 1000;
+    *n64 = emu_ok_ ? p2_n64_ : kP2WarpsHost;
+}
+
+void HMatrix::launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st) { launch_product_with(x, y, mu, cluster_numbering, st, xp.p, xs.p, xexp.p, A.p); }
+
+// The phase-1 tiles on the FP64 pipe and those on the emulation run as two
+// kernels on two streams at once (fork/join through events), so each keeps
+// its own register budget and both pipe families work together.
+void HMatrix::launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A) {
+    const int groups = rhs_groups(mu);
+    launches_        = 0;
+    launch_xexp(x, (long long)nc * mu, w_xexp, st);
+    launch_gather_split(x, nc, cluster_numbering ? nullptr : perm_s.p, nc, mu, w_xexp, w_xp, w_xs, st);
+    launches_ += 2;
+    if (n_p1_dfma_ && n_p1_emu_) {
+        HTGPU_CUDA(cudaEventRecord(fork_, st));
+        HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
+        launch_phase1(p1_d.p, n_p1_dfma_, false, lr_d.p, fac.p, w_xp, w_xs, w_xexp, mu, w_A, st);
+        launch_phase1(p1e_d.p, n_p1_emu_, true, lr_d.p, fac.p, w_xp, w_xs, w_xexp, mu, w_A, aux_);
+        HTGPU_CUDA(cudaEventRecord(join_, aux_));
+        HTGPU_CUDA(cudaStreamWaitEvent(st, join_, 0));
+        launches_ += 2 * groups;
+    } else if (n_p1_dfma_) {
+        launch_phase1(p1_d.p, n_p1_dfma_, false, lr_d.p, fac.p, w_xp, w_xs, w_xexp, mu, w_A, st);
+        launches_ += groups;
+    } else if (n_p1_emu_) {
+        launch_phase1(p1e_d.p, n_p1_emu_, true, lr_d.p, fac.p, w_xp, w_xs, w_xexp, mu, w_A, st);
+        launches_ += groups;
+    }
+    if (!multi_h.empty()) {
+        launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, w_A, st);
+        launches_++;
+    }
+    launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, emu_ok_ ? p2_n64_ : kP2WarpsHost, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
+    launches_ += groups;
+}
+
+void HMatrix::autotune_fp64(int mu, int reps, float *best_ms) {
+    HTGPU_CUDA(cudaSetDevice(device_));
+    ensure_work(mu);
+    HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
+    std::vector<std::pair<int, int>> cands;
+    if (!emu_ok_)
+        cands.push_back({1000, 4});
+    else
+        for (int p1 : {0, 200, 350, 500, 650, 1000})
+            for (int n64 : {0, 1, 2, 4})
+                cands.push_back({p1, n64});
+    cudaEvent_t e0, e1;
+    HTGPU_CUDA(cudaEventCreate(&e0));
+    HTGPU_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    std::pair<int, int> arg = cands[0];
+    for (auto &c : cands) {
+        set_fp64_split(c.first, c.second);
+        launch_product(xstage.p, ystage.p, mu, false, stream_); // warm-up
+        HTGPU_CUDA(cudaEventRecord(e0, stream_));
+        for (int r = 0; r < reps; r++)
+            launch_product(xstage.p, ystage.p, mu, false, stream_);
+        HTGPU_CUDA(cudaEventRecord(e1, stream_));
+        HTGPU_CUDA(cudaEventSynchronize(e1));
+        float ms;
+        HTGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= reps;
+        if (ms < best) {
+            best = ms;
+            arg  = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_fp64_split(arg.first, arg.second);
+    if (best_ms)
+        *best_ms = best;
 }
 
 void HMatrix::profile(int mu, int reps, float *ms) {
@@ -545,14 +694,26 @@ void HMatrix::profile(int mu, int reps, float *ms) {
         HTGPU_CUDA(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
+    const int n64 = emu_ok_ ? p2_n64_ : kP2WarpsHost;
     for (int r = 0; r < reps; r++) {
         HTGPU_CUDA(cudaEventRecord(ev[0], stream_));
-        launch_gather(xstage.p, nc, perm_s.p, nc, mu, xp.p, stream_);
+        launch_xexp(xstage.p, (long long)nc * mu, xexp.p, stream_);
+        launch_gather_split(xstage.p, nc, perm_s.p, nc, mu, xexp.p, xp.p, xs.p, stream_);
         HTGPU_CUDA(cudaEventRecord(ev[1], stream_));
-        if (!p1_h.empty())
-            launch_phase1(p1_d.p, (int)p1_h.size(), lr_d.p, fac.p, xp.p, mu, A.p, stream_);
+        if (n_p1_dfma_ && n_p1_emu_) {
+            HTGPU_CUDA(cudaEventRecord(fork_, stream_));
+            HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
+            launch_phase1(p1_d.p, n_p1_dfma_, false, lr_d.p, fac.p, xp.p, xs.p, xexp.p, mu, A.p, stream_);
+            launch_phase1(p1e_d.p, n_p1_emu_, true, lr_d.p, fac.p, xp.p, xs.p, xexp.p, mu, A.p, aux_);
+            HTGPU_CUDA(cudaEventRecord(join_, aux_));
+            HTGPU_CUDA(cudaStreamWaitEvent(stream_, join_, 0));
+        } else if (n_p1_dfma_ || n_p1_emu_) {
+            launch_phase1(n_p1_dfma_ ? p1_d.p : p1e_d.p, n_p1_dfma_ ? n_p1_dfma_ : n_p1_emu_, n_p1_dfma_ == 0, lr_d.p, fac.p, xp.p, xs.p, xexp.p, mu, A.p, stream_);
+        }
+        if (!multi_h.empty())
+            launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, A.p, stream_);
         HTGPU_CUDA(cudaEventRecord(ev[2], stream_));
-        launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, dn_d.p, fac.p, dense.p, A.p, xp.p, mu, perm_t.p, ystage.p, nr, stream_);
+        launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, fac.p, A.p, xp.p, xs.p, xexp.p, n64, mu, perm_t.p, ystage.p, nr, stream_);
         HTGPU_CUDA(cudaEventRecord(ev[3], stream_));
         HTGPU_CUDA(cudaEventSynchronize(ev[3]));
         float t;
@@ -585,31 +746,48 @@ void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {
     }
 }
 
+// inverse of the final layout, into htool's layouts
 void HMatrix::export_factors(double *uv, double *dn) {
     HTGPU_CUDA(cudaSetDevice(device_));
-    if (uv && !lr_h.empty()) {
-        long long total = 0;
-        for (auto &L : lr_h)
-            total += (long long)L.r * (L.m + L.n);
-        std::vector<double> host(std::max<long long>(total, 1));
-        if (total)
-            HTGPU_CUDA(cudaMemcpy(host.data(), fac.p, sizeof(double) * total, cudaMemcpyDeviceToHost));
-        long long dst = 0;
-        for (auto &L : lr_h) {
-            std::copy(host.begin() + L.u_off, host.begin() + L.u_off + (long long)L.m * L.r, uv + dst);
-            dst += (long long)L.m * L.r;
-            for (int j = 0; j < L.n; j++)
-                for (int k = 0; k < L.r; k++)
-                    uv[dst + k + (long long)L.r * j] = host[L.v_off + j + (long long)L.n * k];
-            dst += (long long)L.n * L.r;
+    std::vector<double> host(std::max<long long>(arena_len, 1));
+    if (arena_len)
+        HTGPU_CUDA(cudaMemcpy(host.data(), fac.p, sizeof(double) * arena_len, cudaMemcpyDeviceToHost));
+    std::vector<long long> u_at(lr_h.size()), v_at(lr_h.size()), d_at(dn_h.size());
+    long long o = 0;
+    for (std::size_t l = 0; l < lr_h.size(); l++) {
+        u_at[l] = o;
+        o += (long long)lr_h[l].m * lr_h[l].r;
+        v_at[l] = o;
+        o += (long long)lr_h[l].n * lr_h[l].r;
+    }
+    o = 0;
+    for (std::size_t d = 0; d < dn_h.size(); d++) {
+        d_at[d] = o;
+        o += (long long)dn_h[d].m * dn_h[d].n;
+    }
+    if (uv)
+        for (auto &it : p1_h) {
+            const LrLeaf &L = lr_h[it.leaf];
+            for (int k = 0; k < L.r; k++)
+                for (int jj = 0; jj < it.jlen; jj++)
+                    uv[v_at[it.leaf] + k + (long long)L.r * (it.j0 + jj)] = host[it.off + jj + (long long)it.jlen * k];
         }
-    }
-    if (dn && !dn_h.empty()) {
-        long long dtot = 0;
-        for (auto &D : dn_h)
-            dtot += (long long)D.m * D.n;
-        HTGPU_CUDA(cudaMemcpy(dn, dense.p, sizeof(double) * dtot, cudaMemcpyDeviceToHost));
-    }
+    for (auto &it : p2_h)
+        for (int c = it.cbeg; c < it.cend; c++) {
+            const int leaf = c_leaf[c];
+            const P2Contrib &pc = c_h[c];
+            if (leaf >= 0 && uv) {
+                const LrLeaf &L = lr_h[leaf];
+                for (int k = 0; k < L.r; k++)
+                    for (int i = 0; i < it.h; i++)
+                        uv[u_at[leaf] + (it.row0 - L.oi + i) + (long long)L.m * k] = host[pc.off + i + (long long)it.h * k];
+            } else if (leaf < 0 && dn) {
+                const DenseLeaf &D = dn_h[~leaf];
+                for (int j = 0; j < D.n; j++)
+                    for (int i = 0; i < it.h; i++)
+                        dn[d_at[~leaf] + (it.row0 - D.oi + i) + (long long)D.m * j] = host[pc.off + i + (long long)it.h * j];
+            }
+        }
 }
 
 long long HMatrix::stored_bytes() const {
@@ -626,6 +804,7 @@ long long HMatrix::product_bytes(int mu) const { return stored_bytes() + 8LL * m
 // HMatrix::ComputeInfos keys (hmatrix.hpp:739-841) for one rank, plus
 // GPU assembly counters
 std::map<std::string, std::string> HMatrix::infos() const {
+
     std::map<std::string, std::string> m;
     const std::size_t big = (std::size_t)std::max(nr, nc);
     std::size_t dmax = 0, dmin = big, lmax = 0, lmin = big, rmax = 0, rmin = big;
@@ -700,6 +879,9 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["GPU_phase1_items"]         = inum((long long)p1_h.size());
     m["GPU_phase2_items"]         = inum((long long)p2_h.size());
     m["GPU_phase2_contributions"] = inum((long long)c_h.size());
+    m["GPU_fp64_emulation_allowed"] = emu_ok_ ? "1" : "0";
+    m["GPU_fp64_phase1_dfma_permille"] = inum(emu_ok_ ? p1_permille_ : 1000);
+    m["GPU_fp64_phase2_dfma_warps"]    = inum(emu_ok_ ? p2_n64_ : kP2WarpsHost);
     return m;
 }
 

@@ -54,8 +54,25 @@ class HMatrix {
 
     BlockTreeParams bp;
 
+    // FP64 product configuration: share (per mille) of phase-1 elements on
+    // the FP64 pipe, number of phase-2 warps (of 4) on the FP64 pipe; the
+    // rest runs the FP32-pipe emulation.  emulation_allowed() is false when
+    // stored entries are too large for it (then everything uses DFMA).
+    void set_fp64_split(int phase1_dfma_permille, int phase2_dfma_warps);
+    void get_fp64_split(int *phase1_dfma_permille, int *phase2_dfma_warps) const;
+    bool emulation_allowed() const { return emu_ok_; }
+    // time every candidate split on the current H-matrix and keep the fastest
+    void autotune_fp64(int mu, int reps, float *best_ms);
+
   private:
-    void plan();
+    // where a leaf's factors sit before the final layout: U (m x r, ld m) at
+    // su and Vt (n x r, ld n) at sv of buffer buf; dense D (m x n, ld m) at sd
+    struct LeafSrc {
+        int buf;
+        long long su, sv;
+    };
+    void finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs);
+    void assign_phase1_modes();
     void ensure_work(int mu);
 
     std::shared_ptr<const ClusterTree> T, S;
@@ -69,16 +86,28 @@ class HMatrix {
     std::vector<P1Item> p1_h;
     std::vector<P2Item> p2_h;
     std::vector<P2Contrib> c_h;
-    long long a_slots = 0;
+    std::vector<int> c_leaf; // per contribution: low-rank leaf l, or ~d for dense leaf d
+    long long a_slots = 0, arena_len = 0;
 
     DevBuf<int> perm_t, perm_s;
-    DevBuf<double> fac, dense;
+    DevBuf<double> fac; // every factor and dense block, in work-item order
     DevBuf<LrLeaf> lr_d;
-    DevBuf<DenseLeaf> dn_d;
     DevBuf<P1Item> p1_d;
     DevBuf<P2Item> p2_d;
     DevBuf<P2Contrib> c_d;
     DevBuf<double> xp, A, xstage, ystage;
+    DevBuf<F2> xs;
+    DevBuf<int> xexp, multi_d;
+    std::vector<int> multi_h;
+    int p1_permille_ = 300, p2_n64_ = 1;
+    bool emu_ok_ = false;
+    void launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st);
+    void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A);
+    void upload_phase1_lists();
+    DevBuf<P1Item> p1e_d; // phase-1 tiles on the emulation (p1_d: on DFMA)
+    int n_p1_dfma_ = 0, n_p1_emu_ = 0;
+    cudaStream_t aux_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
     int mu_cap = 0;
     int launches_ = 0;
     BuildStats st_;

@@ -82,27 +82,41 @@ struct KernelDesc {
 
 struct LrLeaf { // low-rank leaf: y[oi:oi+m] += U (Vt^T x[oj:oj+n])
     int oi, oj, m, n, r;
-    int nch;            // phase-1 column chunks
-    long long u_off;    // U: m x r, column-major, ld = m   (elements)
-    long long v_off;    // Vt: n x r, column-major, ld = n  (elements)
-    long long a_off;    // first slot of the phase-1 sums Vt^T x: slots [nch][r], mu values each
+    int nch;         // phase-1 tiles (<= 256 source rows each)
+    long long a_off; // first slot of the phase-1 sums Vt^T x: slots [nch][r], mu values each
 };
 
 struct DenseLeaf {
     int oi, oj, m, n;
-    long long d_off; // m x n, column-major
 };
 
-struct P1Item { // one warp: rows j0 .. j0+jlen of Vt for one leaf
+struct P1Item { // one warp: Vt tile block (jlen x r, column-major, ld jlen) at off
+    long long off;
     int leaf, chunk, j0, jlen;
+    int pad;
 };
 
-struct P2Item { // one warp: target rows row0 .. row0+h, contributions [cbeg, cend)
+struct P2Item { // one CTA: target rows row0 .. row0+h, contributions [cbeg, cend)
     int row0, h, cbeg, cend;
 };
 
-struct P2Contrib { // leaf >= 0: low-rank leaf; leaf < 0: dense leaf ~leaf
-    int leaf, rowoff;
+struct P2Contrib { // block h x w (column-major, ld h) at off; aux >= 0: low-rank
+    long long off; // leaf, coefficients in phase-1 slots aux ..; aux < 0: dense,
+    int w, aux;    // coefficients x[~aux ...]
+};
+
+struct BlockCopy { // rows x cols, column-major ld_src at src -> contiguous at dst
+    long long src, dst;
+    int rows, cols, ld_src, pad;
+};
+
+struct DenseChunk { // dense rows row0 .. row0+h (cluster numbering) x columns oj .. oj+n
+    long long dst;
+    int row0, h, oj, n;
+};
+
+struct F2 { // a double split into an unevaluated float sum hi + lo (df64.cuh)
+    float hi, lo;
 };
 
 // ---------------------------------------------------------------------------

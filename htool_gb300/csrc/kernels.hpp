@@ -28,18 +28,19 @@ struct PackItem {
 // copy the first r columns of scratch U (ld M) and Vt (ld N) to the arena
 void launch_pack_factors(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st);
 
-// D[i + m j] = G(perm_t[oi + i], perm_s[oj + j]) for every dense leaf
-void launch_dense_fill(const DenseLeaf *leaves, int nleaves, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st);
+// D[dst + i + h j] = G(perm_t[row0 + i], perm_s[oj + j]) for every chunk
+void launch_dense_fill(const DenseChunk *chunks, int nchunks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st);
 
-// ---- product ----------------------------------------------------------------
-// xp[j * mu + c] = x[c * ldx + perm[j]] (perm may be null: identity)
-void launch_gather(const double *x, int ldx, const int *perm, int n, int mu, double *xp, cudaStream_t st);
+// ---- product (FP64 storage; DFMA or FP32-pipe emulation, df64.cuh) ---------
+constexpr int kEmuBit = 1 << 30; // P1Item::chunk flag: tile uses the emulation
 
-// phase 1: A[a_off + (chunk * r + k) * mu + c] = sum_j Vt[j, k] xp[(oj + j) * mu + c]
-void launch_phase1(const P1Item *items, int nitems, const LrLeaf *lr, const double *factors, const double *xp, int mu, double *A, cudaStream_t st);
-
-// phase 2: y[c * ldy + perm[i]] = sum over contributions of row i
-void launch_phase2(const P2Item *items, int nitems, const P2Contrib *contrib, const LrLeaf *lr, const DenseLeaf *dn, const double *factors, const double *dense, const double *A,
-                   const double *xp, int mu, const int *perm, double *y, int ldy, cudaStream_t st);
+int rhs_groups(int mu); // launches per phase for mu right-hand sides
+void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st);
+void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st);
+void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
+void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st);
+void launch_phase2(const P2Item *items, int nitems, const P2Contrib *contrib, const LrLeaf *lr, const double *factors, const double *A, const double *xp, const F2 *xs, const int *xexp, int n64,
+                   int mu, const int *perm, double *y, int ldy, cudaStream_t st);
+void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st);
 
 } // namespace htgpu

@@ -1,239 +1,452 @@
-// H-matrix product kernels (FP64).
+// H-matrix product kernels (FP64 storage, FP64-accurate arithmetic).
 //
-// htool applies every leaf with BLAS gemv/gemm and sums per-thread copies
-// of the output (hmatrix.hpp:844-911).  Here the product is three launches:
+// htool applies every leaf with BLAS gemv/gemm and sums per-thread copies of
+// the output (include/htool/types/hmatrix.hpp:844-911).  Here one product is
 //
-//   gather   xp = x[perm_s] (row-major, mu values per point)
-//   phase 1  for every low-rank leaf: a = Vt^T xp -- one warp per tile of
-//            <= 256 source rows (all rank columns), one fma per stored
-//            element, a butterfly reduce-scatter per 16 columns; partial
-//            sums per tile
-//   phase 2  for every chunk of <= 32 target rows: the sum over every leaf
-//            covering those rows of U a (low-rank, a = sum of the tiles'
-//            partial sums) or D xp (dense), then y[perm_t[i]] = sum.  Each
-//            output row is owned by exactly one CTA and reduced in a fixed
-//            order, so the product is deterministic and needs no atomics.
+//   xexp      largest exponent of |x| (for the emulated path's scaling)
+//   gather    xp = x[perm_s] (row-major, mu values per point) and its
+//             hi/lo float split xs, scaled by 2^-xexp
+//   phase 1   for every low-rank leaf and tile of <= 256 source rows:
+//             partial sums of Vt^T xp -- one warp per tile
+//   tiles     sum of the partials of multi-tile leaves
+//   phase 2   for every chunk of <= 32 target rows: the sum over every leaf
+//             covering those rows of U a (low-rank) or D xp (dense), stored
+//             to y[perm_t[i]].  Each row is written once by one CTA after a
+//             fixed-order reduction: the product is deterministic and uses
+//             no atomics.
 //
-// Stored factors are read exactly once per product (U, Vt, D column-major:
-// every warp load is a contiguous run of rows of one column).
+// Storage (built by HMatrix::finalize_layout): every work item reads ONE
+// contiguous 16-byte-aligned block -- a phase-1 tile of Vt (jlen x r,
+// column-major, ld jlen) or a phase-2 chunk of U or of a dense block (h x w,
+// column-major, ld h).  Loads are fully coalesced, and a single
+// cp.async.bulk.prefetch.L2 (TMA) pulls the next item's block into L2 while
+// the current one is computed.
+//
+// Every multiply-add runs either on the FP64 pipe (DFMA) or on the FP32/INT
+// pipes through the exact double-float emulation of df64.cuh; P1Item flags
+// and the phase-2 warp index choose, HMatrix::autotune_fp64 picks the split.
+#include "df64.cuh"
 #include "kernels.hpp"
 
 namespace htgpu {
 
 namespace {
 
-constexpr int kWarpsPerBlock = 8;
+constexpr int kWarpsPerBlock = 8; // phase 1: warps per CTA
+constexpr int kP2Warps       = 4; // phase 2: warps sharing one row chunk
 
-__global__ void gather_kernel(const double *__restrict__ x, int ldx, const int *__restrict__ perm, int n, int mu, double *__restrict__ xp) {
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+    // TMA bulk prefetch of a contiguous, 16-byte-aligned range into L2
+    bytes = (bytes + 15u) & ~15u;
+    if (bytes)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// biased exponent of max |x| over the input (atomicMax on the exponent field)
+__global__ void xexp_kernel(const double *__restrict__ x, long long total, int *__restrict__ xexp) {
+    int m = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int ex = (int)(((unsigned)__double2hiint(x[e]) >> 20) & 0x7FFu);
+        m            = max(m, ex == 0x7FF ? 0 : ex);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0)
+        atomicMax(xexp, m);
+}
+
+// xp[j*mu + c] = x[c*ldx + perm[j]] and xs = split(xp * 2^(1023 - xexp))
+__global__ void gather_split_kernel(const double *__restrict__ x, int ldx, const int *__restrict__ perm, int n, int mu, const int *__restrict__ xexp, double *__restrict__ xp, F2 *__restrict__ xs) {
     const long long total = (long long)n * mu;
+    const int shift       = 1023 - max(*xexp, 1);
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
         int j = (int)(e / mu), c = (int)(e % mu);
-        int src = perm ? perm[j] : j;
-        xp[e]   = x[(long long)c * ldx + src];
+        int src        = perm ? perm[j] : j;
+        const double v = x[(long long)c * ldx + src];
+        xp[e]          = v;
+        const int ex   = (int)(((unsigned)__double2hiint(v) >> 20) & 0x7FFu);
+        xs[e]          = (ex == 0 || ex + shift < 1) ? F2{0.f, 0.f} : split64(scale_pow2(v, shift));
     }
 }
 
-// Reduce-scatter of 16 per-lane values over the warp: afterwards lanes
-// 2q and 2q+1 both hold the warp-wide sum of value index
-// vidx(lane) = 8*b4 + 4*b3 + 2*b2 + b1 (b = bits of the lane id).  16
-// shuffles instead of 16 * 5 for separate reductions; fixed order, so the
-// result is deterministic.
-__device__ __forceinline__ void reduce_scatter16(double (&v)[16], int lane) {
+// Reduce-scatter of 16 per-lane values over the warp: afterwards lanes 2q
+// and 2q+1 both hold the warp-wide sum of value vidx(lane) = 8*b4 + 4*b3 +
+// 2*b2 + b1 (bits of the lane id) -- 16 shuffles instead of 80; fixed order.
+template <typename T, typename Add, typename Shfl>
+__device__ __forceinline__ void reduce_scatter16(T (&v)[16], int lane, Add add, Shfl shfl) {
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const bool hi = lane & 16;
-        double keep = hi ? v[i + 8] : v[i], send = hi ? v[i] : v[i + 8];
-        v[i]        = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        T keep = hi ? v[i + 8] : v[i], send = hi ? v[i] : v[i + 8];
+        v[i] = add(keep, shfl(send, 16));
     }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const bool hi = lane & 8;
-        double keep = hi ? v[i + 4] : v[i], send = hi ? v[i] : v[i + 4];
-        v[i]        = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        T keep = hi ? v[i + 4] : v[i], send = hi ? v[i] : v[i + 4];
+        v[i] = add(keep, shfl(send, 8));
     }
 #pragma unroll
     for (int i = 0; i < 2; i++) {
         const bool hi = lane & 4;
-        double keep = hi ? v[i + 2] : v[i], send = hi ? v[i] : v[i + 2];
-        v[i]        = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+        T keep = hi ? v[i + 2] : v[i], send = hi ? v[i] : v[i + 2];
+        v[i] = add(keep, shfl(send, 4));
     }
     {
         const bool hi = lane & 2;
-        double keep = hi ? v[1] : v[0], send = hi ? v[0] : v[1];
-        v[0]        = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+        T keep = hi ? v[1] : v[0], send = hi ? v[0] : v[1];
+        v[0] = add(keep, shfl(send, 2));
     }
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    v[0] = add(v[0], shfl(v[0], 1));
 }
 
 __device__ __forceinline__ int rs16_index(int lane) { return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1); }
 
-// Phase 1: one warp per tile of <= kTileRows source rows of one leaf.
-// The tile's x values sit in registers; the 16 accumulators hold
-// KG = 16 / MU columns x MU right-hand sides; each column load is 32
-// consecutive doubles (one 256-byte request per warp).
+struct AddD {
+    __device__ double operator()(double a, double b) const { return a + b; }
+};
+struct ShflD {
+    __device__ double operator()(double v, int o) const { return __shfl_xor_sync(0xffffffffu, v, o); }
+};
+struct AddDF {
+    __device__ DF operator()(DF a, DF b) const { return df_add(a, b); }
+};
+struct ShflDF {
+    __device__ DF operator()(DF v, int o) const {
+        DF r;
+        r.s = __shfl_xor_sync(0xffffffffu, v.s, o);
+        r.c = __shfl_xor_sync(0xffffffffu, v.c, o);
+        return r;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// phase 1: warps loop over tiles w, w + W, ... (W = all warps of the grid)
+// ---------------------------------------------------------------------------
+// DFMA tile: KG = 16 / MU columns per accumulator group, RPL rows per lane;
+// the next column's values are loaded while the current one is used
+// (register double buffering), so every warp keeps 2 * RPL loads in flight
 template <int MU>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) phase1_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const double *__restrict__ fac,
-                                                                      const double *__restrict__ xp, int mu, int c0, double *__restrict__ A) {
-    constexpr int KG  = 16 / MU;     // columns per accumulator group
-    constexpr int RPL = 8 / MU > 0 ? 8 / MU : 1; // rows per lane per sub-tile
-    const int w       = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    const int lane    = threadIdx.x & 31;
-    if (w >= nitems)
-        return;
-    const P1Item it = items[w];
-    const LrLeaf L  = lr[it.leaf];
-    const double *V = fac + L.v_off + it.j0;
-    const double *X = xp + (long long)(L.oj + it.j0) * mu + c0;
-    double *out     = A + (L.a_off + (long long)it.chunk * L.r) * mu + c0;
-    const int jlen  = it.jlen;
-    const int vi    = rs16_index(lane);
+__device__ __forceinline__ void phase1_tile_dfma(const P1Item &it, const LrLeaf &L, const double *__restrict__ fac, const double *__restrict__ xp, int mu, int c0, double *__restrict__ out, int lane) {
+    constexpr int KG  = 16 / MU;
+    constexpr int RPL = 8 / MU > 0 ? 8 / MU : 1;
+    const double *V   = fac + it.off;
+    const double *X   = xp + (long long)(L.oj + it.j0) * mu + c0;
+    const int jlen    = it.jlen;
+    const int vi      = rs16_index(lane);
+    for (int s0 = 0; s0 < jlen; s0 += 32 * RPL) {
+        double xv[RPL][MU];
+#pragma unroll
+        for (int t = 0; t < RPL; t++) {
+            const int jj = s0 + lane + 32 * t;
+#pragma unroll
+            for (int c = 0; c < MU; c++)
+                xv[t][c] = jj < jlen ? X[(long long)jj * mu + c] : 0.;
+        }
+        int ng = 0; // row groups of 32 with at least one live row (warp-uniform)
+#pragma unroll
+        for (int t = 0; t < RPL; t++)
+            ng += (s0 + 32 * t < jlen) ? 1 : 0;
+        double cur[RPL], nxt[RPL];
+#pragma unroll
+        for (int t = 0; t < RPL; t++) {
+            const int jj = s0 + lane + 32 * t;
+            cur[t]       = jj < jlen ? V[jj] : 0.;
+        }
+        for (int kg = 0; kg < L.r; kg += KG) {
+            double acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+                acc[q] = 0.;
+#pragma unroll
+            for (int kk = 0; kk < KG; kk++) {
+                const int k = kg + kk;
+                if (k < L.r) {
+                    const double *Vn = V + (long long)jlen * (k + 1);
+#pragma unroll
+                    for (int t = 0; t < RPL; t++) {
+                        const int jj = s0 + lane + 32 * t;
+                        nxt[t]       = (k + 1 < L.r && jj < jlen) ? Vn[jj] : 0.;
+                    }
+#pragma unroll
+                    for (int t = 0; t < RPL; t++)
+                        if (t < ng)
+#pragma unroll
+                            for (int c = 0; c < MU; c++)
+                                acc[kk * MU + c] = fma(cur[t], xv[t][c], acc[kk * MU + c]);
+#pragma unroll
+                    for (int t = 0; t < RPL; t++)
+                        cur[t] = nxt[t];
+                }
+            }
+            reduce_scatter16(acc, lane, AddD(), ShflD());
+            const int kk = vi / MU, c = vi % MU;
+            // tiles of more than 32 * RPL rows add their row groups in order
+            if ((lane & 1) == 0 && kg + kk < L.r) {
+                double *o = out + (long long)(kg + kk) * mu + c;
+                *o        = s0 == 0 ? acc[0] : *o + acc[0];
+            }
+        }
+    }
+}
+
+template <int MU>
+__device__ __forceinline__ void phase1_tile_emu(const P1Item &it, const LrLeaf &L, const double *__restrict__ fac, const F2 *__restrict__ xs, int shift, int mu, int c0, double *__restrict__ out, int lane) {
+    constexpr int KG  = 16 / MU;
+    constexpr int RPL = 4 / MU > 0 ? 4 / MU : 1;
+    const double *V   = fac + it.off;
+    const F2 *X       = xs + (long long)(L.oj + it.j0) * mu + c0;
+    const int jlen    = it.jlen;
+    const int vi      = rs16_index(lane);
     for (int kg = 0; kg < L.r; kg += KG) {
-        double acc[16];
+        DF acc[16];
 #pragma unroll
         for (int q = 0; q < 16; q++)
-            acc[q] = 0.;
+            df_zero(acc[q]);
         for (int s0 = 0; s0 < jlen; s0 += 32 * RPL) {
-            double xv[RPL][MU];
+            F2 xv[RPL][MU];
 #pragma unroll
             for (int t = 0; t < RPL; t++) {
                 const int jj = s0 + lane + 32 * t;
 #pragma unroll
                 for (int c = 0; c < MU; c++)
-                    xv[t][c] = jj < jlen ? X[(long long)jj * mu + c] : 0.;
+                    xv[t][c] = jj < jlen ? X[(long long)jj * mu + c] : F2{0.f, 0.f};
             }
 #pragma unroll
             for (int kk = 0; kk < KG; kk++) {
                 if (kg + kk < L.r) {
-                    const double *Vk = V + (long long)L.n * (kg + kk);
+                    const double *Vk = V + (long long)jlen * (kg + kk);
+                    double v[RPL];
 #pragma unroll
                     for (int t = 0; t < RPL; t++) {
                         const int jj = s0 + lane + 32 * t;
-                        if (jj < jlen) {
-                            const double v = Vk[jj];
+                        v[t]         = jj < jlen ? Vk[jj] : 0.;
+                    }
+#pragma unroll
+                    for (int t = 0; t < RPL; t++) {
+                        if (s0 + 32 * t < jlen) { // warp-uniform
+                            const F2 a = split64(v[t]);
 #pragma unroll
                             for (int c = 0; c < MU; c++)
-                                acc[kk * MU + c] = fma(v, xv[t][c], acc[kk * MU + c]);
+                                df_fma(acc[kk * MU + c], a, xv[t][c]);
                         }
                     }
                 }
             }
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+                df_renorm(acc[q]);
         }
-        reduce_scatter16(acc, lane);
+        reduce_scatter16(acc, lane, AddDF(), ShflDF());
         const int kk = vi / MU, c = vi % MU;
         if ((lane & 1) == 0 && kg + kk < L.r)
-            out[(long long)(kg + kk) * mu + c] = acc[0];
+            out[(long long)(kg + kk) * mu + c] = scale_pow2(df_to_double(acc[0]), shift);
     }
 }
 
-constexpr int kP2Warps = 4; // warps sharing one phase-2 row chunk
+// one warp per tile, tiles w, w + W, ... (W = all warps of the grid)
+template <int MU, bool EMU>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, EMU ? 3 : 2) phase1_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const double *__restrict__ fac,
+                                                                      const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0,
+                                                                      double *__restrict__ A) {
+    const int lane  = threadIdx.x & 31;
+    const int W     = gridDim.x * kWarpsPerBlock;
+    const int shift = max(*xexp, 1) - 1023; // A holds unscaled sums
+    for (int w = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); w < nitems; w += W) {
+        const P1Item it = items[w];
+        const LrLeaf L  = lr[it.leaf];
+        const int ch    = it.chunk & ~kEmuBit;
+        double *out     = A + (L.a_off + (long long)ch * L.r) * mu + c0;
+        if (EMU)
+            phase1_tile_emu<MU>(it, L, fac, xs, shift, mu, c0, out, lane);
+        else
+            phase1_tile_dfma<MU>(it, L, fac, xp, mu, c0, out, lane);
+    }
+}
 
-// Phase 2: one CTA of kP2Warps warps per chunk of h <= 32 target rows.  Lane
-// -> (row = lane % h, slice = lane / h), S = 32 / h column slices; warp w
-// takes contributions w, w + kP2Warps, ...  Slices, then warps, are summed
-// in a fixed order; the CTA writes every row once.
+// sum the phase-1 tile partials of every multi-tile leaf into tile 0
+__global__ void reduce_tiles_kernel(const LrLeaf *__restrict__ lr, const int *__restrict__ multi, int nmulti, int mu, double *__restrict__ A) {
+    const int b = blockIdx.x;
+    if (b >= nmulti)
+        return;
+    const LrLeaf L       = lr[multi[b]];
+    const long long span = (long long)L.r * mu;
+    double *base         = A + L.a_off * mu;
+    for (long long e = threadIdx.x; e < span; e += blockDim.x) {
+        double s = base[e];
+        for (int ch = 1; ch < L.nch; ch++)
+            s += base[ch * span + e];
+        base[e] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// phase 2: CTAs of kP2Warps warps loop over row chunks; lane -> (row =
+// lane % h, slice = lane / h), S = 32 / h slices; warp w takes
+// contributions w, w + kP2Warps, ... (the next descriptor is loaded and the
+// next block prefetched into L2 while the current one is processed);
+// warps w < n64 use DFMA
+// ---------------------------------------------------------------------------
 template <int MU>
 __global__ void __launch_bounds__(32 * kP2Warps) phase2_kernel(const P2Item *__restrict__ items, int nitems, const P2Contrib *__restrict__ contrib, const LrLeaf *__restrict__ lr,
-                                                                const DenseLeaf *__restrict__ dn, const double *__restrict__ fac, const double *__restrict__ dense,
-                                                                const double *__restrict__ A, const double *__restrict__ xp, int mu, int c0, const int *__restrict__ perm,
-                                                                double *__restrict__ y, int ldy) {
+                                                                const double *__restrict__ fac, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
+                                                                const int *__restrict__ xexp, int n64, int mu, int c0, const int *__restrict__ perm, double *__restrict__ y, int ldy) {
     __shared__ double red[kP2Warps][32][MU];
     const int wid  = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const P2Item it = items[blockIdx.x];
-    const int h     = it.h;
-    const int S     = 32 / h;
-    const int row   = lane % h;
-    const int slice = lane / h;
-    const bool live = slice < S;
-    double acc[MU];
+    const int xe   = max(*xexp, 1);
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const P2Item it = items[item];
+        const int h     = it.h;
+        const int S     = 32 / h;
+        const int row   = lane % h;
+        const int slice = lane / h;
+        const bool live = slice < S;
+        double outv[MU];
+        if (wid < n64) {
+            double acc[MU];
 #pragma unroll
-    for (int c = 0; c < MU; c++)
-        acc[c] = 0.;
-
-    for (int ci = it.cbeg + wid; ci < it.cend; ci += kP2Warps) {
-        const P2Contrib pc = contrib[ci];
-        if (pc.leaf >= 0) {
-            const LrLeaf L   = lr[pc.leaf];
-            const double *U  = fac + L.u_off + pc.rowoff + row;
-            const double *Ab = A + L.a_off * mu + c0;
-            const long long chstride = (long long)L.r * mu;
-            for (int kb = 0; kb < L.r; kb += 32) {
-                const int kc = min(32, L.r - kb);
-                double a[MU];
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    a[c] = 0.;
-                if (lane < kc) {
-                    const double *ap = Ab + (long long)(kb + lane) * mu;
-                    for (int ch = 0; ch < L.nch; ch++)
+            for (int c = 0; c < MU; c++)
+                acc[c] = 0.;
+            P2Contrib nxt = it.cbeg + wid < it.cend ? contrib[it.cbeg + wid] : P2Contrib{0, 0, 0};
+            for (int ci = it.cbeg + wid; ci < it.cend; ci += kP2Warps) {
+                const P2Contrib pc = nxt;
+                if (ci + kP2Warps < it.cend) { // next descriptor and block on their way
+                    nxt = contrib[ci + kP2Warps];
+                    if (lane == 0)
+                        prefetch_l2(fac + nxt.off, (unsigned)((long long)h * nxt.w * 8));
+                }
+                const double *B = fac + pc.off + row;
+                for (int kb = 0; kb < pc.w; kb += 32) {
+                    const int kc = min(32, pc.w - kb);
+                    double a[MU];
+                    if (pc.aux >= 0) { // low-rank: a_k from phase 1, slot pc.aux
+                        const double *Ab = A + (long long)pc.aux * mu + c0;
 #pragma unroll
                         for (int c = 0; c < MU; c++)
-                            a[c] += ap[ch * chstride + c];
-                }
-#pragma unroll 8
-                for (int k0 = 0; k0 < kc; k0 += S) {
-                    const int k   = k0 + slice;
-                    const bool ok = live && k < kc;
-                    const double u = ok ? U[(long long)L.m * (kb + k)] : 0.;
+                            a[c] = lane < kc ? Ab[(long long)(kb + lane) * mu + c] : 0.;
+                    } else { // dense: x
+                        const double *X = xp + (long long)(~pc.aux) * mu + c0;
 #pragma unroll
-                    for (int c = 0; c < MU; c++) {
-                        const double ak = __shfl_sync(0xffffffffu, a[c], ok ? k : 0);
-                        acc[c]          = fma(u, ak, acc[c]);
+                        for (int c = 0; c < MU; c++)
+                            a[c] = lane < kc ? X[(long long)(kb + lane) * mu + c] : 0.;
+                    }
+#pragma unroll 8
+                    for (int k0 = 0; k0 < kc; k0 += S) {
+                        const int k    = k0 + slice;
+                        const bool ok  = live && k < kc;
+                        const double u = ok ? B[(long long)h * (kb + k)] : 0.;
+#pragma unroll
+                        for (int c = 0; c < MU; c++)
+                            acc[c] = fma(u, __shfl_sync(0xffffffffu, a[c], ok ? k : 0), acc[c]);
                     }
                 }
             }
+            for (int s = 1; s < S; s++)
+#pragma unroll
+                for (int c = 0; c < MU; c++) {
+                    const int src   = lane + s * h;
+                    const double vv = __shfl_sync(0xffffffffu, acc[c], src < 32 ? src : lane);
+                    if (slice == 0)
+                        acc[c] += vv;
+                }
+#pragma unroll
+            for (int c = 0; c < MU; c++)
+                outv[c] = acc[c];
         } else {
-            const DenseLeaf D = dn[~pc.leaf];
-            const double *Dp  = dense + D.d_off + pc.rowoff + row;
-            const double *X   = xp + (long long)D.oj * mu + c0;
-            for (int jb = 0; jb < D.n; jb += 32) {
-                const int jc = min(32, D.n - jb);
-                double xv[MU];
+            DF acc[MU];
+#pragma unroll
+            for (int c = 0; c < MU; c++)
+                df_zero(acc[c]);
+            P2Contrib nxt = it.cbeg + wid < it.cend ? contrib[it.cbeg + wid] : P2Contrib{0, 0, 0};
+            for (int ci = it.cbeg + wid; ci < it.cend; ci += kP2Warps) {
+                const P2Contrib pc = nxt;
+                if (ci + kP2Warps < it.cend) {
+                    nxt = contrib[ci + kP2Warps];
+                    if (lane == 0)
+                        prefetch_l2(fac + nxt.off, (unsigned)((long long)h * nxt.w * 8));
+                }
+                const double *B = fac + pc.off + row;
+                for (int kb = 0; kb < pc.w; kb += 32) {
+                    const int kc = min(32, pc.w - kb);
+                    F2 a[MU];
+                    if (pc.aux >= 0) { // a_k, scaled to the units of x
+                        const double *Ab = A + (long long)pc.aux * mu + c0;
+#pragma unroll
+                        for (int c = 0; c < MU; c++) {
+                            const double av = lane < kc ? Ab[(long long)(kb + lane) * mu + c] : 0.;
+                            const int ex    = (int)(((unsigned)__double2hiint(av) >> 20) & 0x7FFu);
+                            a[c]            = (ex == 0 || ex + 1023 - xe < 1) ? F2{0.f, 0.f} : split64(scale_pow2(av, 1023 - xe));
+                        }
+                    } else {
+                        const F2 *X = xs + (long long)(~pc.aux) * mu + c0;
+#pragma unroll
+                        for (int c = 0; c < MU; c++)
+                            a[c] = lane < kc ? X[(long long)(kb + lane) * mu + c] : F2{0.f, 0.f};
+                    }
+#pragma unroll 8
+                    for (int k0 = 0; k0 < kc; k0 += S) {
+                        const int k   = k0 + slice;
+                        const bool ok = live && k < kc;
+                        const F2 u    = split64(ok ? B[(long long)h * (kb + k)] : 0.);
+#pragma unroll
+                        for (int c = 0; c < MU; c++) {
+                            F2 ak;
+                            ak.hi = __shfl_sync(0xffffffffu, a[c].hi, ok ? k : 0);
+                            ak.lo = __shfl_sync(0xffffffffu, a[c].lo, ok ? k : 0);
+                            df_fma(acc[c], u, ak);
+                        }
+                    }
+                }
 #pragma unroll
                 for (int c = 0; c < MU; c++)
-                    xv[c] = lane < jc ? X[(long long)(jb + lane) * mu + c] : 0.;
-#pragma unroll 8
-                for (int j0 = 0; j0 < jc; j0 += S) {
-                    const int j   = j0 + slice;
-                    const bool ok = live && j < jc;
-                    const double d = ok ? Dp[(long long)D.m * (jb + j)] : 0.;
+                    df_renorm(acc[c]);
+            }
+            for (int s = 1; s < S; s++)
 #pragma unroll
-                    for (int c = 0; c < MU; c++) {
-                        const double xj = __shfl_sync(0xffffffffu, xv[c], ok ? j : 0);
-                        acc[c]          = fma(d, xj, acc[c]);
-                    }
+                for (int c = 0; c < MU; c++) {
+                    const int src = lane + s * h;
+                    DF v;
+                    v.s = __shfl_sync(0xffffffffu, acc[c].s, src < 32 ? src : lane);
+                    v.c = __shfl_sync(0xffffffffu, acc[c].c, src < 32 ? src : lane);
+                    if (slice == 0)
+                        acc[c] = df_add(acc[c], v);
                 }
+#pragma unroll
+            for (int c = 0; c < MU; c++)
+                outv[c] = slice == 0 ? scale_pow2(df_to_double(acc[c]), xe - 1023) : 0.;
+        }
+        if (slice == 0)
+#pragma unroll
+            for (int c = 0; c < MU; c++)
+                red[wid][row][c] = outv[c];
+        __syncthreads();
+        if (wid == 0 && lane < h) {
+            const int i   = it.row0 + lane;
+            const int dst = perm ? perm[i] : i;
+#pragma unroll
+            for (int c = 0; c < MU; c++) {
+                double v = red[0][lane][c];
+                for (int q = 1; q < kP2Warps; q++)
+                    v += red[q][lane][c];
+                y[(long long)(c0 + c) * ldy + dst] = v;
             }
         }
-    }
-    // slices -> slice 0 (lanes row + s*h), in order
-    for (int s = 1; s < S; s++)
-#pragma unroll
-        for (int c = 0; c < MU; c++) {
-            const int src   = lane + s * h;
-            const double vv = __shfl_sync(0xffffffffu, acc[c], src < 32 ? src : lane);
-            if (slice == 0)
-                acc[c] += vv;
-        }
-    if (slice == 0)
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            red[wid][row][c] = acc[c];
-    __syncthreads();
-    if (wid == 0 && lane < h) {
-        const int i   = it.row0 + lane;
-        const int dst = perm ? perm[i] : i;
-#pragma unroll
-        for (int c = 0; c < MU; c++) {
-            double v = red[0][lane][c];
-            for (int q = 1; q < kP2Warps; q++)
-                v += red[q][lane][c];
-            y[(long long)(c0 + c) * ldy + dst] = v;
-        }
+        __syncthreads();
     }
 }
 
-inline int blocks_for(int nwarps) { return (nwarps + kWarpsPerBlock - 1) / kWarpsPerBlock; }
+// copy a rows x cols column-major block (leading dimension ld_src) into a
+// contiguous rows x cols block (leading dimension rows)
+__global__ void block_copy_kernel(const BlockCopy *__restrict__ items, const double *__restrict__ src, double *__restrict__ dst) {
+    const BlockCopy b   = items[blockIdx.x];
+    const long long tot = (long long)b.rows * b.cols;
+    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int i = (int)(e % b.rows), k = (int)(e / b.rows);
+        dst[b.dst + e] = src[b.src + i + (long long)b.ld_src * k];
+    }
+}
 
 // split mu right-hand sides into compile-time groups of 8, 4, 2, 1
 template <typename F>
@@ -247,44 +460,91 @@ void for_rhs_groups(int mu, F f) {
     }
 }
 
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0)
+            n = 152;
+    }
+    return n;
+}
+
 } // namespace
 
-void launch_gather(const double *x, int ldx, const int *perm, int n, int mu, double *xp, cudaStream_t st) {
-    long long total = (long long)n * mu;
+int rhs_groups(int mu) {
+    int g = 0;
+    for_rhs_groups(mu, [&](int, int) { g++; });
+    return g;
+}
+
+void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st) {
+    HTGPU_CUDA(cudaMemsetAsync(xexp, 0, sizeof(int), st));
     if (total <= 0)
         return;
-    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
-    gather_kernel<<<blocks, 256, 0, st>>>(x, ldx, perm, n, mu, xp);
+    int blocks = (int)std::min<long long>((total + 255) / 256, (long long)sm_count() * 8);
+    xexp_kernel<<<blocks, 256, 0, st>>>(x, total, xexp);
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_phase1(const P1Item *items, int nitems, const LrLeaf *lr, const double *factors, const double *xp, int mu, double *A, cudaStream_t st) {
+void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st) {
+    long long total = (long long)n * mu;
+    if (total <= 0)
+        return;
+    int blocks = (int)std::min<long long>((total + 255) / 256, (long long)sm_count() * 16);
+    gather_split_kernel<<<blocks, 256, 0, st>>>(x, ldx, perm, n, mu, xexp, xp, xs);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;
+    const int blocks = std::max(1, std::min((nitems + kWarpsPerBlock - 1) / kWarpsPerBlock, sm_count() * 8));
+    for_rhs_groups(mu, [&](int c0, int g) {
+#define HTGPU_P1(G)                                                                                                                             \
+    (emu ? phase1_kernel<G, true><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, xs, xexp, mu, c0, A)                 \
+         : phase1_kernel<G, false><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, xs, xexp, mu, c0, A))
+        switch (g) {
+        case 8: HTGPU_P1(8); break;
+        case 4: HTGPU_P1(4); break;
+        case 2: HTGPU_P1(2); break;
+        default: HTGPU_P1(1); break;
+        }
+#undef HTGPU_P1
+        HTGPU_CUDA(cudaGetLastError());
+    });
+}
+
+void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st) {
+    if (nmulti <= 0)
+        return;
+    reduce_tiles_kernel<<<nmulti, 128, 0, st>>>(lr, multi, nmulti, mu, A);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase2(const P2Item *items, int nitems, const P2Contrib *contrib, const LrLeaf *lr, const double *factors, const double *A, const double *xp, const F2 *xs, const int *xexp, int n64,
+                   int mu, const int *perm, double *y, int ldy, cudaStream_t st) {
+    if (nitems <= 0)
+        return;
+    const int blocks = std::max(1, std::min(nitems, sm_count() * 16));
     for_rhs_groups(mu, [&](int c0, int g) {
         switch (g) {
-        case 8: phase1_kernel<8><<<blocks_for(nitems), 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, mu, c0, A); break;
-        case 4: phase1_kernel<4><<<blocks_for(nitems), 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, mu, c0, A); break;
-        case 2: phase1_kernel<2><<<blocks_for(nitems), 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, mu, c0, A); break;
-        default: phase1_kernel<1><<<blocks_for(nitems), 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, mu, c0, A); break;
+        case 8: phase2_kernel<8><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
+        case 4: phase2_kernel<4><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
+        case 2: phase2_kernel<2><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
+        default: phase2_kernel<1><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
         }
         HTGPU_CUDA(cudaGetLastError());
     });
 }
 
-void launch_phase2(const P2Item *items, int nitems, const P2Contrib *contrib, const LrLeaf *lr, const DenseLeaf *dn, const double *factors, const double *dense, const double *A,
-                   const double *xp, int mu, const int *perm, double *y, int ldy, cudaStream_t st) {
+void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st) {
     if (nitems <= 0)
         return;
-    for_rhs_groups(mu, [&](int c0, int g) {
-        switch (g) {
-        case 8: phase2_kernel<8><<<nitems, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, dn, factors, dense, A, xp, mu, c0, perm, y, ldy); break;
-        case 4: phase2_kernel<4><<<nitems, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, dn, factors, dense, A, xp, mu, c0, perm, y, ldy); break;
-        case 2: phase2_kernel<2><<<nitems, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, dn, factors, dense, A, xp, mu, c0, perm, y, ldy); break;
-        default: phase2_kernel<1><<<nitems, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, dn, factors, dense, A, xp, mu, c0, perm, y, ldy); break;
-        }
-        HTGPU_CUDA(cudaGetLastError());
-    });
+    block_copy_kernel<<<nitems, 128, 0, st>>>(items, src, dst);
+    HTGPU_CUDA(cudaGetLastError());
 }
 
 } // namespace htgpu

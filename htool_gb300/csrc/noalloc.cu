@@ -17,8 +17,9 @@
 namespace htgpu {
 
 // 16 MiB of working memory per device, held by every GPU that loads the
-// library until the process exits.  A product needs nb_cols * mu doubles
-// for the gathered input plus (phase-1 partial-sum slots) * mu doubles.
+// library until the process exits.  A product needs 2 * nb_cols * mu
+// doubles for the gathered input and its float split, one slot for the
+// input's exponent, plus (phase-1 partial-sum slots) * mu doubles.
 constexpr std::size_t kNoAllocScratchDoubles = 2u * 1024u * 1024u;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
@@ -46,9 +47,10 @@ double *scratch_on(int device) {
 } // namespace
 
 std::size_t HMatrix::noalloc_scratch_need(int mu) const {
-    // gathered input, rounded up to 32 doubles (256 bytes), then the partial sums
+    // gathered input and its split, each rounded up to 32 doubles (256
+    // bytes), 32 doubles for the exponent word, then the partial sums
     const std::size_t xp_len = ((std::size_t)nc * mu + 31) / 32 * 32;
-    return xp_len + (std::size_t)std::max<long long>(a_slots, 1) * mu;
+    return 2 * xp_len + 32 + (std::size_t)std::max<long long>(a_slots, 1) * mu;
 }
 
 void HMatrix::mvprod_noalloc(const double *in, double *out, int mu, cudaStream_t st) {
@@ -65,15 +67,15 @@ void HMatrix::mvprod_noalloc(const double *in, double *out, int mu, cudaStream_t
     HTGPU_CUDA(cudaSetDevice(device_));
     if (!st)
         st = stream_;
-    double *base = scratch_on(device_);
-    double *xpw  = base;
-    double *Aw   = base + ((std::size_t)nc * mu + 31) / 32 * 32;
-    // every entry of xpw and of the partial sums is written before it is
-    // read, so nothing needs clearing between calls
-    launch_gather(in, nc, perm_s.p, nc, mu, xpw, st);
-    if (!p1_h.empty())
-        launch_phase1(p1_d.p, (int)p1_h.size(), lr_d.p, fac.p, xpw, mu, Aw, st);
-    launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, dn_d.p, fac.p, dense.p, Aw, xpw, mu, perm_t.p, out, nr, st);
+    double *base          = scratch_on(device_);
+    const std::size_t xpl = ((std::size_t)nc * mu + 31) / 32 * 32;
+    double *xpw           = base;
+    F2 *xsw               = reinterpret_cast<F2 *>(base + xpl);
+    int *xew              = reinterpret_cast<int *>(base + 2 * xpl);
+    double *Aw            = base + 2 * xpl + 32;
+    // the exponent word is cleared by launch_xexp (an asynchronous memset,
+    // no allocation); every other entry is written before it is read
+    launch_product_with(in, out, mu, false, st, xpw, xsw, xew, Aw);
 }
 
 } // namespace htgpu

@@ -147,6 +147,19 @@ int htgpu_hmatrix_last_launches(htgpu_hmatrix h, int *launches);
  * (nb_mat_vec_prod / total_time_mat_vec_prod, hmatrix.hpp:1180-1181). */
 int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
 
+/* How the FP64 product shares its work between the FP64 pipe (DFMA) and the
+ * FP32/INT pipes (exact double-float emulation, ~2^-46 relative per term):
+ * phase1_dfma_permille of the low-rank V-side elements and phase2_dfma_warps
+ * of the 4 warps of every U-side/dense row chunk use DFMA.  No counterpart in
+ * the reference (its BLAS calls decide this, include/htool/types/matrix.hpp:320-383). */
+int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int phase1_dfma_permille, int phase2_dfma_warps);
+int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int *phase2_dfma_warps);
+
+/* Autotuner: times `reps` products with mu right-hand sides for every
+ * candidate FP64 split on this H-matrix and keeps the fastest; *best_ms is
+ * its time per product.  Replaces nothing upstream (htool has no tuning). */
+int htgpu_hmatrix_autotune(htgpu_hmatrix h, int mu, int reps, float *best_ms);
+
 /* No counterpart in the reference.  The product of htgpu_hmatrix_mvprod for
  * device pointers, but allocation-free: it never calls cudaMalloc, cudaFree
  * or any other allocating routine, for callers that cannot let a library
@@ -155,8 +168,8 @@ int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
  * the product from a hot loop.  Its working memory is one fixed 16 MiB
  * array per device inside the library (2^21 doubles, held by every GPU that
  * loads the library until the process exits); a product needs
- * nb_cols * mu (rounded up to 32) + (phase-1 partial sums) * mu doubles, and
- * larger requests fail with HTGPU_ERR_INVALID.  The first call on a device
+ * 2 * nb_cols * mu (each half rounded up to 32) + 32 + (phase-1 partial sums)
+ * * mu doubles, and larger requests fail with HTGPU_ERR_INVALID.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that
  * device current, so make it before any stream capture.  Every call shares
  * the one array, whose contents persist between calls: calls that may

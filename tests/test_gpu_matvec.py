@@ -111,7 +111,7 @@ def test_product_is_deterministic_and_linear():
     ya, yb = GH @ a, GH @ b
     assert np.array_equal(GH @ a, ya)
     yab = GH @ (2.0 * a - 3.0 * b)
-    assert rel(yab, 2.0 * ya - 3.0 * yb) < 1e-14
+    assert rel(yab, 2.0 * ya - 3.0 * yb) < 1e-13
 
 
 @pytest.mark.parametrize("n", [12, 40, 333])
@@ -151,3 +151,48 @@ def test_bad_arguments():
     bad[0, 2] = 10 ** 6
     with pytest.raises(ValueError, match="out of range"):
         H.HMatrix(t, t, 1e-6, 10.0).set_leaves(bad, uv, dn, dd)
+
+
+@pytest.mark.parametrize("split", [(0, 0), (1000, 4), (350, 1), (0, 4), (1000, 0), (650, 2)])
+@pytest.mark.parametrize("name", ["cyl4000_k0", "sphere6000_k1"])
+def test_fp64_split_parity(golden, name, split):
+    """Every DFMA / FP32-pipe-emulation split of the FP64 product stays
+    within 1e-12 of upstream htool's product."""
+    g, meta = golden(name)
+    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    GH.set_fp64_split(*split)
+    assert GH.get_fp64_split() == split
+    for mu in (1, 3):
+        assert rel(GH.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < FP64_TOL
+    x = G.rhs(g["xt"].shape[0], 9, seed=4)
+    ref = GH.mvprod_global_to_global(x, 9)
+    GH.set_fp64_split(1000, 4)
+    assert rel(ref, GH.mvprod_global_to_global(x, 9)) < FP64_TOL
+
+
+def test_fp64_emulation_input_scaling():
+    """The emulated product normalises x by its largest exponent: scaled,
+    tiny and partly zero inputs give exactly scaled results."""
+    pts = G.sphere(5000, seed=13)
+    t = H.Cluster().build(5000, pts)
+    GH = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+    GH.set_fp64_split(0, 0)  # everything on the emulation
+    x = G.rhs(5000, seed=5)
+    x[::7] = 0.0
+    y = GH @ x
+    for k in (-300, -80, 80, 300):
+        yk = GH @ (x * 2.0 ** k)
+        assert rel(yk * 2.0 ** -k, y) < 1e-13
+    GH.set_fp64_split(1000, 4)
+    assert rel(GH @ x, y) < FP64_TOL
+    assert not np.any(GH @ np.zeros(5000))
+
+
+def test_autotune_keeps_parity(golden):
+    g, meta = golden("sphere6000_k1")
+    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    ms = GH.autotune(1, 2)
+    assert ms > 0
+    assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < FP64_TOL
