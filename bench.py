@@ -244,7 +244,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)",
         "config": dict(WORKLOAD, n=n, precision="fp64", parallelism="replicas" if world > 1 else "single", l2="inputs larger than L2: %.2f GB of factors per product" % (prod_bytes / 1e9),
-                       fp64_split={"phase1_dfma_permille": split[0], "phase2_dfma_warps": split[1], "autotune_ms": tune_ms}),
+                       fp64_split={"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune_ms}),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "kernel": dom, "peak_source": peak_kind},
         "whole_product": {"bytes": prod_bytes, "GB_per_s": prod_bytes / (ms_step / 1e3) / 1e9, "frac_of_hbm_peak": prod_bytes / (ms_step / 1e3) / 1e9 / peak, "phase_ms": {"gather": phase_ms[0], "phase1": phase_ms[1], "phase2": phase_ms[2], "total": phase_ms[3]}},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk,

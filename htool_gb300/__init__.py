@@ -28,6 +28,9 @@ KERNELS = {"inv_r_eps": INV_R_EPS, "laplace": LAPLACE}
 HOST_PTRS = 1
 CLUSTER_NUMBERING = 2
 
+PREC_FP64, PREC_FP32, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED, "bf16": PREC_BF16}
+
 _ERRORS = {1: ValueError, 2: NotImplementedError, 3: RuntimeError, 4: MemoryError, 5: RuntimeError}
 
 
@@ -62,8 +65,12 @@ def _load():
         "htgpu_hmatrix_profile": (i, [vp, i, i, vp]),
         "htgpu_hmatrix_set_fp64_split": (i, [vp, i, i]),
         "htgpu_hmatrix_get_fp64_split": (i, [vp, vp, vp]),
+        "htgpu_hmatrix_set_phase2_warps": (i, [vp, i, i, i]),
+        "htgpu_hmatrix_get_phase2_warps": (i, [vp, vp, vp, vp]),
         "htgpu_hmatrix_autotune": (i, [vp, i, i, vp]),
         "htgpu_hmatrix_mvprod_noalloc": (i, [vp, vp, vp, i, vp]),
+        "htgpu_hmatrix_set_precision": (i, [vp, i, d]),
+        "htgpu_hmatrix_precision_info": (i, [vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -263,16 +270,42 @@ class HMatrix:
         _check(lib.htgpu_hmatrix_profile(self.h, mu, reps, _ptr(ms)))
         return tuple(float(v) for v in ms)
 
-    def set_fp64_split(self, phase1_dfma_permille, phase2_dfma_warps):
-        _check(lib.htgpu_hmatrix_set_fp64_split(self.h, int(phase1_dfma_permille), int(phase2_dfma_warps)))
+    def set_fp64_split(self, phase1_dfma_permille, phase2_dfma_permille):
+        """Share (per mille) of the V-side and of the U-side/dense FP64
+        multiply-adds run on the FP64 pipe; the rest uses the FP32-pipe
+        double-float emulation."""
+        _check(lib.htgpu_hmatrix_set_fp64_split(self.h, int(phase1_dfma_permille), int(phase2_dfma_permille)))
 
     def get_fp64_split(self):
         a, b = C.c_int(), C.c_int()
         _check(lib.htgpu_hmatrix_get_fp64_split(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_precision(self, policy, tau=0.25):
+        """Low-rank factor storage for products: 'fp64', 'fp32', 'mixed'
+        (FP32/BF16 per column) or 'bf16'; dense leaves stay FP64."""
+        pid = PRECISIONS[policy] if isinstance(policy, str) else int(policy)
+        _check(lib.htgpu_hmatrix_set_precision(self.h, pid, float(tau)))
+        return self
+
+    def precision_info(self):
+        p, b, f, h = C.c_int(), C.c_longlong(), C.c_longlong(), C.c_longlong()
+        _check(lib.htgpu_hmatrix_precision_info(self.h, C.byref(p), C.byref(b), C.byref(f), C.byref(h)))
+        return {"policy": p.value, "stored_bytes": b.value, "fp32_columns": f.value, "bf16_columns": h.value}
+
+    def set_phase2_warps(self, dfma, emulated, reduced):
+        """Warps (1, 2 or 4) sharing one phase-2 row chunk per panel kind."""
+        _check(lib.htgpu_hmatrix_set_phase2_warps(self.h, int(dfma), int(emulated), int(reduced)))
+        return self
+
+    def get_phase2_warps(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(lib.htgpu_hmatrix_get_phase2_warps(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return (a.value, b.value, c.value)
+
     def autotune(self, mu=1, reps=5):
-        """Pick the fastest FP64 split for this H-matrix; returns ms/product."""
+        """Pick the fastest launch shape (and FP64 split) for this H-matrix and
+        its current storage policy; returns ms/product."""
         ms = C.c_float()
         _check(lib.htgpu_hmatrix_autotune(self.h, int(mu), int(reps), C.byref(ms)))
         return ms.value

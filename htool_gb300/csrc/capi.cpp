@@ -287,8 +287,25 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *p1, int *n64) {
     return guarded([&] {
         need(h, "hmatrix");
         need(p1, "phase1_dfma_permille");
-        need(n64, "phase2_dfma_warps");
+        need(n64, "phase2_dfma_permille");
         h->h->get_fp64_split(p1, n64);
+    });
+}
+
+int htgpu_hmatrix_set_phase2_warps(htgpu_hmatrix h, int dfma, int emulated, int reduced) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_phase2_warps(dfma, emulated, reduced);
+    });
+}
+
+int htgpu_hmatrix_get_phase2_warps(htgpu_hmatrix h, int *dfma, int *emulated, int *reduced) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(dfma, "dfma");
+        need(emulated, "emulated");
+        need(reduced, "reduced");
+        h->h->get_phase2_warps(dfma, emulated, reduced);
     });
 }
 
@@ -296,7 +313,30 @@ int htgpu_hmatrix_autotune(htgpu_hmatrix h, int mu, int reps, float *best_ms) {
     return guarded([&] {
         need(h, "hmatrix");
         htgpu::require(mu > 0 && reps > 0, "mu and reps must be positive");
-        h->h->autotune_fp64(mu, reps, best_ms);
+        h->h->autotune(mu, reps, best_ms);
+    });
+}
+
+int htgpu_hmatrix_set_precision(htgpu_hmatrix h, int policy, double tau) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_precision(policy, tau);
+    });
+}
+
+int htgpu_hmatrix_precision_info(htgpu_hmatrix h, int *policy, long long *stored_bytes, long long *fp32_columns, long long *bf16_columns) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        if (policy)
+            *policy = h->h->precision();
+        long long f = 0, b = 0;
+        h->h->precision_stats(&f, &b);
+        if (stored_bytes)
+            *stored_bytes = h->h->precision() ? h->h->mixed_bytes() : h->h->stored_bytes();
+        if (fp32_columns)
+            *fp32_columns = f;
+        if (bf16_columns)
+            *bf16_columns = b;
     });
 }
 

@@ -51,6 +51,14 @@ __device__ __forceinline__ double scale_pow2(double a, int k) {
     return __longlong_as_double(b);
 }
 
+// a * 2^k, or 0 when the result would leave the normal range downwards
+__device__ __forceinline__ double scale_pow2_safe(double a, int k) {
+    const int e = (int)(((unsigned)__double2hiint(a) >> 20) & 0x7FFu);
+    if (e == 0 || e + k < 1)
+        return 0.;
+    return scale_pow2(a, k);
+}
+
 __device__ __forceinline__ void df_zero(DF &a) {
     a.s = 0.f;
     a.c = 0.f;
@@ -86,5 +94,9 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
 }
 
 __device__ __forceinline__ double df_to_double(DF a) { return (double)a.s + (double)a.c; }
+
+// barrier over the W warps of group g of a CTA (named barrier 1 + g; 0 is
+// __syncthreads)
+__device__ __forceinline__ void group_sync(int g, int W) { asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(32 * W) : "memory"); }
 
 } // namespace htgpu

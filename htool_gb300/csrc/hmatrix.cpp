@@ -14,6 +14,8 @@
 #include <chrono>
 #include <functional>
 #include <cmath>
+#include <cstring>
+#include <map>
 #include <numeric>
 #include <sstream>
 
@@ -35,7 +37,6 @@ int max_profitable_rank(int M, int N) {
 constexpr int kPhase1Chunk = 256;  // source rows per phase-1 warp (tile)
 constexpr int kRowChunk    = 32;   // target rows per phase-2 warp
 constexpr int kDefaultCap  = 48;   // initial ACA scratch columns per block
-constexpr int kP2WarpsHost = 4;    // warps per phase-2 CTA (matvec_kernels.cu)
 
 std::string num(double v) {
     std::ostringstream os;
@@ -422,73 +423,121 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
             off += even((long long)it.jlen * L.r);
         }
     }
-    // atoms
-    std::vector<int> cuts{0, nr};
-    for (auto &L : lr_h)
-        if (L.r > 0) {
-            cuts.push_back(L.oi);
-            cuts.push_back(L.oi + L.m);
-        }
-    for (auto &D : dn_h) {
-        cuts.push_back(D.oi);
-        cuts.push_back(D.oi + D.m);
-    }
-    std::sort(cuts.begin(), cuts.end());
-    cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
-    const int natoms = (int)cuts.size() - 1;
-    auto atom_of     = [&](int row) { return (int)(std::lower_bound(cuts.begin(), cuts.end(), row) - cuts.begin()); };
-    std::vector<int> cnt(natoms + 1, 0);
-    struct Span {
-        int leaf, a0, a1;
+    // phase 2: leaves grouped by their target cluster tau = (offset_i, m);
+    // every group owns a slice of the partial-sum vector z (|tau| rows), cut
+    // into balanced chunks of <= kRowChunk rows, one phase-2 item each,
+    // listing the group's leaves (dense, then low-rank, each by offset_j)
+    std::map<std::pair<int, int>, int> gid;
+    std::vector<std::pair<int, int>> groups; // (offset_i, m)
+    std::vector<std::vector<int>> members;   // ~d for dense leaf d, l for low-rank leaf l
+    auto group_of = [&](int oi, int m) {
+        auto key = std::make_pair(oi, m);
+        auto f   = gid.find(key);
+        if (f != gid.end())
+            return f->second;
+        int g    = (int)groups.size();
+        gid[key] = g;
+        groups.push_back(key);
+        members.emplace_back();
+        return g;
     };
-    std::vector<Span> spans;
     for (int d = 0; d < (int)dn_h.size(); d++)
-        spans.push_back({~d, atom_of(dn_h[d].oi), atom_of(dn_h[d].oi + dn_h[d].m)});
+        members[group_of(dn_h[d].oi, dn_h[d].m)].push_back(~d);
     for (int l = 0; l < (int)lr_h.size(); l++)
         if (lr_h[l].r > 0)
-            spans.push_back({l, atom_of(lr_h[l].oi), atom_of(lr_h[l].oi + lr_h[l].m)});
-    for (auto &sp : spans)
-        for (int a = sp.a0; a < sp.a1; a++)
-            cnt[a + 1]++;
-    std::partial_sum(cnt.begin(), cnt.end(), cnt.begin());
-    std::vector<int> by_atom(cnt[natoms]);
-    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (auto &sp : spans)
-        for (int a = sp.a0; a < sp.a1; a++)
-            by_atom[fill[a]++] = sp.leaf;
+            members[group_of(lr_h[l].oi, lr_h[l].m)].push_back(l);
+    std::vector<int> gorder(groups.size());
+    std::iota(gorder.begin(), gorder.end(), 0);
+    std::sort(gorder.begin(), gorder.end(), [&](int a, int b) { return groups[a].first != groups[b].first ? groups[a].first < groups[b].first : groups[a].second > groups[b].second; });
+    std::vector<long long> zbase(groups.size());
+    zlen_ = 0;
+    for (int g : gorder) {
+        zbase[g] = zlen_ - groups[g].first; // z index of cluster row i is i + zbase
+        zlen_ += groups[g].second;
+    }
     p2_h.clear();
     c_h.clear();
     c_leaf.clear();
-    for (int a = 0; a < natoms; a++) {
-        for (int r0 = cuts[a]; r0 < cuts[a + 1]; r0 += kRowChunk) {
+    p2_row_h.clear();
+    pan_h.clear();
+    cidx_h.clear();
+    for (int g : gorder) {
+        const int oi = groups[g].first, m = groups[g].second;
+        const int nchunk = (m + kRowChunk - 1) / kRowChunk;
+        for (int q = 0; q < nchunk; q++) {
+            const int lo = (int)((long long)m * q / nchunk), hi = (int)((long long)m * (q + 1) / nchunk);
             P2Item it;
-            it.row0 = r0;
-            it.h    = std::min(kRowChunk, cuts[a + 1] - r0);
+            it.row0 = (int)(oi + lo + zbase[g]); // z index of the chunk's first row
+            it.h    = hi - lo;
             it.cbeg = (int)c_h.size();
-            for (int c = cnt[a]; c < cnt[a + 1]; c++) {
-                const int leaf = by_atom[c];
+            PanelItem pi;
+            pi.off  = off;
+            pi.row0 = it.row0;
+            pi.h    = it.h;
+            pi.q0   = (int)cidx_h.size();
+            long long col = 0;
+            for (int leaf : members[g]) { // dense leaves come first in members
                 P2Contrib pc;
-                pc.off = off;
+                pc.off = off + (long long)it.h * col;
                 if (leaf >= 0) {
                     const LrLeaf &L = lr_h[leaf];
                     pc.w            = L.r;
-                    pc.aux          = (int)L.a_off; // phase-1 slot of the coefficients
-                    copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + (r0 - L.oi), off, it.h, L.r, L.m, 0});
+                    pc.aux          = (int)L.a_off;
+                    copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + lo, pc.off, it.h, L.r, L.m, 0});
+                    for (int k = 0; k < L.r; k++)
+                        cidx_h.push_back((int)L.a_off + k);
                 } else {
                     const DenseLeaf &D = dn_h[~leaf];
                     pc.w               = D.n;
                     pc.aux             = ~D.oj;
                     if (dn_src)
-                        copies[(*dn_src)[~leaf].buf].push_back({(*dn_src)[~leaf].su + (r0 - D.oi), off, it.h, D.n, D.m, 0});
+                        copies[(*dn_src)[~leaf].buf].push_back({(*dn_src)[~leaf].su + lo, pc.off, it.h, D.n, D.m, 0});
                     else
-                        fills.push_back({off, r0, it.h, D.oj, D.n});
+                        fills.push_back({pc.off, oi + lo, it.h, D.oj, D.n});
+                    for (int j = 0; j < D.n; j++)
+                        cidx_h.push_back(~(D.oj + j));
                 }
-                off += even((long long)it.h * pc.w);
+                col += pc.w;
                 c_h.push_back(pc);
                 c_leaf.push_back(leaf);
             }
+            pi.ncol = (int)col;
+            off += even((long long)it.h * col);
             it.cend = (int)c_h.size();
             p2_h.push_back(it);
+            p2_row_h.push_back(oi + lo);
+            pan_h.push_back(pi);
+        }
+    }
+    // z sums: target rows cut at every group boundary into atoms; every atom
+    // lists the z bases of the groups covering it, largest group first
+    {
+        std::vector<int> cuts{0, nr};
+        for (auto &gk : groups) {
+            cuts.push_back(gk.first);
+            cuts.push_back(gk.first + gk.second);
+        }
+        std::sort(cuts.begin(), cuts.end());
+        cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+        const int natoms = (int)cuts.size() - 1;
+        auto atom_of     = [&](int row) { return (int)(std::lower_bound(cuts.begin(), cuts.end(), row) - cuts.begin()); };
+        std::vector<std::vector<int>> cover(natoms);
+        std::vector<int> by_size(groups.size());
+        std::iota(by_size.begin(), by_size.end(), 0);
+        std::sort(by_size.begin(), by_size.end(), [&](int a, int b) { return groups[a].second != groups[b].second ? groups[a].second > groups[b].second : groups[a].first < groups[b].first; });
+        for (int g : by_size)
+            for (int a = atom_of(groups[g].first); a < atom_of(groups[g].first + groups[g].second); a++)
+                cover[a].push_back((int)zbase[g]);
+        zi_h.clear();
+        zl_h.clear();
+        for (int a = 0; a < natoms; a++) {
+            ZItem zi;
+            zi.row0 = cuts[a];
+            zi.h    = cuts[a + 1] - cuts[a];
+            zi.lbeg = (int)zl_h.size();
+            zl_h.insert(zl_h.end(), cover[a].begin(), cover[a].end());
+            zi.lend = (int)zl_h.size();
+            zi_h.push_back(zi);
         }
     }
     arena_len = off;
@@ -528,14 +577,18 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     assign_phase1_modes();
     upload_phase1_lists();
     lr_d.upload(lr_h, stream_);
-    p2_d.upload(p2_h, stream_);
-    c_d.upload(c_h, stream_);
+    cidx_d.upload(cidx_h, stream_);
+    if (cidx_h.empty())
+        cidx_d.alloc(1);
+    zi_d.upload(zi_h, stream_);
+    zl_d.upload(zl_h, stream_);
+    if (zl_h.empty())
+        zl_d.alloc(1);
     if (lr_h.empty())
         lr_d.alloc(1);
-    if (c_h.empty())
-        c_d.alloc(1);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
-    mu_cap = 0;
+    mu_cap     = 0;
+    precision_ = 0;
 }
 
 void HMatrix::ensure_work(int mu) {
@@ -545,6 +598,7 @@ void HMatrix::ensure_work(int mu) {
     xs.alloc((std::size_t)nc * mu + 1);
     xexp.alloc(1);
     A.alloc((std::size_t)std::max<long long>(a_slots, 1) * mu);
+    z.alloc((std::size_t)std::max<long long>(zlen_, 1) * mu);
     xstage.alloc((std::size_t)nc * mu);
     ystage.alloc((std::size_t)nr * mu);
     mu_cap = mu;
@@ -597,11 +651,30 @@ void HMatrix::upload_phase1_lists() {
     n_p1_emu_  = (int)b.size();
     p1_d.upload(a, stream_);
     p1e_d.upload(b, stream_);
+    // phase-2 panels: DFMA for p2_permille_ / 1000 of the elements, spread by
+    // error diffusion through the launch
+    std::vector<PanelItem> pa, pb;
+    const double target = emu_ok_ ? p2_n64_ / 1000.0 : 1.0;
+    long long seen = 0, dfma = 0;
+    for (auto &pi : pan_h) {
+        const long long e = (long long)pi.h * pi.ncol;
+        seen += e;
+        if (target >= 1.0 || (double)dfma < target * (double)seen) {
+            dfma += e;
+            pa.push_back(pi);
+        } else {
+            pb.push_back(pi);
+        }
+    }
+    n_p2_dfma_ = (int)pa.size();
+    n_p2_emu_  = (int)pb.size();
+    p2_d.upload(pa, stream_);
+    p2e_d.upload(pb, stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void HMatrix::set_fp64_split(int p1, int n64) {
-    require(p1 >= 0 && p1 <= 1000 && n64 >= 0 && n64 <= 4, "FP64 split: phase-1 share in [0, 1000], phase-2 warps in [0, 4]");
+    require(p1 >= 0 && p1 <= 1000 && n64 >= 0 && n64 <= 1000, "FP64 split: phase-1 and phase-2 DFMA shares in [0, 1000] per mille");
     p1_permille_ = p1;
     p2_n64_      = n64;
     assign_phase1_modes();
@@ -610,20 +683,182 @@ void HMatrix::set_fp64_split(int p1, int n64) {
 
 void HMatrix::get_fp64_split(int *p1, int *n64) const {
     *p1  = emu_ok_ ? p1_permille_ : 1000;
-    *n64 = emu_ok_ ? p2_n64_ : kP2WarpsHost;
+    *n64 = emu_ok_ ? p2_n64_ : 1000;
 }
 
-void HMatrix::launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st) { launch_product_with(x, y, mu, cluster_numbering, st, xp.p, xs.p, xexp.p, A.p); }
+void HMatrix::launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st) { launch_product_with(x, y, mu, cluster_numbering, st, xp.p, xs.p, xexp.p, A.p, z.p); }
+
+// Reduced-precision copy of the low-rank factors (see mixed.cu): column
+// maxima from the FP64 blocks, per-column precision on the host, then one
+// conversion pass into a byte arena laid out like the FP64 one.
+void HMatrix::set_precision(int policy, double tau) {
+    require(policy >= 0 && policy <= 3, "precision policy must be 0 (FP64), 1 (FP32), 2 (FP32/BF16) or 3 (BF16)");
+    require(tau > 0, "tau must be positive");
+    HTGPU_CUDA(cudaSetDevice(device_));
+    precision_ = policy;
+    tau_       = tau;
+    if (policy == 0)
+        return;
+    // 1. column maxima of U (slots [0, a_slots)) and Vt ([a_slots, 2 a_slots))
+    std::vector<ColMaxJob> jobs;
+    for (auto &it : p1_h)
+        jobs.push_back({it.off, it.jlen, lr_h[it.leaf].r, (int)(a_slots + lr_h[it.leaf].a_off), 0});
+    for (auto &it : p2_h)
+        for (int c = it.cbeg; c < it.cend; c++)
+            if (c_leaf[c] >= 0)
+                jobs.push_back({c_h[c].off, it.h, lr_h[c_leaf[c]].r, (int)lr_h[c_leaf[c]].a_off, 0});
+    DevBuf<unsigned> cmax;
+    cmax.alloc(2 * std::max<long long>(a_slots, 1));
+    HTGPU_CUDA(cudaMemsetAsync(cmax.p, 0, sizeof(unsigned) * cmax.n, stream_));
+    {
+        DevBuf<ColMaxJob> dj;
+        dj.upload(jobs, stream_);
+        launch_colmax(dj.p, (int)jobs.size(), fac.p, cmax.p, stream_);
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    }
+    std::vector<unsigned> cm(cmax.n);
+    HTGPU_CUDA(cudaMemcpy(cm.data(), cmax.p, sizeof(unsigned) * cm.size(), cudaMemcpyDeviceToHost));
+    auto asf = [](unsigned u) {
+        float f;
+        std::memcpy(&f, &u, 4);
+        return (double)f;
+    };
+    // 2. per-column scales and the FP32 / BF16 split of every leaf
+    std::vector<double> scale(std::max<long long>(a_slots, 1), 0.);
+    std::vector<int> c32(lr_h.size(), 0);
+    n_f32_cols_ = n_bf16_cols_ = 0;
+    const double bf16_unit = std::ldexp(1.0, -9);
+    for (std::size_t l = 0; l < lr_h.size(); l++) {
+        const LrLeaf &L = lr_h[l];
+        if (L.r == 0)
+            continue;
+        double leaf2 = 0;
+        std::vector<double> bound(L.r);
+        for (int k = 0; k < L.r; k++) {
+            const double su = asf(cm[L.a_off + k]), sv = asf(cm[a_slots + L.a_off + k]);
+            scale[L.a_off + k] = su * sv;
+            bound[k]           = su * sv * std::sqrt((double)L.m * (double)L.n);
+            leaf2 += bound[k] * bound[k];
+        }
+        const double thr = tau * eps_ * std::sqrt(leaf2) / bf16_unit;
+        int split        = 0;
+        for (int k = 0; k < L.r; k++)
+            if (bound[k] >= thr)
+                split = k + 1;
+        c32[l] = policy == 1 ? L.r : policy == 3 ? 0 : split;
+        n_f32_cols_ += c32[l];
+        n_bf16_cols_ += L.r - c32[l];
+    }
+    // 3. layout of the reduced-precision arena (bytes, 16-byte aligned blocks):
+    //    phase-1 tiles, then per phase-2 chunk an FP32 and a BF16 sub-panel
+    auto al16 = [](long long b) { return (b + 15) & ~15LL; };
+    long long off = 0;
+    std::vector<P1Item> p1m;
+    std::vector<ConvertJob> conv;
+    for (auto &it : p1_h) {
+        const LrLeaf &L = lr_h[it.leaf];
+        P1Item m        = it;
+        m.off           = off;
+        m.pad           = c32[it.leaf];
+        p1m.push_back(m);
+        conv.push_back({it.off, off, off + 4LL * it.jlen * c32[it.leaf], it.jlen, L.r, c32[it.leaf], (int)(a_slots + L.a_off)});
+        off += al16(4LL * it.jlen * c32[it.leaf] + 2LL * it.jlen * (L.r - c32[it.leaf]));
+    }
+    std::vector<MixedItem> mit;
+    std::vector<int> cim;
+    mixed_bytes_ = 0;
+    for (std::size_t q = 0; q < p2_h.size(); q++) {
+        const P2Item &it = p2_h[q];
+        MixedItem mi;
+        mi.row0  = it.row0;
+        mi.h     = it.h;
+        mi.off64 = pan_h[q].off;
+        mi.q64   = (int)cim.size();
+        int n64 = 0, n32 = 0, n16 = 0;
+        for (int c = it.cbeg; c < it.cend; c++)
+            if (c_leaf[c] < 0) {
+                const P2Contrib &pc = c_h[c];
+                for (int j = 0; j < pc.w; j++)
+                    cim.push_back(~((~pc.aux) + j));
+                n64 += pc.w;
+            } else {
+                n32 += c32[c_leaf[c]];
+                n16 += lr_h[c_leaf[c]].r - c32[c_leaf[c]];
+            }
+        mi.n64 = n64;
+        mi.q32 = (int)cim.size();
+        mi.n32 = n32;
+        mi.off32 = off;
+        mi.off16 = off + al16(4LL * it.h * n32);
+        for (int c = it.cbeg; c < it.cend; c++)
+            if (c_leaf[c] >= 0)
+                for (int k = 0; k < c32[c_leaf[c]]; k++)
+                    cim.push_back((int)lr_h[c_leaf[c]].a_off + k);
+        mi.q16 = (int)cim.size();
+        mi.n16 = n16;
+        int f32c = 0, b16c = 0;
+        for (int c = it.cbeg; c < it.cend; c++)
+            if (c_leaf[c] >= 0) {
+                const int l     = c_leaf[c];
+                const LrLeaf &L = lr_h[l];
+                for (int k = c32[l]; k < L.r; k++)
+                    cim.push_back((int)L.a_off + k);
+                conv.push_back({c_h[c].off, mi.off32 + 4LL * it.h * f32c, mi.off16 + 2LL * it.h * b16c, it.h, L.r, c32[l], (int)L.a_off});
+                f32c += c32[l];
+                b16c += L.r - c32[l];
+            }
+        mixed_bytes_ += 8LL * it.h * n64;
+        off = mi.off16 + al16(2LL * it.h * n16);
+        mit.push_back(mi);
+    }
+    for (std::size_t l = 0; l < lr_h.size(); l++)
+        mixed_bytes_ += (4LL * c32[l] + 2LL * (lr_h[l].r - c32[l])) * (lr_h[l].m + lr_h[l].n);
+    mix_.alloc(std::max<long long>(off, 16));
+    scale_d.upload(scale, stream_);
+    p1m_d.upload(p1m, stream_);
+    n_p1m_ = (int)p1m.size();
+    mit_d.upload(mit, stream_);
+    n_mit_ = (int)mit.size();
+    cidxm_d.upload(cim, stream_);
+    if (p1m.empty())
+        p1m_d.alloc(1);
+    if (cim.empty())
+        cidxm_d.alloc(1);
+    {
+        DevBuf<ConvertJob> dc;
+        dc.upload(conv, stream_);
+        launch_convert(dc.p, (int)conv.size(), fac.p, cmax.p, mix_.p, stream_);
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    }
+}
 
 // The phase-1 tiles on the FP64 pipe and those on the emulation run as two
 // kernels on two streams at once (fork/join through events), so each keeps
 // its own register budget and both pipe families work together.
-void HMatrix::launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A) {
+void HMatrix::launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks) {
     const int groups = rhs_groups(mu);
     launches_        = 0;
     launch_xexp(x, (long long)nc * mu, w_xexp, st);
     launch_gather_split(x, nc, cluster_numbering ? nullptr : perm_s.p, nc, mu, w_xexp, w_xp, w_xs, st);
     launches_ += 2;
+    if (marks)
+        HTGPU_CUDA(cudaEventRecord(marks[0], st));
+    if (precision_ != 0) {
+        if (n_p1m_) {
+            launch_phase1_mixed(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, w_xexp, mu, w_A, st);
+            launches_ += groups;
+        }
+        if (!multi_h.empty()) {
+            launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, w_A, st);
+            launches_++;
+        }
+        if (marks)
+            HTGPU_CUDA(cudaEventRecord(marks[1], st));
+        launch_phase2_mixed(mit_d.p, n_mit_, p2m_warps_, cidxm_d.p, mix_.p, fac.p, w_A, w_xp, w_xexp, mu, w_z, (int)zlen_, st);
+        launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
+        launches_ += groups + 1;
+        return;
+    }
     if (n_p1_dfma_ && n_p1_emu_) {
         HTGPU_CUDA(cudaEventRecord(fork_, st));
         HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
@@ -643,28 +878,47 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, w_A, st);
         launches_++;
     }
-    launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, emu_ok_ ? p2_n64_ : kP2WarpsHost, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
-    launches_ += groups;
+    if (marks)
+        HTGPU_CUDA(cudaEventRecord(marks[1], st));
+    if (n_p2_dfma_ && n_p2_emu_) {
+        HTGPU_CUDA(cudaEventRecord(fork_, st));
+        HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
+        launch_phase2(p2_d.p, n_p2_dfma_, false, p2_warps_, cidx_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, st);
+        launch_phase2(p2e_d.p, n_p2_emu_, true, p2e_warps_, cidx_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, aux_);
+        HTGPU_CUDA(cudaEventRecord(join_, aux_));
+        HTGPU_CUDA(cudaStreamWaitEvent(st, join_, 0));
+        launches_ += 2 * groups;
+    } else if (n_p2_dfma_ || n_p2_emu_) {
+        const bool emu = n_p2_dfma_ == 0;
+        launch_phase2(emu ? p2e_d.p : p2_d.p, emu ? n_p2_emu_ : n_p2_dfma_, emu, emu ? p2e_warps_ : p2_warps_, cidx_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, st);
+        launches_ += groups;
+    }
+    launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
+    launches_ += 1;
 }
 
-void HMatrix::autotune_fp64(int mu, int reps, float *best_ms) {
+void HMatrix::set_phase2_warps(int dfma, int emulated, int reduced) {
+    auto ok = [](int w) { return w == 1 || w == 2 || w == 4; };
+    require(ok(dfma) && ok(emulated) && ok(reduced), "warps per phase-2 row chunk must be 1, 2 or 4");
+    p2_warps_  = dfma;
+    p2e_warps_ = emulated;
+    p2m_warps_ = reduced;
+}
+
+void HMatrix::get_phase2_warps(int *dfma, int *emulated, int *reduced) const {
+    *dfma     = p2_warps_;
+    *emulated = p2e_warps_;
+    *reduced  = p2m_warps_;
+}
+
+void HMatrix::autotune(int mu, int reps, float *best_ms) {
     HTGPU_CUDA(cudaSetDevice(device_));
     ensure_work(mu);
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
-    std::vector<std::pair<int, int>> cands;
-    if (!emu_ok_)
-        cands.push_back({1000, 4});
-    else
-        for (int p1 : {0, 200, 350, 500, 650, 1000})
-            for (int n64 : {0, 1, 2, 4})
-                cands.push_back({p1, n64});
     cudaEvent_t e0, e1;
     HTGPU_CUDA(cudaEventCreate(&e0));
     HTGPU_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    std::pair<int, int> arg = cands[0];
-    for (auto &c : cands) {
-        set_fp64_split(c.first, c.second);
+    auto timed = [&]() {
         launch_product(xstage.p, ystage.p, mu, false, stream_); // warm-up
         HTGPU_CUDA(cudaEventRecord(e0, stream_));
         for (int r = 0; r < reps; r++)
@@ -673,15 +927,57 @@ void HMatrix::autotune_fp64(int mu, int reps, float *best_ms) {
         HTGPU_CUDA(cudaEventSynchronize(e1));
         float ms;
         HTGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        ms /= reps;
-        if (ms < best) {
-            best = ms;
-            arg  = c;
+        return ms / reps;
+    };
+    // the fastest value of one knob, the others fixed
+    auto pick = [&](int &knob, std::initializer_list<int> values) {
+        float best = 1e30f;
+        int arg    = knob;
+        for (int v : values) {
+            knob           = v;
+            const float ms = timed();
+            if (ms < best) {
+                best = ms;
+                arg  = v;
+            }
         }
+        knob = arg;
+        return best;
+    };
+    float best = 1e30f;
+    if (precision_ != 0) {
+        best = pick(p2m_warps_, {1, 2, 4});
+    } else {
+        // warps per phase-2 row chunk for the DFMA and the emulated panel
+        // lists, each timed with the whole phase 2 on its own pipe
+        const int p1 = p1_permille_, p2 = p2_n64_;
+        set_fp64_split(p1, 1000);
+        best = pick(p2_warps_, {1, 2, 4});
+        if (emu_ok_) {
+            set_fp64_split(p1, 0);
+            pick(p2e_warps_, {1, 2, 4});
+        }
+        std::vector<std::pair<int, int>> cands;
+        if (!emu_ok_)
+            cands.push_back({1000, 1000});
+        else
+            for (int q1 : {0, 350, 650, 1000})
+                for (int q2 : {0, 350, 650, 1000})
+                    cands.push_back({q1, q2});
+        std::pair<int, int> arg = {p1, p2};
+        best                    = 1e30f;
+        for (auto &c : cands) {
+            set_fp64_split(c.first, c.second);
+            const float ms = timed();
+            if (ms < best) {
+                best = ms;
+                arg  = c;
+            }
+        }
+        set_fp64_split(arg.first, arg.second);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    set_fp64_split(arg.first, arg.second);
     if (best_ms)
         *best_ms = best;
 }
@@ -694,26 +990,9 @@ void HMatrix::profile(int mu, int reps, float *ms) {
         HTGPU_CUDA(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
-    const int n64 = emu_ok_ ? p2_n64_ : kP2WarpsHost;
     for (int r = 0; r < reps; r++) {
         HTGPU_CUDA(cudaEventRecord(ev[0], stream_));
-        launch_xexp(xstage.p, (long long)nc * mu, xexp.p, stream_);
-        launch_gather_split(xstage.p, nc, perm_s.p, nc, mu, xexp.p, xp.p, xs.p, stream_);
-        HTGPU_CUDA(cudaEventRecord(ev[1], stream_));
-        if (n_p1_dfma_ && n_p1_emu_) {
-            HTGPU_CUDA(cudaEventRecord(fork_, stream_));
-            HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
-            launch_phase1(p1_d.p, n_p1_dfma_, false, lr_d.p, fac.p, xp.p, xs.p, xexp.p, mu, A.p, stream_);
-            launch_phase1(p1e_d.p, n_p1_emu_, true, lr_d.p, fac.p, xp.p, xs.p, xexp.p, mu, A.p, aux_);
-            HTGPU_CUDA(cudaEventRecord(join_, aux_));
-            HTGPU_CUDA(cudaStreamWaitEvent(stream_, join_, 0));
-        } else if (n_p1_dfma_ || n_p1_emu_) {
-            launch_phase1(n_p1_dfma_ ? p1_d.p : p1e_d.p, n_p1_dfma_ ? n_p1_dfma_ : n_p1_emu_, n_p1_dfma_ == 0, lr_d.p, fac.p, xp.p, xs.p, xexp.p, mu, A.p, stream_);
-        }
-        if (!multi_h.empty())
-            launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, A.p, stream_);
-        HTGPU_CUDA(cudaEventRecord(ev[2], stream_));
-        launch_phase2(p2_d.p, (int)p2_h.size(), c_d.p, lr_d.p, fac.p, A.p, xp.p, xs.p, xexp.p, n64, mu, perm_t.p, ystage.p, nr, stream_);
+        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1);
         HTGPU_CUDA(cudaEventRecord(ev[3], stream_));
         HTGPU_CUDA(cudaEventSynchronize(ev[3]));
         float t;
@@ -772,22 +1051,25 @@ void HMatrix::export_factors(double *uv, double *dn) {
                 for (int jj = 0; jj < it.jlen; jj++)
                     uv[v_at[it.leaf] + k + (long long)L.r * (it.j0 + jj)] = host[it.off + jj + (long long)it.jlen * k];
         }
-    for (auto &it : p2_h)
+    for (std::size_t q = 0; q < p2_h.size(); q++) {
+        const P2Item &it = p2_h[q];
+        const int row0   = p2_row_h[q];
         for (int c = it.cbeg; c < it.cend; c++) {
-            const int leaf = c_leaf[c];
+            const int leaf      = c_leaf[c];
             const P2Contrib &pc = c_h[c];
             if (leaf >= 0 && uv) {
                 const LrLeaf &L = lr_h[leaf];
                 for (int k = 0; k < L.r; k++)
                     for (int i = 0; i < it.h; i++)
-                        uv[u_at[leaf] + (it.row0 - L.oi + i) + (long long)L.m * k] = host[pc.off + i + (long long)it.h * k];
+                        uv[u_at[leaf] + (row0 - L.oi + i) + (long long)L.m * k] = host[pc.off + i + (long long)it.h * k];
             } else if (leaf < 0 && dn) {
                 const DenseLeaf &D = dn_h[~leaf];
                 for (int j = 0; j < D.n; j++)
                     for (int i = 0; i < it.h; i++)
-                        dn[d_at[~leaf] + (it.row0 - D.oi + i) + (long long)D.m * j] = host[pc.off + i + (long long)it.h * j];
+                        dn[d_at[~leaf] + (row0 - D.oi + i) + (long long)D.m * j] = host[pc.off + i + (long long)it.h * j];
             }
         }
+    }
 }
 
 long long HMatrix::stored_bytes() const {
@@ -879,9 +1161,17 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["GPU_phase1_items"]         = inum((long long)p1_h.size());
     m["GPU_phase2_items"]         = inum((long long)p2_h.size());
     m["GPU_phase2_contributions"] = inum((long long)c_h.size());
+    m["GPU_partial_sum_rows"]     = inum(zlen_);
     m["GPU_fp64_emulation_allowed"] = emu_ok_ ? "1" : "0";
+    m["GPU_precision"]              = inum(precision_);
+    m["GPU_mixed_bytes"]            = inum(mixed_bytes_);
+    m["GPU_fp32_columns"]           = inum(n_f32_cols_);
+    m["GPU_bf16_columns"]           = inum(n_bf16_cols_);
     m["GPU_fp64_phase1_dfma_permille"] = inum(emu_ok_ ? p1_permille_ : 1000);
-    m["GPU_fp64_phase2_dfma_warps"]    = inum(emu_ok_ ? p2_n64_ : kP2WarpsHost);
+    m["GPU_fp64_phase2_dfma_permille"] = inum(emu_ok_ ? p2_n64_ : 1000);
+    m["GPU_phase2_warps_dfma"]         = inum(p2_warps_);
+    m["GPU_phase2_warps_emulated"]     = inum(p2e_warps_);
+    m["GPU_phase2_warps_reduced"]      = inum(p2m_warps_);
     return m;
 }
 

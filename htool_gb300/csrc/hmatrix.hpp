@@ -54,15 +54,30 @@ class HMatrix {
 
     BlockTreeParams bp;
 
-    // FP64 product configuration: share (per mille) of phase-1 elements on
-    // the FP64 pipe, number of phase-2 warps (of 4) on the FP64 pipe; the
-    // rest runs the FP32-pipe emulation.  emulation_allowed() is false when
+    // FP64 product configuration: share (per mille) of phase-1 and of
+    // phase-2 elements on the FP64 pipe; the rest runs the FP32-pipe
+    // emulation.  emulation_allowed() is false when
     // stored entries are too large for it (then everything uses DFMA).
-    void set_fp64_split(int phase1_dfma_permille, int phase2_dfma_warps);
-    void get_fp64_split(int *phase1_dfma_permille, int *phase2_dfma_warps) const;
+    void set_fp64_split(int phase1_dfma_permille, int phase2_dfma_permille);
+    void get_fp64_split(int *phase1_dfma_permille, int *phase2_dfma_permille) const;
+    void set_phase2_warps(int dfma, int emulated, int reduced);
+    void get_phase2_warps(int *dfma, int *emulated, int *reduced) const;
     bool emulation_allowed() const { return emu_ok_; }
     // time every candidate split on the current H-matrix and keep the fastest
-    void autotune_fp64(int mu, int reps, float *best_ms);
+    // FP64: warps per phase-2 chunk, then the DFMA/emulation split;
+    // reduced precision: warps per phase-2 chunk
+    void autotune(int mu, int reps, float *best_ms);
+
+    // factor storage used by products: 0 FP64, 1 FP32, 2 FP32/BF16 per
+    // column (BF16 where the column's bound is below tau * eps of the leaf),
+    // 3 BF16; dense leaves stay FP64.  Builds the reduced-precision copy.
+    void set_precision(int policy, double tau);
+    int precision() const { return precision_; }
+    long long mixed_bytes() const { return mixed_bytes_; } // stored bytes read by a reduced-precision product
+    void precision_stats(long long *f32_cols, long long *bf16_cols) const {
+        *f32_cols  = n_f32_cols_;
+        *bf16_cols = n_bf16_cols_;
+    }
 
   private:
     // where a leaf's factors sit before the final layout: U (m x r, ld m) at
@@ -86,27 +101,48 @@ class HMatrix {
     std::vector<P1Item> p1_h;
     std::vector<P2Item> p2_h;
     std::vector<P2Contrib> c_h;
-    std::vector<int> c_leaf; // per contribution: low-rank leaf l, or ~d for dense leaf d
+    std::vector<int> c_leaf;   // per contribution: low-rank leaf l, or ~d for dense leaf d
+    std::vector<int> p2_row_h; // per phase-2 item: first cluster row
+    std::vector<ZItem> zi_h;   // z-sum atoms
+    std::vector<int> zl_h;     // their z bases
+    long long zlen_ = 0;       // rows of the per-cluster partial sums z
     long long a_slots = 0, arena_len = 0;
 
     DevBuf<int> perm_t, perm_s;
     DevBuf<double> fac; // every factor and dense block, in work-item order
     DevBuf<LrLeaf> lr_d;
     DevBuf<P1Item> p1_d;
-    DevBuf<P2Item> p2_d;
-    DevBuf<P2Contrib> c_d;
-    DevBuf<double> xp, A, xstage, ystage;
+    DevBuf<PanelItem> p2_d;
+    DevBuf<double> xp, A, z, xstage, ystage;
+    DevBuf<ZItem> zi_d;
+    DevBuf<int> zl_d;
     DevBuf<F2> xs;
     DevBuf<int> xexp, multi_d;
     std::vector<int> multi_h;
     int p1_permille_ = 300, p2_n64_ = 1;
+    // warps sharing one phase-2 row chunk: DFMA panels, emulated panels,
+    // reduced-precision panels
+    int p2_warps_ = 2, p2e_warps_ = 1, p2m_warps_ = 1;
     bool emu_ok_ = false;
     void launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st);
-    void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A);
+    void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr);
     void upload_phase1_lists();
     DevBuf<P1Item> p1e_d; // phase-1 tiles on the emulation (p1_d: on DFMA)
     int n_p1_dfma_ = 0, n_p1_emu_ = 0;
+    std::vector<PanelItem> pan_h; // phase-2 panels (one per P2Item)
+    std::vector<int> cidx_h;      // panel column coefficients
+    DevBuf<PanelItem> p2e_d;      // phase-2 panels on the emulation (p2_d: on DFMA)
+    DevBuf<int> cidx_d, cidxm_d;
+    DevBuf<MixedItem> mit_d;
+    int n_p2_dfma_ = 0, n_p2_emu_ = 0, n_mit_ = 0;
     cudaStream_t aux_ = nullptr;
+    int precision_ = 0;
+    double tau_    = 0.25;
+    DevBuf<unsigned char> mix_;
+    DevBuf<double> scale_d;
+    DevBuf<P1Item> p1m_d;
+    int n_p1m_ = 0;
+    long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
     int mu_cap = 0;
     int launches_ = 0;

@@ -96,8 +96,24 @@ struct P1Item { // one warp: Vt tile block (jlen x r, column-major, ld jlen) at 
     int pad;
 };
 
-struct P2Item { // one CTA: target rows row0 .. row0+h, contributions [cbeg, cend)
+struct P2Item { // host record of one phase-2 row chunk: leaf blocks [cbeg, cend) of c_h
     int row0, h, cbeg, cend;
+};
+
+struct PanelItem { // one warp: z rows row0 .. row0+h += panel (h x ncol, column-major, ld h)
+    long long off; // at off, times coefficients coef[cidx[q0 + q]] (cidx >= 0: phase-1
+    int row0, h;   // slot; < 0: x index ~cidx)
+    int q0, ncol;
+};
+
+struct MixedItem { // reduced-precision phase 2: dense FP64 columns, FP32 columns, BF16 columns
+    long long off64, off32, off16; // FP64 arena (elements), reduced arena (bytes) x2
+    int row0, h;
+    int q64, n64, q32, n32, q16, n16; // column index ranges in cidx
+};
+
+struct ZItem { // cluster rows row0 .. row0+h: y[perm[i]] = sum over l of z[i + zl[l]], l in [lbeg, lend)
+    int row0, h, lbeg, lend;
 };
 
 struct P2Contrib { // block h x w (column-major, ld h) at off; aux >= 0: low-rank

@@ -33,7 +33,6 @@ namespace htgpu {
 namespace {
 
 constexpr int kWarpsPerBlock = 8; // phase 1: warps per CTA
-constexpr int kP2Warps       = 4; // phase 2: warps sharing one row chunk
 
 __device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
     // TMA bulk prefetch of a contiguous, 16-byte-aligned range into L2
@@ -282,75 +281,63 @@ __global__ void reduce_tiles_kernel(const LrLeaf *__restrict__ lr, const int *__
 }
 
 // ---------------------------------------------------------------------------
-// phase 2: CTAs of kP2Warps warps loop over row chunks; lane -> (row =
-// lane % h, slice = lane / h), S = 32 / h slices; warp w takes
-// contributions w, w + kP2Warps, ... (the next descriptor is loaded and the
-// next block prefetched into L2 while the current one is processed);
-// warps w < n64 use DFMA
+// phase 2: W warps per row chunk (8 / W chunks per CTA at a time); the
+// chunk's leaves are ONE contiguous panel h x ncol (every covering leaf's
+// columns side by side) and the product is a streaming GEMV: warp w of a
+// chunk takes the column blocks w, w+W, ... of 32 columns;
+// lane -> (row = lane % h, slice = lane / h), S = 32 / h
+// column slices; coefficients are gathered 32 at a time (phase-1 sums or x)
+// and broadcast by shuffles.  Slices, then warps, are summed in a fixed
+// order and each z row is written once.
 // ---------------------------------------------------------------------------
-template <int MU>
-__global__ void __launch_bounds__(32 * kP2Warps) phase2_kernel(const P2Item *__restrict__ items, int nitems, const P2Contrib *__restrict__ contrib, const LrLeaf *__restrict__ lr,
-                                                                const double *__restrict__ fac, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
-                                                                const int *__restrict__ xexp, int n64, int mu, int c0, const int *__restrict__ perm, double *__restrict__ y, int ldy) {
-    __shared__ double red[kP2Warps][32][MU];
+template <int MU, bool EMU, int W>
+__global__ void __launch_bounds__(256, MU >= 8 ? 2 : 4) phase2_kernel(const PanelItem *__restrict__ items, int nitems, const int *__restrict__ cidx, const double *__restrict__ fac, const double *__restrict__ A,
+                                                         const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen) {
+    constexpr int G = 8 / W; // row chunks in flight per CTA
+    __shared__ double red[8][32][MU];
     const int wid  = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    const int grp  = wid / W;
+    const int sub  = wid % W;
     const int xe   = max(*xexp, 1);
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const P2Item it = items[item];
-        const int h     = it.h;
-        const int S     = 32 / h;
-        const int row   = lane % h;
-        const int slice = lane / h;
-        const bool live = slice < S;
+    for (int item = blockIdx.x * G + grp; item < nitems; item += gridDim.x * G) {
+        const PanelItem it = items[item];
+        const int h        = it.h;
+        const int S        = 32 / h;
+        const int row      = lane % h;
+        const int slice    = lane / h;
+        const bool live    = slice < S;
+        const double *P    = fac + it.off + row;
+        const int *ci      = cidx + it.q0;
         double outv[MU];
-        if (wid < n64) {
+        if (!EMU) {
             double acc[MU];
 #pragma unroll
             for (int c = 0; c < MU; c++)
                 acc[c] = 0.;
-            P2Contrib nxt = it.cbeg + wid < it.cend ? contrib[it.cbeg + wid] : P2Contrib{0, 0, 0};
-            for (int ci = it.cbeg + wid; ci < it.cend; ci += kP2Warps) {
-                const P2Contrib pc = nxt;
-                if (ci + kP2Warps < it.cend) { // next descriptor and block on their way
-                    nxt = contrib[ci + kP2Warps];
-                    if (lane == 0)
-                        prefetch_l2(fac + nxt.off, (unsigned)((long long)h * nxt.w * 8));
+            for (int q0 = 32 * sub; q0 < it.ncol; q0 += 32 * W) { // column blocks sub, sub + W, ...
+                const int qc = min(32, it.ncol - q0);
+                double a[MU];
+                if (lane < qc) {
+                    const int k = ci[q0 + lane];
+#pragma unroll
+                    for (int c = 0; c < MU; c++)
+                        a[c] = k >= 0 ? A[(long long)k * mu + c0 + c] : xp[(long long)(~k) * mu + c0 + c];
+                } else {
+#pragma unroll
+                    for (int c = 0; c < MU; c++)
+                        a[c] = 0.;
                 }
-                const double *B = fac + pc.off + row;
-                for (int kb = 0; kb < pc.w; kb += 32) {
-                    const int kc = min(32, pc.w - kb);
-                    double a[MU];
-                    if (pc.aux >= 0) { // low-rank: a_k from phase 1, slot pc.aux
-                        const double *Ab = A + (long long)pc.aux * mu + c0;
-#pragma unroll
-                        for (int c = 0; c < MU; c++)
-                            a[c] = lane < kc ? Ab[(long long)(kb + lane) * mu + c] : 0.;
-                    } else { // dense: x
-                        const double *X = xp + (long long)(~pc.aux) * mu + c0;
-#pragma unroll
-                        for (int c = 0; c < MU; c++)
-                            a[c] = lane < kc ? X[(long long)(kb + lane) * mu + c] : 0.;
-                    }
 #pragma unroll 8
-                    for (int k0 = 0; k0 < kc; k0 += S) {
-                        const int k    = k0 + slice;
-                        const bool ok  = live && k < kc;
-                        const double u = ok ? B[(long long)h * (kb + k)] : 0.;
+                for (int j0 = 0; j0 < qc; j0 += S) {
+                    const int j    = j0 + slice;
+                    const bool ok  = live && j < qc;
+                    const double u = ok ? P[(long long)h * (q0 + j)] : 0.;
 #pragma unroll
-                        for (int c = 0; c < MU; c++)
-                            acc[c] = fma(u, __shfl_sync(0xffffffffu, a[c], ok ? k : 0), acc[c]);
-                    }
+                    for (int c = 0; c < MU; c++)
+                        acc[c] = fma(u, __shfl_sync(0xffffffffu, a[c], ok ? j : 0), acc[c]);
                 }
             }
-            for (int s = 1; s < S; s++)
-#pragma unroll
-                for (int c = 0; c < MU; c++) {
-                    const int src   = lane + s * h;
-                    const double vv = __shfl_sync(0xffffffffu, acc[c], src < 32 ? src : lane);
-                    if (slice == 0)
-                        acc[c] += vv;
-                }
 #pragma unroll
             for (int c = 0; c < MU; c++)
                 outv[c] = acc[c];
@@ -359,50 +346,40 @@ __global__ void __launch_bounds__(32 * kP2Warps) phase2_kernel(const P2Item *__r
 #pragma unroll
             for (int c = 0; c < MU; c++)
                 df_zero(acc[c]);
-            P2Contrib nxt = it.cbeg + wid < it.cend ? contrib[it.cbeg + wid] : P2Contrib{0, 0, 0};
-            for (int ci = it.cbeg + wid; ci < it.cend; ci += kP2Warps) {
-                const P2Contrib pc = nxt;
-                if (ci + kP2Warps < it.cend) {
-                    nxt = contrib[ci + kP2Warps];
-                    if (lane == 0)
-                        prefetch_l2(fac + nxt.off, (unsigned)((long long)h * nxt.w * 8));
-                }
-                const double *B = fac + pc.off + row;
-                for (int kb = 0; kb < pc.w; kb += 32) {
-                    const int kc = min(32, pc.w - kb);
-                    F2 a[MU];
-                    if (pc.aux >= 0) { // a_k, scaled to the units of x
-                        const double *Ab = A + (long long)pc.aux * mu + c0;
+            for (int q0 = 32 * sub; q0 < it.ncol; q0 += 32 * W) {
+                const int qc = min(32, it.ncol - q0);
+                F2 a[MU];
 #pragma unroll
-                        for (int c = 0; c < MU; c++) {
-                            const double av = lane < kc ? Ab[(long long)(kb + lane) * mu + c] : 0.;
-                            const int ex    = (int)(((unsigned)__double2hiint(av) >> 20) & 0x7FFu);
-                            a[c]            = (ex == 0 || ex + 1023 - xe < 1) ? F2{0.f, 0.f} : split64(scale_pow2(av, 1023 - xe));
-                        }
-                    } else {
-                        const F2 *X = xs + (long long)(~pc.aux) * mu + c0;
+                for (int c = 0; c < MU; c++)
+                    a[c] = F2{0.f, 0.f};
+                if (lane < qc) {
+                    const int k = ci[q0 + lane];
 #pragma unroll
-                        for (int c = 0; c < MU; c++)
-                            a[c] = lane < kc ? X[(long long)(kb + lane) * mu + c] : F2{0.f, 0.f};
+                    for (int c = 0; c < MU; c++) {
+                        if (k >= 0) // phase-1 sum, scaled to the units of x
+                            a[c] = split64(scale_pow2_safe(A[(long long)k * mu + c0 + c], 1023 - xe));
+                        else
+                            a[c] = xs[(long long)(~k) * mu + c0 + c];
                     }
+                }
 #pragma unroll 8
-                    for (int k0 = 0; k0 < kc; k0 += S) {
-                        const int k   = k0 + slice;
-                        const bool ok = live && k < kc;
-                        const F2 u    = split64(ok ? B[(long long)h * (kb + k)] : 0.);
+                for (int j0 = 0; j0 < qc; j0 += S) {
+                    const int j   = j0 + slice;
+                    const bool ok = live && j < qc;
+                    const F2 u    = split64(ok ? P[(long long)h * (q0 + j)] : 0.);
 #pragma unroll
-                        for (int c = 0; c < MU; c++) {
-                            F2 ak;
-                            ak.hi = __shfl_sync(0xffffffffu, a[c].hi, ok ? k : 0);
-                            ak.lo = __shfl_sync(0xffffffffu, a[c].lo, ok ? k : 0);
-                            df_fma(acc[c], u, ak);
-                        }
+                    for (int c = 0; c < MU; c++) {
+                        F2 ak;
+                        ak.hi = __shfl_sync(0xffffffffu, a[c].hi, ok ? j : 0);
+                        ak.lo = __shfl_sync(0xffffffffu, a[c].lo, ok ? j : 0);
+                        df_fma(acc[c], u, ak);
                     }
                 }
 #pragma unroll
                 for (int c = 0; c < MU; c++)
                     df_renorm(acc[c]);
             }
+            // slices in double-float, then to double in the units of x
             for (int s = 1; s < S; s++)
 #pragma unroll
                 for (int c = 0; c < MU; c++) {
@@ -415,25 +392,39 @@ __global__ void __launch_bounds__(32 * kP2Warps) phase2_kernel(const P2Item *__r
                 }
 #pragma unroll
             for (int c = 0; c < MU; c++)
-                outv[c] = slice == 0 ? scale_pow2(df_to_double(acc[c]), xe - 1023) : 0.;
+                outv[c] = slice == 0 ? scale_pow2_safe(df_to_double(acc[c]), xe - 1023) : 0.;
         }
-        if (slice == 0)
+        if (!EMU)
+            for (int s = 1; s < S; s++)
 #pragma unroll
-            for (int c = 0; c < MU; c++)
-                red[wid][row][c] = outv[c];
-        __syncthreads();
-        if (wid == 0 && lane < h) {
-            const int i   = it.row0 + lane;
-            const int dst = perm ? perm[i] : i;
+                for (int c = 0; c < MU; c++) {
+                    const int src   = lane + s * h;
+                    const double vv = __shfl_sync(0xffffffffu, outv[c], src < 32 ? src : lane);
+                    if (slice == 0)
+                        outv[c] += vv;
+                }
+        double *zr = z + (long long)c0 * zlen + it.row0;
+        if (W == 1) {
+            if (lane < h)
 #pragma unroll
-            for (int c = 0; c < MU; c++) {
-                double v = red[0][lane][c];
-                for (int q = 1; q < kP2Warps; q++)
-                    v += red[q][lane][c];
-                y[(long long)(c0 + c) * ldy + dst] = v;
-            }
+                for (int c = 0; c < MU; c++)
+                    zr[(long long)c * zlen + lane] = outv[c];
+        } else {
+            if (slice == 0)
+#pragma unroll
+                for (int c = 0; c < MU; c++)
+                    red[wid][row][c] = outv[c];
+            group_sync(grp, W);
+            if (sub == 0 && lane < h)
+#pragma unroll
+                for (int c = 0; c < MU; c++) {
+                    double v = red[wid][lane][c];
+                    for (int t = 1; t < W; t++)
+                        v += red[wid + t][lane][c];
+                    zr[(long long)c * zlen + lane] = v;
+                }
+            group_sync(grp, W);
         }
-        __syncthreads();
     }
 }
 
@@ -445,6 +436,26 @@ __global__ void block_copy_kernel(const BlockCopy *__restrict__ items, const dou
     for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
         const int i = (int)(e % b.rows), k = (int)(e / b.rows);
         dst[b.dst + e] = src[b.src + i + (long long)b.ld_src * k];
+    }
+}
+
+// y[c * ldy + perm[i]] = sum over the covering clusters (largest first) of z
+__global__ void zsum_kernel(const ZItem *__restrict__ items, int nitems, const int *__restrict__ zl, const double *__restrict__ z, int zlen, int mu, const int *__restrict__ perm,
+                            double *__restrict__ y, int ldy) {
+    const int w    = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= nitems)
+        return;
+    const ZItem it = items[w];
+    for (int r = lane; r < it.h; r += 32) {
+        const int i   = it.row0 + r;
+        const int dst = perm ? perm[i] : i;
+        for (int c = 0; c < mu; c++) {
+            double s = 0.;
+            for (int l = it.lbeg; l < it.lend; l++)
+                s += z[(long long)c * zlen + i + zl[l]];
+            y[(long long)c * ldy + dst] = s;
+        }
     }
 }
 
@@ -501,7 +512,7 @@ void launch_gather_split(const double *x, int ldx, const int *perm, int n, int m
 void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;
-    const int blocks = std::max(1, std::min((nitems + kWarpsPerBlock - 1) / kWarpsPerBlock, sm_count() * 8));
+    const int blocks = (nitems + kWarpsPerBlock - 1) / kWarpsPerBlock; // one warp per tile: the block scheduler balances uneven tiles
     for_rhs_groups(mu, [&](int c0, int g) {
 #define HTGPU_P1(G)                                                                                                                             \
     (emu ? phase1_kernel<G, true><<<blocks, 32 * kWarpsPerBlock, 0, st>>>(items, nitems, lr, factors, xp, xs, xexp, mu, c0, A)                 \
@@ -524,20 +535,36 @@ void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu,
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_phase2(const P2Item *items, int nitems, const P2Contrib *contrib, const LrLeaf *lr, const double *factors, const double *A, const double *xp, const F2 *xs, const int *xexp, int n64,
-                   int mu, const int *perm, double *y, int ldy, cudaStream_t st) {
+void launch_phase2(const PanelItem *items, int nitems, bool emu, int warps, const int *cidx, const double *factors, const double *A, const double *xp, const F2 *xs, const int *xexp, int mu,
+                   double *z, int zlen, cudaStream_t st) {
     if (nitems <= 0)
         return;
-    const int blocks = std::max(1, std::min(nitems, sm_count() * 16));
+    const int W      = warps >= 4 ? 4 : warps >= 2 ? 2 : 1;
+    const int G      = 8 / W;
+    const int blocks = (nitems + G - 1) / G; // one group per chunk: the block scheduler balances uneven panels
     for_rhs_groups(mu, [&](int c0, int g) {
+#define HTGPU_P2W(MU_, E_)                                                                                                              \
+    (W == 4 ? phase2_kernel<MU_, E_, 4><<<blocks, 256, 0, st>>>(items, nitems, cidx, factors, A, xp, xs, xexp, mu, c0, z, zlen)           \
+     : W == 2 ? phase2_kernel<MU_, E_, 2><<<blocks, 256, 0, st>>>(items, nitems, cidx, factors, A, xp, xs, xexp, mu, c0, z, zlen)         \
+              : phase2_kernel<MU_, E_, 1><<<blocks, 256, 0, st>>>(items, nitems, cidx, factors, A, xp, xs, xexp, mu, c0, z, zlen))
+#define HTGPU_P2(MU_) (emu ? HTGPU_P2W(MU_, true) : HTGPU_P2W(MU_, false))
         switch (g) {
-        case 8: phase2_kernel<8><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
-        case 4: phase2_kernel<4><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
-        case 2: phase2_kernel<2><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
-        default: phase2_kernel<1><<<blocks, 32 * kP2Warps, 0, st>>>(items, nitems, contrib, lr, factors, A, xp, xs, xexp, n64, mu, c0, perm, y, ldy); break;
+        case 8: HTGPU_P2(8); break;
+        case 4: HTGPU_P2(4); break;
+        case 2: HTGPU_P2(2); break;
+        default: HTGPU_P2(1); break;
         }
+#undef HTGPU_P2
+#undef HTGPU_P2W
         HTGPU_CUDA(cudaGetLastError());
     });
+}
+
+void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st) {
+    if (nitems <= 0)
+        return;
+    zsum_kernel<<<(nitems + 7) / 8, 256, 0, st>>>(items, nitems, zl, z, zlen, mu, perm, y, ldy);
+    HTGPU_CUDA(cudaGetLastError());
 }
 
 void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st) {

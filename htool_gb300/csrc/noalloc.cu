@@ -19,7 +19,8 @@ namespace htgpu {
 // 16 MiB of working memory per device, held by every GPU that loads the
 // library until the process exits.  A product needs 2 * nb_cols * mu
 // doubles for the gathered input and its float split, one slot for the
-// input's exponent, plus (phase-1 partial-sum slots) * mu doubles.
+// input's exponent, (phase-1 partial-sum slots) * mu doubles and
+// (per-cluster partial-sum rows) * mu doubles.
 constexpr std::size_t kNoAllocScratchDoubles = 2u * 1024u * 1024u;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
@@ -50,7 +51,7 @@ std::size_t HMatrix::noalloc_scratch_need(int mu) const {
     // gathered input and its split, each rounded up to 32 doubles (256
     // bytes), 32 doubles for the exponent word, then the partial sums
     const std::size_t xp_len = ((std::size_t)nc * mu + 31) / 32 * 32;
-    return 2 * xp_len + 32 + (std::size_t)std::max<long long>(a_slots, 1) * mu;
+    return 2 * xp_len + 32 + (std::size_t)std::max<long long>(a_slots, 1) * mu + (std::size_t)std::max<long long>(zlen_, 1) * mu;
 }
 
 void HMatrix::mvprod_noalloc(const double *in, double *out, int mu, cudaStream_t st) {
@@ -73,9 +74,10 @@ void HMatrix::mvprod_noalloc(const double *in, double *out, int mu, cudaStream_t
     F2 *xsw               = reinterpret_cast<F2 *>(base + xpl);
     int *xew              = reinterpret_cast<int *>(base + 2 * xpl);
     double *Aw            = base + 2 * xpl + 32;
+    double *zw            = Aw + (std::size_t)std::max<long long>(a_slots, 1) * mu;
     // the exponent word is cleared by launch_xexp (an asynchronous memset,
     // no allocation); every other entry is written before it is read
-    launch_product_with(in, out, mu, false, st, xpw, xsw, xew, Aw);
+    launch_product_with(in, out, mu, false, st, xpw, xsw, xew, Aw, zw);
 }
 
 } // namespace htgpu

@@ -149,16 +149,45 @@ int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
 
 /* How the FP64 product shares its work between the FP64 pipe (DFMA) and the
  * FP32/INT pipes (exact double-float emulation, ~2^-46 relative per term):
- * phase1_dfma_permille of the low-rank V-side elements and phase2_dfma_warps
- * of the 4 warps of every U-side/dense row chunk use DFMA.  No counterpart in
+ * phase1_dfma_permille of the low-rank V-side elements and
+ * phase2_dfma_permille of the U-side/dense elements use DFMA.  No counterpart in
  * the reference (its BLAS calls decide this, include/htool/types/matrix.hpp:320-383). */
-int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int phase1_dfma_permille, int phase2_dfma_warps);
-int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int *phase2_dfma_warps);
+int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int phase1_dfma_permille, int phase2_dfma_permille);
+int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int *phase2_dfma_permille);
 
-/* Autotuner: times `reps` products with mu right-hand sides for every
- * candidate FP64 split on this H-matrix and keeps the fastest; *best_ms is
- * its time per product.  Replaces nothing upstream (htool has no tuning). */
+/* Launch shape of phase 2 (the U-side/dense product per target row chunk):
+ * 1, 2 or 4 warps share one chunk's panel, for the DFMA panels, the
+ * emulated FP64 panels and the reduced-precision panels.  Results stay
+ * within the stated tolerances for every shape; the sums are split in a
+ * different order, so shapes differ in the last bits.  No counterpart in
+ * the reference. */
+int htgpu_hmatrix_set_phase2_warps(htgpu_hmatrix h, int dfma, int emulated, int reduced);
+int htgpu_hmatrix_get_phase2_warps(htgpu_hmatrix h, int *dfma, int *emulated, int *reduced);
+
+/* Autotuner: times `reps` products with mu right-hand sides on this
+ * H-matrix and keeps the fastest launch shape for the current storage
+ * policy -- with FP64 factors the warps per phase-2 row chunk and then the
+ * DFMA/emulation split, with reduced-precision factors the warps per
+ * phase-2 row chunk; *best_ms is its time per product.  Replaces nothing
+ * upstream (htool has no tuning). */
 int htgpu_hmatrix_autotune(htgpu_hmatrix h, int mu, int reps, float *best_ms);
+
+/* Storage of the low-rank factors used by the products (no counterpart in
+ * the reference, which is FP64/complex128 throughout): HTGPU_PREC_FP64,
+ * HTGPU_PREC_FP32, HTGPU_PREC_MIXED (per column: FP32 for the leading ACA
+ * crosses, BF16 for those whose bound max|u_k| max|v_k| sqrt(m n) is below
+ * tau * epsilon * (leaf bound) / 2^-9) or HTGPU_PREC_BF16.  Every column is
+ * stored divided by its maximum, with the product of the two maxima kept
+ * in FP64; dense leaves stay FP64; all sums are FP32 or wider.  The FP64
+ * factors are kept, so the policy can be switched back at any time. */
+#define HTGPU_PREC_FP64 0
+#define HTGPU_PREC_FP32 1
+#define HTGPU_PREC_MIXED 2
+#define HTGPU_PREC_BF16 3
+int htgpu_hmatrix_set_precision(htgpu_hmatrix h, int policy, double tau);
+/* Active policy, bytes of factors + dense blocks one product reads, and the
+ * number of FP32 and BF16 low-rank columns. */
+int htgpu_hmatrix_precision_info(htgpu_hmatrix h, int *policy, long long *stored_bytes, long long *fp32_columns, long long *bf16_columns);
 
 /* No counterpart in the reference.  The product of htgpu_hmatrix_mvprod for
  * device pointers, but allocation-free: it never calls cudaMalloc, cudaFree
@@ -168,8 +197,9 @@ int htgpu_hmatrix_autotune(htgpu_hmatrix h, int mu, int reps, float *best_ms);
  * the product from a hot loop.  Its working memory is one fixed 16 MiB
  * array per device inside the library (2^21 doubles, held by every GPU that
  * loads the library until the process exits); a product needs
- * 2 * nb_cols * mu (each half rounded up to 32) + 32 + (phase-1 partial sums)
- * * mu doubles, and larger requests fail with HTGPU_ERR_INVALID.  The first call on a device
+ * 2 * nb_cols * mu (each half rounded up to 32) + 32 + (phase-1 partial sums
+ * + per-cluster partial-sum rows) * mu doubles, and larger requests fail
+ * with HTGPU_ERR_INVALID.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that
  * device current, so make it before any stream capture.  Every call shares
  * the one array, whose contents persist between calls: calls that may

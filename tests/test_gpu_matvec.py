@@ -153,7 +153,7 @@ def test_bad_arguments():
         H.HMatrix(t, t, 1e-6, 10.0).set_leaves(bad, uv, dn, dd)
 
 
-@pytest.mark.parametrize("split", [(0, 0), (1000, 4), (350, 1), (0, 4), (1000, 0), (650, 2)])
+@pytest.mark.parametrize("split", [(0, 0), (1000, 1000), (350, 250), (0, 1000), (1000, 0), (650, 500)])
 @pytest.mark.parametrize("name", ["cyl4000_k0", "sphere6000_k1"])
 def test_fp64_split_parity(golden, name, split):
     """Every DFMA / FP32-pipe-emulation split of the FP64 product stays
@@ -167,7 +167,7 @@ def test_fp64_split_parity(golden, name, split):
         assert rel(GH.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < FP64_TOL
     x = G.rhs(g["xt"].shape[0], 9, seed=4)
     ref = GH.mvprod_global_to_global(x, 9)
-    GH.set_fp64_split(1000, 4)
+    GH.set_fp64_split(1000, 1000)
     assert rel(ref, GH.mvprod_global_to_global(x, 9)) < FP64_TOL
 
 
@@ -184,9 +184,34 @@ def test_fp64_emulation_input_scaling():
     for k in (-300, -80, 80, 300):
         yk = GH @ (x * 2.0 ** k)
         assert rel(yk * 2.0 ** -k, y) < 1e-13
-    GH.set_fp64_split(1000, 4)
+    GH.set_fp64_split(1000, 1000)
     assert rel(GH @ x, y) < FP64_TOL
     assert not np.any(GH @ np.zeros(5000))
+
+
+@pytest.mark.parametrize("warps", [1, 2, 4])
+def test_phase2_warps_parity(golden, warps):
+    """Every phase-2 launch shape (warps per row chunk) gives the reference
+    product: DFMA panels, emulated panels and reduced-precision panels."""
+    g, meta = golden("sphere6000_k1")
+    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    GH.set_phase2_warps(warps, warps, warps)
+    assert GH.get_phase2_warps() == (warps, warps, warps)
+    for split in ((1000, 1000), (0, 0), (650, 500)):
+        GH.set_fp64_split(*split)
+        for mu in (1, 3):
+            y = GH.mvprod_global_to_global(g["x_mu%d" % mu], mu)
+            assert rel(y, g["y_mu%d" % mu]) < FP64_TOL
+            assert np.array_equal(y, GH.mvprod_global_to_global(g["x_mu%d" % mu], mu))
+    x = G.rhs(g["xt"].shape[0], 9, seed=4)
+    GH.set_fp64_split(1000, 1000)
+    ref9 = GH.mvprod_global_to_global(x, 9)
+    GH.set_precision("mixed")
+    assert rel(GH.mvprod_global_to_global(x, 9), ref9) < 1e-6
+    assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-6
+    with pytest.raises(ValueError):
+        GH.set_phase2_warps(3, 1, 1)
 
 
 def test_autotune_keeps_parity(golden):
@@ -195,4 +220,33 @@ def test_autotune_keeps_parity(golden):
     GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
     ms = GH.autotune(1, 2)
     assert ms > 0
+    assert all(w in (1, 2, 4) for w in GH.get_phase2_warps())
     assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < FP64_TOL
+    GH.set_precision("mixed")
+    assert GH.autotune(1, 2) > 0
+    assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["cyl4000_k0", "sphere6000_k1"])
+def test_reduced_precision_products(golden, name):
+    """Low-rank factors in FP32 / FP32+BF16 per column (dense leaves FP64):
+    the product stays within 1e-6 of the FP64 product and reads fewer bytes;
+    switching back to FP64 restores the FP64 result exactly."""
+    g, meta = golden(name)
+    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    GH.set_fp64_split(1000, 1000)
+    base = GH.precision_info()["stored_bytes"]
+    ref = {mu: GH.mvprod_global_to_global(g["x_mu%d" % mu], mu) for mu in (1, 3)}
+    errs = {}
+    for policy, tol in (("fp32", 1e-6), ("mixed", 1e-6), ("bf16", 1e-1)):
+        GH.set_precision(policy)
+        info = GH.precision_info()
+        assert info["stored_bytes"] < base
+        for mu in (1, 3):
+            e = rel(GH.mvprod_global_to_global(g["x_mu%d" % mu], mu), ref[mu])
+            assert e < tol, (policy, mu, e)
+            errs[policy, mu] = e
+    assert errs["fp32", 1] < errs["bf16", 1]
+    GH.set_precision("fp64")
+    assert np.array_equal(GH.mvprod_global_to_global(g["x_mu1"]), ref[1])
