@@ -29,6 +29,7 @@ HOST_PTRS = 1
 CLUSTER_NUMBERING = 2
 
 PREC_FP64, PREC_FP32, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
+PHASE1_TILES, PHASE1_STREAM = 0, 1
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED, "bf16": PREC_BF16}
 
 _ERRORS = {1: ValueError, 2: NotImplementedError, 3: RuntimeError, 4: MemoryError, 5: RuntimeError}
@@ -65,8 +66,9 @@ def _load():
         "htgpu_hmatrix_profile": (i, [vp, i, i, vp]),
         "htgpu_hmatrix_set_fp64_split": (i, [vp, i, i]),
         "htgpu_hmatrix_get_fp64_split": (i, [vp, vp, vp]),
-        "htgpu_hmatrix_set_phase2_warps": (i, [vp, i, i, i]),
-        "htgpu_hmatrix_get_phase2_warps": (i, [vp, vp, vp, vp]),
+        "htgpu_hmatrix_set_phase1_mode": (i, [vp, i]),
+        "htgpu_hmatrix_get_phase1_mode": (i, [vp, vp]),
+        "htgpu_hmatrix_device_status": (i, [vp, vp]),
         "htgpu_hmatrix_autotune": (i, [vp, i, i, vp]),
         "htgpu_hmatrix_mvprod_noalloc": (i, [vp, vp, vp, i, vp]),
         "htgpu_hmatrix_set_precision": (i, [vp, i, d]),
@@ -293,15 +295,22 @@ class HMatrix:
         _check(lib.htgpu_hmatrix_precision_info(self.h, C.byref(p), C.byref(b), C.byref(f), C.byref(h)))
         return {"policy": p.value, "stored_bytes": b.value, "fp32_columns": f.value, "bf16_columns": h.value}
 
-    def set_phase2_warps(self, dfma, emulated, reduced):
-        """Warps (1, 2 or 4) sharing one phase-2 row chunk per panel kind."""
-        _check(lib.htgpu_hmatrix_set_phase2_warps(self.h, int(dfma), int(emulated), int(reduced)))
+    def set_phase1_mode(self, mode):
+        """Phase 1 with one or two right-hand sides: 'tiles' or 'stream'."""
+        m = {"tiles": PHASE1_TILES, "stream": PHASE1_STREAM}[mode] if isinstance(mode, str) else int(mode)
+        _check(lib.htgpu_hmatrix_set_phase1_mode(self.h, m))
         return self
 
-    def get_phase2_warps(self):
-        a, b, c = C.c_int(), C.c_int(), C.c_int()
-        _check(lib.htgpu_hmatrix_get_phase2_warps(self.h, C.byref(a), C.byref(b), C.byref(c)))
-        return (a.value, b.value, c.value)
+    def get_phase1_mode(self):
+        v = C.c_int()
+        _check(lib.htgpu_hmatrix_get_phase1_mode(self.h, C.byref(v)))
+        return v.value
+
+    def device_status(self):
+        """0, or the code of a device wait that ran out during a product."""
+        v = C.c_int()
+        _check(lib.htgpu_hmatrix_device_status(self.h, C.byref(v)))
+        return v.value
 
     def autotune(self, mu=1, reps=5):
         """Pick the fastest launch shape (and FP64 split) for this H-matrix and

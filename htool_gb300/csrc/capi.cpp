@@ -292,20 +292,26 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *p1, int *n64) {
     });
 }
 
-int htgpu_hmatrix_set_phase2_warps(htgpu_hmatrix h, int dfma, int emulated, int reduced) {
+int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode) {
     return guarded([&] {
         need(h, "hmatrix");
-        h->h->set_phase2_warps(dfma, emulated, reduced);
+        h->h->set_phase1_mode(mode);
     });
 }
 
-int htgpu_hmatrix_get_phase2_warps(htgpu_hmatrix h, int *dfma, int *emulated, int *reduced) {
+int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode) {
     return guarded([&] {
         need(h, "hmatrix");
-        need(dfma, "dfma");
-        need(emulated, "emulated");
-        need(reduced, "reduced");
-        h->h->get_phase2_warps(dfma, emulated, reduced);
+        need(mode, "mode");
+        *mode = h->h->phase1_mode();
+    });
+}
+
+int htgpu_hmatrix_device_status(htgpu_hmatrix h, int *status) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(status, "status");
+        *status = h->h->device_status();
     });
 }
 

@@ -14,6 +14,7 @@
 #include <chrono>
 #include <functional>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -577,9 +578,11 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     assign_phase1_modes();
     upload_phase1_lists();
     lr_d.upload(lr_h, stream_);
-    cidx_d.upload(cidx_h, stream_);
-    if (cidx_h.empty())
-        cidx_d.alloc(1);
+    {
+        std::vector<int> padded = cidx_h; // bulk copies read whole 16-byte words
+        padded.resize(cidx_h.size() + 4, 0);
+        cidx_d.upload(padded, stream_);
+    }
     zi_d.upload(zi_h, stream_);
     zl_d.upload(zl_h, stream_);
     if (zl_h.empty())
@@ -622,6 +625,9 @@ void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, bool
     if (host_ptrs) {
         HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * (std::size_t)nr * mu, cudaMemcpyDeviceToHost, st));
         HTGPU_CUDA(cudaStreamSynchronize(st));
+        int status = 0;
+        HTGPU_CUDA(cudaMemcpy(&status, status_d.p, sizeof(int), cudaMemcpyDeviceToHost));
+        require(status == 0, "a device wait of the product ran out (status " + std::to_string(status) + ")", 3);
     }
 }
 
@@ -651,26 +657,68 @@ void HMatrix::upload_phase1_lists() {
     n_p1_emu_  = (int)b.size();
     p1_d.upload(a, stream_);
     p1e_d.upload(b, stream_);
-    // phase-2 panels: DFMA for p2_permille_ / 1000 of the elements, spread by
-    // error diffusion through the launch
-    std::vector<PanelItem> pa, pb;
+    // the same tiles as chunks for the streamed phase 1
+    {
+        std::vector<StreamChunk> ch;
+        for (auto &it : p1_h) {
+            const LrLeaf &L = lr_h[it.leaf];
+            const int slot  = (int)(L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r);
+            tile_section(ch, 8 * it.off, 8, it.jlen, 0, L.r, slot, L.oj + it.j0, (int)L.a_off, (it.chunk & kEmuBit) ? kStreamEmu : kStreamDfma, true);
+        }
+        const std::vector<int> r = stream_ranges(ch, stream_ctas() * kStreamWarpsPerCta * 8);
+        n_p1_ranges_             = (int)r.size() - 1;
+        p1r_d.upload(r, stream_);
+        p1c_d.upload(ch, stream_);
+        if (ch.empty())
+            p1c_d.alloc(1);
+    }
     const double target = emu_ok_ ? p2_n64_ / 1000.0 : 1.0;
     long long seen = 0, dfma = 0;
+    // phase 2: DFMA for p2_n64_ / 1000 of the elements, chunk by chunk,
+    // spread by error diffusion through the stream
+    std::vector<StreamChunk> ch;
+    n_p2_dfma_ = n_p2_emu_ = 0;
     for (auto &pi : pan_h) {
-        const long long e = (long long)pi.h * pi.ncol;
-        seen += e;
-        if (target >= 1.0 || (double)dfma < target * (double)seen) {
-            dfma += e;
-            pa.push_back(pi);
-        } else {
-            pb.push_back(pi);
+        const std::size_t first = ch.size();
+        stream_section(ch, 8 * pi.off, 8, pi.h, pi.ncol, pi.q0, pi.row0, kStreamDfma, 0);
+        for (std::size_t k = first; k < ch.size(); k++) {
+            const long long e = (long long)ch[k].h * ch[k].ncol;
+            seen += e;
+            if (target >= 1.0 || (double)dfma < target * (double)seen)
+                dfma += e;
+            else
+                ch[k].kind = kStreamEmu;
         }
+        ch[first].flags |= kStreamFirst;
+        ch.back().flags |= kStreamLast;
+        (ch[first].kind == kStreamDfma ? n_p2_dfma_ : n_p2_emu_)++;
     }
-    n_p2_dfma_ = (int)pa.size();
-    n_p2_emu_  = (int)pb.size();
-    p2_d.upload(pa, stream_);
-    p2e_d.upload(pb, stream_);
+    n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
+    n_chunks_ = (long long)ch.size();
+    {
+        const std::vector<int> r = stream_ranges(ch, n_sctas_);
+        n_ranges_                = (int)r.size() - 1;
+        sr_d.upload(r, stream_);
+    }
+    sc_d.upload(ch, stream_);
+    if (ch.empty())
+        sc_d.alloc(1);
+    if (!status_d.p) {
+        status_d.alloc(1);
+        HTGPU_CUDA(cudaMemsetAsync(status_d.p, 0, sizeof(int), stream_));
+        tickets_d.alloc(16); // phase 2: 0..7, phase 1: 8
+    }
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+int HMatrix::device_status() {
+    HTGPU_CUDA(cudaSetDevice(device_));
+    int v = 0;
+    if (status_d.p) {
+        HTGPU_CUDA(cudaMemcpyAsync(&v, status_d.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    }
+    return v;
 }
 
 void HMatrix::set_fp64_split(int p1, int n64) {
@@ -815,10 +863,48 @@ void HMatrix::set_precision(int policy, double tau) {
         mixed_bytes_ += (4LL * c32[l] + 2LL * (lr_h[l].r - c32[l])) * (lr_h[l].m + lr_h[l].n);
     mix_.alloc(std::max<long long>(off, 16));
     scale_d.upload(scale, stream_);
+    {
+        std::vector<StreamChunk> ch;
+        for (auto &m : p1m) {
+            const LrLeaf &L = lr_h[m.leaf];
+            const int slot  = (int)(L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r);
+            const int c     = m.pad;
+            if (c > 0)
+                tile_section(ch, m.off, 4, m.jlen, 0, c, slot, L.oj + m.j0, (int)L.a_off, kStreamF32, true);
+            if (L.r > c)
+                tile_section(ch, m.off + 4LL * m.jlen * c, 2, m.jlen, c, L.r - c, slot, L.oj + m.j0, (int)L.a_off, kStreamBf16, c == 0);
+        }
+        const std::vector<int> r = stream_ranges(ch, stream_ctas() * kStreamWarpsPerCta * 8);
+        n_p1m_ranges_            = (int)r.size() - 1;
+        p1rm_d.upload(r, stream_);
+        p1cm_d.upload(ch, stream_);
+        if (ch.empty())
+            p1cm_d.alloc(1);
+    }
     p1m_d.upload(p1m, stream_);
     n_p1m_ = (int)p1m.size();
-    mit_d.upload(mit, stream_);
-    n_mit_ = (int)mit.size();
+    {
+        std::vector<StreamChunk> ch;
+        for (auto &mi : mit) {
+            const std::size_t first = ch.size();
+            if (mi.n64)
+                stream_section(ch, 8 * mi.off64, 8, mi.h, mi.n64, mi.q64, mi.row0, kStreamDfma, kStreamArena1);
+            if (mi.n32)
+                stream_section(ch, mi.off32, 4, mi.h, mi.n32, mi.q32, mi.row0, kStreamF32, 0);
+            if (mi.n16)
+                stream_section(ch, mi.off16, 2, mi.h, mi.n16, mi.q16, mi.row0, kStreamBf16, 0);
+            ch[first].flags |= kStreamFirst;
+            ch.back().flags |= kStreamLast;
+        }
+        n_chunks_m_ = (long long)ch.size();
+        scm_d.upload(ch, stream_);
+        const std::vector<int> r = stream_ranges(ch, n_sctas_);
+        n_ranges_m_              = (int)r.size() - 1;
+        srm_d.upload(r, stream_);
+        if (ch.empty())
+            scm_d.alloc(1);
+    }
+    cim.resize(cim.size() + 4, 0); // bulk copies read whole 16-byte words
     cidxm_d.upload(cim, stream_);
     if (p1m.empty())
         p1m_d.alloc(1);
@@ -844,7 +930,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
     if (marks)
         HTGPU_CUDA(cudaEventRecord(marks[0], st));
     if (precision_ != 0) {
-        if (n_p1m_) {
+        if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
+            launch_phase1_stream(p1cm_d.p, p1rm_d.p, n_p1m_ranges_, tickets_d.p + 8, mix_.p, w_xp, w_xs, scale_d.p, w_xexp, mu, w_A, status_d.p, st);
+            launches_ += 1;
+        } else if (n_p1m_) {
             launch_phase1_mixed(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, w_xexp, mu, w_A, st);
             launches_ += groups;
         }
@@ -854,12 +943,16 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         }
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
-        launch_phase2_mixed(mit_d.p, n_mit_, p2m_warps_, cidxm_d.p, mix_.p, fac.p, w_A, w_xp, w_xexp, mu, w_z, (int)zlen_, st);
+        launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_,
+                             status_d.p, st);
         launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
         launches_ += groups + 1;
         return;
     }
-    if (n_p1_dfma_ && n_p1_emu_) {
+    if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
+        launch_phase1_stream(p1c_d.p, p1r_d.p, n_p1_ranges_, tickets_d.p + 8, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
+        launches_ += 1;
+    } else if (n_p1_dfma_ && n_p1_emu_) {
         HTGPU_CUDA(cudaEventRecord(fork_, st));
         HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
         launch_phase1(p1_d.p, n_p1_dfma_, false, lr_d.p, fac.p, w_xp, w_xs, w_xexp, mu, w_A, st);
@@ -880,35 +973,18 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
     }
     if (marks)
         HTGPU_CUDA(cudaEventRecord(marks[1], st));
-    if (n_p2_dfma_ && n_p2_emu_) {
-        HTGPU_CUDA(cudaEventRecord(fork_, st));
-        HTGPU_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
-        launch_phase2(p2_d.p, n_p2_dfma_, false, p2_warps_, cidx_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, st);
-        launch_phase2(p2e_d.p, n_p2_emu_, true, p2e_warps_, cidx_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, aux_);
-        HTGPU_CUDA(cudaEventRecord(join_, aux_));
-        HTGPU_CUDA(cudaStreamWaitEvent(st, join_, 0));
-        launches_ += 2 * groups;
-    } else if (n_p2_dfma_ || n_p2_emu_) {
-        const bool emu = n_p2_dfma_ == 0;
-        launch_phase2(emu ? p2e_d.p : p2_d.p, emu ? n_p2_emu_ : n_p2_dfma_, emu, emu ? p2e_warps_ : p2_warps_, cidx_d.p, fac.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, st);
+    {
+        const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
+        launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         launches_ += groups;
     }
     launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
     launches_ += 1;
 }
 
-void HMatrix::set_phase2_warps(int dfma, int emulated, int reduced) {
-    auto ok = [](int w) { return w == 1 || w == 2 || w == 4; };
-    require(ok(dfma) && ok(emulated) && ok(reduced), "warps per phase-2 row chunk must be 1, 2 or 4");
-    p2_warps_  = dfma;
-    p2e_warps_ = emulated;
-    p2m_warps_ = reduced;
-}
-
-void HMatrix::get_phase2_warps(int *dfma, int *emulated, int *reduced) const {
-    *dfma     = p2_warps_;
-    *emulated = p2e_warps_;
-    *reduced  = p2m_warps_;
+void HMatrix::set_phase1_mode(int mode) {
+    require(mode == 0 || mode == 1, "phase-1 mode must be 0 (tile kernels) or 1 (streamed chunks)");
+    p1_mode_ = mode;
 }
 
 void HMatrix::autotune(int mu, int reps, float *best_ms) {
@@ -946,34 +1022,30 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
     };
     float best = 1e30f;
     if (precision_ != 0) {
-        best = pick(p2m_warps_, {1, 2, 4});
+        best = pick(p1_mode_, {0, 1});
     } else {
-        // warps per phase-2 row chunk for the DFMA and the emulated panel
-        // lists, each timed with the whole phase 2 on its own pipe
-        const int p1 = p1_permille_, p2 = p2_n64_;
-        set_fp64_split(p1, 1000);
-        best = pick(p2_warps_, {1, 2, 4});
-        if (emu_ok_) {
-            set_fp64_split(p1, 0);
-            pick(p2e_warps_, {1, 2, 4});
-        }
-        std::vector<std::pair<int, int>> cands;
+        // every phase-1 mode with every DFMA/emulation split
+        std::vector<std::pair<int, int>> splits;
         if (!emu_ok_)
-            cands.push_back({1000, 1000});
+            splits.push_back({1000, 1000});
         else
             for (int q1 : {0, 350, 650, 1000})
                 for (int q2 : {0, 350, 650, 1000})
-                    cands.push_back({q1, q2});
-        std::pair<int, int> arg = {p1, p2};
-        best                    = 1e30f;
-        for (auto &c : cands) {
-            set_fp64_split(c.first, c.second);
-            const float ms = timed();
-            if (ms < best) {
-                best = ms;
-                arg  = c;
+                    splits.push_back({q1, q2});
+        int arg_mode             = p1_mode_;
+        std::pair<int, int> arg = {p1_permille_, p2_n64_};
+        for (int mode : {0, 1})
+            for (auto &c : splits) {
+                p1_mode_ = mode;
+                set_fp64_split(c.first, c.second);
+                const float ms = timed();
+                if (ms < best) {
+                    best     = ms;
+                    arg_mode = mode;
+                    arg      = c;
+                }
             }
-        }
+        p1_mode_ = arg_mode;
         set_fp64_split(arg.first, arg.second);
     }
     cudaEventDestroy(e0);
@@ -1169,9 +1241,9 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["GPU_bf16_columns"]           = inum(n_bf16_cols_);
     m["GPU_fp64_phase1_dfma_permille"] = inum(emu_ok_ ? p1_permille_ : 1000);
     m["GPU_fp64_phase2_dfma_permille"] = inum(emu_ok_ ? p2_n64_ : 1000);
-    m["GPU_phase2_warps_dfma"]         = inum(p2_warps_);
-    m["GPU_phase2_warps_emulated"]     = inum(p2e_warps_);
-    m["GPU_phase2_warps_reduced"]      = inum(p2m_warps_);
+    m["GPU_phase2_stream_chunks"]      = inum(precision_ ? n_chunks_m_ : n_chunks_);
+    m["GPU_phase2_stream_ranges"]      = inum(precision_ ? n_ranges_m_ : n_ranges_);
+    m["GPU_phase1_mode"]               = inum(p1_mode_);
     return m;
 }
 

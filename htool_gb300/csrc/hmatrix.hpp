@@ -60,13 +60,18 @@ class HMatrix {
     // stored entries are too large for it (then everything uses DFMA).
     void set_fp64_split(int phase1_dfma_permille, int phase2_dfma_permille);
     void get_fp64_split(int *phase1_dfma_permille, int *phase2_dfma_permille) const;
-    void set_phase2_warps(int dfma, int emulated, int reduced);
-    void get_phase2_warps(int *dfma, int *emulated, int *reduced) const;
+    // phase 1 for one or two right-hand sides: 0 tile kernels (one warp per
+    // tile, DFMA and emulated tiles on two streams), 1 streamed chunks
+    void set_phase1_mode(int mode);
+    int phase1_mode() const { return p1_mode_; }
     bool emulation_allowed() const { return emu_ok_; }
     // time every candidate split on the current H-matrix and keep the fastest
-    // FP64: warps per phase-2 chunk, then the DFMA/emulation split;
-    // reduced precision: warps per phase-2 chunk
+    // FP64: phase-1 mode and the DFMA/emulation split; reduced precision:
+    // phase-1 mode
     void autotune(int mu, int reps, float *best_ms);
+    // nonzero when a bounded device wait of a product ran out (1 producer,
+    // 2 consumer, 3 drain); reading it synchronises the H-matrix's stream
+    int device_status();
 
     // factor storage used by products: 0 FP64, 1 FP32, 2 FP32/BF16 per
     // column (BF16 where the column's bound is below tau * eps of the leaf),
@@ -112,7 +117,6 @@ class HMatrix {
     DevBuf<double> fac; // every factor and dense block, in work-item order
     DevBuf<LrLeaf> lr_d;
     DevBuf<P1Item> p1_d;
-    DevBuf<PanelItem> p2_d;
     DevBuf<double> xp, A, z, xstage, ystage;
     DevBuf<ZItem> zi_d;
     DevBuf<int> zl_d;
@@ -120,9 +124,6 @@ class HMatrix {
     DevBuf<int> xexp, multi_d;
     std::vector<int> multi_h;
     int p1_permille_ = 300, p2_n64_ = 1;
-    // warps sharing one phase-2 row chunk: DFMA panels, emulated panels,
-    // reduced-precision panels
-    int p2_warps_ = 2, p2e_warps_ = 1, p2m_warps_ = 1;
     bool emu_ok_ = false;
     void launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st);
     void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr);
@@ -131,10 +132,8 @@ class HMatrix {
     int n_p1_dfma_ = 0, n_p1_emu_ = 0;
     std::vector<PanelItem> pan_h; // phase-2 panels (one per P2Item)
     std::vector<int> cidx_h;      // panel column coefficients
-    DevBuf<PanelItem> p2e_d;      // phase-2 panels on the emulation (p2_d: on DFMA)
     DevBuf<int> cidx_d, cidxm_d;
-    DevBuf<MixedItem> mit_d;
-    int n_p2_dfma_ = 0, n_p2_emu_ = 0, n_mit_ = 0;
+    int n_p2_dfma_ = 0, n_p2_emu_ = 0; // phase-2 panels by kind of their first chunk
     cudaStream_t aux_ = nullptr;
     int precision_ = 0;
     double tau_    = 0.25;
@@ -144,6 +143,16 @@ class HMatrix {
     int n_p1m_ = 0;
     long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    // streamed phase 2: chunk lists and CTA ranges for the FP64 factors and
+    // for the reduced-precision ones; device status of the bounded waits
+    DevBuf<StreamChunk> sc_d, scm_d;
+    DevBuf<int> sr_d, srm_d, status_d, tickets_d;
+    int n_sctas_ = 0, n_ranges_ = 0, n_ranges_m_ = 0;
+    long long n_chunks_ = 0, n_chunks_m_ = 0;
+    int p1_mode_ = 0;
+    DevBuf<StreamChunk> p1c_d, p1cm_d; // streamed phase 1 (one or two right-hand sides)
+    DevBuf<int> p1r_d, p1rm_d;
+    int n_p1_ranges_ = 0, n_p1m_ranges_ = 0;
     int mu_cap = 0;
     int launches_ = 0;
     BuildStats st_;

@@ -100,16 +100,35 @@ struct P2Item { // host record of one phase-2 row chunk: leaf blocks [cbeg, cend
     int row0, h, cbeg, cend;
 };
 
-struct PanelItem { // one warp: z rows row0 .. row0+h += panel (h x ncol, column-major, ld h)
+struct PanelItem { // z rows row0 .. row0+h += panel (h x ncol, column-major, ld h)
     long long off; // at off, times coefficients coef[cidx[q0 + q]] (cidx >= 0: phase-1
     int row0, h;   // slot; < 0: x index ~cidx)
     int q0, ncol;
 };
 
-struct MixedItem { // reduced-precision phase 2: dense FP64 columns, FP32 columns, BF16 columns
+struct MixedItem { // a reduced-precision phase-2 panel: dense FP64 columns, FP32 columns, BF16 columns
     long long off64, off32, off16; // FP64 arena (elements), reduced arena (bytes) x2
     int row0, h;
     int q64, n64, q32, n32, q16, n16; // column index ranges in cidx
+};
+
+// Streamed products: one chunk = up to kStreamCols columns of one phase-2
+// row chunk's panel, or up to 16 whole columns of one phase-1 tile; all of
+// one element kind, contiguous in an arena
+enum StreamKind : unsigned char { kStreamDfma = 0, kStreamEmu = 1, kStreamF32 = 2, kStreamBf16 = 3 };
+enum StreamFlag : unsigned char { kStreamFirst = 1, kStreamLast = 2, kStreamArena1 = 4 }; // first / last chunk of a row chunk (phase 2) or tile (phase 1)
+constexpr int kStreamStage = 4096; // bytes of one chunk (one pipeline stage)
+constexpr int kStreamCols  = 64;   // columns of one chunk
+struct StreamChunk {
+    long long src;   // byte offset of the chunk in its arena (element aligned)
+    int bytes;       // h * ncol * element size, <= kStreamStage
+    int a;           // phase 2: first column in the coefficient index list;
+                     // phase 1: A slot of the chunk's first column
+    int b;           // phase 2: z row of the first row; phase 1: first x row
+    int c;           // phase 1: per-column scale index of the first column
+    int h, ncol;     // rows (phase 2: <= 32, phase 1: <= 256), columns
+    unsigned char kind, flags;
+    unsigned short pad;
 };
 
 struct ZItem { // cluster rows row0 .. row0+h: y[perm[i]] = sum over l of z[i + zl[l]], l in [lbeg, lend)

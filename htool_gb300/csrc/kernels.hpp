@@ -2,6 +2,8 @@
 #pragma once
 #include "htgpu_internal.hpp"
 
+#include <vector>
+
 namespace htgpu {
 
 // ---- assembly -------------------------------------------------------------
@@ -39,12 +41,31 @@ void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st);
 void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st);
 void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
 void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st);
-// warps: 1, 2 or 4 warps share one row chunk's panel
-void launch_phase2(const PanelItem *items, int nitems, bool emu, int warps, const int *cidx, const double *factors, const double *A, const double *xp, const F2 *xs, const int *xexp, int mu,
-                   double *z, int zlen, cudaStream_t st);
 void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st);
 // y[c * ldy + perm[i]] = sum of the partial sums z of the clusters covering row i
 void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st);
+
+// ---- streamed phase 2 (stream.cu) ------------------------------------------
+// warps claim the chunk ranges rbeg[r] .. rbeg[r+1] (r < nranges) through
+// tickets (8 ints, reset by the launch); chunk bytes at arena0 (or arena1
+// with kStreamArena1); status: nonzero after a wait ran out
+constexpr int kStreamWarpsPerCta = 4;
+int stream_ctas(); // CTAs per launch (all resident)
+void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
+// phase 1 with one or two right-hand sides: tile chunks (kStreamFirst on a
+// tile's first chunk), A slots written directly (tiles of multi-tile leaves
+// still need launch_reduce_tiles); scale: per-column factors (F32/BF16 kinds)
+void launch_phase1_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+                          const int *xexp, int mu, double *A, int *status, cudaStream_t st);
+// append the chunks of columns k0 .. k0+n of one tile (jlen rows, elements
+// of es bytes; column k0 at byte src): A slots slot + k, scale slots sidx + k
+void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile);
+// append the chunks of one panel section (h x n elements of es bytes at byte src)
+void stream_section(std::vector<StreamChunk> &out, long long src, int es, int h, int n, int q0, int row0, unsigned char kind, unsigned char flags);
+// about nranges ranges over a chunk list (row chunks kept whole, none
+// empty), balanced by cost; returns their nranges' + 1 bounds
+std::vector<int> stream_ranges(const std::vector<StreamChunk> &chunks, int nranges);
 
 // ---- mixed precision (mixed.cu) --------------------------------------------
 struct ColMaxJob { // FP64 block rows x cols (ld rows) at off: column maxima -> cmax[slot + k]
@@ -58,7 +79,4 @@ struct ConvertJob { // FP64 block at src (elements) -> FP32 columns at dst32, BF
 void launch_colmax(const ColMaxJob *jobs, int njobs, const double *fac, unsigned *cmax, cudaStream_t st);
 void launch_convert(const ConvertJob *jobs, int njobs, const double *fac, const unsigned *cmax, unsigned char *mix, cudaStream_t st);
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
-void launch_phase2_mixed(const MixedItem *items, int nitems, int warps, const int *cidx, const unsigned char *mix, const double *fac, const double *A, const double *xp, const int *xexp, int mu,
-                         double *z, int zlen, cudaStream_t st);
-
 } // namespace htgpu

@@ -34,13 +34,6 @@ namespace {
 
 constexpr int kWarpsPerBlock = 8; // phase 1: warps per CTA
 
-__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
-    // TMA bulk prefetch of a contiguous, 16-byte-aligned range into L2
-    bytes = (bytes + 15u) & ~15u;
-    if (bytes)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
 // biased exponent of max |x| over the input (atomicMax on the exponent field)
 __global__ void xexp_kernel(const double *__restrict__ x, long long total, int *__restrict__ xexp) {
     int m = 0;
@@ -280,154 +273,6 @@ __global__ void reduce_tiles_kernel(const LrLeaf *__restrict__ lr, const int *__
     }
 }
 
-// ---------------------------------------------------------------------------
-// phase 2: W warps per row chunk (8 / W chunks per CTA at a time); the
-// chunk's leaves are ONE contiguous panel h x ncol (every covering leaf's
-// columns side by side) and the product is a streaming GEMV: warp w of a
-// chunk takes the column blocks w, w+W, ... of 32 columns;
-// lane -> (row = lane % h, slice = lane / h), S = 32 / h
-// column slices; coefficients are gathered 32 at a time (phase-1 sums or x)
-// and broadcast by shuffles.  Slices, then warps, are summed in a fixed
-// order and each z row is written once.
-// ---------------------------------------------------------------------------
-template <int MU, bool EMU, int W>
-__global__ void __launch_bounds__(256, MU >= 8 ? 2 : 4) phase2_kernel(const PanelItem *__restrict__ items, int nitems, const int *__restrict__ cidx, const double *__restrict__ fac, const double *__restrict__ A,
-                                                         const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen) {
-    constexpr int G = 8 / W; // row chunks in flight per CTA
-    __shared__ double red[8][32][MU];
-    const int wid  = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const int grp  = wid / W;
-    const int sub  = wid % W;
-    const int xe   = max(*xexp, 1);
-    for (int item = blockIdx.x * G + grp; item < nitems; item += gridDim.x * G) {
-        const PanelItem it = items[item];
-        const int h        = it.h;
-        const int S        = 32 / h;
-        const int row      = lane % h;
-        const int slice    = lane / h;
-        const bool live    = slice < S;
-        const double *P    = fac + it.off + row;
-        const int *ci      = cidx + it.q0;
-        double outv[MU];
-        if (!EMU) {
-            double acc[MU];
-#pragma unroll
-            for (int c = 0; c < MU; c++)
-                acc[c] = 0.;
-            for (int q0 = 32 * sub; q0 < it.ncol; q0 += 32 * W) { // column blocks sub, sub + W, ...
-                const int qc = min(32, it.ncol - q0);
-                double a[MU];
-                if (lane < qc) {
-                    const int k = ci[q0 + lane];
-#pragma unroll
-                    for (int c = 0; c < MU; c++)
-                        a[c] = k >= 0 ? A[(long long)k * mu + c0 + c] : xp[(long long)(~k) * mu + c0 + c];
-                } else {
-#pragma unroll
-                    for (int c = 0; c < MU; c++)
-                        a[c] = 0.;
-                }
-#pragma unroll 8
-                for (int j0 = 0; j0 < qc; j0 += S) {
-                    const int j    = j0 + slice;
-                    const bool ok  = live && j < qc;
-                    const double u = ok ? P[(long long)h * (q0 + j)] : 0.;
-#pragma unroll
-                    for (int c = 0; c < MU; c++)
-                        acc[c] = fma(u, __shfl_sync(0xffffffffu, a[c], ok ? j : 0), acc[c]);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < MU; c++)
-                outv[c] = acc[c];
-        } else {
-            DF acc[MU];
-#pragma unroll
-            for (int c = 0; c < MU; c++)
-                df_zero(acc[c]);
-            for (int q0 = 32 * sub; q0 < it.ncol; q0 += 32 * W) {
-                const int qc = min(32, it.ncol - q0);
-                F2 a[MU];
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    a[c] = F2{0.f, 0.f};
-                if (lane < qc) {
-                    const int k = ci[q0 + lane];
-#pragma unroll
-                    for (int c = 0; c < MU; c++) {
-                        if (k >= 0) // phase-1 sum, scaled to the units of x
-                            a[c] = split64(scale_pow2_safe(A[(long long)k * mu + c0 + c], 1023 - xe));
-                        else
-                            a[c] = xs[(long long)(~k) * mu + c0 + c];
-                    }
-                }
-#pragma unroll 8
-                for (int j0 = 0; j0 < qc; j0 += S) {
-                    const int j   = j0 + slice;
-                    const bool ok = live && j < qc;
-                    const F2 u    = split64(ok ? P[(long long)h * (q0 + j)] : 0.);
-#pragma unroll
-                    for (int c = 0; c < MU; c++) {
-                        F2 ak;
-                        ak.hi = __shfl_sync(0xffffffffu, a[c].hi, ok ? j : 0);
-                        ak.lo = __shfl_sync(0xffffffffu, a[c].lo, ok ? j : 0);
-                        df_fma(acc[c], u, ak);
-                    }
-                }
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    df_renorm(acc[c]);
-            }
-            // slices in double-float, then to double in the units of x
-            for (int s = 1; s < S; s++)
-#pragma unroll
-                for (int c = 0; c < MU; c++) {
-                    const int src = lane + s * h;
-                    DF v;
-                    v.s = __shfl_sync(0xffffffffu, acc[c].s, src < 32 ? src : lane);
-                    v.c = __shfl_sync(0xffffffffu, acc[c].c, src < 32 ? src : lane);
-                    if (slice == 0)
-                        acc[c] = df_add(acc[c], v);
-                }
-#pragma unroll
-            for (int c = 0; c < MU; c++)
-                outv[c] = slice == 0 ? scale_pow2_safe(df_to_double(acc[c]), xe - 1023) : 0.;
-        }
-        if (!EMU)
-            for (int s = 1; s < S; s++)
-#pragma unroll
-                for (int c = 0; c < MU; c++) {
-                    const int src   = lane + s * h;
-                    const double vv = __shfl_sync(0xffffffffu, outv[c], src < 32 ? src : lane);
-                    if (slice == 0)
-                        outv[c] += vv;
-                }
-        double *zr = z + (long long)c0 * zlen + it.row0;
-        if (W == 1) {
-            if (lane < h)
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    zr[(long long)c * zlen + lane] = outv[c];
-        } else {
-            if (slice == 0)
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    red[wid][row][c] = outv[c];
-            group_sync(grp, W);
-            if (sub == 0 && lane < h)
-#pragma unroll
-                for (int c = 0; c < MU; c++) {
-                    double v = red[wid][lane][c];
-                    for (int t = 1; t < W; t++)
-                        v += red[wid + t][lane][c];
-                    zr[(long long)c * zlen + lane] = v;
-                }
-            group_sync(grp, W);
-        }
-    }
-}
-
 // copy a rows x cols column-major block (leading dimension ld_src) into a
 // contiguous rows x cols block (leading dimension rows)
 __global__ void block_copy_kernel(const BlockCopy *__restrict__ items, const double *__restrict__ src, double *__restrict__ dst) {
@@ -533,31 +378,6 @@ void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu,
         return;
     reduce_tiles_kernel<<<nmulti, 128, 0, st>>>(lr, multi, nmulti, mu, A);
     HTGPU_CUDA(cudaGetLastError());
-}
-
-void launch_phase2(const PanelItem *items, int nitems, bool emu, int warps, const int *cidx, const double *factors, const double *A, const double *xp, const F2 *xs, const int *xexp, int mu,
-                   double *z, int zlen, cudaStream_t st) {
-    if (nitems <= 0)
-        return;
-    const int W      = warps >= 4 ? 4 : warps >= 2 ? 2 : 1;
-    const int G      = 8 / W;
-    const int blocks = (nitems + G - 1) / G; // one group per chunk: the block scheduler balances uneven panels
-    for_rhs_groups(mu, [&](int c0, int g) {
-#define HTGPU_P2W(MU_, E_)                                                                                                              \
-    (W == 4 ? phase2_kernel<MU_, E_, 4><<<blocks, 256, 0, st>>>(items, nitems, cidx, factors, A, xp, xs, xexp, mu, c0, z, zlen)           \
-     : W == 2 ? phase2_kernel<MU_, E_, 2><<<blocks, 256, 0, st>>>(items, nitems, cidx, factors, A, xp, xs, xexp, mu, c0, z, zlen)         \
-              : phase2_kernel<MU_, E_, 1><<<blocks, 256, 0, st>>>(items, nitems, cidx, factors, A, xp, xs, xexp, mu, c0, z, zlen))
-#define HTGPU_P2(MU_) (emu ? HTGPU_P2W(MU_, true) : HTGPU_P2W(MU_, false))
-        switch (g) {
-        case 8: HTGPU_P2(8); break;
-        case 4: HTGPU_P2(4); break;
-        case 2: HTGPU_P2(2); break;
-        default: HTGPU_P2(1); break;
-        }
-#undef HTGPU_P2
-#undef HTGPU_P2W
-        HTGPU_CUDA(cudaGetLastError());
-    });
 }
 
 void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st) {

@@ -7,9 +7,9 @@
 // FP32; from the first column whose bound s_k * sqrt(m n) falls below
 // tau * eps * (leaf bound) / 2^-9 on, columns are BF16 -- the storage error
 // of a BF16 column (relative 2^-9) then stays below tau * eps of the leaf.
-// Products and per-contribution sums are FP32; phase-1 results are FP64,
-// phase-2 contributions are folded into double-float accumulators, dense
-// leaves use DFMA on their FP64 blocks.
+// Products and per-contribution sums are FP32; phase-1 results are FP64;
+// phase 2 (stream.cu) folds its FP32 partial sums into double-float
+// accumulators and uses DFMA on the dense leaves' FP64 blocks.
 #include "df64.cuh"
 #include "kernels.hpp"
 
@@ -164,141 +164,6 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
     }
 }
 
-// DF accumulator += float
-__device__ __forceinline__ void df_addf(DF &a, float p) {
-    const float s   = a.s + p;
-    const float bp  = s - a.s;
-    const float err = (a.s - (s - bp)) + (p - bp);
-    a.s             = s;
-    a.c += err;
-}
-
-// Phase 2: W warps per row chunk (8 / W chunks per CTA at a time), three
-// contiguous sub-panels: the dense leaves' FP64 columns (DFMA against x),
-// the FP32 and the BF16 low-rank columns (FP32 FMAs against the phase-1
-// sums, folded into a double-float accumulator every 32 columns); warp w of
-// a chunk takes the column blocks w, w+W, ... of each sub-panel; the warps'
-// results are summed in a fixed order
-template <int MU, typename T>
-__device__ __forceinline__ void panel_f32(const T *__restrict__ P, int h, int ncol, const int *__restrict__ ci, const double *__restrict__ A, int mu, int c0, int xe, int lane, int row, int slice,
-                                          bool live, int S, int sub, int W, DF (&acc)[MU]) {
-    for (int q0 = 32 * sub; q0 < ncol; q0 += 32 * W) {
-        const int qc = min(32, ncol - q0);
-        float a[MU];
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            a[c] = lane < qc ? (float)scale_pow2_safe(A[(long long)ci[q0 + lane] * mu + c0 + c], 1023 - xe) : 0.f;
-        float part[MU];
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            part[c] = 0.f;
-#pragma unroll 8
-        for (int j0 = 0; j0 < qc; j0 += S) {
-            const int j   = j0 + slice;
-            const bool ok = live && j < qc;
-            float u       = 0.f;
-            if (ok) {
-                if (sizeof(T) == 4)
-                    u = (float)P[(long long)h * (q0 + j)];
-                else
-                    u = bf16_to_f32((unsigned short)P[(long long)h * (q0 + j)]);
-            }
-#pragma unroll
-            for (int c = 0; c < MU; c++)
-                part[c] = fmaf(u, __shfl_sync(0xffffffffu, a[c], ok ? j : 0), part[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            df_addf(acc[c], part[c]);
-    }
-}
-
-template <int MU, int W>
-__global__ void __launch_bounds__(256, MU >= 8 ? 2 : 4) phase2_mixed_kernel(const MixedItem *__restrict__ items, int nitems, const int *__restrict__ cidx, const unsigned char *__restrict__ mix,
-                                                               const double *__restrict__ fac, const double *__restrict__ A, const double *__restrict__ xp, const int *__restrict__ xexp, int mu,
-                                                               int c0, double *__restrict__ z, int zlen) {
-    constexpr int G = 8 / W; // row chunks in flight per CTA
-    __shared__ double red[8][32][MU];
-    const int wid  = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const int grp  = wid / W;
-    const int sub  = wid % W;
-    const int xe   = max(*xexp, 1);
-    for (int item = blockIdx.x * G + grp; item < nitems; item += gridDim.x * G) {
-        const MixedItem it = items[item];
-        const int h        = it.h;
-        const int S        = 32 / h;
-        const int row      = lane % h;
-        const int slice    = lane / h;
-        const bool live    = slice < S;
-        // dense leaves: FP64 panel, DFMA
-        double dacc[MU];
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            dacc[c] = 0.;
-        {
-            const double *P = fac + it.off64 + row;
-            const int *ci   = cidx + it.q64;
-            for (int q0 = 32 * sub; q0 < it.n64; q0 += 32 * W) {
-                const int qc = min(32, it.n64 - q0);
-                double a[MU];
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    a[c] = lane < qc ? xp[(long long)(~ci[q0 + lane]) * mu + c0 + c] : 0.;
-#pragma unroll 8
-                for (int j0 = 0; j0 < qc; j0 += S) {
-                    const int j    = j0 + slice;
-                    const bool ok  = live && j < qc;
-                    const double u = ok ? P[(long long)h * (q0 + j)] : 0.;
-#pragma unroll
-                    for (int c = 0; c < MU; c++)
-                        dacc[c] = fma(u, __shfl_sync(0xffffffffu, a[c], ok ? j : 0), dacc[c]);
-                }
-            }
-        }
-        DF acc[MU];
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            df_zero(acc[c]);
-        panel_f32<MU, float>(reinterpret_cast<const float *>(mix + it.off32) + row, h, it.n32, cidx + it.q32, A, mu, c0, xe, lane, row, slice, live, S, sub, W, acc);
-        panel_f32<MU, unsigned short>(reinterpret_cast<const unsigned short *>(mix + it.off16) + row, h, it.n16, cidx + it.q16, A, mu, c0, xe, lane, row, slice, live, S, sub, W, acc);
-        double outv[MU];
-#pragma unroll
-        for (int c = 0; c < MU; c++)
-            outv[c] = scale_pow2_safe(df_to_double(acc[c]), xe - 1023) + dacc[c];
-        for (int s = 1; s < S; s++)
-#pragma unroll
-            for (int c = 0; c < MU; c++) {
-                const int src   = lane + s * h;
-                const double vv = __shfl_sync(0xffffffffu, outv[c], src < 32 ? src : lane);
-                if (slice == 0)
-                    outv[c] += vv;
-            }
-        double *zr = z + (long long)c0 * zlen + it.row0;
-        if (W == 1) {
-            if (lane < h)
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    zr[(long long)c * zlen + lane] = outv[c];
-        } else {
-            if (slice == 0)
-#pragma unroll
-                for (int c = 0; c < MU; c++)
-                    red[wid][row][c] = outv[c];
-            group_sync(grp, W);
-            if (sub == 0 && lane < h)
-#pragma unroll
-                for (int c = 0; c < MU; c++) {
-                    double v = red[wid][lane][c];
-                    for (int t = 1; t < W; t++)
-                        v += red[wid + t][lane][c];
-                    zr[(long long)c * zlen + lane] = v;
-                }
-            group_sync(grp, W);
-        }
-    }
-}
-
 int sms() {
     static int n = 0;
     if (!n) {
@@ -349,29 +214,6 @@ void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, cons
         case 2: phase1_mixed_kernel<2><<<blocks, 32 * kMixWarps, 0, st>>>(items, nitems, lr, mix, scale, xs, xexp, mu, c0, A); break;
         default: phase1_mixed_kernel<1><<<blocks, 32 * kMixWarps, 0, st>>>(items, nitems, lr, mix, scale, xs, xexp, mu, c0, A); break;
         }
-        HTGPU_CUDA(cudaGetLastError());
-    });
-}
-
-void launch_phase2_mixed(const MixedItem *items, int nitems, int warps, const int *cidx, const unsigned char *mix, const double *fac, const double *A, const double *xp, const int *xexp, int mu,
-                         double *z, int zlen, cudaStream_t st) {
-    if (nitems <= 0)
-        return;
-    const int W      = warps >= 4 ? 4 : warps >= 2 ? 2 : 1;
-    const int G      = 8 / W;
-    const int blocks = (nitems + G - 1) / G; // one group per chunk
-    rhs_groups_each(mu, [&](int c0, int g) {
-#define HTGPU_P2M(MU_)                                                                                                                   \
-    (W == 4 ? phase2_mixed_kernel<MU_, 4><<<blocks, 256, 0, st>>>(items, nitems, cidx, mix, fac, A, xp, xexp, mu, c0, z, zlen)             \
-     : W == 2 ? phase2_mixed_kernel<MU_, 2><<<blocks, 256, 0, st>>>(items, nitems, cidx, mix, fac, A, xp, xexp, mu, c0, z, zlen)           \
-              : phase2_mixed_kernel<MU_, 1><<<blocks, 256, 0, st>>>(items, nitems, cidx, mix, fac, A, xp, xexp, mu, c0, z, zlen))
-        switch (g) {
-        case 8: HTGPU_P2M(8); break;
-        case 4: HTGPU_P2M(4); break;
-        case 2: HTGPU_P2M(2); break;
-        default: HTGPU_P2M(1); break;
-        }
-#undef HTGPU_P2M
         HTGPU_CUDA(cudaGetLastError());
     });
 }

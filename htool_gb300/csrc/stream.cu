@@ -1,0 +1,872 @@
+// Phase 2 of the H-matrix product as one streaming pass over the arena.
+//
+// Every row chunk's panel (h <= 32 rows x all covering leaves' columns) is
+// contiguous, and consecutive panels follow each other, so phase 2 is a walk
+// over a byte range cut into chunks (<= 4 KB and <= 64 columns, one element
+// kind each: FP64 on the DFMA pipe, FP64 emulated on the FP32 pipe, FP32 or
+// BF16).  The host groups the chunks into ranges that end on row-chunk
+// boundaries; warps claim ranges through a global ticket, so uneven ranges
+// balance themselves.
+//
+// Each warp works alone: it owns a ring of three shared-memory stages and
+// keeps two chunks in flight ahead of the one it computes.  A chunk arrives
+// by two bulk copies (cp.async.bulk: the panel bytes and the chunk's column
+// index list) counted on the stage's mbarrier.  While chunk c is computed,
+// the coefficients of chunk c+1 (phase-1 sums or x, gathered through its
+// column indices) are already loading into registers.  Lane -> (row = lane %
+// h, slice = lane / h); coefficients are broadcast by shuffles; the slices
+// are summed in a fixed order at the end of a row chunk and each z row is
+// written once.  No atomics on data: repeated products are bitwise equal.
+//
+// Every wait is bounded (about 2 s of SM clocks); on expiry the warp records
+// a status, waits (again bounded) for the copies it issued and stops.
+#include "df64.cuh"
+#include "kernels.hpp"
+
+#include <algorithm>
+
+namespace htgpu {
+
+namespace {
+
+constexpr int kWarps     = kStreamWarpsPerCta;
+constexpr int kStages    = 3;  // per warp
+constexpr int kDataBuf   = kStreamStage + 32;
+constexpr int kIdxBuf    = kStreamCols * 4 + 32;
+constexpr int kWarpSmem  = (kStages * (kDataBuf + kIdxBuf + (int)sizeof(StreamChunk) + 8) + 127) & ~127;
+constexpr long long kWaitCycles = 4000000000ll;
+
+__device__ __forceinline__ unsigned sa(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count) { asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(b)), "r"(count) : "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long *b, unsigned tx) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(sa(b)), "r"(tx) : "memory");
+}
+
+// true once the phase of parity `parity` has completed; a thread that finds
+// it incomplete sleeps until it completes or about `ns` nanoseconds pass
+__device__ __forceinline__ bool mbar_sleep(unsigned long long *b, unsigned parity, unsigned ns) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(sa(b)), "r"(parity), "r"(ns) : "memory");
+    return ok != 0;
+}
+
+// the whole warp waits for the phase; false when the wait ran out
+__device__ __forceinline__ bool warp_wait(unsigned long long *b, unsigned parity) {
+    bool ok = mbar_sleep(b, parity, 20000);
+    if (!__all_sync(0xffffffffu, ok)) {
+        const long long t0 = clock64();
+        while (true) {
+            ok = mbar_sleep(b, parity, 20000);
+            if (__all_sync(0xffffffffu, ok))
+                break;
+            if (__any_sync(0xffffffffu, clock64() - t0 > kWaitCycles))
+                return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sa(dst)), "l"(src), "r"(bytes), "r"(sa(bar)) : "memory");
+}
+
+__device__ __forceinline__ float bf16f(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
+
+__device__ __forceinline__ void df_addf(DF &a, float p) {
+    const float s   = a.s + p;
+    const float bp  = s - a.s;
+    const float err = (a.s - (s - bp)) + (p - bp);
+    a.s             = s;
+    a.c += err;
+}
+
+__device__ __forceinline__ int warp_ticket(int *ticket) {
+    int t = 0;
+    if ((threadIdx.x & 31) == 0)
+        t = atomicAdd(ticket, 1);
+    return __shfl_sync(0xffffffffu, t, 0);
+}
+
+// chunks of the ranges this warp claimed, in order: the current range
+// [b0, e0) and the next one [b1, e1) (empty when none is left)
+struct Seq {
+    int b0, e0, b1, e1;
+};
+
+template <int MU>
+__global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
+    phase2_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena0,
+                       const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
+                       const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *wbase    = smem + (size_t)wid * kWarpSmem;
+    unsigned char *dbuf     = wbase;                                    // kStages x kDataBuf
+    int *ibuf               = reinterpret_cast<int *>(wbase + kStages * kDataBuf); // kStages x kIdxBuf bytes
+    StreamChunk *desc       = reinterpret_cast<StreamChunk *>(wbase + kStages * (kDataBuf + kIdxBuf));
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + kStages * (kDataBuf + kIdxBuf + (int)sizeof(StreamChunk)));
+    const int xe            = max(*xexp, 1);
+    if (lane == 0)
+        for (int s = 0; s < kStages; s++)
+            mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+
+    auto claim = [&](int &b, int &e) {
+        const int r = warp_ticket(ticket);
+        if (r < nranges) {
+            b = rbeg[r];
+            e = rbeg[r + 1];
+        } else {
+            b = e = 0;
+        }
+    };
+    Seq q;
+    claim(q.b0, q.e0);
+    claim(q.b1, q.e1);
+    // issue position: chunk index ip in range `iw` (0 current, 1 next)
+    int ip = q.b0, iw = 0;
+    int issued = 0, done = 0;
+    // the descriptor of the chunk issued next is loaded one issue ahead
+    StreamChunk pf;
+    int pf_ip = -1;
+    auto issue_more = [&]() {
+        while (issued - done < kStages) {
+            if (iw == 0 && ip >= q.e0) {
+                ip = q.b1;
+                iw = 1;
+            }
+            if (iw == 1 && ip >= q.e1)
+                return;
+            const int s         = issued % kStages;
+            const StreamChunk c = ip == pf_ip ? pf : chunks[ip];
+            {
+                const int k2 = (iw == 0 && ip + 1 >= q.e0) ? q.b1 : ip + 1;
+                const int e2 = (iw == 0 && ip + 1 < q.e0) ? q.e0 : q.e1;
+                if (k2 < e2) {
+                    pf    = chunks[k2];
+                    pf_ip = k2;
+                }
+            }
+            if (lane == 0) {
+                desc[s]                   = c;
+                const unsigned char *base = (c.flags & kStreamArena1) ? arena1 : arena0;
+                const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
+                const long long i0 = (4LL * c.a) & ~15LL, i1 = (4LL * (c.a + c.ncol) + 15) & ~15LL;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0 + i1 - i0));
+                bulk_load(dbuf + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), &bar[s]);
+                bulk_load(reinterpret_cast<unsigned char *>(ibuf) + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), &bar[s]);
+            }
+            issued++;
+            ip++;
+        }
+    };
+    // raw coefficients of a landed chunk into registers: column t = lane + 32 j
+    auto gather = [&](int s, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
+        const StreamChunk &c = desc[s];
+        const int *ix        = reinterpret_cast<const int *>(reinterpret_cast<const unsigned char *>(ibuf) + (size_t)s * kIdxBuf + ((4LL * c.a) & 15));
+        const bool emu       = c.kind == kStreamEmu;
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            const int t = lane + 32 * j;
+            kk[j]       = t < c.ncol ? ix[t] : 0;
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++) {
+                double v = 0.;
+                if (t < c.ncol) {
+                    const int kx = kk[j];
+                    if (kx >= 0)
+                        v = __ldg(A + (long long)kx * mu + c0 + cc);
+                    else if (emu)
+                        v = __longlong_as_double(__ldg(reinterpret_cast<const long long *>(xs) + (long long)(~kx) * mu + c0 + cc));
+                    else
+                        v = __ldg(xp + (long long)(~kx) * mu + c0 + cc);
+                }
+                raw[j][cc] = v;
+            }
+        }
+    };
+
+    double dacc[MU];
+    DF acc[MU];
+#pragma unroll
+    for (int cc = 0; cc < MU; cc++) {
+        dacc[cc] = 0.;
+        df_zero(acc[cc]);
+    }
+    double raw[kStreamCols / 32][MU], rnx[kStreamCols / 32][MU];
+    int kk[kStreamCols / 32], knx[kStreamCols / 32];
+    bool ok = true, have = false, have_nx = false; // coefficients of chunk `done` / `done + 1` loaded
+    int left0 = q.e0 - q.b0;                       // chunks of the current range not yet computed
+    issue_more();
+    while (done < issued) {
+        const int s = done % kStages;
+        if (!have) {
+            if (!warp_wait(&bar[s], (done / kStages) & 1)) {
+                ok = false;
+                break;
+            }
+            gather(s, raw, kk);
+        }
+        // chunk done+1: wait for it (normally landed) and start its coefficients
+        have_nx = false;
+        if (done + 1 < issued) {
+            const int s1 = (done + 1) % kStages;
+            if (!warp_wait(&bar[s1], ((done + 1) / kStages) & 1)) {
+                ok = false;
+                break;
+            }
+            gather(s1, rnx, knx);
+            have_nx = true;
+        }
+        const StreamChunk c = desc[s];
+        const int h = c.h, S = 32 / h, row = lane % h, slice = lane / h;
+        const bool live          = slice < S;
+        const unsigned char *buf = dbuf + (size_t)s * kDataBuf + (c.src & 15);
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            const int q0 = 32 * j;
+            if (q0 >= c.ncol)
+                break;
+            const int qc = min(32, c.ncol - q0);
+            if (c.kind == kStreamDfma) {
+                const double *P = reinterpret_cast<const double *>(buf) + row + (size_t)h * q0;
+#pragma unroll 4
+                for (int j0 = 0; j0 < qc; j0 += S) {
+                    const int jj   = j0 + slice;
+                    const bool use = live && jj < qc;
+                    const double u = use ? P[h * jj] : 0.;
+#pragma unroll
+                    for (int cc = 0; cc < MU; cc++)
+                        dacc[cc] = fma(u, __shfl_sync(0xffffffffu, raw[j][cc], use ? jj : 0), dacc[cc]);
+                }
+            } else if (c.kind == kStreamEmu) {
+                F2 a[MU];
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    if (kk[j] >= 0) // phase-1 sum, in the units of x
+                        a[cc] = split64(scale_pow2_safe(raw[j][cc], 1023 - xe));
+                    else { // x, already split
+                        const long long bits = __double_as_longlong(raw[j][cc]);
+                        a[cc].hi             = __int_as_float((int)(bits & 0xffffffffLL));
+                        a[cc].lo             = __int_as_float((int)(bits >> 32));
+                    }
+                }
+                const double *P = reinterpret_cast<const double *>(buf) + row + (size_t)h * q0;
+#pragma unroll 4
+                for (int j0 = 0; j0 < qc; j0 += S) {
+                    const int jj   = j0 + slice;
+                    const bool use = live && jj < qc;
+                    const F2 u     = split64(use ? P[h * jj] : 0.);
+#pragma unroll
+                    for (int cc = 0; cc < MU; cc++) {
+                        F2 b;
+                        b.hi = __shfl_sync(0xffffffffu, a[cc].hi, use ? jj : 0);
+                        b.lo = __shfl_sync(0xffffffffu, a[cc].lo, use ? jj : 0);
+                        df_fma(acc[cc], u, b);
+                    }
+                }
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    df_renorm(acc[cc]);
+            } else {
+                float a[MU], part[MU];
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    a[cc]    = (float)scale_pow2_safe(raw[j][cc], 1023 - xe);
+                    part[cc] = 0.f;
+                }
+                if (c.kind == kStreamF32) {
+                    const float *P = reinterpret_cast<const float *>(buf) + row + (size_t)h * q0;
+#pragma unroll 4
+                    for (int j0 = 0; j0 < qc; j0 += S) {
+                        const int jj   = j0 + slice;
+                        const bool use = live && jj < qc;
+                        const float u  = use ? P[h * jj] : 0.f;
+#pragma unroll
+                        for (int cc = 0; cc < MU; cc++)
+                            part[cc] = fmaf(u, __shfl_sync(0xffffffffu, a[cc], use ? jj : 0), part[cc]);
+                    }
+                } else {
+                    const unsigned short *P = reinterpret_cast<const unsigned short *>(buf) + row + (size_t)h * q0;
+#pragma unroll 4
+                    for (int j0 = 0; j0 < qc; j0 += S) {
+                        const int jj   = j0 + slice;
+                        const bool use = live && jj < qc;
+                        const float u  = use ? bf16f(P[h * jj]) : 0.f;
+#pragma unroll
+                        for (int cc = 0; cc < MU; cc++)
+                            part[cc] = fmaf(u, __shfl_sync(0xffffffffu, a[cc], use ? jj : 0), part[cc]);
+                    }
+                }
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    df_addf(acc[cc], part[cc]);
+            }
+        }
+        if (c.flags & kStreamLast) {
+            double v[MU];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                v[cc] = dacc[cc] + scale_pow2_safe(df_to_double(acc[cc]), xe - 1023);
+            for (int t = 1; t < S; t++)
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    const int src   = lane + t * h;
+                    const double vv = __shfl_sync(0xffffffffu, v[cc], src < 32 ? src : lane);
+                    if (slice == 0)
+                        v[cc] += vv;
+                }
+            if (slice == 0)
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    z[(long long)(c0 + cc) * zlen + c.b + row] = v[cc];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++) {
+                dacc[cc] = 0.;
+                df_zero(acc[cc]);
+            }
+        }
+        __syncwarp(); // every lane is done with stage s before it is refilled
+        done++;
+        if (--left0 == 0) { // the next range becomes current; claim another
+            if (iw == 0)
+                ip = q.b1;
+            iw   = 0;
+            q.b0 = q.b1;
+            q.e0 = q.e1;
+            left0 = q.e0 - q.b0;
+            claim(q.b1, q.e1);
+        }
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            kk[j] = knx[j];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                raw[j][cc] = rnx[j][cc];
+        }
+        have = have_nx;
+        issue_more();
+    }
+    if (!ok) {
+        if (lane == 0)
+            atomicExch(status, 2);
+        // the copies in flight must land before the warp leaves
+        for (int p = done; p < issued; p++)
+            if (!warp_wait(&bar[p % kStages], (p / kStages) & 1) && lane == 0)
+                atomicExch(status, 3);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// phase 1: chunks of up to 16 whole columns of one tile (jlen <= 256 rows,
+// column-major): every column's dot product with the tile's x rows is
+// complete inside the chunk, so each chunk ends with a reduce-scatter sized
+// to its columns and writes its sums; the x rows of the next tile are
+// loaded into registers while the current chunk is computed.
+// ---------------------------------------------------------------------------
+
+// reduce-scatter of the first N of 16 per-lane values over the warp (N a
+// power of two): afterwards lane l holds in v[0] the warp-wide sum of value
+// index rs_index<N>(l); fixed order
+template <int N, int B, typename T, typename Add, typename Shfl>
+__device__ __forceinline__ void rs_pow2(T (&v)[16], int lane, Add add, Shfl shfl) {
+    if constexpr (N > 1) {
+        const bool hi = lane & B;
+#pragma unroll
+        for (int i = 0; i < N / 2; i++) {
+            T keep = hi ? v[i + N / 2] : v[i], send = hi ? v[i] : v[i + N / 2];
+            v[i] = add(keep, shfl(send, B));
+        }
+    } else {
+        v[0] = add(v[0], shfl(v[0], B));
+    }
+    if constexpr (B > 1)
+        rs_pow2<(N > 1 ? N / 2 : 1), B / 2>(v, lane, add, shfl);
+}
+
+template <int N>
+__device__ __forceinline__ int rs_index(int lane) {
+    int idx = 0, n = N;
+#pragma unroll
+    for (int b = 16; b >= 1 && n > 1; b >>= 1) {
+        n >>= 1;
+        if (lane & b)
+            idx += n;
+    }
+    return idx;
+}
+
+template <int N>
+__host__ __device__ constexpr int rs_quiet() { // lanes that write: the bits below the halving levels are zero
+    return N >= 32 ? 0 : (N == 16 ? 1 : N == 8 ? 3 : N == 4 ? 7 : N == 2 ? 15 : 31);
+}
+
+struct AddD {
+    __device__ double operator()(double a, double b) const { return a + b; }
+};
+struct ShflD {
+    __device__ double operator()(double v, int o) const { return __shfl_xor_sync(0xffffffffu, v, o); }
+};
+struct AddF {
+    __device__ float operator()(float a, float b) const { return a + b; }
+};
+struct ShflF {
+    __device__ float operator()(float v, int o) const { return __shfl_xor_sync(0xffffffffu, v, o); }
+};
+struct AddDF {
+    __device__ DF operator()(DF a, DF b) const { return df_add(a, b); }
+};
+struct ShflDF {
+    __device__ DF operator()(DF v, int o) const {
+        DF r;
+        r.s = __shfl_xor_sync(0xffffffffu, v.s, o);
+        r.c = __shfl_xor_sync(0xffffffffu, v.c, o);
+        return r;
+    }
+};
+
+// sums of value n (n < nv) go to out(n, value) from one lane each
+template <typename T, typename Add, typename Shfl, typename Out>
+__device__ __forceinline__ void reduce_out(T (&v)[16], int nv, int lane, Add add, Shfl shfl, Out out) {
+    if (nv > 8) {
+        rs_pow2<16, 16>(v, lane, add, shfl);
+        if ((lane & rs_quiet<16>()) == 0 && rs_index<16>(lane) < nv)
+            out(rs_index<16>(lane), v[0]);
+    } else if (nv > 4) {
+        rs_pow2<8, 16>(v, lane, add, shfl);
+        if ((lane & rs_quiet<8>()) == 0 && rs_index<8>(lane) < nv)
+            out(rs_index<8>(lane), v[0]);
+    } else if (nv > 2) {
+        rs_pow2<4, 16>(v, lane, add, shfl);
+        if ((lane & rs_quiet<4>()) == 0 && rs_index<4>(lane) < nv)
+            out(rs_index<4>(lane), v[0]);
+    } else if (nv > 1) {
+        rs_pow2<2, 16>(v, lane, add, shfl);
+        if ((lane & rs_quiet<2>()) == 0 && rs_index<2>(lane) < nv)
+            out(rs_index<2>(lane), v[0]);
+    } else {
+        rs_pow2<1, 16>(v, lane, add, shfl);
+        if (lane == 0)
+            out(0, v[0]);
+    }
+}
+
+// np (<= NP) columns p0 .. p0+np of a phase-1 chunk against the tile's x
+// rows (X: row-major, MU per row); sums to A (and the per-column scales)
+template <int NP, int MU>
+__device__ __forceinline__ void tile_group(const StreamChunk &c, const unsigned char *buf, const unsigned long long *X, int p0, int np, int lane, int shift, double *__restrict__ A,
+                                           const double *__restrict__ scale, int mu, int c0) {
+    static_assert(NP * MU <= 16, "reduction group of at most 16 values");
+    const int jlen  = c.h;
+    const int base  = c.a + p0;
+    const bool full = np == NP;
+    if (c.kind == kStreamDfma) {
+        double acc[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            acc[i] = 0.;
+        const double *V = reinterpret_cast<const double *>(buf) + (size_t)jlen * p0 + lane;
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            if (32 * t >= jlen) // warp-uniform
+                break;
+            const int row   = lane + 32 * t;
+            const bool live = row < jlen;
+            double xv[MU];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                xv[cc] = live ? __longlong_as_double((long long)X[row * MU + cc]) : 0.;
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                const double u = (live && (full || p < np)) ? V[jlen * p + 32 * t] : 0.;
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    acc[p * MU + cc] = fma(u, xv[cc], acc[p * MU + cc]);
+            }
+        }
+        reduce_out(acc, np * MU, lane, AddD(), ShflD(), [&](int n, double v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = v; });
+    } else if (c.kind == kStreamEmu) {
+        // two accumulator sets (even / odd row groups) for independent chains
+        DF acc[16], acc2[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            df_zero(acc[i]);
+            df_zero(acc2[i]);
+        }
+        const double *V = reinterpret_cast<const double *>(buf) + (size_t)jlen * p0 + lane;
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            if (32 * t >= jlen) // warp-uniform
+                break;
+            const int row   = lane + 32 * t;
+            const bool live = row < jlen;
+            F2 xv[MU];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++) {
+                const unsigned long long bits = live ? X[row * MU + cc] : 0ull;
+                xv[cc].hi                     = __int_as_float((int)(bits & 0xffffffffull));
+                xv[cc].lo                     = __int_as_float((int)(bits >> 32));
+            }
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                const F2 u = split64((live && (full || p < np)) ? V[jlen * p + 32 * t] : 0.);
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    df_fma((t & 1) ? acc2[p * MU + cc] : acc[p * MU + cc], u, xv[cc]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < NP * MU; i++) {
+            df_renorm(acc[i]);
+            df_renorm(acc2[i]);
+            acc[i] = df_add(acc[i], acc2[i]);
+        }
+        reduce_out(acc, np * MU, lane, AddDF(), ShflDF(), [&](int n, DF v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe(df_to_double(v), shift); });
+    } else {
+        float acc[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            acc[i] = 0.f;
+        const bool f32 = c.kind == kStreamF32;
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            if (32 * t >= jlen) // warp-uniform
+                break;
+            const int row   = lane + 32 * t;
+            const bool live = row < jlen;
+            float xv[MU];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                xv[cc] = live ? __int_as_float((int)(X[row * MU + cc] & 0xffffffffull)) : 0.f;
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                float u = 0.f;
+                if (live && (full || p < np)) {
+                    const size_t e = (size_t)jlen * (p0 + p) + row;
+                    u              = f32 ? reinterpret_cast<const float *>(buf)[e] : bf16f(reinterpret_cast<const unsigned short *>(buf)[e]);
+                }
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    acc[p * MU + cc] = fmaf(u, xv[cc], acc[p * MU + cc]);
+            }
+        }
+        const int sbase = c.c + p0;
+        reduce_out(acc, np * MU, lane, AddF(), ShflF(), [&](int n, float v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe((double)v, shift) * scale[sbase + n / MU]; });
+    }
+}
+
+template <int MU>
+struct P1Smem { // per warp: data stages, descriptors, barriers, two x buffers
+    static constexpr int kDesc  = kStages * kDataBuf;
+    static constexpr int kBar   = kDesc + kStages * (int)sizeof(StreamChunk);
+    static constexpr int kX     = (kBar + kStages * 8 + 15) & ~15;
+    static constexpr int kXBuf  = 256 * MU * 8;
+    static constexpr int kTotal = (kX + 2 * kXBuf + 127) & ~127;
+};
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) { asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa(dst)), "l"(src) : "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int MU>
+__global__ void __launch_bounds__(32 * kWarps, 3)
+    phase1_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena,
+                       const double *__restrict__ xp, const F2 *__restrict__ xs, const double *__restrict__ scale, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ A,
+                       int *__restrict__ status) {
+    using L    = P1Smem<MU>;
+    constexpr int G = 16 / MU; // columns per reduction group
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *wbase    = smem + (size_t)wid * L::kTotal;
+    unsigned char *dbuf     = wbase;
+    StreamChunk *desc       = reinterpret_cast<StreamChunk *>(wbase + L::kDesc);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + L::kBar);
+    unsigned long long *xb  = reinterpret_cast<unsigned long long *>(wbase + L::kX); // 2 x (256 rows x MU)
+    const int shift         = max(*xexp, 1) - 1023;
+    if (lane == 0)
+        for (int s = 0; s < kStages; s++)
+            mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+
+    auto claim = [&](int &b, int &e) {
+        const int r = warp_ticket(ticket);
+        if (r < nranges) {
+            b = rbeg[r];
+            e = rbeg[r + 1];
+        } else {
+            b = e = 0;
+        }
+    };
+    Seq q;
+    claim(q.b0, q.e0);
+    claim(q.b1, q.e1);
+    int ip = q.b0, iw = 0;
+    int issued = 0, done = 0;
+    // the descriptor of the chunk issued next is loaded one issue ahead
+    StreamChunk pf;
+    int pf_ip = -1;
+    auto issue_more = [&]() {
+        while (issued - done < kStages) {
+            if (iw == 0 && ip >= q.e0) {
+                ip = q.b1;
+                iw = 1;
+            }
+            if (iw == 1 && ip >= q.e1)
+                return;
+            const int s         = issued % kStages;
+            const StreamChunk c = ip == pf_ip ? pf : chunks[ip];
+            {
+                const int k2 = (iw == 0 && ip + 1 >= q.e0) ? q.b1 : ip + 1;
+                const int e2 = (iw == 0 && ip + 1 < q.e0) ? q.e0 : q.e1;
+                if (k2 < e2) {
+                    pf    = chunks[k2];
+                    pf_ip = k2;
+                }
+            }
+            if (lane == 0) {
+                desc[s]            = c;
+                const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0));
+                bulk_load(dbuf + (size_t)s * kDataBuf, arena + a0, (unsigned)(a1 - a0), &bar[s]);
+            }
+            issued++;
+            ip++;
+        }
+    };
+    // the x rows of a tile into x buffer `which` (asynchronous copies): FP64
+    // bits for DFMA chunks, the F2 split otherwise; row-major, MU per row
+    auto load_x = [&](const StreamChunk &c, int which) {
+        const unsigned long long *src = c.kind == kStreamDfma ? reinterpret_cast<const unsigned long long *>(xp) : reinterpret_cast<const unsigned long long *>(xs);
+        unsigned long long *dst       = xb + (size_t)which * 256 * MU;
+        for (int row = lane; row < c.h; row += 32)
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                cp_async8(dst + row * MU + cc, src + (long long)(c.b + row) * mu + c0 + cc);
+        cp_async_commit();
+    };
+
+    bool ok = true, pre = false; // pre: x of chunk `done` already requested into buffer xcur
+    int xcur   = 0;
+    int left0  = q.e0 - q.b0;
+    issue_more();
+    while (done < issued) {
+        const int s = done % kStages;
+        if (!warp_wait(&bar[s], (done / kStages) & 1)) {
+            ok = false;
+            break;
+        }
+        const StreamChunk c = desc[s];
+        if ((c.flags & kStreamFirst) && !pre) // a new tile whose x was not prefetched
+            load_x(c, xcur);
+        bool nx_pre = false;
+        if (done + 1 < issued) {
+            const int s1 = (done + 1) % kStages;
+            if (!warp_wait(&bar[s1], ((done + 1) / kStages) & 1)) {
+                ok = false;
+                break;
+            }
+            if (desc[s1].flags & kStreamFirst) { // next tile's x into the other buffer
+                cp_async_wait_all();             // (this tile's copies first, so waits stay simple)
+                load_x(desc[s1], xcur ^ 1);
+                nx_pre = true;
+            }
+        }
+        // this chunk's x copies: all but the group just committed for the next tile
+        if (nx_pre)
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else
+            cp_async_wait_all();
+        __syncwarp();
+        const unsigned long long *X = xb + (size_t)xcur * 256 * MU;
+        const unsigned char *buf    = dbuf + (size_t)s * kDataBuf + (c.src & 15);
+        for (int p0 = 0; p0 < c.ncol; p0 += G) {
+            const int np = min(G, c.ncol - p0);
+            // tight loops for the group's column count (rounded up to a power of two)
+            if (np > 8)
+                tile_group<16 / MU, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
+            else if (np > 4)
+                tile_group<(8 < 16 / MU ? 8 : 16 / MU), MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
+            else if (np > 2)
+                tile_group<4, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
+            else if (np > 1)
+                tile_group<2, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
+            else
+                tile_group<1, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
+        }
+        __syncwarp();
+        done++;
+        if (--left0 == 0) {
+            if (iw == 0)
+                ip = q.b1;
+            iw    = 0;
+            q.b0  = q.b1;
+            q.e0  = q.e1;
+            left0 = q.e0 - q.b0;
+            claim(q.b1, q.e1);
+        }
+        if (nx_pre)
+            xcur ^= 1;
+        pre = nx_pre;
+        issue_more();
+    }
+    cp_async_wait_all();
+    if (!ok) {
+        if (lane == 0)
+            atomicExch(status, 2);
+        for (int p = done; p < issued; p++)
+            if (!warp_wait(&bar[p % kStages], (p / kStages) & 1) && lane == 0)
+                atomicExch(status, 3);
+    }
+}
+
+template <int MU>
+void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+                    const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
+    static unsigned long long done = 0; // devices whose shared-memory limit was raised
+    const int bytes                = kWarps * kWarpSmem;
+    int dev                        = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_warp_kernel<MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    phase2_warp_kernel<MU><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+} // namespace
+
+void stream_section(std::vector<StreamChunk> &out, long long src, int es, int h, int n, int q0, int row0, unsigned char kind, unsigned char flags) {
+    const int maxc = std::max(1, std::min(kStreamCols, kStreamStage / (h * es)));
+    for (int c = 0; c < n; c += maxc) {
+        StreamChunk k;
+        k.ncol  = std::min(maxc, n - c);
+        k.src   = src + (long long)h * c * es;
+        k.bytes = h * k.ncol * es;
+        k.a     = q0 + c;
+        k.b     = row0;
+        k.c     = 0;
+        k.h     = h;
+        k.kind  = kind;
+        k.flags = flags;
+        k.pad   = 0;
+        out.push_back(k);
+    }
+}
+
+std::vector<int> stream_ranges(const std::vector<StreamChunk> &ch, int nranges) {
+    // cost ~ time: DFMA chunks run on the FP64 pipe, slower per byte than the
+    // other kinds; every chunk has a fixed overhead
+    std::vector<double> pre(ch.size() + 1, 0.);
+    std::vector<int> bounds;
+    for (std::size_t k = 0; k < ch.size(); k++) {
+        pre[k + 1] = pre[k] + ch[k].bytes * (ch[k].kind == kStreamDfma ? 2.0 : 1.0) + 256.0;
+        if (ch[k].flags & kStreamFirst)
+            bounds.push_back((int)k);
+    }
+    bounds.push_back((int)ch.size());
+    std::vector<int> r{0};
+    std::size_t b = 0;
+    for (int i = 1; i < nranges; i++) {
+        const double target = pre.back() * i / nranges;
+        while (b + 1 < bounds.size() && pre[bounds[b]] < target)
+            b++;
+        if (bounds[b] > r.back() && bounds[b] < (int)ch.size())
+            r.push_back(bounds[b]);
+    }
+    if ((int)ch.size() > r.back())
+        r.push_back((int)ch.size());
+    return r; // ranges r[i] .. r[i+1], none empty
+}
+
+int stream_ctas() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        n = 4 * (sms > 0 ? sms : 152); // resident at once: 4 CTAs of 4 warps per SM
+    }
+    return n;
+}
+
+void launch_phase1_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+                          const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
+    if (nranges <= 0)
+        return;
+    require(mu >= 1 && mu <= 2, "streamed phase 1 takes one or two right-hand sides");
+    HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int), st));
+    const int bytes = kWarps * (mu == 1 ? P1Smem<1>::kTotal : P1Smem<2>::kTotal);
+    int dev         = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    static unsigned long long done1 = 0, done2 = 0;
+    unsigned long long &done        = mu == 1 ? done1 : done2;
+    if (dev >= 64 || !(done >> dev & 1)) {
+        if (mu == 1)
+            HTGPU_CUDA(cudaFuncSetAttribute(phase1_warp_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        else
+            HTGPU_CUDA(cudaFuncSetAttribute(phase1_warp_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    const int nctas = stream_ctas();
+    if (mu == 1)
+        phase1_warp_kernel<1><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, tickets, arena, xp, xs, scale, xexp, mu, 0, A, status);
+    else
+        phase1_warp_kernel<2><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, tickets, arena, xp, xs, scale, xexp, mu, 0, A, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile) {
+    // emulated columns are long instruction sequences: at most 4 per chunk
+    int P = std::max(1, std::min(kind == kStreamEmu ? 4 : 16, kStreamStage / (jlen * es)));
+    while (P & (P - 1))
+        P &= P - 1; // a power of two
+    for (int k = 0; k < n; k += P) {
+        StreamChunk c;
+        c.ncol  = std::min(P, n - k);
+        c.src   = src + (long long)jlen * k * es;
+        c.bytes = jlen * c.ncol * es;
+        c.a     = slot + k0 + k;
+        c.b     = xrow;
+        c.c     = sidx + k0 + k;
+        c.h     = jlen;
+        c.kind  = kind;
+        c.flags = (first_of_tile && k == 0) ? kStreamFirst : 0;
+        c.pad   = 0;
+        out.push_back(c);
+    }
+}
+
+void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+    if (nranges <= 0)
+        return;
+    HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
+    const int nctas = stream_ctas();
+    int c0 = 0, g = 0;
+    while (c0 < mu) {
+        const int left = mu - c0;
+        const int n    = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        int *t         = tickets + std::min(g, 7);
+        if (g >= 7 && c0 > 0)
+            HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
+        switch (n) {
+        case 8: launch_warp_mu<8>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 4: launch_warp_mu<4>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 2: launch_warp_mu<2>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        default: launch_warp_mu<1>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        }
+        c0 += n;
+        g++;
+    }
+}
+
+} // namespace htgpu

@@ -155,20 +155,28 @@ int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
 int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int phase1_dfma_permille, int phase2_dfma_permille);
 int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int *phase2_dfma_permille);
 
-/* Launch shape of phase 2 (the U-side/dense product per target row chunk):
- * 1, 2 or 4 warps share one chunk's panel, for the DFMA panels, the
- * emulated FP64 panels and the reduced-precision panels.  Results stay
- * within the stated tolerances for every shape; the sums are split in a
- * different order, so shapes differ in the last bits.  No counterpart in
- * the reference. */
-int htgpu_hmatrix_set_phase2_warps(htgpu_hmatrix h, int dfma, int emulated, int reduced);
-int htgpu_hmatrix_get_phase2_warps(htgpu_hmatrix h, int *dfma, int *emulated, int *reduced);
+/* Phase 1 (the V-side sums of every low-rank leaf) with one or two
+ * right-hand sides: HTGPU_PHASE1_TILES (one warp per tile, DFMA and emulated
+ * tiles as two concurrent kernels) or HTGPU_PHASE1_STREAM (tiles cut into
+ * chunks that every warp streams through shared memory with bulk copies).
+ * Results agree within the FP64 tolerance; the autotuner picks one.  No
+ * counterpart in the reference. */
+#define HTGPU_PHASE1_TILES 0
+#define HTGPU_PHASE1_STREAM 1
+int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);
+int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode);
+
+/* Status word of the product kernels' bounded waits: 0, or 1/2/3 when a
+ * wait for a pipeline stage ran out (the product's result is then not
+ * valid).  Synchronises the H-matrix's stream.  Host-pointer products check
+ * it themselves and fail.  No counterpart in the reference. */
+int htgpu_hmatrix_device_status(htgpu_hmatrix h, int *status);
 
 /* Autotuner: times `reps` products with mu right-hand sides on this
- * H-matrix and keeps the fastest launch shape for the current storage
- * policy -- with FP64 factors the warps per phase-2 row chunk and then the
- * DFMA/emulation split, with reduced-precision factors the warps per
- * phase-2 row chunk; *best_ms is its time per product.  Replaces nothing
+ * H-matrix and keeps the fastest configuration for the current storage
+ * policy -- with FP64 factors the phase-1 mode and the DFMA/emulation
+ * split, with reduced-precision factors the phase-1 mode; *best_ms is its
+ * time per product.  Replaces nothing
  * upstream (htool has no tuning). */
 int htgpu_hmatrix_autotune(htgpu_hmatrix h, int mu, int reps, float *best_ms);
 

@@ -189,29 +189,35 @@ def test_fp64_emulation_input_scaling():
     assert not np.any(GH @ np.zeros(5000))
 
 
-@pytest.mark.parametrize("warps", [1, 2, 4])
-def test_phase2_warps_parity(golden, warps):
-    """Every phase-2 launch shape (warps per row chunk) gives the reference
-    product: DFMA panels, emulated panels and reduced-precision panels."""
+@pytest.mark.parametrize("mode", ["tiles", "stream"])
+def test_phase1_modes_parity(golden, mode):
+    """Both phase-1 implementations give the reference product for every
+    DFMA / emulation split and both reduced-precision policies, with one and
+    two right-hand sides (two match two single products exactly)."""
     g, meta = golden("sphere6000_k1")
-    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
     GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
-    GH.set_phase2_warps(warps, warps, warps)
-    assert GH.get_phase2_warps() == (warps, warps, warps)
+    GH.set_phase1_mode(mode)
+    assert GH.get_phase1_mode() == {"tiles": H.PHASE1_TILES, "stream": H.PHASE1_STREAM}[mode]
+    x2 = G.rhs(n, 2, seed=8)
     for split in ((1000, 1000), (0, 0), (650, 500)):
         GH.set_fp64_split(*split)
-        for mu in (1, 3):
-            y = GH.mvprod_global_to_global(g["x_mu%d" % mu], mu)
-            assert rel(y, g["y_mu%d" % mu]) < FP64_TOL
-            assert np.array_equal(y, GH.mvprod_global_to_global(g["x_mu%d" % mu], mu))
-    x = G.rhs(g["xt"].shape[0], 9, seed=4)
-    GH.set_fp64_split(1000, 1000)
-    ref9 = GH.mvprod_global_to_global(x, 9)
-    GH.set_precision("mixed")
-    assert rel(GH.mvprod_global_to_global(x, 9), ref9) < 1e-6
-    assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-6
+        y = GH.mvprod_global_to_global(g["x_mu1"])
+        assert rel(y, g["y_mu1"]) < FP64_TOL
+        assert np.array_equal(y, GH.mvprod_global_to_global(g["x_mu1"]))
+        y2 = GH.mvprod_global_to_global(x2, 2)
+        y11 = np.concatenate([GH @ x2[:n].copy(), GH @ x2[n:].copy()])
+        assert rel(y2, y11) < 1e-14
+    ref2 = y2
+    for policy in ("mixed", "fp32"):
+        GH.set_precision(policy)
+        assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-6
+        assert rel(GH.mvprod_global_to_global(x2, 2), ref2) < 1e-6
+    GH.set_precision("fp64")
     with pytest.raises(ValueError):
-        GH.set_phase2_warps(3, 1, 1)
+        GH.set_phase1_mode(2)
+    assert GH.device_status() == 0
 
 
 def test_autotune_keeps_parity(golden):
@@ -220,7 +226,7 @@ def test_autotune_keeps_parity(golden):
     GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
     ms = GH.autotune(1, 2)
     assert ms > 0
-    assert all(w in (1, 2, 4) for w in GH.get_phase2_warps())
+    assert GH.get_phase1_mode() in (H.PHASE1_TILES, H.PHASE1_STREAM)
     assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < FP64_TOL
     GH.set_precision("mixed")
     assert GH.autotune(1, 2) > 0
