@@ -1,11 +1,17 @@
 """Benchmark: H-matrix product throughput on one GB300 (and N replicas).
 
-Workload (BASELINE configuration 2 geometry): N = 100 000 points uniform on
-the unit sphere (seeded), Laplace single-layer kernel 1/(4 pi r) with a zero
-diagonal, eta = 10, epsilon = 1e-6, partialACA, minclustersize 10; one
-N(0,1) right-hand side per product.  The H-matrix is assembled on the GPU
-(device generator + batched device partialACA); a "step" is one product
-y = H x (mvprod_global_to_global), permutations included.
+Workload: N = 100 000 points uniform on the unit sphere (seeded), Laplace
+single-layer kernel 1/(4 pi r) with a zero diagonal, eta = 10, epsilon =
+1e-6, partialACA, minclustersize 10; one N(0,1) right-hand side per
+product.  The H-matrix is assembled on the GPU (device generator + batched
+device partialACA, timed as `aca_seconds`); a "step" is one product y = H x
+(mvprod_global_to_global), permutations included.
+
+The headline `value` is the mixed-precision product (low-rank factors in
+FP32 / BF16 per column with per-column scaling, dense leaves FP64, FP32/FP64
+accumulation) with its error against the plain FP64 product stated; the
+plain FP64 product is measured in the same run (`fp64`).  Both read more
+than L2 holds per product (0.9 and 2.1 GB of factors), so no flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
@@ -40,6 +46,9 @@ def parse():
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    # fixed configuration instead of the autotuner (e.g. to replay a tuned run under a profiler)
+    p.add_argument("--fp64-split", default=None, help="phase-1,phase-2 DFMA per mille, e.g. 0,650")
+    p.add_argument("--phase1-mode", type=int, default=None, help="0 tile kernels, 1 streamed")
     return p.parse_args()
 
 
@@ -163,6 +172,13 @@ def run_gpu(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    def max_over_ranks(v):
+        if world > 1:
+            tt = torch.tensor([v], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            return float(tt.item())
+        return v
+
     n = args.n
     pts = G.sphere(n, seed=1)
     t = H.Cluster().build(n, pts)
@@ -170,8 +186,6 @@ def run_gpu(args):
     t0 = time.perf_counter()
     hm = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).build(H.LAPLACE, pts)
     aca_seconds = time.perf_counter() - t0
-    tune_ms = hm.autotune(1, 5)  # DFMA / FP32-pipe split of the FP64 product
-    split = hm.get_fp64_split()
     info = hm.get_infos()
 
     x = G.rhs(n, 1, seed=2)
@@ -180,30 +194,67 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
+    peak, peak_kind = measured_peaks()
+
+    def timed_products():
+        for _ in range(args.warmup):
+            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
+        e1.record(stream)
+        barrier()
+        return max_over_ranks(e0.elapsed_time(e1)), hm.last_launches()
+
+    def describe(ms_total):
+        """per-step numbers, phase breakdown and the dominant kernel's roofline"""
+        ms_step = ms_total / args.steps
+        ph = hm.profile(1, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
+        pb = hm.phase_bytes(1)
+        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_warp_kernel", "phase2_warp_kernel", "zsum_kernel"]
+        k = max(range(4), key=lambda i: ph[i])
+        achieved = pb[k] / (ph[k] / 1e3) / 1e9
+        total_bytes = sum(pb)
+        return ms_step, {
+            "phase_ms": {"gather": ph[0], "phase1": ph[1], "phase2": ph[2], "sums": ph[3], "total": ph[4]},
+            "phase_bytes": {"gather": pb[0], "phase1": pb[1], "phase2": pb[2], "sums": pb[3]},
+            "whole_product": {"bytes": total_bytes, "GB_per_s": total_bytes / (ms_step / 1e3) / 1e9, "frac_of_hbm_peak": total_bytes / (ms_step / 1e3) / 1e9 / peak},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "kernel": names[k], "kernel_ms": ph[k], "algorithmic_bytes": pb[k],
+                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
+        }
 
     clocks = Clocks(local)
     clocks.start()
-    time.sleep(0.5)  # let the sampler start before the timed region
-    for _ in range(args.warmup):
-        hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
-    e1.record(stream)
-    barrier()
-    ms_total = e0.elapsed_time(e1)
-    launches_per_step = hm.last_launches()
-    # per-launch breakdown (same stream, events between launches)
-    phase_ms = hm.profile(1, max(3, args.steps // 2))
+    time.sleep(0.5)  # let the sampler start before the timed regions
+    # plain FP64 (autotuned DFMA / FP32-pipe split)
+    hm.set_precision("fp64")
+    fixed = args.fp64_split is not None or args.phase1_mode is not None
+    if fixed:
+        if args.fp64_split is not None:
+            hm.set_fp64_split(*[int(v) for v in args.fp64_split.split(",")])
+        if args.phase1_mode is not None:
+            hm.set_phase1_mode(args.phase1_mode)
+        tune64 = None
+    else:
+        tune64 = hm.autotune(1, 5)
+    split = hm.get_fp64_split()
+    p1mode64 = hm.get_phase1_mode()
+    ms64, _ = timed_products()
+    y64 = yd.cpu().numpy().copy()
+    step64, d64 = describe(ms64)
+    # mixed precision
+    tau = 1.0
+    hm.set_precision("mixed", tau)
+    tunem = None if fixed else hm.autotune(1, 5)
+    msm, launches_per_step = timed_products()
+    ym = yd.cpu().numpy().copy()
+    stepm, dm = describe(msm)
+    pinfo = hm.precision_info()
     clk = clocks.stop()
-    if world > 1:
-        tt = torch.tensor([ms_total], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(tt.item())
-    ms_step = ms_total / args.steps
-    value = world * args.steps / (ms_total / 1e3)
+    value = world * args.steps / (msm / 1e3)
+    value64 = world * args.steps / (ms64 / 1e3)
 
     # end to end through the C ABI: pinned host x -> device -> product -> host y
     xh = torch.from_numpy(x).pin_memory()
@@ -214,41 +265,30 @@ def run_gpu(args):
     w0 = time.perf_counter()
     for _ in range(args.steps):
         hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
-    e2e_s = time.perf_counter() - w0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
+    e2e_s = max_over_ranks(time.perf_counter() - w0)
+    e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n, "precision": "mixed"}
+    status = hm.device_status()
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    y = yh.numpy().copy()
-    err = sampled_dense_error(pts, x, y)
-    peak, peak_kind = measured_peaks()
-    lr, dn = hm.get_leaves()
-    b_v = 8 * int(np.sum(lr[:, 4].astype(np.int64) * lr[:, 3]))
-    b_u = 8 * int(np.sum(lr[:, 4].astype(np.int64) * lr[:, 2]))
-    b_d = 8 * int(np.sum(dn[:, 2].astype(np.int64) * dn[:, 3]))
-    prod_bytes = hm.product_bytes(1)
-    # dominant kernel and its algorithmic bytes per launch
-    k1, k2 = phase_ms[1], phase_ms[2]
-    if k2 >= k1:
-        dom, dom_ms, dom_bytes = "phase2_kernel (U-side + dense + scatter)", k2, b_u + b_d + 12 * n
-    else:
-        dom, dom_ms, dom_bytes = "phase1_kernel (V-side)", k1, b_v
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    err_mixed_vs_fp64 = float(np.linalg.norm(ym - y64) / np.linalg.norm(y64))
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)",
-        "config": dict(WORKLOAD, n=n, precision="fp64", parallelism="replicas" if world > 1 else "single", l2="inputs larger than L2: %.2f GB of factors per product" % (prod_bytes / 1e9),
-                       fp64_split={"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune_ms}),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "kernel": dom, "peak_source": peak_kind},
-        "whole_product": {"bytes": prod_bytes, "GB_per_s": prod_bytes / (ms_step / 1e3) / 1e9, "frac_of_hbm_peak": prod_bytes / (ms_step / 1e3) / 1e9 / peak, "phase_ms": {"gather": phase_ms[0], "phase1": phase_ms[1], "phase2": phase_ms[2], "total": phase_ms[3]}},
-        "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk,
-        "rel_err_vs_dense_1000_rows": err, "aca_seconds": aca_seconds,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": stepm, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed: fp32/bf16 factors (per-column scaled), fp64 dense, fp32+fp64 accumulation",
+        "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)",
+        "config": dict(WORKLOAD, n=n, precision="mixed", tau=tau, parallelism="replicas" if world > 1 else "single",
+                       l2="inputs larger than L2: %.2f GB (mixed) / %.2f GB (fp64) of factors per product" % (pinfo["stored_bytes"] / 1e9, d64["whole_product"]["bytes"] / 1e9)),
+        "rel_err_mixed_vs_fp64": err_mixed_vs_fp64,
+        "speedup_mixed_vs_fp64": value / value64,
+        "roofline": dm["roofline"], "whole_product": dm["whole_product"], "phase_ms": dm["phase_ms"], "phase_bytes": dm["phase_bytes"],
+        "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode()},
+        "fp64": {"value": value64, "unit": UNIT, "ms_per_step": step64, "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
+                 "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64}, "phase1_mode": p1mode64},
+        "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk, "device_status": status,
+        "rel_err_vs_dense_1000_rows": {"fp64": sampled_dense_error(pts, x, y64), "mixed": sampled_dense_error(pts, x, ym)},
+        "aca_seconds": aca_seconds,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},
     }
     if not args.no_cpu_baseline:

@@ -62,6 +62,7 @@ def _load():
         "htgpu_hmatrix_get_factors": (i, [vp, vp, vp]),
         "htgpu_hmatrix_infos": (i, [vp, vp, vp]),
         "htgpu_hmatrix_product_bytes": (i, [vp, i, vp]),
+        "htgpu_hmatrix_phase_bytes": (i, [vp, i, vp]),
         "htgpu_hmatrix_last_launches": (i, [vp, vp]),
         "htgpu_hmatrix_profile": (i, [vp, i, i, vp]),
         "htgpu_hmatrix_set_fp64_split": (i, [vp, i, i]),
@@ -267,10 +268,17 @@ class HMatrix:
         return n.value
 
     def profile(self, mu=1, reps=10):
-        """Average ms per product: (gather, phase 1, phase 2, total)."""
-        ms = np.zeros(4, np.float32)
+        """Average ms per product: (gather, phase 1, phase 2, sums, total)."""
+        ms = np.zeros(5, np.float32)
         _check(lib.htgpu_hmatrix_profile(self.h, mu, reps, _ptr(ms)))
         return tuple(float(v) for v in ms)
+
+    def phase_bytes(self, mu=1):
+        """Algorithmic bytes of (gather, phase 1, phase 2, sums) with the
+        current storage."""
+        b = np.zeros(4, np.int64)
+        _check(lib.htgpu_hmatrix_phase_bytes(self.h, mu, _ptr(b)))
+        return tuple(int(v) for v in b)
 
     def set_fp64_split(self, phase1_dfma_permille, phase2_dfma_permille):
         """Share (per mille) of the V-side and of the U-side/dense FP64

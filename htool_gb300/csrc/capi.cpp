@@ -251,6 +251,15 @@ int htgpu_hmatrix_infos(htgpu_hmatrix h, char *buf, int *len) {
     });
 }
 
+int htgpu_hmatrix_phase_bytes(htgpu_hmatrix h, int mu, long long *bytes) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(bytes, "bytes");
+        htgpu::require(mu > 0, "mu must be positive");
+        h->h->phase_bytes(mu, bytes);
+    });
+}
+
 int htgpu_hmatrix_product_bytes(htgpu_hmatrix h, int mu, long long *bytes) {
     return guarded([&] {
         need(h, "hmatrix");

@@ -531,6 +531,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
                 cover[a].push_back((int)zbase[g]);
         zi_h.clear();
         zl_h.clear();
+        zsum_reads_ = 0;
         for (int a = 0; a < natoms; a++) {
             ZItem zi;
             zi.row0 = cuts[a];
@@ -538,6 +539,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
             zi.lbeg = (int)zl_h.size();
             zl_h.insert(zl_h.end(), cover[a].begin(), cover[a].end());
             zi.lend = (int)zl_h.size();
+            zsum_reads_ += (long long)zi.h * (zi.lend - zi.lbeg);
             zi_h.push_back(zi);
         }
     }
@@ -660,8 +662,10 @@ void HMatrix::upload_phase1_lists() {
     // the same tiles as chunks for the streamed phase 1
     {
         std::vector<StreamChunk> ch;
+        p1_bytes_ = 0;
         for (auto &it : p1_h) {
             const LrLeaf &L = lr_h[it.leaf];
+            p1_bytes_ += 8LL * it.jlen * L.r;
             const int slot  = (int)(L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r);
             tile_section(ch, 8 * it.off, 8, it.jlen, 0, L.r, slot, L.oj + it.j0, (int)L.a_off, (it.chunk & kEmuBit) ? kStreamEmu : kStreamDfma, true);
         }
@@ -678,6 +682,7 @@ void HMatrix::upload_phase1_lists() {
     // spread by error diffusion through the stream
     std::vector<StreamChunk> ch;
     n_p2_dfma_ = n_p2_emu_ = 0;
+    p2_bytes_ = n_cols_ = 0;
     for (auto &pi : pan_h) {
         const std::size_t first = ch.size();
         stream_section(ch, 8 * pi.off, 8, pi.h, pi.ncol, pi.q0, pi.row0, kStreamDfma, 0);
@@ -692,6 +697,8 @@ void HMatrix::upload_phase1_lists() {
         ch[first].flags |= kStreamFirst;
         ch.back().flags |= kStreamLast;
         (ch[first].kind == kStreamDfma ? n_p2_dfma_ : n_p2_emu_)++;
+        p2_bytes_ += 8LL * pi.h * pi.ncol;
+        n_cols_ += pi.ncol;
     }
     n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
     n_chunks_ = (long long)ch.size();
@@ -865,6 +872,7 @@ void HMatrix::set_precision(int policy, double tau) {
     scale_d.upload(scale, stream_);
     {
         std::vector<StreamChunk> ch;
+        p1_bytes_m_ = 0;
         for (auto &m : p1m) {
             const LrLeaf &L = lr_h[m.leaf];
             const int slot  = (int)(L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r);
@@ -873,6 +881,7 @@ void HMatrix::set_precision(int policy, double tau) {
                 tile_section(ch, m.off, 4, m.jlen, 0, c, slot, L.oj + m.j0, (int)L.a_off, kStreamF32, true);
             if (L.r > c)
                 tile_section(ch, m.off + 4LL * m.jlen * c, 2, m.jlen, c, L.r - c, slot, L.oj + m.j0, (int)L.a_off, kStreamBf16, c == 0);
+            p1_bytes_m_ += 4LL * m.jlen * c + 2LL * m.jlen * (L.r - c);
         }
         const std::vector<int> r = stream_ranges(ch, stream_ctas() * kStreamWarpsPerCta * 8);
         n_p1m_ranges_            = (int)r.size() - 1;
@@ -885,8 +894,11 @@ void HMatrix::set_precision(int policy, double tau) {
     n_p1m_ = (int)p1m.size();
     {
         std::vector<StreamChunk> ch;
+        p2_bytes_m_ = n_cols_m_ = 0;
         for (auto &mi : mit) {
             const std::size_t first = ch.size();
+            p2_bytes_m_ += 8LL * mi.h * mi.n64 + 4LL * mi.h * mi.n32 + 2LL * mi.h * mi.n16;
+            n_cols_m_ += mi.n64 + mi.n32 + mi.n16;
             if (mi.n64)
                 stream_section(ch, 8 * mi.off64, 8, mi.h, mi.n64, mi.q64, mi.row0, kStreamDfma, kStreamArena1);
             if (mi.n32)
@@ -945,6 +957,8 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
         launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_,
                              status_d.p, st);
+        if (marks)
+            HTGPU_CUDA(cudaEventRecord(marks[2], st));
         launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
         launches_ += groups + 1;
         return;
@@ -977,6 +991,8 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
         launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         launches_ += groups;
+        if (marks)
+            HTGPU_CUDA(cudaEventRecord(marks[2], st));
     }
     launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
     launches_ += 1;
@@ -1057,28 +1073,36 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
 void HMatrix::profile(int mu, int reps, float *ms) {
     HTGPU_CUDA(cudaSetDevice(device_));
     ensure_work(mu);
-    cudaEvent_t ev[4];
+    cudaEvent_t ev[5];
     for (auto &e : ev)
         HTGPU_CUDA(cudaEventCreate(&e));
-    double acc[4] = {0, 0, 0, 0};
+    double acc[5] = {0, 0, 0, 0, 0};
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
     for (int r = 0; r < reps; r++) {
         HTGPU_CUDA(cudaEventRecord(ev[0], stream_));
         launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1);
-        HTGPU_CUDA(cudaEventRecord(ev[3], stream_));
-        HTGPU_CUDA(cudaEventSynchronize(ev[3]));
+        HTGPU_CUDA(cudaEventRecord(ev[4], stream_));
+        HTGPU_CUDA(cudaEventSynchronize(ev[4]));
         float t;
-        for (int k = 0; k < 3; k++) {
+        for (int k = 0; k < 4; k++) {
             HTGPU_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
             acc[k] += t;
         }
-        HTGPU_CUDA(cudaEventElapsedTime(&t, ev[0], ev[3]));
-        acc[3] += t;
+        HTGPU_CUDA(cudaEventElapsedTime(&t, ev[0], ev[4]));
+        acc[4] += t;
     }
     for (auto &e : ev)
         cudaEventDestroy(e);
-    for (int k = 0; k < 4; k++)
+    for (int k = 0; k < 5; k++)
         ms[k] = (float)(acc[k] / reps);
+}
+
+void HMatrix::phase_bytes(int mu, long long *b) const {
+    const bool red = precision_ != 0;
+    b[0]           = 8LL * nc * mu * 4 + 4LL * nc;                                          // x twice (exponent, gather), xp and xs, perm
+    b[1]           = (red ? p1_bytes_m_ : p1_bytes_) + 8LL * a_slots * mu;                  // V-side factors, partial sums
+    b[2]           = (red ? p2_bytes_m_ : p2_bytes_) + 4LL * (red ? n_cols_m_ : n_cols_) + 8LL * zlen_ * mu; // U-side + dense, column indices, z
+    b[3]           = 8LL * zsum_reads_ * mu + 8LL * nr * mu + 4LL * nr;                    // z, y, perm
 }
 
 void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {

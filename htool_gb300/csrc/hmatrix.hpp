@@ -47,6 +47,9 @@ class HMatrix {
     std::map<std::string, std::string> infos() const;
     long long stored_bytes() const;        // algorithmic bytes of one FP64 product (factors + dense)
     long long product_bytes(int mu) const; // factors + dense + x/y + permutations
+    // algorithmic bytes of the four steps of a product (gather, phase 1,
+    // phase 2, final sums) with the current storage
+    void phase_bytes(int mu, long long *bytes) const;
     const BuildStats &stats() const { return st_; }
     cudaStream_t stream() const { return stream_; }
     int device() const { return device_; }
@@ -150,6 +153,9 @@ class HMatrix {
     int n_sctas_ = 0, n_ranges_ = 0, n_ranges_m_ = 0;
     long long n_chunks_ = 0, n_chunks_m_ = 0;
     int p1_mode_ = 0;
+    // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced
+    // storage), phase-2 columns, z values read by the final sums
+    long long p1_bytes_ = 0, p2_bytes_ = 0, n_cols_ = 0, p1_bytes_m_ = 0, p2_bytes_m_ = 0, n_cols_m_ = 0, zsum_reads_ = 0;
     DevBuf<StreamChunk> p1c_d, p1cm_d; // streamed phase 1 (one or two right-hand sides)
     DevBuf<int> p1r_d, p1rm_d;
     int n_p1_ranges_ = 0, n_p1m_ranges_ = 0;

@@ -142,10 +142,17 @@ int htgpu_hmatrix_last_launches(htgpu_hmatrix h, int *launches);
 /* Timing breakdown of `reps` products with mu right-hand sides on the
  * handle's stream (device-resident input), measured with CUDA events between
  * the launches: ms[0] gather, ms[1] low-rank V-side (phase 1), ms[2]
- * U-side + dense + scatter (phase 2), ms[3] whole product; averages per
- * product.  The counterpart of the timing htool accumulates in its infos map
+ * U-side + dense (phase 2), ms[3] per-cluster sums and scatter, ms[4] whole
+ * product; averages per product.  The counterpart of the timing htool accumulates in its infos map
  * (nb_mat_vec_prod / total_time_mat_vec_prod, hmatrix.hpp:1180-1181). */
 int htgpu_hmatrix_profile(htgpu_hmatrix h, int mu, int reps, float *ms);
+
+/* Algorithmic bytes of the same four steps with the current storage (no
+ * counterpart in the reference): bytes[0] gather (x read twice, gathered
+ * copies written), bytes[1] phase 1 (V-side factors, partial sums written),
+ * bytes[2] phase 2 (U-side and dense blocks, column indices, cluster sums
+ * written), bytes[3] final sums (cluster sums read, y written, perm). */
+int htgpu_hmatrix_phase_bytes(htgpu_hmatrix h, int mu, long long *bytes);
 
 /* How the FP64 product shares its work between the FP64 pipe (DFMA) and the
  * FP32/INT pipes (exact double-float emulation, ~2^-46 relative per term):
