@@ -805,7 +805,7 @@ void HMatrix::set_precision(int policy, double tau) {
         n_bf16_cols_ += L.r - c32[l];
     }
     // 3. layout of the reduced-precision arena (bytes, 16-byte aligned blocks):
-    //    phase-1 tiles, then per phase-2 chunk an FP32 and a BF16 sub-panel
+    //    phase-1 tiles, then the phase-2 chunks of every row chunk
     auto al16 = [](long long b) { return (b + 15) & ~15LL; };
     long long off = 0;
     std::vector<P1Item> p1m;
@@ -819,52 +819,75 @@ void HMatrix::set_precision(int policy, double tau) {
         conv.push_back({it.off, off, off + 4LL * it.jlen * c32[it.leaf], it.jlen, L.r, c32[it.leaf], (int)(a_slots + L.a_off)});
         off += al16(4LL * it.jlen * c32[it.leaf] + 2LL * it.jlen * (L.r - c32[it.leaf]));
     }
-    std::vector<MixedItem> mit;
-    std::vector<int> cim;
+    // phase 2 per row chunk: the dense leaves' FP64 columns are read in place
+    // from the FP64 arena; the FP32 and the BF16 columns of all its low-rank
+    // leaves are cut into chunks stored in the lane order of the phase-2
+    // kernel (SwizzleJob)
+    std::vector<int> cim;          // per reduced-panel column: phase-1 slot (low-rank) or ~x index (dense)
+    std::vector<long long> srcoff; // per column: FP64 arena offset of its first row (low-rank columns)
+    std::vector<SwizzleJob> swz;
+    std::vector<StreamChunk> ch2;
     mixed_bytes_ = 0;
+    p2_bytes_m_ = n_cols_m_ = 0;
     for (std::size_t q = 0; q < p2_h.size(); q++) {
-        const P2Item &it = p2_h[q];
-        MixedItem mi;
-        mi.row0  = it.row0;
-        mi.h     = it.h;
-        mi.off64 = pan_h[q].off;
-        mi.q64   = (int)cim.size();
-        int n64 = 0, n32 = 0, n16 = 0;
+        const P2Item &it        = p2_h[q];
+        const int h             = it.h;
+        const std::size_t first = ch2.size();
+        const int q64           = (int)cim.size();
+        int n64                 = 0;
         for (int c = it.cbeg; c < it.cend; c++)
             if (c_leaf[c] < 0) {
                 const P2Contrib &pc = c_h[c];
-                for (int j = 0; j < pc.w; j++)
+                for (int j = 0; j < pc.w; j++) {
                     cim.push_back(~((~pc.aux) + j));
+                    srcoff.push_back(-1);
+                }
                 n64 += pc.w;
-            } else {
-                n32 += c32[c_leaf[c]];
-                n16 += lr_h[c_leaf[c]].r - c32[c_leaf[c]];
             }
-        mi.n64 = n64;
-        mi.q32 = (int)cim.size();
-        mi.n32 = n32;
-        mi.off32 = off;
-        mi.off16 = off + al16(4LL * it.h * n32);
-        for (int c = it.cbeg; c < it.cend; c++)
-            if (c_leaf[c] >= 0)
-                for (int k = 0; k < c32[c_leaf[c]]; k++)
-                    cim.push_back((int)lr_h[c_leaf[c]].a_off + k);
-        mi.q16 = (int)cim.size();
-        mi.n16 = n16;
-        int f32c = 0, b16c = 0;
-        for (int c = it.cbeg; c < it.cend; c++)
-            if (c_leaf[c] >= 0) {
-                const int l     = c_leaf[c];
-                const LrLeaf &L = lr_h[l];
-                for (int k = c32[l]; k < L.r; k++)
-                    cim.push_back((int)L.a_off + k);
-                conv.push_back({c_h[c].off, mi.off32 + 4LL * it.h * f32c, mi.off16 + 2LL * it.h * b16c, it.h, L.r, c32[l], (int)L.a_off});
-                f32c += c32[l];
-                b16c += L.r - c32[l];
+        if (n64)
+            stream_section(ch2, 8 * pan_h[q].off, 8, h, n64, q64, it.row0, kStreamDfma, kStreamArena1);
+        for (int part = 0; part < 2; part++) { // FP32 columns, then BF16 columns
+            // (single-row chunks keep their BF16 columns as FP32: a lane group
+            // of 8 BF16 columns would span 256 coefficient positions)
+            const int es = (part == 0 || h == 1) ? 4 : 2;
+            const int q0 = (int)cim.size();
+            for (int c = it.cbeg; c < it.cend; c++)
+                if (c_leaf[c] >= 0) {
+                    const LrLeaf &L = lr_h[c_leaf[c]];
+                    const int k0 = part == 0 ? 0 : c32[c_leaf[c]], k1 = part == 0 ? c32[c_leaf[c]] : L.r;
+                    for (int k = k0; k < k1; k++) {
+                        cim.push_back((int)L.a_off + k);
+                        srcoff.push_back(c_h[c].off + (long long)h * k);
+                    }
+                }
+            const int n = (int)cim.size() - q0;
+            const int S = 32 / h, V = 16 / es;
+            const int nmax = std::min(kStreamCols, (kStreamStage / (S * h * 16)) * V * S);
+            for (int c0 = 0; c0 < n; c0 += nmax) {
+                const int nc = std::min(nmax, n - c0);
+                StreamChunk k;
+                k.src   = off;
+                k.bytes = swizzle_bytes(h, nc, es);
+                k.a     = q0 + c0;
+                k.b     = it.row0;
+                k.c     = 0;
+                k.h     = h;
+                k.ncol  = nc;
+                k.kind  = es == 4 ? kStreamF32 : kStreamBf16;
+                k.flags = 0;
+                k.pad   = 0;
+                ch2.push_back(k);
+                swz.push_back({off, q0 + c0, nc, h, es});
+                off += k.bytes;
             }
-        mixed_bytes_ += 8LL * it.h * n64;
-        off = mi.off16 + al16(2LL * it.h * n16);
-        mit.push_back(mi);
+            p2_bytes_m_ += (long long)es * h * n;
+            n_cols_m_ += n;
+        }
+        ch2[first].flags |= kStreamFirst;
+        ch2.back().flags |= kStreamLast;
+        p2_bytes_m_ += 8LL * h * n64;
+        n_cols_m_ += n64;
+        mixed_bytes_ += 8LL * h * n64;
     }
     for (std::size_t l = 0; l < lr_h.size(); l++)
         mixed_bytes_ += (4LL * c32[l] + 2LL * (lr_h[l].r - c32[l])) * (lr_h[l].m + lr_h[l].n);
@@ -892,30 +915,15 @@ void HMatrix::set_precision(int policy, double tau) {
     }
     p1m_d.upload(p1m, stream_);
     n_p1m_ = (int)p1m.size();
+    n_chunks_m_ = (long long)ch2.size();
+    scm_d.upload(ch2, stream_);
     {
-        std::vector<StreamChunk> ch;
-        p2_bytes_m_ = n_cols_m_ = 0;
-        for (auto &mi : mit) {
-            const std::size_t first = ch.size();
-            p2_bytes_m_ += 8LL * mi.h * mi.n64 + 4LL * mi.h * mi.n32 + 2LL * mi.h * mi.n16;
-            n_cols_m_ += mi.n64 + mi.n32 + mi.n16;
-            if (mi.n64)
-                stream_section(ch, 8 * mi.off64, 8, mi.h, mi.n64, mi.q64, mi.row0, kStreamDfma, kStreamArena1);
-            if (mi.n32)
-                stream_section(ch, mi.off32, 4, mi.h, mi.n32, mi.q32, mi.row0, kStreamF32, 0);
-            if (mi.n16)
-                stream_section(ch, mi.off16, 2, mi.h, mi.n16, mi.q16, mi.row0, kStreamBf16, 0);
-            ch[first].flags |= kStreamFirst;
-            ch.back().flags |= kStreamLast;
-        }
-        n_chunks_m_ = (long long)ch.size();
-        scm_d.upload(ch, stream_);
-        const std::vector<int> r = stream_ranges(ch, n_sctas_);
+        const std::vector<int> r = stream_ranges(ch2, n_sctas_);
         n_ranges_m_              = (int)r.size() - 1;
         srm_d.upload(r, stream_);
-        if (ch.empty())
-            scm_d.alloc(1);
     }
+    if (ch2.empty())
+        scm_d.alloc(1);
     cim.resize(cim.size() + 4, 0); // bulk copies read whole 16-byte words
     cidxm_d.upload(cim, stream_);
     if (p1m.empty())
@@ -926,6 +934,11 @@ void HMatrix::set_precision(int policy, double tau) {
         DevBuf<ConvertJob> dc;
         dc.upload(conv, stream_);
         launch_convert(dc.p, (int)conv.size(), fac.p, cmax.p, mix_.p, stream_);
+        DevBuf<SwizzleJob> dz;
+        DevBuf<long long> dso;
+        dz.upload(swz, stream_);
+        dso.upload(srcoff, stream_);
+        launch_swizzle(dz.p, (int)swz.size(), fac.p, dso.p, cidxm_d.p, cmax.p, mix_.p, stream_);
         HTGPU_CUDA(cudaStreamSynchronize(stream_));
     }
 }

@@ -106,12 +106,6 @@ struct PanelItem { // z rows row0 .. row0+h += panel (h x ncol, column-major, ld
     int q0, ncol;
 };
 
-struct MixedItem { // a reduced-precision phase-2 panel: dense FP64 columns, FP32 columns, BF16 columns
-    long long off64, off32, off16; // FP64 arena (elements), reduced arena (bytes) x2
-    int row0, h;
-    int q64, n64, q32, n32, q16, n16; // column index ranges in cidx
-};
-
 // Streamed products: one chunk = up to kStreamCols columns of one phase-2
 // row chunk's panel, or up to 16 whole columns of one phase-1 tile; all of
 // one element kind, contiguous in an arena

@@ -76,6 +76,21 @@ struct ConvertJob { // FP64 block at src (elements) -> FP32 columns at dst32, BF
     long long src, dst32, dst16;
     int rows, cols, c32, slot;
 };
+// one phase-2 chunk of FP32 (es 4) or BF16 (es 2) columns in the lane
+// order the phase-2 kernel reads: columns q0 .. q0+n of the reduced column
+// list (FP64 source of column q at fac + srcoff[q], scale slot cidx[q]),
+// h rows; lane (row, slice) of S = 32 / h slices owns columns slice + S j and
+// finds them V = 16 / es at a time in 16 contiguous bytes (zeros pad)
+struct SwizzleJob {
+    long long dst; // bytes in the reduced arena
+    int q0, n, h, es;
+};
+void launch_swizzle(const SwizzleJob *jobs, int njobs, const double *fac, const long long *srcoff, const int *slot, const unsigned *cmax, unsigned char *mix, cudaStream_t st);
+// bytes of such a chunk
+inline int swizzle_bytes(int h, int n, int es) {
+    const int S = 32 / h, V = 16 / es, J = (n + S - 1) / S;
+    return ((J + V - 1) / V) * S * h * 16;
+}
 void launch_colmax(const ColMaxJob *jobs, int njobs, const double *fac, unsigned *cmax, cudaStream_t st);
 void launch_convert(const ConvertJob *jobs, int njobs, const double *fac, const unsigned *cmax, unsigned char *mix, cudaStream_t st);
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);

@@ -144,7 +144,7 @@ __device__ __forceinline__ void phase1_tile_dfma(const P1Item &it, const LrLeaf 
 #pragma unroll
         for (int t = 0; t < RPL; t++) {
             const int jj = s0 + lane + 32 * t;
-            cur[t]       = jj < jlen ? V[jj] : 0.;
+            cur[t]       = jj < jlen ? __ldcs(V + jj) : 0.; // read once: evict first
         }
         for (int kg = 0; kg < L.r; kg += KG) {
             double acc[16];
@@ -159,7 +159,7 @@ __device__ __forceinline__ void phase1_tile_dfma(const P1Item &it, const LrLeaf 
 #pragma unroll
                     for (int t = 0; t < RPL; t++) {
                         const int jj = s0 + lane + 32 * t;
-                        nxt[t]       = (k + 1 < L.r && jj < jlen) ? Vn[jj] : 0.;
+                        nxt[t]       = (k + 1 < L.r && jj < jlen) ? __ldcs(Vn + jj) : 0.;
                     }
 #pragma unroll
                     for (int t = 0; t < RPL; t++)
@@ -213,7 +213,7 @@ __device__ __forceinline__ void phase1_tile_emu(const P1Item &it, const LrLeaf &
 #pragma unroll
                     for (int t = 0; t < RPL; t++) {
                         const int jj = s0 + lane + 32 * t;
-                        v[t]         = jj < jlen ? Vk[jj] : 0.;
+                        v[t]         = jj < jlen ? __ldcs(Vk + jj) : 0.;
                     }
 #pragma unroll
                     for (int t = 0; t < RPL; t++) {

@@ -55,6 +55,28 @@ __global__ void convert_kernel(const ConvertJob *__restrict__ jobs, const double
     }
 }
 
+__global__ void swizzle_kernel(const SwizzleJob *__restrict__ jobs, const double *__restrict__ fac, const long long *__restrict__ srcoff, const int *__restrict__ slot,
+                               const unsigned *__restrict__ cmax, unsigned char *__restrict__ mix) {
+    const SwizzleJob J = jobs[blockIdx.x];
+    const int S = 32 / J.h, L = S * J.h, V = 16 / J.es;
+    const int G = ((J.n + S - 1) / S + V - 1) / V;
+    const int total = G * L * V;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int g = e / (L * V), rem = e % (L * V), l = rem / V, v = rem % V;
+        const int slice = l / J.h, row = l % J.h;
+        const int q     = slice + S * (g * V + v);
+        float val       = 0.f;
+        if (q < J.n) {
+            const float mx = __uint_as_float(cmax[slot[J.q0 + q]]);
+            val            = mx > 0.f ? (float)(fac[srcoff[J.q0 + q] + row] / (double)mx) : 0.f;
+        }
+        if (J.es == 4)
+            reinterpret_cast<float *>(mix + J.dst)[e] = val;
+        else
+            reinterpret_cast<__nv_bfloat16 *>(mix + J.dst)[e] = __float2bfloat16_rn(val);
+    }
+}
+
 // Phase 1: a_k = s_k * sum_j v_hat[j, k] x[j] per tile, FP32 arithmetic,
 // butterfly reduce-scatter over 16 accumulators, FP64 result
 __device__ __forceinline__ void rs16f(float (&v)[16], int lane) {
@@ -200,6 +222,13 @@ void launch_convert(const ConvertJob *jobs, int njobs, const double *fac, const 
     if (njobs <= 0)
         return;
     convert_kernel<<<njobs, 128, 0, st>>>(jobs, fac, cmax, mix);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_swizzle(const SwizzleJob *jobs, int njobs, const double *fac, const long long *srcoff, const int *slot, const unsigned *cmax, unsigned char *mix, cudaStream_t st) {
+    if (njobs <= 0)
+        return;
+    swizzle_kernel<<<njobs, 128, 0, st>>>(jobs, fac, srcoff, slot, cmax, mix);
     HTGPU_CUDA(cudaGetLastError());
 }
 

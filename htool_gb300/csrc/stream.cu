@@ -33,7 +33,6 @@ constexpr int kWarps     = kStreamWarpsPerCta;
 constexpr int kStages    = 3;  // per warp
 constexpr int kDataBuf   = kStreamStage + 32;
 constexpr int kIdxBuf    = kStreamCols * 4 + 32;
-constexpr int kWarpSmem  = (kStages * (kDataBuf + kIdxBuf + (int)sizeof(StreamChunk) + 8) + 127) & ~127;
 constexpr long long kWaitCycles = 4000000000ll;
 
 __device__ __forceinline__ unsigned sa(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -72,6 +71,19 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sa(dst)), "l"(src), "r"(bytes), "r"(sa(bar)) : "memory");
 }
 
+// L2 policy for data read once (the factor arena): evicted first, so the
+// small vectors gathered per column (phase-1 sums, x) stay in L2
+__device__ __forceinline__ unsigned long long evict_first_policy() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ void bulk_load_stream(void *dst, const void *src, unsigned bytes, unsigned long long *bar, unsigned long long policy) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(sa(dst)), "l"(src), "r"(bytes), "r"(sa(bar)), "l"(policy)
+                 : "memory");
+}
+
 __device__ __forceinline__ float bf16f(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
 
 __device__ __forceinline__ void df_addf(DF &a, float p) {
@@ -96,17 +108,28 @@ struct Seq {
 };
 
 template <int MU>
+struct P2Smem { // per warp: data stages, column-index stages, descriptors, barriers, coefficients
+    static constexpr int kIdx   = kStages * kDataBuf;
+    static constexpr int kDesc  = kIdx + kStages * kIdxBuf;
+    static constexpr int kBar   = kDesc + kStages * (int)sizeof(StreamChunk);
+    static constexpr int kCoef  = (kBar + kStages * 8 + 15) & ~15;
+    static constexpr int kTotal = (kCoef + 128 * MU * 4 + 127) & ~127;
+};
+
+template <int MU>
 __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
     phase2_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena0,
                        const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
                        const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen, int *__restrict__ status) {
+    using L = P2Smem<MU>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *wbase    = smem + (size_t)wid * kWarpSmem;
-    unsigned char *dbuf     = wbase;                                    // kStages x kDataBuf
-    int *ibuf               = reinterpret_cast<int *>(wbase + kStages * kDataBuf); // kStages x kIdxBuf bytes
-    StreamChunk *desc       = reinterpret_cast<StreamChunk *>(wbase + kStages * (kDataBuf + kIdxBuf));
-    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + kStages * (kDataBuf + kIdxBuf + (int)sizeof(StreamChunk)));
+    unsigned char *wbase    = smem + (size_t)wid * L::kTotal;
+    unsigned char *dbuf     = wbase;                                  // kStages x kDataBuf
+    int *ibuf               = reinterpret_cast<int *>(wbase + L::kIdx); // kStages x kIdxBuf bytes
+    StreamChunk *desc       = reinterpret_cast<StreamChunk *>(wbase + L::kDesc);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + L::kBar);
+    float *cf               = reinterpret_cast<float *>(wbase + L::kCoef); // MU x 128: FP32 / BF16 chunk coefficients in lane order
     const int xe            = max(*xexp, 1);
     if (lane == 0)
         for (int s = 0; s < kStages; s++)
@@ -157,8 +180,8 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
                 const long long i0 = (4LL * c.a) & ~15LL, i1 = (4LL * (c.a + c.ncol) + 15) & ~15LL;
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0 + i1 - i0));
-                bulk_load(dbuf + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), &bar[s]);
-                bulk_load(reinterpret_cast<unsigned char *>(ibuf) + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), &bar[s]);
+                bulk_load_stream(dbuf + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), &bar[s], evict_first_policy());
+                bulk_load_stream(reinterpret_cast<unsigned char *>(ibuf) + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), &bar[s], evict_first_policy());
             }
             issued++;
             ip++;
@@ -190,6 +213,30 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
         }
     };
 
+    // coefficients of an FP32 / BF16 chunk (in the units of x, as floats) in
+    // the lane order of its data: column t = slice + S j sits at
+    // ((j / V) S + slice) V + j % V, so a lane reads V of them at once
+    auto stage_coefs = [&](const StreamChunk &c, const double (&r)[kStreamCols / 32][MU]) {
+        if (c.kind != kStreamF32 && c.kind != kStreamBf16)
+            return;
+        const int S = 32 / c.h, V = c.kind == kStreamF32 ? 4 : 8;
+        for (int i = lane; i < 128 * MU; i += 32)
+            cf[i] = 0.f;
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            const int t = lane + 32 * j;
+            if (t < c.ncol) {
+                const int jj = t / S, sl = t - jj * S;
+                const int pos = ((jj / V) * S + sl) * V + jj % V;
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    cf[cc * 128 + pos] = (float)scale_pow2_safe(r[j][cc], 1023 - xe);
+            }
+        }
+        __syncwarp();
+    };
+
     double dacc[MU];
     DF acc[MU];
 #pragma unroll
@@ -210,6 +257,7 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
                 break;
             }
             gather(s, raw, kk);
+            stage_coefs(desc[s], raw);
         }
         // chunk done+1: wait for it (normally landed) and start its coefficients
         have_nx = false;
@@ -272,40 +320,55 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
                     df_renorm(acc[cc]);
-            } else {
-                float a[MU], part[MU];
+            }
+        }
+        if (c.kind == kStreamF32 || c.kind == kStreamBf16) {
+            // lane order: 16 bytes of V elements per lane and group of V
+            // columns, coefficients alongside in shared memory
+            const int V = c.kind == kStreamF32 ? 4 : 8;
+            const int Ln = S * h, J = (c.ncol + S - 1) / S, G = (J + V - 1) / V;
+            float part[MU], part2[MU];
 #pragma unroll
-                for (int cc = 0; cc < MU; cc++) {
-                    a[cc]    = (float)scale_pow2_safe(raw[j][cc], 1023 - xe);
-                    part[cc] = 0.f;
-                }
-                if (c.kind == kStreamF32) {
-                    const float *P = reinterpret_cast<const float *>(buf) + row + (size_t)h * q0;
-#pragma unroll 4
-                    for (int j0 = 0; j0 < qc; j0 += S) {
-                        const int jj   = j0 + slice;
-                        const bool use = live && jj < qc;
-                        const float u  = use ? P[h * jj] : 0.f;
+            for (int cc = 0; cc < MU; cc++)
+                part[cc] = part2[cc] = 0.f;
+            if (lane < Ln) {
+                const uint4 *D = reinterpret_cast<const uint4 *>(buf) + lane;
+                if (V == 4) {
+#pragma unroll 2
+                    for (int g = 0; g < G; g++) {
+                        const uint4 w = D[g * Ln];
 #pragma unroll
-                        for (int cc = 0; cc < MU; cc++)
-                            part[cc] = fmaf(u, __shfl_sync(0xffffffffu, a[cc], use ? jj : 0), part[cc]);
+                        for (int cc = 0; cc < MU; cc++) {
+                            const float4 cv = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 4);
+                            part[cc]        = fmaf(__uint_as_float(w.x), cv.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.y), cv.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.z), cv.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.w), cv.w, part2[cc]);
+                        }
                     }
                 } else {
-                    const unsigned short *P = reinterpret_cast<const unsigned short *>(buf) + row + (size_t)h * q0;
-#pragma unroll 4
-                    for (int j0 = 0; j0 < qc; j0 += S) {
-                        const int jj   = j0 + slice;
-                        const bool use = live && jj < qc;
-                        const float u  = use ? bf16f(P[h * jj]) : 0.f;
+#pragma unroll 2
+                    for (int g = 0; g < G; g++) {
+                        const uint4 w = D[g * Ln];
 #pragma unroll
-                        for (int cc = 0; cc < MU; cc++)
-                            part[cc] = fmaf(u, __shfl_sync(0xffffffffu, a[cc], use ? jj : 0), part[cc]);
+                        for (int cc = 0; cc < MU; cc++) {
+                            const float4 c0 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8);
+                            const float4 c1 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8 + 4);
+                            part[cc]        = fmaf(__uint_as_float(w.x << 16), c0.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.x & 0xffff0000u), c0.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.y << 16), c0.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.y & 0xffff0000u), c0.w, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.z << 16), c1.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.z & 0xffff0000u), c1.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.w << 16), c1.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.w & 0xffff0000u), c1.w, part2[cc]);
+                        }
                     }
                 }
-#pragma unroll
-                for (int cc = 0; cc < MU; cc++)
-                    df_addf(acc[cc], part[cc]);
             }
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                df_addf(acc[cc], part[cc] + part2[cc]);
         }
         if (c.flags & kStreamLast) {
             double v[MU];
@@ -349,6 +412,8 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
                 raw[j][cc] = rnx[j][cc];
         }
         have = have_nx;
+        if (have) // the next chunk's coefficients, loaded during this one
+            stage_coefs(desc[done % kStages], raw);
         issue_more();
     }
     if (!ok) {
@@ -633,7 +698,7 @@ __global__ void __launch_bounds__(32 * kWarps, 3)
                 const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0));
-                bulk_load(dbuf + (size_t)s * kDataBuf, arena + a0, (unsigned)(a1 - a0), &bar[s]);
+                bulk_load_stream(dbuf + (size_t)s * kDataBuf, arena + a0, (unsigned)(a1 - a0), &bar[s], evict_first_policy());
             }
             issued++;
             ip++;
@@ -729,7 +794,7 @@ template <int MU>
 void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
                     const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
-    const int bytes                = kWarps * kWarpSmem;
+    const int bytes                = kWarps * P2Smem<MU>::kTotal;
     int dev                        = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
     if (dev >= 64 || !(done >> dev & 1)) {
