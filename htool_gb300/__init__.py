@@ -74,6 +74,18 @@ def _load():
         "htgpu_hmatrix_mvprod_noalloc": (i, [vp, vp, vp, i, vp]),
         "htgpu_hmatrix_set_precision": (i, [vp, i, d]),
         "htgpu_hmatrix_precision_info": (i, [vp, vp, vp, vp, vp]),
+        "htgpu_mlp_num_params": (i, []),
+        "htgpu_mlp_create": (i, [i, C.c_ulonglong, vp]),
+        "htgpu_mlp_destroy": (i, [vp]),
+        "htgpu_mlp_set_params": (i, [vp, vp]),
+        "htgpu_mlp_get_params": (i, [vp, vp]),
+        "htgpu_mlp_train": (i, [vp, vp, vp, i, i, i, C.c_float, C.c_ulonglong, vp]),
+        "htgpu_mlp_gradient": (i, [vp, vp, vp, i, vp, vp]),
+        "htgpu_mlp_predict": (i, [vp, vp, i, vp]),
+        "htgpu_block_features": (i, [i, i, d, d, vp, vp, d, i, vp]),
+        "htgpu_hmatrix_set_rank_predictor": (i, [vp, vp, d]),
+        "htgpu_hmatrix_set_aca_budget": (i, [vp, C.c_longlong]),
+        "htgpu_hmatrix_aca_samples": (i, [vp, vp, vp, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -351,6 +363,29 @@ class HMatrix:
     def __matmul__(self, x):
         return self.mvprod_global_to_global(x, 1)
 
+    def set_rank_predictor(self, predictor, margin=0.25):
+        """Size the first ACA attempt of later builds with a RankPredictor
+        (None restores the fixed first attempt)."""
+        self._predictor = predictor  # kept alive as long as the H-matrix uses it
+        _check(lib.htgpu_hmatrix_set_rank_predictor(self.h, predictor.h if predictor is not None else None, float(margin)))
+        return self
+
+    def set_aca_budget(self, nbytes):
+        """Device bytes of ACA scratch per slice of blocks (0: 60% of free memory)."""
+        _check(lib.htgpu_hmatrix_set_aca_budget(self.h, int(nbytes)))
+        return self
+
+    def aca_samples(self):
+        """(features n x 10 float32, crosses needed n float32) of every block
+        the last build's partialACA decided."""
+        n = C.c_int()
+        _check(lib.htgpu_hmatrix_aca_samples(self.h, None, None, 0, C.byref(n)))
+        X = np.empty((n.value, 10), np.float32)
+        y = np.empty(n.value, np.float32)
+        if n.value:
+            _check(lib.htgpu_hmatrix_aca_samples(self.h, _ptr(X), _ptr(y), n.value, C.byref(n)))
+        return X, y
+
     def __del__(self):
         try:
             if self.h:
@@ -358,3 +393,69 @@ class HMatrix:
                 self.h = None
         except Exception:
             pass
+
+
+class RankPredictor:
+    """The 10 -> 64 -> 64 -> 1 ACA rank predictor, trained and evaluated on
+    the GPU by the library's own kernels."""
+
+    NUM_PARAMS = None
+
+    def __init__(self, device=0, seed=0):
+        h = C.c_void_p()
+        _check(lib.htgpu_mlp_create(int(device), int(seed), C.byref(h)))
+        self.h = h
+        RankPredictor.NUM_PARAMS = lib.htgpu_mlp_num_params()
+
+    @property
+    def params(self):
+        p = np.empty(lib.htgpu_mlp_num_params(), np.float32)
+        _check(lib.htgpu_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.size != lib.htgpu_mlp_num_params():
+            raise ValueError("[Htool error] expected %d parameters" % lib.htgpu_mlp_num_params())
+        _check(lib.htgpu_mlp_set_params(self.h, _ptr(p)))
+
+    def train(self, X, y, epochs=20, batch=4096, lr=1e-3, seed=0):
+        """Adam on the mean squared error; returns the loss after each epoch."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = np.empty(epochs, np.float32)
+        _check(lib.htgpu_mlp_train(self.h, _ptr(X), _ptr(y), int(y.size), int(epochs), int(batch), float(lr), int(seed), _ptr(loss)))
+        return loss
+
+    def gradient(self, X, y):
+        """(loss, gradient) of the mean squared error over all samples."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.empty(lib.htgpu_mlp_num_params(), np.float32)
+        loss = C.c_float()
+        _check(lib.htgpu_mlp_gradient(self.h, _ptr(X), _ptr(y), int(y.size), _ptr(g), C.byref(loss)))
+        return float(loss.value), g
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.empty(X.shape[0], np.float32)
+        _check(lib.htgpu_mlp_predict(self.h, _ptr(X), int(X.shape[0]), _ptr(y)))
+        return y
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib.htgpu_mlp_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def block_features(M, N, rad_t, rad_s, ctr_t, ctr_s, epsilon, kernel_id):
+    """The predictor's 10 features of one admissible block."""
+    f = np.empty(10, np.float32)
+    ct = np.ascontiguousarray(ctr_t, dtype=np.float64)
+    cs = np.ascontiguousarray(ctr_s, dtype=np.float64)
+    _check(lib.htgpu_block_features(int(M), int(N), float(rad_t), float(rad_s), _ptr(ct), _ptr(cs), float(epsilon), int(kernel_id), _ptr(f)))
+    return f

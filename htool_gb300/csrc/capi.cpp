@@ -15,6 +15,10 @@ struct htgpu_hmatrix_s {
     std::unique_ptr<htgpu::HMatrix> h;
 };
 
+struct htgpu_mlp_s {
+    std::unique_ptr<htgpu::Mlp> m;
+};
+
 namespace {
 thread_local std::string g_last_error;
 
@@ -360,6 +364,121 @@ int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out,
         if (h == nullptr)
             throw htgpu::Error(HTGPU_ERR_INVALID, "[Htool error] hmatrix is null");
         h->h->mvprod_noalloc(in, out, mu, (cudaStream_t)stream);
+    });
+}
+
+// ---- ACA rank predictor ------------------------------------------------------
+int htgpu_mlp_num_params(void) { return htgpu::kMlpParams; }
+
+int htgpu_mlp_create(int device, unsigned long long seed, htgpu_mlp *out) {
+    return guarded([&] {
+        need(out, "out");
+        auto *m = new htgpu_mlp_s;
+        try {
+            m->m.reset(new htgpu::Mlp(seed, device));
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+    });
+}
+
+int htgpu_mlp_destroy(htgpu_mlp m) {
+    return guarded([&] { delete m; });
+}
+
+int htgpu_mlp_set_params(htgpu_mlp m, const float *params) {
+    return guarded([&] {
+        need(m, "mlp");
+        need(params, "params");
+        m->m->set_params(params);
+    });
+}
+
+int htgpu_mlp_get_params(htgpu_mlp m, float *params) {
+    return guarded([&] {
+        need(m, "mlp");
+        need(params, "params");
+        m->m->get_params(params);
+    });
+}
+
+int htgpu_mlp_train(htgpu_mlp m, const float *features, const float *ranks, int n, int epochs, int batch, float lr, unsigned long long seed, float *loss_per_epoch) {
+    return guarded([&] {
+        need(m, "mlp");
+        need(features, "features");
+        need(ranks, "ranks");
+        m->m->train(features, ranks, n, epochs, batch, lr, seed, loss_per_epoch);
+    });
+}
+
+int htgpu_mlp_gradient(htgpu_mlp m, const float *features, const float *ranks, int n, float *grad, float *loss) {
+    return guarded([&] {
+        need(m, "mlp");
+        need(features, "features");
+        need(ranks, "ranks");
+        need(grad, "grad");
+        const float l = m->m->gradient(features, ranks, n, grad);
+        if (loss)
+            *loss = l;
+    });
+}
+
+int htgpu_mlp_predict(htgpu_mlp m, const float *features, int n, float *ranks) {
+    return guarded([&] {
+        need(m, "mlp");
+        htgpu::require(n >= 0, "n must be non-negative");
+        if (n == 0)
+            return;
+        need(features, "features");
+        need(ranks, "ranks");
+        m->m->predict(features, n, ranks);
+    });
+}
+
+int htgpu_block_features(int M, int N, double rad_t, double rad_s, const double *ctr_t, const double *ctr_s, double epsilon, int kernel_id, float *features) {
+    return guarded([&] {
+        need(ctr_t, "ctr_t");
+        need(ctr_s, "ctr_s");
+        need(features, "features");
+        htgpu::require(M > 0 && N > 0, "block sizes must be positive");
+        htgpu::block_features(M, N, rad_t, rad_s, ctr_t, ctr_s, epsilon, kernel_id, features);
+    });
+}
+
+int htgpu_hmatrix_set_rank_predictor(htgpu_hmatrix h, htgpu_mlp m, double margin) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        htgpu::require(margin >= 0, "margin must be non-negative");
+        if (m)
+            htgpu::require(m->m->device() == h->h->device(), "predictor and H-matrix on different devices");
+        h->h->set_rank_predictor(m ? m->m.get() : nullptr, margin);
+    });
+}
+
+int htgpu_hmatrix_set_aca_budget(htgpu_hmatrix h, long long bytes) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        htgpu::require(bytes >= 0, "budget must be non-negative");
+        h->h->set_aca_budget(bytes);
+    });
+}
+
+int htgpu_hmatrix_aca_samples(htgpu_hmatrix h, float *features, float *ranks, int capacity, int *count) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(count, "count");
+        const auto &x = h->h->aca_features();
+        const auto &y = h->h->aca_labels();
+        *count        = (int)y.size();
+        if (features || ranks) {
+            need(features, "features");
+            need(ranks, "ranks");
+            htgpu::require(capacity >= (int)y.size(), "capacity below the number of samples");
+            std::memcpy(features, x.data(), sizeof(float) * x.size());
+            std::memcpy(ranks, y.data(), sizeof(float) * y.size());
+        }
     });
 }
 

@@ -83,6 +83,8 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
     require(kd.id == 0 || kd.id == 1, "device generator id must be 0 (1/(1e-5+r)) or 1 (Laplace) for a real H-matrix", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
     st_             = BuildStats();
+    samples_x_.clear();
+    samples_y_.clear();
     const double t0 = now();
     bp.eta          = eta_;
     std::vector<BlockTask> tasks = build_local_tasks(*T, *S, bp);
@@ -164,10 +166,34 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
         });
         std::size_t free_b = 0, total_b = 0;
         HTGPU_CUDA(cudaMemGetInfo(&free_b, &total_b));
-        const long long budget = (long long)(0.6 * (double)free_b) / 9; // 8 B factors + 1 B flags per slot
+        const long long budget = (aca_budget_ > 0 ? aca_budget_ : (long long)(0.6 * (double)free_b)) / 9; // 8 B factors + 1 B flags per slot
         std::vector<int> next;
         std::size_t pos = 0;
         while (pos < pending.size()) {
+            // first attempts (including blocks split off earlier in this
+            // round): scratch sized by the rank predictor when one is set
+            if (predictor_) {
+                std::vector<int> fresh;
+                for (std::size_t k = pos; k < pending.size(); k++)
+                    if (reqs[pending[k]].cap == 0)
+                        fresh.push_back(pending[k]);
+                if (!fresh.empty()) {
+                    std::vector<float> fx(fresh.size() * kMlpIn), fy(fresh.size());
+                    for (std::size_t i = 0; i < fresh.size(); i++) {
+                        const ClusterNode &tn = T->nodes[reqs[fresh[i]].t], &sn = S->nodes[reqs[fresh[i]].s];
+                        block_features(tn.size, sn.size, tn.rad, sn.rad, tn.ctr, sn.ctr, eps_, kd.id, &fx[i * kMlpIn]);
+                    }
+                    predictor_->predict(fx.data(), (int)fresh.size(), fy.data());
+                    for (std::size_t i = 0; i < fresh.size(); i++) {
+                        Req &r         = reqs[fresh[i]];
+                        const int qmax = max_profitable_rank(T->nodes[r.t].size, S->nodes[r.s].size);
+                        const float pr = fy[i];
+                        const int want = pr >= 60.f ? qmax : (int)std::ceil(std::max(pr, 0.f) * (1.0 + margin_)) + 2;
+                        r.cap          = std::max(1, std::min(qmax, std::max(want, 4)));
+                        st_.predicted_blocks++;
+                    }
+                }
+            }
             // a slice of requests whose scratch fits the budget
             std::vector<AcaBlock> blocks;
             std::vector<int> ids;
@@ -206,6 +232,8 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             DevBuf<int> dranks;
             dblocks.upload(blocks, stream_);
             scratch.alloc(sc);
+            st_.aca_scratch_bytes += 8 * sc;
+            st_.aca_peak_scratch_bytes = std::max(st_.aca_peak_scratch_bytes, 8 * sc);
             flags.alloc(fl);
             dranks.alloc(blocks.size());
             launch_partial_aca(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, perm_t.p, perm_s.p, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
@@ -221,6 +249,13 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             for (std::size_t b = 0; b < blocks.size(); b++) {
                 const int id = ids[b];
                 const int r  = ranks[b];
+                if (r > 0 || r == -1) { // a decided block: a training sample for the rank predictor
+                    const ClusterNode &tn = T->nodes[reqs[id].t], &sn = S->nodes[reqs[id].s];
+                    const std::size_t at  = samples_x_.size();
+                    samples_x_.resize(at + kMlpIn);
+                    block_features(tn.size, sn.size, tn.rad, sn.rad, tn.ctr, sn.ctr, eps_, kd.id, &samples_x_[at]);
+                    samples_y_.push_back((float)(r > 0 ? r : max_profitable_rank(tn.size, sn.size)));
+                }
                 if (r > 0) {
                     reqs[id].state = 1;
                     PackItem it;
@@ -1262,6 +1297,9 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["Local_size_mean"]          = num(nr);
     m["Local_size_min"]           = inum(nr);
     m["GPU_aca_rounds"]           = num(st_.aca_rounds);
+    m["GPU_aca_scratch_bytes"]      = inum(st_.aca_scratch_bytes);
+    m["GPU_aca_peak_scratch_bytes"] = inum(st_.aca_peak_scratch_bytes);
+    m["GPU_aca_predicted_blocks"]   = inum(st_.predicted_blocks);
     m["GPU_aca_blocks"]           = inum(st_.aca_blocks);
     m["GPU_aca_overflow_reruns"]  = num(st_.overflow_reruns);
     m["GPU_aca_seconds"]          = num(st_.aca_seconds);

@@ -12,7 +12,11 @@ struct BuildStats {
     double block_tree_seconds = 0, build_seconds = 0, aca_seconds = 0;
     int aca_rounds = 0, false_positive = 0, overflow_reruns = 0;
     long long aca_blocks = 0;
+    long long aca_scratch_bytes = 0, aca_peak_scratch_bytes = 0; // summed / largest slice of ACA scratch
+    long long predicted_blocks = 0;                              // first attempts sized by the rank predictor
 };
+
+class Mlp;
 
 class HMatrix {
   public:
@@ -22,6 +26,20 @@ class HMatrix {
     // HMatrix::build(gen, xt, xs) with partialACA and a built-in device
     // generator (include/htool/types/hmatrix.hpp:286-341)
     void build(const KernelDesc &kd, const double *xt, const double *xs);
+
+    // ACA scratch: device bytes one slice of blocks may use (0: 60% of the
+    // free memory), and an optional rank predictor that sizes every block's
+    // first attempt (margin: relative head-room over the prediction); the
+    // predictor must outlive the builds that use it
+    void set_aca_budget(long long bytes) { aca_budget_ = bytes; }
+    void set_rank_predictor(Mlp *mlp, double margin) {
+        predictor_ = mlp;
+        margin_    = margin;
+    }
+    // (features, scratch columns needed) of every block the last build's ACA
+    // decided: the rank, or the largest profitable rank for a rejected block
+    const std::vector<float> &aca_features() const { return samples_x_; }
+    const std::vector<float> &aca_labels() const { return samples_y_; }
 
     // adopt leaves computed elsewhere (reference layout: U m x r col-major,
     // V r x n col-major, dense m x n col-major), e.g. exported from htool
@@ -146,6 +164,10 @@ class HMatrix {
     int n_p1m_ = 0;
     long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    long long aca_budget_ = 0;
+    Mlp *predictor_       = nullptr;
+    double margin_        = 0.25;
+    std::vector<float> samples_x_, samples_y_;
     // streamed phase 2: chunk lists and CTA ranges for the FP64 factors and
     // for the reduced-precision ones; device status of the bounded waits
     DevBuf<StreamChunk> sc_d, scm_d;

@@ -94,4 +94,40 @@ inline int swizzle_bytes(int h, int n, int es) {
 void launch_colmax(const ColMaxJob *jobs, int njobs, const double *fac, unsigned *cmax, cudaStream_t st);
 void launch_convert(const ConvertJob *jobs, int njobs, const double *fac, const unsigned *cmax, unsigned char *mix, cudaStream_t st);
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
+// ---- ACA rank predictor (mlp.cu) -------------------------------------------
+constexpr int kMlpIn = 10, kMlpHidden = 64;
+constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
+
+// the kMlpIn features of an admissible block
+void block_features(int M, int N, double rad_t, double rad_s, const double *ctr_t, const double *ctr_s, double eps, int kernel_id, float *f);
+
+class Mlp {
+  public:
+    Mlp(unsigned long long seed, int device);
+    ~Mlp();
+    Mlp(const Mlp &)            = delete;
+    Mlp &operator=(const Mlp &) = delete;
+    void set_params(const float *p); // host, kMlpParams floats; resets the optimiser state
+    void get_params(float *p);
+    // Adam (beta 0.9 / 0.999) on the mean squared error, minibatches of
+    // `batch` shuffled samples; loss over all samples after every epoch
+    void train(const float *X, const float *Y, int n, int epochs, int batch, float lr, unsigned long long seed, float *loss_per_epoch);
+    // gradient of the mean squared error over the n samples (one batch); returns the loss
+    float gradient(const float *X, const float *Y, int n, float *grad);
+    void predict(const float *X, int n, float *y);                         // host arrays
+    void predict_device(const float *X, int n, float *y, cudaStream_t st); // device arrays
+    int device() const { return device_; }
+
+  private:
+    void ensure_batch(int n);
+    void step_launches(const float *X, const float *Y, int n, float lr, cudaStream_t st);
+    int device_;
+    cudaStream_t stream_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    DevBuf<float> params_, m_, v_, grad_, part_, loss_;
+    DevBuf<int> step_;
+    DevBuf<float> h1_, h2_, d1_, d2_, dout_, sq_;
+    int batch_cap_ = 0;
+};
+
 } // namespace htgpu

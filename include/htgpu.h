@@ -38,6 +38,7 @@ extern "C" {
 
 typedef struct htgpu_cluster_s *htgpu_cluster;
 typedef struct htgpu_hmatrix_s *htgpu_hmatrix;
+typedef struct htgpu_mlp_s *htgpu_mlp;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *htgpu_last_error(void);
@@ -223,6 +224,42 @@ int htgpu_hmatrix_precision_info(htgpu_hmatrix h, int *policy, long long *stored
  * in/out: device memory, column-major, user numbering; ordered on `stream`
  * (NULL = the handle's own stream). */
 int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out, int mu, void *stream);
+
+/* ---- ACA rank predictor (no counterpart in the reference) ------------------
+ * A 10 -> 64 -> 64 -> 1 perceptron (FP32, ReLU) that predicts from an
+ * admissible block's geometry how many ACA crosses the block needs; trained
+ * on the GPU on (features, crosses) pairs that partialACA itself produced.
+ * An H-matrix build can use it to size every block's first ACA attempt;
+ * partialACA's own stopping test still decides each rank, and a block whose
+ * scratch runs out is re-run with more, so the H-matrix is the same with or
+ * without the predictor. */
+int htgpu_mlp_num_params(void); /* W1[64][10], b1[64], W2[64][64], b2[64], W3[64], b3 */
+int htgpu_mlp_create(int device, unsigned long long seed, htgpu_mlp *out); /* Glorot-uniform weights from seed */
+int htgpu_mlp_destroy(htgpu_mlp m);
+int htgpu_mlp_set_params(htgpu_mlp m, const float *params); /* host; resets the optimiser */
+int htgpu_mlp_get_params(htgpu_mlp m, float *params);
+/* Adam (0.9, 0.999) on the mean squared error over minibatches of `batch`
+ * shuffled samples (features: n x 10 row-major, host); loss_per_epoch
+ * (optional, `epochs` floats): the loss over all samples after each epoch. */
+int htgpu_mlp_train(htgpu_mlp m, const float *features, const float *ranks, int n, int epochs, int batch, float lr, unsigned long long seed, float *loss_per_epoch);
+/* Gradient (htgpu_mlp_num_params floats) and value of the mean squared error
+ * over the n samples taken as one batch. */
+int htgpu_mlp_gradient(htgpu_mlp m, const float *features, const float *ranks, int n, float *grad, float *loss);
+int htgpu_mlp_predict(htgpu_mlp m, const float *features, int n, float *ranks);
+/* The 10 features of a block (sizes M x N, cluster radii and centres). */
+int htgpu_block_features(int M, int N, double rad_t, double rad_s, const double *ctr_t, const double *ctr_s, double epsilon, int kernel_id, float *features);
+/* Size the first ACA attempt of every block of later builds from the
+ * predictor: max(4, ceil(prediction * (1 + margin)) + 2) crosses, the
+ * largest profitable rank for predictions of 60 and above; NULL restores
+ * the fixed first attempt of 48.  The predictor must outlive those builds. */
+int htgpu_hmatrix_set_rank_predictor(htgpu_hmatrix h, htgpu_mlp m, double margin);
+/* Device bytes of ACA scratch one slice of blocks may use (0: 60% of the
+ * free memory at each round). */
+int htgpu_hmatrix_set_aca_budget(htgpu_hmatrix h, long long bytes);
+/* (features, crosses needed) of every block the last build's partialACA
+ * decided: its rank, or for a rejected block the largest profitable rank.
+ * With features == ranks == NULL only *count is set. */
+int htgpu_hmatrix_aca_samples(htgpu_hmatrix h, float *features, float *ranks, int capacity, int *count);
 
 #ifdef __cplusplus
 }
