@@ -269,6 +269,25 @@ def run_gpu(args):
     e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n, "precision": "mixed"}
     status = hm.device_status()
 
+    # learned rank predictor: trained on the (geometry, crosses) pairs this
+    # build's partialACA produced, then the same mesh re-assembled with it
+    X, yr = hm.aca_samples()
+    mlp = H.RankPredictor(device=local, seed=1)
+    t1 = time.perf_counter()
+    loss = mlp.train(X, np.minimum(yr, 64), epochs=30, batch=2048, lr=3e-3, seed=2)
+    train_s = time.perf_counter() - t1
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    hl = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).set_rank_predictor(mlp).build(H.LAPLACE, pts)
+    aca_learned = time.perf_counter() - t1
+    il = hl.get_infos()
+    same = bool(np.array_equal(hl.get_leaves()[0], hm.get_leaves()[0]) and np.array_equal(hl.get_leaves()[1], hm.get_leaves()[1]))
+    predictor = {"train_samples": int(yr.size), "train_seconds": train_s, "epochs": 30, "final_mse": float(loss[-1]),
+                 "aca_seconds": {"fixed_first_attempt": aca_seconds, "predicted_first_attempt": aca_learned},
+                 "scratch_bytes": {"fixed_first_attempt": int(info["GPU_aca_scratch_bytes"]), "predicted_first_attempt": int(il["GPU_aca_scratch_bytes"])},
+                 "rerun_rate": int(il["GPU_aca_overflow_reruns"]) / max(1, int(il["GPU_aca_predicted_blocks"])), "same_leaves": same}
+    del hl
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -288,7 +307,7 @@ def run_gpu(args):
                  "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64}, "phase1_mode": p1mode64},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk, "device_status": status,
         "rel_err_vs_dense_1000_rows": {"fp64": sampled_dense_error(pts, x, y64), "mixed": sampled_dense_error(pts, x, ym)},
-        "aca_seconds": aca_seconds,
+        "aca_seconds": aca_seconds, "rank_predictor": predictor,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},
     }
     if not args.no_cpu_baseline:

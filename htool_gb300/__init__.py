@@ -86,6 +86,12 @@ def _load():
         "htgpu_hmatrix_set_rank_predictor": (i, [vp, vp, d]),
         "htgpu_hmatrix_set_aca_budget": (i, [vp, C.c_longlong]),
         "htgpu_hmatrix_aca_samples": (i, [vp, vp, vp, i, vp]),
+        "htgpu_batch_create": (i, [i, vp]),
+        "htgpu_batch_destroy": (i, [vp]),
+        "htgpu_batch_add": (i, [vp, vp, vp, vp, i, vp]),
+        "htgpu_batch_capture": (i, [vp, i, vp]),
+        "htgpu_batch_launch": (i, [vp, vp]),
+        "htgpu_batch_sync": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -459,3 +465,42 @@ def block_features(M, N, rad_t, rad_s, ctr_t, ctr_s, epsilon, kernel_id):
     cs = np.ascontiguousarray(ctr_s, dtype=np.float64)
     _check(lib.htgpu_block_features(int(M), int(N), float(rad_t), float(rad_s), _ptr(ct), _ptr(cs), float(epsilon), int(kernel_id), _ptr(f)))
     return f
+
+
+class HBatch:
+    """Products of many H-matrices (device buffers) replayed by one CUDA
+    graph launch."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        _check(lib.htgpu_batch_create(int(device), C.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def add(self, hmatrix, x_ptr, y_ptr, mu=1, keep=None):
+        """y = H x on device pointers; `keep` (e.g. the tensors) is held alive."""
+        idx = C.c_int()
+        _check(lib.htgpu_batch_add(self.h, hmatrix.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), int(mu), C.byref(idx)))
+        self._keep.append((hmatrix, keep))
+        return idx.value
+
+    def capture(self, nstreams=8):
+        """Record all products; returns the number of graph nodes."""
+        n = C.c_longlong()
+        _check(lib.htgpu_batch_capture(self.h, int(nstreams), C.byref(n)))
+        return n.value
+
+    def launch(self, stream=None):
+        sarg = None if stream is None else C.c_void_p(1 if int(stream) == 0 else int(stream))
+        _check(lib.htgpu_batch_launch(self.h, sarg))
+
+    def sync(self):
+        _check(lib.htgpu_batch_sync(self.h))
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib.htgpu_batch_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

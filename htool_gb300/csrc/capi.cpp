@@ -2,6 +2,7 @@
 // Every call catches C++ exceptions and turns them into a status code plus
 // a thread-local message.
 #include "../../include/htgpu.h"
+#include "batch.hpp"
 #include "hmatrix.hpp"
 
 #include <cstring>
@@ -17,6 +18,10 @@ struct htgpu_hmatrix_s {
 
 struct htgpu_mlp_s {
     std::unique_ptr<htgpu::Mlp> m;
+};
+
+struct htgpu_batch_s {
+    std::unique_ptr<htgpu::Batch> b;
 };
 
 namespace {
@@ -479,6 +484,53 @@ int htgpu_hmatrix_aca_samples(htgpu_hmatrix h, float *features, float *ranks, in
             std::memcpy(features, x.data(), sizeof(float) * x.size());
             std::memcpy(ranks, y.data(), sizeof(float) * y.size());
         }
+    });
+}
+
+// ---- batches -------------------------------------------------------------------
+int htgpu_batch_create(int device, htgpu_batch *out) {
+    return guarded([&] {
+        need(out, "out");
+        auto *b = new htgpu_batch_s;
+        b->b.reset(new htgpu::Batch(device));
+        *out = b;
+    });
+}
+
+int htgpu_batch_destroy(htgpu_batch b) {
+    return guarded([&] { delete b; });
+}
+
+int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, int *index) {
+    return guarded([&] {
+        need(b, "batch");
+        need(h, "hmatrix");
+        const int i = b->b->add(h->h.get(), in, out, mu);
+        if (index)
+            *index = i;
+    });
+}
+
+int htgpu_batch_capture(htgpu_batch b, int nstreams, long long *graph_nodes) {
+    return guarded([&] {
+        need(b, "batch");
+        b->b->capture(nstreams);
+        if (graph_nodes)
+            *graph_nodes = b->b->graph_nodes();
+    });
+}
+
+int htgpu_batch_launch(htgpu_batch b, void *stream) {
+    return guarded([&] {
+        need(b, "batch");
+        b->b->launch((cudaStream_t)stream);
+    });
+}
+
+int htgpu_batch_sync(htgpu_batch b) {
+    return guarded([&] {
+        need(b, "batch");
+        b->b->sync();
     });
 }
 

@@ -71,6 +71,7 @@ class HMatrix {
     const BuildStats &stats() const { return st_; }
     cudaStream_t stream() const { return stream_; }
     int device() const { return device_; }
+    void sync() { HTGPU_CUDA(cudaStreamSynchronize(stream_)); } // the handle's own stream
     int last_launch_count() const { return launches_; }
 
     BlockTreeParams bp;

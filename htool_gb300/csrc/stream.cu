@@ -881,7 +881,9 @@ void launch_phase1_stream(const StreamChunk *chunks, const int *rbeg, int nrange
         if (dev < 64)
             done |= 1ull << dev;
     }
-    const int nctas = stream_ctas();
+    // as many warps as ranges, at most every resident CTA: small products
+    // leave room for concurrent work
+    const int nctas = std::max(1, std::min(stream_ctas(), (nranges + kWarps - 1) / kWarps));
     if (mu == 1)
         phase1_warp_kernel<1><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, tickets, arena, xp, xs, scale, xexp, mu, 0, A, status);
     else
@@ -915,7 +917,9 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
     if (nranges <= 0)
         return;
     HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
-    const int nctas = stream_ctas();
+    // as many warps as ranges, at most every resident CTA: small products
+    // leave room for concurrent work
+    const int nctas = std::max(1, std::min(stream_ctas(), (nranges + kWarps - 1) / kWarps));
     int c0 = 0, g = 0;
     while (c0 < mu) {
         const int left = mu - c0;

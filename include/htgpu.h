@@ -39,6 +39,7 @@ extern "C" {
 typedef struct htgpu_cluster_s *htgpu_cluster;
 typedef struct htgpu_hmatrix_s *htgpu_hmatrix;
 typedef struct htgpu_mlp_s *htgpu_mlp;
+typedef struct htgpu_batch_s *htgpu_batch;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *htgpu_last_error(void);
@@ -260,6 +261,21 @@ int htgpu_hmatrix_set_aca_budget(htgpu_hmatrix h, long long bytes);
  * decided: its rank, or for a rejected block the largest profitable rank.
  * With features == ranks == NULL only *count is set. */
 int htgpu_hmatrix_aca_samples(htgpu_hmatrix h, float *features, float *ranks, int capacity, int *count);
+
+/* ---- batched products (no counterpart in the reference) --------------------
+ * Many H-matrices, each with its own device input and output (column-major,
+ * user numbering, mu right-hand sides), applied by one CUDA-graph launch.
+ * htgpu_batch_capture runs every product once, then records them all, spread
+ * over up to nstreams concurrent streams (largest first); each launch
+ * replays the graph and reads / writes the buffers given at add time.  The
+ * H-matrices and buffers must outlive the batch; adding an entry drops the
+ * captured graph.  stream NULL: the batch's own stream. */
+int htgpu_batch_create(int device, htgpu_batch *out);
+int htgpu_batch_destroy(htgpu_batch b);
+int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, int *index);
+int htgpu_batch_capture(htgpu_batch b, int nstreams, long long *graph_nodes);
+int htgpu_batch_launch(htgpu_batch b, void *stream);
+int htgpu_batch_sync(htgpu_batch b);
 
 #ifdef __cplusplus
 }
