@@ -92,6 +92,7 @@ def _load():
         "htgpu_batch_capture": (i, [vp, i, vp]),
         "htgpu_batch_launch": (i, [vp, vp]),
         "htgpu_batch_sync": (i, [vp]),
+        "htgpu_partition_rows": (i, [i, vp, i, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -504,3 +505,12 @@ class HBatch:
                 self.h = None
         except Exception:
             pass
+
+
+def partition_rows(leaves, nr, nparts):
+    """Row cuts (nparts + 1, cluster numbering) for a product split over
+    nparts GPUs; leaves: array of (offset_i, m, stored bytes)."""
+    L = np.ascontiguousarray(np.asarray(leaves, dtype=np.int64).reshape(-1, 3))
+    cuts = np.empty(nparts + 1, np.int32)
+    _check(lib.htgpu_partition_rows(int(L.shape[0]), _ptr(L) if L.size else None, int(nr), int(nparts), _ptr(cuts)))
+    return cuts

@@ -534,4 +534,14 @@ int htgpu_batch_sync(htgpu_batch b) {
     });
 }
 
+int htgpu_partition_rows(int nleaves, const long long *leaves, int nr, int nparts, int *cuts) {
+    return guarded([&] {
+        need(cuts, "cuts");
+        if (nleaves > 0)
+            need(leaves, "leaves");
+        const std::vector<int> c = htgpu::partition_rows(nleaves, leaves, nr, nparts);
+        std::memcpy(cuts, c.data(), sizeof(int) * c.size());
+    });
+}
+
 } // extern "C"

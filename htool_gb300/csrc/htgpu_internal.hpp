@@ -181,4 +181,8 @@ struct DevBuf {
     void upload(const std::vector<T> &v, cudaStream_t st) { upload(v.data(), v.size(), st); }
 };
 
+// row cuts (nparts + 1, cluster numbering) balancing the stored bytes of the
+// leaves (oi, m, bytes per leaf), never inside a leaf's rows
+std::vector<int> partition_rows(int nleaves, const long long *leaves, int nr, int nparts);
+
 } // namespace htgpu

@@ -277,6 +277,14 @@ int htgpu_batch_capture(htgpu_batch b, int nstreams, long long *graph_nodes);
 int htgpu_batch_launch(htgpu_batch b, void *stream);
 int htgpu_batch_sync(htgpu_batch b);
 
+/* Row partition for a product over several GPUs (the distribution of
+ * include/htool/types/hmatrix.hpp:964-977, 1103: every part owns a range of
+ * target rows in cluster numbering and computes them completely; x is
+ * all-gathered before and y after).  leaves: (offset_i, m, stored bytes) per
+ * leaf; cuts: nparts + 1 row offsets, never inside a leaf's rows, balancing
+ * the bytes.  Host only. */
+int htgpu_partition_rows(int nleaves, const long long *leaves, int nr, int nparts, int *cuts);
+
 #ifdef __cplusplus
 }
 #endif
