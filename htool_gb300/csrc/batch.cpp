@@ -30,7 +30,7 @@ int Batch::add(HMatrix *h, const double *x, double *y, int mu) {
     require(h != nullptr && x != nullptr && y != nullptr, "batch entries need an H-matrix and device input and output");
     require(mu >= 1, "number of right-hand sides must be positive");
     require(h->device() == device_, "H-matrix on another device than the batch");
-    entries_.push_back({h, x, y, mu});
+    entries_.push_back({h, x, y, mu, 0});
     release(); // a new entry invalidates the captured graph
     return (int)entries_.size() - 1;
 }
@@ -73,6 +73,8 @@ void Batch::capture(int nstreams) {
         HTGPU_CUDA(cudaStreamWaitEvent(origin, events_[k], 0));
     }
     HTGPU_CUDA(cudaStreamEndCapture(origin, &graph));
+    for (auto &e : entries_)
+        e.gen = e.h->layout_generation();
     std::size_t nodes = 0;
     HTGPU_CUDA(cudaGraphGetNodes(graph, nullptr, &nodes));
     nodes_ = (long long)nodes;
@@ -82,6 +84,8 @@ void Batch::capture(int nstreams) {
 
 void Batch::launch(cudaStream_t st) {
     require(exec_ != nullptr, "batch not captured");
+    for (const auto &e : entries_)
+        require(e.h->layout_generation() == e.gen, "an H-matrix of the batch changed since the capture: capture again");
     HTGPU_CUDA(cudaSetDevice(device_));
     HTGPU_CUDA(cudaGraphLaunch(exec_, st ? st : streams_[0]));
 }

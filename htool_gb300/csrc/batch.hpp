@@ -30,6 +30,7 @@ class Batch {
         const double *x;
         double *y;
         int mu;
+        unsigned long long gen; // layout generation at capture
     };
     int device_;
     std::vector<Entry> entries_;

@@ -430,6 +430,7 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
 //  The arena holds all phase-1 tiles (item order), then all phase-2 blocks
 //  (item order), each block 16-byte aligned.
 void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs) {
+    layout_gen_++; // buffers or launch lists change: captured products are stale
     auto even = [](long long v) { return (v + 1) & ~1LL; };
     long long off = 0;
     std::vector<std::vector<BlockCopy>> copies(bufs.size());
@@ -634,6 +635,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
 void HMatrix::ensure_work(int mu) {
     if (mu <= mu_cap)
         return;
+    layout_gen_++; // work buffers move: captured products are stale
     xp.alloc((std::size_t)nc * mu + 1);
     xs.alloc((std::size_t)nc * mu + 1);
     xexp.alloc(1);
@@ -687,6 +689,7 @@ void HMatrix::assign_phase1_modes() {
 }
 
 void HMatrix::upload_phase1_lists() {
+    layout_gen_++; // buffers or launch lists change: captured products are stale
     std::vector<P1Item> a, b;
     for (auto &it : p1_h)
         ((it.chunk & kEmuBit) ? b : a).push_back(it);
@@ -782,6 +785,7 @@ void HMatrix::launch_product(const double *x, double *y, int mu, bool cluster_nu
 // maxima from the FP64 blocks, per-column precision on the host, then one
 // conversion pass into a byte arena laid out like the FP64 one.
 void HMatrix::set_precision(int policy, double tau) {
+    layout_gen_++; // buffers or launch lists change: captured products are stale
     require(policy >= 0 && policy <= 3, "precision policy must be 0 (FP64), 1 (FP32), 2 (FP32/BF16) or 3 (BF16)");
     require(tau > 0, "tau must be positive");
     HTGPU_CUDA(cudaSetDevice(device_));
@@ -1047,6 +1051,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
 }
 
 void HMatrix::set_phase1_mode(int mode) {
+    layout_gen_++; // buffers or launch lists change: captured products are stale
     require(mode == 0 || mode == 1, "phase-1 mode must be 0 (tile kernels) or 1 (streamed chunks)");
     p1_mode_ = mode;
 }

@@ -72,6 +72,9 @@ class HMatrix {
     cudaStream_t stream() const { return stream_; }
     int device() const { return device_; }
     void sync() { HTGPU_CUDA(cudaStreamSynchronize(stream_)); } // the handle's own stream
+    // changes whenever device buffers or launch lists are rebuilt: a graph
+    // that captured products of this H-matrix is valid only while it is equal
+    unsigned long long layout_generation() const { return layout_gen_; }
     int last_launch_count() const { return launches_; }
 
     BlockTreeParams bp;
@@ -165,6 +168,7 @@ class HMatrix {
     int n_p1m_ = 0;
     long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    unsigned long long layout_gen_ = 0;
     long long aca_budget_ = 0;
     Mlp *predictor_       = nullptr;
     double margin_        = 0.25;

@@ -232,6 +232,11 @@ void Mlp::get_params(float *p) {
 void Mlp::ensure_batch(int n) {
     if (n <= batch_cap_)
         return;
+    // a captured epoch refers to the old buffers: it must not be replayed
+    if (graph_exec_) {
+        cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+    }
     h1_.alloc((size_t)n * kH);
     h2_.alloc((size_t)n * kH);
     d1_.alloc((size_t)n * kH);
@@ -277,7 +282,9 @@ void Mlp::train(const float *X, const float *Y, int n, int epochs, int batch, fl
     DevBuf<float> dx, dy;
     dx.alloc((size_t)n * kIn);
     dy.alloc((size_t)n);
-    ensure_batch(batch);
+    // every buffer the epoch graph or the loss pass touches is sized here,
+    // before the capture: nothing is reallocated while the graph exists
+    ensure_batch(std::max(n, batch));
     // an epoch = nbatch steps over consecutive slices of the (reshuffled)
     // device copy of the samples: captured once, replayed every epoch
     if (graph_exec_) {
@@ -312,7 +319,6 @@ void Mlp::train(const float *X, const float *Y, int n, int epochs, int batch, fl
         HTGPU_CUDA(cudaGraphLaunch(graph_exec_, stream_));
         if (loss_per_epoch) {
             // loss over all samples with the parameters after this epoch
-            ensure_batch(n);
             mlp_sample_kernel<<<(n + 127) / 128, 128, 0, stream_>>>(params_.p, all_x.p, all_y.p, n, h1_.p, h2_.p, d1_.p, d2_.p, dout_.p, sq_.p);
             mlp_loss_kernel<<<1, 256, 0, stream_>>>(sq_.p, n, loss_.p);
             HTGPU_CUDA(cudaGetLastError());
@@ -320,6 +326,9 @@ void Mlp::train(const float *X, const float *Y, int n, int epochs, int batch, fl
         }
         HTGPU_CUDA(cudaStreamSynchronize(stream_)); // xs / ys are refilled next epoch
     }
+    // the graph reads dx / dy, which end with this call
+    cudaGraphExecDestroy(graph_exec_);
+    graph_exec_ = nullptr;
 }
 
 void Mlp::predict_device(const float *X, int n, float *y, cudaStream_t st) {

@@ -50,6 +50,15 @@ def test_batch_matches_individual_products():
             ref = hm.mvprod_global_to_global(bufs[k][0].cpu().numpy(), mu)
             assert np.array_equal(bufs[k][1].cpu().numpy(), ref), k
         assert all(hm.device_status() == 0 for hm, _, _ in items)
+    # a re-laid-out H-matrix invalidates the captured graph
+    items[2][0].set_fp64_split(1000, 1000)
+    with pytest.raises(ValueError):
+        batch.launch()
+    batch.capture(nstreams=2)
+    batch.launch()
+    batch.sync()
+    k = 2
+    assert np.array_equal(bufs[k][1].cpu().numpy(), items[k][0].mvprod_global_to_global(bufs[k][0].cpu().numpy(), items[k][2]))
 
 
 def test_batch_errors():
