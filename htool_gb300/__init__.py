@@ -93,6 +93,7 @@ def _load():
         "htgpu_batch_launch": (i, [vp, vp]),
         "htgpu_batch_sync": (i, [vp]),
         "htgpu_partition_rows": (i, [i, vp, i, i, vp]),
+        "htgpu_hmatrix_mvprod_transp": (i, [vp, vp, vp, i, u, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -354,6 +355,16 @@ class HMatrix:
             raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nc * mu))
         y = np.empty(nr * mu, np.float64)
         _check(lib.htgpu_hmatrix_mvprod(self.h, _ptr(x), _ptr(y), mu, HOST_PTRS, None))
+        return y
+
+    def mvprod_transp_global_to_global(self, x, mu=1):
+        """y = H^T x on host arrays (column-major, mu right-hand sides)."""
+        nr, nc, _, _ = self.sizes()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.size != nr * mu:
+            raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nr * mu))
+        y = np.empty(nc * mu, np.float64)
+        _check(lib.htgpu_hmatrix_mvprod_transp(self.h, _ptr(x), _ptr(y), mu, HOST_PTRS, None))
         return y
 
     def mvprod_ptr(self, x_ptr, y_ptr, mu=1, flags=0, stream=None):

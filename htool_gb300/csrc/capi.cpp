@@ -544,4 +544,14 @@ int htgpu_partition_rows(int nleaves, const long long *leaves, int nr, int npart
     });
 }
 
+int htgpu_hmatrix_mvprod_transp(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned flags, void *stream) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(in, "in");
+        need(out, "out");
+        htgpu::require((flags & ~HTGPU_HOST_PTRS) == 0, "transposed products take HTGPU_HOST_PTRS only");
+        h->h->mvprod_transp(in, out, mu, (flags & HTGPU_HOST_PTRS) != 0, (cudaStream_t)stream);
+    });
+}
+
 } // extern "C"

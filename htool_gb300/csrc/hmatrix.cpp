@@ -431,6 +431,7 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
 //  (item order), each block 16-byte aligned.
 void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs) {
     layout_gen_++; // buffers or launch lists change: captured products are stale
+    transp_.reset();
     auto even = [](long long v) { return (v + 1) & ~1LL; };
     long long off = 0;
     std::vector<std::vector<BlockCopy>> copies(bufs.size());
@@ -1156,6 +1157,55 @@ void HMatrix::phase_bytes(int mu, long long *b) const {
     b[1]           = (red ? p1_bytes_m_ : p1_bytes_) + 8LL * a_slots * mu;                  // V-side factors, partial sums
     b[2]           = (red ? p2_bytes_m_ : p2_bytes_) + 4LL * (red ? n_cols_m_ : n_cols_) + 8LL * zlen_ * mu; // U-side + dense, column indices, z
     b[3]           = 8LL * zsum_reads_ * mu + 8LL * nr * mu + 4LL * nr;                    // z, y, perm
+}
+
+void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st) {
+    require(mu >= 1, "number of right-hand sides must be positive");
+    HTGPU_CUDA(cudaSetDevice(device_));
+    if (!transp_) {
+        // leaves of H^T from the stored ones (one pass through host memory)
+        std::vector<int> lr(5 * lr_h.size()), dn(4 * dn_h.size());
+        leaf_descriptors(lr.data(), dn.data());
+        long long nuv = 0, ndd = 0;
+        for (auto &L : lr_h)
+            nuv += (long long)L.r * (L.m + L.n);
+        for (auto &D : dn_h)
+            ndd += (long long)D.m * D.n;
+        std::vector<double> uv(std::max<long long>(nuv, 1)), dd(std::max<long long>(ndd, 1)), uvt(uv.size()), ddt(dd.size());
+        export_factors(uv.data(), dd.data());
+        long long o = 0;
+        for (std::size_t b = 0; b < lr_h.size(); b++) {
+            const LrLeaf &L = lr_h[b];
+            const double *U = uv.data() + o, *V = U + (long long)L.m * L.r;
+            double *Ut = uvt.data() + o, *Vt = Ut + (long long)L.n * L.r;
+            for (int k = 0; k < L.r; k++)
+                for (int j = 0; j < L.n; j++)
+                    Ut[j + (long long)L.n * k] = V[k + (long long)L.r * j]; // U' = V^T (n x r)
+            for (int i = 0; i < L.m; i++)
+                for (int k = 0; k < L.r; k++)
+                    Vt[k + (long long)L.r * i] = U[i + (long long)L.m * k]; // V' = U^T (r x m)
+            std::swap(lr[5 * b], lr[5 * b + 1]);
+            std::swap(lr[5 * b + 2], lr[5 * b + 3]);
+            o += (long long)L.r * (L.m + L.n);
+        }
+        o = 0;
+        for (std::size_t b = 0; b < dn_h.size(); b++) {
+            const DenseLeaf &D = dn_h[b];
+            for (int j = 0; j < D.n; j++)
+                for (int i = 0; i < D.m; i++)
+                    ddt[o + j + (long long)D.n * i] = dd[o + i + (long long)D.m * j];
+            std::swap(dn[4 * b], dn[4 * b + 1]);
+            std::swap(dn[4 * b + 2], dn[4 * b + 3]);
+            o += (long long)D.m * D.n;
+        }
+        auto t = std::unique_ptr<HMatrix>(new HMatrix(S, T, eps_, eta_, device_));
+        t->set_leaves((int)lr_h.size(), lr.data(), uvt.data(), (int)dn_h.size(), dn.data(), ddt.data());
+        t->set_fp64_split(p1_permille_, p2_n64_);
+        transp_ = std::move(t);
+    }
+    if (transp_->precision() != precision_ || (precision_ != 0 && transp_->tau_ != tau_))
+        transp_->set_precision(precision_, tau_);
+    transp_->mvprod(in, out, mu, host_ptrs, false, st);
 }
 
 void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {

@@ -94,6 +94,11 @@ class HMatrix {
     // FP64: phase-1 mode and the DFMA/emulation split; reduced precision:
     // phase-1 mode
     void autotune(int mu, int reps, float *best_ms);
+    // y = H^T x (mvprod_transp_global_to_global, hmatrix.hpp:1277-1455): the
+    // first call builds a transposed twin (leaves U' = V^T, V' = U^T,
+    // D' = D^T over swapped cluster trees) that later calls reuse
+    void mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st);
+
     // nonzero when a bounded device wait of a product ran out (1 producer,
     // 2 consumer, 3 drain); reading it synchronises the H-matrix's stream
     int device_status();
@@ -169,6 +174,7 @@ class HMatrix {
     long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
     unsigned long long layout_gen_ = 0;
+    std::unique_ptr<HMatrix> transp_; // transposed twin, built on first use
     long long aca_budget_ = 0;
     Mlp *predictor_       = nullptr;
     double margin_        = 0.25;

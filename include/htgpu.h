@@ -285,6 +285,14 @@ int htgpu_batch_sync(htgpu_batch b);
  * the bytes.  Host only. */
 int htgpu_partition_rows(int nleaves, const long long *leaves, int nr, int nparts, int *cuts);
 
+/* y = H^T x (HMatrix::mvprod_transp_global_to_global,
+ * include/htool/types/hmatrix.hpp:1277-1455), user numbering, mu
+ * right-hand sides (in: nr * mu, out: nc * mu).  The first call builds a
+ * transposed copy of the leaves inside the handle (one pass through host
+ * memory, as much device memory again); later calls reuse it and follow the
+ * handle's storage policy.  flags: HTGPU_HOST_PTRS or 0. */
+int htgpu_hmatrix_mvprod_transp(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned flags, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,10 @@ def hmatrix_case(R, name, xt, xs, kernel, eps, eta, mus=(1, 3)):
         x = G.rhs(xs.shape[0], mu, seed=2)
         data["x_mu%d" % mu] = x
         data["y_mu%d" % mu] = H.mvprod(x, mu)
+        # transposed product (mvprod_transp_global_to_global)
+        xT = G.rhs(xt.shape[0], mu, seed=5)
+        data["xT_mu%d" % mu] = xT
+        data["yT_mu%d" % mu] = R.mvprod_transp(H, xT, mu)
     infos = R.infos(H)
     meta = dict(kernel=kernel, eps=eps, eta=eta, minclustersize=10, nb_sons=2, sha_uv=sha(uv), sha_dense=sha(dd), infos=infos, depths_t=ct.depths(), depths_s=cs.depths())
     np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)

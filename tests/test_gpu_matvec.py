@@ -48,6 +48,29 @@ def test_uploaded_leaves_product(port, golden, name):
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_transposed_product_matches_reference(golden, name):
+    """H^T x against upstream htool's mvprod_transp_global_to_global on the
+    same H-matrix (FP64 within 1e-12; reduced precision within 1e-6; a
+    re-laid-out H-matrix drops and rebuilds its transposed copy)."""
+    g, meta = golden(name)
+    t = H.Cluster().build(g["xt"].shape[0], g["xt"])
+    s = H.Cluster().build(g["xs"].shape[0], g["xs"])
+    GH = H.HMatrix(t, s, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"], g["xs"])
+    for mu in (1, 3):
+        assert rel(GH.mvprod_transp_global_to_global(g["xT_mu%d" % mu], mu), g["yT_mu%d" % mu]) < FP64_TOL
+    # reduced precision: as accurate as the forward product of the same
+    # H-matrix (a product whose terms cancel heavily, like the single smooth
+    # leaf of the disk pairs, loses digits in both directions alike)
+    GH.set_precision("mixed")
+    e_fwd = rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"])
+    e_tr = rel(GH.mvprod_transp_global_to_global(g["xT_mu1"]), g["yT_mu1"])
+    assert e_tr <= max(1e-6, 4 * e_fwd)
+    GH.set_precision("fp64")
+    GH.build(meta["kernel"], g["xt"], g["xs"])
+    assert rel(GH.mvprod_transp_global_to_global(g["xT_mu3"], 3), g["yT_mu3"]) < FP64_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
 def test_device_build_matches_reference(port, golden, name):
     g, meta = golden(name)
     t = H.Cluster().build(g["xt"].shape[0], g["xt"])
