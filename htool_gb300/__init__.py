@@ -94,6 +94,10 @@ def _load():
         "htgpu_batch_sync": (i, [vp]),
         "htgpu_partition_rows": (i, [i, vp, i, i, vp]),
         "htgpu_hmatrix_mvprod_transp": (i, [vp, vp, vp, i, u, vp]),
+        "htgpu_cluster_save": (i, [vp, C.c_char_p]),
+        "htgpu_cluster_read": (i, [C.c_char_p, C.c_char_p, vp]),
+        "htgpu_hmatrix_save": (i, [vp, C.c_char_p]),
+        "htgpu_hmatrix_load": (i, [vp, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -175,6 +179,18 @@ class Cluster:
         nd = np.empty((nn, 4), np.float64)
         _check(lib.htgpu_cluster_get_nodes(self.h, _ptr(ni), _ptr(nd)))
         return ni, nd
+
+    def save_cluster(self, filename):
+        """htool's <filename>_permutation.csv and <filename>_tree.csv."""
+        _check(lib.htgpu_cluster_save(self.h, str(filename).encode()))
+
+    def read_cluster(self, file_permutation, file_tree):
+        """Replace this tree by the one in htool's CSV pair."""
+        h = C.c_void_p()
+        _check(lib.htgpu_cluster_read(str(file_permutation).encode(), str(file_tree).encode(), C.byref(h)))
+        self._free()
+        self.h = h
+        return self
 
     def _free(self):
         if self.h:
@@ -380,6 +396,15 @@ class HMatrix:
 
     def __matmul__(self, x):
         return self.mvprod_global_to_global(x, 1)
+
+    def save(self, path):
+        """Binary dump of the leaves and factors (reloadable with load)."""
+        _check(lib.htgpu_hmatrix_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        """Leaves and factors from a dump made on the same cluster trees."""
+        _check(lib.htgpu_hmatrix_load(self.h, str(path).encode()))
+        return self
 
     def set_rank_predictor(self, predictor, margin=0.25):
         """Size the first ACA attempt of later builds with a RankPredictor

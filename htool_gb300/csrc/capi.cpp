@@ -554,4 +554,44 @@ int htgpu_hmatrix_mvprod_transp(htgpu_hmatrix h, const double *in, double *out, 
     });
 }
 
+int htgpu_cluster_save(htgpu_cluster c, const char *name) {
+    return guarded([&] {
+        need(c, "cluster");
+        need(name, "name");
+        htgpu::save_cluster(*c->tree, name);
+    });
+}
+
+int htgpu_cluster_read(const char *perm_file, const char *tree_file, htgpu_cluster *out) {
+    return guarded([&] {
+        need(perm_file, "perm_file");
+        need(tree_file, "tree_file");
+        need(out, "out");
+        auto *c = new htgpu_cluster_s;
+        try {
+            c->tree = std::make_shared<htgpu::ClusterTree>(htgpu::read_cluster(perm_file, tree_file));
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *out = c;
+    });
+}
+
+int htgpu_hmatrix_save(htgpu_hmatrix h, const char *path) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(path, "path");
+        h->h->save(path);
+    });
+}
+
+int htgpu_hmatrix_load(htgpu_hmatrix h, const char *path) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(path, "path");
+        h->h->load(path);
+    });
+}
+
 } // extern "C"

@@ -99,6 +99,11 @@ class HMatrix {
     // D' = D^T over swapped cluster trees) that later calls reuse
     void mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st);
 
+    // binary dump of the leaves and factors (htool layout) and its reload
+    // onto the same cluster trees
+    void save(const std::string &path);
+    void load(const std::string &path);
+
     // nonzero when a bounded device wait of a product ran out (1 producer,
     // 2 consumer, 3 drain); reading it synchronises the H-matrix's stream
     int device_status();

@@ -185,4 +185,8 @@ struct DevBuf {
 // leaves (oi, m, bytes per leaf), never inside a leaf's rows
 std::vector<int> partition_rows(int nleaves, const long long *leaves, int nr, int nparts);
 
+// htool's CSV pair for cluster trees (cluster.hpp:433-583)
+void save_cluster(const ClusterTree &T, const std::string &name);
+ClusterTree read_cluster(const std::string &perm_file, const std::string &tree_file);
+
 } // namespace htgpu

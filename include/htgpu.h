@@ -293,6 +293,20 @@ int htgpu_partition_rows(int nleaves, const long long *leaves, int nr, int npart
  * handle's storage policy.  flags: HTGPU_HOST_PTRS or 0. */
 int htgpu_hmatrix_mvprod_transp(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned flags, void *stream);
 
+/* Cluster trees in htool's CSV pair (VirtualCluster::save_cluster /
+ * read_cluster, include/htool/clustering/cluster.hpp:433-583):
+ * <name>_permutation.csv and <name>_tree.csv, radii and centres with 6
+ * significant digits as htool writes them.  Host only. */
+int htgpu_cluster_save(htgpu_cluster c, const char *name);
+int htgpu_cluster_read(const char *perm_file, const char *tree_file, htgpu_cluster *out);
+
+/* Binary dump of an assembled H-matrix (leaf lists and factors in htool's
+ * layout, sizes and permutation hashes in the header; no counterpart in the
+ * reference) and its reload into a handle on the same cluster trees, e.g.
+ * to reuse a large build. */
+int htgpu_hmatrix_save(htgpu_hmatrix h, const char *path);
+int htgpu_hmatrix_load(htgpu_hmatrix h, const char *path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -143,6 +143,15 @@ void ref_cluster_export(void *p, int *perm, int *node_i, double *node_d) {
     });
 }
 
+// VirtualCluster::save_cluster / read_cluster (cluster.hpp:433-583)
+void ref_cluster_save(void *p, const char *name) { ((RefCluster *)p)->c->save_cluster(name); }
+void *ref_cluster_read(const char *perm_file, const char *tree_file) {
+    auto *rc = new RefCluster;
+    rc->c    = std::make_shared<ClusterT>(3);
+    rc->c->read_cluster(perm_file, tree_file);
+    return rc;
+}
+
 int ref_cluster_depths(void *p, int *mn, int *mx) {
     auto &c = *((RefCluster *)p)->c;
     *mn     = c.get_min_depth();

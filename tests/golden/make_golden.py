@@ -107,6 +107,9 @@ def main():
         s = G.disk_glibc(1000, 1.0 + dz)
         hmatrix_case(R, "disks2000x1000_%s_k1" % tag, t, s, 1, 1e-3, 10.0)
     aca_case(R)
+    # htool's own CSV pair for the configuration-1 cluster tree (save_cluster)
+    ct = R.cluster(cyl)
+    R._L.ref_cluster_save(ct.h, os.path.join(OUT, "cyl4000_cluster").encode())
 
 
 if __name__ == "__main__":
