@@ -23,7 +23,8 @@ LIB_PATH = os.path.join(_HERE, "libhtgpu.so")
 
 INV_R_EPS = 0  # 1 / (1e-5 + r)
 LAPLACE = 1  # 1 / (4 pi r), 0 on the diagonal
-KERNELS = {"inv_r_eps": INV_R_EPS, "laplace": LAPLACE}
+HELMHOLTZ = 2  # exp(i k r) / (4 pi r), 0 on the diagonal (complex H-matrices)
+KERNELS = {"inv_r_eps": INV_R_EPS, "laplace": LAPLACE, "helmholtz": HELMHOLTZ}
 
 HOST_PTRS = 1
 CLUSTER_NUMBERING = 2
@@ -51,6 +52,7 @@ def _load():
         "htgpu_block_tasks": (i, [vp, vp, d, vp, vp]),
         "htgpu_hmatrix_create": (i, [vp, vp, d, d, i, vp]),
         "htgpu_hmatrix_destroy": (i, [vp]),
+        "htgpu_hmatrix_create_complex": (i, [vp, vp, d, d, i, vp]),
         "htgpu_hmatrix_set_maxblocksize": (i, [vp, u]),
         "htgpu_hmatrix_set_mintargetdepth": (i, [vp, u]),
         "htgpu_hmatrix_set_minsourcedepth": (i, [vp, u]),
@@ -218,12 +220,14 @@ class HMatrix:
     """HMatrix<double> (hmatrix.hpp:44-270) with partialACA compression,
     stored and applied on the GPU."""
 
-    def __init__(self, cluster_tree_t, cluster_tree_s, epsilon=1e-6, eta=10.0, symmetry="N", UPLO="N", device=0):
+    def __init__(self, cluster_tree_t, cluster_tree_s, epsilon=1e-6, eta=10.0, symmetry="N", UPLO="N", device=0, dtype=np.float64):
         if symmetry != "N" or UPLO != "N":
             raise NotImplementedError("[Htool error] only non-symmetric storage ('N', 'N') is supported")
         self.t, self.s = cluster_tree_t, cluster_tree_s
+        self.complex = np.dtype(dtype) == np.complex128
         h = C.c_void_p()
-        _check(lib.htgpu_hmatrix_create(cluster_tree_t.h, cluster_tree_s.h, float(epsilon), float(eta), int(device), C.byref(h)))
+        create = lib.htgpu_hmatrix_create_complex if self.complex else lib.htgpu_hmatrix_create
+        _check(create(cluster_tree_t.h, cluster_tree_s.h, float(epsilon), float(eta), int(device), C.byref(h)))
         self.h = h
         self.epsilon, self.eta = epsilon, eta
 
@@ -364,17 +368,26 @@ class HMatrix:
         return ms.value
 
     def mvprod_global_to_global(self, x, mu=1):
-        """Host arrays in and out (column-major, mu right-hand sides)."""
+        """Host arrays in and out (column-major, mu right-hand sides;
+        complex128 for a complex H-matrix)."""
         nr, nc, _, _ = self.sizes()
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        if x.size != nc * mu:
-            raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nc * mu))
-        y = np.empty(nr * mu, np.float64)
+        if self.complex:
+            x = np.ascontiguousarray(x, dtype=np.complex128)
+            if 2 * x.size != nc * mu:
+                raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nc * mu // 2))
+            y = np.empty(nr * mu // 2, np.complex128)
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            if x.size != nc * mu:
+                raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nc * mu))
+            y = np.empty(nr * mu, np.float64)
         _check(lib.htgpu_hmatrix_mvprod(self.h, _ptr(x), _ptr(y), mu, HOST_PTRS, None))
         return y
 
     def mvprod_transp_global_to_global(self, x, mu=1):
         """y = H^T x on host arrays (column-major, mu right-hand sides)."""
+        if self.complex:
+            raise NotImplementedError("[Htool error] transposed products of complex H-matrices are not supported")
         nr, nc, _, _ = self.sizes()
         x = np.ascontiguousarray(x, dtype=np.float64)
         if x.size != nr * mu:

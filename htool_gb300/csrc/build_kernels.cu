@@ -323,6 +323,232 @@ __global__ void dense_fill_kernel(const DenseChunk *__restrict__ chunks, const d
     }
 }
 
+// ---------------------------------------------------------------------------
+// complex kernels (Helmholtz, id 2): partialACA in complex arithmetic, and
+// the packing of the complex crosses / dense blocks into the real form used
+// by the product: entry z of a complex matrix becomes the 2x2 block
+// [[re, -im], [im, re]] at rows (2i, 2i+1), columns (2j, 2j+1)
+// ---------------------------------------------------------------------------
+struct zd {
+    double re, im;
+};
+__device__ __forceinline__ zd zmul(zd a, zd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ zd zsub(zd a, zd b) { return {a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ zd zadd(zd a, zd b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ zd zconj(zd a) { return {a.re, -a.im}; }
+__device__ __forceinline__ double zabs(zd a) { return hypot(a.re, a.im); }
+__device__ __forceinline__ zd zrecip(zd a) { // 1 / a
+    const double d = a.re * a.re + a.im * a.im;
+    return {a.re / d, -a.im / d};
+}
+
+// exp(i k r) / (4 pi r), 0 at r == 0
+__device__ __forceinline__ zd kernel_entry_z(const KernelDesc &kd, const double *a, const double *b) {
+    const double r = dist3(a, b);
+    if (r == 0.)
+        return {0., 0.};
+    double sn, cs;
+    sincos(kd.param * r, &sn, &cs);
+    const double f = 1. / (kFourPi * r);
+    return {cs * f, sn * f};
+}
+
+// One CTA per block; scratch columns U_s[:, k] (M complex) and Vt_s[:, k]
+// (N complex), as the real kernel; the Frobenius estimator with htool's
+// conjugated dot products: |c.c| |r.r| + 2 Re sum_p (vv_p . r)(uu_p . c)
+__global__ void __launch_bounds__(kAcaThreads) partial_aca_z_kernel(const AcaBlock *__restrict__ blocks, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t,
+                                                                     const int *__restrict__ perm_s, KernelDesc kd, double eps, double *__restrict__ scratch, unsigned char *__restrict__ flags,
+                                                                     int *__restrict__ rank_out) {
+    constexpr int NT = kAcaThreads;
+    __shared__ double sv[NT / 32];
+    __shared__ int si[NT / 32];
+    __shared__ double sre[NT / 32], sim[NT / 32];
+    __shared__ double sacc[4]; // |c.c||r.r|, Re sum, pending (vv_p . r) re / im
+
+    const AcaBlock B = blocks[blockIdx.x];
+    const int M = B.M, N = B.N, tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int *rows = perm_t + B.row_off;
+    const int *cols = perm_s + B.col_off;
+    zd *U               = reinterpret_cast<zd *>(scratch + B.u_off);
+    zd *Vt              = reinterpret_cast<zd *>(scratch + B.v_off);
+    unsigned char *vrow = flags + B.flag_off;
+    unsigned char *vcol = vrow + M;
+    for (int i = tid; i < M + N; i += NT)
+        vrow[i] = 0;
+
+    double best = 1e300;
+    int I       = 0x7fffffff;
+    for (int i = tid; i < M; i += NT) {
+        const double *p = xt + 3 * (size_t)rows[i];
+        double s        = 0.;
+        for (int d = 0; d < 3; d++)
+            s = s + (p[d] - B.ctr[d]) * (p[d] - B.ctr[d]);
+        double ad = sqrt(s);
+        if (ad < best) {
+            best = ad;
+            I    = i;
+        }
+    }
+    BlockReduce<NT>::argmin(best, I, sv, si);
+    if (!(best < 1e30))
+        I = 0;
+
+    // a complex dot product over the CTA, summed per thread, warp and CTA
+    auto cdot = [&](int len, auto term) {
+        double re = 0., im = 0.;
+        for (int i = tid; i < len; i += NT) {
+            const zd t = term(i);
+            re         = re + t.re;
+            im         = im + t.im;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            re = re + __shfl_down_sync(0xffffffffu, re, o);
+            im = im + __shfl_down_sync(0xffffffffu, im, o);
+        }
+        if (lane == 0) {
+            sre[warp] = re;
+            sim[warp] = im;
+        }
+        __syncthreads();
+        zd r = {0., 0.};
+        for (int w = 0; w < NT / 32; w++) {
+            r.re = r.re + sre[w];
+            r.im = r.im + sim[w];
+        }
+        __syncthreads();
+        return r;
+    };
+
+    const int MN32 = (int)((unsigned)M * (unsigned)N);
+    int q          = 0;
+    double frob = 0., aux = 0.;
+    while (true) {
+        if (!(q == 0 || sqrt(aux / frob) > eps))
+            break;
+        q += 1;
+        if ((int)((unsigned)q * (unsigned)(M + N)) > MN32) {
+            q = -1;
+            break;
+        }
+        if (q > B.cap) {
+            q = -2;
+            break;
+        }
+        const int k = q - 1;
+        const double *pI = xt + 3 * (size_t)rows[I];
+        double piv       = -1.;
+        int J            = -1;
+        for (int j = tid; j < N; j += NT) {
+            zd v = kernel_entry_z(kd, pI, xs + 3 * (size_t)cols[j]);
+            for (int p = 0; p < k; p++)
+                v = zsub(v, zmul(U[I + (size_t)M * p], Vt[j + (size_t)N * p]));
+            Vt[j + (size_t)N * k] = v;
+            if (!vcol[j]) {
+                const double a = zabs(v);
+                if (!(a < piv)) {
+                    piv = a;
+                    J   = j;
+                }
+            }
+        }
+        BlockReduce<NT>::argmax(piv, J, sv, si);
+        if (J < 0) {
+            q = q - 1 == 0 ? -1 : q - 1;
+            break;
+        }
+        if (tid == 0)
+            vrow[I] = 1;
+        __syncthreads();
+        const zd rJ = Vt[J + (size_t)N * k];
+        if (zabs(rJ) > 1e-15) {
+            const zd gamma   = zrecip(rJ);
+            const double *pJ = xs + 3 * (size_t)cols[J];
+            double piv2      = -1.;
+            int I2           = -1;
+            for (int i = tid; i < M; i += NT) {
+                zd v = kernel_entry_z(kd, xt + 3 * (size_t)rows[i], pJ);
+                for (int p = 0; p < k; p++)
+                    v = zsub(v, zmul(Vt[J + (size_t)N * p], U[i + (size_t)M * p]));
+                v                    = zmul(v, gamma);
+                U[i + (size_t)M * k] = v;
+                if (!vrow[i]) {
+                    const double a = zabs(v);
+                    if (!(a < piv2)) {
+                        piv2 = a;
+                        I2   = i;
+                    }
+                }
+            }
+            BlockReduce<NT>::argmax(piv2, I2, sv, si);
+            if (I2 < 0)
+                break;
+            if (tid == 0)
+                vcol[J] = 1;
+            const zd cc = cdot(M, [&](int i) { const zd c = U[i + (size_t)M * k]; return zmul(zconj(c), c); });
+            const zd rr = cdot(N, [&](int j) { const zd r = Vt[j + (size_t)N * k]; return zmul(zconj(r), r); });
+            aux         = zabs(cc) * zabs(rr);
+            zd fa       = {0., 0.};
+            for (int p = 0; p < k; p++) {
+                const zd vr = cdot(N, [&](int j) { return zmul(zconj(Vt[j + (size_t)N * p]), Vt[j + (size_t)N * k]); });
+                const zd uc = cdot(M, [&](int i) { return zmul(zconj(U[i + (size_t)M * p]), U[i + (size_t)M * k]); });
+                fa          = zadd(fa, zmul(vr, uc));
+            }
+            frob = frob + (aux + 2 * fa.re);
+            I    = I2;
+            __syncthreads();
+        } else {
+            q -= 1;
+            if (q == 0)
+                q = -1;
+            break;
+        }
+    }
+    if (tid == 0)
+        rank_out[blockIdx.x] = q;
+}
+
+// complex crosses (U_s M x r, Vt_s N x r, complex) -> real form: U2 (2M x 2r)
+// and Vt2 (2N x 2r) such that U2 Vt2^T is the real form of U Vt^T
+__global__ void pack_z_kernel(const PackItem *__restrict__ items, const double *__restrict__ scratch, double *__restrict__ arena) {
+    const PackItem it = items[blockIdx.x];
+    const int M = it.M, N = it.N, r = it.r; // complex sizes
+    const zd *U = reinterpret_cast<const zd *>(scratch + it.src_u);
+    const zd *V = reinterpret_cast<const zd *>(scratch + it.src_v);
+    double *U2 = arena + it.dst_u, *V2 = arena + it.dst_v;
+    // U2[2i+a, 2k+b] = [[re, -im], [im, re]][a][b] of U[i, k]
+    for (long long e = threadIdx.x; e < 4LL * M * r; e += blockDim.x) {
+        const int row = (int)(e % (2 * M)), col = (int)(e / (2 * M));
+        const zd u    = U[row / 2 + (size_t)M * (col / 2)];
+        const int a = row & 1, b = col & 1;
+        U2[e]       = a == b ? u.re : (a ? u.im : -u.im);
+    }
+    // Vt2 = (V2)^T with V2 the real form of V = Vt^T: V2[2k+b, 2j+c] = form(V[k, j]),
+    // so Vt2[2j+c, 2k+b] = form(Vt[j, k])[b][c]
+    for (long long e = threadIdx.x; e < 4LL * N * r; e += blockDim.x) {
+        const int row = (int)(e % (2 * N)), col = (int)(e / (2 * N)); // row 2j+c, col 2k+b
+        const zd v    = V[row / 2 + (size_t)N * (col / 2)];
+        const int c = row & 1, b = col & 1;
+        V2[e]       = b == c ? v.re : (b ? v.im : -v.im);
+    }
+}
+
+// dense leaves of a complex matrix in real form: rows / columns are indices
+// of the doubled numbering, whose permutation keeps the component (2p + c)
+__global__ void dense_fill_z_kernel(const DenseChunk *__restrict__ chunks, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t, const int *__restrict__ perm_s,
+                                    KernelDesc kd, double *__restrict__ arena) {
+    const DenseChunk C = chunks[blockIdx.x];
+    const int hn       = C.h * C.n;
+    for (int e = threadIdx.x; e < hn; e += blockDim.x) {
+        const int i = e % C.h, j = e / C.h;
+        const int pi = perm_t[C.row0 + i], pj = perm_s[C.oj + j];
+        const zd z   = kernel_entry_z(kd, xt + 3 * (size_t)(pi >> 1), xs + 3 * (size_t)(pj >> 1));
+        const int a = pi & 1, b = pj & 1;
+        arena[C.dst + e] = a == b ? z.re : (a ? z.im : -z.im);
+    }
+}
+
 } // namespace
 
 void launch_partial_aca(const AcaBlock *blocks, int nblocks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double eps, double *scratch, unsigned char *flags,
@@ -343,7 +569,25 @@ void launch_pack_factors(const PackItem *items, int nitems, const double *scratc
 void launch_dense_fill(const DenseChunk *chunks, int nchunks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st) {
     if (nchunks <= 0)
         return;
-    dense_fill_kernel<<<nchunks, 128, 0, st>>>(chunks, xt, xs, perm_t, perm_s, kd, arena);
+    if (kd.id == 2)
+        dense_fill_z_kernel<<<nchunks, 128, 0, st>>>(chunks, xt, xs, perm_t, perm_s, kd, arena);
+    else
+        dense_fill_kernel<<<nchunks, 128, 0, st>>>(chunks, xt, xs, perm_t, perm_s, kd, arena);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_partial_aca_z(const AcaBlock *blocks, int nblocks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double eps, double *scratch,
+                          unsigned char *flags, int *rank_out, cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    partial_aca_z_kernel<<<nblocks, kAcaThreads, 0, st>>>(blocks, xt, xs, perm_t, perm_s, kd, eps, scratch, flags, rank_out);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_pack_z(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st) {
+    if (nitems <= 0)
+        return;
+    pack_z_kernel<<<nitems, 128, 0, st>>>(items, scratch, arena);
     HTGPU_CUDA(cudaGetLastError());
 }
 

@@ -157,6 +157,22 @@ int htgpu_hmatrix_create(htgpu_cluster t, htgpu_cluster s, double epsilon, doubl
     });
 }
 
+int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out) {
+    return guarded([&] {
+        need(t, "target cluster");
+        need(s, "source cluster");
+        need(out, "out");
+        auto *h = new htgpu_hmatrix_s;
+        try {
+            h->h.reset(new htgpu::HMatrix(t->tree, s->tree, epsilon, eta, device, true));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
 int htgpu_hmatrix_destroy(htgpu_hmatrix h) {
     return guarded([&] { delete h; });
 }

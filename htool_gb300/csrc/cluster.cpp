@@ -344,4 +344,23 @@ std::vector<BlockTask> build_local_tasks(const ClusterTree &T, const ClusterTree
     return local;
 }
 
+// the tree of the interleaved real form of a complex vector: point p becomes
+// indices 2p and 2p+1, every node keeps its geometry with doubled offset and
+// size, and perm2[2i + c] = 2 perm[i] + c
+ClusterTree double_tree(const ClusterTree &T) {
+    ClusterTree D      = T;
+    D.n                = 2 * T.n;
+    D.minclustersize   = 2 * T.minclustersize;
+    D.perm.resize(2 * T.perm.size());
+    for (std::size_t i = 0; i < T.perm.size(); i++) {
+        D.perm[2 * i]     = 2 * T.perm[i];
+        D.perm[2 * i + 1] = 2 * T.perm[i] + 1;
+    }
+    for (auto &c : D.nodes) {
+        c.offset *= 2;
+        c.size *= 2;
+    }
+    return D;
+}
+
 } // namespace htgpu

@@ -50,8 +50,14 @@ std::string inum(long long v) { return std::to_string(v); }
 
 } // namespace
 
-HMatrix::HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const ClusterTree> s, double eps, double eta, int device) : T(std::move(t)), S(std::move(s)), eps_(eps), eta_(eta), device_(device) {
-    require(T && S, "HMatrix needs target and source cluster trees");
+HMatrix::HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const ClusterTree> s, double eps, double eta, int device, bool complex)
+    : T(complex ? std::make_shared<const ClusterTree>(double_tree(*t)) : t), S(complex ? std::make_shared<const ClusterTree>(double_tree(*s)) : s), eps_(eps), eta_(eta), device_(device) {
+    require(t && s, "HMatrix needs target and source cluster trees");
+    if (complex) {
+        complex_ = true;
+        Tz_      = std::move(t);
+        Sz_      = std::move(s);
+    }
     require(eps > 0, "epsilon must be positive");
     require(eta >= 0, "eta must be non-negative");
     bp.eta = eta;
@@ -80,19 +86,32 @@ HMatrix::~HMatrix() {
 }
 
 void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
-    require(kd.id == 0 || kd.id == 1, "device generator id must be 0 (1/(1e-5+r)) or 1 (Laplace) for a real H-matrix", 2);
+    if (complex_)
+        require(kd.id == 2, "a complex H-matrix needs the Helmholtz device generator (id 2)", 2);
+    else
+        require(kd.id == 0 || kd.id == 1, "device generator id must be 0 (1/(1e-5+r)) or 1 (Laplace) for a real H-matrix", 2);
+    // block tree and ACA on the trees of the points; a complex H-matrix is
+    // stored in real form on doubled trees (T, S), its leaves scaled by f
+    const ClusterTree &Ta = complex_ ? *Tz_ : *T, &Sa = complex_ ? *Sz_ : *S;
+    const int f           = complex_ ? 2 : 1;
     HTGPU_CUDA(cudaSetDevice(device_));
     st_             = BuildStats();
     samples_x_.clear();
     samples_y_.clear();
     const double t0 = now();
     bp.eta          = eta_;
-    std::vector<BlockTask> tasks = build_local_tasks(*T, *S, bp);
+    std::vector<BlockTask> tasks = build_local_tasks(Ta, Sa, bp);
     st_.block_tree_seconds       = now() - t0;
 
     DevBuf<double> dxt, dxs;
-    dxt.upload(xt, 3 * (std::size_t)nr, stream_);
-    dxs.upload(xs, 3 * (std::size_t)nc, stream_);
+    dxt.upload(xt, 3 * (std::size_t)Ta.n, stream_);
+    dxs.upload(xs, 3 * (std::size_t)Sa.n, stream_);
+    DevBuf<int> zperm_t, zperm_s; // complex: the permutations of the points
+    if (complex_) {
+        zperm_t.upload(Ta.perm, stream_);
+        zperm_s.upload(Sa.perm, stream_);
+    }
+    const int *aca_pt = complex_ ? zperm_t.p : perm_t.p, *aca_ps = complex_ ? zperm_s.p : perm_s.p;
 
     // ---- recursion state of ComputeAdmissibleBlock
     struct Req {
@@ -109,7 +128,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
     std::vector<int> pending;
 
     std::function<void(int)> split = [&](int id) {
-        const ClusterNode &tn = T->nodes[reqs[id].t], &sn = S->nodes[reqs[id].s];
+        const ClusterNode &tn = Ta.nodes[reqs[id].t], &sn = Sa.nodes[reqs[id].s];
         reqs[id].state = 2;
         if (tn.nb_sons == 0 && sn.nb_sons == 0)
             return;
@@ -121,7 +140,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             Req r;
             r.t   = by_t ? first + p : reqs[id].t;
             r.s   = by_t ? reqs[id].s : first + p;
-            r.adm = admissible(T->nodes[r.t], S->nodes[r.s], eta_);
+            r.adm = admissible(Ta.nodes[r.t], Sa.nodes[r.s], eta_);
             mine[p] = (int)reqs.size();
             reqs.push_back(r);
         }
@@ -160,8 +179,8 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
     const double ta = now();
     while (!pending.empty()) {
         std::sort(pending.begin(), pending.end(), [&](int a, int b) {
-            long long ca = (long long)T->nodes[reqs[a].t].size + S->nodes[reqs[a].s].size;
-            long long cb = (long long)T->nodes[reqs[b].t].size + S->nodes[reqs[b].s].size;
+            long long ca = (long long)Ta.nodes[reqs[a].t].size + Sa.nodes[reqs[a].s].size;
+            long long cb = (long long)Ta.nodes[reqs[b].t].size + Sa.nodes[reqs[b].s].size;
             return ca != cb ? ca > cb : a < b;
         });
         std::size_t free_b = 0, total_b = 0;
@@ -180,13 +199,13 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
                 if (!fresh.empty()) {
                     std::vector<float> fx(fresh.size() * kMlpIn), fy(fresh.size());
                     for (std::size_t i = 0; i < fresh.size(); i++) {
-                        const ClusterNode &tn = T->nodes[reqs[fresh[i]].t], &sn = S->nodes[reqs[fresh[i]].s];
+                        const ClusterNode &tn = Ta.nodes[reqs[fresh[i]].t], &sn = Sa.nodes[reqs[fresh[i]].s];
                         block_features(tn.size, sn.size, tn.rad, sn.rad, tn.ctr, sn.ctr, eps_, kd.id, &fx[i * kMlpIn]);
                     }
                     predictor_->predict(fx.data(), (int)fresh.size(), fy.data());
                     for (std::size_t i = 0; i < fresh.size(); i++) {
                         Req &r         = reqs[fresh[i]];
-                        const int qmax = max_profitable_rank(T->nodes[r.t].size, S->nodes[r.s].size);
+                        const int qmax = max_profitable_rank(Ta.nodes[r.t].size, Sa.nodes[r.s].size);
                         const float pr = fy[i];
                         const int want = pr >= 60.f ? qmax : (int)std::ceil(std::max(pr, 0.f) * (1.0 + margin_)) + 2;
                         r.cap          = std::max(1, std::min(qmax, std::max(want, 4)));
@@ -200,12 +219,12 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             long long sc = 0, fl = 0;
             while (pos < pending.size()) {
                 Req &r = reqs[pending[pos]];
-                const ClusterNode &tn = T->nodes[r.t], &sn = S->nodes[r.s];
+                const ClusterNode &tn = Ta.nodes[r.t], &sn = Sa.nodes[r.s];
                 const int M = tn.size, N = sn.size;
                 int qmax    = max_profitable_rank(M, N);
                 if (r.cap == 0)
                     r.cap = std::max(1, std::min(qmax, kDefaultCap));
-                long long need = (long long)r.cap * (M + N);
+                long long need = (long long)f * r.cap * (M + N); // doubles (complex entries take two)
                 if (!blocks.empty() && sc + need > budget)
                     break;
                 AcaBlock b;
@@ -216,7 +235,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
                 b.cap     = r.cap;
                 b.pad     = 0;
                 b.u_off   = sc;
-                b.v_off   = sc + (long long)M * r.cap;
+                b.v_off   = sc + (long long)f * M * r.cap;
                 b.flag_off = fl;
                 for (int d = 0; d < 3; d++)
                     b.ctr[d] = tn.ctr[d];
@@ -236,7 +255,10 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             st_.aca_peak_scratch_bytes = std::max(st_.aca_peak_scratch_bytes, 8 * sc);
             flags.alloc(fl);
             dranks.alloc(blocks.size());
-            launch_partial_aca(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, perm_t.p, perm_s.p, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+            if (complex_)
+                launch_partial_aca_z(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+            else
+                launch_partial_aca(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
             std::vector<int> ranks(blocks.size());
             HTGPU_CUDA(cudaMemcpyAsync(ranks.data(), dranks.p, sizeof(int) * ranks.size(), cudaMemcpyDeviceToHost, stream_));
             HTGPU_CUDA(cudaStreamSynchronize(stream_));
@@ -250,7 +272,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
                 const int id = ids[b];
                 const int r  = ranks[b];
                 if (r > 0 || r == -1) { // a decided block: a training sample for the rank predictor
-                    const ClusterNode &tn = T->nodes[reqs[id].t], &sn = S->nodes[reqs[id].s];
+                    const ClusterNode &tn = Ta.nodes[reqs[id].t], &sn = Sa.nodes[reqs[id].s];
                     const std::size_t at  = samples_x_.size();
                     samples_x_.resize(at + kMlpIn);
                     block_features(tn.size, sn.size, tn.rad, sn.rad, tn.ctr, sn.ctr, eps_, kd.id, &samples_x_[at]);
@@ -265,16 +287,16 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
                     it.N     = blocks[b].N;
                     it.r     = r;
                     it.pad   = 0;
-                    it.dst_u = packed;
-                    it.dst_v = packed + (long long)it.M * r;
-                    packed += (long long)r * (it.M + it.N);
+                    it.dst_u = packed; // real form: f M x f r and f N x f r
+                    it.dst_v = packed + (long long)f * f * it.M * r;
+                    packed += (long long)f * f * r * (it.M + it.N);
                     items.push_back(it);
                     acc.push_back({id, round, r, it.dst_u, it.dst_v});
                 } else if (r == -1) {
                     st_.false_positive++;
                     split(id);
                 } else if (r == -2) {
-                    const ClusterNode &tn = T->nodes[reqs[id].t], &sn = S->nodes[reqs[id].s];
+                    const ClusterNode &tn = Ta.nodes[reqs[id].t], &sn = Sa.nodes[reqs[id].s];
                     reqs[id].cap = std::min(max_profitable_rank(tn.size, sn.size), std::max(2 * reqs[id].cap, 64));
                     st_.overflow_reruns++;
                     next.push_back(id);
@@ -287,7 +309,10 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             if (!items.empty()) {
                 DevBuf<PackItem> ditems;
                 ditems.upload(items, stream_);
-                launch_pack_factors(ditems.p, (int)items.size(), scratch.p, buf->p, stream_);
+                if (complex_)
+                    launch_pack_z(ditems.p, (int)items.size(), scratch.p, buf->p, stream_);
+                else
+                    launch_pack_factors(ditems.p, (int)items.size(), scratch.p, buf->p, stream_);
                 HTGPU_CUDA(cudaStreamSynchronize(stream_));
             }
             round_bufs.push_back(std::move(buf));
@@ -313,7 +338,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             np[k] = not_pushed(kids[r.first_kid + k]);
             all   = all && np[k];
         }
-        const std::size_t bsize = (std::size_t)T->nodes[r.t].size * (std::size_t)S->nodes[r.s].size;
+        const std::size_t bsize = (std::size_t)Ta.nodes[r.t].size * (std::size_t)Sa.nodes[r.s].size;
         if (bsize <= bp.maxblocksize && all)
             return true;
         for (int k = 0; k < r.nkids; k++)
@@ -327,35 +352,35 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
 
     // ---- final layout: low-rank leaves sorted by (offset_i, offset_j)
     std::sort(acc.begin(), acc.end(), [&](const Accepted &a, const Accepted &b) {
-        int ia = T->nodes[reqs[a.req].t].offset, ib = T->nodes[reqs[b.req].t].offset;
+        int ia = Ta.nodes[reqs[a.req].t].offset, ib = Ta.nodes[reqs[b.req].t].offset;
         if (ia != ib)
             return ia < ib;
-        return S->nodes[reqs[a.req].s].offset < S->nodes[reqs[b.req].s].offset;
+        return Sa.nodes[reqs[a.req].s].offset < Sa.nodes[reqs[b.req].s].offset;
     });
     lr_h.clear();
     std::vector<LeafSrc> lr_src;
     for (auto &a : acc) {
-        const ClusterNode &tn = T->nodes[reqs[a.req].t], &sn = S->nodes[reqs[a.req].s];
+        const ClusterNode &tn = Ta.nodes[reqs[a.req].t], &sn = Sa.nodes[reqs[a.req].s];
         LrLeaf L;
-        L.oi    = tn.offset;
-        L.oj    = sn.offset;
-        L.m     = tn.size;
-        L.n     = sn.size;
-        L.r     = a.r;
+        L.oi    = f * tn.offset;
+        L.oj    = f * sn.offset;
+        L.m     = f * tn.size;
+        L.n     = f * sn.size;
+        L.r     = f * a.r;
         L.nch   = 0;
         L.a_off = 0;
         lr_h.push_back(L);
         lr_src.push_back({a.round, a.u, a.v});
     }
     std::sort(dense_ts.begin(), dense_ts.end(), [&](const std::pair<int, int> &a, const std::pair<int, int> &b) {
-        int ia = T->nodes[a.first].offset, ib = T->nodes[b.first].offset;
+        int ia = Ta.nodes[a.first].offset, ib = Ta.nodes[b.first].offset;
         if (ia != ib)
             return ia < ib;
-        return S->nodes[a.second].offset < S->nodes[b.second].offset;
+        return Sa.nodes[a.second].offset < Sa.nodes[b.second].offset;
     });
     dn_h.clear();
     for (auto &d : dense_ts)
-        dn_h.push_back({T->nodes[d.first].offset, S->nodes[d.second].offset, T->nodes[d.first].size, S->nodes[d.second].size});
+        dn_h.push_back({f * Ta.nodes[d.first].offset, f * Sa.nodes[d.second].offset, f * Ta.nodes[d.first].size, f * Sa.nodes[d.second].size});
     std::vector<const double *> bufs;
     for (auto &b : round_bufs)
         bufs.push_back(b->p);
@@ -1161,6 +1186,7 @@ void HMatrix::phase_bytes(int mu, long long *b) const {
 
 void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st) {
     require(mu >= 1, "number of right-hand sides must be positive");
+    require(!complex_, "transposed products of complex H-matrices are not supported", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
     if (!transp_) {
         // leaves of H^T from the stored ones (one pass through host memory)
@@ -1287,17 +1313,22 @@ long long HMatrix::product_bytes(int mu) const { return stored_bytes() + 8LL * m
 std::map<std::string, std::string> HMatrix::infos() const {
 
     std::map<std::string, std::string> m;
+    // a complex H-matrix reports its complex sizes and ranks (stored in real
+    // form: every size doubled, every block four times larger)
+    const int f = complex_ ? 2 : 1;
+    const ClusterTree &Ti = complex_ ? *Tz_ : *T, &Si = complex_ ? *Sz_ : *S;
+    const int nri = nr / f, nci = nc / f;
     const std::size_t big = (std::size_t)std::max(nr, nc);
     std::size_t dmax = 0, dmin = big, lmax = 0, lmin = big, rmax = 0, rmin = big;
     double dmean = 0, lmean = 0, rmean = 0;
     for (auto &D : dn_h) {
-        std::size_t s = (std::size_t)D.m * D.n;
+        std::size_t s = (std::size_t)D.m * D.n / (f * f);
         dmax          = std::max(dmax, s);
         dmin          = std::min(dmin, s);
         dmean += s;
     }
     for (auto &L : lr_h) {
-        std::size_t s = (std::size_t)L.m * L.n, r = (std::size_t)L.r;
+        std::size_t s = (std::size_t)L.m * L.n / (f * f), r = (std::size_t)L.r / f;
         lmax          = std::max(lmax, s);
         lmin          = std::min(lmin, s);
         lmean += s;
@@ -1315,8 +1346,8 @@ std::map<std::string, std::string> HMatrix::infos() const {
     for (auto &D : dn_h)
         compressed += (double)D.m * (double)D.n;
     const double uncompressed = (double)((long)nr) * nc;
-    m["Source_size"]              = inum(nc);
-    m["Target_size"]              = inum(nr);
+    m["Source_size"]              = inum(nci);
+    m["Target_size"]              = inum(nri);
     m["Dimension"]                = "1";
     m["Dense_block_size_max"]     = inum((long long)dmax);
     m["Dense_block_size_mean"]    = num(dmean);
@@ -1336,21 +1367,22 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["Eps"]                      = num(eps_);
     m["MinTargetDepth"]           = num(bp.mintargetdepth);
     m["MinSourceDepth"]           = num(bp.minsourcedepth);
-    m["MinClusterSizeTarget"]     = num(T->minclustersize);
-    m["MinClusterSizeSource"]     = num(S->minclustersize);
-    m["MinClusterDepthTarget"]    = num(T->min_depth);
-    m["MaxClusterDepthTarget"]    = num(T->max_depth);
-    m["MinClusterDepthSource"]    = num(S->min_depth);
-    m["MaxClusterDepthSource"]    = num(S->max_depth);
+    m["MinClusterSizeTarget"]     = num(Ti.minclustersize);
+    m["MinClusterSizeSource"]     = num(Si.minclustersize);
+    m["MinClusterDepthTarget"]    = num(Ti.min_depth);
+    m["MaxClusterDepthTarget"]    = num(Ti.max_depth);
+    m["MinClusterDepthSource"]    = num(Si.min_depth);
+    m["MaxClusterDepthSource"]    = num(Si.max_depth);
     m["MaxBlockSize"]             = inum((long long)bp.maxblocksize);
     m["Block_tree_max"]           = num(st_.block_tree_seconds);
     m["Block_tree_mean"]          = num(st_.block_tree_seconds);
     m["Blocks_max"]               = num(st_.build_seconds - st_.block_tree_seconds);
     m["Blocks_mean"]              = num(st_.build_seconds - st_.block_tree_seconds);
     m["Number_of_MPI_tasks"]      = "1";
-    m["Local_size_max"]           = inum(nr);
-    m["Local_size_mean"]          = num(nr);
-    m["Local_size_min"]           = inum(nr);
+    m["Local_size_max"]           = inum(nr / (complex_ ? 2 : 1));
+    m["Local_size_mean"]          = num(nr / (complex_ ? 2 : 1));
+    m["Local_size_min"]           = inum(nr / (complex_ ? 2 : 1));
+    m["GPU_complex"]              = inum(complex_ ? 1 : 0);
     m["GPU_aca_rounds"]           = num(st_.aca_rounds);
     m["GPU_aca_scratch_bytes"]      = inum(st_.aca_scratch_bytes);
     m["GPU_aca_peak_scratch_bytes"] = inum(st_.aca_peak_scratch_bytes);

@@ -20,7 +20,11 @@ class Mlp;
 
 class HMatrix {
   public:
-    HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const ClusterTree> s, double eps, double eta, int device);
+    // complex: a complex (Helmholtz) H-matrix on the trees t, s of its
+    // points, stored and applied in real form on doubled trees (complex
+    // entry z -> [[re, -im], [im, re]]; vectors as interleaved re, im)
+    HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const ClusterTree> s, double eps, double eta, int device, bool complex = false);
+    bool is_complex() const { return complex_; }
     ~HMatrix();
 
     // HMatrix::build(gen, xt, xs) with partialACA and a built-in device
@@ -179,6 +183,8 @@ class HMatrix {
     long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
     unsigned long long layout_gen_ = 0;
+    bool complex_ = false;
+    std::shared_ptr<const ClusterTree> Tz_, Sz_; // complex: the trees of the points
     std::unique_ptr<HMatrix> transp_; // transposed twin, built on first use
     long long aca_budget_ = 0;
     Mlp *predictor_       = nullptr;

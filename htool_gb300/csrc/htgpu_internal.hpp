@@ -189,4 +189,7 @@ std::vector<int> partition_rows(int nleaves, const long long *leaves, int nr, in
 void save_cluster(const ClusterTree &T, const std::string &name);
 ClusterTree read_cluster(const std::string &perm_file, const std::string &tree_file);
 
+// tree of the interleaved (re, im) real form of vectors on the points of T
+ClusterTree double_tree(const ClusterTree &T);
+
 } // namespace htgpu

@@ -30,7 +30,17 @@ struct PackItem {
 // copy the first r columns of scratch U (ld M) and Vt (ld N) to the arena
 void launch_pack_factors(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st);
 
+// complex (Helmholtz, kd.id 2) partialACA: AcaBlock offsets count doubles,
+// each scratch entry is a complex (2 doubles); perm_t / perm_s are the
+// complex-point permutations
+void launch_partial_aca_z(const AcaBlock *blocks, int nblocks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double eps, double *scratch,
+                          unsigned char *flags, int *rank_out, cudaStream_t st);
+// complex crosses (PackItem sizes complex, offsets in doubles) -> real form
+// U2 (2M x 2r) at dst_u and Vt2 (2N x 2r) at dst_v
+void launch_pack_z(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st);
+
 // D[dst + i + h j] = G(perm_t[row0 + i], perm_s[oj + j]) for every chunk
+// (kd.id 2: the real form of the complex kernel, on doubled numberings)
 void launch_dense_fill(const DenseChunk *chunks, int nchunks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double *arena, cudaStream_t st);
 
 // ---- product (FP64 storage; DFMA or FP32-pipe emulation, df64.cuh) ---------

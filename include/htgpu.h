@@ -35,6 +35,7 @@ extern "C" {
  * VirtualGenerator<T>::copy_submatrix, include/htool/types/virtual_generator.hpp:22) */
 #define HTGPU_KERNEL_INV_R_EPS 0 /* 1 / (1e-5 + |x - y|) */
 #define HTGPU_KERNEL_LAPLACE 1   /* 1 / (4 pi |x - y|), 0 where x == y */
+#define HTGPU_KERNEL_HELMHOLTZ 2 /* exp(i k |x - y|) / (4 pi |x - y|), 0 where x == y; complex handles only */
 
 typedef struct htgpu_cluster_s *htgpu_cluster;
 typedef struct htgpu_hmatrix_s *htgpu_hmatrix;
@@ -86,6 +87,17 @@ int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks,
  * The matrix lives on CUDA device `device`. */
 int htgpu_hmatrix_create(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out);
 int htgpu_hmatrix_destroy(htgpu_hmatrix h);
+
+/* HMatrix<std::complex<double>>(t, s, epsilon, eta) (hmatrix.hpp:44-270)
+ * with partialACA; build with HTGPU_KERNEL_HELMHOLTZ (exp(i k r)/(4 pi r),
+ * 0 at r = 0, k = kernel_param).  Complex vectors are interleaved (re, im)
+ * doubles, column-major per right-hand side (std::complex<double> layout):
+ * every product entry point takes them with twice the real sizes.  The
+ * matrix is stored and applied in real form (entry z -> [[re, -im],
+ * [im, re]]), so every storage policy and the batched products apply;
+ * htgpu_hmatrix_get_leaves / get_factors describe that real form;
+ * transposed products are not available for complex handles. */
+int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out);
 
 /* set_maxblocksize / set_mintargetdepth / set_minsourcedepth (hmatrix.hpp:213-215). */
 int htgpu_hmatrix_set_maxblocksize(htgpu_hmatrix h, unsigned int maxblocksize);

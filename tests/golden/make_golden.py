@@ -17,6 +17,7 @@ Usage (needs the upstream sources, i.e. only in the build container):
     make -C oracle/refbuild REF=/root/reference/include
     python tests/golden/make_golden.py
 """
+import ctypes as C
 import hashlib
 import json
 import os
@@ -63,6 +64,41 @@ def hmatrix_case(R, name, xt, xs, kernel, eps, eta, mus=(1, 3)):
     print(name, "leaves", lr.shape[0], dn.shape[0], "ranks", lr[:, 4].min() if len(lr) else None, lr[:, 4].max() if len(lr) else None)
 
 
+def helmholtz_case(R, name, n, k, eps, eta, mus=(1, 3)):
+    """complex H-matrix (HMatrix<std::complex<double>>, partialACA) of
+    exp(i k r)/(4 pi r) on the unit-cube surface: points, right-hand sides,
+    upstream products and leaf lists (the factors are too large to keep)"""
+    L = R._L
+    vp = C.c_void_p
+    L.ref_hmatrix_build_z.restype = vp
+    L.ref_hmatrix_build_z.argtypes = [vp, vp, C.c_int, vp, C.c_int, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char, C.c_int]
+    L.ref_hmatrix_counts_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_leaves_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_mvprod_z.argtypes = [vp, vp, vp, C.c_int]
+    L.ref_hmatrix_free_z.argtypes = [vp]
+    pts = G.cube_surface(n, seed=1)
+    ct = R.cluster(pts)
+    h = L.ref_hmatrix_build_z(ct.h, ct.h, n, pts.ctypes.data, n, pts.ctypes.data, k, eps, eta, 0, b"N", b"N", 0)
+    nlr, nd = C.c_int(), C.c_int()
+    L.ref_hmatrix_counts_z(h, C.byref(nlr), C.byref(nd))
+    lr = np.empty((nlr.value, 5), np.int32)
+    dn = np.empty((nd.value, 4), np.int32)
+    L.ref_hmatrix_leaves_z(h, lr.ctypes.data, dn.ctypes.data)
+    data = dict(xt=pts, lr=lr, dense=dn)
+    rng = np.random.default_rng(7)
+    for mu in mus:
+        x = rng.standard_normal(n * mu) + 1j * rng.standard_normal(n * mu)
+        y = np.empty(n * mu, np.complex128)
+        L.ref_hmatrix_mvprod_z(h, x.ctypes.data, y.ctypes.data, mu)
+        data["x_mu%d" % mu] = x
+        data["y_mu%d" % mu] = y
+    L.ref_hmatrix_free_z(h)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
+    with open(os.path.join(OUT, name + ".json"), "w") as f:
+        json.dump(dict(kernel=2, wavenumber=k, eps=eps, eta=eta, minclustersize=10, nb_sons=2), f, indent=1, sort_keys=True)
+    print(name, "leaves", lr.shape[0], dn.shape[0], "ranks", lr[:, 4].min(), lr[:, 4].max())
+
+
 def aca_case(R):
     """test_lrmat_partialACA.cpp: 500 x 100 disks at distances 15..40, srand(1)
     before each pair, fixed rank 10 and adaptive eps = 1e-4."""
@@ -107,6 +143,9 @@ def main():
         s = G.disk_glibc(1000, 1.0 + dz)
         hmatrix_case(R, "disks2000x1000_%s_k1" % tag, t, s, 1, 1e-3, 10.0)
     aca_case(R)
+    # configuration 3 at fixture size: Helmholtz k = 20 on the cube surface,
+    # eta 3, eps 1e-5, complex128
+    helmholtz_case(R, "helmholtz_cube2000", 2000, 20.0, 1e-5, 3.0)
     # htool's own CSV pair for the configuration-1 cluster tree (save_cluster)
     ct = R.cluster(cyl)
     R._L.ref_cluster_save(ct.h, os.path.join(OUT, "cyl4000_cluster").encode())

@@ -1,0 +1,60 @@
+"""Complex H-matrices (Helmholtz exp(i k r)/(4 pi r), k = 20, on the unit
+cube surface, eta 3, eps 1e-5): the device assembly reproduces upstream
+htool's complex leaf partition and ranks, and its products match upstream's
+complex products on the same inputs."""
+import numpy as np
+import pytest
+
+import htool_gb300 as H
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def case(golden):
+    g, meta = golden("helmholtz_cube2000")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    hm = H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128).build(H.HELMHOLTZ, g["xt"], kernel_param=meta["wavenumber"])
+    return g, meta, hm
+
+
+def test_complex_leaves_match_upstream(case):
+    g, meta, hm = case
+    lr, dn = hm.get_leaves()  # real form: every size doubled
+    assert np.all(lr[:, :5] % 2 == 0) and np.all(dn % 2 == 0)
+    assert np.array_equal(lr // 2, g["lr"])
+    assert np.array_equal(dn // 2, g["dense"])
+    info = hm.get_infos()
+    assert int(info["Number_of_lrmat"]) == g["lr"].shape[0]
+    assert int(info["Rank_max"]) == int(g["lr"][:, 4].max())
+    assert int(info["Target_size"]) == g["xt"].shape[0]
+
+
+def test_complex_products_match_upstream(case):
+    g, meta, hm = case
+    for mu in (1, 3):
+        y = hm.mvprod_global_to_global(g["x_mu%d" % mu], mu)
+        assert y.dtype == np.complex128
+        assert rel(y, g["y_mu%d" % mu]) < 1e-10
+    assert hm.device_status() == 0
+
+
+def test_complex_dense_rows_and_precision(case):
+    g, meta, hm = case
+    pts, x = g["xt"], g["x_mu1"]
+    y = hm.mvprod_global_to_global(x)
+    rows = np.random.default_rng(3).choice(pts.shape[0], 200, replace=False)
+    r = np.sqrt(((pts[rows, None, :] - pts[None, :, :]) ** 2).sum(-1))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        K = np.where(r == 0, 0.0, np.exp(1j * meta["wavenumber"] * r) / (4 * np.pi * r))
+    assert rel(y[rows], K @ x) < 10 * meta["eps"]
+    hm.set_precision("mixed")
+    assert rel(hm.mvprod_global_to_global(x), y) < 10 * meta["eps"]
+    hm.set_precision("fp64")
+    with pytest.raises(NotImplementedError):
+        hm.mvprod_transp_global_to_global(np.zeros(pts.shape[0], np.complex128))
