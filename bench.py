@@ -49,6 +49,8 @@ def parse():
     # fixed configuration instead of the autotuner (e.g. to replay a tuned run under a profiler)
     p.add_argument("--fp64-split", default=None, help="phase-1,phase-2 DFMA per mille, e.g. 0,650")
     p.add_argument("--phase1-mode", type=int, default=None, help="0 tile kernels, 1 streamed")
+    p.add_argument("--mixed-split", type=int, default=None, help="mixed precision: DFMA per mille of the dense blocks")
+    p.add_argument("--mixed-phase1-mode", type=int, default=None, help="mixed precision: 0 tile kernels, 1 streamed")
     return p.parse_args()
 
 
@@ -213,7 +215,7 @@ def run_gpu(args):
         ms_step = ms_total / args.steps
         ph = hm.profile(1, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
         pb = hm.phase_bytes(1)
-        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_warp_kernel", "phase2_warp_kernel", "zsum_kernel"]
+        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_warp_kernel", "phase2_ws_kernel", "zsum_kernel"]
         k = max(range(4), key=lambda i: ph[i])
         achieved = pb[k] / (ph[k] / 1e3) / 1e9
         total_bytes = sum(pb)
@@ -230,7 +232,7 @@ def run_gpu(args):
     time.sleep(0.5)  # let the sampler start before the timed regions
     # plain FP64 (autotuned DFMA / FP32-pipe split)
     hm.set_precision("fp64")
-    fixed = args.fp64_split is not None or args.phase1_mode is not None
+    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode))
     if fixed:
         if args.fp64_split is not None:
             hm.set_fp64_split(*[int(v) for v in args.fp64_split.split(",")])
@@ -247,7 +249,15 @@ def run_gpu(args):
     # mixed precision
     tau = 1.0
     hm.set_precision("mixed", tau)
-    tunem = None if fixed else hm.autotune(1, 5)
+    if fixed:
+        if args.mixed_split is not None:
+            hm.set_fp64_split(split[0], args.mixed_split)
+        if args.mixed_phase1_mode is not None:
+            hm.set_phase1_mode(args.mixed_phase1_mode)
+        tunem = None
+    else:
+        tunem = hm.autotune(1, 5)
+    splitm = hm.get_fp64_split()[1]
     msm, launches_per_step = timed_products()
     ym = yd.cpu().numpy().copy()
     stepm, dm = describe(msm)
@@ -302,7 +312,7 @@ def run_gpu(args):
         "rel_err_mixed_vs_fp64": err_mixed_vs_fp64,
         "speedup_mixed_vs_fp64": value / value64,
         "roofline": dm["roofline"], "whole_product": dm["whole_product"], "phase_ms": dm["phase_ms"], "phase_bytes": dm["phase_bytes"],
-        "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode()},
+        "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "dense_dfma_permille": splitm},
         "fp64": {"value": value64, "unit": UNIT, "ms_per_step": step64, "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
                  "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64}, "phase1_mode": p1mode64},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk, "device_status": status,

@@ -323,7 +323,9 @@ class HMatrix:
     def set_fp64_split(self, phase1_dfma_permille, phase2_dfma_permille):
         """Share (per mille) of the V-side and of the U-side/dense FP64
         multiply-adds run on the FP64 pipe; the rest uses the FP32-pipe
-        double-float emulation."""
+        double-float emulation.  Under a reduced precision, the phase-2 share
+        applies to that product's dense blocks (each precision keeps its own
+        split)."""
         _check(lib.htgpu_hmatrix_set_fp64_split(self.h, int(phase1_dfma_permille), int(phase2_dfma_permille)))
 
     def get_fp64_split(self):

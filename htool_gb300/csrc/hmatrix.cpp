@@ -764,12 +764,11 @@ void HMatrix::upload_phase1_lists() {
         p2_bytes_ += 8LL * pi.h * pi.ncol;
         n_cols_ += pi.ncol;
     }
-    n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
+    n_sctas_  = stream2_units_target();
     n_chunks_ = (long long)ch.size();
     {
-        const std::vector<int> r = stream_ranges(ch, n_sctas_);
-        n_ranges_                = (int)r.size() - 1;
-        sr_d.upload(r, stream_);
+        const std::vector<int> u = stream_units(ch, n_sctas_, &n_ranges_);
+        sr_d.upload(u, stream_);
     }
     sc_d.upload(ch, stream_);
     if (ch.empty())
@@ -792,8 +791,40 @@ int HMatrix::device_status() {
     return v;
 }
 
+// phase 2 of a reduced-precision product: its dense blocks stay FP64, on
+// the DFMA pipe for p2m_n64_ / 1000 of their elements and emulated on the
+// FP32 pipe for the rest (error diffusion, chunk by chunk)
+void HMatrix::upload_mixed_phase2() {
+    layout_gen_++; // launch lists change: captured products are stale
+    const double target = emu_ok_ ? p2m_n64_ / 1000.0 : 1.0;
+    long long seen = 0, dfma = 0;
+    for (auto &k : ch2_h_) {
+        if (k.kind != kStreamDfma && k.kind != kStreamEmu)
+            continue;
+        const long long e = (long long)k.h * k.ncol;
+        seen += e;
+        if (target >= 1.0 || (double)dfma < target * (double)seen) {
+            dfma += e;
+            k.kind = kStreamDfma;
+        } else
+            k.kind = kStreamEmu;
+    }
+    n_chunks_m_ = (long long)ch2_h_.size();
+    scm_d.upload(ch2_h_, stream_);
+    if (ch2_h_.empty())
+        scm_d.alloc(1);
+    const std::vector<int> u = stream_units(ch2_h_, n_sctas_, &n_ranges_m_);
+    srm_d.upload(u, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void HMatrix::set_fp64_split(int p1, int n64) {
     require(p1 >= 0 && p1 <= 1000 && n64 >= 0 && n64 <= 1000, "FP64 split: phase-1 and phase-2 DFMA shares in [0, 1000] per mille");
+    if (precision_ != 0) { // the dense blocks of a reduced-precision product
+        p2m_n64_ = n64;
+        upload_mixed_phase2();
+        return;
+    }
     p1_permille_ = p1;
     p2_n64_      = n64;
     assign_phase1_modes();
@@ -801,6 +832,11 @@ void HMatrix::set_fp64_split(int p1, int n64) {
 }
 
 void HMatrix::get_fp64_split(int *p1, int *n64) const {
+    if (precision_ != 0) {
+        *p1  = emu_ok_ ? p1_permille_ : 1000;
+        *n64 = emu_ok_ ? p2m_n64_ : 1000;
+        return;
+    }
     *p1  = emu_ok_ ? p1_permille_ : 1000;
     *n64 = emu_ok_ ? p2_n64_ : 1000;
 }
@@ -980,15 +1016,8 @@ void HMatrix::set_precision(int policy, double tau) {
     }
     p1m_d.upload(p1m, stream_);
     n_p1m_ = (int)p1m.size();
-    n_chunks_m_ = (long long)ch2.size();
-    scm_d.upload(ch2, stream_);
-    {
-        const std::vector<int> r = stream_ranges(ch2, n_sctas_);
-        n_ranges_m_              = (int)r.size() - 1;
-        srm_d.upload(r, stream_);
-    }
-    if (ch2.empty())
-        scm_d.alloc(1);
+    ch2_h_ = std::move(ch2);
+    upload_mixed_phase2();
     cim.resize(cim.size() + 4, 0); // bulk copies read whole 16-byte words
     cidxm_d.upload(cim, stream_);
     if (p1m.empty())
@@ -1100,24 +1129,26 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         HTGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         return ms / reps;
     };
-    // the fastest value of one knob, the others fixed
-    auto pick = [&](int &knob, std::initializer_list<int> values) {
-        float best = 1e30f;
-        int arg    = knob;
-        for (int v : values) {
-            knob           = v;
-            const float ms = timed();
-            if (ms < best) {
-                best = ms;
-                arg  = v;
-            }
-        }
-        knob = arg;
-        return best;
-    };
     float best = 1e30f;
     if (precision_ != 0) {
-        best = pick(p1_mode_, {0, 1});
+        // phase-1 modes with the dense blocks' DFMA / emulation split
+        int arg_mode = p1_mode_, arg_split = p2m_n64_;
+        const std::vector<int> shares = emu_ok_ ? std::vector<int>{0, 350, 650, 1000} : std::vector<int>{1000};
+        for (int mode : {0, 1})
+            for (int q2 : shares) {
+                p1_mode_ = mode;
+                p2m_n64_ = q2;
+                upload_mixed_phase2();
+                const float ms = timed();
+                if (ms < best) {
+                    best      = ms;
+                    arg_mode  = mode;
+                    arg_split = q2;
+                }
+            }
+        p1_mode_ = arg_mode;
+        p2m_n64_ = arg_split;
+        upload_mixed_phase2();
     } else {
         // every phase-1 mode with every DFMA/emulation split
         std::vector<std::pair<int, int>> splits;

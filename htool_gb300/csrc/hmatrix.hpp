@@ -163,6 +163,9 @@ class HMatrix {
     DevBuf<int> xexp, multi_d;
     std::vector<int> multi_h;
     int p1_permille_ = 300, p2_n64_ = 1;
+    int p2m_n64_ = 650; // reduced-precision products: DFMA share of the dense blocks (per mille)
+    std::vector<StreamChunk> ch2_h_; // their phase-2 chunks
+    void upload_mixed_phase2();
     bool emu_ok_ = false;
     void launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st);
     void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr);

@@ -4,22 +4,25 @@
 // contiguous, and consecutive panels follow each other, so phase 2 is a walk
 // over a byte range cut into chunks (<= 4 KB and <= 64 columns, one element
 // kind each: FP64 on the DFMA pipe, FP64 emulated on the FP32 pipe, FP32 or
-// BF16).  The host groups the chunks into ranges that end on row-chunk
-// boundaries; warps claim ranges through a global ticket, so uneven ranges
-// balance themselves.
+// BF16).  The host groups whole row chunks into units balanced by cost.
 //
-// Each warp works alone: it owns a ring of three shared-memory stages and
-// keeps two chunks in flight ahead of the one it computes.  A chunk arrives
-// by two bulk copies (cp.async.bulk: the panel bytes and the chunk's column
-// index list) counted on the stage's mbarrier.  While chunk c is computed,
-// the coefficients of chunk c+1 (phase-1 sums or x, gathered through its
-// column indices) are already loading into registers.  Lane -> (row = lane %
-// h, slice = lane / h); coefficients are broadcast by shuffles; the slices
-// are summed in a fixed order at the end of a row chunk and each z row is
-// written once.  No atomics on data: repeated products are bitwise equal.
+// Warp-specialised CTAs: a producer warp claims units through a global
+// ticket (uneven units balance themselves), hands their row chunks to its
+// consumer warps as they become free, and issues every chunk as two bulk
+// copies (cp.async.bulk: the panel bytes and the chunk's column index list)
+// into the consumer's ring of three shared-memory stages, counted on the
+// stage's full mbarrier.  Consumers keep no bookkeeping: wait, gather the
+// coefficients of the next chunk (phase-1 sums or x, through its column
+// indices) while computing the current one, release the stage on its empty
+// mbarrier.  Lane -> (row = lane % h, slice = lane / h); coefficients are
+// broadcast by shuffles or staged in shared memory in the data's lane order;
+// the slices are summed in a fixed order at the end of a row chunk and each
+// z row is written once.  No atomics on data: repeated products are bitwise
+// equal.
 //
 // Every wait is bounded (about 2 s of SM clocks); on expiry the warp records
-// a status, waits (again bounded) for the copies it issued and stops.
+// a status and stops, and the producer waits (again bounded) for the copies
+// it issued before the CTA ends.
 #include "df64.cuh"
 #include "kernels.hpp"
 
@@ -34,6 +37,24 @@ constexpr int kStages    = 3;  // per warp
 constexpr int kDataBuf   = kStreamStage + 32;
 constexpr int kIdxBuf    = kStreamCols * 4 + 32;
 constexpr long long kWaitCycles = 4000000000ll;
+
+// floor(t / d) for 0 <= t < 128 and 1 <= d <= 32 as (t * r_d) >> 16 with
+// r_d = floor(65536 / d) + 1: the product overshoots t / d by less than
+// 128 / 65536, below the 1 / d gap to the next integer.  Row, slice and
+// lane-order positions of a chunk are computed per chunk, and a division by
+// a run-time divisor costs tens of instructions.
+struct RcpTable {
+    unsigned v[33];
+};
+constexpr RcpTable make_rcp() {
+    RcpTable t{};
+    for (int d = 1; d <= 32; d++)
+        t.v[d] = 65536u / (unsigned)d + 1u;
+    return t;
+}
+__constant__ RcpTable kRcp = make_rcp();
+
+__device__ __forceinline__ int div_small(int t, int d) { return (int)(((unsigned)t * kRcp.v[d]) >> 16); }
 
 __device__ __forceinline__ unsigned sa(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -107,91 +128,176 @@ struct Seq {
     int b0, e0, b1, e1;
 };
 
+// ---------------------------------------------------------------------------
+// phase 2, warp-specialised: one producer warp per CTA feeds kCons consumer
+// warps.  Each consumer owns a ring of kStages shared-memory stages (data,
+// column indices, descriptor; a full and an empty mbarrier each).  The
+// producer claims units of whole row chunks from a global ticket, hands row
+// chunks to consumers as they become free (lane w of the producer serves
+// consumer w, so all consumers are served by one instruction stream), keeps
+// every consumer's next descriptor prefetched in registers and issues the
+// bulk copies; after the last chunk it posts a stop descriptor.  A consumer
+// only waits for its stage, gathers the coefficients of the chunk after the
+// current one, computes, writes z at the end of each row chunk and releases
+// the stage.
 template <int MU>
-struct P2Smem { // per warp: data stages, column-index stages, descriptors, barriers, coefficients
-    static constexpr int kIdx   = kStages * kDataBuf;
-    static constexpr int kDesc  = kIdx + kStages * kIdxBuf;
-    static constexpr int kBar   = kDesc + kStages * (int)sizeof(StreamChunk);
-    static constexpr int kCoef  = (kBar + kStages * 8 + 15) & ~15;
-    static constexpr int kTotal = (kCoef + 128 * MU * 4 + 127) & ~127;
+struct WsCfg {
+    static constexpr int kCons = MU >= 8 ? 4 : MU >= 4 ? 6 : MU >= 2 ? 7 : 8; // two CTAs per SM
 };
 
 template <int MU>
-__global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
-    phase2_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena0,
-                       const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
-                       const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen, int *__restrict__ status) {
-    using L = P2Smem<MU>;
+struct WsSmem { // per consumer
+    static constexpr int kIdx   = kStages * kDataBuf;
+    static constexpr int kDesc  = kIdx + kStages * kIdxBuf;
+    static constexpr int kFull  = kDesc + kStages * 48;
+    static constexpr int kEmpty = kFull + kStages * 8;
+    static constexpr int kCoef  = (kEmpty + kStages * 8 + 15) & ~15;
+    static constexpr int kTotal = (kCoef + 128 * MU * 4 + 127) & ~127;
+};
+
+constexpr unsigned char kStreamStop = 0xFF; // descriptor kind: no more chunks
+
+// non-blocking: has the phase of parity `parity` completed
+__device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(sa(b)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(sa(b)) : "memory");
+}
+
+// one thread waits (bounded) for a phase
+__device__ __forceinline__ bool lane_wait(unsigned long long *b, unsigned parity) {
+    if (mbar_sleep(b, parity, 20000))
+        return true;
+    const long long t0 = clock64();
+    while (!mbar_sleep(b, parity, 20000))
+        if (clock64() - t0 > kWaitCycles)
+            return false;
+    return true;
+}
+
+template <int MU>
+__global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), 2)
+    phase2_ws_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ units, int nunits, const int *__restrict__ rcs, int *__restrict__ ticket,
+                     const unsigned char *__restrict__ arena0, const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A,
+                     const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen,
+                     int *__restrict__ status) {
+    constexpr int kCons = WsCfg<MU>::kCons;
+    using L             = WsSmem<MU>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *wbase    = smem + (size_t)wid * L::kTotal;
-    unsigned char *dbuf     = wbase;                                  // kStages x kDataBuf
-    int *ibuf               = reinterpret_cast<int *>(wbase + L::kIdx); // kStages x kIdxBuf bytes
-    StreamChunk *desc       = reinterpret_cast<StreamChunk *>(wbase + L::kDesc);
-    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + L::kBar);
-    float *cf               = reinterpret_cast<float *>(wbase + L::kCoef); // MU x 128: FP32 / BF16 chunk coefficients in lane order
-    const int xe            = max(*xexp, 1);
-    if (lane == 0)
-        for (int s = 0; s < kStages; s++)
-            mbar_init(&bar[s], 1);
+    auto ring     = [&](int w) { return smem + (size_t)w * L::kTotal; };
+    auto fullb    = [&](int w, int s) { return reinterpret_cast<unsigned long long *>(ring(w) + L::kFull) + s; };
+    auto emptyb   = [&](int w, int s) { return reinterpret_cast<unsigned long long *>(ring(w) + L::kEmpty) + s; };
+    auto sdesc    = [&](int w, int s) { return reinterpret_cast<StreamChunk *>(ring(w) + L::kDesc + 48 * s); };
+    if (threadIdx.x < kCons * kStages) {
+        mbar_init(fullb(threadIdx.x / kStages, threadIdx.x % kStages), 1);
+        mbar_init(emptyb(threadIdx.x / kStages, threadIdx.x % kStages), 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncwarp();
+    __syncthreads();
 
-    auto claim = [&](int &b, int &e) {
-        const int r = warp_ticket(ticket);
-        if (r < nranges) {
-            b = rbeg[r];
-            e = rbeg[r + 1];
-        } else {
-            b = e = 0;
-        }
-    };
-    Seq q;
-    claim(q.b0, q.e0);
-    claim(q.b1, q.e1);
-    // issue position: chunk index ip in range `iw` (0 current, 1 next)
-    int ip = q.b0, iw = 0;
-    int issued = 0, done = 0;
-    // the descriptor of the chunk issued next is loaded one issue ahead
-    StreamChunk pf;
-    int pf_ip = -1;
-    auto issue_more = [&]() {
-        while (issued - done < kStages) {
-            if (iw == 0 && ip >= q.e0) {
-                ip = q.b1;
-                iw = 1;
+    if (wid == kCons) {
+        // ---------------- producer: lane w < kCons serves consumer w
+        const bool mine = lane < kCons;
+        int k = 0, e = 0; // chunks [k, e) of consumer w's row chunk still to issue
+        int iss   = 0;    // stages filled for consumer w (stop included)
+        bool fin  = !mine, stop = false;
+        StreamChunk dn{};   // descriptor of chunk k
+        int rb = 0, re = 0, rnext = 0, win = 0; // claimed row chunks [rb, re); lane j: start of row chunk rb + j
+        bool more = true;
+        auto claim_unit = [&]() {
+            int u = 0;
+            if (lane == 0)
+                u = atomicAdd(ticket, 1);
+            u = __shfl_sync(0xffffffffu, u, 0);
+            if (u >= nunits)
+                return false;
+            rb    = units[u];
+            re    = units[u + 1]; // re - rb <= 31
+            win   = rcs[min(rb + lane, re)];
+            rnext = rb;
+            return true;
+        };
+        more                           = claim_unit();
+        const unsigned long long pol   = evict_first_policy();
+        long long idle0                = clock64();
+        bool timed_out                 = false;
+        while (__any_sync(0xffffffffu, !fin)) {
+            // consumers between row chunks take the next row chunks in lane order
+            unsigned need = __ballot_sync(0xffffffffu, !fin && !stop && k >= e);
+            while (need) {
+                const int v = __ffs(need) - 1;
+                need &= need - 1;
+                if (more && rnext >= re)
+                    more = claim_unit();
+                if (more) {
+                    const int s0 = __shfl_sync(0xffffffffu, win, rnext - rb), s1 = __shfl_sync(0xffffffffu, win, rnext + 1 - rb);
+                    if (lane == v) {
+                        k  = s0;
+                        e  = s1;
+                        dn = chunks[k];
+                    }
+                    rnext++;
+                } else if (lane == v)
+                    stop = true;
             }
-            if (iw == 1 && ip >= q.e1)
-                return;
-            const int s         = issued % kStages;
-            const StreamChunk c = ip == pf_ip ? pf : chunks[ip];
-            {
-                const int k2 = (iw == 0 && ip + 1 >= q.e0) ? q.b1 : ip + 1;
-                const int e2 = (iw == 0 && ip + 1 < q.e0) ? q.e0 : q.e1;
-                if (k2 < e2) {
-                    pf    = chunks[k2];
-                    pf_ip = k2;
+            bool ready = false;
+            if (!fin) {
+                const int s = iss % kStages;
+                ready       = iss < kStages || mbar_test(emptyb(lane, s), ((iss / kStages) & 1) ^ 1);
+                if (ready) {
+                    StreamChunk *d = sdesc(lane, s);
+                    if (stop) {
+                        d->kind = kStreamStop;
+                        mbar_arrive(fullb(lane, s));
+                        fin = true;
+                    } else {
+                        *d                        = dn;
+                        const unsigned char *base = (dn.flags & kStreamArena1) ? arena1 : arena0;
+                        const long long a0 = dn.src & ~15LL, a1 = (dn.src + dn.bytes + 15) & ~15LL;
+                        const long long i0 = (4LL * dn.a) & ~15LL, i1 = (4LL * (dn.a + dn.ncol) + 15) & ~15LL;
+                        mbar_arrive_tx(fullb(lane, s), (unsigned)(a1 - a0 + i1 - i0));
+                        bulk_load_stream(ring(lane) + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), fullb(lane, s), pol);
+                        bulk_load_stream(ring(lane) + L::kIdx + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), fullb(lane, s), pol);
+                        if (++k < e)
+                            dn = chunks[k];
+                    }
+                    iss++;
                 }
             }
-            if (lane == 0) {
-                desc[s]                   = c;
-                const unsigned char *base = (c.flags & kStreamArena1) ? arena1 : arena0;
-                const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
-                const long long i0 = (4LL * c.a) & ~15LL, i1 = (4LL * (c.a + c.ncol) + 15) & ~15LL;
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0 + i1 - i0));
-                bulk_load_stream(dbuf + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), &bar[s], evict_first_policy());
-                bulk_load_stream(reinterpret_cast<unsigned char *>(ibuf) + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), &bar[s], evict_first_policy());
+            if (__any_sync(0xffffffffu, ready))
+                idle0 = clock64();
+            else {
+                if (__any_sync(0xffffffffu, clock64() - idle0 > kWaitCycles)) { // no consumer released a stage for ~2 s
+                    timed_out = true;
+                    break;
+                }
+                __nanosleep(32);
             }
-            issued++;
-            ip++;
         }
-    };
+        if (timed_out && lane == 0)
+            atomicExch(status, 3);
+        // copies still in flight (none on the normal path) land before the CTA ends
+        if (mine)
+            for (int j = 1; j <= min(iss, kStages); j++)
+                if (!lane_wait(fullb(lane, (iss - j) % kStages), ((iss - j) / kStages) & 1))
+                    atomicExch(status, 3);
+        return;
+    }
+
+    // ---------------- consumers
+    unsigned char *wbase = ring(wid);
+    float *cf            = reinterpret_cast<float *>(wbase + L::kCoef); // MU x 128: FP32 / BF16 chunk coefficients in lane order
+    const int xe         = max(*xexp, 1);
+
     // raw coefficients of a landed chunk into registers: column t = lane + 32 j
-    auto gather = [&](int s, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
-        const StreamChunk &c = desc[s];
-        const int *ix        = reinterpret_cast<const int *>(reinterpret_cast<const unsigned char *>(ibuf) + (size_t)s * kIdxBuf + ((4LL * c.a) & 15));
-        const bool emu       = c.kind == kStreamEmu;
+    auto gather = [&](int s, const StreamChunk &c, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
+        const int *ix  = reinterpret_cast<const int *>(wbase + L::kIdx + (size_t)s * kIdxBuf + ((4LL * c.a) & 15));
+        const bool emu = c.kind == kStreamEmu;
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             const int t = lane + 32 * j;
@@ -212,23 +318,23 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
             }
         }
     };
-
     // coefficients of an FP32 / BF16 chunk (in the units of x, as floats) in
     // the lane order of its data: column t = slice + S j sits at
     // ((j / V) S + slice) V + j % V, so a lane reads V of them at once
     auto stage_coefs = [&](const StreamChunk &c, const double (&r)[kStreamCols / 32][MU]) {
         if (c.kind != kStreamF32 && c.kind != kStreamBf16)
             return;
-        const int S = 32 / c.h, V = c.kind == kStreamF32 ? 4 : 8;
-        for (int i = lane; i < 128 * MU; i += 32)
-            cf[i] = 0.f;
+        const int S = div_small(32, c.h), lv = c.kind == kStreamF32 ? 2 : 3; // V = 1 << lv
+#pragma unroll
+        for (int i = 0; i < 4 * MU; i++)
+            cf[lane + 32 * i] = 0.f;
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             const int t = lane + 32 * j;
             if (t < c.ncol) {
-                const int jj = t / S, sl = t - jj * S;
-                const int pos = ((jj / V) * S + sl) * V + jj % V;
+                const int jj = div_small(t, S), sl = t - jj * S;
+                const int pos = ((((jj >> lv) * S + sl) << lv) | (jj & ((1 << lv) - 1)));
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
                     cf[cc * 128 + pos] = (float)scale_pow2_safe(r[j][cc], 1023 - xe);
@@ -246,34 +352,30 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
     }
     double raw[kStreamCols / 32][MU], rnx[kStreamCols / 32][MU];
     int kk[kStreamCols / 32], knx[kStreamCols / 32];
-    bool ok = true, have = false, have_nx = false; // coefficients of chunk `done` / `done + 1` loaded
-    int left0 = q.e0 - q.b0;                       // chunks of the current range not yet computed
-    issue_more();
-    while (done < issued) {
-        const int s = done % kStages;
-        if (!have) {
-            if (!warp_wait(&bar[s], (done / kStages) & 1)) {
-                ok = false;
-                break;
-            }
-            gather(s, raw, kk);
-            stage_coefs(desc[s], raw);
+    int s = 0;
+    unsigned par = 0;
+    bool ok = true;
+    if (!warp_wait(fullb(wid, 0), 0))
+        ok = false;
+    StreamChunk c = *sdesc(wid, 0);
+    if (ok && c.kind != kStreamStop) {
+        gather(0, c, raw, kk);
+        stage_coefs(c, raw);
+    }
+    while (ok && c.kind != kStreamStop) {
+        const int s1          = s + 1 == kStages ? 0 : s + 1;
+        const unsigned par1   = s + 1 == kStages ? par ^ 1 : par;
+        // the next chunk: when it has landed already, start its coefficients now
+        bool have_nx = __all_sync(0xffffffffu, mbar_test(fullb(wid, s1), par1));
+        StreamChunk cn;
+        if (have_nx) {
+            cn = *sdesc(wid, s1);
+            if (cn.kind != kStreamStop)
+                gather(s1, cn, rnx, knx);
         }
-        // chunk done+1: wait for it (normally landed) and start its coefficients
-        have_nx = false;
-        if (done + 1 < issued) {
-            const int s1 = (done + 1) % kStages;
-            if (!warp_wait(&bar[s1], ((done + 1) / kStages) & 1)) {
-                ok = false;
-                break;
-            }
-            gather(s1, rnx, knx);
-            have_nx = true;
-        }
-        const StreamChunk c = desc[s];
-        const int h = c.h, S = 32 / h, row = lane % h, slice = lane / h;
+        const int h = c.h, S = div_small(32, h), slice = div_small(lane, h), row = lane - slice * h;
         const bool live          = slice < S;
-        const unsigned char *buf = dbuf + (size_t)s * kDataBuf + (c.src & 15);
+        const unsigned char *buf = wbase + (size_t)s * kDataBuf + (c.src & 15);
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             const int q0 = 32 * j;
@@ -325,8 +427,8 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
         if (c.kind == kStreamF32 || c.kind == kStreamBf16) {
             // lane order: 16 bytes of V elements per lane and group of V
             // columns, coefficients alongside in shared memory
-            const int V = c.kind == kStreamF32 ? 4 : 8;
-            const int Ln = S * h, J = (c.ncol + S - 1) / S, G = (J + V - 1) / V;
+            const int V = c.kind == kStreamF32 ? 4 : 8, lv = V == 4 ? 2 : 3;
+            const int Ln = S * h, J = div_small(c.ncol + S - 1, S), G = (J + V - 1) >> lv;
             float part[MU], part2[MU];
 #pragma unroll
             for (int cc = 0; cc < MU; cc++)
@@ -352,16 +454,16 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
                         const uint4 w = D[g * Ln];
 #pragma unroll
                         for (int cc = 0; cc < MU; cc++) {
-                            const float4 c0 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8);
-                            const float4 c1 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8 + 4);
-                            part[cc]        = fmaf(__uint_as_float(w.x << 16), c0.x, part[cc]);
-                            part2[cc]       = fmaf(__uint_as_float(w.x & 0xffff0000u), c0.y, part2[cc]);
-                            part[cc]        = fmaf(__uint_as_float(w.y << 16), c0.z, part[cc]);
-                            part2[cc]       = fmaf(__uint_as_float(w.y & 0xffff0000u), c0.w, part2[cc]);
-                            part[cc]        = fmaf(__uint_as_float(w.z << 16), c1.x, part[cc]);
-                            part2[cc]       = fmaf(__uint_as_float(w.z & 0xffff0000u), c1.y, part2[cc]);
-                            part[cc]        = fmaf(__uint_as_float(w.w << 16), c1.z, part[cc]);
-                            part2[cc]       = fmaf(__uint_as_float(w.w & 0xffff0000u), c1.w, part2[cc]);
+                            const float4 k0 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8);
+                            const float4 k1 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8 + 4);
+                            part[cc]        = fmaf(__uint_as_float(w.x << 16), k0.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.x & 0xffff0000u), k0.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.y << 16), k0.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.y & 0xffff0000u), k0.w, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.z << 16), k1.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.z & 0xffff0000u), k1.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.w << 16), k1.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.w & 0xffff0000u), k1.w, part2[cc]);
                         }
                     }
                 }
@@ -393,17 +495,23 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
                 df_zero(acc[cc]);
             }
         }
-        __syncwarp(); // every lane is done with stage s before it is refilled
-        done++;
-        if (--left0 == 0) { // the next range becomes current; claim another
-            if (iw == 0)
-                ip = q.b1;
-            iw   = 0;
-            q.b0 = q.b1;
-            q.e0 = q.e1;
-            left0 = q.e0 - q.b0;
-            claim(q.b1, q.e1);
+        __syncwarp(); // every lane is done with stage s: hand it back
+        if (lane == 0)
+            mbar_arrive(emptyb(wid, s));
+        if (!have_nx) { // the producer was behind: wait for the next chunk now
+            if (!warp_wait(fullb(wid, s1), par1)) {
+                ok = false;
+                break;
+            }
+            cn = *sdesc(wid, s1);
+            if (cn.kind != kStreamStop)
+                gather(s1, cn, rnx, knx);
         }
+        s   = s1;
+        par = par1;
+        c   = cn;
+        if (c.kind == kStreamStop)
+            break;
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             kk[j] = knx[j];
@@ -411,19 +519,10 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : 4)
             for (int cc = 0; cc < MU; cc++)
                 raw[j][cc] = rnx[j][cc];
         }
-        have = have_nx;
-        if (have) // the next chunk's coefficients, loaded during this one
-            stage_coefs(desc[done % kStages], raw);
-        issue_more();
+        stage_coefs(c, raw);
     }
-    if (!ok) {
-        if (lane == 0)
-            atomicExch(status, 2);
-        // the copies in flight must land before the warp leaves
-        for (int p = done; p < issued; p++)
-            if (!warp_wait(&bar[p % kStages], (p / kStages) & 1) && lane == 0)
-                atomicExch(status, 3);
-    }
+    if (!ok && lane == 0)
+        atomicExch(status, 2);
 }
 
 // ---------------------------------------------------------------------------
@@ -791,18 +890,23 @@ __global__ void __launch_bounds__(32 * kWarps, 3)
 }
 
 template <int MU>
-void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
-                    const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
+void launch_ws_mu(const StreamChunk *chunks, const int *units, int nunits, int *ticket, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+                  const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
+    constexpr int kCons            = WsCfg<MU>::kCons;
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
-    const int bytes                = kWarps * P2Smem<MU>::kTotal;
-    int dev                        = 0;
+    const int bytes                = kCons * WsSmem<MU>::kTotal;
+    int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
     if (dev >= 64 || !(done >> dev & 1)) {
-        HTGPU_CUDA(cudaFuncSetAttribute(phase2_warp_kernel<MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_ws_kernel<MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         if (dev < 64)
             done |= 1ull << dev;
     }
-    phase2_warp_kernel<MU><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // two CTAs per SM, at most one per unit: small products leave room for
+    // concurrent work
+    const int nctas = std::max(1, std::min(2 * std::max(sms, 1), nunits));
+    phase2_ws_kernel<MU><<<nctas, 32 * (kCons + 1), bytes, st>>>(chunks, units, nunits, units + nunits + 1, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
@@ -912,14 +1016,11 @@ void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen
     }
 }
 
-void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+void launch_phase2_stream(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
                           const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
-    if (nranges <= 0)
+    if (nunits <= 0)
         return;
     HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
-    // as many warps as ranges, at most every resident CTA: small products
-    // leave room for concurrent work
-    const int nctas = std::max(1, std::min(stream_ctas(), (nranges + kWarps - 1) / kWarps));
     int c0 = 0, g = 0;
     while (c0 < mu) {
         const int left = mu - c0;
@@ -928,14 +1029,58 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
         if (g >= 7 && c0 > 0)
             HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
         switch (n) {
-        case 8: launch_warp_mu<8>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 4: launch_warp_mu<4>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 2: launch_warp_mu<2>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        default: launch_warp_mu<1>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 8: launch_ws_mu<8>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 4: launch_ws_mu<4>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 2: launch_ws_mu<2>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        default: launch_ws_mu<1>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
         }
         c0 += n;
         g++;
     }
+}
+
+std::vector<int> stream_units(const std::vector<StreamChunk> &ch, int target_units, int *nunits) {
+    // row chunks (first .. last flag) and their cost ~ time: DFMA chunks run
+    // on the FP64 pipe, slower per byte than the other kinds; every chunk has
+    // a fixed overhead
+    std::vector<int> rcs;
+    std::vector<double> cost;
+    for (std::size_t k = 0; k < ch.size(); k++) {
+        if ((ch[k].flags & kStreamFirst) || rcs.empty()) {
+            rcs.push_back((int)k);
+            cost.push_back(0.);
+        }
+        cost.back() += ch[k].bytes * (ch[k].kind == kStreamDfma ? 2.0 : 1.0) + 256.0;
+    }
+    rcs.push_back((int)ch.size());
+    const int nrc = (int)cost.size();
+    double total  = 0;
+    for (double c : cost)
+        total += c;
+    const double target = total / std::max(target_units, 1);
+    std::vector<int> u{0};
+    double acc = 0;
+    for (int i = 0; i < nrc; i++) {
+        acc += cost[i];
+        if (i + 1 < nrc && (acc >= target || i + 1 - u.back() >= kUnitRowChunks)) {
+            u.push_back(i + 1);
+            acc = 0;
+        }
+    }
+    if (nrc > 0)
+        u.push_back(nrc);
+    *nunits = (int)u.size() - 1;
+    // units (row-chunk indices), then the first chunk of every row chunk and the end
+    std::vector<int> out(u);
+    out.insert(out.end(), rcs.begin(), rcs.end());
+    return out;
+}
+
+int stream2_units_target() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return 2 * (sms > 0 ? sms : 152) * 6; // ~6 units per CTA: balance through the ticket
 }
 
 } // namespace htgpu

@@ -171,8 +171,12 @@ int htgpu_hmatrix_phase_bytes(htgpu_hmatrix h, int mu, long long *bytes);
 /* How the FP64 product shares its work between the FP64 pipe (DFMA) and the
  * FP32/INT pipes (exact double-float emulation, ~2^-46 relative per term):
  * phase1_dfma_permille of the low-rank V-side elements and
- * phase2_dfma_permille of the U-side/dense elements use DFMA.  No counterpart in
- * the reference (its BLAS calls decide this, include/htool/types/matrix.hpp:320-383). */
+ * phase2_dfma_permille of the U-side/dense elements use DFMA.  With a reduced
+ * precision set (htgpu_hmatrix_set_precision), the call sets and reads the split
+ * of that product's dense blocks, which stay FP64 (phase2_dfma_permille; the
+ * phase-1 share is kept for the FP64 product).  Each precision keeps its own
+ * split.  No counterpart in the reference (its BLAS calls decide this,
+ * include/htool/types/matrix.hpp:320-383). */
 int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int phase1_dfma_permille, int phase2_dfma_permille);
 int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int *phase2_dfma_permille);
 
