@@ -731,14 +731,13 @@ void HMatrix::upload_phase1_lists() {
             const LrLeaf &L = lr_h[it.leaf];
             p1_bytes_ += 8LL * it.jlen * L.r;
             const int slot  = (int)(L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r);
-            tile_section(ch, 8 * it.off, 8, it.jlen, 0, L.r, slot, L.oj + it.j0, (int)L.a_off, (it.chunk & kEmuBit) ? kStreamEmu : kStreamDfma, true);
+            tile_section(ch, 8 * it.off, 8, it.jlen, it.jlen, 0, L.r, slot, L.oj + it.j0, (int)L.a_off, (it.chunk & kEmuBit) ? kStreamEmu : kStreamDfma, true);
         }
-        const std::vector<int> r = stream_ranges(ch, stream_ctas() * kStreamWarpsPerCta * 8);
-        n_p1_ranges_             = (int)r.size() - 1;
-        p1r_d.upload(r, stream_);
+        const std::vector<P1Stage> st = pack_stages(ch);
+        n_p1_ranges_                  = (int)st.size();
+        p1r_d.upload(st, stream_);
+        ch.push_back(StreamChunk{}); // stage copies read chunk descriptors in whole 16-byte words
         p1c_d.upload(ch, stream_);
-        if (ch.empty())
-            p1c_d.alloc(1);
     }
     const double target = emu_ok_ ? p2_n64_ / 1000.0 : 1.0;
     long long seen = 0, dfma = 0;
@@ -764,11 +763,12 @@ void HMatrix::upload_phase1_lists() {
         p2_bytes_ += 8LL * pi.h * pi.ncol;
         n_cols_ += pi.ncol;
     }
-    n_sctas_  = stream2_units_target();
+    n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
     n_chunks_ = (long long)ch.size();
     {
-        const std::vector<int> u = stream_units(ch, n_sctas_, &n_ranges_);
-        sr_d.upload(u, stream_);
+        const std::vector<int> r = stream_ranges(ch, n_sctas_);
+        n_ranges_                = (int)r.size() - 1;
+        sr_d.upload(r, stream_);
     }
     sc_d.upload(ch, stream_);
     if (ch.empty())
@@ -813,8 +813,9 @@ void HMatrix::upload_mixed_phase2() {
     scm_d.upload(ch2_h_, stream_);
     if (ch2_h_.empty())
         scm_d.alloc(1);
-    const std::vector<int> u = stream_units(ch2_h_, n_sctas_, &n_ranges_m_);
-    srm_d.upload(u, stream_);
+    const std::vector<int> r = stream_ranges(ch2_h_, n_sctas_);
+    n_ranges_m_              = (int)r.size() - 1;
+    srm_d.upload(r, stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -917,8 +918,8 @@ void HMatrix::set_precision(int policy, double tau) {
         m.off           = off;
         m.pad           = c32[it.leaf];
         p1m.push_back(m);
-        conv.push_back({it.off, off, off + 4LL * it.jlen * c32[it.leaf], it.jlen, L.r, c32[it.leaf], (int)(a_slots + L.a_off)});
-        off += al16(4LL * it.jlen * c32[it.leaf] + 2LL * it.jlen * (L.r - c32[it.leaf]));
+        conv.push_back({it.off, off, off + 4LL * ld_f32(it.jlen) * c32[it.leaf], it.jlen, L.r, c32[it.leaf], (int)(a_slots + L.a_off)});
+        off += al16(4LL * ld_f32(it.jlen) * c32[it.leaf] + 2LL * ld_bf16(it.jlen) * (L.r - c32[it.leaf]));
     }
     // phase 2 per row chunk: the dense leaves' FP64 columns are read in place
     // from the FP64 arena; the FP32 and the BF16 columns of all its low-rank
@@ -1002,17 +1003,16 @@ void HMatrix::set_precision(int policy, double tau) {
             const int slot  = (int)(L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r);
             const int c     = m.pad;
             if (c > 0)
-                tile_section(ch, m.off, 4, m.jlen, 0, c, slot, L.oj + m.j0, (int)L.a_off, kStreamF32, true);
+                tile_section(ch, m.off, 4, m.jlen, ld_f32(m.jlen), 0, c, slot, L.oj + m.j0, (int)L.a_off, kStreamF32, true);
             if (L.r > c)
-                tile_section(ch, m.off + 4LL * m.jlen * c, 2, m.jlen, c, L.r - c, slot, L.oj + m.j0, (int)L.a_off, kStreamBf16, c == 0);
+                tile_section(ch, m.off + 4LL * ld_f32(m.jlen) * c, 2, m.jlen, ld_bf16(m.jlen), c, L.r - c, slot, L.oj + m.j0, (int)L.a_off, kStreamBf16, c == 0);
             p1_bytes_m_ += 4LL * m.jlen * c + 2LL * m.jlen * (L.r - c);
         }
-        const std::vector<int> r = stream_ranges(ch, stream_ctas() * kStreamWarpsPerCta * 8);
-        n_p1m_ranges_            = (int)r.size() - 1;
-        p1rm_d.upload(r, stream_);
+        const std::vector<P1Stage> st = pack_stages(ch);
+        n_p1m_ranges_                 = (int)st.size();
+        p1rm_d.upload(st, stream_);
+        ch.push_back(StreamChunk{}); // stage copies read chunk descriptors in whole 16-byte words
         p1cm_d.upload(ch, stream_);
-        if (ch.empty())
-            p1cm_d.alloc(1);
     }
     p1m_d.upload(p1m, stream_);
     n_p1m_ = (int)p1m.size();
@@ -1050,7 +1050,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         HTGPU_CUDA(cudaEventRecord(marks[0], st));
     if (precision_ != 0) {
         if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
-            launch_phase1_stream(p1cm_d.p, p1rm_d.p, n_p1m_ranges_, tickets_d.p + 8, mix_.p, w_xp, w_xs, scale_d.p, w_xexp, mu, w_A, status_d.p, st);
+            launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, mix_.p, w_xp, w_xs, scale_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
         } else if (n_p1m_) {
             launch_phase1_mixed(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, w_xexp, mu, w_A, st);
@@ -1071,7 +1071,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         return;
     }
     if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
-        launch_phase1_stream(p1c_d.p, p1r_d.p, n_p1_ranges_, tickets_d.p + 8, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
+        launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
         launches_ += 1;
     } else if (n_p1_dfma_ && n_p1_emu_) {
         HTGPU_CUDA(cudaEventRecord(fork_, st));

@@ -203,8 +203,8 @@ class HMatrix {
     // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced
     // storage), phase-2 columns, z values read by the final sums
     long long p1_bytes_ = 0, p2_bytes_ = 0, n_cols_ = 0, p1_bytes_m_ = 0, p2_bytes_m_ = 0, n_cols_m_ = 0, zsum_reads_ = 0;
-    DevBuf<StreamChunk> p1c_d, p1cm_d; // streamed phase 1 (one or two right-hand sides)
-    DevBuf<int> p1r_d, p1rm_d;
+    DevBuf<StreamChunk> p1c_d, p1cm_d; // streamed phase 1 (one or two right-hand sides): chunks
+    DevBuf<P1Stage> p1r_d, p1rm_d;     // and their stages
     int n_p1_ranges_ = 0, n_p1m_ranges_ = 0;
     int mu_cap = 0;
     int launches_ = 0;

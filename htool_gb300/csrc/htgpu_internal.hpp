@@ -125,6 +125,15 @@ struct StreamChunk {
     unsigned short pad;
 };
 
+// Streamed phase 1: consecutive phase-1 chunks packed into one bulk copy of
+// `bytes` (a multiple of 16) from arena offset a0 (16-byte aligned); its
+// chunk descriptors are item0 .. item0 + nitems
+struct P1Stage {
+    long long a0;
+    int bytes, item0, nitems, pad;
+};
+constexpr int kP1Chunk = 8192; // bytes of one streamed phase-1 chunk at most
+
 struct ZItem { // cluster rows row0 .. row0+h: y[perm[i]] = sum over l of z[i + zl[l]], l in [lbeg, lend)
     int row0, h, lbeg, lend;
 };

@@ -56,32 +56,38 @@ void launch_block_copy(const BlockCopy *items, int nitems, const double *src, do
 void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st);
 
 // ---- streamed phase 2 (stream.cu) ------------------------------------------
-// one producer warp per CTA claims units of row chunks through tickets (8
-// ints, reset by the launch) and feeds its consumer warps; units as built by
-// stream_units (nunits + 1 unit bounds in row chunks, then the first chunk
-// of every row chunk and the end); chunk bytes at arena0 (or arena1 with
-// kStreamArena1); status: nonzero after a wait ran out
-constexpr int kStreamWarpsPerCta = 4; // streamed phase 1
-constexpr int kUnitRowChunks     = 31; // row chunks per unit at most
-int stream_ctas(); // streamed phase 1: CTAs per launch (all resident)
-void launch_phase2_stream(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+// warps claim the chunk ranges rbeg[r] .. rbeg[r+1] (r < nranges) through
+// tickets (8 ints, reset by the launch); chunk bytes at arena0 (or arena1
+// with kStreamArena1); status: nonzero after a wait ran out
+constexpr int kStreamWarpsPerCta = 4;
+int stream_ctas(); // CTAs per launch (all resident)
+void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
                           const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
-// about `target` units over a phase-2 chunk list, balanced by cost, each at
-// most kUnitRowChunks row chunks; returns units then row-chunk starts
-std::vector<int> stream_units(const std::vector<StreamChunk> &chunks, int target, int *nunits);
-int stream2_units_target(); // units for a product launch on this device
-// phase 1 with one or two right-hand sides: tile chunks (kStreamFirst on a
-// tile's first chunk), A slots written directly (tiles of multi-tile leaves
-// still need launch_reduce_tiles); scale: per-column factors (F32/BF16 kinds)
-void launch_phase1_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+// phase 1 with one or two right-hand sides from stages of tile chunks
+// (kStreamFirst on a tile's first chunk), A slots written directly (tiles of
+// multi-tile leaves still need launch_reduce_tiles); scale: per-column
+// factors (F32/BF16 kinds); the chunk array is padded by 16 bytes
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
                           const int *xexp, int mu, double *A, int *status, cudaStream_t st);
-// append the chunks of columns k0 .. k0+n of one tile (jlen rows, elements
-// of es bytes; column k0 at byte src): A slots slot + k, scale slots sidx + k
-void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile);
+// stages over a phase-1 chunk list in arena order
+std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &chunks);
+// append the chunks of columns k0 .. k0+n of one tile (jlen rows stored with
+// column stride ld, elements of es bytes; column k0 at byte src): A slots
+// slot + k, scale slots sidx + k
+void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int ld, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile);
+// column stride (rows) of the reduced-precision phase-1 tiles: whole 16-byte
+// words per column, zero rows past the tile
+#ifdef __CUDACC__
+#define HTGPU_HD __host__ __device__
+#else
+#define HTGPU_HD
+#endif
+HTGPU_HD inline int ld_f32(int jlen) { return (jlen + 3) & ~3; }
+HTGPU_HD inline int ld_bf16(int jlen) { return (jlen + 7) & ~7; }
 // append the chunks of one panel section (h x n elements of es bytes at byte src)
 void stream_section(std::vector<StreamChunk> &out, long long src, int es, int h, int n, int q0, int row0, unsigned char kind, unsigned char flags);
-// about nranges ranges over a streamed phase-1 chunk list (tiles kept
-// whole, none empty), balanced by cost; returns their nranges' + 1 bounds
+// about nranges ranges over a chunk list (row chunks or tiles kept whole,
+// none empty), balanced by cost; returns their nranges' + 1 bounds
 std::vector<int> stream_ranges(const std::vector<StreamChunk> &chunks, int nranges);
 
 // ---- mixed precision (mixed.cu) --------------------------------------------
@@ -89,8 +95,8 @@ struct ColMaxJob { // FP64 block rows x cols (ld rows) at off: column maxima -> 
     long long off;
     int rows, cols, slot, pad;
 };
-struct ConvertJob { // FP64 block at src (elements) -> FP32 columns at dst32, BF16 columns at dst16 (bytes)
-    long long src, dst32, dst16;
+struct ConvertJob { // FP64 block at src (elements) -> FP32 columns at dst32, BF16 columns at dst16 (bytes),
+    long long src, dst32, dst16; // column strides ld_f32(rows) / ld_bf16(rows), zero-padded
     int rows, cols, c32, slot;
 };
 // one phase-2 chunk of FP32 (es 4) or BF16 (es 2) columns in the lane

@@ -39,19 +39,24 @@ __global__ void colmax_kernel(const ColMaxJob *__restrict__ jobs, const double *
 // columns [c32, cols), each divided by its column maximum
 __global__ void convert_kernel(const ConvertJob *__restrict__ jobs, const double *__restrict__ fac, const unsigned *__restrict__ cmax, unsigned char *__restrict__ mix) {
     const ConvertJob J = jobs[blockIdx.x];
-    const long long n  = (long long)J.rows * J.cols;
-    float *f32         = reinterpret_cast<float *>(mix + J.dst32);
-    __nv_bfloat16 *b16 = reinterpret_cast<__nv_bfloat16 *>(mix + J.dst16);
+    const int l32 = ld_f32(J.rows), l16 = ld_bf16(J.rows);
+    const long long n32 = (long long)l32 * J.c32, n = n32 + (long long)l16 * (J.cols - J.c32);
+    float *f32          = reinterpret_cast<float *>(mix + J.dst32);
+    __nv_bfloat16 *b16  = reinterpret_cast<__nv_bfloat16 *>(mix + J.dst16);
     for (long long e = threadIdx.x; e < n; e += blockDim.x) {
-        const int k     = (int)(e / J.rows);
-        const int i     = (int)(e % J.rows);
-        const float mx  = __uint_as_float(cmax[J.slot + k]);
-        const double v  = fac[J.src + e];
-        const double nv = mx > 0.f ? v / (double)mx : 0.;
-        if (k < J.c32)
+        const bool is32 = e < n32;
+        const int k     = is32 ? (int)(e / l32) : J.c32 + (int)((e - n32) / l16);
+        const int i     = is32 ? (int)(e % l32) : (int)((e - n32) % l16);
+        double nv       = 0.; // zero rows past the tile
+        if (i < J.rows) {
+            const float mx = __uint_as_float(cmax[J.slot + k]);
+            const double v = fac[J.src + (long long)k * J.rows + i];
+            nv             = mx > 0.f ? v / (double)mx : 0.;
+        }
+        if (is32)
             f32[e] = (float)nv;
         else
-            b16[(long long)(k - J.c32) * J.rows + i] = __float2bfloat16_rn((float)nv);
+            b16[e - n32] = __float2bfloat16_rn((float)nv);
     }
 }
 
@@ -121,8 +126,9 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
         const LrLeaf L    = lr[it.leaf];
         const int c32     = it.pad;
         const int jlen    = it.jlen;
+        const int l32     = ld_f32(jlen), l16 = ld_bf16(jlen);
         const float *V32  = reinterpret_cast<const float *>(mix + it.off);
-        const unsigned short *V16 = reinterpret_cast<const unsigned short *>(mix + it.off + 4LL * jlen * c32);
+        const unsigned short *V16 = reinterpret_cast<const unsigned short *>(mix + it.off + 4LL * l32 * c32);
         const F2 *X       = xs + (long long)(L.oj + it.j0) * mu + c0;
         double *out       = A + (L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r) * mu + c0;
         float xv[RPL][MU];
@@ -153,14 +159,14 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
                     if (k < L.r) {
                         float v[RPL];
                         if (k < c32) {
-                            const float *Vk = V32 + (long long)jlen * k;
+                            const float *Vk = V32 + (long long)l32 * k;
 #pragma unroll
                             for (int t = 0; t < RPL; t++) {
                                 const int jj = s0 + lane + 32 * t;
                                 v[t]         = jj < jlen ? Vk[jj] : 0.f;
                             }
                         } else {
-                            const unsigned short *Vk = V16 + (long long)jlen * (k - c32);
+                            const unsigned short *Vk = V16 + (long long)l16 * (k - c32);
 #pragma unroll
                             for (int t = 0; t < RPL; t++) {
                                 const int jj = s0 + lane + 32 * t;
@@ -184,18 +190,6 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
             }
         }
     }
-}
-
-int sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0)
-            n = 152;
-    }
-    return n;
 }
 
 template <typename F>

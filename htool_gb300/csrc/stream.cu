@@ -64,6 +64,10 @@ __device__ __forceinline__ void mbar_arrive_tx(unsigned long long *b, unsigned t
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(sa(b)), "r"(tx) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(sa(b)) : "memory");
+}
+
 // true once the phase of parity `parity` has completed; a thread that finds
 // it incomplete sleeps until it completes or about `ns` nanoseconds pass
 __device__ __forceinline__ bool mbar_sleep(unsigned long long *b, unsigned parity, unsigned ns) {
@@ -115,47 +119,19 @@ __device__ __forceinline__ void df_addf(DF &a, float p) {
     a.c += err;
 }
 
-__device__ __forceinline__ int warp_ticket(int *ticket) {
-    int t = 0;
-    if ((threadIdx.x & 31) == 0)
-        t = atomicAdd(ticket, 1);
-    return __shfl_sync(0xffffffffu, t, 0);
-}
-
-// chunks of the ranges this warp claimed, in order: the current range
-// [b0, e0) and the next one [b1, e1) (empty when none is left)
-struct Seq {
-    int b0, e0, b1, e1;
-};
-
-// ---------------------------------------------------------------------------
-// phase 2, warp-specialised: one producer warp per CTA feeds kCons consumer
-// warps.  Each consumer owns a ring of kStages shared-memory stages (data,
-// column indices, descriptor; a full and an empty mbarrier each).  The
-// producer claims units of whole row chunks from a global ticket, hands row
-// chunks to consumers as they become free (lane w of the producer serves
-// consumer w, so all consumers are served by one instruction stream), keeps
-// every consumer's next descriptor prefetched in registers and issues the
-// bulk copies; after the last chunk it posts a stop descriptor.  A consumer
-// only waits for its stage, gathers the coefficients of the chunk after the
-// current one, computes, writes z at the end of each row chunk and releases
-// the stage.
 template <int MU>
-struct WsCfg {
-    static constexpr int kCons = MU >= 8 ? 4 : MU >= 4 ? 6 : MU >= 2 ? 7 : 8; // two CTAs per SM
-};
-
-template <int MU>
-struct WsSmem { // per consumer
+struct P2Smem { // per warp: data stages, column-index stages, descriptors, barriers, coefficients
     static constexpr int kIdx   = kStages * kDataBuf;
     static constexpr int kDesc  = kIdx + kStages * kIdxBuf;
-    static constexpr int kFull  = kDesc + kStages * 48;
-    static constexpr int kEmpty = kFull + kStages * 8;
-    static constexpr int kCoef  = (kEmpty + kStages * 8 + 15) & ~15;
+    static constexpr int kBar   = kDesc + kStages * 48;
+    static constexpr int kCoef  = (kBar + kStages * 8 + 15) & ~15;
     static constexpr int kTotal = (kCoef + 128 * MU * 4 + 127) & ~127;
 };
 
-constexpr unsigned char kStreamStop = 0xFF; // descriptor kind: no more chunks
+struct Window { // lane i: chunk i of the window (i < len)
+    StreamChunk d;
+    int len;
+};
 
 // non-blocking: has the phase of parity `parity` completed
 __device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
@@ -164,135 +140,95 @@ __device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity
     return ok != 0;
 }
 
-__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(sa(b)) : "memory");
-}
-
-// one thread waits (bounded) for a phase
-__device__ __forceinline__ bool lane_wait(unsigned long long *b, unsigned parity) {
-    if (mbar_sleep(b, parity, 20000))
-        return true;
-    const long long t0 = clock64();
-    while (!mbar_sleep(b, parity, 20000))
-        if (clock64() - t0 > kWaitCycles)
-            return false;
-    return true;
-}
-
 template <int MU>
-__global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), 2)
-    phase2_ws_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ units, int nunits, const int *__restrict__ rcs, int *__restrict__ ticket,
-                     const unsigned char *__restrict__ arena0, const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A,
-                     const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen,
-                     int *__restrict__ status) {
-    constexpr int kCons = WsCfg<MU>::kCons;
-    using L             = WsSmem<MU>;
+__global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
+    phase2_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena0,
+                       const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
+                       const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen, int *__restrict__ status) {
+    using L = P2Smem<MU>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    auto ring     = [&](int w) { return smem + (size_t)w * L::kTotal; };
-    auto fullb    = [&](int w, int s) { return reinterpret_cast<unsigned long long *>(ring(w) + L::kFull) + s; };
-    auto emptyb   = [&](int w, int s) { return reinterpret_cast<unsigned long long *>(ring(w) + L::kEmpty) + s; };
-    auto sdesc    = [&](int w, int s) { return reinterpret_cast<StreamChunk *>(ring(w) + L::kDesc + 48 * s); };
-    if (threadIdx.x < kCons * kStages) {
-        mbar_init(fullb(threadIdx.x / kStages, threadIdx.x % kStages), 1);
-        mbar_init(emptyb(threadIdx.x / kStages, threadIdx.x % kStages), 1);
-    }
+    unsigned char *wbase    = smem + (size_t)wid * L::kTotal;
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + L::kBar);
+    float *cf               = reinterpret_cast<float *>(wbase + L::kCoef); // MU x 128: FP32 / BF16 chunk coefficients in lane order
+    auto sdesc              = [&](int s) { return reinterpret_cast<StreamChunk *>(wbase + L::kDesc + 48 * s); };
+    const int xe            = max(*xexp, 1);
+    if (lane == 0)
+        for (int s = 0; s < kStages; s++)
+            mbar_init(&bar[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncthreads();
+    __syncwarp();
 
-    if (wid == kCons) {
-        // ---------------- producer: lane w < kCons serves consumer w
-        const bool mine = lane < kCons;
-        int k = 0, e = 0; // chunks [k, e) of consumer w's row chunk still to issue
-        int iss   = 0;    // stages filled for consumer w (stop included)
-        bool fin  = !mine, stop = false;
-        StreamChunk dn{};   // descriptor of chunk k
-        int rb = 0, re = 0, rnext = 0, win = 0; // claimed row chunks [rb, re); lane j: start of row chunk rb + j
-        bool more = true;
-        auto claim_unit = [&]() {
-            int u = 0;
+    // ---- ranges and windows
+    int tk = 0; // lane 0: the ticket after the next one (fetched, not yet used)
+    if (lane == 0)
+        tk = atomicAdd(ticket, 1);
+    int nb = -1, ne = -1; // bounds of the next range (-1: none)
+    {
+        const int t = __shfl_sync(0xffffffffu, tk, 0);
+        if (t < nranges) {
+            nb = rbeg[t];
+            ne = rbeg[t + 1];
             if (lane == 0)
-                u = atomicAdd(ticket, 1);
-            u = __shfl_sync(0xffffffffu, u, 0);
-            if (u >= nunits)
-                return false;
-            rb    = units[u];
-            re    = units[u + 1]; // re - rb <= 31
-            win   = rcs[min(rb + lane, re)];
-            rnext = rb;
-            return true;
-        };
-        more                           = claim_unit();
-        const unsigned long long pol   = evict_first_policy();
-        long long idle0                = clock64();
-        bool timed_out                 = false;
-        while (__any_sync(0xffffffffu, !fin)) {
-            // consumers between row chunks take the next row chunks in lane order
-            unsigned need = __ballot_sync(0xffffffffu, !fin && !stop && k >= e);
-            while (need) {
-                const int v = __ffs(need) - 1;
-                need &= need - 1;
-                if (more && rnext >= re)
-                    more = claim_unit();
-                if (more) {
-                    const int s0 = __shfl_sync(0xffffffffu, win, rnext - rb), s1 = __shfl_sync(0xffffffffu, win, rnext + 1 - rb);
-                    if (lane == v) {
-                        k  = s0;
-                        e  = s1;
-                        dn = chunks[k];
-                    }
-                    rnext++;
-                } else if (lane == v)
-                    stop = true;
-            }
-            bool ready = false;
-            if (!fin) {
-                const int s = iss % kStages;
-                ready       = iss < kStages || mbar_test(emptyb(lane, s), ((iss / kStages) & 1) ^ 1);
-                if (ready) {
-                    StreamChunk *d = sdesc(lane, s);
-                    if (stop) {
-                        d->kind = kStreamStop;
-                        mbar_arrive(fullb(lane, s));
-                        fin = true;
-                    } else {
-                        *d                        = dn;
-                        const unsigned char *base = (dn.flags & kStreamArena1) ? arena1 : arena0;
-                        const long long a0 = dn.src & ~15LL, a1 = (dn.src + dn.bytes + 15) & ~15LL;
-                        const long long i0 = (4LL * dn.a) & ~15LL, i1 = (4LL * (dn.a + dn.ncol) + 15) & ~15LL;
-                        mbar_arrive_tx(fullb(lane, s), (unsigned)(a1 - a0 + i1 - i0));
-                        bulk_load_stream(ring(lane) + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), fullb(lane, s), pol);
-                        bulk_load_stream(ring(lane) + L::kIdx + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), fullb(lane, s), pol);
-                        if (++k < e)
-                            dn = chunks[k];
-                    }
-                    iss++;
-                }
-            }
-            if (__any_sync(0xffffffffu, ready))
-                idle0 = clock64();
-            else {
-                if (__any_sync(0xffffffffu, clock64() - idle0 > kWaitCycles)) { // no consumer released a stage for ~2 s
-                    timed_out = true;
-                    break;
-                }
-                __nanosleep(32);
-            }
+                tk = atomicAdd(ticket, 1);
         }
-        if (timed_out && lane == 0)
-            atomicExch(status, 3);
-        // copies still in flight (none on the normal path) land before the CTA ends
-        if (mine)
-            for (int j = 1; j <= min(iss, kStages); j++)
-                if (!lane_wait(fullb(lane, (iss - j) % kStages), ((iss - j) / kStages) & 1))
-                    atomicExch(status, 3);
-        return;
     }
-
-    // ---------------- consumers
-    unsigned char *wbase = ring(wid);
-    float *cf            = reinterpret_cast<float *>(wbase + L::kCoef); // MU x 128: FP32 / BF16 chunk coefficients in lane order
-    const int xe         = max(*xexp, 1);
+    int rk = 0, re = 0; // chunks [rk, re) of the claimed range not yet in a window
+    auto claim = [&]() {
+        rk = nb;
+        re = ne;
+        if (rk < 0)
+            return false;
+        const int t = __shfl_sync(0xffffffffu, tk, 0);
+        if (t < nranges) {
+            nb = rbeg[t];
+            ne = rbeg[t + 1];
+            if (lane == 0)
+                tk = atomicAdd(ticket, 1);
+        } else
+            nb = ne = -1;
+        return true;
+    };
+    auto load_window = [&](Window &w) {
+        w.len = 0;
+        while (rk >= re)
+            if (!claim())
+                return;
+        w.len = min(32, re - rk);
+        if (lane < w.len)
+            w.d = chunks[rk + lane];
+        rk += w.len;
+    };
+    Window cur, nxt;
+    load_window(cur);
+    load_window(nxt);
+    int wpos = 0; // next chunk of `cur` to issue
+    int issued = 0, done = 0;
+    const unsigned long long pol = evict_first_policy();
+    auto issue_more = [&]() {
+        while (issued - done < kStages) {
+            if (wpos == cur.len) {
+                if (nxt.len == 0)
+                    return;
+                cur  = nxt;
+                wpos = 0;
+                load_window(nxt);
+            }
+            const int s = issued % kStages;
+            if (lane == wpos) {
+                const StreamChunk &c = cur.d;
+                *sdesc(s)            = c;
+                const unsigned char *base = (c.flags & kStreamArena1) ? arena1 : arena0;
+                const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
+                const long long i0 = (4LL * c.a) & ~15LL, i1 = (4LL * (c.a + c.ncol) + 15) & ~15LL;
+                mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0 + i1 - i0));
+                bulk_load_stream(wbase + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), &bar[s], pol);
+                bulk_load_stream(wbase + L::kIdx + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), &bar[s], pol);
+            }
+            issued++;
+            wpos++;
+        }
+    };
 
     // raw coefficients of a landed chunk into registers: column t = lane + 32 j
     auto gather = [&](int s, const StreamChunk &c, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
@@ -352,26 +288,28 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), 2)
     }
     double raw[kStreamCols / 32][MU], rnx[kStreamCols / 32][MU];
     int kk[kStreamCols / 32], knx[kStreamCols / 32];
-    int s = 0;
-    unsigned par = 0;
     bool ok = true;
-    if (!warp_wait(fullb(wid, 0), 0))
-        ok = false;
-    StreamChunk c = *sdesc(wid, 0);
-    if (ok && c.kind != kStreamStop) {
+    issue_more();
+    StreamChunk c;
+    if (done < issued) {
+        if (!warp_wait(&bar[0], 0))
+            ok = false;
+        c = *sdesc(0);
         gather(0, c, raw, kk);
         stage_coefs(c, raw);
     }
-    while (ok && c.kind != kStreamStop) {
-        const int s1          = s + 1 == kStages ? 0 : s + 1;
-        const unsigned par1   = s + 1 == kStages ? par ^ 1 : par;
+    int s = 0;
+    unsigned par = 0;
+    while (ok && done < issued) {
+        const int s1        = s + 1 == kStages ? 0 : s + 1;
+        const unsigned par1 = s + 1 == kStages ? par ^ 1 : par;
+        const bool more     = done + 1 < issued;
         // the next chunk: when it has landed already, start its coefficients now
-        bool have_nx = __all_sync(0xffffffffu, mbar_test(fullb(wid, s1), par1));
+        const bool have_nx = more && __all_sync(0xffffffffu, mbar_test(&bar[s1], par1));
         StreamChunk cn;
         if (have_nx) {
-            cn = *sdesc(wid, s1);
-            if (cn.kind != kStreamStop)
-                gather(s1, cn, rnx, knx);
+            cn = *sdesc(s1);
+            gather(s1, cn, rnx, knx);
         }
         const int h = c.h, S = div_small(32, h), slice = div_small(lane, h), row = lane - slice * h;
         const bool live          = slice < S;
@@ -495,23 +433,22 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), 2)
                 df_zero(acc[cc]);
             }
         }
-        __syncwarp(); // every lane is done with stage s: hand it back
-        if (lane == 0)
-            mbar_arrive(emptyb(wid, s));
-        if (!have_nx) { // the producer was behind: wait for the next chunk now
-            if (!warp_wait(fullb(wid, s1), par1)) {
+        __syncwarp(); // every lane is done with stage s before it is refilled
+        done++;
+        if (!more)
+            break;
+        if (!have_nx) { // not landed before the compute: wait now
+            if (!warp_wait(&bar[s1], par1)) {
                 ok = false;
                 break;
             }
-            cn = *sdesc(wid, s1);
-            if (cn.kind != kStreamStop)
-                gather(s1, cn, rnx, knx);
+            cn = *sdesc(s1);
+            gather(s1, cn, rnx, knx);
         }
+        issue_more(); // refills stage s
         s   = s1;
         par = par1;
         c   = cn;
-        if (c.kind == kStreamStop)
-            break;
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             kk[j] = knx[j];
@@ -521,8 +458,14 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), 2)
         }
         stage_coefs(c, raw);
     }
-    if (!ok && lane == 0)
-        atomicExch(status, 2);
+    if (!ok) {
+        if (lane == 0)
+            atomicExch(status, 2);
+        // the copies in flight must land before the warp leaves
+        for (int p = done; p < issued; p++)
+            if (!warp_wait(&bar[p % kStages], (p / kStages) & 1) && lane == 0)
+                atomicExch(status, 3);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -593,6 +536,11 @@ struct ShflDF {
     }
 };
 
+// the value index lane `lane` writes in reduce_out(.., nv, ..)
+__device__ __forceinline__ int rs_slot(int nv, int lane) {
+    return nv > 8 ? rs_index<16>(lane) : nv > 4 ? rs_index<8>(lane) : nv > 2 ? rs_index<4>(lane) : nv > 1 ? rs_index<2>(lane) : 0;
+}
+
 // sums of value n (n < nv) go to out(n, value) from one lane each
 template <typename T, typename Add, typename Shfl, typename Out>
 __device__ __forceinline__ void reduce_out(T (&v)[16], int nv, int lane, Add add, Shfl shfl, Out out) {
@@ -619,16 +567,19 @@ __device__ __forceinline__ void reduce_out(T (&v)[16], int nv, int lane, Add add
     }
 }
 
-// np (<= NP) columns p0 .. p0+np of a phase-1 chunk against the tile's x
-// rows (X: row-major, MU per row); sums to A (and the per-column scales)
-template <int NP, int MU>
-__device__ __forceinline__ void tile_group(const StreamChunk &c, const unsigned char *buf, const unsigned long long *X, int p0, int np, int lane, int shift, double *__restrict__ A,
-                                           const double *__restrict__ scale, int mu, int c0) {
+// np (<= NP) columns p0 .. p0+np of a phase-1 chunk of element kind KIND
+// against the tile's x rows (xw[t][cc]: row lane + 32 t, right-hand side
+// cc, as 64-bit words: FP64 bits for DFMA chunks, the F2 split otherwise;
+// zero past the tile); sums to A (and the per-column scales).  One kind per
+// instantiation keeps each consumer loop small in the instruction cache.
+template <int NP, int MU, int KIND>
+__device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned char *buf, const unsigned long long (&xw)[8][MU], int p0, int np, int lane, int shift, double *__restrict__ A,
+                                          const double *__restrict__ scale, int mu, int c0) {
     static_assert(NP * MU <= 16, "reduction group of at most 16 values");
     const int jlen  = c.h;
     const int base  = c.a + p0;
     const bool full = np == NP;
-    if (c.kind == kStreamDfma) {
+    if constexpr (KIND == kStreamDfma) {
         double acc[16];
 #pragma unroll
         for (int i = 0; i < 16; i++)
@@ -638,12 +589,11 @@ __device__ __forceinline__ void tile_group(const StreamChunk &c, const unsigned 
         for (int t = 0; t < 8; t++) {
             if (32 * t >= jlen) // warp-uniform
                 break;
-            const int row   = lane + 32 * t;
-            const bool live = row < jlen;
+            const bool live = lane + 32 * t < jlen;
             double xv[MU];
 #pragma unroll
             for (int cc = 0; cc < MU; cc++)
-                xv[cc] = live ? __longlong_as_double((long long)X[row * MU + cc]) : 0.;
+                xv[cc] = __longlong_as_double((long long)xw[t][cc]);
 #pragma unroll
             for (int p = 0; p < NP; p++) {
                 const double u = (live && (full || p < np)) ? V[jlen * p + 32 * t] : 0.;
@@ -653,7 +603,7 @@ __device__ __forceinline__ void tile_group(const StreamChunk &c, const unsigned 
             }
         }
         reduce_out(acc, np * MU, lane, AddD(), ShflD(), [&](int n, double v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = v; });
-    } else if (c.kind == kStreamEmu) {
+    } else if constexpr (KIND == kStreamEmu) {
         // two accumulator sets (even / odd row groups) for independent chains
         DF acc[16], acc2[16];
 #pragma unroll
@@ -666,14 +616,12 @@ __device__ __forceinline__ void tile_group(const StreamChunk &c, const unsigned 
         for (int t = 0; t < 8; t++) {
             if (32 * t >= jlen) // warp-uniform
                 break;
-            const int row   = lane + 32 * t;
-            const bool live = row < jlen;
+            const bool live = lane + 32 * t < jlen;
             F2 xv[MU];
 #pragma unroll
             for (int cc = 0; cc < MU; cc++) {
-                const unsigned long long bits = live ? X[row * MU + cc] : 0ull;
-                xv[cc].hi                     = __int_as_float((int)(bits & 0xffffffffull));
-                xv[cc].lo                     = __int_as_float((int)(bits >> 32));
+                xv[cc].hi = __int_as_float((int)(xw[t][cc] & 0xffffffffull));
+                xv[cc].lo = __int_as_float((int)(xw[t][cc] >> 32));
             }
 #pragma unroll
             for (int p = 0; p < NP; p++) {
@@ -691,222 +639,268 @@ __device__ __forceinline__ void tile_group(const StreamChunk &c, const unsigned 
         }
         reduce_out(acc, np * MU, lane, AddDF(), ShflDF(), [&](int n, DF v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe(df_to_double(v), shift); });
     } else {
+        // FP32 / BF16 columns with stride ld_f32 / ld_bf16 (whole 16-byte
+        // words, zero rows past the tile): lane l reads rows 4l.. (+128) or
+        // 8l.. as one 16-byte word, against the x rows xw[q] of the same
+        // mapping (row 4l + q % 4 + 128 (q / 4), or 8l + q)
         float acc[16];
 #pragma unroll
         for (int i = 0; i < 16; i++)
             acc[i] = 0.f;
-        const bool f32 = c.kind == kStreamF32;
+        // the scale of the column this lane writes, requested before the sums
+        const int mine  = rs_slot(np * MU, lane) / MU;
+        const double sc = mine < np ? __ldg(scale + c.c + p0 + mine) : 0.;
+        float xv[8][MU];
 #pragma unroll
-        for (int t = 0; t < 8; t++) {
-            if (32 * t >= jlen) // warp-uniform
-                break;
-            const int row   = lane + 32 * t;
-            const bool live = row < jlen;
-            float xv[MU];
+        for (int q = 0; q < 8; q++)
 #pragma unroll
             for (int cc = 0; cc < MU; cc++)
-                xv[cc] = live ? __int_as_float((int)(X[row * MU + cc] & 0xffffffffull)) : 0.f;
+                xv[q][cc] = __int_as_float((int)(xw[q][cc] & 0xffffffffull));
+        if constexpr (KIND == kStreamF32) {
+            const int ld4   = ld_f32(jlen) >> 2; // 16-byte words per column
+            const uint4 *V  = reinterpret_cast<const uint4 *>(buf) + (size_t)ld4 * p0 + lane;
+#pragma unroll
+            for (int t = 0; t < 2; t++) {
+                if (32 * t >= ld4) // warp-uniform
+                    break;
+                const bool live = lane + 32 * t < ld4;
+#pragma unroll
+                for (int p = 0; p < NP; p++) {
+                    const uint4 w = (live && (full || p < np)) ? V[ld4 * p + 32 * t] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                    for (int cc = 0; cc < MU; cc++) {
+                        float a = acc[p * MU + cc];
+                        a       = fmaf(__uint_as_float(w.x), xv[4 * t + 0][cc], a);
+                        a       = fmaf(__uint_as_float(w.y), xv[4 * t + 1][cc], a);
+                        a       = fmaf(__uint_as_float(w.z), xv[4 * t + 2][cc], a);
+                        a       = fmaf(__uint_as_float(w.w), xv[4 * t + 3][cc], a);
+                        acc[p * MU + cc] = a;
+                    }
+                }
+            }
+        } else {
+            const int ld8   = ld_bf16(jlen) >> 3; // 16-byte words per column
+            const uint4 *V  = reinterpret_cast<const uint4 *>(buf) + (size_t)ld8 * p0 + lane;
+            const bool live = lane < ld8;
 #pragma unroll
             for (int p = 0; p < NP; p++) {
-                float u = 0.f;
-                if (live && (full || p < np)) {
-                    const size_t e = (size_t)jlen * (p0 + p) + row;
-                    u              = f32 ? reinterpret_cast<const float *>(buf)[e] : bf16f(reinterpret_cast<const unsigned short *>(buf)[e]);
-                }
+                const uint4 w = (live && (full || p < np)) ? V[ld8 * p] : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-                for (int cc = 0; cc < MU; cc++)
-                    acc[p * MU + cc] = fmaf(u, xv[cc], acc[p * MU + cc]);
+                for (int cc = 0; cc < MU; cc++) {
+                    float a = acc[p * MU + cc];
+                    a       = fmaf(__uint_as_float(w.x << 16), xv[0][cc], a);
+                    a       = fmaf(__uint_as_float(w.x & 0xffff0000u), xv[1][cc], a);
+                    a       = fmaf(__uint_as_float(w.y << 16), xv[2][cc], a);
+                    a       = fmaf(__uint_as_float(w.y & 0xffff0000u), xv[3][cc], a);
+                    a       = fmaf(__uint_as_float(w.z << 16), xv[4][cc], a);
+                    a       = fmaf(__uint_as_float(w.z & 0xffff0000u), xv[5][cc], a);
+                    a       = fmaf(__uint_as_float(w.w << 16), xv[6][cc], a);
+                    a       = fmaf(__uint_as_float(w.w & 0xffff0000u), xv[7][cc], a);
+                    acc[p * MU + cc] = a;
+                }
             }
         }
-        const int sbase = c.c + p0;
-        reduce_out(acc, np * MU, lane, AddF(), ShflF(), [&](int n, float v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe((double)v, shift) * scale[sbase + n / MU]; });
+        reduce_out(acc, np * MU, lane, AddF(), ShflF(), [&](int n, float v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe((double)v, shift) * sc; });
     }
 }
 
-template <int MU>
-struct P1Smem { // per warp: data stages, descriptors, barriers, two x buffers
-    static constexpr int kDesc  = kStages * kDataBuf;
-    static constexpr int kBar   = kDesc + kStages * (int)sizeof(StreamChunk);
-    static constexpr int kX     = (kBar + kStages * 8 + 15) & ~15;
-    static constexpr int kXBuf  = 256 * MU * 8;
-    static constexpr int kTotal = (kX + 2 * kXBuf + 127) & ~127;
+// ---------------------------------------------------------------------------
+// phase 1, CTA-staged: one CTA per SM.  The host packs consecutive phase-1
+// chunks (whole columns of one tile, contiguous in the arena) into stages of
+// at most kP1Stage bytes; CTA b takes stages b, b + G, b + 2G, ...  A
+// producer warp fills a ring of kP1Ring stages, each by two bulk copies
+// (the bytes and the stage's chunk descriptors) counted on the stage's full
+// mbarrier; lane i of the producer holds the descriptor of the CTA's stage
+// i of the current window of 32 (loaded a window ahead) and issues it.  The
+// consumer warps take the chunks of a landed stage one at a time through a
+// shared counter, compute them from shared memory (x rows from global, L2
+// resident) and each arrive once on the stage's empty mbarrier after the
+// counter ran out.
+constexpr int kP1Stage = 32768; // bytes of a stage
+constexpr int kP1Items = 32;    // chunks per stage at most
+constexpr int kP1Ring  = 5;     // stages per CTA
+constexpr int kP1Cons  = 11;    // consumer warps per CTA (with the producer: 384 threads, 168 registers each)
+
+struct P1Cta { // shared-memory layout
+    static constexpr int kDataBuf = kP1Stage + 32;
+    static constexpr int kItemBuf = kP1Items * (int)sizeof(StreamChunk) + 32;
+    static constexpr int kItems   = kP1Ring * kDataBuf;
+    static constexpr int kMeta    = kItems + kP1Ring * kItemBuf;
+    static constexpr int kFull    = kMeta + kP1Ring * 32;
+    static constexpr int kEmpty   = kFull + kP1Ring * 8;
+    static constexpr int kTotal   = kEmpty + kP1Ring * 8;
+};
+static_assert(P1Cta::kDataBuf % 16 == 0 && P1Cta::kItemBuf % 16 == 0 && P1Cta::kItems % 16 == 0, "bulk-copy destinations 16-byte aligned");
+
+struct P1Meta { // per ring stage: the landed stage's arena offset, chunk count, chunk-list offset, work counter
+    long long a0;
+    int nitems, ioff, cnt, pad[3];
 };
 
-__device__ __forceinline__ void cp_async8(void *dst, const void *src) { asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa(dst)), "l"(src) : "memory"); }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 template <int MU>
-__global__ void __launch_bounds__(32 * kWarps, 3)
-    phase1_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena,
-                       const double *__restrict__ xp, const F2 *__restrict__ xs, const double *__restrict__ scale, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ A,
-                       int *__restrict__ status) {
-    using L    = P1Smem<MU>;
+__global__ void __launch_bounds__(32 * (kP1Cons + 1), 1)
+    phase1_cta_kernel(const P1Stage *__restrict__ stages, int nstages, const StreamChunk *__restrict__ chunks, const unsigned char *__restrict__ arena, const double *__restrict__ xp,
+                      const F2 *__restrict__ xs, const double *__restrict__ scale, const int *__restrict__ xexp, int mu, double *__restrict__ A, int *__restrict__ status) {
     constexpr int G = 16 / MU; // columns per reduction group
     extern __shared__ __align__(128) unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *wbase    = smem + (size_t)wid * L::kTotal;
-    unsigned char *dbuf     = wbase;
-    StreamChunk *desc       = reinterpret_cast<StreamChunk *>(wbase + L::kDesc);
-    unsigned long long *bar = reinterpret_cast<unsigned long long *>(wbase + L::kBar);
-    unsigned long long *xb  = reinterpret_cast<unsigned long long *>(wbase + L::kX); // 2 x (256 rows x MU)
-    const int shift         = max(*xexp, 1) - 1023;
-    if (lane == 0)
-        for (int s = 0; s < kStages; s++)
-            mbar_init(&bar[s], 1);
+    P1Meta *meta             = reinterpret_cast<P1Meta *>(smem + P1Cta::kMeta);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem + P1Cta::kFull);
+    unsigned long long *empt = reinterpret_cast<unsigned long long *>(smem + P1Cta::kEmpty);
+    const int shift          = max(*xexp, 1) - 1023;
+    const int nmine          = blockIdx.x < nstages ? (nstages - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (threadIdx.x < kP1Ring) {
+        mbar_init(&full[threadIdx.x], 1);
+        mbar_init(&empt[threadIdx.x], kP1Cons);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncwarp();
+    __syncthreads();
 
-    auto claim = [&](int &b, int &e) {
-        const int r = warp_ticket(ticket);
-        if (r < nranges) {
-            b = rbeg[r];
-            e = rbeg[r + 1];
-        } else {
-            b = e = 0;
-        }
-    };
-    Seq q;
-    claim(q.b0, q.e0);
-    claim(q.b1, q.e1);
-    int ip = q.b0, iw = 0;
-    int issued = 0, done = 0;
-    // the descriptor of the chunk issued next is loaded one issue ahead
-    StreamChunk pf;
-    int pf_ip = -1;
-    auto issue_more = [&]() {
-        while (issued - done < kStages) {
-            if (iw == 0 && ip >= q.e0) {
-                ip = q.b1;
-                iw = 1;
+    if (wid == kP1Cons) {
+        // ---------------- producer
+        P1Stage cur{}, nxt{};
+        auto load = [&](P1Stage &w, int i0) {
+            const int i = i0 + lane;
+            if (i < nmine)
+                w = stages[blockIdx.x + (long long)i * gridDim.x];
+        };
+        load(cur, 0);
+        load(nxt, 32);
+        const unsigned long long pol = evict_first_policy();
+        int issued = 0;
+        bool failed = false;
+        for (int i = 0; i < nmine; i++) {
+            if (i > 0 && (i & 31) == 0) {
+                cur = nxt;
+                load(nxt, i + 32);
             }
-            if (iw == 1 && ip >= q.e1)
-                return;
-            const int s         = issued % kStages;
-            const StreamChunk c = ip == pf_ip ? pf : chunks[ip];
-            {
-                const int k2 = (iw == 0 && ip + 1 >= q.e0) ? q.b1 : ip + 1;
-                const int e2 = (iw == 0 && ip + 1 < q.e0) ? q.e0 : q.e1;
-                if (k2 < e2) {
-                    pf    = chunks[k2];
-                    pf_ip = k2;
+            const int s = i % kP1Ring;
+            bool okl    = true;
+            if (lane == (i & 31)) {
+                if (i >= kP1Ring) {
+                    // every consumer is done with the stage's previous fill
+                    const unsigned par = ((i / kP1Ring) - 1) & 1;
+                    if (!mbar_sleep(&empt[s], par, 20000)) {
+                        const long long t0 = clock64();
+                        while (!mbar_sleep(&empt[s], par, 20000))
+                            if (clock64() - t0 > kWaitCycles) {
+                                okl = false;
+                                break;
+                            }
+                    }
+                }
+                if (okl) {
+                    const long long i0 = (long long)sizeof(StreamChunk) * cur.item0;
+                    const long long ia = i0 & ~15LL, ib = ((long long)sizeof(StreamChunk) * (cur.item0 + cur.nitems) + 15) & ~15LL;
+                    meta[s].a0     = cur.a0;
+                    meta[s].nitems = cur.nitems;
+                    meta[s].ioff   = (int)(i0 - ia);
+                    meta[s].cnt    = 0;
+                    mbar_arrive_tx(&full[s], (unsigned)(cur.bytes + (ib - ia)));
+                    bulk_load_stream(smem + (size_t)s * P1Cta::kDataBuf, arena + cur.a0, (unsigned)cur.bytes, &full[s], pol);
+                    bulk_load_stream(smem + P1Cta::kItems + (size_t)s * P1Cta::kItemBuf, reinterpret_cast<const unsigned char *>(chunks) + ia, (unsigned)(ib - ia), &full[s], pol);
                 }
             }
-            if (lane == 0) {
-                desc[s]            = c;
-                const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0));
-                bulk_load_stream(dbuf + (size_t)s * kDataBuf, arena + a0, (unsigned)(a1 - a0), &bar[s], evict_first_policy());
-            }
-            issued++;
-            ip++;
-        }
-    };
-    // the x rows of a tile into x buffer `which` (asynchronous copies): FP64
-    // bits for DFMA chunks, the F2 split otherwise; row-major, MU per row
-    auto load_x = [&](const StreamChunk &c, int which) {
-        const unsigned long long *src = c.kind == kStreamDfma ? reinterpret_cast<const unsigned long long *>(xp) : reinterpret_cast<const unsigned long long *>(xs);
-        unsigned long long *dst       = xb + (size_t)which * 256 * MU;
-        for (int row = lane; row < c.h; row += 32)
-#pragma unroll
-            for (int cc = 0; cc < MU; cc++)
-                cp_async8(dst + row * MU + cc, src + (long long)(c.b + row) * mu + c0 + cc);
-        cp_async_commit();
-    };
-
-    bool ok = true, pre = false; // pre: x of chunk `done` already requested into buffer xcur
-    int xcur   = 0;
-    int left0  = q.e0 - q.b0;
-    issue_more();
-    while (done < issued) {
-        const int s = done % kStages;
-        if (!warp_wait(&bar[s], (done / kStages) & 1)) {
-            ok = false;
-            break;
-        }
-        const StreamChunk c = desc[s];
-        if ((c.flags & kStreamFirst) && !pre) // a new tile whose x was not prefetched
-            load_x(c, xcur);
-        bool nx_pre = false;
-        if (done + 1 < issued) {
-            const int s1 = (done + 1) % kStages;
-            if (!warp_wait(&bar[s1], ((done + 1) / kStages) & 1)) {
-                ok = false;
+            if (!__all_sync(0xffffffffu, okl)) {
+                failed = true;
                 break;
             }
-            if (desc[s1].flags & kStreamFirst) { // next tile's x into the other buffer
-                cp_async_wait_all();             // (this tile's copies first, so waits stay simple)
-                load_x(desc[s1], xcur ^ 1);
-                nx_pre = true;
-            }
+            issued++;
         }
-        // this chunk's x copies: all but the group just committed for the next tile
-        if (nx_pre)
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        else
-            cp_async_wait_all();
-        __syncwarp();
-        const unsigned long long *X = xb + (size_t)xcur * 256 * MU;
-        const unsigned char *buf    = dbuf + (size_t)s * kDataBuf + (c.src & 15);
-        for (int p0 = 0; p0 < c.ncol; p0 += G) {
-            const int np = min(G, c.ncol - p0);
-            // tight loops for the group's column count (rounded up to a power of two)
-            if (np > 8)
-                tile_group<16 / MU, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
-            else if (np > 4)
-                tile_group<(8 < 16 / MU ? 8 : 16 / MU), MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
-            else if (np > 2)
-                tile_group<4, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
-            else if (np > 1)
-                tile_group<2, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
-            else
-                tile_group<1, MU>(c, buf, X, p0, np, lane, shift, A, scale, mu, c0);
-        }
-        __syncwarp();
-        done++;
-        if (--left0 == 0) {
-            if (iw == 0)
-                ip = q.b1;
-            iw    = 0;
-            q.b0  = q.b1;
-            q.e0  = q.e1;
-            left0 = q.e0 - q.b0;
-            claim(q.b1, q.e1);
-        }
-        if (nx_pre)
-            xcur ^= 1;
-        pre = nx_pre;
-        issue_more();
-    }
-    cp_async_wait_all();
-    if (!ok) {
+        if (failed && lane == 0)
+            atomicExch(status, 3);
+        // the copies of the last stages land before the CTA ends
         if (lane == 0)
-            atomicExch(status, 2);
-        for (int p = done; p < issued; p++)
-            if (!warp_wait(&bar[p % kStages], (p / kStages) & 1) && lane == 0)
-                atomicExch(status, 3);
+            for (int i = max(0, issued - kP1Ring); i < issued; i++) {
+                const unsigned par = (i / kP1Ring) & 1;
+                if (!mbar_sleep(&full[i % kP1Ring], par, 20000)) {
+                    const long long t0 = clock64();
+                    while (!mbar_sleep(&full[i % kP1Ring], par, 20000))
+                        if (clock64() - t0 > kWaitCycles) {
+                            atomicExch(status, 3);
+                            break;
+                        }
+                }
+            }
+        return;
+    }
+
+    // ---------------- consumers
+    for (int i = 0; i < nmine; i++) {
+        const int s = i % kP1Ring;
+        if (!warp_wait(&full[s], (i / kP1Ring) & 1)) {
+            if (lane == 0)
+                atomicExch(status, 2);
+            return;
+        }
+        const long long a0             = meta[s].a0;
+        const int nitems               = meta[s].nitems;
+        const unsigned char *data      = smem + (size_t)s * P1Cta::kDataBuf;
+        const StreamChunk *items       = reinterpret_cast<const StreamChunk *>(smem + P1Cta::kItems + (size_t)s * P1Cta::kItemBuf + meta[s].ioff);
+        while (true) {
+            int it = 0;
+            if (lane == 0)
+                it = atomicAdd(&meta[s].cnt, 1);
+            it = __shfl_sync(0xffffffffu, it, 0);
+            if (it >= nitems)
+                break;
+            const StreamChunk c         = items[it];
+            const unsigned long long *X = (c.kind == kStreamDfma ? reinterpret_cast<const unsigned long long *>(xp) : reinterpret_cast<const unsigned long long *>(xs)) + (long long)c.b * mu;
+            const unsigned char *buf    = data + (c.src - a0);
+            // the chunk's x rows, all requested before the first use, in the
+            // row mapping of its kind
+            unsigned long long xw[8][MU];
+            const int r0 = c.kind == kStreamF32 ? 4 * lane : c.kind == kStreamBf16 ? 8 * lane : lane;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int row = c.kind == kStreamF32 ? r0 + (q & 3) + 128 * (q >> 2) : c.kind == kStreamBf16 ? r0 + q : r0 + 32 * q;
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    xw[q][cc] = row < c.h ? __ldg(X + (long long)row * MU + cc) : 0ull;
+            }
+            if (c.kind == kStreamEmu) // at most 4 columns per chunk
+                for (int p0 = 0; p0 < c.ncol; p0 += 4)
+                    tile_cols<4, MU, kStreamEmu>(c, buf, xw, p0, min(4, c.ncol - p0), lane, shift, A, scale, mu, 0);
+            else
+                for (int p0 = 0; p0 < c.ncol; p0 += G) {
+                    const int np = min(G, c.ncol - p0);
+                    if (c.kind == kStreamDfma) {
+                        if (np > 4)
+                            tile_cols<16 / MU, MU, kStreamDfma>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                        else
+                            tile_cols<4, MU, kStreamDfma>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                    } else if (c.kind == kStreamF32) {
+                        if (np > 4)
+                            tile_cols<16 / MU, MU, kStreamF32>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                        else
+                            tile_cols<4, MU, kStreamF32>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                    } else {
+                        if (np > 4)
+                            tile_cols<16 / MU, MU, kStreamBf16>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                        else
+                            tile_cols<4, MU, kStreamBf16>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                    }
+                }
+        }
+        __syncwarp();
+        if (lane == 0)
+            mbar_arrive(&empt[s]);
     }
 }
 
 template <int MU>
-void launch_ws_mu(const StreamChunk *chunks, const int *units, int nunits, int *ticket, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
-                  const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
-    constexpr int kCons            = WsCfg<MU>::kCons;
+void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+                    const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
-    const int bytes                = kCons * WsSmem<MU>::kTotal;
-    int dev = 0, sms = 0;
+    const int bytes                = kWarps * P2Smem<MU>::kTotal;
+    int dev                        = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
     if (dev >= 64 || !(done >> dev & 1)) {
-        HTGPU_CUDA(cudaFuncSetAttribute(phase2_ws_kernel<MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_warp_kernel<MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         if (dev < 64)
             done |= 1ull << dev;
     }
-    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // two CTAs per SM, at most one per unit: small products leave room for
-    // concurrent work
-    const int nctas = std::max(1, std::min(2 * std::max(sms, 1), nunits));
-    phase2_ws_kernel<MU><<<nctas, 32 * (kCons + 1), bytes, st>>>(chunks, units, nunits, units + nunits + 1, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
+    phase2_warp_kernel<MU><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
@@ -966,45 +960,67 @@ int stream_ctas() {
     return n;
 }
 
-void launch_phase1_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
                           const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
-    if (nranges <= 0)
+    if (nstages <= 0)
         return;
     require(mu >= 1 && mu <= 2, "streamed phase 1 takes one or two right-hand sides");
-    HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int), st));
-    const int bytes = kWarps * (mu == 1 ? P1Smem<1>::kTotal : P1Smem<2>::kTotal);
-    int dev         = 0;
+    int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
-    static unsigned long long done1 = 0, done2 = 0;
+    static unsigned long long done1 = 0, done2 = 0; // devices whose shared-memory limit was raised
     unsigned long long &done        = mu == 1 ? done1 : done2;
     if (dev >= 64 || !(done >> dev & 1)) {
         if (mu == 1)
-            HTGPU_CUDA(cudaFuncSetAttribute(phase1_warp_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
         else
-            HTGPU_CUDA(cudaFuncSetAttribute(phase1_warp_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
         if (dev < 64)
             done |= 1ull << dev;
     }
-    // as many warps as ranges, at most every resident CTA: small products
-    // leave room for concurrent work
-    const int nctas = std::max(1, std::min(stream_ctas(), (nranges + kWarps - 1) / kWarps));
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int nctas = std::max(1, std::min(std::max(sms, 1), nstages)); // one CTA per SM
     if (mu == 1)
-        phase1_warp_kernel<1><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, tickets, arena, xp, xs, scale, xexp, mu, 0, A, status);
+        phase1_cta_kernel<1><<<nctas, 32 * (kP1Cons + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
     else
-        phase1_warp_kernel<2><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, tickets, arena, xp, xs, scale, xexp, mu, 0, A, status);
+        phase1_cta_kernel<2><<<nctas, 32 * (kP1Cons + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile) {
+std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &ch) {
+    // consecutive chunks (ascending in the arena) while the 16-byte aligned
+    // span stays within a stage and the chunk count within kP1Items
+    std::vector<P1Stage> out;
+    std::size_t k = 0;
+    while (k < ch.size()) {
+        P1Stage st;
+        st.a0          = ch[k].src & ~15LL;
+        st.item0       = (int)k;
+        long long end  = ch[k].src + ch[k].bytes;
+        std::size_t e  = k + 1;
+        while (e < ch.size() && (int)(e - k) < kP1Items && ch[e].src >= end && (((ch[e].src + ch[e].bytes + 15) & ~15LL) - st.a0) <= kP1Stage) {
+            end = ch[e].src + ch[e].bytes;
+            e++;
+        }
+        st.nitems = (int)(e - k);
+        st.bytes  = (int)(((end + 15) & ~15LL) - st.a0);
+        st.pad    = 0;
+        require(st.bytes <= kP1Stage + 16, "phase-1 chunk larger than a stage");
+        out.push_back(st);
+        k = e;
+    }
+    return out;
+}
+
+void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int ld, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile) {
     // emulated columns are long instruction sequences: at most 4 per chunk
-    int P = std::max(1, std::min(kind == kStreamEmu ? 4 : 16, kStreamStage / (jlen * es)));
+    int P = std::max(1, std::min(kind == kStreamEmu ? 4 : 16, kP1Chunk / (ld * es)));
     while (P & (P - 1))
         P &= P - 1; // a power of two
     for (int k = 0; k < n; k += P) {
         StreamChunk c;
         c.ncol  = std::min(P, n - k);
-        c.src   = src + (long long)jlen * k * es;
-        c.bytes = jlen * c.ncol * es;
+        c.src   = src + (long long)ld * k * es;
+        c.bytes = ld * c.ncol * es;
         c.a     = slot + k0 + k;
         c.b     = xrow;
         c.c     = sidx + k0 + k;
@@ -1016,11 +1032,14 @@ void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen
     }
 }
 
-void launch_phase2_stream(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
                           const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
-    if (nunits <= 0)
+    if (nranges <= 0)
         return;
     HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
+    // as many warps as ranges, at most every resident CTA: small products
+    // leave room for concurrent work
+    const int nctas = std::max(1, std::min(stream_ctas(), (nranges + kWarps - 1) / kWarps));
     int c0 = 0, g = 0;
     while (c0 < mu) {
         const int left = mu - c0;
@@ -1029,58 +1048,14 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *units, int nunit
         if (g >= 7 && c0 > 0)
             HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
         switch (n) {
-        case 8: launch_ws_mu<8>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 4: launch_ws_mu<4>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 2: launch_ws_mu<2>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        default: launch_ws_mu<1>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 8: launch_warp_mu<8>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 4: launch_warp_mu<4>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 2: launch_warp_mu<2>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        default: launch_warp_mu<1>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
         }
         c0 += n;
         g++;
     }
-}
-
-std::vector<int> stream_units(const std::vector<StreamChunk> &ch, int target_units, int *nunits) {
-    // row chunks (first .. last flag) and their cost ~ time: DFMA chunks run
-    // on the FP64 pipe, slower per byte than the other kinds; every chunk has
-    // a fixed overhead
-    std::vector<int> rcs;
-    std::vector<double> cost;
-    for (std::size_t k = 0; k < ch.size(); k++) {
-        if ((ch[k].flags & kStreamFirst) || rcs.empty()) {
-            rcs.push_back((int)k);
-            cost.push_back(0.);
-        }
-        cost.back() += ch[k].bytes * (ch[k].kind == kStreamDfma ? 2.0 : 1.0) + 256.0;
-    }
-    rcs.push_back((int)ch.size());
-    const int nrc = (int)cost.size();
-    double total  = 0;
-    for (double c : cost)
-        total += c;
-    const double target = total / std::max(target_units, 1);
-    std::vector<int> u{0};
-    double acc = 0;
-    for (int i = 0; i < nrc; i++) {
-        acc += cost[i];
-        if (i + 1 < nrc && (acc >= target || i + 1 - u.back() >= kUnitRowChunks)) {
-            u.push_back(i + 1);
-            acc = 0;
-        }
-    }
-    if (nrc > 0)
-        u.push_back(nrc);
-    *nunits = (int)u.size() - 1;
-    // units (row-chunk indices), then the first chunk of every row chunk and the end
-    std::vector<int> out(u);
-    out.insert(out.end(), rcs.begin(), rcs.end());
-    return out;
-}
-
-int stream2_units_target() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return 2 * (sms > 0 ? sms : 152) * 6; // ~6 units per CTA: balance through the ticket
 }
 
 } // namespace htgpu
