@@ -1002,10 +1002,7 @@ void HMatrix::set_precision(int policy, double tau) {
             const LrLeaf &L = lr_h[m.leaf];
             const int slot  = (int)(L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r);
             const int c     = m.pad;
-            if (c > 0)
-                tile_section(ch, m.off, 4, m.jlen, ld_f32(m.jlen), 0, c, slot, L.oj + m.j0, (int)L.a_off, kStreamF32, true);
-            if (L.r > c)
-                tile_section(ch, m.off + 4LL * ld_f32(m.jlen) * c, 2, m.jlen, ld_bf16(m.jlen), c, L.r - c, slot, L.oj + m.j0, (int)L.a_off, kStreamBf16, c == 0);
+            reduced_tile_chunks(ch, m.off, m.jlen, L.r, c, slot, L.oj + m.j0, (int)L.a_off);
             p1_bytes_m_ += 4LL * m.jlen * c + 2LL * m.jlen * (L.r - c);
         }
         const std::vector<P1Stage> st = pack_stages(ch);

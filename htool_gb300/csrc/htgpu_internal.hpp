@@ -132,7 +132,8 @@ struct P1Stage {
     long long a0;
     int bytes, item0, nitems, pad;
 };
-constexpr int kP1Chunk = 8192; // bytes of one streamed phase-1 chunk at most
+constexpr int kP1Chunk   = 16384; // bytes of one streamed reduced-precision phase-1 chunk at most
+constexpr int kP1Chunk64 = 8192;  // and of one FP64 chunk
 
 struct ZItem { // cluster rows row0 .. row0+h: y[perm[i]] = sum over l of z[i + zl[l]], l in [lbeg, lend)
     int row0, h, lbeg, lend;

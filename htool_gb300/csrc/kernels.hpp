@@ -75,6 +75,11 @@ std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &chunks);
 // column stride ld, elements of es bytes; column k0 at byte src): A slots
 // slot + k, scale slots sidx + k
 void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int ld, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile);
+// append the chunks of one reduced-precision tile (jlen rows; c32 FP32
+// columns then r - c32 BF16 columns at byte src, strides ld_f32 / ld_bf16):
+// column ranges of at most 32 columns and kP1Chunk bytes, kind kStreamF32,
+// pad = FP32 columns of the range
+void reduced_tile_chunks(std::vector<StreamChunk> &out, long long src, int jlen, int r, int c32, int slot, int xrow, int sidx);
 // column stride (rows) of the reduced-precision phase-1 tiles: whole 16-byte
 // words per column, zero rows past the tile
 #ifdef __CUDACC__

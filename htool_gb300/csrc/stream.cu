@@ -92,10 +92,6 @@ __device__ __forceinline__ bool warp_wait(unsigned long long *b, unsigned parity
     return true;
 }
 
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sa(dst)), "l"(src), "r"(bytes), "r"(sa(bar)) : "memory");
-}
-
 // L2 policy for data read once (the factor arena): evicted first, so the
 // small vectors gathered per column (phase-1 sums, x) stay in L2
 __device__ __forceinline__ unsigned long long evict_first_policy() {
@@ -108,8 +104,6 @@ __device__ __forceinline__ void bulk_load_stream(void *dst, const void *src, uns
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(sa(dst)), "l"(src), "r"(bytes), "r"(sa(bar)), "l"(policy)
                  : "memory");
 }
-
-__device__ __forceinline__ float bf16f(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
 
 __device__ __forceinline__ void df_addf(DF &a, float p) {
     const float s   = a.s + p;
@@ -704,6 +698,81 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
     }
 }
 
+// The reduced-precision part of one phase-1 tile as one chunk: n32 FP32
+// columns (stride ld_f32(jlen) rows) followed by the BF16 columns (stride
+// ld_bf16(jlen)), both in whole 16-byte words with zero rows past the tile.
+// Lane l holds the partial sums of rows 4l .. 4l+3 and 128+4l .. (FP32
+// words) or 8l .. 8l+7 (BF16 words); the columns go in groups of 8 / MU, a
+// group may mix both kinds, and one reduce-scatter per group sums them
+// over the warp.
+template <int MU>
+__device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned char *buf, int lane, int shift, const F2 *__restrict__ xs, double *__restrict__ A,
+                                           const double *__restrict__ scale, int mu, int c0) {
+    constexpr int GC = 8 / MU; // columns per group
+    const int jlen = c.h, ncol = c.ncol, n32 = min((int)c.pad, ncol);
+    const int W32 = ld_f32(jlen) >> 2, W16 = ld_bf16(jlen) >> 3; // 16-byte words per column
+    const F2 *X   = xs + (long long)c.b * mu + c0;
+    float xf[8][MU], xb[8][MU];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int rf = 4 * lane + (q & 3) + 128 * (q >> 2), rb = 8 * lane + q;
+#pragma unroll
+        for (int cc = 0; cc < MU; cc++) {
+            xf[q][cc] = (n32 > 0 && rf < jlen) ? X[(long long)rf * mu + cc].hi : 0.f;
+            xb[q][cc] = (ncol > n32 && rb < jlen) ? X[(long long)rb * mu + cc].hi : 0.f;
+        }
+    }
+    const uint4 *V32 = reinterpret_cast<const uint4 *>(buf);
+    const uint4 *V16 = reinterpret_cast<const uint4 *>(buf + 16LL * W32 * n32);
+    const bool f0 = lane < W32, f1 = lane + 32 < W32, b0 = lane < W16;
+    for (int g = 0; g < ncol; g += GC) {
+        float acc[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            acc[i] = 0.f;
+        const int ng = min(GC, ncol - g);
+        // the scale of the column this lane writes, requested before the sums
+        const int mine  = rs_slot(ng * MU, lane) / MU;
+        const double sc = mine < ng ? __ldg(scale + c.c + g + mine) : 0.;
+#pragma unroll
+        for (int p = 0; p < GC; p++) {
+            const int k = g + p;
+            if (k < n32) { // warp-uniform
+                const uint4 w0 = f0 ? V32[(size_t)W32 * k + lane] : make_uint4(0u, 0u, 0u, 0u);
+                const uint4 w1 = f1 ? V32[(size_t)W32 * k + lane + 32] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    float a = __uint_as_float(w0.x) * xf[0][cc];
+                    a       = fmaf(__uint_as_float(w0.y), xf[1][cc], a);
+                    a       = fmaf(__uint_as_float(w0.z), xf[2][cc], a);
+                    a       = fmaf(__uint_as_float(w0.w), xf[3][cc], a);
+                    a       = fmaf(__uint_as_float(w1.x), xf[4][cc], a);
+                    a       = fmaf(__uint_as_float(w1.y), xf[5][cc], a);
+                    a       = fmaf(__uint_as_float(w1.z), xf[6][cc], a);
+                    a       = fmaf(__uint_as_float(w1.w), xf[7][cc], a);
+                    acc[p * MU + cc] = a;
+                }
+            } else if (k < ncol) {
+                const uint4 w = b0 ? V16[(size_t)W16 * (k - n32) + lane] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    float a = __uint_as_float(w.x << 16) * xb[0][cc];
+                    a       = fmaf(__uint_as_float(w.x & 0xffff0000u), xb[1][cc], a);
+                    a       = fmaf(__uint_as_float(w.y << 16), xb[2][cc], a);
+                    a       = fmaf(__uint_as_float(w.y & 0xffff0000u), xb[3][cc], a);
+                    a       = fmaf(__uint_as_float(w.z << 16), xb[4][cc], a);
+                    a       = fmaf(__uint_as_float(w.z & 0xffff0000u), xb[5][cc], a);
+                    a       = fmaf(__uint_as_float(w.w << 16), xb[6][cc], a);
+                    a       = fmaf(__uint_as_float(w.w & 0xffff0000u), xb[7][cc], a);
+                    acc[p * MU + cc] = a;
+                }
+            }
+        }
+        const int base = c.a + g;
+        reduce_out(acc, ng * MU, lane, AddF(), ShflF(), [&](int n, float v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe((double)v, shift) * sc; });
+    }
+}
+
 // ---------------------------------------------------------------------------
 // phase 1, CTA-staged: one CTA per SM.  The host packs consecutive phase-1
 // chunks (whole columns of one tile, contiguous in the arena) into stages of
@@ -719,7 +788,10 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
 constexpr int kP1Stage = 32768; // bytes of a stage
 constexpr int kP1Items = 32;    // chunks per stage at most
 constexpr int kP1Ring  = 5;     // stages per CTA
-constexpr int kP1Cons  = 11;    // consumer warps per CTA (with the producer: 384 threads, 168 registers each)
+// consumer warps per CTA: FP64 chunks need many registers (11 + 1 warps,
+// 168 registers each), reduced-precision tiles few (22 + 1 warps, 88 each)
+template <bool RED>
+__host__ __device__ constexpr int p1_cons() { return RED ? 22 : 11; }
 
 struct P1Cta { // shared-memory layout
     static constexpr int kDataBuf = kP1Stage + 32;
@@ -737,11 +809,12 @@ struct P1Meta { // per ring stage: the landed stage's arena offset, chunk count,
     int nitems, ioff, cnt, pad[3];
 };
 
-template <int MU>
-__global__ void __launch_bounds__(32 * (kP1Cons + 1), 1)
+template <int MU, bool RED>
+__global__ void __launch_bounds__(32 * (p1_cons<RED>() + 1), 1)
     phase1_cta_kernel(const P1Stage *__restrict__ stages, int nstages, const StreamChunk *__restrict__ chunks, const unsigned char *__restrict__ arena, const double *__restrict__ xp,
                       const F2 *__restrict__ xs, const double *__restrict__ scale, const int *__restrict__ xexp, int mu, double *__restrict__ A, int *__restrict__ status) {
-    constexpr int G = 16 / MU; // columns per reduction group
+    constexpr int G      = 16 / MU; // columns per reduction group
+    constexpr int kP1Cons = p1_cons<RED>();
     extern __shared__ __align__(128) unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     P1Meta *meta             = reinterpret_cast<P1Meta *>(smem + P1Cta::kMeta);
@@ -844,16 +917,19 @@ __global__ void __launch_bounds__(32 * (kP1Cons + 1), 1)
             it = __shfl_sync(0xffffffffu, it, 0);
             if (it >= nitems)
                 break;
-            const StreamChunk c         = items[it];
+            const StreamChunk c      = items[it];
+            const unsigned char *buf = data + (c.src - a0);
+            if constexpr (RED) { // a reduced-precision tile: FP32 then BF16 columns
+                tile_mixed<MU>(c, buf, lane, shift, xs, A, scale, mu, 0);
+                continue;
+            } else {
+            // FP64 chunks: the chunk's x rows (FP64 bits for DFMA, the F2
+            // split for emulation), all requested before the first use
             const unsigned long long *X = (c.kind == kStreamDfma ? reinterpret_cast<const unsigned long long *>(xp) : reinterpret_cast<const unsigned long long *>(xs)) + (long long)c.b * mu;
-            const unsigned char *buf    = data + (c.src - a0);
-            // the chunk's x rows, all requested before the first use, in the
-            // row mapping of its kind
             unsigned long long xw[8][MU];
-            const int r0 = c.kind == kStreamF32 ? 4 * lane : c.kind == kStreamBf16 ? 8 * lane : lane;
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                const int row = c.kind == kStreamF32 ? r0 + (q & 3) + 128 * (q >> 2) : c.kind == kStreamBf16 ? r0 + q : r0 + 32 * q;
+                const int row = lane + 32 * q;
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
                     xw[q][cc] = row < c.h ? __ldg(X + (long long)row * MU + cc) : 0ull;
@@ -864,23 +940,12 @@ __global__ void __launch_bounds__(32 * (kP1Cons + 1), 1)
             else
                 for (int p0 = 0; p0 < c.ncol; p0 += G) {
                     const int np = min(G, c.ncol - p0);
-                    if (c.kind == kStreamDfma) {
-                        if (np > 4)
-                            tile_cols<16 / MU, MU, kStreamDfma>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
-                        else
-                            tile_cols<4, MU, kStreamDfma>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
-                    } else if (c.kind == kStreamF32) {
-                        if (np > 4)
-                            tile_cols<16 / MU, MU, kStreamF32>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
-                        else
-                            tile_cols<4, MU, kStreamF32>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
-                    } else {
-                        if (np > 4)
-                            tile_cols<16 / MU, MU, kStreamBf16>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
-                        else
-                            tile_cols<4, MU, kStreamBf16>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
-                    }
+                    if (np > 4)
+                        tile_cols<16 / MU, MU, kStreamDfma>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
+                    else
+                        tile_cols<4, MU, kStreamDfma>(c, buf, xw, p0, np, lane, shift, A, scale, mu, 0);
                 }
+            }
         }
         __syncwarp();
         if (lane == 0)
@@ -960,30 +1025,35 @@ int stream_ctas() {
     return n;
 }
 
-void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
-                          const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
-    if (nstages <= 0)
-        return;
-    require(mu >= 1 && mu <= 2, "streamed phase 1 takes one or two right-hand sides");
+template <int MU, bool RED>
+void launch_p1_cta(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale, const int *xexp, int mu,
+                   double *A, int *status, cudaStream_t st) {
+    static unsigned long long done = 0; // devices whose shared-memory limit was raised
     int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
-    static unsigned long long done1 = 0, done2 = 0; // devices whose shared-memory limit was raised
-    unsigned long long &done        = mu == 1 ? done1 : done2;
     if (dev >= 64 || !(done >> dev & 1)) {
-        if (mu == 1)
-            HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
-        else
-            HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
+        HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<MU, RED>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
         if (dev < 64)
             done |= 1ull << dev;
     }
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int nctas = std::max(1, std::min(std::max(sms, 1), nstages)); // one CTA per SM
-    if (mu == 1)
-        phase1_cta_kernel<1><<<nctas, 32 * (kP1Cons + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
-    else
-        phase1_cta_kernel<2><<<nctas, 32 * (kP1Cons + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
+    phase1_cta_kernel<MU, RED><<<nctas, 32 * (p1_cons<RED>() + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
     HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+                          const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
+    if (nstages <= 0)
+        return;
+    require(mu >= 1 && mu <= 2, "streamed phase 1 takes one or two right-hand sides");
+    const bool red = scale != nullptr; // reduced-precision tiles (with per-column scales)
+    if (mu == 1)
+        red ? launch_p1_cta<1, true>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st)
+            : launch_p1_cta<1, false>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
+    else
+        red ? launch_p1_cta<2, true>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st)
+            : launch_p1_cta<2, false>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
 }
 
 std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &ch) {
@@ -1013,7 +1083,7 @@ std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &ch) {
 
 void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen, int ld, int k0, int n, int slot, int xrow, int sidx, unsigned char kind, bool first_of_tile) {
     // emulated columns are long instruction sequences: at most 4 per chunk
-    int P = std::max(1, std::min(kind == kStreamEmu ? 4 : 16, kP1Chunk / (ld * es)));
+    int P = std::max(1, std::min(kind == kStreamEmu ? 4 : 16, kP1Chunk64 / (ld * es)));
     while (P & (P - 1))
         P &= P - 1; // a power of two
     for (int k = 0; k < n; k += P) {
@@ -1030,6 +1100,40 @@ void tile_section(std::vector<StreamChunk> &out, long long src, int es, int jlen
         c.pad   = 0;
         out.push_back(c);
     }
+}
+
+void reduced_tile_chunks(std::vector<StreamChunk> &out, long long src, int jlen, int r, int c32, int slot, int xrow, int sidx) {
+    const long long l32 = 4LL * ld_f32(jlen), l16 = 2LL * ld_bf16(jlen);
+    auto bytes = [&](int k0, int k1) { return l32 * (std::min(k1, c32) - std::min(k0, c32)) + l16 * (std::max(k1, c32) - std::max(k0, c32)); };
+    // greedy column ranges (at most `cap` columns and kP1Chunk bytes each)
+    auto cut = [&](int cap, bool emit) {
+        int k0 = 0, n = 0;
+        while (k0 < r) {
+            int k1 = k0 + 1;
+            while (k1 < r && k1 - k0 < cap && bytes(k0, k1 + 1) <= kP1Chunk)
+                k1++;
+            if (emit) {
+                StreamChunk c;
+                c.src   = src + (k0 < c32 ? l32 * k0 : l32 * c32 + l16 * (k0 - c32));
+                c.bytes = (int)bytes(k0, k1);
+                c.a     = slot + k0;
+                c.b     = xrow;
+                c.c     = sidx + k0;
+                c.h     = jlen;
+                c.ncol  = k1 - k0;
+                c.kind  = kStreamF32;
+                c.flags = k0 == 0 ? kStreamFirst : 0;
+                c.pad   = (unsigned short)std::max(0, std::min(c32, k1) - k0);
+                out.push_back(c);
+            }
+            k0 = k1;
+            n++;
+        }
+        return n;
+    };
+    // as many ranges as the greedy cut needs, with their columns evened out
+    const int n = cut(32, false);
+    cut((r + n - 1) / n, true);
 }
 
 void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
