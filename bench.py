@@ -215,7 +215,7 @@ def run_gpu(args):
         ms_step = ms_total / args.steps
         ph = hm.profile(1, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
         pb = hm.phase_bytes(1)
-        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_warp_kernel", "phase2_ws_kernel", "zsum_kernel"]
+        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_cta_kernel", "phase2_warp_kernel", "zsum_kernel"]
         k = max(range(4), key=lambda i: ph[i])
         achieved = pb[k] / (ph[k] / 1e3) / 1e9
         total_bytes = sum(pb)

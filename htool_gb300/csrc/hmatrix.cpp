@@ -735,6 +735,7 @@ void HMatrix::upload_phase1_lists() {
         }
         const std::vector<P1Stage> st = pack_stages(ch);
         n_p1_ranges_                  = (int)st.size();
+        p1_kinds_                     = chunk_kinds(ch);
         p1r_d.upload(st, stream_);
         ch.push_back(StreamChunk{}); // stage copies read chunk descriptors in whole 16-byte words
         p1c_d.upload(ch, stream_);
@@ -1007,6 +1008,7 @@ void HMatrix::set_precision(int policy, double tau) {
         }
         const std::vector<P1Stage> st = pack_stages(ch);
         n_p1m_ranges_                 = (int)st.size();
+        p1m_kinds_                    = chunk_kinds(ch);
         p1rm_d.upload(st, stream_);
         ch.push_back(StreamChunk{}); // stage copies read chunk descriptors in whole 16-byte words
         p1cm_d.upload(ch, stream_);
@@ -1047,7 +1049,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         HTGPU_CUDA(cudaEventRecord(marks[0], st));
     if (precision_ != 0) {
         if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
-            launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, mix_.p, w_xp, w_xs, scale_d.p, w_xexp, mu, w_A, status_d.p, st);
+            launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scale_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
         } else if (n_p1m_) {
             launch_phase1_mixed(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, w_xexp, mu, w_A, st);
@@ -1068,7 +1070,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         return;
     }
     if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
-        launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
+        launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, p1_kinds_, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
         launches_ += 1;
     } else if (n_p1_dfma_ && n_p1_emu_) {
         HTGPU_CUDA(cudaEventRecord(fork_, st));

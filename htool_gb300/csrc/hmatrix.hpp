@@ -206,6 +206,7 @@ class HMatrix {
     DevBuf<StreamChunk> p1c_d, p1cm_d; // streamed phase 1 (one or two right-hand sides): chunks
     DevBuf<P1Stage> p1r_d, p1rm_d;     // and their stages
     int n_p1_ranges_ = 0, n_p1m_ranges_ = 0;
+    int p1_kinds_ = 0, p1m_kinds_ = 1; // element kinds of those chunk lists
     int mu_cap = 0;
     int launches_ = 0;
     BuildStats st_;

@@ -67,8 +67,11 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
 // (kStreamFirst on a tile's first chunk), A slots written directly (tiles of
 // multi-tile leaves still need launch_reduce_tiles); scale: per-column
 // factors (F32/BF16 kinds); the chunk array is padded by 16 bytes
-void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
                           const int *xexp, int mu, double *A, int *status, cudaStream_t st);
+// element kinds present in a streamed phase-1 chunk list (1: reduced-precision
+// tiles, 2: FP64 DFMA, 4: FP64 emulated)
+int chunk_kinds(const std::vector<StreamChunk> &chunks);
 // stages over a phase-1 chunk list in arena order
 std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &chunks);
 // append the chunks of columns k0 .. k0+n of one tile (jlen rows stored with

@@ -790,8 +790,11 @@ constexpr int kP1Items = 32;    // chunks per stage at most
 constexpr int kP1Ring  = 5;     // stages per CTA
 // consumer warps per CTA: FP64 chunks need many registers (11 + 1 warps,
 // 168 registers each), reduced-precision tiles few (22 + 1 warps, 88 each)
-template <bool RED>
-__host__ __device__ constexpr int p1_cons() { return RED ? 22 : 11; }
+// KM: element kinds of a kernel's chunks (1: reduced-precision tiles, 2:
+// FP64 on the DFMA pipe, 4: FP64 emulated); without DFMA chunks fewer
+// registers leave room for twice the consumer warps
+template <int KM>
+__host__ __device__ constexpr int p1_cons() { return (KM & 2) ? 11 : 22; }
 
 struct P1Cta { // shared-memory layout
     static constexpr int kDataBuf = kP1Stage + 32;
@@ -809,12 +812,12 @@ struct P1Meta { // per ring stage: the landed stage's arena offset, chunk count,
     int nitems, ioff, cnt, pad[3];
 };
 
-template <int MU, bool RED>
-__global__ void __launch_bounds__(32 * (p1_cons<RED>() + 1), 1)
+template <int MU, int KM>
+__global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
     phase1_cta_kernel(const P1Stage *__restrict__ stages, int nstages, const StreamChunk *__restrict__ chunks, const unsigned char *__restrict__ arena, const double *__restrict__ xp,
                       const F2 *__restrict__ xs, const double *__restrict__ scale, const int *__restrict__ xexp, int mu, double *__restrict__ A, int *__restrict__ status) {
     constexpr int G      = 16 / MU; // columns per reduction group
-    constexpr int kP1Cons = p1_cons<RED>();
+    constexpr int kP1Cons = p1_cons<KM>();
     extern __shared__ __align__(128) unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     P1Meta *meta             = reinterpret_cast<P1Meta *>(smem + P1Cta::kMeta);
@@ -919,7 +922,7 @@ __global__ void __launch_bounds__(32 * (p1_cons<RED>() + 1), 1)
                 break;
             const StreamChunk c      = items[it];
             const unsigned char *buf = data + (c.src - a0);
-            if constexpr (RED) { // a reduced-precision tile: FP32 then BF16 columns
+            if constexpr (KM == 1) { // a reduced-precision tile: FP32 then BF16 columns
                 tile_mixed<MU>(c, buf, lane, shift, xs, A, scale, mu, 0);
                 continue;
             } else {
@@ -934,10 +937,11 @@ __global__ void __launch_bounds__(32 * (p1_cons<RED>() + 1), 1)
                 for (int cc = 0; cc < MU; cc++)
                     xw[q][cc] = row < c.h ? __ldg(X + (long long)row * MU + cc) : 0ull;
             }
-            if (c.kind == kStreamEmu) // at most 4 columns per chunk
-                for (int p0 = 0; p0 < c.ncol; p0 += 4)
-                    tile_cols<4, MU, kStreamEmu>(c, buf, xw, p0, min(4, c.ncol - p0), lane, shift, A, scale, mu, 0);
-            else
+            if ((KM & 4) && c.kind == kStreamEmu) { // at most 4 columns per chunk
+                if constexpr ((KM & 4) != 0)
+                    for (int p0 = 0; p0 < c.ncol; p0 += 4)
+                        tile_cols<4, MU, kStreamEmu>(c, buf, xw, p0, min(4, c.ncol - p0), lane, shift, A, scale, mu, 0);
+            } else if constexpr ((KM & 2) != 0)
                 for (int p0 = 0; p0 < c.ncol; p0 += G) {
                     const int np = min(G, c.ncol - p0);
                     if (np > 4)
@@ -1025,35 +1029,51 @@ int stream_ctas() {
     return n;
 }
 
-template <int MU, bool RED>
+template <int MU, int KM>
 void launch_p1_cta(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale, const int *xexp, int mu,
                    double *A, int *status, cudaStream_t st) {
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
     int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
     if (dev >= 64 || !(done >> dev & 1)) {
-        HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<MU, RED>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
+        HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<MU, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
         if (dev < 64)
             done |= 1ull << dev;
     }
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int nctas = std::max(1, std::min(std::max(sms, 1), nstages)); // one CTA per SM
-    phase1_cta_kernel<MU, RED><<<nctas, 32 * (p1_cons<RED>() + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
+    phase1_cta_kernel<MU, KM><<<nctas, 32 * (p1_cons<KM>() + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+template <int MU>
+void launch_p1_kinds(int kinds, const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+                     const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
+    switch (kinds) {
+    case 1: launch_p1_cta<MU, 1>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
+    case 2: launch_p1_cta<MU, 2>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
+    case 4: launch_p1_cta<MU, 4>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
+    default: launch_p1_cta<MU, 6>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
+    }
+}
+
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
                           const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
     if (nstages <= 0)
         return;
     require(mu >= 1 && mu <= 2, "streamed phase 1 takes one or two right-hand sides");
-    const bool red = scale != nullptr; // reduced-precision tiles (with per-column scales)
+    require(kinds == 1 || (kinds & ~6) == 0, "streamed phase 1: reduced-precision tiles or FP64 chunks");
     if (mu == 1)
-        red ? launch_p1_cta<1, true>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st)
-            : launch_p1_cta<1, false>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
+        launch_p1_kinds<1>(kinds, stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
     else
-        red ? launch_p1_cta<2, true>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st)
-            : launch_p1_cta<2, false>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
+        launch_p1_kinds<2>(kinds, stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
+}
+
+int chunk_kinds(const std::vector<StreamChunk> &ch) {
+    int k = 0;
+    for (auto &c : ch)
+        k |= c.kind == kStreamDfma ? 2 : c.kind == kStreamEmu ? 4 : 1;
+    return k;
 }
 
 std::vector<P1Stage> pack_stages(const std::vector<StreamChunk> &ch) {
