@@ -91,6 +91,7 @@ def _load():
         "htgpu_batch_create": (i, [i, vp]),
         "htgpu_batch_destroy": (i, [vp]),
         "htgpu_batch_add": (i, [vp, vp, vp, vp, i, vp]),
+        "htgpu_batch_add_flags": (i, [vp, vp, vp, vp, i, C.c_uint, vp]),
         "htgpu_batch_capture": (i, [vp, i, vp]),
         "htgpu_batch_launch": (i, [vp, vp]),
         "htgpu_batch_sync": (i, [vp]),
@@ -99,6 +100,7 @@ def _load():
         "htgpu_cluster_save": (i, [vp, C.c_char_p]),
         "htgpu_cluster_read": (i, [C.c_char_p, C.c_char_p, vp]),
         "htgpu_hmatrix_save": (i, [vp, C.c_char_p]),
+        "htgpu_hmatrix_save_plot": (i, [vp, C.c_char_p]),
         "htgpu_hmatrix_load": (i, [vp, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
@@ -416,6 +418,10 @@ class HMatrix:
         """Binary dump of the leaves and factors (reloadable with load)."""
         _check(lib.htgpu_hmatrix_save(self.h, str(path).encode()))
 
+    def save_plot(self, outputname):
+        """htool's leaf map: writes <outputname>_0.csv (HMatrix::save_plot)."""
+        _check(lib.htgpu_hmatrix_save_plot(self.h, str(outputname).encode()))
+
     def load(self, path):
         """Leaves and factors from a dump made on the same cluster trees."""
         _check(lib.htgpu_hmatrix_load(self.h, str(path).encode()))
@@ -529,10 +535,11 @@ class HBatch:
         self.h = h
         self._keep = []
 
-    def add(self, hmatrix, x_ptr, y_ptr, mu=1, keep=None):
-        """y = H x on device pointers; `keep` (e.g. the tensors) is held alive."""
+    def add(self, hmatrix, x_ptr, y_ptr, mu=1, keep=None, flags=0):
+        """y = H x on device pointers (CLUSTER_NUMBERING in flags: cluster
+        numbering); `keep` (e.g. the tensors) is held alive."""
         idx = C.c_int()
-        _check(lib.htgpu_batch_add(self.h, hmatrix.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), int(mu), C.byref(idx)))
+        _check(lib.htgpu_batch_add_flags(self.h, hmatrix.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), int(mu), int(flags), C.byref(idx)))
         self._keep.append((hmatrix, keep))
         return idx.value
 

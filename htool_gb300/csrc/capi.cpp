@@ -517,11 +517,14 @@ int htgpu_batch_destroy(htgpu_batch b) {
     return guarded([&] { delete b; });
 }
 
-int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, int *index) {
+int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, int *index) { return htgpu_batch_add_flags(b, h, in, out, mu, 0u, index); }
+
+int htgpu_batch_add_flags(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, int *index) {
     return guarded([&] {
         need(b, "batch");
         need(h, "hmatrix");
-        const int i = b->b->add(h->h.get(), in, out, mu);
+        htgpu::require((flags & ~HTGPU_CLUSTER_NUMBERING) == 0, "batch entries take device pointers; the only flag is HTGPU_CLUSTER_NUMBERING");
+        const int i = b->b->add(h->h.get(), in, out, mu, (flags & HTGPU_CLUSTER_NUMBERING) != 0);
         if (index)
             *index = i;
     });
@@ -599,6 +602,14 @@ int htgpu_hmatrix_save(htgpu_hmatrix h, const char *path) {
         need(h, "hmatrix");
         need(path, "path");
         h->h->save(path);
+    });
+}
+
+int htgpu_hmatrix_save_plot(htgpu_hmatrix h, const char *outputname) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(outputname, "outputname");
+        h->h->save_plot(outputname);
     });
 }
 

@@ -107,6 +107,7 @@ class HMatrix {
     // onto the same cluster trees
     void save(const std::string &path);
     void load(const std::string &path);
+    void save_plot(const std::string &outputname) const;
 
     // nonzero when a bounded device wait of a product ran out (1 producer,
     // 2 consumer, 3 drain); reading it synchronises the H-matrix's stream

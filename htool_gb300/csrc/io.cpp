@@ -185,6 +185,26 @@ void HMatrix::save(const std::string &path) {
     require((bool)f, "writing " + path + " failed", 3);
 }
 
+// htool's leaf map (HMatrix::save_plot, hmatrix.hpp:1696-1712): the file
+// <outputname>_<rank>.csv (one rank here: _0) holds "nr,nc" and then one line
+// "offset_i,size_i,offset_j,size_j,rank" per leaf, the dense leaves first
+// (rank -1), each list in htool's order; a complex H-matrix reports its
+// complex sizes and ranks (the real form doubles them)
+void HMatrix::save_plot(const std::string &outputname) const {
+    std::vector<int> lr(5 * lr_h.size()), dn(4 * dn_h.size());
+    leaf_descriptors(lr.data(), dn.data());
+    const int f = complex_ ? 2 : 1;
+    const std::string path = outputname + "_0.csv";
+    std::ofstream out(path);
+    require((bool)out, "cannot write " + path, 3);
+    out << nr / f << "," << nc / f << "\n";
+    for (std::size_t d = 0; d < dn_h.size(); d++)
+        out << dn[4 * d] / f << "," << dn[4 * d + 2] / f << "," << dn[4 * d + 1] / f << "," << dn[4 * d + 3] / f << "," << -1 << "\n";
+    for (std::size_t l = 0; l < lr_h.size(); l++)
+        out << lr[5 * l] / f << "," << lr[5 * l + 2] / f << "," << lr[5 * l + 1] / f << "," << lr[5 * l + 3] / f << "," << lr[5 * l + 4] / f << "\n";
+    require((bool)out, "writing " + path + " failed", 3);
+}
+
 void HMatrix::load(const std::string &path) {
     std::ifstream f(path, std::ios::binary);
     require((bool)f, "cannot open " + path);

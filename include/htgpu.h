@@ -289,6 +289,11 @@ int htgpu_hmatrix_aca_samples(htgpu_hmatrix h, float *features, float *ranks, in
 int htgpu_batch_create(int device, htgpu_batch *out);
 int htgpu_batch_destroy(htgpu_batch b);
 int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, int *index);
+/* The same with flags: HTGPU_CLUSTER_NUMBERING makes the entry a product in
+ * cluster (local) numbering, htool's mvprod_local_to_local on one rank
+ * (hmatrix.hpp:1185-1274): what HPDDM's GMV calls in a Krylov loop
+ * (wrappers/wrapper_hpddm.hpp:41-83). */
+int htgpu_batch_add_flags(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, int *index);
 int htgpu_batch_capture(htgpu_batch b, int nstreams, long long *graph_nodes);
 int htgpu_batch_launch(htgpu_batch b, void *stream);
 int htgpu_batch_sync(htgpu_batch b);
@@ -322,6 +327,12 @@ int htgpu_cluster_read(const char *perm_file, const char *tree_file, htgpu_clust
  * to reuse a large build. */
 int htgpu_hmatrix_save(htgpu_hmatrix h, const char *path);
 int htgpu_hmatrix_load(htgpu_hmatrix h, const char *path);
+
+/* htool's leaf map, HMatrix::save_plot (include/htool/types/hmatrix.hpp:1696-1712):
+ * writes <outputname>_0.csv (one rank) with "nr,nc" and one line
+ * "offset_i,size_i,offset_j,size_j,rank" per leaf, dense leaves first with
+ * rank -1, in htool's leaf order; the file tools/plot_hmatrix.py reads. */
+int htgpu_hmatrix_save_plot(htgpu_hmatrix h, const char *outputname);
 
 #ifdef __cplusplus
 }

@@ -178,6 +178,8 @@ class Oracle:
             L.ref_cluster_export.argtypes = [_vp, _vp, _vp, _vp]
             L.ref_cluster_depths.argtypes = [_vp, _vp, _vp]
             L.ref_cluster_save.argtypes = [_vp, C.c_char_p]
+            L.ref_hmatrix_save_plot_d.argtypes = [_vp, C.c_char_p]
+            L.ref_hmatrix_save_plot_z.argtypes = [_vp, C.c_char_p]
             L.ref_cluster_read.restype = _vp
             L.ref_cluster_read.argtypes = [C.c_char_p, C.c_char_p]
             L.ref_block_tasks.argtypes = [_vp, _vp, _d, C.c_char, _i, _vp]

@@ -143,6 +143,10 @@ void ref_cluster_export(void *p, int *perm, int *node_i, double *node_d) {
     });
 }
 
+// HMatrix::save_plot (hmatrix.hpp:1696-1712)
+void ref_hmatrix_save_plot_d(void *p, const char *name) { ((RefHMat<double> *)p)->h->save_plot(name); }
+void ref_hmatrix_save_plot_z(void *p, const char *name) { ((RefHMat<std::complex<double>> *)p)->h->save_plot(name); }
+
 // VirtualCluster::save_cluster / read_cluster (cluster.hpp:433-583)
 void ref_cluster_save(void *p, const char *name) { ((RefCluster *)p)->c->save_cluster(name); }
 void *ref_cluster_read(const char *perm_file, const char *tree_file) {

@@ -15,7 +15,8 @@ they produce:
 
 Usage (needs the upstream sources, i.e. only in the build container):
     make -C oracle/refbuild REF=/root/reference/include
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # everything but the leaf maps
+    python tests/golden/make_golden.py plot     # the save_plot leaf maps only
 """
 import ctypes as C
 import hashlib
@@ -151,5 +152,28 @@ def main():
     R._L.ref_cluster_save(ct.h, os.path.join(OUT, "cyl4000_cluster").encode())
 
 
+def plot_cases():
+    """htool's leaf maps (HMatrix::save_plot) of the configuration-1 and
+    Helmholtz fixtures, written by upstream itself (one thread)"""
+    R = Oracle("reference")
+    R.set_num_threads(1)
+    cyl = G.cylinder(4000, seed=1)
+    ct = R.cluster(cyl)
+    H = R.hmatrix(ct, ct, cyl, cyl, 0, 1e-6, 10.0)
+    R._L.ref_hmatrix_save_plot_d(H.h, os.path.join(OUT, "cyl4000_plot").encode())
+    L, vp = R._L, C.c_void_p
+    L.ref_hmatrix_build_z.restype = vp
+    L.ref_hmatrix_build_z.argtypes = [vp, vp, C.c_int, vp, C.c_int, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char, C.c_int]
+    L.ref_hmatrix_free_z.argtypes = [vp]
+    pts = G.cube_surface(2000, seed=1)
+    cz = R.cluster(pts)
+    h = L.ref_hmatrix_build_z(cz.h, cz.h, 2000, pts.ctypes.data, 2000, pts.ctypes.data, 20.0, 1e-5, 3.0, 0, b"N", b"N", 0)
+    L.ref_hmatrix_save_plot_z(h, os.path.join(OUT, "helmholtz_cube2000_plot").encode())
+    L.ref_hmatrix_free_z(h)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["plot"]:
+        plot_cases()
+    else:
+        main()

@@ -64,3 +64,41 @@ def test_hmatrix_dump_round_trip(tmp_path):
     other = H.Cluster().build(n, G.sphere(n, seed=2))
     with pytest.raises(ValueError):
         H.HMatrix(other, other, 1e-6, 10.0).load(tmp_path / "h.bin")
+
+
+def plot_lines(path):
+    """header and the sets of dense / low-rank lines of a save_plot file
+    (htool writes its leaves in OpenMP insertion order, so only the sets
+    are defined)"""
+    lines = open(path).read().splitlines()
+    body = lines[1:]
+    return lines[0], sorted(l for l in body if l.endswith(",-1")), sorted(l for l in body if not l.endswith(",-1"))
+
+
+def leaf_lines(n, lr, dn):
+    dense = sorted("%d,%d,%d,%d,-1" % (oi, m, oj, nn) for oi, oj, m, nn in dn)
+    low = sorted("%d,%d,%d,%d,%d" % (oi, m, oj, nn, r) for oi, oj, m, nn, r in lr)
+    return "%d,%d" % (n, n), dense, low
+
+
+@pytest.mark.parametrize("case,plot", [("cyl4000_k0", "cyl4000_plot_0.csv"), ("helmholtz_cube2000", "helmholtz_cube2000_plot_0.csv")])
+def test_upstream_plot_matches_golden_leaves(case, plot):
+    """upstream's save_plot files agree with the pinned upstream leaf lists"""
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    assert plot_lines(os.path.join(GOLDEN, plot)) == leaf_lines(g["xt"].shape[0], g["lr"], g["dense"])
+
+
+@pytest.mark.gpu
+def test_save_plot_matches_upstream(tmp_path):
+    """HMatrix::save_plot of the device-built configuration-1 and Helmholtz
+    H-matrices: the same header and leaf lines as upstream's files"""
+    pts = G.cylinder(4000, seed=1)
+    t = H.Cluster().build(4000, pts)
+    hm = H.HMatrix(t, t, 1e-6, 10.0).build(H.INV_R_EPS, pts)
+    hm.save_plot(tmp_path / "cyl")
+    assert plot_lines(tmp_path / "cyl_0.csv") == plot_lines(os.path.join(GOLDEN, "cyl4000_plot_0.csv"))
+    pz = G.cube_surface(2000, seed=1)
+    tz = H.Cluster().build(2000, pz)
+    hz = H.HMatrix(tz, tz, 1e-5, 3.0, dtype=np.complex128).build(H.HELMHOLTZ, pz, kernel_param=20.0)
+    hz.save_plot(tmp_path / "cube")
+    assert plot_lines(tmp_path / "cube_0.csv") == plot_lines(os.path.join(GOLDEN, "helmholtz_cube2000_plot_0.csv"))
