@@ -31,6 +31,7 @@ CLUSTER_NUMBERING = 2
 
 PREC_FP64, PREC_FP32, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
 PHASE1_TILES, PHASE1_STREAM = 0, 1
+PHASE2_WARP, PHASE2_PRODUCER = 0, 1
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED, "bf16": PREC_BF16}
 
 _ERRORS = {1: ValueError, 2: NotImplementedError, 3: RuntimeError, 4: MemoryError, 5: RuntimeError}
@@ -71,6 +72,8 @@ def _load():
         "htgpu_hmatrix_get_fp64_split": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_phase1_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_phase1_mode": (i, [vp, vp]),
+        "htgpu_hmatrix_set_phase2_mode": (i, [vp, i]),
+        "htgpu_hmatrix_get_phase2_mode": (i, [vp, vp]),
         "htgpu_hmatrix_device_status": (i, [vp, vp]),
         "htgpu_hmatrix_autotune": (i, [vp, i, i, vp]),
         "htgpu_hmatrix_mvprod_noalloc": (i, [vp, vp, vp, i, vp]),
@@ -356,6 +359,18 @@ class HMatrix:
     def get_phase1_mode(self):
         v = C.c_int()
         _check(lib.htgpu_hmatrix_get_phase1_mode(self.h, C.byref(v)))
+        return v.value
+
+    def set_phase2_mode(self, mode):
+        """Phase 2: 'warp' (every warp streams its own chunks) or
+        'producer' (producer warps feed consumer warps)."""
+        m = {"warp": PHASE2_WARP, "producer": PHASE2_PRODUCER}[mode] if isinstance(mode, str) else int(mode)
+        _check(lib.htgpu_hmatrix_set_phase2_mode(self.h, m))
+        return self
+
+    def get_phase2_mode(self):
+        v = C.c_int()
+        _check(lib.htgpu_hmatrix_get_phase2_mode(self.h, C.byref(v)))
         return v.value
 
     def device_status(self):

@@ -326,6 +326,21 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *p1, int *n64) {
     });
 }
 
+int htgpu_hmatrix_set_phase2_mode(htgpu_hmatrix h, int mode) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_phase2_mode(mode);
+    });
+}
+
+int htgpu_hmatrix_get_phase2_mode(htgpu_hmatrix h, int *mode) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(mode, "mode");
+        *mode = h->h->phase2_mode();
+    });
+}
+
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode) {
     return guarded([&] {
         need(h, "hmatrix");

@@ -770,6 +770,7 @@ void HMatrix::upload_phase1_lists() {
         const std::vector<int> r = stream_ranges(ch, n_sctas_);
         n_ranges_                = (int)r.size() - 1;
         sr_d.upload(r, stream_);
+        su_d.upload(stream_units(ch, stream2_units_target(), &n_units_), stream_);
     }
     sc_d.upload(ch, stream_);
     if (ch.empty())
@@ -817,6 +818,7 @@ void HMatrix::upload_mixed_phase2() {
     const std::vector<int> r = stream_ranges(ch2_h_, n_sctas_);
     n_ranges_m_              = (int)r.size() - 1;
     srm_d.upload(r, stream_);
+    sum_d.upload(stream_units(ch2_h_, stream2_units_target(), &n_units_m_), stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -1061,8 +1063,12 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         }
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
-        launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_,
-                             status_d.p, st);
+        if (p2_mode_ == 1)
+            launch_phase2_producer(scm_d.p, sum_d.p, n_units_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
+                                   (int)zlen_, status_d.p, st);
+        else
+            launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
+                                 (int)zlen_, status_d.p, st);
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
         launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
@@ -1095,13 +1101,22 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         HTGPU_CUDA(cudaEventRecord(marks[1], st));
     {
         const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
-        launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+        if (p2_mode_ == 1)
+            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+        else
+            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         launches_ += groups;
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
     }
     launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
     launches_ += 1;
+}
+
+void HMatrix::set_phase2_mode(int mode) {
+    layout_gen_++; // captured products are stale
+    require(mode == 0 || mode == 1, "phase-2 mode must be 0 (per-warp streams) or 1 (producer-fed)");
+    p2_mode_ = mode;
 }
 
 void HMatrix::set_phase1_mode(int mode) {
@@ -1172,6 +1187,25 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
             }
         p1_mode_ = arg_mode;
         set_fp64_split(arg.first, arg.second);
+    }
+    // then the phase-2 kernel for the chosen configuration
+    {
+        const int keep = p2_mode_;
+        float b2       = best;
+        int arg2       = keep;
+        for (int m : {0, 1}) {
+            if (m == keep)
+                continue;
+            p2_mode_       = m;
+            const float ms = timed();
+            if (ms < b2) {
+                b2   = ms;
+                arg2 = m;
+            }
+        }
+        p2_mode_ = arg2;
+        best     = b2;
+        layout_gen_++;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

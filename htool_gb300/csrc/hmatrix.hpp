@@ -93,6 +93,8 @@ class HMatrix {
     // tile, DFMA and emulated tiles on two streams), 1 streamed chunks
     void set_phase1_mode(int mode);
     int phase1_mode() const { return p1_mode_; }
+    void set_phase2_mode(int mode);
+    int phase2_mode() const { return p2_mode_; }
     bool emulation_allowed() const { return emu_ok_; }
     // time every candidate split on the current H-matrix and keep the fastest
     // FP64: phase-1 mode and the DFMA/emulation split; reduced precision:
@@ -201,6 +203,9 @@ class HMatrix {
     int n_sctas_ = 0, n_ranges_ = 0, n_ranges_m_ = 0;
     long long n_chunks_ = 0, n_chunks_m_ = 0;
     int p1_mode_ = 0;
+    int p2_mode_ = 0;                  // 0: per-warp streams, 1: producer-fed CTAs
+    DevBuf<int> su_d, sum_d;           // phase-2 units (producer-fed) of the FP64 / reduced chunk lists
+    int n_units_ = 0, n_units_m_ = 0;
     // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced
     // storage), phase-2 columns, z values read by the final sums
     long long p1_bytes_ = 0, p2_bytes_ = 0, n_cols_ = 0, p1_bytes_m_ = 0, p2_bytes_m_ = 0, n_cols_m_ = 0, zsum_reads_ = 0;

@@ -463,6 +463,395 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
 }
 
 // ---------------------------------------------------------------------------
+// phase 2, warp-specialised (phase-2 mode 1): one producer warp per CTA feeds kCons consumer
+// warps.  Each consumer owns a ring of kStages shared-memory stages (data,
+// column indices, descriptor; a full and an empty mbarrier each).  The
+// producer claims units of whole row chunks from a global ticket, hands row
+// chunks to consumers as they become free (lane w of the producer serves
+// consumer w, so all consumers are served by one instruction stream), keeps
+// every consumer's next descriptor prefetched in registers and issues the
+// bulk copies; after the last chunk it posts a stop descriptor.  A consumer
+// only waits for its stage, gathers the coefficients of the chunk after the
+// current one, computes, writes z at the end of each row chunk and releases
+// the stage.
+template <int MU>
+struct WsCfg { // consumers per producer and resident CTAs per SM (shared memory bound)
+    static constexpr int kCons = MU >= 8 ? 4 : MU >= 4 ? 6 : 4;
+    static constexpr int kCtas = MU >= 8 ? 2 : MU >= 4 ? 2 : MU >= 2 ? 3 : 4;
+};
+
+template <int MU>
+struct WsSmem { // per consumer
+    static constexpr int kIdx   = kStages * kDataBuf;
+    static constexpr int kDesc  = kIdx + kStages * kIdxBuf;
+    static constexpr int kFull  = kDesc + kStages * 48;
+    static constexpr int kEmpty = kFull + kStages * 8;
+    static constexpr int kCoef  = (kEmpty + kStages * 8 + 15) & ~15;
+    static constexpr int kTotal = (kCoef + 128 * MU * 4 + 127) & ~127;
+};
+
+constexpr unsigned char kStreamStop = 0xFF; // descriptor kind: no more chunks
+
+
+
+// one thread waits (bounded) for a phase
+__device__ __forceinline__ bool lane_wait(unsigned long long *b, unsigned parity) {
+    if (mbar_sleep(b, parity, 20000))
+        return true;
+    const long long t0 = clock64();
+    while (!mbar_sleep(b, parity, 20000))
+        if (clock64() - t0 > kWaitCycles)
+            return false;
+    return true;
+}
+
+template <int MU>
+__global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
+    phase2_ws_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ units, int nunits, const int *__restrict__ rcs, int *__restrict__ ticket,
+                     const unsigned char *__restrict__ arena0, const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A,
+                     const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen,
+                     int *__restrict__ status) {
+    constexpr int kCons = WsCfg<MU>::kCons;
+    using L             = WsSmem<MU>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    auto ring     = [&](int w) { return smem + (size_t)w * L::kTotal; };
+    auto fullb    = [&](int w, int s) { return reinterpret_cast<unsigned long long *>(ring(w) + L::kFull) + s; };
+    auto emptyb   = [&](int w, int s) { return reinterpret_cast<unsigned long long *>(ring(w) + L::kEmpty) + s; };
+    auto sdesc    = [&](int w, int s) { return reinterpret_cast<StreamChunk *>(ring(w) + L::kDesc + 48 * s); };
+    if (threadIdx.x < kCons * kStages) {
+        mbar_init(fullb(threadIdx.x / kStages, threadIdx.x % kStages), 1);
+        mbar_init(emptyb(threadIdx.x / kStages, threadIdx.x % kStages), 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+
+    if (wid == kCons) {
+        // ---------------- producer: lane w < kCons serves consumer w
+        const bool mine = lane < kCons;
+        int k = 0, e = 0; // chunks [k, e) of consumer w's row chunk still to issue
+        int iss   = 0;    // stages filled for consumer w (stop included)
+        bool fin  = !mine, stop = false;
+        StreamChunk dn{};   // descriptor of chunk k
+        int rb = 0, re = 0, rnext = 0, win = 0; // claimed row chunks [rb, re); lane j: start of row chunk rb + j
+        bool more = true;
+        auto claim_unit = [&]() {
+            int u = 0;
+            if (lane == 0)
+                u = atomicAdd(ticket, 1);
+            u = __shfl_sync(0xffffffffu, u, 0);
+            if (u >= nunits)
+                return false;
+            rb    = units[u];
+            re    = units[u + 1]; // re - rb <= 31
+            win   = rcs[min(rb + lane, re)];
+            rnext = rb;
+            return true;
+        };
+        more                           = claim_unit();
+        const unsigned long long pol   = evict_first_policy();
+        long long idle0                = clock64();
+        bool timed_out                 = false;
+        while (__any_sync(0xffffffffu, !fin)) {
+            // consumers between row chunks take the next row chunks in lane order
+            unsigned need = __ballot_sync(0xffffffffu, !fin && !stop && k >= e);
+            while (need) {
+                const int v = __ffs(need) - 1;
+                need &= need - 1;
+                if (more && rnext >= re)
+                    more = claim_unit();
+                if (more) {
+                    const int s0 = __shfl_sync(0xffffffffu, win, rnext - rb), s1 = __shfl_sync(0xffffffffu, win, rnext + 1 - rb);
+                    if (lane == v) {
+                        k  = s0;
+                        e  = s1;
+                        dn = chunks[k];
+                    }
+                    rnext++;
+                } else if (lane == v)
+                    stop = true;
+            }
+            bool ready = false;
+            if (!fin) {
+                const int s = iss % kStages;
+                ready       = iss < kStages || mbar_test(emptyb(lane, s), ((iss / kStages) & 1) ^ 1);
+                if (ready) {
+                    StreamChunk *d = sdesc(lane, s);
+                    if (stop) {
+                        d->kind = kStreamStop;
+                        mbar_arrive(fullb(lane, s));
+                        fin = true;
+                    } else {
+                        *d                        = dn;
+                        const unsigned char *base = (dn.flags & kStreamArena1) ? arena1 : arena0;
+                        const long long a0 = dn.src & ~15LL, a1 = (dn.src + dn.bytes + 15) & ~15LL;
+                        const long long i0 = (4LL * dn.a) & ~15LL, i1 = (4LL * (dn.a + dn.ncol) + 15) & ~15LL;
+                        mbar_arrive_tx(fullb(lane, s), (unsigned)(a1 - a0 + i1 - i0));
+                        bulk_load_stream(ring(lane) + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), fullb(lane, s), pol);
+                        bulk_load_stream(ring(lane) + L::kIdx + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), fullb(lane, s), pol);
+                        if (++k < e)
+                            dn = chunks[k];
+                    }
+                    iss++;
+                }
+            }
+            if (__any_sync(0xffffffffu, ready))
+                idle0 = clock64();
+            else {
+                if (__any_sync(0xffffffffu, clock64() - idle0 > kWaitCycles)) { // no consumer released a stage for ~2 s
+                    timed_out = true;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        if (timed_out && lane == 0)
+            atomicExch(status, 3);
+        // copies still in flight (none on the normal path) land before the CTA ends
+        if (mine)
+            for (int j = 1; j <= min(iss, kStages); j++)
+                if (!lane_wait(fullb(lane, (iss - j) % kStages), ((iss - j) / kStages) & 1))
+                    atomicExch(status, 3);
+        return;
+    }
+
+    // ---------------- consumers
+    unsigned char *wbase = ring(wid);
+    float *cf            = reinterpret_cast<float *>(wbase + L::kCoef); // MU x 128: FP32 / BF16 chunk coefficients in lane order
+    const int xe         = max(*xexp, 1);
+
+    // raw coefficients of a landed chunk into registers: column t = lane + 32 j
+    auto gather = [&](int s, const StreamChunk &c, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
+        const int *ix  = reinterpret_cast<const int *>(wbase + L::kIdx + (size_t)s * kIdxBuf + ((4LL * c.a) & 15));
+        const bool emu = c.kind == kStreamEmu;
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            const int t = lane + 32 * j;
+            kk[j]       = t < c.ncol ? ix[t] : 0;
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++) {
+                double v = 0.;
+                if (t < c.ncol) {
+                    const int kx = kk[j];
+                    if (kx >= 0)
+                        v = __ldg(A + (long long)kx * mu + c0 + cc);
+                    else if (emu)
+                        v = __longlong_as_double(__ldg(reinterpret_cast<const long long *>(xs) + (long long)(~kx) * mu + c0 + cc));
+                    else
+                        v = __ldg(xp + (long long)(~kx) * mu + c0 + cc);
+                }
+                raw[j][cc] = v;
+            }
+        }
+    };
+    // coefficients of an FP32 / BF16 chunk (in the units of x, as floats) in
+    // the lane order of its data: column t = slice + S j sits at
+    // ((j / V) S + slice) V + j % V, so a lane reads V of them at once
+    auto stage_coefs = [&](const StreamChunk &c, const double (&r)[kStreamCols / 32][MU]) {
+        if (c.kind != kStreamF32 && c.kind != kStreamBf16)
+            return;
+        const int S = div_small(32, c.h), lv = c.kind == kStreamF32 ? 2 : 3; // V = 1 << lv
+#pragma unroll
+        for (int i = 0; i < 4 * MU; i++)
+            cf[lane + 32 * i] = 0.f;
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            const int t = lane + 32 * j;
+            if (t < c.ncol) {
+                const int jj = div_small(t, S), sl = t - jj * S;
+                const int pos = ((((jj >> lv) * S + sl) << lv) | (jj & ((1 << lv) - 1)));
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    cf[cc * 128 + pos] = (float)scale_pow2_safe(r[j][cc], 1023 - xe);
+            }
+        }
+        __syncwarp();
+    };
+
+    double dacc[MU];
+    DF acc[MU];
+#pragma unroll
+    for (int cc = 0; cc < MU; cc++) {
+        dacc[cc] = 0.;
+        df_zero(acc[cc]);
+    }
+    double raw[kStreamCols / 32][MU], rnx[kStreamCols / 32][MU];
+    int kk[kStreamCols / 32], knx[kStreamCols / 32];
+    int s = 0;
+    unsigned par = 0;
+    bool ok = true;
+    if (!warp_wait(fullb(wid, 0), 0))
+        ok = false;
+    StreamChunk c = *sdesc(wid, 0);
+    if (ok && c.kind != kStreamStop) {
+        gather(0, c, raw, kk);
+        stage_coefs(c, raw);
+    }
+    while (ok && c.kind != kStreamStop) {
+        const int s1          = s + 1 == kStages ? 0 : s + 1;
+        const unsigned par1   = s + 1 == kStages ? par ^ 1 : par;
+        // the next chunk: when it has landed already, start its coefficients now
+        bool have_nx = __all_sync(0xffffffffu, mbar_test(fullb(wid, s1), par1));
+        StreamChunk cn;
+        if (have_nx) {
+            cn = *sdesc(wid, s1);
+            if (cn.kind != kStreamStop)
+                gather(s1, cn, rnx, knx);
+        }
+        const int h = c.h, S = div_small(32, h), slice = div_small(lane, h), row = lane - slice * h;
+        const bool live          = slice < S;
+        const unsigned char *buf = wbase + (size_t)s * kDataBuf + (c.src & 15);
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            const int q0 = 32 * j;
+            if (q0 >= c.ncol)
+                break;
+            const int qc = min(32, c.ncol - q0);
+            if (c.kind == kStreamDfma) {
+                const double *P = reinterpret_cast<const double *>(buf) + row + (size_t)h * q0;
+#pragma unroll 4
+                for (int j0 = 0; j0 < qc; j0 += S) {
+                    const int jj   = j0 + slice;
+                    const bool use = live && jj < qc;
+                    const double u = use ? P[h * jj] : 0.;
+#pragma unroll
+                    for (int cc = 0; cc < MU; cc++)
+                        dacc[cc] = fma(u, __shfl_sync(0xffffffffu, raw[j][cc], use ? jj : 0), dacc[cc]);
+                }
+            } else if (c.kind == kStreamEmu) {
+                F2 a[MU];
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    if (kk[j] >= 0) // phase-1 sum, in the units of x
+                        a[cc] = split64(scale_pow2_safe(raw[j][cc], 1023 - xe));
+                    else { // x, already split
+                        const long long bits = __double_as_longlong(raw[j][cc]);
+                        a[cc].hi             = __int_as_float((int)(bits & 0xffffffffLL));
+                        a[cc].lo             = __int_as_float((int)(bits >> 32));
+                    }
+                }
+                const double *P = reinterpret_cast<const double *>(buf) + row + (size_t)h * q0;
+#pragma unroll 4
+                for (int j0 = 0; j0 < qc; j0 += S) {
+                    const int jj   = j0 + slice;
+                    const bool use = live && jj < qc;
+                    const F2 u     = split64(use ? P[h * jj] : 0.);
+#pragma unroll
+                    for (int cc = 0; cc < MU; cc++) {
+                        F2 b;
+                        b.hi = __shfl_sync(0xffffffffu, a[cc].hi, use ? jj : 0);
+                        b.lo = __shfl_sync(0xffffffffu, a[cc].lo, use ? jj : 0);
+                        df_fma(acc[cc], u, b);
+                    }
+                }
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    df_renorm(acc[cc]);
+            }
+        }
+        if (c.kind == kStreamF32 || c.kind == kStreamBf16) {
+            // lane order: 16 bytes of V elements per lane and group of V
+            // columns, coefficients alongside in shared memory
+            const int V = c.kind == kStreamF32 ? 4 : 8, lv = V == 4 ? 2 : 3;
+            const int Ln = S * h, J = div_small(c.ncol + S - 1, S), G = (J + V - 1) >> lv;
+            float part[MU], part2[MU];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                part[cc] = part2[cc] = 0.f;
+            if (lane < Ln) {
+                const uint4 *D = reinterpret_cast<const uint4 *>(buf) + lane;
+                if (V == 4) {
+#pragma unroll 2
+                    for (int g = 0; g < G; g++) {
+                        const uint4 w = D[g * Ln];
+#pragma unroll
+                        for (int cc = 0; cc < MU; cc++) {
+                            const float4 cv = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 4);
+                            part[cc]        = fmaf(__uint_as_float(w.x), cv.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.y), cv.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.z), cv.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.w), cv.w, part2[cc]);
+                        }
+                    }
+                } else {
+#pragma unroll 2
+                    for (int g = 0; g < G; g++) {
+                        const uint4 w = D[g * Ln];
+#pragma unroll
+                        for (int cc = 0; cc < MU; cc++) {
+                            const float4 k0 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8);
+                            const float4 k1 = *reinterpret_cast<const float4 *>(cf + cc * 128 + (g * S + slice) * 8 + 4);
+                            part[cc]        = fmaf(__uint_as_float(w.x << 16), k0.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.x & 0xffff0000u), k0.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.y << 16), k0.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.y & 0xffff0000u), k0.w, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.z << 16), k1.x, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.z & 0xffff0000u), k1.y, part2[cc]);
+                            part[cc]        = fmaf(__uint_as_float(w.w << 16), k1.z, part[cc]);
+                            part2[cc]       = fmaf(__uint_as_float(w.w & 0xffff0000u), k1.w, part2[cc]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                df_addf(acc[cc], part[cc] + part2[cc]);
+        }
+        if (c.flags & kStreamLast) {
+            double v[MU];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                v[cc] = dacc[cc] + scale_pow2_safe(df_to_double(acc[cc]), xe - 1023);
+            for (int t = 1; t < S; t++)
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++) {
+                    const int src   = lane + t * h;
+                    const double vv = __shfl_sync(0xffffffffu, v[cc], src < 32 ? src : lane);
+                    if (slice == 0)
+                        v[cc] += vv;
+                }
+            if (slice == 0)
+#pragma unroll
+                for (int cc = 0; cc < MU; cc++)
+                    z[(long long)(c0 + cc) * zlen + c.b + row] = v[cc];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++) {
+                dacc[cc] = 0.;
+                df_zero(acc[cc]);
+            }
+        }
+        __syncwarp(); // every lane is done with stage s: hand it back
+        if (lane == 0)
+            mbar_arrive(emptyb(wid, s));
+        if (!have_nx) { // the producer was behind: wait for the next chunk now
+            if (!warp_wait(fullb(wid, s1), par1)) {
+                ok = false;
+                break;
+            }
+            cn = *sdesc(wid, s1);
+            if (cn.kind != kStreamStop)
+                gather(s1, cn, rnx, knx);
+        }
+        s   = s1;
+        par = par1;
+        c   = cn;
+        if (c.kind == kStreamStop)
+            break;
+#pragma unroll
+        for (int j = 0; j < kStreamCols / 32; j++) {
+            kk[j] = knx[j];
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                raw[j][cc] = rnx[j][cc];
+        }
+        stage_coefs(c, raw);
+    }
+    if (!ok && lane == 0)
+        atomicExch(status, 2);
+}
+
+// ---------------------------------------------------------------------------
 // phase 1: chunks of up to 16 whole columns of one tile (jlen <= 256 rows,
 // column-major): every column's dot product with the tile's x rows is
 // complete inside the chunk, so each chunk ends with a reduce-scatter sized
@@ -958,6 +1347,27 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
 }
 
 template <int MU>
+void launch_ws_mu(const StreamChunk *chunks, const int *units, int nunits, int *ticket, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+                  const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
+    constexpr int kCons            = WsCfg<MU>::kCons;
+    static unsigned long long done = 0; // devices whose shared-memory limit was raised
+    const int bytes                = kCons * WsSmem<MU>::kTotal;
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_ws_kernel<MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // every resident CTA, at most one per unit: small products leave room
+    // for concurrent work
+    const int nctas = std::max(1, std::min(WsCfg<MU>::kCtas * std::max(sms, 1), nunits));
+    phase2_ws_kernel<MU><<<nctas, 32 * (kCons + 1), bytes, st>>>(chunks, units, nunits, units + nunits + 1, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+template <int MU>
 void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
                     const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
@@ -1180,6 +1590,73 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
         c0 += n;
         g++;
     }
+}
+
+void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx,
+                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+    if (nunits <= 0)
+        return;
+    HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
+    int c0 = 0, g = 0;
+    while (c0 < mu) {
+        const int left = mu - c0;
+        const int n    = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        int *t         = tickets + std::min(g, 7);
+        if (g >= 7 && c0 > 0)
+            HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
+        switch (n) {
+        case 8: launch_ws_mu<8>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 4: launch_ws_mu<4>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 2: launch_ws_mu<2>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        default: launch_ws_mu<1>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        }
+        c0 += n;
+        g++;
+    }
+}
+
+std::vector<int> stream_units(const std::vector<StreamChunk> &ch, int target_units, int *nunits) {
+    // row chunks (first .. last flag) and their cost ~ time: DFMA chunks run
+    // on the FP64 pipe, slower per byte than the other kinds; every chunk has
+    // a fixed overhead
+    std::vector<int> rcs;
+    std::vector<double> cost;
+    for (std::size_t k = 0; k < ch.size(); k++) {
+        if ((ch[k].flags & kStreamFirst) || rcs.empty()) {
+            rcs.push_back((int)k);
+            cost.push_back(0.);
+        }
+        cost.back() += ch[k].bytes * (ch[k].kind == kStreamDfma ? 2.0 : 1.0) + 256.0;
+    }
+    rcs.push_back((int)ch.size());
+    const int nrc = (int)cost.size();
+    double total  = 0;
+    for (double c : cost)
+        total += c;
+    const double target = total / std::max(target_units, 1);
+    std::vector<int> u{0};
+    double acc = 0;
+    for (int i = 0; i < nrc; i++) {
+        acc += cost[i];
+        if (i + 1 < nrc && (acc >= target || i + 1 - u.back() >= kUnitRowChunks)) {
+            u.push_back(i + 1);
+            acc = 0;
+        }
+    }
+    if (nrc > 0)
+        u.push_back(nrc);
+    *nunits = (int)u.size() - 1;
+    // units (row-chunk indices), then the first chunk of every row chunk and the end
+    std::vector<int> out(u);
+    out.insert(out.end(), rcs.begin(), rcs.end());
+    return out;
+}
+
+int stream2_units_target() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return 4 * (sms > 0 ? sms : 152) * 6; // ~6 units per CTA: balance through the ticket
 }
 
 } // namespace htgpu

@@ -182,14 +182,25 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int
 
 /* Phase 1 (the V-side sums of every low-rank leaf) with one or two
  * right-hand sides: HTGPU_PHASE1_TILES (one warp per tile, DFMA and emulated
- * tiles as two concurrent kernels) or HTGPU_PHASE1_STREAM (tiles cut into
- * chunks that every warp streams through shared memory with bulk copies).
- * Results agree within the FP64 tolerance; the autotuner picks one.  No
- * counterpart in the reference. */
+ * tiles as two concurrent kernels) or HTGPU_PHASE1_STREAM (consecutive tile
+ * chunks staged into shared memory by a producer warp with bulk copies and
+ * shared by the CTA's consumer warps).  Results agree within the FP64
+ * tolerance; the autotuner picks one.  No counterpart in the reference. */
 #define HTGPU_PHASE1_TILES 0
 #define HTGPU_PHASE1_STREAM 1
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode);
+
+/* Phase 2 (the U-side and dense blocks, per row chunk): HTGPU_PHASE2_WARP
+ * (every warp streams its own chunks, claiming ranges of row chunks) or
+ * HTGPU_PHASE2_PRODUCER (a producer warp per CTA claims units of row chunks
+ * and feeds its consumer warps).  Bitwise equal results (the same per-row
+ * summation order); the autotuner picks one.  No counterpart in the
+ * reference. */
+#define HTGPU_PHASE2_WARP 0
+#define HTGPU_PHASE2_PRODUCER 1
+int htgpu_hmatrix_set_phase2_mode(htgpu_hmatrix h, int mode);
+int htgpu_hmatrix_get_phase2_mode(htgpu_hmatrix h, int *mode);
 
 /* Status word of the product kernels' bounded waits: 0, or 1/2/3 when a
  * wait for a pipeline stage ran out (the product's result is then not

@@ -243,6 +243,32 @@ def test_phase1_modes_parity(golden, mode):
     assert GH.device_status() == 0
 
 
+def test_phase2_modes_bitwise(golden):
+    """Both phase-2 kernels (per-warp streams, producer-fed CTAs) sum every
+    row in the same order: bitwise equal products for FP64 (every split),
+    the reduced precisions and several right-hand sides."""
+    g, meta = golden("sphere6000_k1")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    x3 = G.rhs(n, 3, seed=9)
+    for policy in ("fp64", "mixed", "bf16"):
+        GH.set_precision(policy)
+        for split in ((0, 0), (650, 650), (1000, 1000)):
+            GH.set_fp64_split(*split)
+            out = []
+            for mode in ("warp", "producer"):
+                GH.set_phase2_mode(mode)
+                assert GH.get_phase2_mode() == {"warp": H.PHASE2_WARP, "producer": H.PHASE2_PRODUCER}[mode]
+                out.append((GH.mvprod_global_to_global(g["x_mu1"]), GH.mvprod_global_to_global(x3, 3)))
+            assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1]), (policy, split)
+            if policy == "fp64":
+                assert rel(out[0][0], g["y_mu1"]) < FP64_TOL
+    with pytest.raises(ValueError):
+        GH.set_phase2_mode(2)
+    assert GH.device_status() == 0
+
+
 def test_autotune_keeps_parity(golden):
     g, meta = golden("sphere6000_k1")
     t = H.Cluster().build(g["xt"].shape[0], g["xt"])
