@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--phase1-mode", type=int, default=None, help="0 tile kernels, 1 streamed")
     p.add_argument("--mixed-split", type=int, default=None, help="mixed precision: DFMA per mille of the dense blocks")
     p.add_argument("--mixed-phase1-mode", type=int, default=None, help="mixed precision: 0 tile kernels, 1 streamed")
+    p.add_argument("--phase2-mode", type=int, default=None, help="FP64: 0 per-warp streams, 1 producer-fed")
+    p.add_argument("--mixed-phase2-mode", type=int, default=None, help="mixed precision: 0 per-warp streams, 1 producer-fed")
     return p.parse_args()
 
 
@@ -210,12 +212,29 @@ def run_gpu(args):
         barrier()
         return max_over_ranks(e0.elapsed_time(e1)), hm.last_launches()
 
+    def profiled_traffic(kernel, precision):
+        """DRAM bytes per launch of `kernel` from the committed ncu summaries
+        (lines "traffic: kernel=K precision=P n=N bytes_per_launch=B"), for
+        this workload size; None when no capture covers it"""
+        pdir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles")
+        if not os.path.isdir(pdir):
+            return None
+        for name in sorted(os.listdir(pdir)):
+            if not name.endswith(".md"):
+                continue
+            for line in open(os.path.join(pdir, name)):
+                if line.startswith("traffic:"):
+                    kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
+                    if kv.get("kernel") == kernel and kv.get("precision") == precision and int(kv.get("n", -1)) == n:
+                        return int(kv["bytes_per_launch"])
+        return None
+
     def describe(ms_total):
         """per-step numbers, phase breakdown and the dominant kernel's roofline"""
         ms_step = ms_total / args.steps
         ph = hm.profile(1, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
         pb = hm.phase_bytes(1)
-        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_cta_kernel", "phase2_warp_kernel", "zsum_kernel"]
+        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_cta_kernel", "phase2_warp_kernel" if hm.get_phase2_mode() == 0 else "phase2_ws_kernel", "zsum_kernel"]
         k = max(range(4), key=lambda i: ph[i])
         achieved = pb[k] / (ph[k] / 1e3) / 1e9
         total_bytes = sum(pb)
@@ -223,7 +242,7 @@ def run_gpu(args):
             "phase_ms": {"gather": ph[0], "phase1": ph[1], "phase2": ph[2], "sums": ph[3], "total": ph[4]},
             "phase_bytes": {"gather": pb[0], "phase1": pb[1], "phase2": pb[2], "sums": pb[3]},
             "whole_product": {"bytes": total_bytes, "GB_per_s": total_bytes / (ms_step / 1e3) / 1e9, "frac_of_hbm_peak": total_bytes / (ms_step / 1e3) / 1e9 / peak},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "kernel": names[k], "kernel_ms": ph[k], "algorithmic_bytes": pb[k],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": profiled_traffic(names[k], "fp64" if hm.precision_info()["policy"] == 0 else "mixed"), "kernel": names[k], "kernel_ms": ph[k], "algorithmic_bytes": pb[k],
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
         }
 
@@ -232,17 +251,20 @@ def run_gpu(args):
     time.sleep(0.5)  # let the sampler start before the timed regions
     # plain FP64 (autotuned DFMA / FP32-pipe split)
     hm.set_precision("fp64")
-    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode))
+    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode))
     if fixed:
         if args.fp64_split is not None:
             hm.set_fp64_split(*[int(v) for v in args.fp64_split.split(",")])
         if args.phase1_mode is not None:
             hm.set_phase1_mode(args.phase1_mode)
+        if args.phase2_mode is not None:
+            hm.set_phase2_mode(args.phase2_mode)
         tune64 = None
     else:
         tune64 = hm.autotune(1, 5)
     split = hm.get_fp64_split()
     p1mode64 = hm.get_phase1_mode()
+    p2mode64 = hm.get_phase2_mode()
     ms64, _ = timed_products()
     y64 = yd.cpu().numpy().copy()
     step64, d64 = describe(ms64)
@@ -254,6 +276,8 @@ def run_gpu(args):
             hm.set_fp64_split(split[0], args.mixed_split)
         if args.mixed_phase1_mode is not None:
             hm.set_phase1_mode(args.mixed_phase1_mode)
+        if args.mixed_phase2_mode is not None:
+            hm.set_phase2_mode(args.mixed_phase2_mode)
         tunem = None
     else:
         tunem = hm.autotune(1, 5)
@@ -312,9 +336,9 @@ def run_gpu(args):
         "rel_err_mixed_vs_fp64": err_mixed_vs_fp64,
         "speedup_mixed_vs_fp64": value / value64,
         "roofline": dm["roofline"], "whole_product": dm["whole_product"], "phase_ms": dm["phase_ms"], "phase_bytes": dm["phase_bytes"],
-        "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "dense_dfma_permille": splitm},
+        "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "phase2_mode": hm.get_phase2_mode(), "dense_dfma_permille": splitm},
         "fp64": {"value": value64, "unit": UNIT, "ms_per_step": step64, "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
-                 "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64}, "phase1_mode": p1mode64},
+                 "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64}, "phase1_mode": p1mode64, "phase2_mode": p2mode64},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk, "device_status": status,
         "rel_err_vs_dense_1000_rows": {"fp64": sampled_dense_error(pts, x, y64), "mixed": sampled_dense_error(pts, x, ym)},
         "aca_seconds": aca_seconds, "rank_predictor": predictor,
