@@ -51,6 +51,10 @@ def _load():
         "htgpu_cluster_get_perm": (i, [vp, vp]),
         "htgpu_cluster_get_nodes": (i, [vp, vp, vp]),
         "htgpu_block_tasks": (i, [vp, vp, d, vp, vp]),
+        "htgpu_block_tasks_sym": (i, [vp, vp, d, C.c_char, i, vp, vp]),
+        "htgpu_hmatrix_build_sym": (i, [vp, i, d, vp]),
+        "htgpu_hmatrix_set_symmetry": (i, [vp, C.c_char, C.c_char]),
+        "htgpu_hmatrix_set_compression": (i, [vp, i]),
         "htgpu_hmatrix_create": (i, [vp, vp, d, d, i, vp]),
         "htgpu_hmatrix_destroy": (i, [vp]),
         "htgpu_hmatrix_create_complex": (i, [vp, vp, d, d, i, vp]),
@@ -211,23 +215,26 @@ class Cluster:
             pass
 
 
-def block_tasks(t, s, eta):
-    """Block::build('N') local tasks (blocks.hpp:237-278): int[n,5] =
-    t.offset, t.size, s.offset, s.size, admissible."""
+def block_tasks(t, s, eta, UPLO="N", force_sym=False):
+    """Block::build(UPLO, force_sym) local tasks (blocks.hpp:237-278):
+    int[n,5] = t.offset, t.size, s.offset, s.size, admissible."""
     n = C.c_int()
-    _check(lib.htgpu_block_tasks(t.h, s.h, eta, C.byref(n), None))
+    u = UPLO.encode()
+    _check(lib.htgpu_block_tasks_sym(t.h, s.h, eta, u, int(force_sym), C.byref(n), None))
     out = np.empty((n.value, 5), np.int32)
-    _check(lib.htgpu_block_tasks(t.h, s.h, eta, C.byref(n), _ptr(out)))
+    _check(lib.htgpu_block_tasks_sym(t.h, s.h, eta, u, int(force_sym), C.byref(n), _ptr(out)))
     return out
 
 
+COMPRESSIONS = {"partialACA": 0, "sympartialACA": 1}
+
+
 class HMatrix:
-    """HMatrix<double> (hmatrix.hpp:44-270) with partialACA compression,
-    stored and applied on the GPU."""
+    """HMatrix<double> (hmatrix.hpp:44-270), stored and applied on the GPU;
+    partialACA compression unless set_compression says otherwise; symmetry
+    'S' with UPLO 'U' or 'L' stores one triangle."""
 
     def __init__(self, cluster_tree_t, cluster_tree_s, epsilon=1e-6, eta=10.0, symmetry="N", UPLO="N", device=0, dtype=np.float64):
-        if symmetry != "N" or UPLO != "N":
-            raise NotImplementedError("[Htool error] only non-symmetric storage ('N', 'N') is supported")
         self.t, self.s = cluster_tree_t, cluster_tree_s
         self.complex = np.dtype(dtype) == np.complex128
         h = C.c_void_p()
@@ -235,6 +242,23 @@ class HMatrix:
         _check(create(cluster_tree_t.h, cluster_tree_s.h, float(epsilon), float(eta), int(device), C.byref(h)))
         self.h = h
         self.epsilon, self.eta = epsilon, eta
+        if symmetry != "N" or UPLO != "N":
+            _check(lib.htgpu_hmatrix_set_symmetry(self.h, symmetry.encode(), UPLO.encode()))
+        self.symmetry, self.UPLO = symmetry, UPLO
+
+    def set_compression(self, compressor):
+        """'partialACA' (partialACA.hpp) or 'sympartialACA' (htool's default,
+        sympartialACA.hpp)."""
+        _check(lib.htgpu_hmatrix_set_compression(self.h, COMPRESSIONS[compressor] if isinstance(compressor, str) else int(compressor)))
+        return self
+
+    def build_sym(self, kernel, xt, kernel_param=0.0):
+        """HMatrix::build(generator, xt): one point array and the symmetric
+        block tree (hmatrix.hpp:343-400)."""
+        kid = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+        xt = np.ascontiguousarray(xt, dtype=np.float64)
+        _check(lib.htgpu_hmatrix_build_sym(self.h, kid, float(kernel_param), _ptr(xt)))
+        return self
 
     def set_maxblocksize(self, v):
         _check(lib.htgpu_hmatrix_set_maxblocksize(self.h, int(v)))

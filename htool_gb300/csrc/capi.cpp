@@ -119,13 +119,18 @@ int htgpu_cluster_get_nodes(htgpu_cluster c, int *node_i, double *node_d) {
     });
 }
 
-int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks, int *out) {
+int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks, int *out) { return htgpu_block_tasks_sym(t, s, eta, 'N', 0, ntasks, out); }
+
+int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char uplo, int force_sym, int *ntasks, int *out) {
     return guarded([&] {
         need(t, "target cluster");
         need(s, "source cluster");
         need(ntasks, "ntasks");
+        htgpu::require(uplo == 'N' || uplo == 'U' || uplo == 'L', "UPLO must be 'N', 'U' or 'L'");
         htgpu::BlockTreeParams p;
         p.eta      = eta;
+        p.uplo     = uplo;
+        p.sym_tree = uplo != 'N' || force_sym != 0;
         auto tasks = htgpu::build_local_tasks(*t->tree, *s->tree, p);
         *ntasks    = (int)tasks.size();
         if (out)
@@ -206,6 +211,31 @@ int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, con
         kd.id    = kernel_id;
         kd.param = kernel_param;
         h->h->build(kd, xt, xs);
+    });
+}
+
+int htgpu_hmatrix_build_sym(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(xt, "xt");
+        htgpu::KernelDesc kd;
+        kd.id    = kernel_id;
+        kd.param = kernel_param;
+        h->h->build(kd, xt, xt, true);
+    });
+}
+
+int htgpu_hmatrix_set_symmetry(htgpu_hmatrix h, char symmetry, char uplo) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_symmetry(symmetry, uplo);
+    });
+}
+
+int htgpu_hmatrix_set_compression(htgpu_hmatrix h, int compressor) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_compression(compressor);
     });
 }
 

@@ -322,19 +322,79 @@ struct BlockBuilder {
                 tasks.push_back({kt[q], ks[q], kadm[q] != 0});
         return false;
     }
+
+    // a block a symmetric tree may emit: exactly diagonal, or its target and
+    // source ranges apart (blocks.hpp:150)
+    static bool sym_ok(const ClusterNode &t, const ClusterNode &s) {
+        if (t.offset == s.offset)
+            return t.size == s.size;
+        return t.offset < s.offset ? s.offset - t.offset >= t.size : t.offset - s.offset >= s.size;
+    }
+
+    // Block::build_sym_block_tree (blocks.hpp:140-235): emitted blocks must be
+    // sym_ok; a block with two splittable clusters is cut into all pairs of
+    // sons, source sons outer
+    bool visit_sym(int t, int s, bool adm) {
+        const ClusterNode &tn = T.nodes[t], &sn = S.nodes[s];
+        if (adm && deep(tn, sn) && sym_ok(tn, sn)) {
+            tasks.push_back({t, s, true});
+            return false;
+        }
+        if (sn.nb_sons == 0 && tn.nb_sons == 0)
+            return true;
+        std::vector<int> kt, ks;
+        if (sn.nb_sons == 0) {
+            for (int p = 0; p < tn.nb_sons; p++) {
+                kt.push_back(tn.first_son + p);
+                ks.push_back(s);
+            }
+        } else if (tn.nb_sons == 0) {
+            for (int p = 0; p < sn.nb_sons; p++) {
+                kt.push_back(t);
+                ks.push_back(sn.first_son + p);
+            }
+        } else {
+            for (int l = 0; l < sn.nb_sons; l++)
+                for (int p = 0; p < tn.nb_sons; p++) {
+                    kt.push_back(tn.first_son + p);
+                    ks.push_back(sn.first_son + l);
+                }
+        }
+        const int ns = (int)kt.size();
+        std::vector<char> kadm(ns), quiet(ns);
+        bool all_quiet = true;
+        for (int q = 0; q < ns; q++) {
+            kadm[q]   = admissible(T.nodes[kt[q]], S.nodes[ks[q]], p.eta);
+            quiet[q]  = visit_sym(kt[q], ks[q], kadm[q]);
+            all_quiet = all_quiet && quiet[q];
+        }
+        const std::size_t bsize = (std::size_t)tn.size * (std::size_t)sn.size;
+        if (bsize <= p.maxblocksize && all_quiet && deep(tn, sn) && sym_ok(tn, sn))
+            return true;
+        for (int q = 0; q < ns; q++)
+            if (quiet[q])
+                tasks.push_back({kt[q], ks[q], kadm[q] != 0});
+        return false;
+    }
 };
 } // namespace
 
 std::vector<BlockTask> build_local_tasks(const ClusterTree &T, const ClusterTree &S, const BlockTreeParams &p) {
     BlockBuilder B{T, S, p, {}};
     bool adm = admissible(T.nodes[0], S.nodes[0], p.eta);
-    if (B.visit(0, 0, adm))
+    if (p.sym_tree ? B.visit_sym(0, 0, adm) : B.visit(0, 0, adm))
         B.tasks.push_back({0, 0, adm});
-    // local tasks of the single rank: targets of rank 0, ordered by offsets
+    // local tasks of the single rank: targets of rank 0 (in the triangle
+    // UPLO names), ordered by offsets (blocks.hpp:251-277)
     std::vector<BlockTask> local;
-    for (auto &b : B.tasks)
-        if (T.nodes[b.t].rank == 0)
-            local.push_back(b);
+    for (auto &b : B.tasks) {
+        if (T.nodes[b.t].rank != 0)
+            continue;
+        const int to = T.nodes[b.t].offset, so = S.nodes[b.s].offset;
+        if ((p.uplo == 'L' && so > to) || (p.uplo == 'U' && so < to))
+            continue;
+        local.push_back(b);
+    }
     std::sort(local.begin(), local.end(), [&](const BlockTask &a, const BlockTask &b) {
         int ta = T.nodes[a.t].offset, tb = T.nodes[b.t].offset;
         if (ta != tb)

@@ -85,11 +85,56 @@ HMatrix::~HMatrix() {
         cudaStreamDestroy(stream_);
 }
 
-void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
+void HMatrix::set_symmetry(char symmetry, char uplo) {
+    // the combinations HMatrix's constructor accepts (hmatrix.hpp:116-121);
+    // 'H' needs a complex type
+    require((symmetry == 'N' && uplo == 'N') || (symmetry == 'S' && (uplo == 'U' || uplo == 'L')) || (symmetry == 'H' && (uplo == 'U' || uplo == 'L')),
+            "Invalid arguments to create HMatrix: symmetry must be 'N' with UPLO 'N', or 'S'/'H' with UPLO 'U' or 'L'");
+    require(symmetry != 'H', "Hermitian H-matrices ('H') are not available", 2);
+    if (symmetry == 'S')
+        require(T->n == S->n && T->perm == S->perm, "a symmetric H-matrix needs the same target and source cluster tree");
+    symmetry_ = symmetry;
+    uplo_     = uplo;
+}
+
+void HMatrix::set_compression(int compressor) {
+    require(compressor == 0 || compressor == 1, "compression must be 0 (partialACA) or 1 (sympartialACA)");
+    compression_ = compressor;
+}
+
+// transposed twins of the off-diagonal leaves of a symmetric H-matrix,
+// after htool's own leaves: the twin of a low-rank leaf reads the same
+// factors with U and V^T exchanged, the twin of a dense leaf is generated
+// (the built-in generators are symmetric bit for bit)
+void HMatrix::add_symmetric_twins(std::vector<LeafSrc> &lr_src) {
+    nlr_stored_ = (int)lr_h.size();
+    ndn_stored_ = (int)dn_h.size();
+    for (int l = 0; l < nlr_stored_; l++) {
+        const LrLeaf L = lr_h[l];
+        if (L.oi == L.oj)
+            continue;
+        LrLeaf W = L;
+        W.oi     = L.oj;
+        W.oj     = L.oi;
+        W.m      = L.n;
+        W.n      = L.m;
+        lr_h.push_back(W);
+        lr_src.push_back({lr_src[l].buf, lr_src[l].sv, lr_src[l].su});
+    }
+    for (int d = 0; d < ndn_stored_; d++) {
+        const DenseLeaf D = dn_h[d];
+        if (D.oi != D.oj)
+            dn_h.push_back({D.oj, D.oi, D.n, D.m});
+    }
+}
+
+void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bool force_sym) {
     if (complex_)
         require(kd.id == 2, "a complex H-matrix needs the Helmholtz device generator (id 2)", 2);
     else
         require(kd.id == 0 || kd.id == 1, "device generator id must be 0 (1/(1e-5+r)) or 1 (Laplace) for a real H-matrix", 2);
+    require(!complex_ || (compression_ == 0 && symmetry_ == 'N'), "complex H-matrices take partialACA and no symmetry", 2);
+    nlr_stored_ = ndn_stored_ = -1;
     // block tree and ACA on the trees of the points; a complex H-matrix is
     // stored in real form on doubled trees (T, S), its leaves scaled by f
     const ClusterTree &Ta = complex_ ? *Tz_ : *T, &Sa = complex_ ? *Sz_ : *S;
@@ -100,6 +145,8 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
     samples_y_.clear();
     const double t0 = now();
     bp.eta          = eta_;
+    bp.sym_tree     = uplo_ != 'N' || force_sym; // Block::build (blocks.hpp:237-246)
+    bp.uplo         = uplo_;
     std::vector<BlockTask> tasks = build_local_tasks(Ta, Sa, bp);
     st_.block_tree_seconds       = now() - t0;
 
@@ -127,19 +174,33 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
     std::vector<std::pair<int, int>> dense_ts;
     std::vector<int> pending;
 
+    // sons of a rejected block: ComputeAdmissibleBlock splits the larger
+    // cluster (hmatrix.hpp:525-606); ComputeAdmissibleBlocksSym (symmetric
+    // H-matrices, hmatrix.hpp:610-700) splits both, source sons outer
+    const bool sym_rec = symmetry_ != 'N';
     std::function<void(int)> split = [&](int id) {
         const ClusterNode &tn = Ta.nodes[reqs[id].t], &sn = Sa.nodes[reqs[id].s];
         reqs[id].state = 2;
         if (tn.nb_sons == 0 && sn.nb_sons == 0)
             return;
-        const bool by_t = sn.nb_sons == 0 ? true : (tn.nb_sons == 0 ? false : tn.size > sn.size);
-        const int ns    = by_t ? tn.nb_sons : sn.nb_sons;
-        const int first = by_t ? tn.first_son : sn.first_son;
+        std::vector<std::pair<int, int>> ts;
+        if (sym_rec && tn.nb_sons > 0 && sn.nb_sons > 0) {
+            for (int l = 0; l < sn.nb_sons; l++)
+                for (int p = 0; p < tn.nb_sons; p++)
+                    ts.push_back({tn.first_son + p, sn.first_son + l});
+        } else {
+            const bool by_t = sn.nb_sons == 0 ? true : (tn.nb_sons == 0 ? false : (sym_rec ? false : tn.size > sn.size));
+            const int ns    = by_t ? tn.nb_sons : sn.nb_sons;
+            const int first = by_t ? tn.first_son : sn.first_son;
+            for (int p = 0; p < ns; p++)
+                ts.push_back({by_t ? first + p : reqs[id].t, by_t ? reqs[id].s : first + p});
+        }
+        const int ns = (int)ts.size();
         std::vector<int> mine(ns);
         for (int p = 0; p < ns; p++) {
             Req r;
-            r.t   = by_t ? first + p : reqs[id].t;
-            r.s   = by_t ? reqs[id].s : first + p;
+            r.t   = ts[p].first;
+            r.s   = ts[p].second;
             r.adm = admissible(Ta.nodes[r.t], Sa.nodes[r.s], eta_);
             mine[p] = (int)reqs.size();
             reqs.push_back(r);
@@ -213,38 +274,48 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
                     }
                 }
             }
-            // a slice of requests whose scratch fits the budget
-            std::vector<AcaBlock> blocks;
-            std::vector<int> ids;
+            // a slice of requests whose scratch fits the budget.  With
+            // sympartialACA a block whose target comes before its source is
+            // compressed as its mirror (rows of s, columns of t, first row
+            // nearest the centre of s: sympartialACA.hpp:33-60) and its
+            // factors exchanged; these blocks follow the others in the slice
+            // and run as a second launch on swapped point arrays
+            std::vector<AcaBlock> blocks, mirrored;
+            std::vector<int> ids, ids_m;
             long long sc = 0, fl = 0;
             while (pos < pending.size()) {
                 Req &r = reqs[pending[pos]];
                 const ClusterNode &tn = Ta.nodes[r.t], &sn = Sa.nodes[r.s];
-                const int M = tn.size, N = sn.size;
+                const bool mir = compression_ == 1 && tn.offset < sn.offset;
+                const ClusterNode &rn = mir ? sn : tn, &cn = mir ? tn : sn;
+                const int M = rn.size, N = cn.size;
                 int qmax    = max_profitable_rank(M, N);
                 if (r.cap == 0)
                     r.cap = std::max(1, std::min(qmax, kDefaultCap));
                 long long need = (long long)f * r.cap * (M + N); // doubles (complex entries take two)
-                if (!blocks.empty() && sc + need > budget)
+                if ((!blocks.empty() || !mirrored.empty()) && sc + need > budget)
                     break;
                 AcaBlock b;
                 b.M       = M;
                 b.N       = N;
-                b.row_off = tn.offset;
-                b.col_off = sn.offset;
+                b.row_off = rn.offset;
+                b.col_off = cn.offset;
                 b.cap     = r.cap;
                 b.pad     = 0;
                 b.u_off   = sc;
                 b.v_off   = sc + (long long)f * M * r.cap;
                 b.flag_off = fl;
                 for (int d = 0; d < 3; d++)
-                    b.ctr[d] = tn.ctr[d];
+                    b.ctr[d] = rn.ctr[d];
                 sc += need;
                 fl += M + N;
-                blocks.push_back(b);
-                ids.push_back(pending[pos]);
+                (mir ? mirrored : blocks).push_back(b);
+                (mir ? ids_m : ids).push_back(pending[pos]);
                 pos++;
             }
+            const int n_direct = (int)blocks.size();
+            blocks.insert(blocks.end(), mirrored.begin(), mirrored.end());
+            ids.insert(ids.end(), ids_m.begin(), ids_m.end());
             DevBuf<AcaBlock> dblocks;
             DevBuf<double> scratch;
             DevBuf<unsigned char> flags;
@@ -257,8 +328,12 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
             dranks.alloc(blocks.size());
             if (complex_)
                 launch_partial_aca_z(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
-            else
-                launch_partial_aca(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+            else {
+                if (n_direct > 0)
+                    launch_partial_aca(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+                if ((int)blocks.size() > n_direct)
+                    launch_partial_aca(dblocks.p + n_direct, (int)blocks.size() - n_direct, dxs.p, dxt.p, aca_ps, aca_pt, kd, eps_, scratch.p, flags.p, dranks.p + n_direct, stream_);
+            }
             std::vector<int> ranks(blocks.size());
             HTGPU_CUDA(cudaMemcpyAsync(ranks.data(), dranks.p, sizeof(int) * ranks.size(), cudaMemcpyDeviceToHost, stream_));
             HTGPU_CUDA(cudaStreamSynchronize(stream_));
@@ -291,7 +366,10 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
                     it.dst_v = packed + (long long)f * f * it.M * r;
                     packed += (long long)f * f * r * (it.M + it.N);
                     items.push_back(it);
-                    acc.push_back({id, round, r, it.dst_u, it.dst_v});
+                    if ((int)b < n_direct)
+                        acc.push_back({id, round, r, it.dst_u, it.dst_v});
+                    else // mirrored: U of the block is V^T of the mirror and V^T its U
+                        acc.push_back({id, round, r, it.dst_v, it.dst_u});
                 } else if (r == -1) {
                     st_.false_positive++;
                     split(id);
@@ -381,6 +459,8 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
     dn_h.clear();
     for (auto &d : dense_ts)
         dn_h.push_back({f * Ta.nodes[d.first].offset, f * Sa.nodes[d.second].offset, f * Ta.nodes[d.first].size, f * Sa.nodes[d.second].size});
+    if (symmetry_ == 'S')
+        add_symmetric_twins(lr_src);
     std::vector<const double *> bufs;
     for (auto &b : round_bufs)
         bufs.push_back(b->p);
@@ -389,6 +469,8 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs) {
 }
 
 void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dn) {
+    require(symmetry_ == 'N', "adopting leaves of a symmetric H-matrix is not available", 2);
+    nlr_stored_ = ndn_stored_ = -1;
     HTGPU_CUDA(cudaSetDevice(device_));
     lr_h.clear();
     dn_h.clear();
@@ -1249,6 +1331,10 @@ void HMatrix::phase_bytes(int mu, long long *b) const {
 }
 
 void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st) {
+    if (symmetry_ == 'S') { // H^T = H
+        mvprod(in, out, mu, host_ptrs, false, st);
+        return;
+    }
     require(mu >= 1, "number of right-hand sides must be positive");
     require(!complex_, "transposed products of complex H-matrices are not supported", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
@@ -1299,14 +1385,14 @@ void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptr
 }
 
 void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {
-    for (std::size_t b = 0; b < lr_h.size(); b++) {
+    for (int b = 0; b < n_lowrank(); b++) {
         lr_desc[5 * b]     = lr_h[b].oi;
         lr_desc[5 * b + 1] = lr_h[b].oj;
         lr_desc[5 * b + 2] = lr_h[b].m;
         lr_desc[5 * b + 3] = lr_h[b].n;
         lr_desc[5 * b + 4] = lr_h[b].r;
     }
-    for (std::size_t b = 0; b < dn_h.size(); b++) {
+    for (int b = 0; b < n_dense(); b++) {
         d_desc[4 * b]     = dn_h[b].oi;
         d_desc[4 * b + 1] = dn_h[b].oj;
         d_desc[4 * b + 2] = dn_h[b].m;
@@ -1320,21 +1406,25 @@ void HMatrix::export_factors(double *uv, double *dn) {
     std::vector<double> host(std::max<long long>(arena_len, 1));
     if (arena_len)
         HTGPU_CUDA(cudaMemcpy(host.data(), fac.p, sizeof(double) * arena_len, cudaMemcpyDeviceToHost));
+    // htool's leaves only (a symmetric H-matrix's transposed twins follow them)
+    const int nl = n_lowrank(), nd = n_dense();
     std::vector<long long> u_at(lr_h.size()), v_at(lr_h.size()), d_at(dn_h.size());
     long long o = 0;
-    for (std::size_t l = 0; l < lr_h.size(); l++) {
+    for (int l = 0; l < nl; l++) {
         u_at[l] = o;
         o += (long long)lr_h[l].m * lr_h[l].r;
         v_at[l] = o;
         o += (long long)lr_h[l].n * lr_h[l].r;
     }
     o = 0;
-    for (std::size_t d = 0; d < dn_h.size(); d++) {
+    for (int d = 0; d < nd; d++) {
         d_at[d] = o;
         o += (long long)dn_h[d].m * dn_h[d].n;
     }
     if (uv)
         for (auto &it : p1_h) {
+            if (it.leaf >= nl)
+                continue;
             const LrLeaf &L = lr_h[it.leaf];
             for (int k = 0; k < L.r; k++)
                 for (int jj = 0; jj < it.jlen; jj++)
@@ -1346,6 +1436,8 @@ void HMatrix::export_factors(double *uv, double *dn) {
         for (int c = it.cbeg; c < it.cend; c++) {
             const int leaf      = c_leaf[c];
             const P2Contrib &pc = c_h[c];
+            if (leaf >= nl || (leaf < 0 && ~leaf >= nd))
+                continue;
             if (leaf >= 0 && uv) {
                 const LrLeaf &L = lr_h[leaf];
                 for (int k = 0; k < L.r; k++)
@@ -1385,13 +1477,16 @@ std::map<std::string, std::string> HMatrix::infos() const {
     const std::size_t big = (std::size_t)std::max(nr, nc);
     std::size_t dmax = 0, dmin = big, lmax = 0, lmin = big, rmax = 0, rmin = big;
     double dmean = 0, lmean = 0, rmean = 0;
-    for (auto &D : dn_h) {
+    // htool's leaves (a symmetric H-matrix's transposed twins are not counted)
+    const std::vector<DenseLeaf> dns(dn_h.begin(), dn_h.begin() + n_dense());
+    const std::vector<LrLeaf> lrs(lr_h.begin(), lr_h.begin() + n_lowrank());
+    for (auto &D : dns) {
         std::size_t s = (std::size_t)D.m * D.n / (f * f);
         dmax          = std::max(dmax, s);
         dmin          = std::min(dmin, s);
         dmean += s;
     }
-    for (auto &L : lr_h) {
+    for (auto &L : lrs) {
         std::size_t s = (std::size_t)L.m * L.n / (f * f), r = (std::size_t)L.r / f;
         lmax          = std::max(lmax, s);
         lmin          = std::min(lmin, s);
@@ -1400,15 +1495,15 @@ std::map<std::string, std::string> HMatrix::infos() const {
         rmin = std::min(rmin, r);
         rmean += r;
     }
-    const int nd = (int)dn_h.size(), nl = (int)lr_h.size();
+    const int nd = (int)dns.size(), nl = (int)lrs.size();
     dmean = nd ? dmean / nd : 0;
     lmean = nl ? lmean / nl : 0;
     rmean = nl ? rmean / nl : 0;
     double compressed = 0;
-    for (auto &L : lr_h)
+    for (auto &L : lrs)
         compressed += (double)L.r * ((double)L.m + (double)L.n);
-    for (auto &D : dn_h)
-        compressed += (double)D.m * (double)D.n;
+    for (auto &D : dns) // a symmetric H-matrix counts its square diagonal blocks once (hmatrix.hpp:1615-1619)
+        compressed += (symmetry_ != 'N' && D.oi == D.oj && D.m == D.n) ? ((double)D.m * ((double)D.n + 1)) / 2 : (double)D.m * (double)D.n;
     const double uncompressed = (double)((long)nr) * nc;
     m["Source_size"]              = inum(nci);
     m["Target_size"]              = inum(nri);

@@ -27,9 +27,21 @@ class HMatrix {
     bool is_complex() const { return complex_; }
     ~HMatrix();
 
-    // HMatrix::build(gen, xt, xs) with partialACA and a built-in device
-    // generator (include/htool/types/hmatrix.hpp:286-341)
-    void build(const KernelDesc &kd, const double *xt, const double *xs);
+    // HMatrix::build(gen, xt, xs) with a built-in device generator
+    // (include/htool/types/hmatrix.hpp:286-341); force_sym: the one-array
+    // build(gen, xt) (hmatrix.hpp:343-400), which always uses the symmetric
+    // block tree
+    void build(const KernelDesc &kd, const double *xt, const double *xs, bool force_sym = false);
+
+    // HMatrix(t, s, eps, eta, symmetry, UPLO) (hmatrix.hpp:115-122): 'N'/'N'
+    // or 'S' with 'U' or 'L' (one triangle stored, applied with its
+    // transpose; needs t and s to be the same tree); compression 0
+    // partialACA, 1 sympartialACA (lrmat/sympartialACA.hpp:28-210)
+    void set_symmetry(char symmetry, char uplo);
+    char symmetry() const { return symmetry_; }
+    char uplo() const { return uplo_; }
+    void set_compression(int compressor);
+    int compression() const { return compression_; }
 
     // ACA scratch: device bytes one slice of blocks may use (0: 60% of the
     // free memory), and an optional rank predictor that sizes every block's
@@ -62,8 +74,10 @@ class HMatrix {
 
     int nb_rows() const { return nr; }
     int nb_cols() const { return nc; }
-    int n_lowrank() const { return (int)lr_h.size(); }
-    int n_dense() const { return (int)dn_h.size(); }
+    // htool's leaves: a symmetric H-matrix also applies transposed twins of
+    // its off-diagonal leaves, kept after these in lr_h / dn_h
+    int n_lowrank() const { return nlr_stored_ >= 0 ? nlr_stored_ : (int)lr_h.size(); }
+    int n_dense() const { return ndn_stored_ >= 0 ? ndn_stored_ : (int)dn_h.size(); }
     void leaf_descriptors(int *lr_desc, int *d_desc) const;
     void export_factors(double *uv, double *dense);
     std::map<std::string, std::string> infos() const;
@@ -203,6 +217,10 @@ class HMatrix {
     int n_sctas_ = 0, n_ranges_ = 0, n_ranges_m_ = 0;
     long long n_chunks_ = 0, n_chunks_m_ = 0;
     int p1_mode_ = 0;
+    char symmetry_ = 'N', uplo_ = 'N';
+    int compression_ = 0;
+    int nlr_stored_ = -1, ndn_stored_ = -1; // htool's leaves when twins follow them
+    void add_symmetric_twins(std::vector<LeafSrc> &lr_src);
     int p2_mode_ = 0;                  // 0: per-warp streams, 1: producer-fed CTAs
     DevBuf<int> su_d, sum_d;           // phase-2 units (producer-fed) of the FP64 / reduced chunk lists
     int n_units_ = 0, n_units_m_ = 0;

@@ -65,6 +65,8 @@ struct BlockTreeParams {
     double eta = 10;
     int mintargetdepth = 0, minsourcedepth = 0;
     std::size_t maxblocksize = 1000000;
+    bool sym_tree = false; // Block::build_sym_block_tree (blocks.hpp:140-235)
+    char uplo     = 'N';   // local tasks of one triangle: 'U' s.offset >= t.offset, 'L' s.offset <= t.offset
 };
 
 bool admissible(const ClusterNode &t, const ClusterNode &s, double eta);

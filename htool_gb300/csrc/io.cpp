@@ -157,20 +157,21 @@ ClusterTree read_cluster(const std::string &perm_file, const std::string &tree_f
 }
 
 void HMatrix::save(const std::string &path) {
+    require(symmetry_ == 'N', "dumps of symmetric H-matrices are not available", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
-    std::vector<int> lr(5 * lr_h.size()), dn(4 * dn_h.size());
+    std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
     long long nuv = 0, ndd = 0;
-    for (auto &L : lr_h)
-        nuv += (long long)L.r * (L.m + L.n);
-    for (auto &D : dn_h)
-        ndd += (long long)D.m * D.n;
+    for (int l = 0; l < n_lowrank(); l++)
+        nuv += (long long)lr_h[l].r * (lr_h[l].m + lr_h[l].n);
+    for (int d = 0; d < n_dense(); d++)
+        ndd += (long long)dn_h[d].m * dn_h[d].n;
     std::vector<double> uv(std::max<long long>(nuv, 1)), dd(std::max<long long>(ndd, 1));
     export_factors(uv.data(), dd.data());
     std::ofstream f(path, std::ios::binary);
     require((bool)f, "cannot write " + path, 3);
     const std::uint32_t version = 1;
-    const std::int64_t hdr[4]   = {nr, nc, (std::int64_t)lr_h.size(), (std::int64_t)dn_h.size()};
+    const std::int64_t hdr[4]   = {nr, nc, (std::int64_t)n_lowrank(), (std::int64_t)n_dense()};
     const double par[2]         = {eps_, eta_};
     const std::uint64_t hash[2] = {fnv1a(T->perm), fnv1a(S->perm)};
     f.write(kMagic, 8);
@@ -191,21 +192,22 @@ void HMatrix::save(const std::string &path) {
 // (rank -1), each list in htool's order; a complex H-matrix reports its
 // complex sizes and ranks (the real form doubles them)
 void HMatrix::save_plot(const std::string &outputname) const {
-    std::vector<int> lr(5 * lr_h.size()), dn(4 * dn_h.size());
+    std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
     const int f = complex_ ? 2 : 1;
     const std::string path = outputname + "_0.csv";
     std::ofstream out(path);
     require((bool)out, "cannot write " + path, 3);
     out << nr / f << "," << nc / f << "\n";
-    for (std::size_t d = 0; d < dn_h.size(); d++)
+    for (int d = 0; d < n_dense(); d++)
         out << dn[4 * d] / f << "," << dn[4 * d + 2] / f << "," << dn[4 * d + 1] / f << "," << dn[4 * d + 3] / f << "," << -1 << "\n";
-    for (std::size_t l = 0; l < lr_h.size(); l++)
+    for (int l = 0; l < n_lowrank(); l++)
         out << lr[5 * l] / f << "," << lr[5 * l + 2] / f << "," << lr[5 * l + 1] / f << "," << lr[5 * l + 3] / f << "," << lr[5 * l + 4] / f << "\n";
     require((bool)out, "writing " + path + " failed", 3);
 }
 
 void HMatrix::load(const std::string &path) {
+    require(symmetry_ == 'N', "dumps of symmetric H-matrices are not available", 2);
     std::ifstream f(path, std::ios::binary);
     require((bool)f, "cannot open " + path);
     char magic[8];

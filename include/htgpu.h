@@ -77,6 +77,12 @@ int htgpu_cluster_get_nodes(htgpu_cluster c, int *node_i, double *node_d);
  * t.offset, t.size, s.offset, s.size, admissible. */
 int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks, int *out);
 
+/* The same for Block::build(UPLO, force_sym) (blocks.hpp:237-278): uplo 'U' /
+ * 'L' keeps the tasks of one triangle (s.offset >= t.offset / <=); with
+ * uplo != 'N' or force_sym the tree is build_sym_block_tree's
+ * (blocks.hpp:140-235). */
+int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char uplo, int force_sym, int *ntasks, int *out);
+
 /* ---------------------------------------------------------------------------
  * H-matrices (double precision, non-symmetric storage)
  * -------------------------------------------------------------------------*/
@@ -111,6 +117,27 @@ int htgpu_hmatrix_set_minsourcedepth(htgpu_hmatrix h, unsigned int depth);
  * htool's rejection and recursion rules (hmatrix.hpp:504-607).  xt / xs are
  * the host point arrays used to build the cluster trees. */
 int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt, const double *xs);
+
+/* HMatrix<double>::build(mat, xt) (hmatrix.hpp:343-400): one point array
+ * for rows and columns and the symmetric block tree (force_sym). */
+int htgpu_hmatrix_build_sym(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt);
+
+/* Before a build: the symmetry and UPLO arguments of HMatrix's constructor
+ * (hmatrix.hpp:115-122): 'N' with 'N', or 'S' with 'U' / 'L' -- one triangle
+ * of the block tree is stored (ComputeAdmissibleBlocksSym recursion,
+ * hmatrix.hpp:610-700) and products apply every stored off-diagonal leaf and
+ * its transpose (hmatrix.hpp:844-911); t and s must be the same tree.  'H'
+ * (complex Hermitian) is not available. */
+int htgpu_hmatrix_set_symmetry(htgpu_hmatrix h, char symmetry, char uplo);
+
+/* Before a build: set_compression (hmatrix.hpp:220) with
+ * HTGPU_COMPRESSION_PARTIAL_ACA (lrmat/partialACA.hpp:39-171, the default of
+ * this library) or HTGPU_COMPRESSION_SYM_PARTIAL_ACA (lrmat/sympartialACA.hpp:
+ * 28-210, htool's default: a block whose target comes before its source is
+ * compressed as its mirror); real H-matrices only. */
+#define HTGPU_COMPRESSION_PARTIAL_ACA 0
+#define HTGPU_COMPRESSION_SYM_PARTIAL_ACA 1
+int htgpu_hmatrix_set_compression(htgpu_hmatrix h, int compressor);
 
 /* Adopt leaves built elsewhere, e.g. exported from an htool HMatrix through
  * get_MyFarFieldMats / get_MyNearFieldMats (hmatrix.hpp:193-198) and

@@ -266,15 +266,19 @@ class Oracle:
             self._L.ref_block_tasks(ct.h, cs.h, eta, b"N", 0, _ptr(out))
         return out
 
-    def hmatrix(self, ct, cs, xt, xs, kernel, eps=1e-6, eta=10.0):
-        """Non-symmetric HMatrix<double> with partialACA."""
+    def hmatrix(self, ct, cs, xt, xs, kernel, eps=1e-6, eta=10.0, compressor=0, symmetry="N", uplo="N", symbuild=False):
+        """HMatrix<double>: non-symmetric with partialACA by default; the
+        reference also takes sympartialACA (compressor 1), symmetry 'S' with
+        UPLO 'U' / 'L', and the one-array build(mat, xt) (symbuild)."""
         xt = np.ascontiguousarray(xt, dtype=np.float64)
         xs = np.ascontiguousarray(xs, dtype=np.float64)
         nr, nc = xt.shape[0], xs.shape[0]
         if self.kind == "port":
+            if compressor != 0 or symmetry != "N" or uplo != "N" or symbuild:
+                raise NotImplementedError("the port restates the non-symmetric partialACA build only")
             h = self._L.orc_hmatrix_build(ct.h, cs.h, nr, _ptr(xt), nc, _ptr(xs), kernel, eps, eta)
         else:
-            h = self._L.ref_hmatrix_build_d(ct.h, cs.h, nr, _ptr(xt), nc, _ptr(xs), kernel, eps, eta, 0, b"N", b"N", 0)
+            h = self._L.ref_hmatrix_build_d(ct.h, cs.h, nr, _ptr(xt), nc, _ptr(xs), kernel, eps, eta, int(compressor), symmetry.encode(), uplo.encode(), int(bool(symbuild)))
             if not h:
                 raise RuntimeError(self._L.ref_last_error().decode())
         return HMat(self, h, nr, nc, (xt, xs, ct, cs))

@@ -17,6 +17,7 @@ Usage (needs the upstream sources, i.e. only in the build container):
     make -C oracle/refbuild REF=/root/reference/include
     python tests/golden/make_golden.py          # everything but the leaf maps
     python tests/golden/make_golden.py plot     # the save_plot leaf maps only
+    python tests/golden/make_golden.py sym      # the symmetric / sympartialACA builds only
 """
 import ctypes as C
 import hashlib
@@ -152,6 +153,43 @@ def main():
     R._L.ref_cluster_save(ct.h, os.path.join(OUT, "cyl4000_cluster").encode())
 
 
+SYM_CASES = [
+    # name, geometry, kernel, compressor (0 partialACA, 1 sympartialACA), symmetry, UPLO, one-array build
+    ("cyl4000_k0_symU", "cyl", 0, 1, "S", "U", True),
+    ("cyl4000_k0_symL", "cyl", 0, 1, "S", "L", True),
+    ("sphere6000_k1_symU", "sph", 1, 1, "S", "U", True),
+    ("cyl4000_k0_symaca", "cyl", 0, 1, "N", "N", False),
+    ("sphere6000_k1_forcesym", "sph", 1, 1, "N", "N", True),
+]
+
+
+def sym_cases():
+    """symmetric H-matrices (one triangle stored, sympartialACA) and the
+    sympartialACA / symmetric-tree variants of non-symmetric ones, built by
+    upstream: leaf lists, task lists, SHA-256 of the factors, products"""
+    R = Oracle("reference")
+    R.set_num_threads(1)
+    geo = {"cyl": G.cylinder(4000, seed=1), "sph": G.sphere(6000, seed=1)}
+    for name, g, kernel, comp, sym, uplo, one in SYM_CASES:
+        pts = geo[g]
+        ct = R.cluster(pts)
+        H = R.hmatrix(ct, ct, pts, pts, kernel, 1e-6, 10.0, compressor=comp, symmetry=sym, uplo=uplo, symbuild=one)
+        lr, dn, uv, dd = H.factors()
+        k = R._L.ref_block_tasks(ct.h, ct.h, 10.0, uplo.encode(), int(one), None)
+        tasks = np.empty((k, 5), np.int32)
+        R._L.ref_block_tasks(ct.h, ct.h, 10.0, uplo.encode(), int(one), tasks.ctypes.data)
+        data = dict(xt=pts, lr=lr, dense=dn, tasks=tasks)
+        for mu in (1, 3):
+            x = G.rhs(pts.shape[0], mu, seed=2)
+            data["x_mu%d" % mu] = x
+            data["y_mu%d" % mu] = H.mvprod(x, mu)
+        meta = dict(kernel=kernel, eps=1e-6, eta=10.0, compressor=comp, symmetry=sym, uplo=uplo, one_array_build=one, sha_uv=sha(uv), sha_dense=sha(dd), infos=R.infos(H))
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
+        with open(os.path.join(OUT, name + ".json"), "w") as f:
+            json.dump(meta, f, indent=1, sort_keys=True)
+        print(name, "tasks", k, "leaves", lr.shape[0], dn.shape[0])
+
+
 def plot_cases():
     """htool's leaf maps (HMatrix::save_plot) of the configuration-1 and
     Helmholtz fixtures, written by upstream itself (one thread)"""
@@ -175,5 +213,7 @@ def plot_cases():
 if __name__ == "__main__":
     if sys.argv[1:] == ["plot"]:
         plot_cases()
+    elif sys.argv[1:] == ["sym"]:
+        sym_cases()
     else:
         main()

@@ -1,0 +1,88 @@
+"""Symmetric H-matrices and sympartialACA, against upstream's own builds.
+
+Fixtures (tests/golden/*_sym*.npz, make_golden.py sym) hold what upstream
+htool produced for symmetric storage ('S' with UPLO 'U' / 'L', one triangle
+of the block tree, ComputeAdmissibleBlocksSym, sympartialACA), for
+sympartialACA on a non-symmetric build and for the symmetric block tree of
+the one-array build(mat, xt): task lists, leaf lists, SHA-256 of the factors,
+products."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import htool_gb300 as H
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+CASES = ["cyl4000_k0_symU", "cyl4000_k0_symL", "sphere6000_k1_symU", "cyl4000_k0_symaca", "sphere6000_k1_forcesym"]
+FP64_TOL = 1e-12
+
+
+def load(name):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    return g, meta
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_block_tree_matches_upstream(name):
+    """Block::build(UPLO, force_sym) task lists are upstream's exactly"""
+    g, meta = load(name)
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    tasks = H.block_tasks(t, t, meta["eta"], meta["uplo"], meta["one_array_build"])
+    assert np.array_equal(tasks, g["tasks"])
+
+
+@pytest.mark.gpu
+def test_symmetry_arguments_checked():
+    from htool_gb300 import geometry as G
+
+    pts = G.cylinder(500, seed=1)
+    t = H.Cluster().build(500, pts)
+    s = H.Cluster().build(400, G.cylinder(400, seed=2))
+    for sym, uplo in (("N", "U"), ("S", "N"), ("X", "N")):
+        with pytest.raises(ValueError):
+            H.HMatrix(t, t, 1e-6, 10.0, symmetry=sym, UPLO=uplo)
+    with pytest.raises(ValueError):  # one tree for a symmetric matrix
+        H.HMatrix(t, s, 1e-6, 10.0, symmetry="S", UPLO="U")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_build_and_product_match_upstream(name):
+    g, meta = load(name)
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    hm = H.HMatrix(t, t, meta["eps"], meta["eta"], symmetry=meta["symmetry"], UPLO=meta["uplo"])
+    hm.set_compression(meta["compressor"])
+    if meta["one_array_build"]:
+        hm.build_sym(meta["kernel"], g["xt"])
+    else:
+        hm.build(meta["kernel"], g["xt"], g["xt"])
+    lr, dn = hm.get_leaves()
+    assert np.array_equal(lr, g["lr"]) and np.array_equal(dn, g["dense"])
+    info = hm.get_infos()
+    for key in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_min", "Dense_block_size_max", "Low_rank_block_size_max"):
+        assert info[key] == meta["infos"][key], key
+    for key in ("Compression_ratio", "Space_saving", "Rank_mean"):
+        assert abs(float(info[key]) - float(meta["infos"][key])) <= 1e-5 * abs(float(meta["infos"][key])), key
+    _, _, uv, dd = hm.get_factors()
+    assert hashlib.sha256(np.ascontiguousarray(dd).tobytes()).hexdigest() == meta["sha_dense"]
+    assert hashlib.sha256(np.ascontiguousarray(uv).tobytes()).hexdigest() == meta["sha_uv"]
+    for mu in (1, 3):
+        assert rel(hm.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < FP64_TOL
+    if meta["symmetry"] == "S":
+        x = g["x_mu1"]
+        assert np.array_equal(hm.mvprod_transp_global_to_global(x), hm.mvprod_global_to_global(x))
+        hm.set_precision("mixed")
+        assert rel(hm.mvprod_global_to_global(x), g["y_mu1"]) < 1e-6
+        hm.set_precision("fp64")
+        with pytest.raises(NotImplementedError):
+            hm.save("/dev/null")
