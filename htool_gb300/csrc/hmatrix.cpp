@@ -1140,7 +1140,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             launches_ += groups;
         }
         if (!multi_h.empty()) {
-            launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, w_A, st);
+            launch_reduce_tiles_f(lr_d.p, multi_d.p, (int)multi_h.size(), mu, reinterpret_cast<float *>(w_A), st); // float sums
             launches_++;
         }
         if (marks)

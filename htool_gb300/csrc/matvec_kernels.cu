@@ -258,15 +258,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, EMU ? 3 : 2) phase1_kerne
 }
 
 // sum the phase-1 tile partials of every multi-tile leaf into tile 0
-__global__ void reduce_tiles_kernel(const LrLeaf *__restrict__ lr, const int *__restrict__ multi, int nmulti, int mu, double *__restrict__ A) {
+// T: double for the FP64 product, float for the reduced-precision ones
+// (whose phase-1 sums are floats)
+template <typename T>
+__global__ void reduce_tiles_kernel(const LrLeaf *__restrict__ lr, const int *__restrict__ multi, int nmulti, int mu, T *__restrict__ A) {
     const int b = blockIdx.x;
     if (b >= nmulti)
         return;
     const LrLeaf L       = lr[multi[b]];
     const long long span = (long long)L.r * mu;
-    double *base         = A + L.a_off * mu;
+    T *base              = A + L.a_off * mu;
     for (long long e = threadIdx.x; e < span; e += blockDim.x) {
-        double s = base[e];
+        T s = base[e];
         for (int ch = 1; ch < L.nch; ch++)
             s += base[ch * span + e];
         base[e] = s;
@@ -376,7 +379,14 @@ void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, 
 void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st) {
     if (nmulti <= 0)
         return;
-    reduce_tiles_kernel<<<nmulti, 128, 0, st>>>(lr, multi, nmulti, mu, A);
+    reduce_tiles_kernel<double><<<nmulti, 128, 0, st>>>(lr, multi, nmulti, mu, A);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st) {
+    if (nmulti <= 0)
+        return;
+    reduce_tiles_kernel<float><<<nmulti, 128, 0, st>>>(lr, multi, nmulti, mu, A);
     HTGPU_CUDA(cudaGetLastError());
 }
 

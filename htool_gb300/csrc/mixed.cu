@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
         const float *V32  = reinterpret_cast<const float *>(mix + it.off);
         const unsigned short *V16 = reinterpret_cast<const unsigned short *>(mix + it.off + 4LL * l32 * c32);
         const F2 *X       = xs + (long long)(L.oj + it.j0) * mu + c0;
-        double *out       = A + (L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r) * mu + c0;
+        float *out        = reinterpret_cast<float *>(A) + (L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r) * mu + c0; // float sums
         float xv[RPL][MU];
 #pragma unroll
         for (int t = 0; t < RPL; t++) {
@@ -183,9 +183,11 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
                 rs16f(acc, lane);
                 const int kk = vi / MU, c = vi % MU;
                 if ((lane & 1) == 0 && kg + kk < L.r) {
-                    const double val = scale_pow2_safe((double)acc[0], shift) * scale[L.a_off + kg + kk];
-                    double *o        = out + (long long)(kg + kk) * mu + c;
-                    *o               = s0 == 0 ? val : *o + val;
+                    // the phase-2 coefficient as a float (x's exponent shift
+                    // cancels between the phases); the buffer holds floats
+                    const float val = (float)((double)acc[0] * scale[L.a_off + kg + kk]);
+                    float *o        = out + (long long)(kg + kk) * mu + c;
+                    *o              = s0 == 0 ? val : *o + val;
                 }
             }
         }

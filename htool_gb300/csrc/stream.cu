@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
     // raw coefficients of a landed chunk into registers: column t = lane + 32 j
     auto gather = [&](int s, const StreamChunk &c, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
         const int *ix  = reinterpret_cast<const int *>(wbase + L::kIdx + (size_t)s * kIdxBuf + ((4LL * c.a) & 15));
-        const bool emu = c.kind == kStreamEmu;
+        const bool emu = c.kind == kStreamEmu, red = c.kind == kStreamF32 || c.kind == kStreamBf16;
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             const int t = lane + 32 * j;
@@ -237,7 +237,9 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
                 double v = 0.;
                 if (t < c.ncol) {
                     const int kx = kk[j];
-                    if (kx >= 0)
+                    if (kx >= 0 && red) // float phase-1 sum, bits kept in the register
+                        v = __longlong_as_double((long long)__float_as_uint(__ldg(reinterpret_cast<const float *>(A) + (long long)kx * mu + c0 + cc)));
+                    else if (kx >= 0)
                         v = __ldg(A + (long long)kx * mu + c0 + cc);
                     else if (emu)
                         v = __longlong_as_double(__ldg(reinterpret_cast<const long long *>(xs) + (long long)(~kx) * mu + c0 + cc));
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
                 const int pos = ((((jj >> lv) * S + sl) << lv) | (jj & ((1 << lv) - 1)));
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
-                    cf[cc * 128 + pos] = (float)scale_pow2_safe(r[j][cc], 1023 - xe);
+                    cf[cc * 128 + pos] = __uint_as_float((unsigned)__double_as_longlong(r[j][cc]));
             }
         }
         __syncwarp();
@@ -623,7 +625,7 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
     // raw coefficients of a landed chunk into registers: column t = lane + 32 j
     auto gather = [&](int s, const StreamChunk &c, double (&raw)[kStreamCols / 32][MU], int (&kk)[kStreamCols / 32]) {
         const int *ix  = reinterpret_cast<const int *>(wbase + L::kIdx + (size_t)s * kIdxBuf + ((4LL * c.a) & 15));
-        const bool emu = c.kind == kStreamEmu;
+        const bool emu = c.kind == kStreamEmu, red = c.kind == kStreamF32 || c.kind == kStreamBf16;
 #pragma unroll
         for (int j = 0; j < kStreamCols / 32; j++) {
             const int t = lane + 32 * j;
@@ -633,7 +635,9 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
                 double v = 0.;
                 if (t < c.ncol) {
                     const int kx = kk[j];
-                    if (kx >= 0)
+                    if (kx >= 0 && red) // float phase-1 sum, bits kept in the register
+                        v = __longlong_as_double((long long)__float_as_uint(__ldg(reinterpret_cast<const float *>(A) + (long long)kx * mu + c0 + cc)));
+                    else if (kx >= 0)
                         v = __ldg(A + (long long)kx * mu + c0 + cc);
                     else if (emu)
                         v = __longlong_as_double(__ldg(reinterpret_cast<const long long *>(xs) + (long long)(~kx) * mu + c0 + cc));
@@ -663,7 +667,7 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
                 const int pos = ((((jj >> lv) * S + sl) << lv) | (jj & ((1 << lv) - 1)));
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
-                    cf[cc * 128 + pos] = (float)scale_pow2_safe(r[j][cc], 1023 - xe);
+                    cf[cc * 128 + pos] = __uint_as_float((unsigned)__double_as_longlong(r[j][cc]));
             }
         }
         __syncwarp();
@@ -1083,7 +1087,7 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
                 }
             }
         }
-        reduce_out(acc, np * MU, lane, AddF(), ShflF(), [&](int n, float v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe((double)v, shift) * sc; });
+        reduce_out(acc, np * MU, lane, AddF(), ShflF(), [&](int n, float v) { reinterpret_cast<float *>(A)[(long long)(base + n / MU) * mu + c0 + n % MU] = (float)((double)v * sc); });
     }
 }
 
@@ -1158,7 +1162,10 @@ __device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned 
             }
         }
         const int base = c.a + g;
-        reduce_out(acc, ng * MU, lane, AddF(), ShflF(), [&](int n, float v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe((double)v, shift) * sc; });
+        // the phase-2 coefficient as a float: x's exponent shift cancels
+        // between the phases, and the reduced-precision product keeps its
+        // phase-1 sums as floats
+        reduce_out(acc, ng * MU, lane, AddF(), ShflF(), [&](int n, float v) { reinterpret_cast<float *>(A)[(long long)(base + n / MU) * mu + c0 + n % MU] = (float)((double)v * sc); });
     }
 }
 
