@@ -428,14 +428,19 @@ class HMatrix:
         return y
 
     def mvprod_transp_global_to_global(self, x, mu=1):
-        """y = H^T x on host arrays (column-major, mu right-hand sides)."""
-        if self.complex:
-            raise NotImplementedError("[Htool error] transposed products of complex H-matrices are not supported")
+        """y = H^T x on host arrays (column-major, mu right-hand sides;
+        complex128 for a complex H-matrix: the plain transpose, htool's op 'T')."""
         nr, nc, _, _ = self.sizes()
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        if x.size != nr * mu:
-            raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nr * mu))
-        y = np.empty(nc * mu, np.float64)
+        if self.complex:
+            x = np.ascontiguousarray(x, dtype=np.complex128)
+            if 2 * x.size != nr * mu:
+                raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nr * mu // 2))
+            y = np.empty(nc * mu // 2, np.complex128)
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            if x.size != nr * mu:
+                raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nr * mu))
+            y = np.empty(nc * mu, np.float64)
         _check(lib.htgpu_hmatrix_mvprod_transp(self.h, _ptr(x), _ptr(y), mu, HOST_PTRS, None))
         return y
 

@@ -1336,7 +1336,6 @@ void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptr
         return;
     }
     require(mu >= 1, "number of right-hand sides must be positive");
-    require(!complex_, "transposed products of complex H-matrices are not supported", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
     if (!transp_) {
         // leaves of H^T from the stored ones (one pass through host memory)
@@ -1381,7 +1380,28 @@ void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptr
     }
     if (transp_->precision() != precision_ || (precision_ != 0 && transp_->tau_ != tau_))
         transp_->set_precision(precision_, tau_);
-    transp_->mvprod(in, out, mu, host_ptrs, false, st);
+    if (!complex_) {
+        transp_->mvprod(in, out, mu, host_ptrs, false, st);
+        return;
+    }
+    // complex: the transpose of the real form is the real form of the
+    // adjoint, so H^T x (htool's op 'T') = conj(H^H conj(x))
+    const long long nin = (long long)nr * mu, nout = (long long)nc * mu;
+    if (host_ptrs) {
+        std::vector<double> xc(in, in + nin);
+        for (long long i = 1; i < nin; i += 2)
+            xc[i] = -xc[i];
+        transp_->mvprod(xc.data(), out, mu, true, false, st);
+        for (long long i = 1; i < nout; i += 2)
+            out[i] = -out[i];
+        return;
+    }
+    cudaStream_t s2 = st ? st : transp_->stream();
+    if (conj_in_.n < (std::size_t)nin)
+        conj_in_.alloc(nin);
+    launch_conj(in, conj_in_.p, nin, s2);
+    transp_->mvprod(conj_in_.p, out, mu, false, false, s2);
+    launch_conj(out, out, nout, s2);
 }
 
 void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {

@@ -217,6 +217,7 @@ class HMatrix {
     int n_sctas_ = 0, n_ranges_ = 0, n_ranges_m_ = 0;
     long long n_chunks_ = 0, n_chunks_m_ = 0;
     int p1_mode_ = 0;
+    DevBuf<double> conj_in_; // complex transposed products: the conjugated input
     char symmetry_ = 'N', uplo_ = 'N';
     int compression_ = 0;
     int nlr_stored_ = -1, ndn_stored_ = -1; // htool's leaves when twins follow them

@@ -51,6 +51,8 @@ void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st);
 void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st);
 void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
 void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st);
+// complex conjugate of n interleaved (re, im) doubles (dst may be src)
+void launch_conj(const double *src, double *dst, long long n, cudaStream_t st);
 // the same over float phase-1 sums (reduced-precision products)
 void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st);
 void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st);

@@ -383,6 +383,21 @@ void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu,
     HTGPU_CUDA(cudaGetLastError());
 }
 
+// dst[i] = src[i] with every odd entry negated: the complex conjugate of
+// interleaved (re, im) values
+__global__ void conj_kernel(const double *__restrict__ src, double *__restrict__ dst, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (i & 1) ? -src[i] : src[i];
+}
+
+void launch_conj(const double *src, double *dst, long long n, cudaStream_t st) {
+    if (n <= 0)
+        return;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+    conj_kernel<<<blocks, 256, 0, st>>>(src, dst, n);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
 void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st) {
     if (nmulti <= 0)
         return;

@@ -102,7 +102,7 @@ int htgpu_hmatrix_destroy(htgpu_hmatrix h);
  * matrix is stored and applied in real form (entry z -> [[re, -im],
  * [im, re]]), so every storage policy and the batched products apply;
  * htgpu_hmatrix_get_leaves / get_factors describe that real form;
- * transposed products are not available for complex handles. */
+ * htgpu_hmatrix_mvprod_transp gives the plain transpose (htool's op 'T'). */
 int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out);
 
 /* set_maxblocksize / set_mintargetdepth / set_minsourcedepth (hmatrix.hpp:213-215). */

@@ -323,6 +323,9 @@ void ref_hmatrix_mvprod_z(void *p, const void *x, void *y, int mu) {
 }
 // HMatrix::mvprod_transp_global_to_global (hmatrix.hpp:1277-1354)
 void ref_hmatrix_mvprod_transp_d(void *p, const double *x, double *y, int mu) { ((RefHMat<double> *)p)->h->mvprod_transp_global_to_global(x, y, mu); }
+void ref_hmatrix_mvprod_transp_z(void *p, const void *x, void *y, int mu) {
+    ((RefHMat<std::complex<double>> *)p)->h->mvprod_transp_global_to_global((const std::complex<double> *)x, (std::complex<double> *)y, mu);
+}
 
 // Median wall time of `reps` products after one warm-up.
 double ref_hmatrix_time_mvprod_d(void *p, const double *x, double *y, int mu, int reps) {

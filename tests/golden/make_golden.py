@@ -18,6 +18,7 @@ Usage (needs the upstream sources, i.e. only in the build container):
     python tests/golden/make_golden.py          # everything but the leaf maps
     python tests/golden/make_golden.py plot     # the save_plot leaf maps only
     python tests/golden/make_golden.py sym      # the symmetric / sympartialACA builds only
+    python tests/golden/make_golden.py ztransp  # transposed products of the Helmholtz fixture
 """
 import ctypes as C
 import hashlib
@@ -190,6 +191,31 @@ def sym_cases():
         print(name, "tasks", k, "leaves", lr.shape[0], dn.shape[0])
 
 
+def ztransp_case():
+    """upstream's transposed products (op 'T') of the Helmholtz fixture"""
+    R = Oracle("reference")
+    R.set_num_threads(1)
+    L, vp = R._L, C.c_void_p
+    L.ref_hmatrix_build_z.restype = vp
+    L.ref_hmatrix_build_z.argtypes = [vp, vp, C.c_int, vp, C.c_int, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char, C.c_int]
+    L.ref_hmatrix_mvprod_transp_z.argtypes = [vp, vp, vp, C.c_int]
+    L.ref_hmatrix_free_z.argtypes = [vp]
+    n = 2000
+    pts = G.cube_surface(n, seed=1)
+    ct = R.cluster(pts)
+    h = L.ref_hmatrix_build_z(ct.h, ct.h, n, pts.ctypes.data, n, pts.ctypes.data, 20.0, 1e-5, 3.0, 0, b"N", b"N", 0)
+    rng = np.random.default_rng(11)
+    data = {}
+    for mu in (1, 3):
+        x = rng.standard_normal(n * mu) + 1j * rng.standard_normal(n * mu)
+        y = np.empty(n * mu, np.complex128)
+        L.ref_hmatrix_mvprod_transp_z(h, x.ctypes.data, y.ctypes.data, mu)
+        data["xT_mu%d" % mu] = x
+        data["yT_mu%d" % mu] = y
+    L.ref_hmatrix_free_z(h)
+    np.savez_compressed(os.path.join(OUT, "helmholtz_cube2000_transp.npz"), **data)
+
+
 def plot_cases():
     """htool's leaf maps (HMatrix::save_plot) of the configuration-1 and
     Helmholtz fixtures, written by upstream itself (one thread)"""
@@ -215,5 +241,7 @@ if __name__ == "__main__":
         plot_cases()
     elif sys.argv[1:] == ["sym"]:
         sym_cases()
+    elif sys.argv[1:] == ["ztransp"]:
+        ztransp_case()
     else:
         main()

@@ -56,5 +56,24 @@ def test_complex_dense_rows_and_precision(case):
     hm.set_precision("mixed")
     assert rel(hm.mvprod_global_to_global(x), y) < 10 * meta["eps"]
     hm.set_precision("fp64")
-    with pytest.raises(NotImplementedError):
-        hm.mvprod_transp_global_to_global(np.zeros(pts.shape[0], np.complex128))
+
+
+def test_complex_transposed_products_match_upstream(case):
+    """mvprod_transp_global_to_global of a complex H-matrix is the plain
+    transpose (htool's op 'T', hmatrix.hpp:1277-1354): host arrays, device
+    pointers, and the mixed storage"""
+    import os
+
+    torch = pytest.importorskip("torch")
+    g, meta, hm = case
+    gt = np.load(os.path.join(os.path.dirname(__file__), "golden", "helmholtz_cube2000_transp.npz"))
+    for mu in (1, 3):
+        assert rel(hm.mvprod_transp_global_to_global(gt["xT_mu%d" % mu], mu), gt["yT_mu%d" % mu]) < 1e-10
+    x = torch.from_numpy(gt["xT_mu3"].view(np.float64).copy()).cuda()
+    y = torch.empty_like(x)
+    # on the legacy default stream, which torch's copy back orders against
+    H._check(H.lib.htgpu_hmatrix_mvprod_transp(hm.h, H.C.c_void_p(x.data_ptr()), H.C.c_void_p(y.data_ptr()), 3, 0, H.C.c_void_p(1)))
+    assert rel(y.cpu().numpy().view(np.complex128), gt["yT_mu3"]) < 1e-10
+    hm.set_precision("mixed")
+    assert rel(hm.mvprod_transp_global_to_global(gt["xT_mu1"]), gt["yT_mu1"]) < 1e-4
+    hm.set_precision("fp64")
