@@ -138,6 +138,10 @@ inline int swizzle_bytes(int h, int n, int es) {
 void launch_colmax(const ColMaxJob *jobs, int njobs, const double *fac, unsigned *cmax, cudaStream_t st);
 void launch_convert(const ConvertJob *jobs, int njobs, const double *fac, const unsigned *cmax, unsigned char *mix, cudaStream_t st);
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
+// the same contraction on the tensor cores (mma.sync TF32, three products
+// per step), for products with many right-hand sides; float sums into A
+constexpr int kMmaMinRhs = 8; // right-hand sides from which products take it
+void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, int mu, double *A, cudaStream_t st);
 // ---- ACA rank predictor (mlp.cu) -------------------------------------------
 constexpr int kMlpIn = 10, kMlpHidden = 64;
 constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;

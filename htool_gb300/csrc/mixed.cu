@@ -228,6 +228,121 @@ void launch_swizzle(const SwizzleJob *jobs, int njobs, const double *fac, const 
     HTGPU_CUDA(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------------------
+// Phase 1 of a reduced-precision product with many right-hand sides on the
+// tensor cores: per tile, C (r x mu) = V^T X with V the tile's FP32 / BF16
+// columns (rows j < jlen) and X its x rows (the float part of the split),
+// by mma.sync m16n8k8 in TF32 with three products per step (hi*hi + hi*lo
+// + lo*hi of the TF32 splits of both operands, FP32 accumulation): about
+// FP32 accuracy.  One warp per tile, V columns in pairs of 16-row tiles,
+// right-hand sides in blocks of 64 (eight 8-column tiles).  Fragment
+// layouts of m16n8k8 .tf32 (g = lane / 4, t = lane % 4): A a0 (g, t), a1
+// (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4); B b0 (t, g), b1 (t + 4, g);
+// C c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1).
+constexpr int kMmaWarps = 4;
+
+__device__ __forceinline__ unsigned tf32_of(float a) {
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(a));
+    return r;
+}
+
+__device__ __forceinline__ void split_tf32(float v, unsigned &hi, unsigned &lo) {
+    hi = tf32_of(v);
+    lo = tf32_of(v - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const unsigned char *__restrict__ mix,
+                                                                     const double *__restrict__ scale, const F2 *__restrict__ xs, int mu, double *__restrict__ A) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int W    = gridDim.x * kMmaWarps;
+    float *Af      = reinterpret_cast<float *>(A); // float phase-1 sums
+    for (int w = blockIdx.x * kMmaWarps + (threadIdx.x >> 5); w < nitems; w += W) {
+        const P1Item it = items[w];
+        const LrLeaf L  = lr[it.leaf];
+        const int jlen = it.jlen, r = L.r, c32 = it.pad;
+        const int l32 = ld_f32(jlen), l16 = ld_bf16(jlen);
+        const float *V32          = reinterpret_cast<const float *>(mix + it.off);
+        const unsigned short *V16 = reinterpret_cast<const unsigned short *>(mix + it.off + 4LL * l32 * c32);
+        const F2 *X               = xs + (long long)(L.oj + it.j0) * mu;
+        float *out                = Af + (L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r) * mu;
+        auto vload = [&](int j, int k) -> float { // V[j][k], zero outside the tile
+            if (j >= jlen || k >= r)
+                return 0.f;
+            return k < c32 ? V32[(long long)k * l32 + j] : bf16_to_f32(V16[(long long)(k - c32) * l16 + j]);
+        };
+        for (int cb = 0; cb < mu; cb += 64) {
+            const int nnt = min(8, (mu - cb + 7) >> 3); // 8-column tiles of this block
+            for (int mb = 0; mb < r; mb += 32) {
+                const int nmt = r - mb > 16 ? 2 : 1;
+                float acc[2][8][4];
+#pragma unroll
+                for (int a = 0; a < 2; a++)
+#pragma unroll
+                    for (int b = 0; b < 8; b++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            acc[a][b][q] = 0.f;
+                for (int j0 = 0; j0 < jlen; j0 += 8) {
+                    unsigned ah[2][4], al[2][4];
+#pragma unroll
+                    for (int mt = 0; mt < 2; mt++) {
+                        const int k0 = mb + 16 * mt + g;
+                        split_tf32(vload(j0 + t, k0), ah[mt][0], al[mt][0]);
+                        split_tf32(vload(j0 + t, k0 + 8), ah[mt][1], al[mt][1]);
+                        split_tf32(vload(j0 + t + 4, k0), ah[mt][2], al[mt][2]);
+                        split_tf32(vload(j0 + t + 4, k0 + 8), ah[mt][3], al[mt][3]);
+                    }
+#pragma unroll
+                    for (int nt = 0; nt < 8; nt++) {
+                        if (nt >= nnt) // warp-uniform
+                            break;
+                        const int c   = cb + 8 * nt + g;
+                        const float x0 = (j0 + t < jlen && c < mu) ? X[(long long)(j0 + t) * mu + c].hi : 0.f;
+                        const float x1 = (j0 + t + 4 < jlen && c < mu) ? X[(long long)(j0 + t + 4) * mu + c].hi : 0.f;
+                        unsigned bh0, bl0, bh1, bl1;
+                        split_tf32(x0, bh0, bl0);
+                        split_tf32(x1, bh1, bl1);
+#pragma unroll
+                        for (int mt = 0; mt < 2; mt++) {
+                            if (mt >= nmt) // warp-uniform
+                                break;
+                            mma_tf32(acc[mt][nt], al[mt], bh0, bh1);
+                            mma_tf32(acc[mt][nt], ah[mt], bl0, bl1);
+                            mma_tf32(acc[mt][nt], ah[mt], bh0, bh1);
+                        }
+                    }
+                }
+                // scaled by the column factors: the phase-2 coefficients
+#pragma unroll
+                for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            const int k = mb + 16 * mt + g + 8 * (q >> 1), c = cb + 8 * nt + 2 * t + (q & 1);
+                            if (mt < nmt && nt < nnt && k < r && c < mu)
+                                out[(long long)k * mu + c] = (float)((double)acc[mt][nt][q] * scale[L.a_off + k]);
+                        }
+            }
+        }
+    }
+}
+
+void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, int mu, double *A, cudaStream_t st) {
+    if (nitems <= 0)
+        return;
+    const int blocks = (nitems + kMmaWarps - 1) / kMmaWarps; // one warp per tile
+    phase1_mma_kernel<<<blocks, 32 * kMmaWarps, 0, st>>>(items, nitems, lr, mix, scale, xs, mu, A);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;

@@ -269,6 +269,29 @@ def test_phase2_modes_bitwise(golden):
     assert GH.device_status() == 0
 
 
+def test_many_rhs_tensor_core_phase1(golden):
+    """Reduced-precision products with many right-hand sides run phase 1 on
+    the tensor cores (TF32, three products per step): every column agrees
+    with the FP64 product within the mixed tolerance and with the
+    one-right-hand-side product (CUDA-core kernels) to FP32 rounding, for
+    block sizes that fill 8-column tiles and one that does not."""
+    g, meta = golden("sphere6000_k1")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    for mu in (8, 13, 64):
+        X = G.rhs(n, mu, seed=20 + mu)
+        y64 = GH.mvprod_global_to_global(X, mu)
+        GH.set_precision("mixed")
+        ym = GH.mvprod_global_to_global(X, mu)
+        for c in range(0, mu, max(1, mu // 4)):
+            col = slice(c * n, (c + 1) * n)
+            assert rel(ym[col], y64[col]) < 1e-6
+            assert rel(ym[col], GH.mvprod_global_to_global(X[col].copy())) < 1e-6
+        GH.set_precision("fp64")
+    assert GH.device_status() == 0
+
+
 def test_autotune_keeps_parity(golden):
     g, meta = golden("sphere6000_k1")
     t = H.Cluster().build(g["xt"].shape[0], g["xt"])
