@@ -76,6 +76,8 @@ def _load():
         "htgpu_hmatrix_get_fp64_split": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_phase1_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_phase1_mode": (i, [vp, vp]),
+        "htgpu_hmatrix_set_presplit": (i, [vp, i]),
+        "htgpu_hmatrix_get_presplit": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_phase2_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_phase2_mode": (i, [vp, vp]),
         "htgpu_hmatrix_device_status": (i, [vp, vp]),
@@ -384,6 +386,18 @@ class HMatrix:
         v = C.c_int()
         _check(lib.htgpu_hmatrix_get_phase1_mode(self.h, C.byref(v)))
         return v.value
+
+    def set_presplit(self, on):
+        """Keep the data of the emulated FP64 chunks pre-split into (hi, lo)
+        float pairs (more device memory, bitwise the same products)."""
+        _check(lib.htgpu_hmatrix_set_presplit(self.h, 1 if on else 0))
+        return self
+
+    def get_presplit(self):
+        """(on, device bytes the pre-split copy holds now)."""
+        v, b = C.c_int(), C.c_longlong()
+        _check(lib.htgpu_hmatrix_get_presplit(self.h, C.byref(v), C.byref(b)))
+        return bool(v.value), b.value
 
     def set_phase2_mode(self, mode):
         """Phase 2: 'warp' (every warp streams its own chunks) or

@@ -386,6 +386,23 @@ int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode) {
     });
 }
 
+int htgpu_hmatrix_set_presplit(htgpu_hmatrix h, int on) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_presplit(on != 0);
+    });
+}
+
+int htgpu_hmatrix_get_presplit(htgpu_hmatrix h, int *on, long long *bytes) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(on, "on");
+        *on = h->h->presplit() ? 1 : 0;
+        if (bytes)
+            *bytes = h->h->presplit_bytes();
+    });
+}
+
 int htgpu_hmatrix_device_status(htgpu_hmatrix h, int *status) {
     return guarded([&] {
         need(h, "hmatrix");

@@ -722,6 +722,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
         emu_ok_ = ef < 1023 + 60;
     }
     assign_phase1_modes();
+    emu_fresh_ = false; // fac was rewritten
     upload_phase1_lists();
     lr_d.upload(lr_h, stream_);
     {
@@ -819,6 +820,22 @@ void HMatrix::upload_phase1_lists() {
         n_p1_ranges_                  = (int)st.size();
         p1_kinds_                     = chunk_kinds(ch);
         p1r_d.upload(st, stream_);
+        // all tiles emulated: the streamed phase 1 reads a pre-split copy
+        // of the tile region (the same (hi, lo) pairs it would form itself)
+        if (p1_kinds_ == 4 && presplit_on_ && precision_ == 0) {
+            long long len = 0;
+            for (auto &it : p1_h)
+                len = std::max(len, it.off + (long long)it.jlen * lr_h[it.leaf].r);
+            len += 2; // stage copies end on a 16-byte boundary
+            if (!emu_fresh_ || (long long)emu_.n < len) {
+                emu_.alloc((std::size_t)len);
+                launch_presplit(fac.p, std::min(len, arena_len), emu_.p, stream_);
+                emu_fresh_ = true;
+            }
+        } else {
+            emu_.release();
+            emu_fresh_ = false;
+        }
         ch.push_back(StreamChunk{}); // stage copies read chunk descriptors in whole 16-byte words
         p1c_d.upload(ch, stream_);
     }
@@ -846,6 +863,35 @@ void HMatrix::upload_phase1_lists() {
         p2_bytes_ += 8LL * pi.h * pi.ncol;
         n_cols_ += pi.ncol;
     }
+    // the emulated chunks read (hi, lo) pairs from a compact pre-split
+    // mirror: runs of consecutive emulated chunks, each run starting at the
+    // same offset modulo 16 bytes as in fac, so every stage copy keeps its
+    // shape
+    emu2_.release();
+    if (presplit_on_ && precision_ == 0) {
+        std::vector<SplitSeg> segs;
+        long long cur = 0; // next free pair
+        for (auto &k : ch) {
+            if (k.kind != kStreamEmu)
+                continue;
+            const long long s0 = k.src >> 3;
+            if (segs.empty() || s0 != segs.back().src + segs.back().n)
+                segs.push_back({s0, ((cur + 1) & ~1LL) + (s0 & 1), 0});
+            SplitSeg &g = segs.back();
+            k.src       = 8 * (g.dst + (s0 - g.src));
+            k.flags |= kStreamArena1 | kStreamPre;
+            g.n = s0 + (k.bytes >> 3) - g.src;
+            cur = g.dst + g.n;
+        }
+        if (!segs.empty()) {
+            emu2_.alloc((std::size_t)cur + 2); // stage copies end on a 16-byte boundary
+            DevBuf<SplitSeg> sd;
+            sd.upload(segs, stream_);
+            launch_presplit_segs(fac.p, sd.p, (int)segs.size(), emu2_.p, stream_);
+            HTGPU_CUDA(cudaStreamSynchronize(stream_));
+        }
+    }
+    fp64_lists_stale_ = presplit_on_ && precision_ != 0; // mirrors wait for the FP64 policy
     n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
     n_chunks_ = (long long)ch.size();
     {
@@ -939,8 +985,17 @@ void HMatrix::set_precision(int policy, double tau) {
     HTGPU_CUDA(cudaSetDevice(device_));
     precision_ = policy;
     tau_       = tau;
-    if (policy == 0)
+    if (policy == 0) {
+        if (fp64_lists_stale_) // FP64 chunk lists and pre-split mirrors back
+            upload_phase1_lists();
         return;
+    }
+    if (emu_.p || emu2_.p) { // the reduced-precision products need no FP64 mirrors
+        emu_.release();
+        emu2_.release();
+        emu_fresh_        = false;
+        fp64_lists_stale_ = true;
+    }
     // 1. column maxima of U (slots [0, a_slots)) and Vt ([a_slots, 2 a_slots))
     std::vector<ColMaxJob> jobs;
     for (auto &it : p1_h)
@@ -1161,7 +1216,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         return;
     }
     if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
-        launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, p1_kinds_, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
+        if (emu_fresh_)
+            launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, p1_kinds_, reinterpret_cast<const unsigned char *>(emu_.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st, true);
+        else
+            launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, p1_kinds_, reinterpret_cast<const unsigned char *>(fac.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st);
         launches_ += 1;
     } else if (n_p1_dfma_ && n_p1_emu_) {
         HTGPU_CUDA(cudaEventRecord(fork_, st));
@@ -1186,10 +1244,11 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         HTGPU_CUDA(cudaEventRecord(marks[1], st));
     {
         const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
+        const unsigned char *pre   = emu2_.p ? reinterpret_cast<const unsigned char *>(emu2_.p) : arena; // kStreamPre chunks
         if (p2_mode_ == 1)
-            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         else
-            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         launches_ += groups;
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
@@ -1208,6 +1267,14 @@ void HMatrix::set_phase1_mode(int mode) {
     layout_gen_++; // buffers or launch lists change: captured products are stale
     require(mode == 0 || mode == 1, "phase-1 mode must be 0 (tile kernels) or 1 (streamed chunks)");
     p1_mode_ = mode;
+}
+
+void HMatrix::set_presplit(bool on) {
+    HTGPU_CUDA(cudaSetDevice(device_));
+    presplit_on_ = on;
+    if (fac.p)
+        upload_phase1_lists();
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void HMatrix::autotune(int mu, int reps, float *best_ms) {
@@ -1588,6 +1655,7 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["GPU_phase2_stream_chunks"]      = inum(precision_ ? n_chunks_m_ : n_chunks_);
     m["GPU_phase2_stream_ranges"]      = inum(precision_ ? n_ranges_m_ : n_ranges_);
     m["GPU_phase1_mode"]               = inum(p1_mode_);
+    m["GPU_presplit_bytes"]            = inum(presplit_bytes());
     return m;
 }
 

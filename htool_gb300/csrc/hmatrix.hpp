@@ -107,6 +107,9 @@ class HMatrix {
     // tile, DFMA and emulated tiles on two streams), 1 streamed chunks
     void set_phase1_mode(int mode);
     int phase1_mode() const { return p1_mode_; }
+    void set_presplit(bool on);
+    bool presplit() const { return presplit_on_; }
+    long long presplit_bytes() const { return (long long)(((emu_fresh_ ? emu_.n : 0) + emu2_.n) * sizeof(F2)); }
     void set_phase2_mode(int mode);
     int phase2_mode() const { return p2_mode_; }
     bool emulation_allowed() const { return emu_ok_; }
@@ -188,6 +191,11 @@ class HMatrix {
     void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr);
     void upload_phase1_lists();
     DevBuf<P1Item> p1e_d; // phase-1 tiles on the emulation (p1_d: on DFMA)
+    DevBuf<F2> emu_;          // (hi, lo) split of the phase-1 region of fac, for an all-emulated streamed phase 1 (FP64 products)
+    bool emu_fresh_ = false;  // emu_ matches fac
+    DevBuf<F2> emu2_;         // compact (hi, lo) split of the emulated phase-2 chunks of fac (FP64 products)
+    bool presplit_on_      = true;
+    bool fp64_lists_stale_ = false; // FP64 launch lists built while a reduced precision was set
     int n_p1_dfma_ = 0, n_p1_emu_ = 0;
     std::vector<PanelItem> pan_h; // phase-2 panels (one per P2Item)
     std::vector<int> cidx_h;      // panel column coefficients

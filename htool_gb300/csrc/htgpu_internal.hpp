@@ -112,7 +112,15 @@ struct PanelItem { // z rows row0 .. row0+h += panel (h x ncol, column-major, ld
 // row chunk's panel, or up to 16 whole columns of one phase-1 tile; all of
 // one element kind, contiguous in an arena
 enum StreamKind : unsigned char { kStreamDfma = 0, kStreamEmu = 1, kStreamF32 = 2, kStreamBf16 = 3 };
-enum StreamFlag : unsigned char { kStreamFirst = 1, kStreamLast = 2, kStreamArena1 = 4 }; // first / last chunk of a row chunk (phase 2) or tile (phase 1)
+// first / last chunk of a row chunk (phase 2) or tile (phase 1); data in the
+// second arena; an emulated chunk whose data are (hi, lo) float pairs
+enum StreamFlag : unsigned char { kStreamFirst = 1, kStreamLast = 2, kStreamArena1 = 4, kStreamPre = 8 };
+
+// one run of doubles copied as (hi, lo) float pairs: n values from double
+// index src of the arena to pair index dst of a pre-split mirror
+struct SplitSeg {
+    long long src, dst, n;
+};
 constexpr int kStreamStage = 4096; // bytes of one chunk (one pipeline stage)
 constexpr int kStreamCols  = 64;   // columns of one chunk
 struct StreamChunk {

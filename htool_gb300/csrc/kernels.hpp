@@ -48,6 +48,10 @@ constexpr int kEmuBit = 1 << 30; // P1Item::chunk flag: tile uses the emulation
 
 int rhs_groups(int mu); // launches per phase for mu right-hand sides
 void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st);
+// out[i] = the (hi, lo) float split of in[i], for n doubles
+void launch_presplit(const double *in, long long n, F2 *out, cudaStream_t st);
+// the same for runs of doubles into a compact mirror
+void launch_presplit_segs(const double *in, const SplitSeg *segs, int nsegs, F2 *out, cudaStream_t st);
 void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st);
 void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
 void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st);
@@ -79,9 +83,11 @@ int stream2_units_target(); // units for a product launch on this device
 // phase 1 with one or two right-hand sides from stages of tile chunks
 // (kStreamFirst on a tile's first chunk), A slots written directly (tiles of
 // multi-tile leaves still need launch_reduce_tiles); scale: per-column
-// factors (F32/BF16 kinds); the chunk array is padded by 16 bytes
+// factors (F32/BF16 kinds); the chunk array is padded by 16 bytes.
+// presplit (emulated chunks only, kinds 4): arena is the launch_presplit
+// mirror of the FP64 arena, the same offsets holding (hi, lo) float pairs
 void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
-                          const int *xexp, int mu, double *A, int *status, cudaStream_t st);
+                          const int *xexp, int mu, double *A, int *status, cudaStream_t st, bool presplit = false);
 // element kinds present in a streamed phase-1 chunk list (1: reduced-precision
 // tiles, 2: FP64 DFMA, 4: FP64 emulated)
 int chunk_kinds(const std::vector<StreamChunk> &chunks);

@@ -348,6 +348,43 @@ void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st) {
     HTGPU_CUDA(cudaGetLastError());
 }
 
+// out[i] = split64(in[i]): the (hi, lo) float pairs the emulated phase 1
+// would form from each stored double, written once so the product reads them
+// instead of splitting every element again
+__global__ void presplit_kernel(const double *__restrict__ in, long long n, float2 *__restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const F2 f = split64(in[i]);
+        out[i]     = make_float2(f.hi, f.lo);
+    }
+}
+
+// the same for runs of doubles (one CTA per run at a time)
+__global__ void presplit_segs_kernel(const double *__restrict__ in, const SplitSeg *__restrict__ segs, int nsegs, float2 *__restrict__ out) {
+    for (int g = blockIdx.x; g < nsegs; g += gridDim.x) {
+        const SplitSeg sg = segs[g];
+        for (long long i = threadIdx.x; i < sg.n; i += blockDim.x) {
+            const F2 f       = split64(in[sg.src + i]);
+            out[sg.dst + i] = make_float2(f.hi, f.lo);
+        }
+    }
+}
+
+void launch_presplit_segs(const double *in, const SplitSeg *segs, int nsegs, F2 *out, cudaStream_t st) {
+    if (nsegs <= 0)
+        return;
+    int blocks = std::min(nsegs, sm_count() * 8);
+    presplit_segs_kernel<<<blocks, 256, 0, st>>>(in, segs, nsegs, reinterpret_cast<float2 *>(out));
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_presplit(const double *in, long long n, F2 *out, cudaStream_t st) {
+    if (n <= 0)
+        return;
+    int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
+    presplit_kernel<<<blocks, 256, 0, st>>>(in, n, reinterpret_cast<float2 *>(out));
+    HTGPU_CUDA(cudaGetLastError());
+}
+
 void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st) {
     long long total = (long long)n * mu;
     if (total <= 0)

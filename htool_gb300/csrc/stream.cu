@@ -24,6 +24,7 @@
 // a status and stops, and the producer waits (again bounded) for the copies
 // it issued before the CTA ends.
 #include "df64.cuh"
+#include <type_traits>
 #include "kernels.hpp"
 
 #include <algorithm>
@@ -340,19 +341,33 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
                     }
                 }
                 const double *P = reinterpret_cast<const double *>(buf) + row + (size_t)h * q0;
+                // pre: the chunk holds (hi, lo) float pairs in place of its doubles
+                auto emu_cols = [&](auto pre) {
 #pragma unroll 4
-                for (int j0 = 0; j0 < qc; j0 += S) {
-                    const int jj   = j0 + slice;
-                    const bool use = live && jj < qc;
-                    const F2 u     = split64(use ? P[h * jj] : 0.);
+                    for (int j0 = 0; j0 < qc; j0 += S) {
+                        const int jj   = j0 + slice;
+                        const bool use = live && jj < qc;
+                        F2 u;
+                        if constexpr (decltype(pre)::value) {
+                            const float2 w = use ? reinterpret_cast<const float2 *>(P)[h * jj] : make_float2(0.f, 0.f);
+                            u.hi           = w.x;
+                            u.lo           = w.y;
+                        } else {
+                            u = split64(use ? P[h * jj] : 0.);
+                        }
 #pragma unroll
-                    for (int cc = 0; cc < MU; cc++) {
-                        F2 b;
-                        b.hi = __shfl_sync(0xffffffffu, a[cc].hi, use ? jj : 0);
-                        b.lo = __shfl_sync(0xffffffffu, a[cc].lo, use ? jj : 0);
-                        df_fma(acc[cc], u, b);
+                        for (int cc = 0; cc < MU; cc++) {
+                            F2 b;
+                            b.hi = __shfl_sync(0xffffffffu, a[cc].hi, use ? jj : 0);
+                            b.lo = __shfl_sync(0xffffffffu, a[cc].lo, use ? jj : 0);
+                            df_fma(acc[cc], u, b);
+                        }
                     }
-                }
+                };
+                if (c.flags & kStreamPre)
+                    emu_cols(std::true_type{});
+                else
+                    emu_cols(std::false_type{});
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
                     df_renorm(acc[cc]);
@@ -736,19 +751,33 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
                     }
                 }
                 const double *P = reinterpret_cast<const double *>(buf) + row + (size_t)h * q0;
+                // pre: the chunk holds (hi, lo) float pairs in place of its doubles
+                auto emu_cols = [&](auto pre) {
 #pragma unroll 4
-                for (int j0 = 0; j0 < qc; j0 += S) {
-                    const int jj   = j0 + slice;
-                    const bool use = live && jj < qc;
-                    const F2 u     = split64(use ? P[h * jj] : 0.);
+                    for (int j0 = 0; j0 < qc; j0 += S) {
+                        const int jj   = j0 + slice;
+                        const bool use = live && jj < qc;
+                        F2 u;
+                        if constexpr (decltype(pre)::value) {
+                            const float2 w = use ? reinterpret_cast<const float2 *>(P)[h * jj] : make_float2(0.f, 0.f);
+                            u.hi           = w.x;
+                            u.lo           = w.y;
+                        } else {
+                            u = split64(use ? P[h * jj] : 0.);
+                        }
 #pragma unroll
-                    for (int cc = 0; cc < MU; cc++) {
-                        F2 b;
-                        b.hi = __shfl_sync(0xffffffffu, a[cc].hi, use ? jj : 0);
-                        b.lo = __shfl_sync(0xffffffffu, a[cc].lo, use ? jj : 0);
-                        df_fma(acc[cc], u, b);
+                        for (int cc = 0; cc < MU; cc++) {
+                            F2 b;
+                            b.hi = __shfl_sync(0xffffffffu, a[cc].hi, use ? jj : 0);
+                            b.lo = __shfl_sync(0xffffffffu, a[cc].lo, use ? jj : 0);
+                            df_fma(acc[cc], u, b);
+                        }
                     }
-                }
+                };
+                if (c.flags & kStreamPre)
+                    emu_cols(std::true_type{});
+                else
+                    emu_cols(std::false_type{});
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
                     df_renorm(acc[cc]);
@@ -954,12 +983,14 @@ __device__ __forceinline__ void reduce_out(T (&v)[16], int nv, int lane, Add add
     }
 }
 
-// np (<= NP) columns p0 .. p0+np of a phase-1 chunk of element kind KIND
-// against the tile's x rows (xw[t][cc]: row lane + 32 t, right-hand side
-// cc, as 64-bit words: FP64 bits for DFMA chunks, the F2 split otherwise;
-// zero past the tile); sums to A (and the per-column scales).  One kind per
-// instantiation keeps each consumer loop small in the instruction cache.
-template <int NP, int MU, int KIND>
+// np (<= NP) columns p0 .. p0+np of an FP64 phase-1 chunk of element kind
+// KIND (DFMA or emulated) against the tile's x rows (xw[t][cc]: row
+// lane + 32 t, right-hand side cc, as 64-bit words: FP64 bits for DFMA
+// chunks, the F2 split otherwise; zero past the tile); sums to A.  One kind
+// per instantiation keeps each consumer loop small in the instruction cache.
+// PRE: the emulated chunk holds (hi, lo) float pairs (launch_presplit) in
+// place of its doubles.
+template <int NP, int MU, int KIND, bool PRE = false>
 __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned char *buf, const unsigned long long (&xw)[8][MU], int p0, int np, int lane, int shift, double *__restrict__ A,
                                           const double *__restrict__ scale, int mu, int c0) {
     static_assert(NP * MU <= 16, "reduction group of at most 16 values");
@@ -1012,7 +1043,14 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
             }
 #pragma unroll
             for (int p = 0; p < NP; p++) {
-                const F2 u = split64((live && (full || p < np)) ? V[jlen * p + 32 * t] : 0.);
+                F2 u;
+                if constexpr (PRE) {
+                    const float2 w = (live && (full || p < np)) ? reinterpret_cast<const float2 *>(V)[jlen * p + 32 * t] : make_float2(0.f, 0.f);
+                    u.hi           = w.x;
+                    u.lo           = w.y;
+                } else {
+                    u = split64((live && (full || p < np)) ? V[jlen * p + 32 * t] : 0.);
+                }
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++)
                     df_fma((t & 1) ? acc2[p * MU + cc] : acc[p * MU + cc], u, xv[cc]);
@@ -1026,68 +1064,7 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
         }
         reduce_out(acc, np * MU, lane, AddDF(), ShflDF(), [&](int n, DF v) { A[(long long)(base + n / MU) * mu + c0 + n % MU] = scale_pow2_safe(df_to_double(v), shift); });
     } else {
-        // FP32 / BF16 columns with stride ld_f32 / ld_bf16 (whole 16-byte
-        // words, zero rows past the tile): lane l reads rows 4l.. (+128) or
-        // 8l.. as one 16-byte word, against the x rows xw[q] of the same
-        // mapping (row 4l + q % 4 + 128 (q / 4), or 8l + q)
-        float acc[16];
-#pragma unroll
-        for (int i = 0; i < 16; i++)
-            acc[i] = 0.f;
-        // the scale of the column this lane writes, requested before the sums
-        const int mine  = rs_slot(np * MU, lane) / MU;
-        const double sc = mine < np ? __ldg(scale + c.c + p0 + mine) : 0.;
-        float xv[8][MU];
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-#pragma unroll
-            for (int cc = 0; cc < MU; cc++)
-                xv[q][cc] = __int_as_float((int)(xw[q][cc] & 0xffffffffull));
-        if constexpr (KIND == kStreamF32) {
-            const int ld4   = ld_f32(jlen) >> 2; // 16-byte words per column
-            const uint4 *V  = reinterpret_cast<const uint4 *>(buf) + (size_t)ld4 * p0 + lane;
-#pragma unroll
-            for (int t = 0; t < 2; t++) {
-                if (32 * t >= ld4) // warp-uniform
-                    break;
-                const bool live = lane + 32 * t < ld4;
-#pragma unroll
-                for (int p = 0; p < NP; p++) {
-                    const uint4 w = (live && (full || p < np)) ? V[ld4 * p + 32 * t] : make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-                    for (int cc = 0; cc < MU; cc++) {
-                        float a = acc[p * MU + cc];
-                        a       = fmaf(__uint_as_float(w.x), xv[4 * t + 0][cc], a);
-                        a       = fmaf(__uint_as_float(w.y), xv[4 * t + 1][cc], a);
-                        a       = fmaf(__uint_as_float(w.z), xv[4 * t + 2][cc], a);
-                        a       = fmaf(__uint_as_float(w.w), xv[4 * t + 3][cc], a);
-                        acc[p * MU + cc] = a;
-                    }
-                }
-            }
-        } else {
-            const int ld8   = ld_bf16(jlen) >> 3; // 16-byte words per column
-            const uint4 *V  = reinterpret_cast<const uint4 *>(buf) + (size_t)ld8 * p0 + lane;
-            const bool live = lane < ld8;
-#pragma unroll
-            for (int p = 0; p < NP; p++) {
-                const uint4 w = (live && (full || p < np)) ? V[ld8 * p] : make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-                for (int cc = 0; cc < MU; cc++) {
-                    float a = acc[p * MU + cc];
-                    a       = fmaf(__uint_as_float(w.x << 16), xv[0][cc], a);
-                    a       = fmaf(__uint_as_float(w.x & 0xffff0000u), xv[1][cc], a);
-                    a       = fmaf(__uint_as_float(w.y << 16), xv[2][cc], a);
-                    a       = fmaf(__uint_as_float(w.y & 0xffff0000u), xv[3][cc], a);
-                    a       = fmaf(__uint_as_float(w.z << 16), xv[4][cc], a);
-                    a       = fmaf(__uint_as_float(w.z & 0xffff0000u), xv[5][cc], a);
-                    a       = fmaf(__uint_as_float(w.w << 16), xv[6][cc], a);
-                    a       = fmaf(__uint_as_float(w.w & 0xffff0000u), xv[7][cc], a);
-                    acc[p * MU + cc] = a;
-                }
-            }
-        }
-        reduce_out(acc, np * MU, lane, AddF(), ShflF(), [&](int n, float v) { reinterpret_cast<float *>(A)[(long long)(base + n / MU) * mu + c0 + n % MU] = (float)((double)v * sc); });
+        static_assert(KIND == kStreamDfma || KIND == kStreamEmu, "reduced-precision tiles go through tile_mixed");
     }
 }
 
@@ -1336,7 +1313,7 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
             if ((KM & 4) && c.kind == kStreamEmu) { // at most 4 columns per chunk
                 if constexpr ((KM & 4) != 0)
                     for (int p0 = 0; p0 < c.ncol; p0 += 4)
-                        tile_cols<4, MU, kStreamEmu>(c, buf, xw, p0, min(4, c.ncol - p0), lane, shift, A, scale, mu, 0);
+                        tile_cols<4, MU, kStreamEmu, (KM & 8) != 0>(c, buf, xw, p0, min(4, c.ncol - p0), lane, shift, A, scale, mu, 0);
             } else if constexpr ((KM & 2) != 0)
                 for (int p0 = 0; p0 < c.ncol; p0 += G) {
                     const int np = min(G, c.ncol - p0);
@@ -1470,16 +1447,20 @@ void launch_p1_kinds(int kinds, const P1Stage *stages, int nstages, const Stream
     case 1: launch_p1_cta<MU, 1>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
     case 2: launch_p1_cta<MU, 2>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
     case 4: launch_p1_cta<MU, 4>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
+    case 12: launch_p1_cta<MU, 12>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
     default: launch_p1_cta<MU, 6>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
     }
 }
 
 void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
-                          const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
+                          const int *xexp, int mu, double *A, int *status, cudaStream_t st, bool presplit) {
     if (nstages <= 0)
         return;
     require(mu >= 1 && mu <= 2, "streamed phase 1 takes one or two right-hand sides");
     require(kinds == 1 || (kinds & ~6) == 0, "streamed phase 1: reduced-precision tiles or FP64 chunks");
+    require(!presplit || kinds == 4, "streamed phase 1: a pre-split arena holds emulated chunks only");
+    if (presplit)
+        kinds = 12;
     if (mu == 1)
         launch_p1_kinds<1>(kinds, stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st);
     else

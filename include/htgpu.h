@@ -218,6 +218,17 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode);
 
+/* Pre-split FP64 data for the FP32-pipe emulation (on by default): FP64
+ * products keep a second copy of the data their emulated chunks read as
+ * (hi, lo) float pairs, so the kernels read the pairs instead of splitting
+ * every double again -- the V-side factors when every phase-1 tile is
+ * emulated (streamed phase 1), and the emulated phase-2 chunks.  Costs those
+ * bytes once more in device memory while the FP64 policy is set (bytes:
+ * the current size); results are bitwise the same either way.  No
+ * counterpart in the reference. */
+int htgpu_hmatrix_set_presplit(htgpu_hmatrix h, int on);
+int htgpu_hmatrix_get_presplit(htgpu_hmatrix h, int *on, long long *bytes);
+
 /* Phase 2 (the U-side and dense blocks, per row chunk): HTGPU_PHASE2_WARP
  * (every warp streams its own chunks, claiming ranges of row chunks) or
  * HTGPU_PHASE2_PRODUCER (a producer warp per CTA claims units of row chunks

@@ -243,6 +243,44 @@ def test_phase1_modes_parity(golden, mode):
     assert GH.device_status() == 0
 
 
+def test_presplit_bitwise(golden):
+    """Emulated chunks reading pre-split (hi, lo) pairs (the all-emulated
+    streamed phase 1, the emulated phase-2 chunks) give bitwise the products
+    of splitting every double in the kernels, in both phase-2 modes; the
+    copies exist only while the FP64 policy is set."""
+    g, meta = golden("sphere6000_k1")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    GH.set_phase1_mode("stream")
+    x3 = G.rhs(n, 3, seed=10)
+    for split in ((0, 0), (0, 650), (0, 1000), (300, 350)):
+        GH.set_fp64_split(*split)
+        for mode in ("warp", "producer"):
+            GH.set_phase2_mode(mode)
+            out = []
+            for on in (True, False):
+                GH.set_presplit(on)
+                flag, nbytes = GH.get_presplit()
+                assert flag == on and (nbytes > 0) == on
+                assert int(GH.get_infos()["GPU_presplit_bytes"]) == nbytes
+                out.append((GH.mvprod_global_to_global(g["x_mu1"]), GH.mvprod_global_to_global(x3, 3)))
+            assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1]), (split, mode)
+            assert rel(out[0][0], g["y_mu1"]) < FP64_TOL
+    GH.set_presplit(True)
+    GH.set_fp64_split(300, 1000)  # DFMA tiles and no emulated phase-2 chunk: no copy
+    assert GH.get_presplit() == (True, 0)
+    GH.set_fp64_split(0, 650)
+    y = GH.mvprod_global_to_global(g["x_mu1"])
+    GH.set_precision("mixed")  # the reduced-precision products drop the copies
+    assert GH.get_presplit() == (True, 0)
+    assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-6
+    GH.set_precision("fp64")  # and the FP64 policy brings them back
+    assert GH.get_presplit()[1] > 0
+    assert np.array_equal(GH.mvprod_global_to_global(g["x_mu1"]), y)
+    assert GH.device_status() == 0
+
+
 def test_phase2_modes_bitwise(golden):
     """Both phase-2 kernels (per-warp streams, producer-fed CTAs) sum every
     row in the same order: bitwise equal products for FP64 (every split),
