@@ -797,6 +797,35 @@ void HMatrix::assign_phase1_modes() {
     }
 }
 
+// The emulated FP64 chunks of a phase-2 list read (hi, lo) pairs from a
+// compact pre-split mirror: runs of consecutive emulated chunks, each run
+// starting at the same offset modulo 16 bytes as in fac so every stage copy
+// keeps its shape; the chunks are re-pointed there (kStreamPre).
+void HMatrix::presplit_chunks(std::vector<StreamChunk> &ch, DevBuf<F2> &mirror) {
+    std::vector<SplitSeg> segs;
+    long long cur = 0; // next free pair
+    for (auto &k : ch) {
+        if (k.kind != kStreamEmu)
+            continue;
+        const long long s0 = k.src >> 3;
+        if (segs.empty() || s0 != segs.back().src + segs.back().n)
+            segs.push_back({s0, ((cur + 1) & ~1LL) + (s0 & 1), 0});
+        SplitSeg &g = segs.back();
+        k.src       = 8 * (g.dst + (s0 - g.src));
+        k.flags |= kStreamPre;
+        g.n = s0 + (k.bytes >> 3) - g.src;
+        cur = g.dst + g.n;
+    }
+    mirror.release();
+    if (segs.empty())
+        return;
+    mirror.alloc((std::size_t)cur + 2); // stage copies end on a 16-byte boundary
+    DevBuf<SplitSeg> sd;
+    sd.upload(segs, stream_);
+    launch_presplit_segs(fac.p, sd.p, (int)segs.size(), mirror.p, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void HMatrix::upload_phase1_lists() {
     layout_gen_++; // buffers or launch lists change: captured products are stale
     std::vector<P1Item> a, b;
@@ -863,34 +892,9 @@ void HMatrix::upload_phase1_lists() {
         p2_bytes_ += 8LL * pi.h * pi.ncol;
         n_cols_ += pi.ncol;
     }
-    // the emulated chunks read (hi, lo) pairs from a compact pre-split
-    // mirror: runs of consecutive emulated chunks, each run starting at the
-    // same offset modulo 16 bytes as in fac, so every stage copy keeps its
-    // shape
     emu2_.release();
-    if (presplit_on_ && precision_ == 0) {
-        std::vector<SplitSeg> segs;
-        long long cur = 0; // next free pair
-        for (auto &k : ch) {
-            if (k.kind != kStreamEmu)
-                continue;
-            const long long s0 = k.src >> 3;
-            if (segs.empty() || s0 != segs.back().src + segs.back().n)
-                segs.push_back({s0, ((cur + 1) & ~1LL) + (s0 & 1), 0});
-            SplitSeg &g = segs.back();
-            k.src       = 8 * (g.dst + (s0 - g.src));
-            k.flags |= kStreamArena1 | kStreamPre;
-            g.n = s0 + (k.bytes >> 3) - g.src;
-            cur = g.dst + g.n;
-        }
-        if (!segs.empty()) {
-            emu2_.alloc((std::size_t)cur + 2); // stage copies end on a 16-byte boundary
-            DevBuf<SplitSeg> sd;
-            sd.upload(segs, stream_);
-            launch_presplit_segs(fac.p, sd.p, (int)segs.size(), emu2_.p, stream_);
-            HTGPU_CUDA(cudaStreamSynchronize(stream_));
-        }
-    }
+    if (presplit_on_ && precision_ == 0)
+        presplit_chunks(ch, emu2_);
     fp64_lists_stale_ = presplit_on_ && precision_ != 0; // mirrors wait for the FP64 policy
     n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
     n_chunks_ = (long long)ch.size();
@@ -939,8 +943,13 @@ void HMatrix::upload_mixed_phase2() {
         } else
             k.kind = kStreamEmu;
     }
-    n_chunks_m_ = (long long)ch2_h_.size();
-    scm_d.upload(ch2_h_, stream_);
+    // emulated dense chunks read pre-split pairs (ch2_h_ keeps the fac offsets)
+    std::vector<StreamChunk> ch2 = ch2_h_;
+    emu3_.release();
+    if (presplit_on_)
+        presplit_chunks(ch2, emu3_);
+    n_chunks_m_ = (long long)ch2.size();
+    scm_d.upload(ch2, stream_);
     if (ch2_h_.empty())
         scm_d.alloc(1);
     const std::vector<int> r = stream_ranges(ch2_h_, n_sctas_);
@@ -986,6 +995,7 @@ void HMatrix::set_precision(int policy, double tau) {
     precision_ = policy;
     tau_       = tau;
     if (policy == 0) {
+        emu3_.release(); // the reduced-precision products' mirror
         if (fp64_lists_stale_) // FP64 chunk lists and pre-split mirrors back
             upload_phase1_lists();
         return;
@@ -1204,10 +1214,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
         if (p2_mode_ == 1)
-            launch_phase2_producer(scm_d.p, sum_d.p, n_units_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
+            launch_phase2_producer(scm_d.p, sum_d.p, n_units_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
                                    (int)zlen_, status_d.p, st);
         else
-            launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
+            launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
                                  (int)zlen_, status_d.p, st);
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
@@ -1244,11 +1254,11 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         HTGPU_CUDA(cudaEventRecord(marks[1], st));
     {
         const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
-        const unsigned char *pre   = emu2_.p ? reinterpret_cast<const unsigned char *>(emu2_.p) : arena; // kStreamPre chunks
+        const unsigned char *pre   = reinterpret_cast<const unsigned char *>(emu2_.p); // kStreamPre chunks
         if (p2_mode_ == 1)
-            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         else
-            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
         launches_ += groups;
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
@@ -1272,8 +1282,11 @@ void HMatrix::set_phase1_mode(int mode) {
 void HMatrix::set_presplit(bool on) {
     HTGPU_CUDA(cudaSetDevice(device_));
     presplit_on_ = on;
-    if (fac.p)
+    if (fac.p) {
         upload_phase1_lists();
+        if (precision_ != 0 && !ch2_h_.empty())
+            upload_mixed_phase2();
+    }
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 

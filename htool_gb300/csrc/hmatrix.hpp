@@ -109,7 +109,7 @@ class HMatrix {
     int phase1_mode() const { return p1_mode_; }
     void set_presplit(bool on);
     bool presplit() const { return presplit_on_; }
-    long long presplit_bytes() const { return (long long)(((emu_fresh_ ? emu_.n : 0) + emu2_.n) * sizeof(F2)); }
+    long long presplit_bytes() const { return (long long)(((emu_fresh_ ? emu_.n : 0) + emu2_.n + emu3_.n) * sizeof(F2)); }
     void set_phase2_mode(int mode);
     int phase2_mode() const { return p2_mode_; }
     bool emulation_allowed() const { return emu_ok_; }
@@ -194,6 +194,8 @@ class HMatrix {
     DevBuf<F2> emu_;          // (hi, lo) split of the phase-1 region of fac, for an all-emulated streamed phase 1 (FP64 products)
     bool emu_fresh_ = false;  // emu_ matches fac
     DevBuf<F2> emu2_;         // compact (hi, lo) split of the emulated phase-2 chunks of fac (FP64 products)
+    DevBuf<F2> emu3_;         // the same for the emulated dense chunks of the reduced-precision products
+    void presplit_chunks(std::vector<StreamChunk> &ch, DevBuf<F2> &mirror);
     bool presplit_on_      = true;
     bool fp64_lists_stale_ = false; // FP64 launch lists built while a reduced precision was set
     int n_p1_dfma_ = 0, n_p1_emu_ = 0;

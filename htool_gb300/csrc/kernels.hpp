@@ -65,18 +65,19 @@ void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z,
 
 // ---- streamed phase 2 (stream.cu) ------------------------------------------
 // warps claim the chunk ranges rbeg[r] .. rbeg[r+1] (r < nranges) through
-// tickets (8 ints, reset by the launch); chunk bytes at arena0 (or arena1
-// with kStreamArena1); status: nonzero after a wait ran out
+// tickets (8 ints, reset by the launch); chunk bytes at arena0, or arena1
+// with kStreamArena1, or arena2 with kStreamPre (emulated chunks stored as
+// (hi, lo) float pairs); status: nonzero after a wait ran out
 constexpr int kStreamWarpsPerCta = 4;
 int stream_ctas(); // CTAs per launch (all resident)
-void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
                           const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
 // phase-2 mode 1: CTAs of one producer warp and consumer warps; the producer
 // claims units of whole row chunks (stream_units: nunits + 1 unit bounds in
 // row chunks, then the first chunk of every row chunk and the end) and feeds
 // its consumers
 constexpr int kUnitRowChunks = 31; // row chunks per unit at most
-void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx,
+void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx,
                             const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
 std::vector<int> stream_units(const std::vector<StreamChunk> &chunks, int target, int *nunits);
 int stream2_units_target(); // units for a product launch on this device

@@ -138,7 +138,7 @@ __device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity
 template <int MU>
 __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
     phase2_warp_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rbeg, int nranges, int *__restrict__ ticket, const unsigned char *__restrict__ arena0,
-                       const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
+                       const unsigned char *__restrict__ arena1, const unsigned char *__restrict__ arena2, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp, const F2 *__restrict__ xs,
                        const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen, int *__restrict__ status) {
     using L = P2Smem<MU>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
             if (lane == wpos) {
                 const StreamChunk &c = cur.d;
                 *sdesc(s)            = c;
-                const unsigned char *base = (c.flags & kStreamArena1) ? arena1 : arena0;
+                const unsigned char *base = (c.flags & kStreamPre) ? arena2 : (c.flags & kStreamArena1) ? arena1 : arena0;
                 const long long a0 = c.src & ~15LL, a1 = (c.src + c.bytes + 15) & ~15LL;
                 const long long i0 = (4LL * c.a) & ~15LL, i1 = (4LL * (c.a + c.ncol) + 15) & ~15LL;
                 mbar_arrive_tx(&bar[s], (unsigned)(a1 - a0 + i1 - i0));
@@ -525,7 +525,7 @@ __device__ __forceinline__ bool lane_wait(unsigned long long *b, unsigned parity
 template <int MU>
 __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
     phase2_ws_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ units, int nunits, const int *__restrict__ rcs, int *__restrict__ ticket,
-                     const unsigned char *__restrict__ arena0, const unsigned char *__restrict__ arena1, const int *__restrict__ cidx, const double *__restrict__ A,
+                     const unsigned char *__restrict__ arena0, const unsigned char *__restrict__ arena1, const unsigned char *__restrict__ arena2, const int *__restrict__ cidx, const double *__restrict__ A,
                      const double *__restrict__ xp, const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, int c0, double *__restrict__ z, int zlen,
                      int *__restrict__ status) {
     constexpr int kCons = WsCfg<MU>::kCons;
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
                         fin = true;
                     } else {
                         *d                        = dn;
-                        const unsigned char *base = (dn.flags & kStreamArena1) ? arena1 : arena0;
+                        const unsigned char *base = (dn.flags & kStreamPre) ? arena2 : (dn.flags & kStreamArena1) ? arena1 : arena0;
                         const long long a0 = dn.src & ~15LL, a1 = (dn.src + dn.bytes + 15) & ~15LL;
                         const long long i0 = (4LL * dn.a) & ~15LL, i1 = (4LL * (dn.a + dn.ncol) + 15) & ~15LL;
                         mbar_arrive_tx(fullb(lane, s), (unsigned)(a1 - a0 + i1 - i0));
@@ -1331,7 +1331,7 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
 }
 
 template <int MU>
-void launch_ws_mu(const StreamChunk *chunks, const int *units, int nunits, int *ticket, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+void launch_ws_mu(const StreamChunk *chunks, const int *units, int nunits, int *ticket, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
                   const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
     constexpr int kCons            = WsCfg<MU>::kCons;
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
@@ -1347,12 +1347,12 @@ void launch_ws_mu(const StreamChunk *chunks, const int *units, int nunits, int *
     // every resident CTA, at most one per unit: small products leave room
     // for concurrent work
     const int nctas = std::max(1, std::min(WsCfg<MU>::kCtas * std::max(sms, 1), nunits));
-    phase2_ws_kernel<MU><<<nctas, 32 * (kCons + 1), bytes, st>>>(chunks, units, nunits, units + nunits + 1, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
+    phase2_ws_kernel<MU><<<nctas, 32 * (kCons + 1), bytes, st>>>(chunks, units, nunits, units + nunits + 1, ticket, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
 template <int MU>
-void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int *ticket, int nctas, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
                     const double *xp, const F2 *xs, const int *xexp, int mu, int c0, double *z, int zlen, int *status, cudaStream_t st) {
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
     const int bytes                = kWarps * P2Smem<MU>::kTotal;
@@ -1363,7 +1363,7 @@ void launch_warp_mu(const StreamChunk *chunks, const int *rbeg, int nranges, int
         if (dev < 64)
             done |= 1ull << dev;
     }
-    phase2_warp_kernel<MU><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, ticket, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
+    phase2_warp_kernel<MU><<<nctas, 32 * kWarps, bytes, st>>>(chunks, rbeg, nranges, ticket, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
@@ -1554,7 +1554,7 @@ void reduced_tile_chunks(std::vector<StreamChunk> &out, long long src, int jlen,
     cut((r + n - 1) / n, true);
 }
 
-void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx, const double *A,
+void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
                           const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
     if (nranges <= 0)
         return;
@@ -1570,17 +1570,17 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
         if (g >= 7 && c0 > 0)
             HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
         switch (n) {
-        case 8: launch_warp_mu<8>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 4: launch_warp_mu<4>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 2: launch_warp_mu<2>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        default: launch_warp_mu<1>(chunks, rbeg, nranges, t, nctas, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 8: launch_warp_mu<8>(chunks, rbeg, nranges, t, nctas, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 4: launch_warp_mu<4>(chunks, rbeg, nranges, t, nctas, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 2: launch_warp_mu<2>(chunks, rbeg, nranges, t, nctas, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        default: launch_warp_mu<1>(chunks, rbeg, nranges, t, nctas, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
         }
         c0 += n;
         g++;
     }
 }
 
-void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const int *cidx,
+void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx,
                             const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
     if (nunits <= 0)
         return;
@@ -1593,10 +1593,10 @@ void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nun
         if (g >= 7 && c0 > 0)
             HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
         switch (n) {
-        case 8: launch_ws_mu<8>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 4: launch_ws_mu<4>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        case 2: launch_ws_mu<2>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
-        default: launch_ws_mu<1>(chunks, units, nunits, t, arena0, arena1, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 8: launch_ws_mu<8>(chunks, units, nunits, t, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 4: launch_ws_mu<4>(chunks, units, nunits, t, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        case 2: launch_ws_mu<2>(chunks, units, nunits, t, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
+        default: launch_ws_mu<1>(chunks, units, nunits, t, arena0, arena1, arena2, cidx, A, xp, xs, xexp, mu, c0, z, zlen, status, st); break;
         }
         c0 += n;
         g++;

@@ -272,11 +272,24 @@ def test_presplit_bitwise(golden):
     assert GH.get_presplit() == (True, 0)
     GH.set_fp64_split(0, 650)
     y = GH.mvprod_global_to_global(g["x_mu1"])
-    GH.set_precision("mixed")  # the reduced-precision products drop the copies
-    assert GH.get_presplit() == (True, 0)
-    assert rel(GH.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-6
-    GH.set_precision("fp64")  # and the FP64 policy brings them back
-    assert GH.get_presplit()[1] > 0
+    fp64_bytes = GH.get_presplit()[1]
+    # reduced precision: the FP64 copies go, the emulated dense chunks get theirs
+    GH.set_precision("mixed")
+    for split in ((0, 1000), (0, 650), (0, 0)):
+        GH.set_fp64_split(*split)  # dense blocks of the reduced-precision product
+        for mode in ("warp", "producer"):
+            GH.set_phase2_mode(mode)
+            out = []
+            for on in (True, False):
+                GH.set_presplit(on)
+                nbytes = GH.get_presplit()[1]
+                assert (nbytes > 0) == (on and split[1] < 1000) and nbytes < fp64_bytes
+                out.append((GH.mvprod_global_to_global(g["x_mu1"]), GH.mvprod_global_to_global(x3, 3)))
+            assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1]), (split, mode)
+            assert rel(out[0][0], g["y_mu1"]) < 1e-6
+    GH.set_presplit(True)
+    GH.set_precision("fp64")  # and the FP64 policy brings its copies back
+    assert GH.get_presplit()[1] == fp64_bytes
     assert np.array_equal(GH.mvprod_global_to_global(g["x_mu1"]), y)
     assert GH.device_status() == 0
 
