@@ -1076,21 +1076,40 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
 // group may mix both kinds, and one reduce-scatter per group sums them
 // over the warp.
 template <int MU>
-__device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned char *buf, int lane, int shift, const F2 *__restrict__ xs, double *__restrict__ A,
-                                           const double *__restrict__ scale, int mu, int c0) {
+__device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned char *buf, int lane, float *__restrict__ xsm, int &xrow, int &xlen, const F2 *__restrict__ xs,
+                                           double *__restrict__ A, const double *__restrict__ scale, int mu, int c0) {
     constexpr int GC = 8 / MU; // columns per group
     const int jlen = c.h, ncol = c.ncol, n32 = min((int)c.pad, ncol);
     const int W32 = ld_f32(jlen) >> 2, W16 = ld_bf16(jlen) >> 3; // 16-byte words per column
-    const F2 *X   = xs + (long long)c.b * mu + c0;
+    // the tile's x rows (leading floats), zero past the tile, staged in the
+    // warp's scratch by coalesced loads and kept while the warp's chunks come
+    // from the same tile
+    if (c.b != xrow || jlen != xlen) {
+        const F2 *X = xs + (long long)c.b * mu + c0;
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int row = lane + 32 * q;
+#pragma unroll
+            for (int cc = 0; cc < MU; cc++)
+                xsm[cc * 256 + row] = row < jlen ? X[(long long)row * mu + cc].hi : 0.f;
+        }
+        __syncwarp();
+        xrow = c.b;
+        xlen = jlen;
+    }
     float xf[8][MU], xb[8][MU];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int rf = 4 * lane + (q & 3) + 128 * (q >> 2), rb = 8 * lane + q;
-#pragma unroll
-        for (int cc = 0; cc < MU; cc++) {
-            xf[q][cc] = (n32 > 0 && rf < jlen) ? X[(long long)rf * mu + cc].hi : 0.f;
-            xb[q][cc] = (ncol > n32 && rb < jlen) ? X[(long long)rb * mu + cc].hi : 0.f;
-        }
+    for (int cc = 0; cc < MU; cc++) {
+        // FP32 words: rows 4 lane .. 4 lane + 3 and 128 + 4 lane ..; BF16 words: rows 8 lane .. 8 lane + 7
+        const float4 f0 = *reinterpret_cast<const float4 *>(xsm + cc * 256 + 4 * lane);
+        const float4 f1 = *reinterpret_cast<const float4 *>(xsm + cc * 256 + 128 + 4 * lane);
+        const float4 b0 = *reinterpret_cast<const float4 *>(xsm + cc * 256 + 8 * lane);
+        const float4 b1 = *reinterpret_cast<const float4 *>(xsm + cc * 256 + 8 * lane + 4);
+        xf[0][cc] = f0.x, xf[1][cc] = f0.y, xf[2][cc] = f0.z, xf[3][cc] = f0.w;
+        xf[4][cc] = f1.x, xf[5][cc] = f1.y, xf[6][cc] = f1.z, xf[7][cc] = f1.w;
+        xb[0][cc] = b0.x, xb[1][cc] = b0.y, xb[2][cc] = b0.z, xb[3][cc] = b0.w;
+        xb[4][cc] = b1.x, xb[5][cc] = b1.y, xb[6][cc] = b1.z, xb[7][cc] = b1.w;
     }
     const uint4 *V32 = reinterpret_cast<const uint4 *>(buf);
     const uint4 *V16 = reinterpret_cast<const uint4 *>(buf + 16LL * W32 * n32);
@@ -1179,6 +1198,11 @@ struct P1Cta { // shared-memory layout
     static constexpr int kTotal   = kEmpty + kP1Ring * 8;
 };
 static_assert(P1Cta::kDataBuf % 16 == 0 && P1Cta::kItemBuf % 16 == 0 && P1Cta::kItems % 16 == 0, "bulk-copy destinations 16-byte aligned");
+// dynamic shared memory of a launch: the stages, then for reduced-precision
+// tiles each consumer warp's x scratch (256 rows per right-hand side)
+template <int MU, int KM>
+constexpr int p1_smem() { return ((P1Cta::kTotal + 15) & ~15) + (KM == 1 ? p1_cons<KM>() * 256 * MU * 4 : 0); }
+static_assert(p1_smem<2, 1>() <= 227 * 1024, "phase-1 shared memory within a CTA's limit");
 
 struct P1Meta { // per ring stage: the landed stage's arena offset, chunk count, chunk-list offset, work counter
     long long a0;
@@ -1275,6 +1299,8 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
     }
 
     // ---------------- consumers
+    float *xsm = reinterpret_cast<float *>(smem + ((P1Cta::kTotal + 15) & ~15)) + (size_t)wid * 256 * MU; // x scratch (reduced-precision tiles)
+    int xrow = -1, xlen = 0;                                                                          // the tile whose x rows it holds
     for (int i = 0; i < nmine; i++) {
         const int s = i % kP1Ring;
         if (!warp_wait(&full[s], (i / kP1Ring) & 1)) {
@@ -1296,7 +1322,7 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
             const StreamChunk c      = items[it];
             const unsigned char *buf = data + (c.src - a0);
             if constexpr (KM == 1) { // a reduced-precision tile: FP32 then BF16 columns
-                tile_mixed<MU>(c, buf, lane, shift, xs, A, scale, mu, 0);
+                tile_mixed<MU>(c, buf, lane, xsm, xrow, xlen, xs, A, scale, mu, 0);
                 continue;
             } else {
             // FP64 chunks: the chunk's x rows (FP64 bits for DFMA, the F2
@@ -1430,13 +1456,13 @@ void launch_p1_cta(const P1Stage *stages, int nstages, const StreamChunk *chunks
     int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
     if (dev >= 64 || !(done >> dev & 1)) {
-        HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<MU, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, P1Cta::kTotal));
+        HTGPU_CUDA(cudaFuncSetAttribute(phase1_cta_kernel<MU, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, p1_smem<MU, KM>()));
         if (dev < 64)
             done |= 1ull << dev;
     }
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int nctas = std::max(1, std::min(std::max(sms, 1), nstages)); // one CTA per SM
-    phase1_cta_kernel<MU, KM><<<nctas, 32 * (p1_cons<KM>() + 1), P1Cta::kTotal, st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
+    phase1_cta_kernel<MU, KM><<<nctas, 32 * (p1_cons<KM>() + 1), p1_smem<MU, KM>(), st>>>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
