@@ -1146,6 +1146,12 @@ void HMatrix::set_precision(int policy, double tau) {
     mix_.alloc(std::max<long long>(off, 16));
     scale_d.upload(scale, stream_);
     {
+        std::vector<float> sf(scale.size());
+        for (std::size_t i = 0; i < scale.size(); i++)
+            sf[i] = (float)scale[i];
+        scalef_d.upload(sf, stream_);
+    }
+    {
         std::vector<StreamChunk> ch;
         p1_bytes_m_ = 0;
         for (auto &m : p1m) {
@@ -1198,7 +1204,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         HTGPU_CUDA(cudaEventRecord(marks[0], st));
     if (precision_ != 0) {
         if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
-            launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scale_d.p, w_xexp, mu, w_A, status_d.p, st);
+            launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
         } else if (n_p1m_ && mu >= kMmaMinRhs) {
             launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, mu, w_A, st);

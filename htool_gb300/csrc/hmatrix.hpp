@@ -208,6 +208,7 @@ class HMatrix {
     double tau_    = 0.25;
     DevBuf<unsigned char> mix_;
     DevBuf<double> scale_d;
+    DevBuf<float> scalef_d; // the same rounded to FP32 (streamed phase 1)
     DevBuf<P1Item> p1m_d;
     int n_p1m_ = 0;
     long long mixed_bytes_ = 0, n_f32_cols_ = 0, n_bf16_cols_ = 0;

@@ -84,10 +84,11 @@ int stream2_units_target(); // units for a product launch on this device
 // phase 1 with one or two right-hand sides from stages of tile chunks
 // (kStreamFirst on a tile's first chunk), A slots written directly (tiles of
 // multi-tile leaves still need launch_reduce_tiles); scale: per-column
-// factors (F32/BF16 kinds); the chunk array is padded by 16 bytes.
+// factors rounded to FP32 (F32/BF16 kinds); the chunk array is padded by 16
+// bytes.
 // presplit (emulated chunks only, kinds 4): arena is the launch_presplit
 // mirror of the FP64 arena, the same offsets holding (hi, lo) float pairs
-void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const float *scale,
                           const int *xexp, int mu, double *A, int *status, cudaStream_t st, bool presplit = false);
 // element kinds present in a streamed phase-1 chunk list (1: reduced-precision
 // tiles, 2: FP64 DFMA, 4: FP64 emulated)

@@ -358,11 +358,12 @@ __global__ void presplit_kernel(const double *__restrict__ in, long long n, floa
     }
 }
 
-// the same for runs of doubles (one CTA per run at a time)
+// the same for runs of doubles (short runs: one warp per run at a time)
 __global__ void presplit_segs_kernel(const double *__restrict__ in, const SplitSeg *__restrict__ segs, int nsegs, float2 *__restrict__ out) {
-    for (int g = blockIdx.x; g < nsegs; g += gridDim.x) {
+    const int lane = threadIdx.x & 31, nw = gridDim.x * (blockDim.x >> 5);
+    for (int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < nsegs; g += nw) {
         const SplitSeg sg = segs[g];
-        for (long long i = threadIdx.x; i < sg.n; i += blockDim.x) {
+        for (long long i = lane; i < sg.n; i += 32) {
             const F2 f       = split64(in[sg.src + i]);
             out[sg.dst + i] = make_float2(f.hi, f.lo);
         }
@@ -372,7 +373,7 @@ __global__ void presplit_segs_kernel(const double *__restrict__ in, const SplitS
 void launch_presplit_segs(const double *in, const SplitSeg *segs, int nsegs, F2 *out, cudaStream_t st) {
     if (nsegs <= 0)
         return;
-    int blocks = std::min(nsegs, sm_count() * 8);
+    int blocks = std::min((nsegs + 7) / 8, sm_count() * 8);
     presplit_segs_kernel<<<blocks, 256, 0, st>>>(in, segs, nsegs, reinterpret_cast<float2 *>(out));
     HTGPU_CUDA(cudaGetLastError());
 }

@@ -992,7 +992,7 @@ __device__ __forceinline__ void reduce_out(T (&v)[16], int nv, int lane, Add add
 // place of its doubles.
 template <int NP, int MU, int KIND, bool PRE = false>
 __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned char *buf, const unsigned long long (&xw)[8][MU], int p0, int np, int lane, int shift, double *__restrict__ A,
-                                          const double *__restrict__ scale, int mu, int c0) {
+                                          const float *__restrict__ scale, int mu, int c0) {
     static_assert(NP * MU <= 16, "reduction group of at most 16 values");
     const int jlen  = c.h;
     const int base  = c.a + p0;
@@ -1072,12 +1072,11 @@ __device__ __forceinline__ void tile_cols(const StreamChunk &c, const unsigned c
 // columns (stride ld_f32(jlen) rows) followed by the BF16 columns (stride
 // ld_bf16(jlen)), both in whole 16-byte words with zero rows past the tile.
 // Lane l holds the partial sums of rows 4l .. 4l+3 and 128+4l .. (FP32
-// words) or 8l .. 8l+7 (BF16 words); the columns go in groups of 8 / MU, a
-// group may mix both kinds, and one reduce-scatter per group sums them
-// over the warp.
+// words) or 8l .. 8l+7 (BF16 words); the columns of each kind go in groups
+// of 8 / MU, and one reduce-scatter per group sums them over the warp.
 template <int MU>
 __device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned char *buf, int lane, float *__restrict__ xsm, int &xrow, int &xlen, const F2 *__restrict__ xs,
-                                           double *__restrict__ A, const double *__restrict__ scale, int mu, int c0) {
+                                           double *__restrict__ A, const float *__restrict__ scale, int mu, int c0) {
     constexpr int GC = 8 / MU; // columns per group
     const int jlen = c.h, ncol = c.ncol, n32 = min((int)c.pad, ncol);
     const int W32 = ld_f32(jlen) >> 2, W16 = ld_bf16(jlen) >> 3; // 16-byte words per column
@@ -1114,21 +1113,23 @@ __device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned 
     const uint4 *V32 = reinterpret_cast<const uint4 *>(buf);
     const uint4 *V16 = reinterpret_cast<const uint4 *>(buf + 16LL * W32 * n32);
     const bool f0 = lane < W32, f1 = lane + 32 < W32, b0 = lane < W16;
-    for (int g = 0; g < ncol; g += GC) {
+    // columns g .. g+ng of one kind: the group's columns run without
+    // branches (loads past the group read zeros), so their FMA chains overlap
+    auto group = [&](int g, int ng, auto fp32) {
         float acc[16];
 #pragma unroll
         for (int i = 0; i < 16; i++)
             acc[i] = 0.f;
-        const int ng = min(GC, ncol - g);
         // the scale of the column this lane writes, requested before the sums
-        const int mine  = rs_slot(ng * MU, lane) / MU;
-        const double sc = mine < ng ? __ldg(scale + c.c + g + mine) : 0.;
+        const int mine = rs_slot(ng * MU, lane) / MU;
+        const float sc = mine < ng ? __ldg(scale + c.c + g + mine) : 0.f;
 #pragma unroll
         for (int p = 0; p < GC; p++) {
-            const int k = g + p;
-            if (k < n32) { // warp-uniform
-                const uint4 w0 = f0 ? V32[(size_t)W32 * k + lane] : make_uint4(0u, 0u, 0u, 0u);
-                const uint4 w1 = f1 ? V32[(size_t)W32 * k + lane + 32] : make_uint4(0u, 0u, 0u, 0u);
+            const int k   = g + p;
+            const bool in = p < ng;
+            if constexpr (decltype(fp32)::value) {
+                const uint4 w0 = (in && f0) ? V32[(size_t)W32 * k + lane] : make_uint4(0u, 0u, 0u, 0u);
+                const uint4 w1 = (in && f1) ? V32[(size_t)W32 * k + lane + 32] : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++) {
                     float a = __uint_as_float(w0.x) * xf[0][cc];
@@ -1141,8 +1142,8 @@ __device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned 
                     a       = fmaf(__uint_as_float(w1.w), xf[7][cc], a);
                     acc[p * MU + cc] = a;
                 }
-            } else if (k < ncol) {
-                const uint4 w = b0 ? V16[(size_t)W16 * (k - n32) + lane] : make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                const uint4 w = (in && b0) ? V16[(size_t)W16 * (k - n32) + lane] : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                 for (int cc = 0; cc < MU; cc++) {
                     float a = __uint_as_float(w.x << 16) * xb[0][cc];
@@ -1160,9 +1161,13 @@ __device__ __forceinline__ void tile_mixed(const StreamChunk &c, const unsigned 
         const int base = c.a + g;
         // the phase-2 coefficient as a float: x's exponent shift cancels
         // between the phases, and the reduced-precision product keeps its
-        // phase-1 sums as floats
-        reduce_out(acc, ng * MU, lane, AddF(), ShflF(), [&](int n, float v) { reinterpret_cast<float *>(A)[(long long)(base + n / MU) * mu + c0 + n % MU] = (float)((double)v * sc); });
-    }
+        // phase-1 sums as floats (scaled in FP32: no FP64-pipe work)
+        reduce_out(acc, ng * MU, lane, AddF(), ShflF(), [&](int n, float v) { reinterpret_cast<float *>(A)[(long long)(base + n / MU) * mu + c0 + n % MU] = v * sc; });
+    };
+    for (int g = 0; g < n32; g += GC)
+        group(g, min(GC, n32 - g), std::true_type{});
+    for (int g = n32; g < ncol; g += GC)
+        group(g, min(GC, ncol - g), std::false_type{});
 }
 
 // ---------------------------------------------------------------------------
@@ -1212,7 +1217,7 @@ struct P1Meta { // per ring stage: the landed stage's arena offset, chunk count,
 template <int MU, int KM>
 __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
     phase1_cta_kernel(const P1Stage *__restrict__ stages, int nstages, const StreamChunk *__restrict__ chunks, const unsigned char *__restrict__ arena, const double *__restrict__ xp,
-                      const F2 *__restrict__ xs, const double *__restrict__ scale, const int *__restrict__ xexp, int mu, double *__restrict__ A, int *__restrict__ status) {
+                      const F2 *__restrict__ xs, const float *__restrict__ scale, const int *__restrict__ xexp, int mu, double *__restrict__ A, int *__restrict__ status) {
     constexpr int G      = 16 / MU; // columns per reduction group
     constexpr int kP1Cons = p1_cons<KM>();
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1450,7 +1455,7 @@ int stream_ctas() {
 }
 
 template <int MU, int KM>
-void launch_p1_cta(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale, const int *xexp, int mu,
+void launch_p1_cta(const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const float *scale, const int *xexp, int mu,
                    double *A, int *status, cudaStream_t st) {
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
     int dev = 0, sms = 0;
@@ -1467,7 +1472,7 @@ void launch_p1_cta(const P1Stage *stages, int nstages, const StreamChunk *chunks
 }
 
 template <int MU>
-void launch_p1_kinds(int kinds, const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+void launch_p1_kinds(int kinds, const P1Stage *stages, int nstages, const StreamChunk *chunks, const unsigned char *arena, const double *xp, const F2 *xs, const float *scale,
                      const int *xexp, int mu, double *A, int *status, cudaStream_t st) {
     switch (kinds) {
     case 1: launch_p1_cta<MU, 1>(stages, nstages, chunks, arena, xp, xs, scale, xexp, mu, A, status, st); break;
@@ -1478,7 +1483,7 @@ void launch_p1_kinds(int kinds, const P1Stage *stages, int nstages, const Stream
     }
 }
 
-void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const double *scale,
+void launch_phase1_stream(const P1Stage *stages, int nstages, const StreamChunk *chunks, int kinds, const unsigned char *arena, const double *xp, const F2 *xs, const float *scale,
                           const int *xexp, int mu, double *A, int *status, cudaStream_t st, bool presplit) {
     if (nstages <= 0)
         return;
