@@ -543,7 +543,16 @@ __global__ void dense_fill_z_kernel(const DenseChunk *__restrict__ chunks, const
     for (int e = threadIdx.x; e < hn; e += blockDim.x) {
         const int i = e % C.h, j = e / C.h;
         const int pi = perm_t[C.row0 + i], pj = perm_s[C.oj + j];
-        const zd z   = kernel_entry_z(kd, xt + 3 * (size_t)(pi >> 1), xs + 3 * (size_t)(pj >> 1));
+        zd z         = kernel_entry_z(kd, xt + 3 * (size_t)(pi >> 1), xs + 3 * (size_t)(pj >> 1));
+        if (C.mode != kDenseAsIs) {
+            // complex indices in the cluster numbering (doubled trees keep
+            // both components of a point next to each other)
+            const int ci = (C.row0 + i) >> 1, cj = (C.oj + j) >> 1;
+            if (C.mode == kDenseConj || (C.mode == kDenseHermL && ci < cj) || (C.mode == kDenseHermU && ci > cj))
+                z.im = -z.im;
+            else if (ci == cj) // hemv reads the real part of the diagonal
+                z.im = 0.;
+        }
         const int a = pi & 1, b = pj & 1;
         arena[C.dst + e] = a == b ? z.re : (a ? z.im : -z.im);
     }

@@ -90,11 +90,24 @@ void HMatrix::set_symmetry(char symmetry, char uplo) {
     // 'H' needs a complex type
     require((symmetry == 'N' && uplo == 'N') || (symmetry == 'S' && (uplo == 'U' || uplo == 'L')) || (symmetry == 'H' && (uplo == 'U' || uplo == 'L')),
             "Invalid arguments to create HMatrix: symmetry must be 'N' with UPLO 'N', or 'S'/'H' with UPLO 'U' or 'L'");
-    require(symmetry != 'H', "Hermitian H-matrices ('H') are not available", 2);
-    if (symmetry == 'S')
+    require(symmetry != 'H' || complex_, "Hermitian H-matrices ('H') need a complex type", 2);
+    if (symmetry != 'N')
         require(T->n == S->n && T->perm == S->perm, "a symmetric H-matrix needs the same target and source cluster tree");
     symmetry_ = symmetry;
     uplo_     = uplo;
+}
+
+// the fill of dense leaf d: complex Hermitian H-matrices conjugate the twins
+// of the stored off-diagonal blocks (B^H of a symmetric generator's B is
+// conj(B^T)) and complete the diagonal blocks from their UPLO triangle with
+// a real diagonal, as hemv / hemm read them (matrix.hpp:386-447)
+int HMatrix::dense_mode(int d) const {
+    if (!complex_ || symmetry_ != 'H')
+        return kDenseAsIs;
+    const DenseLeaf &D = dn_h[d];
+    if (D.oi == D.oj)
+        return uplo_ == 'L' ? kDenseHermL : kDenseHermU;
+    return ndn_stored_ >= 0 && d >= ndn_stored_ ? kDenseConj : kDenseAsIs;
 }
 
 void HMatrix::set_compression(int compressor) {
@@ -105,7 +118,8 @@ void HMatrix::set_compression(int compressor) {
 // transposed twins of the off-diagonal leaves of a symmetric H-matrix,
 // after htool's own leaves: the twin of a low-rank leaf reads the same
 // factors with U and V^T exchanged, the twin of a dense leaf is generated
-// (the built-in generators are symmetric bit for bit)
+// (the built-in generators are symmetric bit for bit; a Hermitian twin
+// takes the conjugates, dense_mode)
 void HMatrix::add_symmetric_twins(std::vector<LeafSrc> &lr_src) {
     nlr_stored_ = (int)lr_h.size();
     ndn_stored_ = (int)dn_h.size();
@@ -119,7 +133,11 @@ void HMatrix::add_symmetric_twins(std::vector<LeafSrc> &lr_src) {
         W.m      = L.n;
         W.n      = L.m;
         lr_h.push_back(W);
-        lr_src.push_back({lr_src[l].buf, lr_src[l].sv, lr_src[l].su});
+        // complex real form: the twin of a symmetric block is R(B^T) =
+        // J R(B)^T J (both factors copied as J X J once more), that of a
+        // Hermitian block R(B^H) = R(B)^T
+        const int neg = complex_ && symmetry_ == 'S' ? lr_src[l].neg ^ 1 : lr_src[l].neg;
+        lr_src.push_back({lr_src[l].buf, lr_src[l].sv, lr_src[l].su, neg});
     }
     for (int d = 0; d < ndn_stored_; d++) {
         const DenseLeaf D = dn_h[d];
@@ -133,7 +151,6 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
         require(kd.id == 2, "a complex H-matrix needs the Helmholtz device generator (id 2)", 2);
     else
         require(kd.id == 0 || kd.id == 1, "device generator id must be 0 (1/(1e-5+r)) or 1 (Laplace) for a real H-matrix", 2);
-    require(!complex_ || (compression_ == 0 && symmetry_ == 'N'), "complex H-matrices take partialACA and no symmetry", 2);
     nlr_stored_ = ndn_stored_ = -1;
     // block tree and ACA on the trees of the points; a complex H-matrix is
     // stored in real form on doubled trees (T, S), its leaves scaled by f
@@ -234,6 +251,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
     struct Accepted {
         int req, round, r;
         long long u, v; // offsets in the round's packed buffer
+        int neg;        // complex mirror: both factors copied as J X J
     };
     std::vector<Accepted> acc;
     std::vector<std::unique_ptr<DevBuf<double>>> round_bufs;
@@ -326,9 +344,12 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
             st_.aca_peak_scratch_bytes = std::max(st_.aca_peak_scratch_bytes, 8 * sc);
             flags.alloc(fl);
             dranks.alloc(blocks.size());
-            if (complex_)
-                launch_partial_aca_z(dblocks.p, (int)blocks.size(), dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
-            else {
+            if (complex_) {
+                if (n_direct > 0)
+                    launch_partial_aca_z(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+                if ((int)blocks.size() > n_direct)
+                    launch_partial_aca_z(dblocks.p + n_direct, (int)blocks.size() - n_direct, dxs.p, dxt.p, aca_ps, aca_pt, kd, eps_, scratch.p, flags.p, dranks.p + n_direct, stream_);
+            } else {
                 if (n_direct > 0)
                     launch_partial_aca(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
                 if ((int)blocks.size() > n_direct)
@@ -367,9 +388,11 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
                     packed += (long long)f * f * r * (it.M + it.N);
                     items.push_back(it);
                     if ((int)b < n_direct)
-                        acc.push_back({id, round, r, it.dst_u, it.dst_v});
-                    else // mirrored: U of the block is V^T of the mirror and V^T its U
-                        acc.push_back({id, round, r, it.dst_v, it.dst_u});
+                        acc.push_back({id, round, r, it.dst_u, it.dst_v, 0});
+                    else // mirrored: U of the block is V^T of the mirror and V^T its U; in
+                         // real form R(X^T) = J R(X)^T J (J = diag(1, -1, ..)), so both
+                         // stored factors are copied as J X J
+                        acc.push_back({id, round, r, it.dst_v, it.dst_u, complex_ ? 1 : 0});
                 } else if (r == -1) {
                     st_.false_positive++;
                     split(id);
@@ -448,7 +471,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
         L.nch   = 0;
         L.a_off = 0;
         lr_h.push_back(L);
-        lr_src.push_back({a.round, a.u, a.v});
+        lr_src.push_back({a.round, a.u, a.v, a.neg});
     }
     std::sort(dense_ts.begin(), dense_ts.end(), [&](const std::pair<int, int> &a, const std::pair<int, int> &b) {
         int ia = Ta.nodes[a.first].offset, ib = Ta.nodes[b.first].offset;
@@ -459,7 +482,7 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
     dn_h.clear();
     for (auto &d : dense_ts)
         dn_h.push_back({f * Ta.nodes[d.first].offset, f * Sa.nodes[d.second].offset, f * Ta.nodes[d.first].size, f * Sa.nodes[d.second].size});
-    if (symmetry_ == 'S')
+    if (symmetry_ != 'N')
         add_symmetric_twins(lr_src);
     std::vector<const double *> bufs;
     for (auto &b : round_bufs)
@@ -564,7 +587,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
             it.pad   = 0;
             it.off   = off;
             p1_h.push_back(it);
-            copies[lr_src[l].buf].push_back({lr_src[l].sv + it.j0, off, it.jlen, L.r, L.n, 0});
+            copies[lr_src[l].buf].push_back({lr_src[l].sv + it.j0, off, it.jlen, L.r, L.n, lr_src[l].neg ? 1 | (it.j0 & 1) << 1 : 0});
             off += even((long long)it.jlen * L.r);
         }
     }
@@ -628,7 +651,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
                     const LrLeaf &L = lr_h[leaf];
                     pc.w            = L.r;
                     pc.aux          = (int)L.a_off;
-                    copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + lo, pc.off, it.h, L.r, L.m, 0});
+                    copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + lo, pc.off, it.h, L.r, L.m, lr_src[leaf].neg ? 1 | (lo & 1) << 1 : 0});
                     for (int k = 0; k < L.r; k++)
                         cidx_h.push_back((int)L.a_off + k);
                 } else {
@@ -638,7 +661,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
                     if (dn_src)
                         copies[(*dn_src)[~leaf].buf].push_back({(*dn_src)[~leaf].su + lo, pc.off, it.h, D.n, D.m, 0});
                     else
-                        fills.push_back({pc.off, oi + lo, it.h, D.oj, D.n});
+                        fills.push_back({pc.off, oi + lo, it.h, D.oj, D.n, dense_mode(~leaf), 0});
                     for (int j = 0; j < D.n; j++)
                         cidx_h.push_back(~(D.oj + j));
                 }
@@ -1426,6 +1449,25 @@ void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptr
     }
     require(mu >= 1, "number of right-hand sides must be positive");
     HTGPU_CUDA(cudaSetDevice(device_));
+    if (symmetry_ == 'H') { // H^T = conj(H), applied as conj(H conj(x)) (hmatrix.hpp:1282-1287)
+        const long long nin = (long long)nr * mu, nout = (long long)nc * mu;
+        if (host_ptrs) {
+            std::vector<double> xc(in, in + nin);
+            for (long long i = 1; i < nin; i += 2)
+                xc[i] = -xc[i];
+            mvprod(xc.data(), out, mu, true, false, st);
+            for (long long i = 1; i < nout; i += 2)
+                out[i] = -out[i];
+            return;
+        }
+        cudaStream_t s2 = st ? st : stream_;
+        if (conj_in_.n < (std::size_t)nin)
+            conj_in_.alloc(nin);
+        launch_conj(in, conj_in_.p, nin, s2);
+        mvprod(conj_in_.p, out, mu, false, false, s2);
+        launch_conj(out, out, nout, s2);
+        return;
+    }
     if (!transp_) {
         // leaves of H^T from the stored ones (one pass through host memory)
         std::vector<int> lr(5 * lr_h.size()), dn(4 * dn_h.size());
@@ -1611,8 +1653,10 @@ std::map<std::string, std::string> HMatrix::infos() const {
     double compressed = 0;
     for (auto &L : lrs)
         compressed += (double)L.r * ((double)L.m + (double)L.n);
-    for (auto &D : dns) // a symmetric H-matrix counts its square diagonal blocks once (hmatrix.hpp:1615-1619)
-        compressed += (symmetry_ != 'N' && D.oi == D.oj && D.m == D.n) ? ((double)D.m * ((double)D.n + 1)) / 2 : (double)D.m * (double)D.n;
+    for (auto &D : dns) { // a symmetric H-matrix counts its square diagonal blocks once (hmatrix.hpp:1615-1619)
+        const double dm = (double)(D.m / f), dn = (double)(D.n / f); // complex sizes
+        compressed += f * f * ((symmetry_ != 'N' && D.oi == D.oj && D.m == D.n) ? dm * (dn + 1) / 2 : dm * dn);
+    }
     const double uncompressed = (double)((long)nr) * nc;
     m["Source_size"]              = inum(nci);
     m["Target_size"]              = inum(nri);

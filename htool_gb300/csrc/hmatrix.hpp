@@ -149,7 +149,9 @@ class HMatrix {
     struct LeafSrc {
         int buf;
         long long su, sv;
+        int neg = 0; // complex real form: copy both factors as J X J (BlockCopy::neg)
     };
+    int dense_mode(int d) const; // DenseMode of the fill of dense leaf d
     void finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs);
     void assign_phase1_modes();
     void ensure_work(int mu);

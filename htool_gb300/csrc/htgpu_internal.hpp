@@ -154,14 +154,24 @@ struct P2Contrib { // block h x w (column-major, ld h) at off; aux >= 0: low-ran
     int w, aux;    // coefficients x[~aux ...]
 };
 
-struct BlockCopy { // rows x cols, column-major ld_src at src -> contiguous at dst
+// rows x cols, column-major ld_src at src -> contiguous at dst; neg bit 0:
+// copy J X J (J = diag(1, -1, 1, ..)), i.e. negate the entries whose row and
+// column indices differ in parity, the row index counted in the source from
+// bit 1 of neg: a complex factor in real form R(X) becomes R(conj(X))
+// (J R(X)^T J = R(X^T) for the transposed roles)
+struct BlockCopy {
     long long src, dst;
-    int rows, cols, ld_src, pad;
+    int rows, cols, ld_src, neg;
 };
+
+// complex dense fills of symmetric H-matrices: the entries as generated, their
+// conjugates (the twin of a Hermitian block), or the Hermitian completion of
+// a diagonal block from its lower ('L') / upper ('U') triangle
+enum DenseMode : int { kDenseAsIs = 0, kDenseConj = 1, kDenseHermL = 2, kDenseHermU = 3 };
 
 struct DenseChunk { // dense rows row0 .. row0+h (cluster numbering) x columns oj .. oj+n
     long long dst;
-    int row0, h, oj, n;
+    int row0, h, oj, n, mode, pad;
 };
 
 struct F2 { // a double split into an unevaluated float sum hi + lo (df64.cuh)

@@ -342,9 +342,11 @@ double ref_hmatrix_time_mvprod_d(void *p, const double *x, double *y, int mu, in
 }
 
 // "key=value\n" lines of HMatrix::get_infos (hmatrix.hpp:739-841)
-int ref_hmatrix_infos_d(void *p, char *buf, int len) {
+extern "C++" {
+template <typename T>
+static int infos(void *p, char *buf, int len) {
     std::ostringstream os;
-    for (auto &kv : ((RefHMat<double> *)p)->h->get_infos())
+    for (auto &kv : ((RefHMat<T> *)p)->h->get_infos())
         os << kv.first << "=" << kv.second << "\n";
     std::string s = os.str();
     if (buf && len > 0) {
@@ -353,6 +355,9 @@ int ref_hmatrix_infos_d(void *p, char *buf, int len) {
     }
     return (int)s.size() + 1;
 }
+}
+int ref_hmatrix_infos_d(void *p, char *buf, int len) { return infos<double>(p, buf, len); }
+int ref_hmatrix_infos_z(void *p, char *buf, int len) { return infos<std::complex<double>>(p, buf, len); }
 double ref_hmatrix_compression_ratio_d(void *p) { return ((RefHMat<double> *)p)->h->compression_ratio(); }
 double ref_hmatrix_space_saving_d(void *p) { return ((RefHMat<double> *)p)->h->space_saving(); }
 

@@ -19,6 +19,7 @@ Usage (needs the upstream sources, i.e. only in the build container):
     python tests/golden/make_golden.py plot     # the save_plot leaf maps only
     python tests/golden/make_golden.py sym      # the symmetric / sympartialACA builds only
     python tests/golden/make_golden.py ztransp  # transposed products of the Helmholtz fixture
+    python tests/golden/make_golden.py zsym     # symmetric / Hermitian complex H-matrices
 """
 import ctypes as C
 import hashlib
@@ -216,6 +217,66 @@ def ztransp_case():
     np.savez_compressed(os.path.join(OUT, "helmholtz_cube2000_transp.npz"), **data)
 
 
+ZSYM_CASES = [
+    # name, compressor (0 partialACA, 1 sympartialACA), symmetry, UPLO, one-array build
+    ("helmholtz_cube2000_zsymSU", 1, "S", "U", True),
+    ("helmholtz_cube2000_zsymSL", 1, "S", "L", True),
+    ("helmholtz_cube2000_zsymHU", 1, "H", "U", True),
+    ("helmholtz_cube2000_zsymHL", 1, "H", "L", True),
+    ("helmholtz_cube2000_zsymaca", 1, "N", "N", False),
+]
+
+
+def zsym_cases():
+    """complex H-matrices of the Helmholtz fixture geometry stored as one
+    triangle ('S' complex symmetric, 'H' Hermitian) and the sympartialACA
+    build of a non-symmetric one, built by upstream: leaf lists, infos,
+    products and transposed products"""
+    R = Oracle("reference")
+    R.set_num_threads(1)
+    L, vp = R._L, C.c_void_p
+    L.ref_hmatrix_build_z.restype = vp
+    L.ref_hmatrix_build_z.argtypes = [vp, vp, C.c_int, vp, C.c_int, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char, C.c_int]
+    L.ref_hmatrix_counts_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_leaves_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_mvprod_z.argtypes = [vp, vp, vp, C.c_int]
+    L.ref_hmatrix_mvprod_transp_z.argtypes = [vp, vp, vp, C.c_int]
+    L.ref_hmatrix_infos_z.argtypes = [vp, vp, C.c_int]
+    L.ref_hmatrix_free_z.argtypes = [vp]
+    n, k, eps, eta = 2000, 20.0, 1e-5, 3.0
+    pts = G.cube_surface(n, seed=1)
+    ct = R.cluster(pts)
+    for name, comp, sym, uplo, one in ZSYM_CASES:
+        h = L.ref_hmatrix_build_z(ct.h, ct.h, n, pts.ctypes.data, n, pts.ctypes.data, k, eps, eta, comp, sym.encode(), uplo.encode(), int(one))
+        assert h, name
+        nlr, nd = C.c_int(), C.c_int()
+        L.ref_hmatrix_counts_z(h, C.byref(nlr), C.byref(nd))
+        lr = np.empty((nlr.value, 5), np.int32)
+        dn = np.empty((nd.value, 4), np.int32)
+        L.ref_hmatrix_leaves_z(h, lr.ctypes.data, dn.ctypes.data)
+        data = dict(xt=pts, lr=lr, dense=dn)
+        rng = np.random.default_rng(13)
+        for mu in (1, 3):
+            x = rng.standard_normal(n * mu) + 1j * rng.standard_normal(n * mu)
+            y = np.empty(n * mu, np.complex128)
+            L.ref_hmatrix_mvprod_z(h, x.ctypes.data, y.ctypes.data, mu)
+            data["x_mu%d" % mu] = x
+            data["y_mu%d" % mu] = y
+            yT = np.empty(n * mu, np.complex128)
+            L.ref_hmatrix_mvprod_transp_z(h, x.ctypes.data, yT.ctypes.data, mu)
+            data["yT_mu%d" % mu] = yT
+        m = L.ref_hmatrix_infos_z(h, None, 0)
+        buf = C.create_string_buffer(m)
+        L.ref_hmatrix_infos_z(h, buf, m)
+        infos = dict(l.split("=", 1) for l in buf.value.decode().splitlines() if "=" in l)
+        L.ref_hmatrix_free_z(h)
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
+        meta = dict(kernel=2, wavenumber=k, eps=eps, eta=eta, compressor=comp, symmetry=sym, uplo=uplo, one_array_build=one, infos=infos)
+        with open(os.path.join(OUT, name + ".json"), "w") as f:
+            json.dump(meta, f, indent=1, sort_keys=True)
+        print(name, "leaves", lr.shape[0], dn.shape[0], "ranks", lr[:, 4].min(), lr[:, 4].max())
+
+
 def plot_cases():
     """htool's leaf maps (HMatrix::save_plot) of the configuration-1 and
     Helmholtz fixtures, written by upstream itself (one thread)"""
@@ -243,5 +304,7 @@ if __name__ == "__main__":
         sym_cases()
     elif sys.argv[1:] == ["ztransp"]:
         ztransp_case()
+    elif sys.argv[1:] == ["zsym"]:
+        zsym_cases()
     else:
         main()

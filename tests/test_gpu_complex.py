@@ -77,3 +77,39 @@ def test_complex_transposed_products_match_upstream(case):
     hm.set_precision("mixed")
     assert rel(hm.mvprod_transp_global_to_global(gt["xT_mu1"]), gt["yT_mu1"]) < 1e-4
     hm.set_precision("fp64")
+
+
+ZSYM = ["helmholtz_cube2000_zsymSU", "helmholtz_cube2000_zsymSL", "helmholtz_cube2000_zsymHU", "helmholtz_cube2000_zsymHL", "helmholtz_cube2000_zsymaca"]
+
+
+@pytest.mark.parametrize("name", ZSYM)
+def test_complex_symmetric_matches_upstream(golden, name):
+    """Complex symmetric ('S') and Hermitian ('H') H-matrices storing one
+    triangle (sympartialACA, build(mat, xt)), and the sympartialACA build
+    of a non-symmetric one: upstream's leaf partition, ranks and infos, its
+    products and transposed products (hmatrix.hpp:843-911, 1277-1287) for
+    one and three right-hand sides, host and reduced-precision storage."""
+    g, meta = golden(name)
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    hm = H.HMatrix(t, t, meta["eps"], meta["eta"], symmetry=meta["symmetry"], UPLO=meta["uplo"], dtype=np.complex128)
+    hm.set_compression(meta["compressor"])
+    if meta["one_array_build"]:
+        hm.build_sym(H.HELMHOLTZ, g["xt"], kernel_param=meta["wavenumber"])
+    else:
+        hm.build(H.HELMHOLTZ, g["xt"], kernel_param=meta["wavenumber"])
+    lr, dn = hm.get_leaves()  # real form: every size doubled; upstream's leaves only
+    assert np.array_equal(lr // 2, g["lr"])
+    assert np.array_equal(dn // 2, g["dense"])
+    info, ref = hm.get_infos(), meta["infos"]
+    for key in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_min", "Dense_block_size_max", "Low_rank_block_size_max"):
+        assert info[key] == ref[key], key
+    for key in ("Compression_ratio", "Space_saving", "Rank_mean"):
+        assert abs(float(info[key]) - float(ref[key])) <= 1e-5 * abs(float(ref[key])), key
+    for mu in (1, 3):
+        assert rel(hm.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < 1e-10
+        assert rel(hm.mvprod_transp_global_to_global(g["x_mu%d" % mu], mu), g["yT_mu%d" % mu]) < 1e-10
+    hm.set_precision("mixed")
+    assert rel(hm.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-4
+    hm.set_precision("fp64")
+    assert hm.device_status() == 0
