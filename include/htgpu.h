@@ -123,11 +123,13 @@ int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, con
 int htgpu_hmatrix_build_sym(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt);
 
 /* Before a build: the symmetry and UPLO arguments of HMatrix's constructor
- * (hmatrix.hpp:115-122): 'N' with 'N', or 'S' with 'U' / 'L' -- one triangle
- * of the block tree is stored (ComputeAdmissibleBlocksSym recursion,
- * hmatrix.hpp:610-700) and products apply every stored off-diagonal leaf and
- * its transpose (hmatrix.hpp:844-911); t and s must be the same tree.  'H'
- * (complex Hermitian) is not available. */
+ * (hmatrix.hpp:115-122): 'N' with 'N', or 'S' / 'H' with 'U' / 'L' -- one
+ * triangle of the block tree is stored (ComputeAdmissibleBlocksSym
+ * recursion, hmatrix.hpp:610-700) and products apply every stored
+ * off-diagonal leaf and its transpose ('S') or conjugate transpose ('H'),
+ * diagonal blocks as symv / hemv read their UPLO triangle
+ * (hmatrix.hpp:844-911, matrix.hpp:386-447); t and s must be the same tree.
+ * 'H' needs a complex handle. */
 int htgpu_hmatrix_set_symmetry(htgpu_hmatrix h, char symmetry, char uplo);
 
 /* Before a build: set_compression (hmatrix.hpp:220) with
