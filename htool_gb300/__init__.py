@@ -54,6 +54,7 @@ def _load():
         "htgpu_block_tasks_sym": (i, [vp, vp, d, C.c_char, i, vp, vp]),
         "htgpu_hmatrix_build_sym": (i, [vp, i, d, vp]),
         "htgpu_hmatrix_set_symmetry": (i, [vp, C.c_char, C.c_char]),
+        "htgpu_hmatrix_get_symmetry": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_compression": (i, [vp, i]),
         "htgpu_hmatrix_create": (i, [vp, vp, d, d, i, vp]),
         "htgpu_hmatrix_destroy": (i, [vp]),
@@ -481,8 +482,12 @@ class HMatrix:
         _check(lib.htgpu_hmatrix_save_plot(self.h, str(outputname).encode()))
 
     def load(self, path):
-        """Leaves and factors from a dump made on the same cluster trees."""
+        """Leaves and factors from a dump made on the same cluster trees
+        (the dump's symmetry and UPLO come with it)."""
         _check(lib.htgpu_hmatrix_load(self.h, str(path).encode()))
+        s, u = C.c_char(), C.c_char()
+        _check(lib.htgpu_hmatrix_get_symmetry(self.h, C.byref(s), C.byref(u)))
+        self.symmetry, self.UPLO = s.value.decode(), u.value.decode()
         return self
 
     def set_rank_predictor(self, predictor, margin=0.25):

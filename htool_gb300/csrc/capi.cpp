@@ -232,6 +232,16 @@ int htgpu_hmatrix_set_symmetry(htgpu_hmatrix h, char symmetry, char uplo) {
     });
 }
 
+int htgpu_hmatrix_get_symmetry(htgpu_hmatrix h, char *symmetry, char *uplo) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(symmetry, "symmetry");
+        need(uplo, "uplo");
+        *symmetry = h->h->symmetry();
+        *uplo     = h->h->uplo();
+    });
+}
+
 int htgpu_hmatrix_set_compression(htgpu_hmatrix h, int compressor) {
     return guarded([&] {
         need(h, "hmatrix");

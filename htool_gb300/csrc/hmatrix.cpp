@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <set>
 #include <numeric>
 #include <sstream>
 
@@ -492,7 +493,6 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
 }
 
 void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dn) {
-    require(symmetry_ == 'N', "adopting leaves of a symmetric H-matrix is not available", 2);
     nlr_stored_ = ndn_stored_ = -1;
     HTGPU_CUDA(cudaSetDevice(device_));
     lr_h.clear();
@@ -542,6 +542,30 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
         const long long e = (long long)dn_h[d].m * dn_h[d].n;
         std::copy(dn + dsrc, dn + dsrc + e, host.begin() + dn_src[d].su);
         dsrc += e;
+    }
+    if (symmetry_ != 'N') {
+        // one triangle as given: every off-diagonal leaf gets its twin, a
+        // dense twin being the transposed copy of its block (J X J for a
+        // complex-symmetric block in real form, BlockCopy::neg)
+        std::set<std::pair<int, int>> seen;
+        for (auto &L : lr_h)
+            require(seen.insert({L.oi, L.oj}).second, "two leaves of a symmetric H-matrix share a block");
+        for (auto &D : dn_h)
+            require(seen.insert({D.oi, D.oj}).second, "two leaves of a symmetric H-matrix share a block");
+        for (auto &L : lr_h)
+            require(L.oi == L.oj || !seen.count({L.oj, L.oi}), "a symmetric H-matrix stores one of two mirrored blocks");
+        for (auto &D : dn_h)
+            require(D.oi == D.oj ? D.m == D.n : !seen.count({D.oj, D.oi}), "a symmetric H-matrix stores one of two mirrored blocks, and square diagonal blocks");
+        for (auto &L : lr_h)
+            require(L.oi != L.oj, "a diagonal block of a symmetric H-matrix is dense");
+        add_symmetric_twins(lr_src);
+        for (int d = 0; d < ndn_stored_; d++)
+            if (dn_h[d].oi != dn_h[d].oj) {
+                LeafSrc w = dn_src[d];
+                w.neg     = complex_ && symmetry_ == 'S' ? 1 : 0;
+                w.tr      = 1;
+                dn_src.push_back(w);
+            }
     }
     DevBuf<double> staging;
     staging.upload(host, stream_);
@@ -658,8 +682,11 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
                     const DenseLeaf &D = dn_h[~leaf];
                     pc.w               = D.n;
                     pc.aux             = ~D.oj;
-                    if (dn_src)
-                        copies[(*dn_src)[~leaf].buf].push_back({(*dn_src)[~leaf].su + lo, pc.off, it.h, D.n, D.m, 0});
+                    const LeafSrc *ds = dn_src ? &(*dn_src)[~leaf] : nullptr;
+                    if (ds && ds->tr) // rows lo.. of the transposed block: columns lo.. of the stored one (D.n x D.m)
+                        copies[ds->buf].push_back({ds->su + (long long)D.n * lo, pc.off, it.h, D.n, D.n, (ds->neg ? 1 | (lo & 1) << 1 : 0) | 4});
+                    else if (ds)
+                        copies[ds->buf].push_back({ds->su + lo, pc.off, it.h, D.n, D.m, ds->neg ? 1 | (lo & 1) << 1 : 0});
                     else
                         fills.push_back({pc.off, oi + lo, it.h, D.oj, D.n, dense_mode(~leaf), 0});
                     for (int j = 0; j < D.n; j++)

@@ -150,6 +150,7 @@ class HMatrix {
         int buf;
         long long su, sv;
         int neg = 0; // complex real form: copy both factors as J X J (BlockCopy::neg)
+        int tr  = 0; // dense: the leaf is the transpose of the block at su (D.n x D.m stored)
     };
     int dense_mode(int d) const; // DenseMode of the fill of dense leaf d
     void finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs);

@@ -156,9 +156,10 @@ struct P2Contrib { // block h x w (column-major, ld h) at off; aux >= 0: low-ran
 
 // rows x cols, column-major ld_src at src -> contiguous at dst; neg bit 0:
 // copy J X J (J = diag(1, -1, 1, ..)), i.e. negate the entries whose row and
-// column indices differ in parity, the row index counted in the source from
-// bit 1 of neg: a complex factor in real form R(X) becomes R(conj(X))
-// (J R(X)^T J = R(X^T) for the transposed roles)
+// column indices differ in parity, the row index counted from bit 1 of neg:
+// a complex factor in real form R(X) becomes R(conj(X)) (J R(X)^T J =
+// R(X^T) for the transposed roles); bit 2: the source is read transposed,
+// entry (i, k) at src + k + ld_src i
 struct BlockCopy {
     long long src, dst;
     int rows, cols, ld_src, neg;

@@ -156,8 +156,12 @@ ClusterTree read_cluster(const std::string &perm_file, const std::string &tree_f
     return T;
 }
 
+// Binary dump: magic, version (2), nr, nc, leaf counts, eps, eta, hashes of
+// both permutations, symmetry / UPLO / complex flag, then htool's leaves
+// (a symmetric H-matrix: the stored triangle; load makes the twins again)
+// and their factors in the set_leaves layout.  Version 1 (no symmetry
+// record) still loads.
 void HMatrix::save(const std::string &path) {
-    require(symmetry_ == 'N', "dumps of symmetric H-matrices are not available", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
     std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
@@ -170,15 +174,17 @@ void HMatrix::save(const std::string &path) {
     export_factors(uv.data(), dd.data());
     std::ofstream f(path, std::ios::binary);
     require((bool)f, "cannot write " + path, 3);
-    const std::uint32_t version = 1;
+    const std::uint32_t version = 2;
     const std::int64_t hdr[4]   = {nr, nc, (std::int64_t)n_lowrank(), (std::int64_t)n_dense()};
     const double par[2]         = {eps_, eta_};
     const std::uint64_t hash[2] = {fnv1a(T->perm), fnv1a(S->perm)};
+    const char sym[8]           = {symmetry_, uplo_, (char)(complex_ ? 1 : 0), 0, 0, 0, 0, 0};
     f.write(kMagic, 8);
     f.write((const char *)&version, 4);
     f.write((const char *)hdr, sizeof(hdr));
     f.write((const char *)par, sizeof(par));
     f.write((const char *)hash, sizeof(hash));
+    f.write(sym, 8);
     f.write((const char *)lr.data(), sizeof(int) * lr.size());
     f.write((const char *)dn.data(), sizeof(int) * dn.size());
     f.write((const char *)uv.data(), sizeof(double) * nuv);
@@ -207,7 +213,6 @@ void HMatrix::save_plot(const std::string &outputname) const {
 }
 
 void HMatrix::load(const std::string &path) {
-    require(symmetry_ == 'N', "dumps of symmetric H-matrices are not available", 2);
     std::ifstream f(path, std::ios::binary);
     require((bool)f, "cannot open " + path);
     char magic[8];
@@ -220,8 +225,14 @@ void HMatrix::load(const std::string &path) {
     f.read((char *)hdr, sizeof(hdr));
     f.read((char *)par, sizeof(par));
     f.read((char *)hash, sizeof(hash));
-    require((bool)f && std::memcmp(magic, kMagic, 8) == 0 && version == 1, path + " is not an H-matrix dump");
+    require((bool)f && std::memcmp(magic, kMagic, 8) == 0 && (version == 1 || version == 2), path + " is not an H-matrix dump");
     require(hdr[0] == nr && hdr[1] == nc && hash[0] == fnv1a(T->perm) && hash[1] == fnv1a(S->perm), path + " was saved on other cluster trees");
+    char sym[8] = {'N', 'N', 0, 0, 0, 0, 0, 0};
+    if (version == 2)
+        f.read(sym, 8);
+    require((bool)f, path + " is truncated");
+    require((sym[2] != 0) == complex_, path + (complex_ ? " holds a real H-matrix" : " holds a complex H-matrix"));
+    set_symmetry(sym[0], sym[1]); // the dump's storage (checks the combination and the trees)
     const std::int64_t nlr = hdr[2], nd = hdr[3];
     require(nlr >= 0 && nd >= 0 && nlr < (1LL << 31) && nd < (1LL << 31), path + ": bad leaf counts");
     std::vector<int> lr(5 * nlr), dn(4 * nd);

@@ -283,8 +283,8 @@ __global__ void block_copy_kernel(const BlockCopy *__restrict__ items, const dou
     const long long tot = (long long)b.rows * b.cols;
     for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
         const int i = (int)(e % b.rows), k = (int)(e / b.rows);
-        const double v = src[b.src + i + (long long)b.ld_src * k];
-        dst[b.dst + e] = ((b.neg & 1) && (((i + (b.neg >> 1)) ^ k) & 1)) ? -v : v;
+        const double v = (b.neg & 4) ? src[b.src + k + (long long)b.ld_src * i] : src[b.src + i + (long long)b.ld_src * k];
+        dst[b.dst + e] = ((b.neg & 1) && (((i + ((b.neg >> 1) & 1)) ^ k) & 1)) ? -v : v;
     }
 }
 

@@ -131,6 +131,7 @@ int htgpu_hmatrix_build_sym(htgpu_hmatrix h, int kernel_id, double kernel_param,
  * (hmatrix.hpp:844-911, matrix.hpp:386-447); t and s must be the same tree.
  * 'H' needs a complex handle. */
 int htgpu_hmatrix_set_symmetry(htgpu_hmatrix h, char symmetry, char uplo);
+int htgpu_hmatrix_get_symmetry(htgpu_hmatrix h, char *symmetry, char *uplo);
 
 /* Before a build: set_compression (hmatrix.hpp:220) with
  * HTGPU_COMPRESSION_PARTIAL_ACA (lrmat/partialACA.hpp:39-171, the default of
@@ -147,7 +148,10 @@ int htgpu_hmatrix_set_compression(htgpu_hmatrix h, int compressor);
  * lr_desc[5 * b ...] = offset_i, offset_j, m, n, rank (cluster numbering);
  * uv = for each low-rank leaf in order, U (m x rank, column-major) then
  * V (rank x n, column-major); d_desc[4 * b ...] = offset_i, offset_j, m, n;
- * dense = each dense leaf m x n column-major.  Host memory; copied. */
+ * dense = each dense leaf m x n column-major.  Host memory; copied.  On a
+ * handle with symmetry 'S' / 'H' the leaves are one triangle (diagonal
+ * blocks dense and square, no block together with its mirror) and the
+ * product adds every off-diagonal leaf's (conjugate) transpose. */
 int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const double *uv, int ndense, const int *d_desc, const double *dense);
 
 /* Replaces HMatrix<double>::mvprod_global_to_global(in, out, mu)
@@ -373,9 +377,11 @@ int htgpu_cluster_save(htgpu_cluster c, const char *name);
 int htgpu_cluster_read(const char *perm_file, const char *tree_file, htgpu_cluster *out);
 
 /* Binary dump of an assembled H-matrix (leaf lists and factors in htool's
- * layout, sizes and permutation hashes in the header; no counterpart in the
- * reference) and its reload into a handle on the same cluster trees, e.g.
- * to reuse a large build. */
+ * layout, sizes, permutation hashes, symmetry / UPLO and the complex flag in
+ * the header; no counterpart in the reference) and its reload into a handle
+ * of the same type on the same cluster trees, e.g. to reuse a large build.
+ * A symmetric H-matrix dumps its stored triangle; the reload takes the
+ * dump's symmetry and makes the twins again (bitwise the same products). */
 int htgpu_hmatrix_save(htgpu_hmatrix h, const char *path);
 int htgpu_hmatrix_load(htgpu_hmatrix h, const char *path);
 

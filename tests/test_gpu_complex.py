@@ -83,7 +83,7 @@ ZSYM = ["helmholtz_cube2000_zsymSU", "helmholtz_cube2000_zsymSL", "helmholtz_cub
 
 
 @pytest.mark.parametrize("name", ZSYM)
-def test_complex_symmetric_matches_upstream(golden, name):
+def test_complex_symmetric_matches_upstream(golden, name, tmp_path):
     """Complex symmetric ('S') and Hermitian ('H') H-matrices storing one
     triangle (sympartialACA, build(mat, xt)), and the sympartialACA build
     of a non-symmetric one: upstream's leaf partition, ranks and infos, its
@@ -112,4 +112,14 @@ def test_complex_symmetric_matches_upstream(golden, name):
     hm.set_precision("mixed")
     assert rel(hm.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-4
     hm.set_precision("fp64")
+    # dump of the stored triangle, reloaded into a plain complex handle: the
+    # twins come back as transposed copies, bitwise the same products
+    hm.save(tmp_path / "z.bin")
+    h2 = H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128).load(tmp_path / "z.bin")
+    assert (h2.symmetry, h2.UPLO) == (meta["symmetry"], meta["uplo"])
+    x3 = g["x_mu3"]
+    assert np.array_equal(h2.mvprod_global_to_global(x3, 3), hm.mvprod_global_to_global(x3, 3))
+    assert np.array_equal(h2.mvprod_transp_global_to_global(x3, 3), hm.mvprod_transp_global_to_global(x3, 3))
+    with pytest.raises(ValueError):  # a complex dump does not load into a real handle
+        H.HMatrix(t, t, meta["eps"], meta["eta"]).load(tmp_path / "z.bin")
     assert hm.device_status() == 0
