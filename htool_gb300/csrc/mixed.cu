@@ -343,6 +343,107 @@ void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const 
     HTGPU_CUDA(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------------------
+// Phase 2 of a reduced-precision product with many right-hand sides on the
+// tensor cores: per row chunk (h <= 32 rows), Z (h x mu) = U C over its FP32
+// / BF16 chunks, U the chunk columns as stored in lane order (column q of
+// slice q mod S = 32 / h, element ((g Ln + slice h + row) V + v) for
+// j = q / S = g V + v) and C their coefficients, the float phase-1 sums
+// gathered through the column indices.  mma.sync m16n8k8 TF32 with three
+// products per step as in phase 1, FP32 accumulation over the row chunk;
+// one warp per row chunk, right-hand sides in blocks of 64.  The row
+// chunk's z rows are written (FP64, x's exponent shift undone); its dense
+// FP64 chunks are added by the streamed kernel afterwards.
+__global__ void __launch_bounds__(32 * kMmaWarps) phase2_mma_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ mix,
+                                                                     const int *__restrict__ cidx, const double *__restrict__ A, const int *__restrict__ xexp, int mu,
+                                                                     double *__restrict__ z, int zlen) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int W    = gridDim.x * kMmaWarps;
+    const float *Af = reinterpret_cast<const float *>(A); // float phase-1 sums
+    const int shift = max(*xexp, 1) - 1023;
+    for (int w = blockIdx.x * kMmaWarps + (threadIdx.x >> 5); w < nrc; w += W) {
+        const int kb = rc[w], ke = rc[w + 1];
+        const StreamChunk head = chunks[kb];
+        const int h = head.h, zrow = head.b, nmt = h > 16 ? 2 : 1;
+        for (int cb = 0; cb < mu; cb += 64) {
+            const int nnt = min(8, (mu - cb + 7) >> 3); // 8-column tiles of this block
+            float acc[2][8][4];
+#pragma unroll
+            for (int a = 0; a < 2; a++)
+#pragma unroll
+                for (int b = 0; b < 8; b++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        acc[a][b][q] = 0.f;
+            for (int k = kb; k < ke; k++) {
+                const StreamChunk c = chunks[k];
+                if (c.kind != kStreamF32 && c.kind != kStreamBf16) // dense FP64: the streamed kernel
+                    continue;
+                const int S = 32 / h, Ln = S * h, lv = c.kind == kStreamF32 ? 2 : 3;
+                const unsigned char *base = mix + c.src;
+                auto uload = [&](int row, int q) -> float { // U[row][q], zero outside the chunk
+                    if (row >= h || q >= c.ncol)
+                        return 0.f;
+                    const int j = q / S, sl = q - j * S;
+                    const long long e = (((long long)(j >> lv) * Ln + sl * h + row) << lv) + (j & ((1 << lv) - 1));
+                    return lv == 2 ? reinterpret_cast<const float *>(base)[e] : bf16_to_f32(reinterpret_cast<const unsigned short *>(base)[e]);
+                };
+                for (int q0 = 0; q0 < c.ncol; q0 += 8) {
+                    unsigned ah[2][4], al[2][4];
+#pragma unroll
+                    for (int mt = 0; mt < 2; mt++) {
+                        const int r0 = 16 * mt + g;
+                        split_tf32(uload(r0, q0 + t), ah[mt][0], al[mt][0]);
+                        split_tf32(uload(r0 + 8, q0 + t), ah[mt][1], al[mt][1]);
+                        split_tf32(uload(r0, q0 + t + 4), ah[mt][2], al[mt][2]);
+                        split_tf32(uload(r0 + 8, q0 + t + 4), ah[mt][3], al[mt][3]);
+                    }
+                    // coefficient rows of columns q0 + t and q0 + t + 4 (phase-1 slots)
+                    const int kx0 = q0 + t < c.ncol ? cidx[c.a + q0 + t] : -1;
+                    const int kx1 = q0 + t + 4 < c.ncol ? cidx[c.a + q0 + t + 4] : -1;
+#pragma unroll
+                    for (int nt = 0; nt < 8; nt++) {
+                        if (nt >= nnt) // warp-uniform
+                            break;
+                        const int col  = cb + 8 * nt + g;
+                        const float b0 = (kx0 >= 0 && col < mu) ? __ldg(Af + (long long)kx0 * mu + col) : 0.f;
+                        const float b1 = (kx1 >= 0 && col < mu) ? __ldg(Af + (long long)kx1 * mu + col) : 0.f;
+                        unsigned bh0, bl0, bh1, bl1;
+                        split_tf32(b0, bh0, bl0);
+                        split_tf32(b1, bh1, bl1);
+#pragma unroll
+                        for (int mt = 0; mt < 2; mt++) {
+                            if (mt >= nmt) // warp-uniform
+                                break;
+                            mma_tf32(acc[mt][nt], al[mt], bh0, bh1);
+                            mma_tf32(acc[mt][nt], ah[mt], bl0, bl1);
+                            mma_tf32(acc[mt][nt], ah[mt], bh0, bh1);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int row = 16 * mt + g + 8 * (q >> 1), col = cb + 8 * nt + 2 * t + (q & 1);
+                        if (mt < nmt && nt < nnt && row < h && col < mu)
+                            z[(long long)col * zlen + zrow + row] = scale_pow2_safe((double)acc[mt][nt][q], shift);
+                    }
+        }
+    }
+}
+
+void launch_phase2_mma(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const double *A, const int *xexp, int mu, double *z, int zlen, cudaStream_t st) {
+    if (nrc <= 0)
+        return;
+    const int blocks = (nrc + kMmaWarps - 1) / kMmaWarps; // one warp per row chunk
+    phase2_mma_kernel<<<blocks, 32 * kMmaWarps, 0, st>>>(chunks, rc, nrc, mix, cidx, A, xexp, mu, z, zlen);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;

@@ -44,6 +44,24 @@ def test_complex_products_match_upstream(case):
     assert hm.device_status() == 0
 
 
+def test_complex_many_rhs_tensor_cores(case):
+    """The 64-right-hand-side complex product in reduced precision (both
+    low-rank contractions on the tensor cores, real form) against the FP64
+    product and upstream's three-right-hand-side product."""
+    g, meta, hm = case
+    n = g["xt"].shape[0]
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal(n * 64) + 1j * rng.standard_normal(n * 64)
+    X[: 3 * n] = g["x_mu3"]
+    y64 = hm.mvprod_global_to_global(X, 64)
+    hm.set_precision("mixed")
+    ym = hm.mvprod_global_to_global(X, 64)
+    hm.set_precision("fp64")
+    assert rel(ym, y64) < 1e-5
+    assert rel(ym[: 3 * n], g["y_mu3"]) < 1e-5
+    assert hm.device_status() == 0
+
+
 def test_complex_dense_rows_and_precision(case):
     g, meta, hm = case
     pts, x = g["xt"], g["x_mu1"]

@@ -320,20 +320,25 @@ def test_phase2_modes_bitwise(golden):
     assert GH.device_status() == 0
 
 
-def test_many_rhs_tensor_core_phase1(golden):
-    """Reduced-precision products with many right-hand sides run phase 1 on
-    the tensor cores (TF32, three products per step): every column agrees
-    with the FP64 product within the mixed tolerance and with the
-    one-right-hand-side product (CUDA-core kernels) to FP32 rounding, for
-    block sizes that fill 8-column tiles and one that does not."""
+def test_many_rhs_tensor_cores(golden):
+    """Reduced-precision products with many right-hand sides run both
+    low-rank contractions on the tensor cores (TF32, three products per
+    step; phase 2 writes the row chunks' low-rank sums, the dense FP64
+    chunks are added by the streamed kernel): every column agrees with the
+    FP64 product within the mixed tolerance and with the one-right-hand-side
+    product (CUDA-core kernels) to FP32 rounding, for block sizes that fill
+    8-column tiles and one that does not, with the dense blocks on DFMA or
+    the emulation and either phase-2 kernel."""
     g, meta = golden("sphere6000_k1")
     n = g["xt"].shape[0]
     t = H.Cluster().build(n, g["xt"])
     GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
-    for mu in (8, 13, 64):
+    for mu, split, mode in ((8, 1000, "producer"), (13, 350, "warp"), (64, 0, "producer"), (64, 1000, "warp")):
         X = G.rhs(n, mu, seed=20 + mu)
         y64 = GH.mvprod_global_to_global(X, mu)
         GH.set_precision("mixed")
+        GH.set_fp64_split(0, split)
+        GH.set_phase2_mode(mode)
         ym = GH.mvprod_global_to_global(X, mu)
         for c in range(0, mu, max(1, mu // 4)):
             col = slice(c * n, (c + 1) * n)
