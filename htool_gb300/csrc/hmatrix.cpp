@@ -1006,39 +1006,21 @@ void HMatrix::upload_mixed_phase2() {
     n_ranges_m_              = (int)r.size() - 1;
     srm_d.upload(r, stream_);
     sum_d.upload(stream_units(ch2_h_, stream2_units_target(), &n_units_m_), stream_);
-    // many right-hand sides: the FP32 / BF16 chunks of every row chunk on
-    // the tensor cores (first chunk of each row chunk), then the dense
-    // chunks alone through the streamed kernel, added onto z
+    // many right-hand sides: the first chunk of every row chunk, for the
+    // tensor-core pass over the FP32 / BF16 chunks and the double-float pass
+    // over the dense ones
     {
         std::vector<int> rc;
-        std::vector<StreamChunk> dense;
+        n_chunks_md_ = 0;
         for (std::size_t k = 0; k < ch2.size(); k++) {
             if (ch2[k].flags & kStreamFirst)
                 rc.push_back((int)k);
-            if (ch2[k].kind == kStreamDfma || ch2[k].kind == kStreamEmu) {
-                StreamChunk c = ch2[k];
-                c.flags &= ~(kStreamFirst | kStreamLast);
-                if (dense.empty() || (ch2[k].flags & kStreamFirst) || dense.back().b != c.b) {
-                    if (!dense.empty())
-                        dense.back().flags |= kStreamLast;
-                    c.flags |= kStreamFirst;
-                }
-                dense.push_back(c);
-            }
+            if (ch2[k].kind == kStreamDfma || ch2[k].kind == kStreamEmu)
+                n_chunks_md_++;
         }
-        if (!dense.empty())
-            dense.back().flags |= kStreamLast;
         n_p2rc_m_ = (int)rc.size();
         rc.push_back((int)ch2.size());
         p2rcm_d.upload(rc, stream_);
-        n_chunks_md_ = (long long)dense.size();
-        const std::vector<int> rd = stream_ranges(dense, n_sctas_);
-        n_ranges_md_              = (int)rd.size() - 1;
-        srmd_d.upload(rd, stream_);
-        sumd_d.upload(stream_units(dense, stream2_units_target(), &n_units_md_), stream_);
-        scmd_d.upload(dense, stream_);
-        if (dense.empty())
-            scmd_d.alloc(1);
     }
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
@@ -1307,12 +1289,9 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
             launches_ += 1;
             if (n_chunks_md_ > 0) {
-                if (p2_mode_ == 1)
-                    launch_phase2_producer(scmd_d.p, sumd_d.p, n_units_md_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp,
-                                           w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st, 1);
-                else
-                    launch_phase2_stream(scmd_d.p, srmd_d.p, n_ranges_md_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs,
-                                         w_xexp, mu, w_z, (int)zlen_, status_d.p, st, 1);
+                launch_dense_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_xs, w_xexp, mu, w_z,
+                                  (int)zlen_, st);
+                launches_ += 1;
             }
         } else if (p2_mode_ == 1)
             launch_phase2_producer(scm_d.p, sum_d.p, n_units_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,

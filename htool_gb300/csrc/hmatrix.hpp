@@ -240,10 +240,9 @@ class HMatrix {
     DevBuf<int> su_d, sum_d;           // phase-2 units (producer-fed) of the FP64 / reduced chunk lists
     int n_units_ = 0, n_units_m_ = 0;
     // reduced precision, many right-hand sides: first chunk of every row
-    // chunk (tensor-core phase 2) and the dense-only chunk list
-    DevBuf<int> p2rcm_d, srmd_d, sumd_d;
-    DevBuf<StreamChunk> scmd_d;
-    int n_p2rc_m_ = 0, n_ranges_md_ = 0, n_units_md_ = 0;
+    // chunk (tensor-core phase 2, then its dense chunks) and the dense chunk count
+    DevBuf<int> p2rcm_d;
+    int n_p2rc_m_ = 0;
     long long n_chunks_md_ = 0;
     // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced
     // storage), phase-2 columns, z values read by the final sums

@@ -67,19 +67,18 @@ void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z,
 // warps claim the chunk ranges rbeg[r] .. rbeg[r+1] (r < nranges) through
 // tickets (8 ints, reset by the launch); chunk bytes at arena0, or arena1
 // with kStreamArena1, or arena2 with kStreamPre (emulated chunks stored as
-// (hi, lo) float pairs); status: nonzero after a wait ran out; zadd: add the
-// row chunks' sums to z instead of writing them
+// (hi, lo) float pairs); status: nonzero after a wait ran out
 constexpr int kStreamWarpsPerCta = 4;
 int stream_ctas(); // CTAs per launch (all resident)
 void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
-                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st, int zadd = 0);
+                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
 // phase-2 mode 1: CTAs of one producer warp and consumer warps; the producer
 // claims units of whole row chunks (stream_units: nunits + 1 unit bounds in
 // row chunks, then the first chunk of every row chunk and the end) and feeds
 // its consumers
 constexpr int kUnitRowChunks = 31; // row chunks per unit at most
 void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx,
-                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st, int zadd = 0);
+                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
 std::vector<int> stream_units(const std::vector<StreamChunk> &chunks, int target, int *nunits);
 int stream2_units_target(); // units for a product launch on this device
 // phase 1 with one or two right-hand sides from stages of tile chunks
@@ -154,8 +153,12 @@ void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const 
 // phase 2 of a reduced-precision product with mu >= kMmaMinRhs: the FP32 /
 // BF16 chunks of every row chunk (rc: first chunk of row chunk i, nrc + 1
 // entries) on the tensor cores; writes the row chunk's z rows (the dense
-// chunks are added afterwards: launch_phase2_producer / stream with zadd)
+// chunks are added afterwards: launch_dense_mrhs)
 void launch_phase2_mma(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const double *A, const int *xexp, int mu, double *z, int zlen, cudaStream_t st);
+// the dense FP64 chunks of those row chunks added onto z (double-float on the
+// FP32 pipe; pre: the pre-split mirror of kStreamPre chunks)
+void launch_dense_mrhs(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *fac, const unsigned char *pre, const int *cidx, const F2 *xs, const int *xexp, int mu, double *z, int zlen,
+                       cudaStream_t st);
 // ---- ACA rank predictor (mlp.cu) -------------------------------------------
 constexpr int kMlpIn = 10, kMlpHidden = 64;
 constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;

@@ -353,20 +353,31 @@ void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const 
 // products per step as in phase 1, FP32 accumulation over the row chunk;
 // one warp per row chunk, right-hand sides in blocks of 64.  The row
 // chunk's z rows are written (FP64, x's exponent shift undone); its dense
-// FP64 chunks are added by the streamed kernel afterwards.
+// FP64 chunks are added afterwards by dense_mrhs_kernel.  Each chunk's bytes
+// and the coefficients of 32 of its columns are staged in the warp's shared
+// memory (every load issued before the first use), the fragments read there.
+// per warp: the chunk's bytes and the coefficients of up to 32 of its
+// columns for 64 right-hand sides (row stride 72 floats: the B fragments of
+// a step hit 32 distinct banks)
+constexpr int kP2Slab = 32, kP2CoefLd = 72;
+constexpr int kP2MmaSmem = kMmaWarps * (kStreamStage + 4 * kP2Slab * kP2CoefLd);
+
 __global__ void __launch_bounds__(32 * kMmaWarps) phase2_mma_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ mix,
                                                                      const int *__restrict__ cidx, const double *__restrict__ A, const int *__restrict__ xexp, int mu,
                                                                      double *__restrict__ z, int zlen) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int W    = gridDim.x * kMmaWarps;
-    const float *Af = reinterpret_cast<const float *>(A); // float phase-1 sums
-    const int shift = max(*xexp, 1) - 1023;
-    for (int w = blockIdx.x * kMmaWarps + (threadIdx.x >> 5); w < nrc; w += W) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int W      = gridDim.x * kMmaWarps;
+    unsigned char *sd = smem + (size_t)wid * (kStreamStage + 4 * kP2Slab * kP2CoefLd); // the chunk's bytes
+    float *scf        = reinterpret_cast<float *>(sd + kStreamStage);                   // coefficients [column][rhs]
+    const float *Af   = reinterpret_cast<const float *>(A);                             // float phase-1 sums
+    const int shift   = max(*xexp, 1) - 1023;
+    for (int w = blockIdx.x * kMmaWarps + wid; w < nrc; w += W) {
         const int kb = rc[w], ke = rc[w + 1];
         const StreamChunk head = chunks[kb];
         const int h = head.h, zrow = head.b, nmt = h > 16 ? 2 : 1;
         for (int cb = 0; cb < mu; cb += 64) {
-            const int nnt = min(8, (mu - cb + 7) >> 3); // 8-column tiles of this block
+            const int nn = min(64, mu - cb), nnt = (nn + 7) >> 3; // right-hand sides of this block, 8-column tiles
             float acc[2][8][4];
 #pragma unroll
             for (int a = 0; a < 2; a++)
@@ -379,45 +390,84 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase2_mma_kernel(const Stream
                 const StreamChunk c = chunks[k];
                 if (c.kind != kStreamF32 && c.kind != kStreamBf16) // dense FP64: the streamed kernel
                     continue;
+                // the chunk's bytes into shared memory: every load issued before the first store
+                {
+                    const uint4 *src = reinterpret_cast<const uint4 *>(mix + c.src);
+                    uint4 *dst       = reinterpret_cast<uint4 *>(sd);
+                    const int nw     = c.bytes >> 4; // <= 256
+                    uint4 r[kStreamStage / 512];
+                    __syncwarp(); // the previous chunk is read out
+#pragma unroll
+                    for (int i = 0; i < kStreamStage / 512; i++)
+                        r[i] = lane + 32 * i < nw ? __ldg(src + lane + 32 * i) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                    for (int i = 0; i < kStreamStage / 512; i++)
+                        if (lane + 32 * i < nw)
+                            dst[lane + 32 * i] = r[i];
+                }
                 const int S = 32 / h, Ln = S * h, lv = c.kind == kStreamF32 ? 2 : 3;
-                const unsigned char *base = mix + c.src;
                 auto uload = [&](int row, int q) -> float { // U[row][q], zero outside the chunk
                     if (row >= h || q >= c.ncol)
                         return 0.f;
                     const int j = q / S, sl = q - j * S;
-                    const long long e = (((long long)(j >> lv) * Ln + sl * h + row) << lv) + (j & ((1 << lv) - 1));
-                    return lv == 2 ? reinterpret_cast<const float *>(base)[e] : bf16_to_f32(reinterpret_cast<const unsigned short *>(base)[e]);
+                    const int e = (((j >> lv) * Ln + sl * h + row) << lv) + (j & ((1 << lv) - 1));
+                    return lv == 2 ? reinterpret_cast<const float *>(sd)[e] : bf16_to_f32(reinterpret_cast<const unsigned short *>(sd)[e]);
                 };
-                for (int q0 = 0; q0 < c.ncol; q0 += 8) {
-                    unsigned ah[2][4], al[2][4];
+                for (int qs = 0; qs < c.ncol; qs += kP2Slab) {
+                    const int ns = min(kP2Slab, c.ncol - qs);
+                    // coefficients of columns qs .. qs + ns (zero past them and past nn)
+                    const int kxl = lane < ns ? cidx[c.a + qs + lane] : -1;
+                    if (qs > 0)
+                        __syncwarp(); // the previous slab is read out
+                    if ((mu & 3) == 0) {
+                        float4 r[kP2Slab * 16 / 32];
 #pragma unroll
-                    for (int mt = 0; mt < 2; mt++) {
-                        const int r0 = 16 * mt + g;
-                        split_tf32(uload(r0, q0 + t), ah[mt][0], al[mt][0]);
-                        split_tf32(uload(r0 + 8, q0 + t), ah[mt][1], al[mt][1]);
-                        split_tf32(uload(r0, q0 + t + 4), ah[mt][2], al[mt][2]);
-                        split_tf32(uload(r0 + 8, q0 + t + 4), ah[mt][3], al[mt][3]);
+                        for (int i = 0; i < kP2Slab * 16 / 32; i++) {
+                            const int e = lane + 32 * i, j = e >> 4, c4 = e & 15;
+                            const int kx = __shfl_sync(0xffffffffu, kxl, j);
+                            r[i]         = (kx >= 0 && 4 * c4 < nn) ? __ldg(reinterpret_cast<const float4 *>(Af + (long long)kx * mu + cb) + c4) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
+#pragma unroll
+                        for (int i = 0; i < kP2Slab * 16 / 32; i++) {
+                            const int e = lane + 32 * i, j = e >> 4, c4 = e & 15;
+                            *reinterpret_cast<float4 *>(scf + j * kP2CoefLd + 4 * c4) = r[i];
+                        }
+                    } else {
+                        for (int j = 0; j < kP2Slab; j++) {
+                            const int kx = __shfl_sync(0xffffffffu, kxl, j);
+                            for (int cc = lane; cc < 64; cc += 32)
+                                scf[j * kP2CoefLd + cc] = (kx >= 0 && cc < nn) ? __ldg(Af + (long long)kx * mu + cb + cc) : 0.f;
+                        }
                     }
-                    // coefficient rows of columns q0 + t and q0 + t + 4 (phase-1 slots)
-                    const int kx0 = q0 + t < c.ncol ? cidx[c.a + q0 + t] : -1;
-                    const int kx1 = q0 + t + 4 < c.ncol ? cidx[c.a + q0 + t + 4] : -1;
-#pragma unroll
-                    for (int nt = 0; nt < 8; nt++) {
-                        if (nt >= nnt) // warp-uniform
-                            break;
-                        const int col  = cb + 8 * nt + g;
-                        const float b0 = (kx0 >= 0 && col < mu) ? __ldg(Af + (long long)kx0 * mu + col) : 0.f;
-                        const float b1 = (kx1 >= 0 && col < mu) ? __ldg(Af + (long long)kx1 * mu + col) : 0.f;
-                        unsigned bh0, bl0, bh1, bl1;
-                        split_tf32(b0, bh0, bl0);
-                        split_tf32(b1, bh1, bl1);
+                    __syncwarp();
+                    for (int q0 = 0; q0 < ns; q0 += 8) {
+                        unsigned ah[2][4], al[2][4];
 #pragma unroll
                         for (int mt = 0; mt < 2; mt++) {
-                            if (mt >= nmt) // warp-uniform
+                            const int r0 = 16 * mt + g;
+                            split_tf32(uload(r0, qs + q0 + t), ah[mt][0], al[mt][0]);
+                            split_tf32(uload(r0 + 8, qs + q0 + t), ah[mt][1], al[mt][1]);
+                            split_tf32(uload(r0, qs + q0 + t + 4), ah[mt][2], al[mt][2]);
+                            split_tf32(uload(r0 + 8, qs + q0 + t + 4), ah[mt][3], al[mt][3]);
+                        }
+#pragma unroll
+                        for (int nt = 0; nt < 8; nt++) {
+                            if (nt >= nnt) // warp-uniform
                                 break;
-                            mma_tf32(acc[mt][nt], al[mt], bh0, bh1);
-                            mma_tf32(acc[mt][nt], ah[mt], bl0, bl1);
-                            mma_tf32(acc[mt][nt], ah[mt], bh0, bh1);
+                            // zero past the slab's columns (those rows of scf are zero or stale: masked)
+                            const float b0 = q0 + t < ns ? scf[(q0 + t) * kP2CoefLd + 8 * nt + g] : 0.f;
+                            const float b1 = q0 + t + 4 < ns ? scf[(q0 + t + 4) * kP2CoefLd + 8 * nt + g] : 0.f;
+                            unsigned bh0, bl0, bh1, bl1;
+                            split_tf32(b0, bh0, bl0);
+                            split_tf32(b1, bh1, bl1);
+#pragma unroll
+                            for (int mt = 0; mt < 2; mt++) {
+                                if (mt >= nmt) // warp-uniform
+                                    break;
+                                mma_tf32(acc[mt][nt], al[mt], bh0, bh1);
+                                mma_tf32(acc[mt][nt], ah[mt], bl0, bl1);
+                                mma_tf32(acc[mt][nt], ah[mt], bh0, bh1);
+                            }
                         }
                     }
                 }
@@ -439,8 +489,136 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase2_mma_kernel(const Stream
 void launch_phase2_mma(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const double *A, const int *xexp, int mu, double *z, int zlen, cudaStream_t st) {
     if (nrc <= 0)
         return;
+    static unsigned long long done = 0; // devices whose shared-memory limit was raised
+    int dev = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kP2MmaSmem));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
     const int blocks = (nrc + kMmaWarps - 1) / kMmaWarps; // one warp per row chunk
-    phase2_mma_kernel<<<blocks, 32 * kMmaWarps, 0, st>>>(chunks, rc, nrc, mix, cidx, A, xexp, mu, z, zlen);
+    phase2_mma_kernel<<<blocks, 32 * kMmaWarps, kP2MmaSmem, st>>>(chunks, rc, nrc, mix, cidx, A, xexp, mu, z, zlen);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// The dense FP64 chunks of a reduced-precision product with many right-hand
+// sides, added onto the tensor-core part of z: per row chunk (one warp, lane
+// = row), right-hand sides in blocks of 16, each dense chunk (h x ncol,
+// column-major, doubles or their pre-split (hi, lo) pairs) and the split x
+// rows of its columns staged in shared memory, products on the FP32 pipe in
+// double-float arithmetic (FP64-accurate, as the streamed kernel's emulated
+// chunks).
+constexpr int kDnRhs  = 16;
+constexpr int kDnWarp = kStreamStage + kStreamCols * kDnRhs * 8; // bytes of shared memory per warp
+constexpr int kDnSmem = kMmaWarps * kDnWarp;
+
+__global__ void __launch_bounds__(32 * kMmaWarps) dense_mrhs_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ fac,
+                                                                     const unsigned char *__restrict__ pre, const int *__restrict__ cidx, const F2 *__restrict__ xs,
+                                                                     const int *__restrict__ xexp, int mu, double *__restrict__ z, int zlen) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int W       = gridDim.x * kMmaWarps;
+    unsigned char *sd = smem + (size_t)wid * kDnWarp;                  // the chunk's doubles or pairs
+    float2 *sx        = reinterpret_cast<float2 *>(sd + kStreamStage); // x pairs [column][rhs]
+    const int shift   = max(*xexp, 1) - 1023;
+    for (int w = blockIdx.x * kMmaWarps + wid; w < nrc; w += W) {
+        const int kb = rc[w], ke = rc[w + 1];
+        bool any = false;
+        for (int k = kb; k < ke && !any; k++)
+            any = chunks[k].kind == kStreamDfma || chunks[k].kind == kStreamEmu;
+        if (!any)
+            continue;
+        const StreamChunk head = chunks[kb];
+        const int h = head.h, zrow = head.b;
+        for (int cb = 0; cb < mu; cb += kDnRhs) {
+            const int nn = min(kDnRhs, mu - cb);
+            DF acc[kDnRhs];
+#pragma unroll
+            for (int cc = 0; cc < kDnRhs; cc++)
+                df_zero(acc[cc]);
+            for (int k = kb; k < ke; k++) {
+                const StreamChunk c = chunks[k];
+                if (c.kind != kStreamDfma && c.kind != kStreamEmu)
+                    continue;
+                const bool split_done = (c.flags & kStreamPre) != 0;
+                // x rows of the chunk's columns (cidx ~j), then the chunk's 8-byte elements
+                const int j0 = lane < c.ncol ? ~cidx[c.a + lane] : 0, j1 = lane + 32 < c.ncol ? ~cidx[c.a + lane + 32] : 0;
+                __syncwarp(); // the previous chunk is read out
+                {
+                    float2 r[kStreamCols * kDnRhs / 32];
+#pragma unroll
+                    for (int i = 0; i < kStreamCols * kDnRhs / 32; i++) {
+                        const int e = lane + 32 * i, tcol = e / kDnRhs, cc = e % kDnRhs;
+                        // columns 2i and 2i + 1 in this step: both below 32 or both above
+                        const int jh = 2 * i < 32 ? j0 : j1;
+                        const int j  = __shfl_sync(0xffffffffu, jh, tcol & 31);
+                        r[i]        = (tcol < c.ncol && cc < nn) ? __ldg(reinterpret_cast<const float2 *>(xs) + (long long)j * mu + cb + cc) : make_float2(0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int i = 0; i < kStreamCols * kDnRhs / 32; i++)
+                        sx[lane + 32 * i] = r[i];
+                }
+                {
+                    const unsigned long long *src = reinterpret_cast<const unsigned long long *>((split_done ? pre : fac) + c.src);
+                    unsigned long long *dst       = reinterpret_cast<unsigned long long *>(sd);
+                    const int nw                  = c.bytes >> 3; // <= 512
+                    unsigned long long r[kStreamStage / 256];
+#pragma unroll
+                    for (int i = 0; i < kStreamStage / 256; i++)
+                        r[i] = lane + 32 * i < nw ? __ldg(src + lane + 32 * i) : 0ull;
+#pragma unroll
+                    for (int i = 0; i < kStreamStage / 256; i++)
+                        if (lane + 32 * i < nw)
+                            dst[lane + 32 * i] = r[i];
+                }
+                __syncwarp();
+                if (lane < h) {
+                    for (int tcol = 0; tcol < c.ncol; tcol++) {
+                        F2 u;
+                        if (split_done) {
+                            const float2 p = reinterpret_cast<const float2 *>(sd)[lane + h * tcol];
+                            u.hi           = p.x;
+                            u.lo           = p.y;
+                        } else {
+                            u = split64(reinterpret_cast<const double *>(sd)[lane + h * tcol]);
+                        }
+                        const float4 *xr = reinterpret_cast<const float4 *>(sx + tcol * kDnRhs);
+#pragma unroll
+                        for (int q = 0; q < kDnRhs / 2; q++) {
+                            const float4 v = xr[q]; // two pairs: right-hand sides 2q, 2q + 1
+                            F2 b;
+                            b.hi = v.x;
+                            b.lo = v.y;
+                            df_fma(acc[2 * q], u, b);
+                            b.hi = v.z;
+                            b.lo = v.w;
+                            df_fma(acc[2 * q + 1], u, b);
+                        }
+                    }
+#pragma unroll
+                    for (int cc = 0; cc < kDnRhs; cc++)
+                        df_renorm(acc[cc]);
+                }
+            }
+            if (lane < h)
+#pragma unroll
+                for (int cc = 0; cc < kDnRhs; cc++)
+                    if (cc < nn) {
+                        double *zp = z + (long long)(cb + cc) * zlen + zrow + lane;
+                        *zp += scale_pow2_safe(df_to_double(acc[cc]), shift);
+                    }
+        }
+    }
+}
+
+void launch_dense_mrhs(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *fac, const unsigned char *pre, const int *cidx, const F2 *xs, const int *xexp, int mu, double *z, int zlen,
+                       cudaStream_t st) {
+    if (nrc <= 0)
+        return;
+    const int blocks = (nrc + kMmaWarps - 1) / kMmaWarps; // one warp per row chunk
+    dense_mrhs_kernel<<<blocks, 32 * kMmaWarps, kDnSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, xs, xexp, mu, z, zlen);
     HTGPU_CUDA(cudaGetLastError());
 }
 
