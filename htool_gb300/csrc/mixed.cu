@@ -235,7 +235,8 @@ void launch_swizzle(const SwizzleJob *jobs, int njobs, const double *fac, const 
 // by mma.sync m16n8k8 in TF32 with three products per step (hi*hi + hi*lo
 // + lo*hi of the TF32 splits of both operands, FP32 accumulation): about
 // FP32 accuracy.  One warp per tile, V columns in pairs of 16-row tiles,
-// right-hand sides in blocks of 64 (eight 8-column tiles).  Fragment
+// right-hand sides in blocks of 64 (eight 8-column tiles); 32-row slabs of
+// the tile and of x staged in the warp's shared memory.  Fragment
 // layouts of m16n8k8 .tf32 (g = lane / 4, t = lane % 4): A a0 (g, t), a1
 // (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4); B b0 (t, g), b1 (t + 4, g);
 // C c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1).
@@ -258,12 +259,22 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], 
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// per warp: a 32-row slab of the tile for 32 of its columns (row stride 36
+// floats) and of x for 64 right-hand sides (row stride 72): the A and B
+// fragments of a step hit 32 distinct banks
+constexpr int kP1Slab = 32, kP1VLd = 36, kP1XLd = 72;
+constexpr int kP1MmaWarp = 4 * (kP1Slab * kP1VLd + kP1Slab * kP1XLd);
+constexpr int kP1MmaSmem = kMmaWarps * kP1MmaWarp;
+
 __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const unsigned char *__restrict__ mix,
                                                                      const double *__restrict__ scale, const F2 *__restrict__ xs, int mu, double *__restrict__ A) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int W    = gridDim.x * kMmaWarps;
-    float *Af      = reinterpret_cast<float *>(A); // float phase-1 sums
-    for (int w = blockIdx.x * kMmaWarps + (threadIdx.x >> 5); w < nitems; w += W) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int W   = gridDim.x * kMmaWarps;
+    float *sv     = reinterpret_cast<float *>(smem + (size_t)wid * kP1MmaWarp); // [column][row of the slab]
+    float *sxs    = sv + kP1Slab * kP1VLd;                                      // [row of the slab][rhs]
+    float *Af     = reinterpret_cast<float *>(A);                               // float phase-1 sums
+    for (int w = blockIdx.x * kMmaWarps + wid; w < nitems; w += W) {
         const P1Item it = items[w];
         const LrLeaf L  = lr[it.leaf];
         const int jlen = it.jlen, r = L.r, c32 = it.pad;
@@ -272,15 +283,10 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item
         const unsigned short *V16 = reinterpret_cast<const unsigned short *>(mix + it.off + 4LL * l32 * c32);
         const F2 *X               = xs + (long long)(L.oj + it.j0) * mu;
         float *out                = Af + (L.a_off + (long long)(it.chunk & ~kEmuBit) * L.r) * mu;
-        auto vload = [&](int j, int k) -> float { // V[j][k], zero outside the tile
-            if (j >= jlen || k >= r)
-                return 0.f;
-            return k < c32 ? V32[(long long)k * l32 + j] : bf16_to_f32(V16[(long long)(k - c32) * l16 + j]);
-        };
         for (int cb = 0; cb < mu; cb += 64) {
-            const int nnt = min(8, (mu - cb + 7) >> 3); // 8-column tiles of this block
-            for (int mb = 0; mb < r; mb += 32) {
-                const int nmt = r - mb > 16 ? 2 : 1;
+            const int nn = min(64, mu - cb), nnt = (nn + 7) >> 3; // right-hand sides of this block, 8-column tiles
+            for (int mb = 0; mb < r; mb += kP1Slab) {
+                const int nk = min(kP1Slab, r - mb), nmt = nk > 16 ? 2 : 1;
                 float acc[2][8][4];
 #pragma unroll
                 for (int a = 0; a < 2; a++)
@@ -289,33 +295,70 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item
 #pragma unroll
                         for (int q = 0; q < 4; q++)
                             acc[a][b][q] = 0.f;
-                for (int j0 = 0; j0 < jlen; j0 += 8) {
-                    unsigned ah[2][4], al[2][4];
+                for (int js = 0; js < jlen; js += kP1Slab) {
+                    // the slab of V (lane = row; every load issued before the stores),
+                    // zero past the tile and past the columns
+                    __syncwarp(); // the previous slab is read out
+                    {
+                        const int j = js + lane;
+#pragma unroll 1
+                        for (int k8 = 0; k8 < kP1Slab; k8 += 8) {
+                            float v[8];
 #pragma unroll
-                    for (int mt = 0; mt < 2; mt++) {
-                        const int k0 = mb + 16 * mt + g;
-                        split_tf32(vload(j0 + t, k0), ah[mt][0], al[mt][0]);
-                        split_tf32(vload(j0 + t, k0 + 8), ah[mt][1], al[mt][1]);
-                        split_tf32(vload(j0 + t + 4, k0), ah[mt][2], al[mt][2]);
-                        split_tf32(vload(j0 + t + 4, k0 + 8), ah[mt][3], al[mt][3]);
+                            for (int kk = 0; kk < 8; kk++) {
+                                const int kc = mb + k8 + kk;
+                                v[kk]        = 0.f;
+                                if (k8 + kk < nk && j < jlen)
+                                    v[kk] = kc < c32 ? __ldg(V32 + (long long)kc * l32 + j) : bf16_to_f32(__ldg(V16 + (long long)(kc - c32) * l16 + j));
+                            }
+#pragma unroll
+                            for (int kk = 0; kk < 8; kk++)
+                                sv[(k8 + kk) * kP1VLd + lane] = v[kk];
+                        }
                     }
+                    // the slab of x: rows js .. js + 32, right-hand sides cb + lane, cb + 32 + lane
+#pragma unroll 1
+                    for (int j8 = 0; j8 < kP1Slab; j8 += 8) {
+                        float a[8], b[8];
 #pragma unroll
-                    for (int nt = 0; nt < 8; nt++) {
-                        if (nt >= nnt) // warp-uniform
-                            break;
-                        const int c   = cb + 8 * nt + g;
-                        const float x0 = (j0 + t < jlen && c < mu) ? X[(long long)(j0 + t) * mu + c].hi : 0.f;
-                        const float x1 = (j0 + t + 4 < jlen && c < mu) ? X[(long long)(j0 + t + 4) * mu + c].hi : 0.f;
-                        unsigned bh0, bl0, bh1, bl1;
-                        split_tf32(x0, bh0, bl0);
-                        split_tf32(x1, bh1, bl1);
+                        for (int jj = 0; jj < 8; jj++) {
+                            const int j = js + j8 + jj;
+                            a[jj]       = (j < jlen && lane < nn) ? X[(long long)j * mu + cb + lane].hi : 0.f;
+                            b[jj]       = (j < jlen && lane + 32 < nn) ? X[(long long)j * mu + cb + lane + 32].hi : 0.f;
+                        }
+#pragma unroll
+                        for (int jj = 0; jj < 8; jj++) {
+                            sxs[(j8 + jj) * kP1XLd + lane]      = a[jj];
+                            sxs[(j8 + jj) * kP1XLd + lane + 32] = b[jj];
+                        }
+                    }
+                    __syncwarp();
+                    const int nj = min(kP1Slab, jlen - js);
+                    for (int j0 = 0; j0 < nj; j0 += 8) {
+                        unsigned ah[2][4], al[2][4];
 #pragma unroll
                         for (int mt = 0; mt < 2; mt++) {
-                            if (mt >= nmt) // warp-uniform
+                            const int k0 = 16 * mt + g; // columns of V = rows of the A tile
+                            split_tf32(sv[k0 * kP1VLd + j0 + t], ah[mt][0], al[mt][0]);
+                            split_tf32(sv[(k0 + 8) * kP1VLd + j0 + t], ah[mt][1], al[mt][1]);
+                            split_tf32(sv[k0 * kP1VLd + j0 + t + 4], ah[mt][2], al[mt][2]);
+                            split_tf32(sv[(k0 + 8) * kP1VLd + j0 + t + 4], ah[mt][3], al[mt][3]);
+                        }
+#pragma unroll
+                        for (int nt = 0; nt < 8; nt++) {
+                            if (nt >= nnt) // warp-uniform
                                 break;
-                            mma_tf32(acc[mt][nt], al[mt], bh0, bh1);
-                            mma_tf32(acc[mt][nt], ah[mt], bl0, bl1);
-                            mma_tf32(acc[mt][nt], ah[mt], bh0, bh1);
+                            unsigned bh0, bl0, bh1, bl1;
+                            split_tf32(sxs[(j0 + t) * kP1XLd + 8 * nt + g], bh0, bl0);
+                            split_tf32(sxs[(j0 + t + 4) * kP1XLd + 8 * nt + g], bh1, bl1);
+#pragma unroll
+                            for (int mt = 0; mt < 2; mt++) {
+                                if (mt >= nmt) // warp-uniform
+                                    break;
+                                mma_tf32(acc[mt][nt], al[mt], bh0, bh1);
+                                mma_tf32(acc[mt][nt], ah[mt], bl0, bl1);
+                                mma_tf32(acc[mt][nt], ah[mt], bh0, bh1);
+                            }
                         }
                     }
                 }
@@ -338,8 +381,16 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item
 void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;
+    static unsigned long long done = 0; // devices whose shared-memory limit was raised
+    int dev = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase1_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kP1MmaSmem));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
     const int blocks = (nitems + kMmaWarps - 1) / kMmaWarps; // one warp per tile
-    phase1_mma_kernel<<<blocks, 32 * kMmaWarps, 0, st>>>(items, nitems, lr, mix, scale, xs, mu, A);
+    phase1_mma_kernel<<<blocks, 32 * kMmaWarps, kP1MmaSmem, st>>>(items, nitems, lr, mix, scale, xs, mu, A);
     HTGPU_CUDA(cudaGetLastError());
 }
 
