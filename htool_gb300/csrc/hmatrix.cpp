@@ -1273,7 +1273,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
         } else if (n_p1m_ && mu >= kMmaMinRhs) {
-            launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, mu, w_A, st);
+            launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scalef_d.p, w_xs, mu, w_A, st);
             launches_ += 1;
         } else if (n_p1m_) {
             launch_phase1_mixed(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, w_xexp, mu, w_A, st);

@@ -149,7 +149,7 @@ void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, cons
 // the same contraction on the tensor cores (mma.sync TF32, three products
 // per step), for products with many right-hand sides; float sums into A
 constexpr int kMmaMinRhs = 8; // right-hand sides from which products take it
-void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, int mu, double *A, cudaStream_t st);
+void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const float *scale, const F2 *xs, int mu, double *A, cudaStream_t st);
 // phase 2 of a reduced-precision product with mu >= kMmaMinRhs: the FP32 /
 // BF16 chunks of every row chunk (rc: first chunk of row chunk i, nrc + 1
 // entries) on the tensor cores; writes the row chunk's z rows (the dense

@@ -267,7 +267,7 @@ constexpr int kP1MmaWarp = 4 * (kP1Slab * kP1VLd + kP1Slab * kP1XLd);
 constexpr int kP1MmaSmem = kMmaWarps * kP1MmaWarp;
 
 __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const unsigned char *__restrict__ mix,
-                                                                     const double *__restrict__ scale, const F2 *__restrict__ xs, int mu, double *__restrict__ A) {
+                                                                     const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, double *__restrict__ A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
     const int W   = gridDim.x * kMmaWarps;
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item
                         }
                     }
                 }
-                // scaled by the column factors: the phase-2 coefficients
+                // scaled by the column factors (FP32, no FP64-pipe work): the phase-2 coefficients
 #pragma unroll
                 for (int mt = 0; mt < 2; mt++)
 #pragma unroll
@@ -371,14 +371,14 @@ __global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item
                         for (int q = 0; q < 4; q++) {
                             const int k = mb + 16 * mt + g + 8 * (q >> 1), c = cb + 8 * nt + 2 * t + (q & 1);
                             if (mt < nmt && nt < nnt && k < r && c < mu)
-                                out[(long long)k * mu + c] = (float)((double)acc[mt][nt][q] * scale[L.a_off + k]);
+                                out[(long long)k * mu + c] = acc[mt][nt][q] * scale[L.a_off + k];
                         }
             }
         }
     }
 }
 
-void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, int mu, double *A, cudaStream_t st) {
+void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const float *scale, const F2 *xs, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;
     static unsigned long long done = 0; // devices whose shared-memory limit was raised
