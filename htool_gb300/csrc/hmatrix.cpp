@@ -948,6 +948,15 @@ void HMatrix::upload_phase1_lists() {
     fp64_lists_stale_ = presplit_on_ && precision_ != 0; // mirrors wait for the FP64 policy
     n_sctas_  = stream_ctas() * kStreamWarpsPerCta * 8; // ranges: ~8 per warp
     n_chunks_ = (long long)ch.size();
+    { // first chunk of every row chunk (many right-hand sides)
+        std::vector<int> rc;
+        for (std::size_t k = 0; k < ch.size(); k++)
+            if (ch[k].flags & kStreamFirst)
+                rc.push_back((int)k);
+        n_p2rc_ = (int)rc.size();
+        rc.push_back((int)ch.size());
+        p2rc_d.upload(rc, stream_);
+    }
     {
         const std::vector<int> r = stream_ranges(ch, n_sctas_);
         n_ranges_                = (int)r.size() - 1;
@@ -1289,8 +1298,8 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
             launches_ += 1;
             if (n_chunks_md_ > 0) {
-                launch_dense_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_xs, w_xexp, mu, w_z,
-                                  (int)zlen_, st);
+                launch_phase2_df_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xs, w_xexp, mu,
+                                      w_z, (int)zlen_, true, st);
                 launches_ += 1;
             }
         } else if (p2_mode_ == 1)
@@ -1305,7 +1314,12 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         launches_ += groups + 1;
         return;
     }
-    if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
+    const bool many = mu >= kMmaMinRhs; // many right-hand sides: double-float kernels over 16 per pass
+    if (many) {
+        launch_phase1_df_mrhs(p1_d.p, n_p1_dfma_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
+        launch_phase1_df_mrhs(p1e_d.p, n_p1_emu_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
+        launches_ += (n_p1_dfma_ > 0) + (n_p1_emu_ > 0);
+    } else if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
         if (emu_fresh_)
             launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, p1_kinds_, reinterpret_cast<const unsigned char *>(emu_.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st, true);
         else
@@ -1335,11 +1349,16 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
     {
         const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
         const unsigned char *pre   = reinterpret_cast<const unsigned char *>(emu2_.p); // kStreamPre chunks
-        if (p2_mode_ == 1)
+        if (many) {
+            launch_phase2_df_mrhs(sc_d.p, p2rc_d.p, n_p2rc_, arena, pre, cidx_d.p, w_A, w_xs, w_xexp, mu, w_z, (int)zlen_, false, st);
+            launches_ += 1;
+        } else if (p2_mode_ == 1) {
             launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
-        else
+            launches_ += groups;
+        } else {
             launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
-        launches_ += groups;
+            launches_ += groups;
+        }
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
     }

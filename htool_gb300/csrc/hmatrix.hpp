@@ -241,8 +241,8 @@ class HMatrix {
     int n_units_ = 0, n_units_m_ = 0;
     // reduced precision, many right-hand sides: first chunk of every row
     // chunk (tensor-core phase 2, then its dense chunks) and the dense chunk count
-    DevBuf<int> p2rcm_d;
-    int n_p2rc_m_ = 0;
+    DevBuf<int> p2rcm_d, p2rc_d; // and of the FP64 list
+    int n_p2rc_m_ = 0, n_p2rc_ = 0;
     long long n_chunks_md_ = 0;
     // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced
     // storage), phase-2 columns, z values read by the final sums

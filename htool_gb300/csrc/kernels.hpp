@@ -153,12 +153,20 @@ void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const 
 // phase 2 of a reduced-precision product with mu >= kMmaMinRhs: the FP32 /
 // BF16 chunks of every row chunk (rc: first chunk of row chunk i, nrc + 1
 // entries) on the tensor cores; writes the row chunk's z rows (the dense
-// chunks are added afterwards: launch_dense_mrhs)
+// chunks are added afterwards: launch_phase2_df_mrhs)
 void launch_phase2_mma(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const double *A, const int *xexp, int mu, double *z, int zlen, cudaStream_t st);
-// the dense FP64 chunks of those row chunks added onto z (double-float on the
-// FP32 pipe; pre: the pre-split mirror of kStreamPre chunks)
-void launch_dense_mrhs(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *fac, const unsigned char *pre, const int *cidx, const F2 *xs, const int *xexp, int mu, double *z, int zlen,
-                       cudaStream_t st);
+// ---- many right-hand sides in double-float arithmetic (mrhs.cu) -----------
+// phase 1 of an FP64 product with mu >= kMmaMinRhs: every tile (DFMA or
+// emulated alike) for 16 right-hand sides per pass, A slots written as in
+// launch_phase1 (multi-tile leaves still need launch_reduce_tiles)
+void launch_phase1_df_mrhs(const P1Item *items, int nitems, const LrLeaf *lr, const double *factors, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
+// phase 2 over the FP64 chunks (kinds DFMA / emulated; doubles in fac or,
+// with kStreamPre, pairs in pre) of every row chunk (rc: first chunk of row
+// chunk i, nrc + 1 entries), 16 right-hand sides per pass; coefficients: the
+// FP64 phase-1 sums in A (slots) or x (~j); add: onto z (the tensor-core
+// part of a reduced-precision product) instead of writing it
+void launch_phase2_df_mrhs(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *fac, const unsigned char *pre, const int *cidx, const double *A, const F2 *xs, const int *xexp,
+                           int mu, double *z, int zlen, bool add, cudaStream_t st);
 // ---- ACA rank predictor (mlp.cu) -------------------------------------------
 constexpr int kMlpIn = 10, kMlpHidden = 64;
 constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;

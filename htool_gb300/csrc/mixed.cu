@@ -404,7 +404,7 @@ void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const 
 // products per step as in phase 1, FP32 accumulation over the row chunk;
 // one warp per row chunk, right-hand sides in blocks of 64.  The row
 // chunk's z rows are written (FP64, x's exponent shift undone); its dense
-// FP64 chunks are added afterwards by dense_mrhs_kernel.  Each chunk's bytes
+// FP64 chunks are added afterwards by phase2_df_mrhs_kernel (mrhs.cu).  Each chunk's bytes
 // and the coefficients of 32 of its columns are staged in the warp's shared
 // memory (every load issued before the first use), the fragments read there.
 // per warp: the chunk's bytes and the coefficients of up to 32 of its
@@ -550,126 +550,6 @@ void launch_phase2_mma(const StreamChunk *chunks, const int *rc, int nrc, const 
     }
     const int blocks = (nrc + kMmaWarps - 1) / kMmaWarps; // one warp per row chunk
     phase2_mma_kernel<<<blocks, 32 * kMmaWarps, kP2MmaSmem, st>>>(chunks, rc, nrc, mix, cidx, A, xexp, mu, z, zlen);
-    HTGPU_CUDA(cudaGetLastError());
-}
-
-// ---------------------------------------------------------------------------
-// The dense FP64 chunks of a reduced-precision product with many right-hand
-// sides, added onto the tensor-core part of z: per row chunk (one warp, lane
-// = row), right-hand sides in blocks of 16, each dense chunk (h x ncol,
-// column-major, doubles or their pre-split (hi, lo) pairs) and the split x
-// rows of its columns staged in shared memory, products on the FP32 pipe in
-// double-float arithmetic (FP64-accurate, as the streamed kernel's emulated
-// chunks).
-constexpr int kDnRhs  = 16;
-constexpr int kDnWarp = kStreamStage + kStreamCols * kDnRhs * 8; // bytes of shared memory per warp
-constexpr int kDnSmem = kMmaWarps * kDnWarp;
-
-__global__ void __launch_bounds__(32 * kMmaWarps) dense_mrhs_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ fac,
-                                                                     const unsigned char *__restrict__ pre, const int *__restrict__ cidx, const F2 *__restrict__ xs,
-                                                                     const int *__restrict__ xexp, int mu, double *__restrict__ z, int zlen) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int W       = gridDim.x * kMmaWarps;
-    unsigned char *sd = smem + (size_t)wid * kDnWarp;                  // the chunk's doubles or pairs
-    float2 *sx        = reinterpret_cast<float2 *>(sd + kStreamStage); // x pairs [column][rhs]
-    const int shift   = max(*xexp, 1) - 1023;
-    for (int w = blockIdx.x * kMmaWarps + wid; w < nrc; w += W) {
-        const int kb = rc[w], ke = rc[w + 1];
-        bool any = false;
-        for (int k = kb; k < ke && !any; k++)
-            any = chunks[k].kind == kStreamDfma || chunks[k].kind == kStreamEmu;
-        if (!any)
-            continue;
-        const StreamChunk head = chunks[kb];
-        const int h = head.h, zrow = head.b;
-        for (int cb = 0; cb < mu; cb += kDnRhs) {
-            const int nn = min(kDnRhs, mu - cb);
-            DF acc[kDnRhs];
-#pragma unroll
-            for (int cc = 0; cc < kDnRhs; cc++)
-                df_zero(acc[cc]);
-            for (int k = kb; k < ke; k++) {
-                const StreamChunk c = chunks[k];
-                if (c.kind != kStreamDfma && c.kind != kStreamEmu)
-                    continue;
-                const bool split_done = (c.flags & kStreamPre) != 0;
-                // x rows of the chunk's columns (cidx ~j), then the chunk's 8-byte elements
-                const int j0 = lane < c.ncol ? ~cidx[c.a + lane] : 0, j1 = lane + 32 < c.ncol ? ~cidx[c.a + lane + 32] : 0;
-                __syncwarp(); // the previous chunk is read out
-                {
-                    float2 r[kStreamCols * kDnRhs / 32];
-#pragma unroll
-                    for (int i = 0; i < kStreamCols * kDnRhs / 32; i++) {
-                        const int e = lane + 32 * i, tcol = e / kDnRhs, cc = e % kDnRhs;
-                        // columns 2i and 2i + 1 in this step: both below 32 or both above
-                        const int jh = 2 * i < 32 ? j0 : j1;
-                        const int j  = __shfl_sync(0xffffffffu, jh, tcol & 31);
-                        r[i]        = (tcol < c.ncol && cc < nn) ? __ldg(reinterpret_cast<const float2 *>(xs) + (long long)j * mu + cb + cc) : make_float2(0.f, 0.f);
-                    }
-#pragma unroll
-                    for (int i = 0; i < kStreamCols * kDnRhs / 32; i++)
-                        sx[lane + 32 * i] = r[i];
-                }
-                {
-                    const unsigned long long *src = reinterpret_cast<const unsigned long long *>((split_done ? pre : fac) + c.src);
-                    unsigned long long *dst       = reinterpret_cast<unsigned long long *>(sd);
-                    const int nw                  = c.bytes >> 3; // <= 512
-                    unsigned long long r[kStreamStage / 256];
-#pragma unroll
-                    for (int i = 0; i < kStreamStage / 256; i++)
-                        r[i] = lane + 32 * i < nw ? __ldg(src + lane + 32 * i) : 0ull;
-#pragma unroll
-                    for (int i = 0; i < kStreamStage / 256; i++)
-                        if (lane + 32 * i < nw)
-                            dst[lane + 32 * i] = r[i];
-                }
-                __syncwarp();
-                if (lane < h) {
-                    for (int tcol = 0; tcol < c.ncol; tcol++) {
-                        F2 u;
-                        if (split_done) {
-                            const float2 p = reinterpret_cast<const float2 *>(sd)[lane + h * tcol];
-                            u.hi           = p.x;
-                            u.lo           = p.y;
-                        } else {
-                            u = split64(reinterpret_cast<const double *>(sd)[lane + h * tcol]);
-                        }
-                        const float4 *xr = reinterpret_cast<const float4 *>(sx + tcol * kDnRhs);
-#pragma unroll
-                        for (int q = 0; q < kDnRhs / 2; q++) {
-                            const float4 v = xr[q]; // two pairs: right-hand sides 2q, 2q + 1
-                            F2 b;
-                            b.hi = v.x;
-                            b.lo = v.y;
-                            df_fma(acc[2 * q], u, b);
-                            b.hi = v.z;
-                            b.lo = v.w;
-                            df_fma(acc[2 * q + 1], u, b);
-                        }
-                    }
-#pragma unroll
-                    for (int cc = 0; cc < kDnRhs; cc++)
-                        df_renorm(acc[cc]);
-                }
-            }
-            if (lane < h)
-#pragma unroll
-                for (int cc = 0; cc < kDnRhs; cc++)
-                    if (cc < nn) {
-                        double *zp = z + (long long)(cb + cc) * zlen + zrow + lane;
-                        *zp += scale_pow2_safe(df_to_double(acc[cc]), shift);
-                    }
-        }
-    }
-}
-
-void launch_dense_mrhs(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *fac, const unsigned char *pre, const int *cidx, const F2 *xs, const int *xexp, int mu, double *z, int zlen,
-                       cudaStream_t st) {
-    if (nrc <= 0)
-        return;
-    const int blocks = (nrc + kMmaWarps - 1) / kMmaWarps; // one warp per row chunk
-    dense_mrhs_kernel<<<blocks, 32 * kMmaWarps, kDnSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, xs, xexp, mu, z, zlen);
     HTGPU_CUDA(cudaGetLastError());
 }
 
