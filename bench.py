@@ -14,6 +14,13 @@ plain FP64 product is measured in the same run (`fp64`).  Both read more
 than L2 holds per product (0.9 and 2.1 GB of factors), so no flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+    python bench.py --workload batched [--steps K] [--warmup W]
+
+The batched workload: 256 independent Laplace H-matrices on ellipsoids
+(N_i log-uniform in [2 000, 50 000], axes uniform in [0.5, 2], 1 to 8
+right-hand sides each, seed 4), all products captured as one CUDA graph and
+replayed by one launch per step; `value` = right-hand sides applied per
+second over the whole batch.
 
 Prints one JSON line.  `value` is the device-resident throughput (x and y in
 HBM); `e2e` is the same product through the C ABI from pinned host memory,
@@ -46,6 +53,8 @@ def parse():
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="sphere", choices=["sphere", "batched"], help="sphere: the N = 100 000 product; batched: 256 H-matrices in one graph launch")
+    p.add_argument("--count", type=int, default=256, help="batched: number of H-matrices")
     # fixed configuration instead of the autotuner (e.g. to replay a tuned run under a profiler)
     p.add_argument("--fp64-split", default=None, help="phase-1,phase-2 DFMA per mille, e.g. 0,650")
     p.add_argument("--phase1-mode", type=int, default=None, help="0 tile kernels, 1 streamed")
@@ -353,9 +362,120 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+# storage bound of the batched workload's mixed products (tau * epsilon per
+# leaf): 0.5 keeps every one of the 256 products within 1e-6 of its FP64
+# product (tau = 1 gives 1.2e-6 on the worst ellipsoid)
+BATCH_TAU = 0.5
+
+
+def batched_items(count, seed=4):
+    """(n, axes, mu) of the batched workload's H-matrices"""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(2000), np.log(50000)))))
+        axes = rng.uniform(0.5, 2.0, 3)
+        mu = int(rng.integers(1, 9))
+        out.append((n, axes, mu))
+    return out
+
+
+def run_batched(args):
+    """256 H-matrices, one graph launch per step (replicas under torchrun)"""
+    import torch
+    import htool_gb300 as H
+    from htool_gb300 import geometry as G
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    items = batched_items(args.count)
+    t0 = time.perf_counter()
+    hms, bufs = [], []
+    batch = H.HBatch(local)
+    total_mu = 0
+    nbytes = 0
+    for k, (n, axes, mu) in enumerate(items):
+        pts = G.ellipsoid(n, axes, seed=100 + k)
+        t = H.Cluster().build(n, pts)
+        hm = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).build(H.LAPLACE, pts)
+        x = torch.from_numpy(G.rhs(n, mu, seed=10 + k)).cuda()
+        y = torch.zeros(n * mu, dtype=torch.float64, device="cuda")
+        batch.add(hm, x.data_ptr(), y.data_ptr(), mu, keep=(x, y))
+        hms.append(hm)
+        bufs.append((x, y))
+        total_mu += mu
+        nbytes += sum(hm.phase_bytes(mu))
+    build_s = time.perf_counter() - t0
+    free_b, total_b = torch.cuda.mem_get_info()
+    stream = torch.cuda.current_stream()
+
+    def timed_batch():
+        """(ms per graph launch over the timed steps, ms of the products one by one)"""
+        batch.capture(nstreams=8)
+        for _ in range(max(args.warmup, 3)):
+            batch.launch(stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for hm, (x, y), (n, _, mu) in zip(hms, bufs, items):
+            hm.mvprod_ptr(x.data_ptr(), y.data_ptr(), mu, 0, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        single = e0.elapsed_time(e1)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(args.steps):
+            batch.launch(stream.cuda_stream)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        return s0.elapsed_time(s1) / args.steps, single
+
+    ms64, single64 = timed_batch()
+    y64 = [y.clone() for _, y in bufs]
+    nbytes64 = nbytes
+    for hm in hms:
+        hm.set_precision("mixed", BATCH_TAU)
+    nbytes = sum(sum(hm.phase_bytes(mu)) for hm, (_, _, mu) in zip(hms, items))
+    clocks = Clocks(local)
+    clocks.start()
+    ms, single_ms = timed_batch()
+    ck = clocks.stop()
+    err = max(float(torch.linalg.norm(y - r) / torch.linalg.norm(r)) for (_, y), r in zip(bufs, y64))
+    peak, peak_src = measured_peaks()
+    line = {
+        "metric": "H-matvec/s over a batch of %d H-matrices (one graph launch per step), mixed vs plain FP64" % len(items),
+        "value": world * total_mu / (ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32/bf16 factors, f64 dense",
+        "data": "synthetic (seeded ellipsoids)",
+        "config": {"workload": "batched_laplace_ellipsoids", "count": len(items), "n_total": int(sum(i[0] for i in items)), "rhs_total": total_mu, "epsilon": WORKLOAD["epsilon"], "eta": WORKLOAD["eta"], "tau": BATCH_TAU, "l2": "inputs larger than L2 (%.1f GB per step)" % (nbytes / 1e9)},
+        "max_rel_err_vs_fp64": err,
+        "one_by_one_ms": single_ms,
+        "whole_batch": {"bytes": nbytes, "GB_per_s": nbytes / (ms * 1e-3) / 1e9, "frac_of_hbm_peak": nbytes / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_src},
+        "fp64": {"value": world * total_mu / (ms64 * 1e-3), "ms_per_step": ms64, "one_by_one_ms": single64, "bytes": nbytes64, "GB_per_s": nbytes64 / (ms64 * 1e-3) / 1e9},
+        "build_seconds": build_s,
+        "device_gb_in_use": (total_b - free_b) / 1e9,
+        "clocks": ck,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "batched":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no reference arm in this script; the sphere workload carries it"}), flush=True)
+            return
+        run_batched(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -185,8 +185,11 @@ class HMatrix {
     DevBuf<F2> xs;
     DevBuf<int> xexp, multi_d;
     std::vector<int> multi_h;
-    int p1_permille_ = 300, p2_n64_ = 1;
-    int p2m_n64_ = 650; // reduced-precision products: DFMA share of the dense blocks (per mille)
+    // defaults: the choices of the autotuner on the Laplace spheres of 1e5 and
+    // 1e6 points (phase 1 emulated, phase 2 35% DFMA; reduced-precision dense
+    // blocks emulated; staged phase 1, producer-fed phase 2)
+    int p1_permille_ = 0, p2_n64_ = 350;
+    int p2m_n64_ = 0; // reduced-precision products: DFMA share of the dense blocks (per mille)
     std::vector<StreamChunk> ch2_h_; // their phase-2 chunks
     void upload_mixed_phase2();
     bool emu_ok_ = false;
@@ -230,13 +233,13 @@ class HMatrix {
     DevBuf<int> sr_d, srm_d, status_d, tickets_d;
     int n_sctas_ = 0, n_ranges_ = 0, n_ranges_m_ = 0;
     long long n_chunks_ = 0, n_chunks_m_ = 0;
-    int p1_mode_ = 0;
+    int p1_mode_ = 1;
     DevBuf<double> conj_in_; // complex transposed products: the conjugated input
     char symmetry_ = 'N', uplo_ = 'N';
     int compression_ = 0;
     int nlr_stored_ = -1, ndn_stored_ = -1; // htool's leaves when twins follow them
     void add_symmetric_twins(std::vector<LeafSrc> &lr_src);
-    int p2_mode_ = 0;                  // 0: per-warp streams, 1: producer-fed CTAs
+    int p2_mode_ = 1;                  // 0: per-warp streams, 1: producer-fed CTAs
     DevBuf<int> su_d, sum_d;           // phase-2 units (producer-fed) of the FP64 / reduced chunk lists
     int n_units_ = 0, n_units_m_ = 0;
     // reduced precision, many right-hand sides: first chunk of every row

@@ -208,8 +208,9 @@ int htgpu_hmatrix_phase_bytes(htgpu_hmatrix h, int mu, long long *bytes);
  * precision set (htgpu_hmatrix_set_precision), the call sets and reads the split
  * of that product's dense blocks, which stay FP64 (phase2_dfma_permille; the
  * phase-1 share is kept for the FP64 product).  Each precision keeps its own
- * split.  No counterpart in the reference (its BLAS calls decide this,
- * include/htool/types/matrix.hpp:320-383). */
+ * split; defaults 0 / 350 (FP64) and 0 (reduced-precision dense blocks),
+ * what the autotuner picks on Laplace spheres.  No counterpart in the
+ * reference (its BLAS calls decide this, include/htool/types/matrix.hpp:320-383). */
 int htgpu_hmatrix_set_fp64_split(htgpu_hmatrix h, int phase1_dfma_permille, int phase2_dfma_permille);
 int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int *phase2_dfma_permille);
 
@@ -217,8 +218,9 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int
  * right-hand sides: HTGPU_PHASE1_TILES (one warp per tile, DFMA and emulated
  * tiles as two concurrent kernels) or HTGPU_PHASE1_STREAM (consecutive tile
  * chunks staged into shared memory by a producer warp with bulk copies and
- * shared by the CTA's consumer warps).  Results agree within the FP64
- * tolerance; the autotuner picks one.  No counterpart in the reference. */
+ * shared by the CTA's consumer warps, the default).  Results agree within
+ * the FP64 tolerance; the autotuner picks one.  No counterpart in the
+ * reference. */
 #define HTGPU_PHASE1_TILES 0
 #define HTGPU_PHASE1_STREAM 1
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);
@@ -238,7 +240,7 @@ int htgpu_hmatrix_get_presplit(htgpu_hmatrix h, int *on, long long *bytes);
 /* Phase 2 (the U-side and dense blocks, per row chunk): HTGPU_PHASE2_WARP
  * (every warp streams its own chunks, claiming ranges of row chunks) or
  * HTGPU_PHASE2_PRODUCER (a producer warp per CTA claims units of row chunks
- * and feeds its consumer warps).  Bitwise equal results (the same per-row
+ * and feeds its consumer warps, the default).  Bitwise equal results (the same per-row
  * summation order); the autotuner picks one.  No counterpart in the
  * reference. */
 #define HTGPU_PHASE2_WARP 0
