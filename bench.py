@@ -362,12 +362,6 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-# storage bound of the batched workload's mixed products (tau * epsilon per
-# leaf): 0.5 keeps every one of the 256 products within 1e-6 of its FP64
-# product (tau = 1 gives 1.2e-6 on the worst ellipsoid)
-BATCH_TAU = 0.5
-
-
 def batched_items(count, seed=4):
     """(n, axes, mu) of the batched workload's H-matrices"""
     rng = np.random.default_rng(seed)
@@ -434,7 +428,7 @@ def run_batched(args):
     y64 = [y.clone() for _, y in bufs]
     nbytes64 = nbytes
     for hm in hms:
-        hm.set_precision("mixed", BATCH_TAU)
+        hm.set_precision("mixed", 1.0)
     nbytes = sum(sum(hm.phase_bytes(mu)) for hm, (_, _, mu) in zip(hms, items))
     clocks = Clocks(local)
     clocks.start()
@@ -455,7 +449,7 @@ def run_batched(args):
         "vs_baseline": None,
         "dtype": "f32/bf16 factors, f64 dense",
         "data": "synthetic (seeded ellipsoids)",
-        "config": {"workload": "batched_laplace_ellipsoids", "count": len(items), "n_total": int(sum(i[0] for i in items)), "rhs_total": total_mu, "epsilon": WORKLOAD["epsilon"], "eta": WORKLOAD["eta"], "tau": BATCH_TAU, "l2": "inputs larger than L2 (%.1f GB per step)" % (nbytes / 1e9)},
+        "config": {"workload": "batched_laplace_ellipsoids", "count": len(items), "n_total": int(sum(i[0] for i in items)), "rhs_total": total_mu, "epsilon": WORKLOAD["epsilon"], "eta": WORKLOAD["eta"], "tau": 1.0, "l2": "inputs larger than L2 (%.1f GB per step)" % (nbytes / 1e9)},
         "max_rel_err_vs_fp64": err,
         "one_by_one_ms": single_ms,
         "whole_batch": {"bytes": nbytes, "GB_per_s": nbytes / (ms * 1e-3) / 1e9, "frac_of_hbm_peak": nbytes / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_src},

@@ -1277,11 +1277,13 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
     launches_ += 2;
     if (marks)
         HTGPU_CUDA(cudaEventRecord(marks[0], st));
+    // many right-hand sides on the tensor cores when epsilon leaves room for their FP32 sums
+    const bool mma = mu >= kMmaMinRhs && eps_ >= kMmaMinEps;
     if (precision_ != 0) {
         if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
-        } else if (n_p1m_ && mu >= kMmaMinRhs) {
+        } else if (n_p1m_ && mma) {
             launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scalef_d.p, w_xs, mu, w_A, st);
             launches_ += 1;
         } else if (n_p1m_) {
@@ -1294,7 +1296,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         }
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
-        if (mu >= kMmaMinRhs && n_p2rc_m_ > 0) { // low-rank part on the tensor cores, then the dense chunks added
+        if (mma && n_p2rc_m_ > 0) { // low-rank part on the tensor cores, then the dense chunks added
             launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
             launches_ += 1;
             if (n_chunks_md_ > 0) {
@@ -1314,7 +1316,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         launches_ += groups + 1;
         return;
     }
-    const bool many = mu >= kMmaMinRhs; // many right-hand sides: double-float kernels over 16 per pass
+    const bool many = mu >= kDfMinRhs; // many right-hand sides: double-float kernels over 16 per pass
     if (many) {
         launch_phase1_df_mrhs(p1_d.p, n_p1_dfma_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
         launch_phase1_df_mrhs(p1e_d.p, n_p1_emu_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);

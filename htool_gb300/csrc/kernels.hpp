@@ -148,7 +148,16 @@ void launch_convert(const ConvertJob *jobs, int njobs, const double *fac, const 
 void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const double *scale, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
 // the same contraction on the tensor cores (mma.sync TF32, three products
 // per step), for products with many right-hand sides; float sums into A
-constexpr int kMmaMinRhs = 8; // right-hand sides from which products take it
+// right-hand sides from which reduced-precision products take it, and the
+// smallest epsilon of an H-matrix that does: the tensor cores' FP32 sums
+// carry about 5e-7 of the product (up to 1.2e-6 on Laplace matrices), room
+// an H-matrix at epsilon 1e-5 has and one at 1e-6 has not (the CUDA-core
+// kernels stay near 1.5e-7)
+constexpr int kMmaMinRhs    = 8;
+constexpr double kMmaMinEps = 1e-5;
+// right-hand sides from which FP64 products take the double-float
+// many-right-hand-side kernels (mrhs.cu)
+constexpr int kDfMinRhs = 8;
 void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const float *scale, const F2 *xs, int mu, double *A, cudaStream_t st);
 // phase 2 of a reduced-precision product with mu >= kMmaMinRhs: the FP32 /
 // BF16 chunks of every row chunk (rc: first chunk of row chunk i, nrc + 1
@@ -156,7 +165,7 @@ void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const 
 // chunks are added afterwards: launch_phase2_df_mrhs)
 void launch_phase2_mma(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const double *A, const int *xexp, int mu, double *z, int zlen, cudaStream_t st);
 // ---- many right-hand sides in double-float arithmetic (mrhs.cu) -----------
-// phase 1 of an FP64 product with mu >= kMmaMinRhs: every tile (DFMA or
+// phase 1 of an FP64 product with mu >= kDfMinRhs: every tile (DFMA or
 // emulated alike) for 16 right-hand sides per pass, A slots written as in
 // launch_phase1 (multi-tile leaves still need launch_reduce_tiles)
 void launch_phase1_df_mrhs(const P1Item *items, int nitems, const LrLeaf *lr, const double *factors, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);

@@ -320,22 +320,26 @@ def test_phase2_modes_bitwise(golden):
     assert GH.device_status() == 0
 
 
-def test_many_rhs_tensor_cores(golden):
-    """Reduced-precision products with many right-hand sides run both
-    low-rank contractions on the tensor cores (TF32, three products per
-    step; phase 2 writes the row chunks' low-rank sums, the dense FP64
-    chunks are added by the streamed kernel): every column agrees with the
-    FP64 product within the mixed tolerance and with the one-right-hand-side
-    product (CUDA-core kernels) to FP32 rounding, for block sizes that fill
-    8-column tiles and one that does not, with the dense blocks on DFMA or
-    the emulation and either phase-2 kernel."""
+@pytest.mark.parametrize("eps", [1e-5, 1e-6])
+def test_many_rhs(golden, eps):
+    """Products with many right-hand sides.  FP64: the double-float kernels
+    (16 right-hand sides per pass) give every column of the single product
+    to 1e-13.  Reduced precision at epsilon 1e-5: both low-rank contractions
+    on the tensor cores (TF32, three products per step, FP32 sums; phase 2
+    writes the row chunks' low-rank sums, the dense FP64 chunks are added by
+    the double-float kernel): every column within epsilon of the FP64
+    product and within 2e-6 of the one-right-hand-side product (CUDA-core
+    kernels).  At epsilon 1e-6 the CUDA-core kernels keep every column
+    within 1e-6.  Block sizes that fill 8-column tiles and ones that do not,
+    dense blocks on DFMA or the emulation, either phase-2 kernel."""
     g, meta = golden("sphere6000_k1")
     n = g["xt"].shape[0]
     t = H.Cluster().build(n, g["xt"])
-    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    GH = H.HMatrix(t, t, eps, meta["eta"]).build(meta["kernel"], g["xt"])
+    tol_fp64, tol_one = (eps, 2e-6) if eps >= 1e-5 else (1e-6, 1e-6)
     for mu, split, mode in ((8, 1000, "producer"), (13, 350, "warp"), (64, 0, "producer"), (64, 1000, "warp")):
         X = G.rhs(n, mu, seed=20 + mu)
-        y64 = GH.mvprod_global_to_global(X, mu)  # FP64: the double-float many-right-hand-side kernels
+        y64 = GH.mvprod_global_to_global(X, mu)
         for c in range(0, mu, max(1, mu // 3)):
             col = slice(c * n, (c + 1) * n)
             assert rel(y64[col], GH.mvprod_global_to_global(X[col].copy())) < 1e-13
@@ -345,8 +349,8 @@ def test_many_rhs_tensor_cores(golden):
         ym = GH.mvprod_global_to_global(X, mu)
         for c in range(0, mu, max(1, mu // 4)):
             col = slice(c * n, (c + 1) * n)
-            assert rel(ym[col], y64[col]) < 1e-6
-            assert rel(ym[col], GH.mvprod_global_to_global(X[col].copy())) < 1e-6
+            assert rel(ym[col], y64[col]) < tol_fp64
+            assert rel(ym[col], GH.mvprod_global_to_global(X[col].copy())) < tol_one
         GH.set_precision("fp64")
     assert GH.device_status() == 0
 
