@@ -127,6 +127,13 @@ def test_complex_symmetric_matches_upstream(golden, name, tmp_path):
     for mu in (1, 3):
         assert rel(hm.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < 1e-10
         assert rel(hm.mvprod_transp_global_to_global(g["x_mu%d" % mu], mu), g["yT_mu%d" % mu]) < 1e-10
+    # nine right-hand sides (the double-float many-right-hand-side kernels
+    # over the twins): every column equals its single product to 1e-13
+    X9 = np.concatenate([g["x_mu3"]] * 3)
+    Y9 = hm.mvprod_global_to_global(X9, 9)
+    for c in (0, 4, 8):
+        col = slice(c * n, (c + 1) * n)
+        assert rel(Y9[col], hm.mvprod_global_to_global(X9[col].copy())) < 1e-13
     hm.set_precision("mixed")
     assert rel(hm.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-4
     hm.set_precision("fp64")

@@ -80,6 +80,12 @@ def test_build_and_product_match_upstream(name, tmp_path):
     assert hashlib.sha256(np.ascontiguousarray(uv).tobytes()).hexdigest() == meta["sha_uv"]
     for mu in (1, 3):
         assert rel(hm.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < FP64_TOL
+    # nine right-hand sides through the double-float many-right-hand-side kernels
+    X9 = np.concatenate([g["x_mu3"]] * 3)
+    Y9 = hm.mvprod_global_to_global(X9, 9)
+    for c in (0, 4, 8):
+        col = slice(c * n, (c + 1) * n)
+        assert rel(Y9[col], hm.mvprod_global_to_global(X9[col].copy())) < 1e-13
     if meta["symmetry"] == "S":
         x = g["x_mu1"]
         assert np.array_equal(hm.mvprod_transp_global_to_global(x), hm.mvprod_global_to_global(x))
