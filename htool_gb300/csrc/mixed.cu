@@ -266,7 +266,7 @@ constexpr int kP1Slab = 32, kP1VLd = 36, kP1XLd = 72;
 constexpr int kP1MmaWarp = 4 * (kP1Slab * kP1VLd + kP1Slab * kP1XLd);
 constexpr int kP1MmaSmem = kMmaWarps * kP1MmaWarp;
 
-__global__ void __launch_bounds__(32 * kMmaWarps) phase1_mma_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const unsigned char *__restrict__ mix,
+__global__ void __launch_bounds__(32 * kMmaWarps, 4) phase1_mma_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const unsigned char *__restrict__ mix,
                                                                      const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, double *__restrict__ A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
