@@ -132,10 +132,10 @@ def aca_case(R):
 def main():
     R = Oracle("reference")
     R.set_num_threads(1)
-    # BASELINE configuration 1: cylinder, 1/(1e-5 + r), eta 10, eps 1e-6
+    # the cylinder workload: 4 000 points, 1/(1e-5 + r), eta 10, eps 1e-6
     cyl = G.cylinder(4000, seed=1)
     hmatrix_case(R, "cyl4000_k0", cyl, cyl, 0, 1e-6, 10.0)
-    # Laplace sphere (the configuration-2 geometry at a fixture-sized N)
+    # Laplace sphere (the 100 000-point sphere workload at a fixture-sized N)
     sph = G.sphere(6000, seed=1)
     hmatrix_case(R, "sphere6000_k1", sph, sph, 1, 1e-6, 10.0)
     # htool's product test geometry: two glibc-rand disks, 2000 x 1000,
@@ -147,10 +147,10 @@ def main():
         s = G.disk_glibc(1000, 1.0 + dz)
         hmatrix_case(R, "disks2000x1000_%s_k1" % tag, t, s, 1, 1e-3, 10.0)
     aca_case(R)
-    # configuration 3 at fixture size: Helmholtz k = 20 on the cube surface,
+    # the Helmholtz workload at fixture size: k = 20 on the cube surface,
     # eta 3, eps 1e-5, complex128
     helmholtz_case(R, "helmholtz_cube2000", 2000, 20.0, 1e-5, 3.0)
-    # htool's own CSV pair for the configuration-1 cluster tree (save_cluster)
+    # htool's own CSV pair for the 4 000-point cylinder's cluster tree (save_cluster)
     ct = R.cluster(cyl)
     R._L.ref_cluster_save(ct.h, os.path.join(OUT, "cyl4000_cluster").encode())
 
@@ -278,7 +278,7 @@ def zsym_cases():
 
 
 def plot_cases():
-    """htool's leaf maps (HMatrix::save_plot) of the configuration-1 and
+    """htool's leaf maps (HMatrix::save_plot) of the 4 000-point cylinder and
     Helmholtz fixtures, written by upstream itself (one thread)"""
     R = Oracle("reference")
     R.set_num_threads(1)

@@ -90,7 +90,7 @@ def test_upstream_plot_matches_golden_leaves(case, plot):
 
 @pytest.mark.gpu
 def test_save_plot_matches_upstream(tmp_path):
-    """HMatrix::save_plot of the device-built configuration-1 and Helmholtz
+    """HMatrix::save_plot of the device-built 4 000-point cylinder and Helmholtz
     H-matrices: the same header and leaf lines as upstream's files"""
     pts = G.cylinder(4000, seed=1)
     t = H.Cluster().build(4000, pts)

@@ -24,7 +24,7 @@ def test_gmres_dense_cpu():
 
 @pytest.mark.gpu
 def test_gmres_graph_product():
-    """H x = b for the configuration-1 H-matrix, every product one graph
+    """H x = b for the 4 000-point cylinder H-matrix, every product one graph
     launch; the solution checked with the oracle's product, and the solve
     in cluster numbering (local products) equal to the solve in user
     numbering"""
