@@ -1,19 +1,26 @@
 """Benchmark: H-matrix product throughput on one GB300 (and N replicas).
 
-Workload: N = 100 000 points uniform on the unit sphere (seeded), Laplace
-single-layer kernel 1/(4 pi r) with a zero diagonal, eta = 10, epsilon =
-1e-6, partialACA, minclustersize 10; one N(0,1) right-hand side per
-product.  The H-matrix is assembled on the GPU (device generator + batched
-device partialACA, timed as `aca_seconds`); a "step" is one product y = H x
-(mvprod_global_to_global), permutations included.
+Workload (default): N = 1 000 000 points uniform on the unit sphere
+(seeded), Laplace single-layer kernel 1/(4 pi r) with a zero diagonal, eta =
+10, epsilon = 1e-6, partialACA, minclustersize 10; one N(0,1) right-hand side
+per product.  The H-matrix is assembled on the GPU (device generator +
+batched device partialACA, timed as `aca_seconds`); a "step" is one product
+y = H x (mvprod_global_to_global), permutations included.
 
-The headline `value` is the mixed-precision product (low-rank factors in
-FP32 / BF16 per column with per-column scaling, dense leaves FP64, FP32/FP64
-accumulation) with its error against the plain FP64 product stated; the
-plain FP64 product is measured in the same run (`fp64`).  Both read more
-than L2 holds per product (0.9 and 2.1 GB of factors), so no flush is needed.
+The headline `value` is the plain FP64 product (FP64 storage; each element
+on the FP64 pipe or in double-float arithmetic on the FP32 pipe, as the
+autotuner splits them), the arithmetic of the reference's CPU product it is
+compared with.  The mixed-precision product (low-rank factors in FP32 / BF16
+per column with per-column scaling, dense leaves FP64, FP32/FP64
+accumulation) is measured in the same run (`mixed`), with its error against
+the FP64 product and its speed-up over it.  Both read more than L2 holds per
+product (tens of GB of factors), so no flush is needed.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+Parity at full size: the CPU oracle builds the same H-matrix (bit-identical
+leaves) and applies it to the same input; `rel_err_vs_reference` compares
+the GPU products with that product.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--n N]
     python bench.py --workload batched [--steps K] [--warmup W]
 
 The batched workload: 256 independent Laplace H-matrices on ellipsoids
@@ -25,9 +32,11 @@ second over the whole batch.
 Prints one JSON line.  `value` is the device-resident throughput (x and y in
 HBM); `e2e` is the same product through the C ABI from pinned host memory,
 host<->device copies inside the timed region.  `--impl reference` times the
-CPU restatement of htool's product (oracle/) on all host cores instead.
+CPU restatement of htool's product (oracle/) on all host cores instead; that
+arm does not load this package's library.
 """
 import argparse
+import importlib.util
 import json
 import os
 import subprocess
@@ -42,18 +51,22 @@ sys.path.insert(0, ROOT)
 
 METRIC = "H-matvec/s and % HBM roofline at rel err ≤1e-6, mixed vs plain FP64; ACA secs"
 UNIT = "H-matvec/s"
-WORKLOAD = dict(workload="laplace_sphere", n=100000, kernel="1/(4 pi r), 0 on the diagonal", eta=10.0, epsilon=1e-6, minclustersize=10, compressor="partialACA", mu=1)
+# the same `config` in both arms
+WORKLOAD = dict(workload="laplace_sphere", n=1000000, kernel="1/(4 pi r), 0 on the diagonal", eta=10.0, epsilon=1e-6, minclustersize=10, compressor="partialACA", mu=1,
+                l2="inputs larger than L2: the stored H-matrix read by every product is tens of GB")
+DTYPE = "f64 (FP64 storage; DFMA and double-float FP32-pipe evaluation)"
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=300)
-    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="sphere", choices=["sphere", "batched"], help="sphere: the N = 100 000 product; batched: 256 H-matrices in one graph launch")
+    p.add_argument("--no-predictor", action="store_true", help="skip the rank-predictor rebuild")
+    p.add_argument("--workload", default="sphere", choices=["sphere", "batched"], help="sphere: the one-H-matrix product; batched: 256 H-matrices in one graph launch")
     p.add_argument("--count", type=int, default=256, help="batched: number of H-matrices")
     # fixed configuration instead of the autotuner (e.g. to replay a tuned run under a profiler)
     p.add_argument("--fp64-split", default=None, help="phase-1,phase-2 DFMA per mille, e.g. 0,650")
@@ -67,6 +80,22 @@ def parse():
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def geometry():
+    """htool_gb300/geometry.py loaded on its own: the point generators,
+    without the package (whose import maps the GPU library)"""
+    spec = importlib.util.spec_from_file_location("htool_gb300_geometry", os.path.join(ROOT, "htool_gb300", "geometry.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
 def measured_peaks():
@@ -122,49 +151,73 @@ class Clocks:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n, reps=10):
-    """The CPU restatement of htool's product (oracle/htool_oracle.c) on all
-    host cores, same workload; its assembly is not timed."""
-    from htool_gb300 import geometry as G
+def cpu_reference(n, reps, single_thread_reps=1, x=None, warmup=1):
+    """The CPU restatement of htool's product (oracle/htool_oracle.c, pinned
+    to upstream htool) on the same workload: its assembly (HMatrix::build
+    with partialACA, timed), then `reps` products on all host cores (median
+    after one warm-up) and `single_thread_reps` on one core.  Returns the
+    figures and the product of the seeded right-hand side."""
+    G = geometry()
     from oracle.oracle import Oracle, build_port
 
     build_port()
     O = Oracle("port")
-    threads = os.cpu_count() or 1
+    threads = host_cores()
     O.set_num_threads(threads)
     pts = G.sphere(n, seed=1)
     t = O.cluster(pts)
     t0 = time.perf_counter()
     H = O.hmatrix(t, t, pts, pts, 1, WORKLOAD["epsilon"], WORKLOAD["eta"])
     build_s = time.perf_counter() - t0
-    x = G.rhs(n, 1, seed=2)
+    if x is None:
+        x = G.rhs(n, 1, seed=2)
+    for _ in range(max(0, warmup - 1)):  # time_mvprod warms up once more itself
+        H.mvprod(x, 1)
     sec = H.time_mvprod(x, 1, reps)
-    return {"value": 1.0 / sec, "unit": UNIT, "cores": threads, "kind": "port", "sample": "%d products (median) of the N=%d Laplace-sphere H-matrix after one warm-up; assembly %.2f s not timed" % (reps, n, build_s), "build_seconds": build_s}
+    y = H.mvprod(x, 1)
+    out = {"value": 1.0 / sec, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "%d products (median, after %d warm-up) of the N=%d Laplace-sphere H-matrix on %d threads; its assembly (%.2f s) not in the figure" % (reps, max(1, warmup), n, threads, build_s),
+           "build_seconds": build_s, "threads": threads}
+    if single_thread_reps:
+        O.set_num_threads(1)
+        t1 = time.perf_counter()
+        for _ in range(single_thread_reps):
+            H.mvprod(x, 1)
+        st = (time.perf_counter() - t1) / single_thread_reps
+        O.set_num_threads(threads)
+        out["single_thread"] = {"value": 1.0 / st, "unit": UNIT, "cores": 1, "sample": "%d product(s), one thread" % single_thread_reps}
+    lr, dn = H.leaves()
+    return out, y, (lr, dn)
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    cb = cpu_baseline(args.n, reps=max(args.steps, 3))
+    cb, _, _ = cpu_reference(args.n, reps=max(args.steps, 3), single_thread_reps=0, warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere)", "config": dict(WORKLOAD, n=args.n),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)", "config": dict(WORKLOAD, n=args.n),
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "aca_seconds": cb["build_seconds"]}
     print(json.dumps(line), flush=True)
 
 
-def sampled_dense_error(pts, x, y, nrows=1000, seed=3):
-    """||y - A x|| / ||A x|| over nrows sampled rows of the dense kernel matrix."""
+def sampled_dense_rows(pts, x, nrows=1000, seed=3):
+    """rows (seeded sample) and (A x)[rows] of the dense Laplace matrix, in
+    FP64 on the device (torch), 50 rows at a time"""
+    import torch
+
     rows = np.random.default_rng(seed).choice(pts.shape[0], nrows, replace=False)
-    ref = np.empty(nrows)
+    P = torch.from_numpy(pts).cuda()
+    X = torch.from_numpy(x).cuda()
+    ref = torch.empty(nrows, dtype=torch.float64, device="cuda")
     for a in range(0, nrows, 50):
-        r = rows[a:a + 50]
-        d = np.sqrt(((pts[r, None, :] - pts[None, :, :]) ** 2).sum(-1))
-        with np.errstate(divide="ignore"):
-            k = np.where(d == 0, 0.0, 1.0 / (4 * np.pi * d))
-        ref[a:a + 50] = k @ x
-    return float(np.linalg.norm(y[rows] - ref) / np.linalg.norm(ref))
+        r = torch.from_numpy(rows[a:a + 50]).cuda()
+        d = torch.sqrt(((P[r][:, None, :] - P[None, :, :]) ** 2).sum(-1))
+        k = torch.where(d == 0, torch.zeros_like(d), 1.0 / (4 * np.pi * d))
+        ref[a:a + 50] = k @ X
+        del d, k
+    return rows, ref.cpu().numpy()
 
 
 def run_gpu(args):
@@ -221,24 +274,41 @@ def run_gpu(args):
         barrier()
         return max_over_ranks(e0.elapsed_time(e1)), hm.last_launches()
 
-    def profiled_traffic(kernel, precision):
+    def timed_e2e():
+        """the product through the C ABI with host buffers: pinned x copied
+        in, y copied out, inside the timed region, every step"""
+        xh = torch.from_numpy(x).pin_memory()
+        yh = torch.empty(n, dtype=torch.float64).pin_memory()
+        for _ in range(max(2, args.warmup)):
+            hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
+        barrier()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
+        e2e_s = max_over_ranks(time.perf_counter() - w0)
+        return {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
+
+    def profiled_traffic(kernel, precision, algorithmic):
         """DRAM bytes per launch of `kernel` from the committed ncu summaries
-        (lines "traffic: kernel=K precision=P n=N bytes_per_launch=B"), for
-        this workload size; None when no capture covers it"""
-        pdir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles")
+        (lines "traffic: kernel=K precision=P n=N bytes_per_launch=B
+        algorithmic=A"): the captured launch's DRAM bytes scaled to this
+        launch by its algorithmic bytes (traffic grows with the bytes
+        streamed); None when no capture covers the kernel"""
+        pdir = os.path.join(ROOT, "profiles")
         if not os.path.isdir(pdir):
-            return None
+            return None, None
         for name in sorted(os.listdir(pdir)):
             if not name.endswith(".md"):
                 continue
             for line in open(os.path.join(pdir, name)):
                 if line.startswith("traffic:"):
                     kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
-                    if kv.get("kernel") == kernel and kv.get("precision") == precision and int(kv.get("n", -1)) == n:
-                        return int(kv["bytes_per_launch"])
-        return None
+                    if kv.get("kernel") == kernel and kv.get("precision") == precision and "algorithmic" in kv:
+                        ratio = int(kv["bytes_per_launch"]) / int(kv["algorithmic"])
+                        return int(round(ratio * algorithmic)), "profiles/%s (n=%s capture, DRAM/algorithmic %.3f, scaled to this launch)" % (name, kv.get("n"), ratio)
+        return None, None
 
-    def describe(ms_total):
+    def describe(ms_total, precision):
         """per-step numbers, phase breakdown and the dominant kernel's roofline"""
         ms_step = ms_total / args.steps
         ph = hm.profile(1, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
@@ -247,20 +317,21 @@ def run_gpu(args):
         k = max(range(4), key=lambda i: ph[i])
         achieved = pb[k] / (ph[k] / 1e3) / 1e9
         total_bytes = sum(pb)
+        traffic, traffic_src = profiled_traffic(names[k], precision, pb[k])
         return ms_step, {
             "phase_ms": {"gather": ph[0], "phase1": ph[1], "phase2": ph[2], "sums": ph[3], "total": ph[4]},
             "phase_bytes": {"gather": pb[0], "phase1": pb[1], "phase2": pb[2], "sums": pb[3]},
             "whole_product": {"bytes": total_bytes, "GB_per_s": total_bytes / (ms_step / 1e3) / 1e9, "frac_of_hbm_peak": total_bytes / (ms_step / 1e3) / 1e9 / peak},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": profiled_traffic(names[k], "fp64" if hm.precision_info()["policy"] == 0 else "mixed"), "kernel": names[k], "kernel_ms": ph[k], "algorithmic_bytes": pb[k],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src, "kernel": names[k], "kernel_ms": ph[k], "algorithmic_bytes": pb[k],
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
         }
 
+    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode))
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.5)  # let the sampler start before the timed regions
-    # plain FP64 (autotuned DFMA / FP32-pipe split)
+    # plain FP64 (autotuned DFMA / FP32-pipe split): the headline
     hm.set_precision("fp64")
-    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode))
     if fixed:
         if args.fp64_split is not None:
             hm.set_fp64_split(*[int(v) for v in args.fp64_split.split(",")])
@@ -272,11 +343,11 @@ def run_gpu(args):
     else:
         tune64 = hm.autotune(1, 5)
     split = hm.get_fp64_split()
-    p1mode64 = hm.get_phase1_mode()
-    p2mode64 = hm.get_phase2_mode()
-    ms64, _ = timed_products()
+    p1mode64, p2mode64 = hm.get_phase1_mode(), hm.get_phase2_mode()
+    ms64, launches64 = timed_products()
     y64 = yd.cpu().numpy().copy()
-    step64, d64 = describe(ms64)
+    step64, d64 = describe(ms64, "fp64")
+    e2e64 = timed_e2e()
     # mixed precision
     tau = 1.0
     hm.set_precision("mixed", tau)
@@ -291,72 +362,73 @@ def run_gpu(args):
     else:
         tunem = hm.autotune(1, 5)
     splitm = hm.get_fp64_split()[1]
-    msm, launches_per_step = timed_products()
+    msm, launchesm = timed_products()
     ym = yd.cpu().numpy().copy()
-    stepm, dm = describe(msm)
+    stepm, dm = describe(msm, "mixed")
+    e2em = timed_e2e()
     pinfo = hm.precision_info()
     clk = clocks.stop()
-    value = world * args.steps / (msm / 1e3)
     value64 = world * args.steps / (ms64 / 1e3)
-
-    # end to end through the C ABI: pinned host x -> device -> product -> host y
-    xh = torch.from_numpy(x).pin_memory()
-    yh = torch.empty(n, dtype=torch.float64).pin_memory()
-    for _ in range(2):
-        hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
-    barrier()
-    w0 = time.perf_counter()
-    for _ in range(args.steps):
-        hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
-    e2e_s = max_over_ranks(time.perf_counter() - w0)
-    e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n, "precision": "mixed"}
+    valuem = world * args.steps / (msm / 1e3)
     status = hm.device_status()
+    hm.set_precision("fp64")
+    rows, dense_ref = sampled_dense_rows(pts, x)
 
     # learned rank predictor: trained on the (geometry, crosses) pairs this
     # build's partialACA produced, then the same mesh re-assembled with it
-    X, yr = hm.aca_samples()
-    mlp = H.RankPredictor(device=local, seed=1)
-    t1 = time.perf_counter()
-    loss = mlp.train(X, np.minimum(yr, 64), epochs=30, batch=2048, lr=3e-3, seed=2)
-    train_s = time.perf_counter() - t1
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    hl = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).set_rank_predictor(mlp).build(H.LAPLACE, pts)
-    aca_learned = time.perf_counter() - t1
-    il = hl.get_infos()
-    same = bool(np.array_equal(hl.get_leaves()[0], hm.get_leaves()[0]) and np.array_equal(hl.get_leaves()[1], hm.get_leaves()[1]))
-    predictor = {"train_samples": int(yr.size), "train_seconds": train_s, "epochs": 30, "final_mse": float(loss[-1]),
-                 "aca_seconds": {"fixed_first_attempt": aca_seconds, "predicted_first_attempt": aca_learned},
-                 "scratch_bytes": {"fixed_first_attempt": int(info["GPU_aca_scratch_bytes"]), "predicted_first_attempt": int(il["GPU_aca_scratch_bytes"])},
-                 "rerun_rate": int(il["GPU_aca_overflow_reruns"]) / max(1, int(il["GPU_aca_predicted_blocks"])), "same_leaves": same}
-    del hl
+    predictor = None
+    if not args.no_predictor:
+        X, yr = hm.aca_samples()
+        mlp = H.RankPredictor(device=local, seed=1)
+        t1 = time.perf_counter()
+        loss = mlp.train(X, np.minimum(yr, 64), epochs=30, batch=2048, lr=3e-3, seed=2)
+        train_s = time.perf_counter() - t1
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        hl = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).set_rank_predictor(mlp).build(H.LAPLACE, pts)
+        aca_learned = time.perf_counter() - t1
+        il = hl.get_infos()
+        same = bool(np.array_equal(hl.get_leaves()[0], hm.get_leaves()[0]) and np.array_equal(hl.get_leaves()[1], hm.get_leaves()[1]))
+        predictor = {"train_samples": int(yr.size), "train_seconds": train_s, "epochs": 30, "final_mse": float(loss[-1]),
+                     "aca_seconds": {"fixed_first_attempt": aca_seconds, "predicted_first_attempt": aca_learned},
+                     "scratch_bytes": {"fixed_first_attempt": int(info["GPU_aca_scratch_bytes"]), "predicted_first_attempt": int(il["GPU_aca_scratch_bytes"])},
+                     "rerun_rate": int(il["GPU_aca_overflow_reruns"]) / max(1, int(il["GPU_aca_predicted_blocks"])), "same_leaves": same}
+        del hl
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
     err_mixed_vs_fp64 = float(np.linalg.norm(ym - y64) / np.linalg.norm(y64))
+    gpu_leaves = hm.get_leaves()
+    dense_err = {k: float(np.linalg.norm(v[rows] - dense_ref) / np.linalg.norm(dense_ref)) for k, v in (("fp64", y64), ("mixed", ym))}
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": stepm, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "mixed: fp32/bf16 factors (per-column scaled), fp64 dense, fp32+fp64 accumulation",
+        "metric": METRIC, "value": value64, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step64, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
         "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)",
-        "config": dict(WORKLOAD, n=n, precision="mixed", tau=tau, parallelism="replicas" if world > 1 else "single",
-                       l2="inputs larger than L2: %.2f GB (mixed) / %.2f GB (fp64) of factors per product" % (pinfo["stored_bytes"] / 1e9, d64["whole_product"]["bytes"] / 1e9)),
-        "rel_err_mixed_vs_fp64": err_mixed_vs_fp64,
-        "speedup_mixed_vs_fp64": value / value64,
-        "roofline": dm["roofline"], "whole_product": dm["whole_product"], "phase_ms": dm["phase_ms"], "phase_bytes": dm["phase_bytes"],
-        "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "phase2_mode": hm.get_phase2_mode(), "dense_dfma_permille": splitm},
-        "fp64": {"value": value64, "unit": UNIT, "ms_per_step": step64, "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
-                 "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64}, "phase1_mode": p1mode64, "phase2_mode": p2mode64},
-        "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk, "device_status": status,
-        "rel_err_vs_dense_1000_rows": {"fp64": sampled_dense_error(pts, x, y64), "mixed": sampled_dense_error(pts, x, ym)},
+        "config": dict(WORKLOAD, n=n),
+        "run": {"precision": "fp64", "parallelism": "replicas" if world > 1 else "single", "stored_gb": {"fp64": d64["whole_product"]["bytes"] / 1e9, "mixed": dm["whole_product"]["bytes"] / 1e9}},
+        "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
+        "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64, "phase1_mode": p1mode64, "phase2_mode": p2mode64},
+        "e2e": e2e64,
+        "mixed": {"value": valuem, "unit": UNIT, "ms_per_step": stepm, "speedup_vs_fp64": valuem / value64, "rel_err_vs_fp64": err_mixed_vs_fp64, "tau": tau,
+                  "dtype": "fp32/bf16 factors (per-column scaled), fp64 dense, fp32+fp64 accumulation", "e2e": e2em,
+                  "roofline": dm["roofline"], "whole_product": dm["whole_product"], "phase_ms": dm["phase_ms"], "phase_bytes": dm["phase_bytes"],
+                  "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "phase2_mode": hm.get_phase2_mode(), "dense_dfma_permille": splitm},
+                  "gpu_launches": launchesm * args.steps},
+        "gpu_launches": launches64 * args.steps, "clocks": clk, "device_status": status,
+        "rel_err_vs_dense_1000_rows": dense_err,
         "aca_seconds": aca_seconds, "rank_predictor": predictor,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},
     }
     if not args.no_cpu_baseline:
-        cb = cpu_baseline(n)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cb, y_ref, ref_leaves = cpu_reference(n, reps=5, single_thread_reps=1, x=x)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread")}
         line["cpu_aca_seconds"] = cb["build_seconds"]
+        line["rel_err_vs_reference"] = {
+            "fp64": float(np.linalg.norm(y64 - y_ref) / np.linalg.norm(y_ref)), "mixed": float(np.linalg.norm(ym - y_ref) / np.linalg.norm(y_ref)),
+            "same_leaves": bool(np.array_equal(gpu_leaves[0], ref_leaves[0]) and np.array_equal(gpu_leaves[1], ref_leaves[1])),
+            "reference": "the CPU oracle's product (oracle/htool_oracle.c, pinned to upstream htool) of its own build of this H-matrix on the same input"}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -72,6 +72,9 @@ HMatrix::HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const Clu
     perm_t.upload(T->perm, stream_);
     perm_s.upload(S->perm, stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    // the allocation-free product's fixed array is made resident here, not
+    // on its first call, which may come after a caller has taken the memory
+    noalloc_reserve(device_);
 }
 
 HMatrix::~HMatrix() {

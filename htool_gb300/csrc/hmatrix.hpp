@@ -18,6 +18,11 @@ struct BuildStats {
 
 class Mlp;
 
+// Loads the allocation-free product's working array on `device` (the
+// current device) and caches its address; errors are left to the first
+// allocation-free product (noalloc.cu)
+void noalloc_reserve(int device) noexcept;
+
 class HMatrix {
   public:
     // complex: a complex (Helmholtz) H-matrix on the trees t, s of its

@@ -8,16 +8,20 @@
 // memory for its own pool, or an iterative solver that drives the product
 // from a hot loop where an allocation (and the device synchronisation it
 // implies) is not acceptable.  This file gives them one product call whose
-// working memory is a fixed array in the library's own device image,
-// reserved when the library is loaded.
+// working memory is a fixed array in the library's own device image.
+// CUDA loads a module's device globals lazily, so the array is brought in
+// by an explicit address lookup, done when an H-matrix is created on the
+// device (noalloc_reserve): by the time a caller's pool has taken the GPU's
+// memory, the array is already resident.
 #include "hmatrix.hpp"
 
 #include <mutex>
 
 namespace htgpu {
 
-// 16 MiB of working memory per device, held by every GPU that loads the
-// library until the process exits.  A product needs 2 * nb_cols * mu
+// 16 MiB of working memory per device, held by every GPU on which an
+// H-matrix was created (or an allocation-free product was called) until the
+// process exits.  A product needs 2 * nb_cols * mu
 // doubles for the gathered input and its float split, one slot for the
 // input's exponent, (phase-1 partial-sum slots) * mu doubles and
 // (per-cluster partial-sum rows) * mu doubles.
@@ -46,6 +50,17 @@ double *scratch_on(int device) {
     return g_scratch_addr[device];
 }
 } // namespace
+
+void noalloc_reserve(int device) noexcept {
+    try {
+        scratch_on(device);
+    } catch (...) {
+        // leave the failure to the first allocation-free product, which
+        // repeats the lookup and reports it; clear the non-sticky error so
+        // that it does not surface in an unrelated call
+        cudaGetLastError();
+    }
+}
 
 std::size_t HMatrix::noalloc_scratch_need(int mu) const {
     // gathered input and its split, each rounded up to 32 doubles (256

@@ -285,16 +285,24 @@ int htgpu_hmatrix_precision_info(htgpu_hmatrix h, int *policy, long long *stored
  * allocate device memory mid-run -- e.g. a process whose framework has
  * already reserved the GPU's memory for its own pool, or a solver driving
  * the product from a hot loop.  Its working memory is one fixed 16 MiB
- * array per device inside the library (2^21 doubles, held by every GPU that
- * loads the library until the process exits); a product needs
+ * array per device inside the library (2^21 doubles); a product needs
  * 2 * nb_cols * mu (each half rounded up to 32) + 32 + (phase-1 partial sums
  * + per-cluster partial-sum rows) * mu doubles, and larger requests fail
- * with HTGPU_ERR_INVALID.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current, so make it before any stream capture.  Every call shares
- * the one array, whose contents persist between calls: calls that may
- * overlap on the GPU (different streams, or different handles on one
- * device) race with each other and must be serialised by the caller.
+ * with HTGPU_ERR_INVALID.  The array is made resident, and its device
+ * address looked up (cudaGetSymbolAddress, with that device current), when
+ * the first H-matrix is created on a device -- before a caller's memory
+ * pool is likely to hold the GPU -- and it stays until the process exits;
+ * if that lookup failed, the first call here repeats it, so that call should
+ * then come before any stream capture.  Every call shares the one array,
+ * whose contents persist between calls: calls that may overlap on the GPU
+ * (different streams, or different handles on one device) race with each
+ * other and must be serialised by the caller.  The call also uses the
+ * handle's own status word and work tickets, like htgpu_hmatrix_mvprod:
+ * any two products of one handle that may overlap on the GPU, this one or
+ * the regular ones, must be serialised.  Like the device-pointer
+ * htgpu_hmatrix_mvprod, it returns before the product ran and does not read
+ * the status of the kernels' bounded waits: after synchronising, a caller
+ * that must know the result is valid reads htgpu_hmatrix_device_status.
  * in/out: device memory, column-major, user numbering; ordered on `stream`
  * (NULL = the handle's own stream). */
 int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out, int mu, void *stream);

@@ -21,7 +21,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhtool_ref.so")
-REF_SRC_DEFAULT = "/root/reference/include"
 
 _vp = C.c_void_p
 _i = C.c_int
@@ -45,9 +44,23 @@ def build_port(force=False):
     return PORT_SO
 
 
-def build_reference(ref_include=REF_SRC_DEFAULT):
+def reference_include():
+    """The upstream htool include directory: $HTOOL_INCLUDE, else the
+    recipe's default (oracle/refbuild/Makefile, `make print-ref`); None when
+    that directory does not exist on this machine."""
+    ref = os.environ.get("HTOOL_INCLUDE")
+    if not ref:
+        try:
+            ref = subprocess.run(["make", "-s", "print-ref"], cwd=os.path.join(HERE, "refbuild"), capture_output=True, text=True, check=True).stdout.strip()
+        except (OSError, subprocess.CalledProcessError):
+            return None
+    return ref if ref and os.path.isdir(ref) else None
+
+
+def build_reference(ref_include=None):
     """Compile the upstream headers into oracle/_ref (only where they exist)."""
-    if not os.path.isdir(ref_include):
+    ref_include = ref_include or reference_include()
+    if ref_include is None:
         return None
     subprocess.check_call(["make", "-s", "REF=" + ref_include], cwd=os.path.join(HERE, "refbuild"))
     return REF_SO

@@ -14,12 +14,13 @@ they produce:
   (tests/functional_tests/lrmat/test_lrmat_partialACA.cpp:21-67).
 
 Usage (needs the upstream sources, i.e. only in the build container):
-    make -C oracle/refbuild REF=/root/reference/include
+    make -C oracle/refbuild [REF=<htool source tree>/include]
     python tests/golden/make_golden.py          # everything but the leaf maps
     python tests/golden/make_golden.py plot     # the save_plot leaf maps only
     python tests/golden/make_golden.py sym      # the symmetric / sympartialACA builds only
     python tests/golden/make_golden.py ztransp  # transposed products of the Helmholtz fixture
     python tests/golden/make_golden.py zsym     # symmetric / Hermitian complex H-matrices
+    python tests/golden/make_golden.py zleaves  # upstream's complex leaves and their products
 """
 import ctypes as C
 import hashlib
@@ -277,6 +278,63 @@ def zsym_cases():
         print(name, "leaves", lr.shape[0], dn.shape[0], "ranks", lr[:, 4].min(), lr[:, 4].max())
 
 
+def helix(n, seed=1):
+    """n points on one turn of a helix of radius 1 and height 2 (seeded,
+    sorted parameters): a curve, so that a small complex H-matrix already
+    has most of its bytes in low-rank leaves and its fixture stays small"""
+    g = np.random.default_rng(seed)
+    t = np.sort(g.uniform(0.0, 1.0, n))
+    th = 2.0 * np.pi * t
+    return np.ascontiguousarray(np.stack([np.cos(th), np.sin(th), 2.0 * t], 1))
+
+
+def zleaves_case(n=1000):
+    """upstream's own complex leaves (Helmholtz exp(ikr)/(4 pi r), k = 20,
+    eta = 3, epsilon = 1e-5, points on a helix): leaf lists, U / V factors
+    and dense blocks in htool's layouts, with upstream's products and
+    transposed products on them, so that a GPU product over exactly these
+    leaves can be held to the FP64 tolerance independently of the
+    assembly's rounding"""
+    R = Oracle("reference")
+    R.set_num_threads(1)
+    L, vp = R._L, C.c_void_p
+    L.ref_hmatrix_build_z.restype = vp
+    L.ref_hmatrix_build_z.argtypes = [vp, vp, C.c_int, vp, C.c_int, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char, C.c_int]
+    L.ref_hmatrix_counts_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_leaves_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_factors_z.argtypes = [vp, vp, vp]
+    L.ref_hmatrix_mvprod_z.argtypes = [vp, vp, vp, C.c_int]
+    L.ref_hmatrix_mvprod_transp_z.argtypes = [vp, vp, vp, C.c_int]
+    L.ref_hmatrix_free_z.argtypes = [vp]
+    pts = helix(n, seed=1)
+    ct = R.cluster(pts)
+    h = L.ref_hmatrix_build_z(ct.h, ct.h, n, pts.ctypes.data, n, pts.ctypes.data, 20.0, 1e-5, 3.0, 0, b"N", b"N", 0)
+    a, b = C.c_int(), C.c_int()
+    L.ref_hmatrix_counts_z(h, C.byref(a), C.byref(b))
+    lr = np.empty((a.value, 5), np.int32)
+    dn = np.empty((b.value, 4), np.int32)
+    L.ref_hmatrix_leaves_z(h, lr.ctypes.data, dn.ctypes.data)
+    uv = np.empty(int((lr[:, 4].astype(np.int64) * (lr[:, 2] + lr[:, 3])).sum()), np.complex128)
+    dd = np.empty(int((dn[:, 2].astype(np.int64) * dn[:, 3]).sum()), np.complex128)
+    L.ref_hmatrix_factors_z(h, uv.ctypes.data, dd.ctypes.data)
+    perm = ct.export()[0]
+    rng = np.random.default_rng(12)
+    data = dict(xt=pts, perm=perm, lr=lr, dense=dn, uv=uv, dd=dd)
+    for mu in (1, 3):
+        x = rng.standard_normal(n * mu) + 1j * rng.standard_normal(n * mu)
+        y = np.empty(n * mu, np.complex128)
+        L.ref_hmatrix_mvprod_z(h, x.ctypes.data, y.ctypes.data, mu)
+        yt = np.empty(n * mu, np.complex128)
+        L.ref_hmatrix_mvprod_transp_z(h, x.ctypes.data, yt.ctypes.data, mu)
+        data["x_mu%d" % mu] = x
+        data["y_mu%d" % mu] = y
+        data["yT_mu%d" % mu] = yt
+    L.ref_hmatrix_free_z(h)
+    name = "helmholtz_helix%d_leaves" % n
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
+    print(name, "leaves", lr.shape[0], dn.shape[0], "complex entries", uv.size + dd.size)
+
+
 def plot_cases():
     """htool's leaf maps (HMatrix::save_plot) of the 4 000-point cylinder and
     Helmholtz fixtures, written by upstream itself (one thread)"""
@@ -306,5 +364,7 @@ if __name__ == "__main__":
         ztransp_case()
     elif sys.argv[1:] == ["zsym"]:
         zsym_cases()
+    elif sys.argv[1:] == ["zleaves"]:
+        zleaves_case()
     else:
         main()

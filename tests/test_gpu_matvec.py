@@ -111,19 +111,31 @@ def test_device_pointers_and_stream():
         assert np.array_equal(yd.cpu().numpy(), ref)  # deterministic: bitwise equal
 
 
-def test_cluster_numbering_flag():
+def test_cluster_numbering_flag(port):
+    """htool's local product on one rank (mvprod_local_to_local,
+    hmatrix.hpp:1185-1274: in and out in cluster numbering, no permutation)
+    against the oracle's product permuted into cluster numbering, and
+    bitwise against this library's own user-numbering product"""
     torch = pytest.importorskip("torch")
     pts = G.cylinder(3000, seed=2)
     t = H.Cluster().build(3000, pts)
     GH = H.HMatrix(t, t, 1e-6, 10.0).build(H.INV_R_EPS, pts)
-    x = G.rhs(3000)
-    y = GH.mvprod_global_to_global(x)
     perm = t.get_perm()
-    xd = torch.from_numpy(np.ascontiguousarray(x[perm])).cuda()
-    yd = torch.empty(3000, dtype=torch.float64, device="cuda")
-    GH.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, H.CLUSTER_NUMBERING, torch.cuda.current_stream().cuda_stream)
-    torch.cuda.synchronize()
-    assert np.array_equal(yd.cpu().numpy(), y[perm])
+    ot = port.cluster(pts)
+    assert np.array_equal(ot.export()[0], perm)
+    OH = port.hmatrix(ot, ot, pts, pts, H.INV_R_EPS, 1e-6, 10.0)
+    for mu in (1, 3):
+        x = G.rhs(3000, mu)
+        y = GH.mvprod_global_to_global(x, mu)
+        xl = np.ascontiguousarray(x.reshape(mu, 3000)[:, perm].ravel())
+        yl_oracle = OH.mvprod(x, mu).reshape(mu, 3000)[:, perm].ravel()
+        xd = torch.from_numpy(xl).cuda()
+        yd = torch.empty(3000 * mu, dtype=torch.float64, device="cuda")
+        GH.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), mu, H.CLUSTER_NUMBERING, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        yl = yd.cpu().numpy()
+        assert rel(yl, yl_oracle) < FP64_TOL
+        assert np.array_equal(yl, y.reshape(mu, 3000)[:, perm].ravel())
 
 
 def test_product_is_deterministic_and_linear():

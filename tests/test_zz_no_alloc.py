@@ -32,14 +32,13 @@ def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-def test_noalloc_product_matches_regular_product_twice():
-    torch = pytest.importorskip("torch")
-    n = 6000
-    pts = G.sphere(n, seed=21)
-    t = H.Cluster().build(n, pts)
-    hm = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
-    for mu in (1, 3):
-        x = torch.from_numpy(G.rhs(n, mu, seed=30 + mu)).cuda()
+def _check_twice(hm, n, mus, seed):
+    """the allocation-free product against the regular device-pointer product
+    of the same handle, twice in a row, for each number of right-hand sides"""
+    import torch
+
+    for mu in mus:
+        x = torch.from_numpy(G.rhs(n, mu, seed=seed + mu)).cuda()
         ref = torch.empty(n * mu, dtype=torch.float64, device="cuda")
         hm.mvprod_ptr(x.data_ptr(), ref.data_ptr(), mu, 0, None)
         torch.cuda.synchronize()
@@ -50,7 +49,34 @@ def test_noalloc_product_matches_regular_product_twice():
             rc = _noalloc(hm.h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), mu, None)
             assert rc == 0, H.lib.htgpu_last_error().decode()
             torch.cuda.synchronize()
+            assert hm.device_status() == 0
             assert rel(y.cpu().numpy(), ref_h) < FP64_TOL, (mu, call)
+
+
+def test_noalloc_product_matches_regular_product_twice():
+    """FP64 factors: one and three right-hand sides (the one-right-hand-side
+    kernels) and sixteen (the many-right-hand-side double-float kernels);
+    then mixed FP32/BF16 factors with one and sixteen"""
+    pytest.importorskip("torch")
+    n = 6000
+    pts = G.sphere(n, seed=21)
+    t = H.Cluster().build(n, pts)
+    hm = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+    _check_twice(hm, n, (1, 3, 16), seed=30)
+    hm.set_precision("mixed", 1.0)
+    _check_twice(hm, n, (1, 16), seed=40)
+
+
+def test_noalloc_tensor_core_path():
+    """epsilon 1e-5 with mixed factors and eight right-hand sides: the
+    products whose low-rank contractions run on the tensor cores"""
+    pytest.importorskip("torch")
+    n = 6000
+    pts = G.sphere(n, seed=23)
+    t = H.Cluster().build(n, pts)
+    hm = H.HMatrix(t, t, 1e-5, 10.0).build(H.LAPLACE, pts)
+    hm.set_precision("mixed", 1.0)
+    _check_twice(hm, n, (8,), seed=50)
 
 
 def test_noalloc_rejects_requests_beyond_its_array():
