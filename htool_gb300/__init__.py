@@ -112,6 +112,13 @@ def _load():
         "htgpu_hmatrix_save": (i, [vp, C.c_char_p]),
         "htgpu_hmatrix_save_plot": (i, [vp, C.c_char_p]),
         "htgpu_hmatrix_load": (i, [vp, C.c_char_p]),
+        "htgpu_hmatrix_build_host": (i, [vp, vp, vp, vp, vp]),
+        "htgpu_hmatrix_build_host_sym": (i, [vp, vp, vp, vp]),
+        "htgpu_aca_create": (i, [i, vp]),
+        "htgpu_aca_destroy": (i, [vp]),
+        "htgpu_aca_compress": (i, [vp, vp, vp, d, i, i, vp, vp, vp, vp, i, vp]),
+        "htgpu_aca_factors": (i, [vp, vp, vp]),
+        "htgpu_cluster_import": (i, [i, vp, i, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -194,6 +201,18 @@ class Cluster:
         _check(lib.htgpu_cluster_get_nodes(self.h, _ptr(ni), _ptr(nd)))
         return ni, nd
 
+    def import_tree(self, perm, node_i, node_d):
+        """Replace this tree by one given node by node in pre-order (the
+        layout of get_nodes), e.g. walked from any htool VirtualCluster."""
+        perm = np.ascontiguousarray(perm, dtype=np.int32)
+        node_i = np.ascontiguousarray(node_i, dtype=np.int32)
+        node_d = np.ascontiguousarray(node_d, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib.htgpu_cluster_import(perm.size, _ptr(perm), node_i.shape[0], _ptr(node_i), _ptr(node_d), C.byref(h)))
+        self._free()
+        self.h = h
+        return self
+
     def save_cluster(self, filename):
         """htool's <filename>_permutation.csv and <filename>_tree.csv."""
         _check(lib.htgpu_cluster_save(self.h, str(filename).encode()))
@@ -230,6 +249,97 @@ def block_tasks(t, s, eta, UPLO="N", force_sym=False):
 
 
 COMPRESSIONS = {"partialACA": 0, "sympartialACA": 1}
+
+# htgpu_generator_fn: int (*)(void *ctx, int M, int N, const int *rows, const int *cols, double *ptr)
+GENERATOR_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double))
+
+
+class VirtualGenerator:
+    """htool's VirtualGenerator<double> (types/virtual_generator.hpp:13-32):
+    subclass and implement copy_submatrix(rows, cols, out), filling the
+    M x N array `out` (column-major view) with A(rows[i], cols[j]) in user
+    numbering.  The library calls it from several threads (under the GIL)."""
+
+    def __init__(self, nr, nc, dimension=1):
+        self.nr, self.nc, self.dimension = nr, nc, dimension
+
+    def nb_rows(self):
+        return self.nr
+
+    def nb_cols(self):
+        return self.nc
+
+    def copy_submatrix(self, rows, cols, out):
+        raise NotImplementedError
+
+
+class _Trampoline:
+    """a VirtualGenerator (or a callable (rows, cols) -> M x N array) as an
+    htgpu_generator_fn; the first exception it raises is kept and re-raised
+    by the caller"""
+
+    def __init__(self, gen):
+        self.gen = gen
+        self.error = None
+
+        def call(ctx, M, N, rows, cols, ptr):
+            try:
+                r = np.ctypeslib.as_array(rows, (M,)).copy()
+                c = np.ctypeslib.as_array(cols, (N,)).copy()
+                out = np.ctypeslib.as_array(ptr, (M * N,)).reshape(N, M).T  # column-major M x N view
+                if isinstance(self.gen, VirtualGenerator):
+                    self.gen.copy_submatrix(r, c, out)
+                else:
+                    out[...] = self.gen(r, c)
+                return 0
+            except BaseException as e:  # noqa: BLE001 -- reported through the status code
+                if self.error is None:
+                    self.error = e
+                return 1
+
+        self.fn = GENERATOR_FN(call)
+
+    def check(self, status):
+        if self.error is not None:
+            e, self.error = self.error, None
+            raise e
+        _check(status)
+
+
+class DeviceACA:
+    """partialACA on the device for one block with a host generator: htool's
+    VirtualLowRankGenerator<double>::copy_low_rank_approximation
+    (lrmat/virtual_lrmat_generator.hpp:15) as partialACA implements it."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        _check(lib.htgpu_aca_create(int(device), C.byref(h)))
+        self.h = h
+
+    def copy_low_rank_approximation(self, epsilon, rows, cols, generator, xt=None, ctr=None, rank=-1):
+        """(rank, U (M x r), V (r x N)); rank -1 (and no factors) when the
+        block is not worth compressing"""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        cols = np.ascontiguousarray(cols, dtype=np.int32)
+        xt = None if xt is None else np.ascontiguousarray(xt, dtype=np.float64)
+        ctr = None if ctr is None else np.ascontiguousarray(ctr, dtype=np.float64)
+        tr = _Trampoline(generator)
+        r = C.c_int()
+        tr.check(lib.htgpu_aca_compress(self.h, tr.fn, None, float(epsilon), rows.size, cols.size, _ptr(rows), _ptr(cols), None if xt is None else _ptr(xt), None if ctr is None else _ptr(ctr), int(rank), C.byref(r)))
+        if r.value <= 0:
+            return r.value, None, None
+        U = np.empty(rows.size * r.value)
+        V = np.empty(r.value * cols.size)
+        _check(lib.htgpu_aca_factors(self.h, _ptr(U), _ptr(V)))
+        return r.value, U.reshape(r.value, rows.size).T, V.reshape(cols.size, r.value).T
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib.htgpu_aca_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
 
 
 class HMatrix:
@@ -279,6 +389,20 @@ class HMatrix:
         xt = np.ascontiguousarray(xt, dtype=np.float64)
         xs = xt if xs is None else np.ascontiguousarray(xs, dtype=np.float64)
         _check(lib.htgpu_hmatrix_build(self.h, kid, float(kernel_param), _ptr(xt), _ptr(xs)))
+        return self
+
+    def build_generator(self, generator, xt, xs=None):
+        """HMatrix::build(mat, xt, xs) (hmatrix.hpp:286-341) with a host
+        generator: a VirtualGenerator or a callable (rows, cols) -> array;
+        partialACA runs on the device, fed row by row and column by column.
+        Without xs: the one-array build(mat, xt) (hmatrix.hpp:343-400)."""
+        xt = np.ascontiguousarray(xt, dtype=np.float64)
+        tr = _Trampoline(generator)
+        if xs is None:
+            tr.check(lib.htgpu_hmatrix_build_host_sym(self.h, tr.fn, None, _ptr(xt)))
+        else:
+            xs = np.ascontiguousarray(xs, dtype=np.float64)
+            tr.check(lib.htgpu_hmatrix_build_host(self.h, tr.fn, None, _ptr(xt), _ptr(xs)))
         return self
 
     def set_leaves(self, lr_desc, uv, dense_desc, dense):

@@ -304,6 +304,229 @@ __global__ void __launch_bounds__(kAcaThreads) partial_aca_kernel(const AcaBlock
         rank_out[blockIdx.x] = q;
 }
 
+// ---------------------------------------------------------------------------
+// partialACA fed by a host generator, one step per launch.  The arithmetic
+// of every step is partial_aca_kernel's (and so htool's, partialACA.hpp:
+// 68-158): the same residual updates with explicit fma, the same last-max
+// pivots, the same tree-summed Frobenius estimator; only the generator
+// entries come from the host's copy_submatrix rows / columns staged in
+// device memory instead of a device generator.
+// ---------------------------------------------------------------------------
+
+// htool's loop test and the next cross's admission (partialACA.hpp:68-76):
+// returns true when the block needs the row of the next cross
+__device__ __forceinline__ bool aca_next_cross(AcaStep &S, int M, int N, int cap, double eps) {
+    const bool go = S.reqrank > 0 ? S.q < min(S.reqrank, min(M, N)) : (S.q == 0 || sqrt(S.aux / S.frob) > eps);
+    if (!go)
+        return false;
+    S.q += 1;
+    if ((int)((unsigned)S.q * (unsigned)(M + N)) > (int)((unsigned)M * (unsigned)N)) {
+        S.q = -1;
+        return false;
+    }
+    if (S.q > cap) {
+        S.q = -2;
+        return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kAcaThreads) aca_step_init_kernel(const AcaBlock *__restrict__ blocks, const double *__restrict__ xt, const int *__restrict__ perm_t, int host_first_row, double eps,
+                                                                     unsigned char *__restrict__ flags, AcaStep *__restrict__ state) {
+    constexpr int NT = kAcaThreads;
+    __shared__ double sv[NT / 32];
+    __shared__ int si[NT / 32];
+    const AcaBlock B = blocks[blockIdx.x];
+    const int M = B.M, N = B.N, tid = threadIdx.x;
+    unsigned char *vrow = flags + B.flag_off;
+    for (int i = tid; i < M + N; i += NT)
+        vrow[i] = 0;
+    AcaStep S = state[blockIdx.x];
+    if (!host_first_row) {
+        const int *rows = perm_t + B.row_off;
+        double best     = 1e300;
+        int I           = 0x7fffffff;
+        for (int i = tid; i < M; i += NT) {
+            const double *p = xt + 3 * (size_t)rows[i];
+            double s        = 0.;
+            for (int d = 0; d < 3; d++)
+                s = s + (p[d] - B.ctr[d]) * (p[d] - B.ctr[d]);
+            double ad = sqrt(s);
+            if (ad < best) {
+                best = ad;
+                I    = i;
+            }
+        }
+        BlockReduce<NT>::argmin(best, I, sv, si);
+        S.I = best < 1e30 ? I : 0;
+    }
+    S.q    = 0;
+    S.J    = 0;
+    S.frob = 0.;
+    S.aux  = 0.;
+    S.gamma = 0.;
+    S.status = aca_next_cross(S, M, N, B.cap, eps) ? kAcaNeedRow : kAcaDone;
+    __syncthreads();
+    if (tid == 0)
+        state[blockIdx.x] = S;
+}
+
+__global__ void __launch_bounds__(kAcaThreads) aca_step_kernel(const AcaBlock *__restrict__ blocks, const int *__restrict__ active, const long long *__restrict__ stage_off,
+                                                                const double *__restrict__ stage, double eps, double *__restrict__ scratch, unsigned char *__restrict__ flags,
+                                                                AcaStep *__restrict__ state) {
+    constexpr int NT = kAcaThreads;
+    __shared__ double sv[NT / 32];
+    __shared__ int si[NT / 32];
+    __shared__ double sdot[NT / 32][kDotChunk];
+    __shared__ double sres[kDotChunk];
+    __shared__ double sacc[3];
+
+    const int b      = active[blockIdx.x];
+    const AcaBlock B = blocks[b];
+    AcaStep S        = state[b];
+    const int M = B.M, N = B.N, tid = threadIdx.x;
+    double *U           = scratch + B.u_off;
+    double *Vt          = scratch + B.v_off;
+    unsigned char *vrow = flags + B.flag_off;
+    unsigned char *vcol = vrow + M;
+    const double *g     = stage + stage_off[blockIdx.x];
+    const int k         = S.q - 1;
+    if (S.status == kAcaNeedRow) {
+        // ---- row I of the residual -> Vt_s[:, k]  (partialACA.hpp:83-100)
+        const int I = S.I;
+        double piv  = -1.;
+        int J       = -1;
+        for (int j = tid; j < N; j += NT) {
+            double v = g[j];
+            for (int p = 0; p < k; p++)
+                v = fma(-U[I + (size_t)M * p], Vt[j + (size_t)N * p], v);
+            Vt[j + (size_t)N * k] = v;
+            if (!vcol[j]) {
+                double a = fabs(v);
+                if (!(a < piv)) {
+                    piv = a;
+                    J   = j;
+                }
+            }
+        }
+        BlockReduce<NT>::argmax(piv, J, sv, si);
+        if (J < 0) { // no admissible pivot column (only with non-finite entries)
+            S.q      = S.q - 1 == 0 ? -1 : S.q - 1;
+            S.status = kAcaDone;
+        } else {
+            if (tid == 0)
+                vrow[I] = 1;
+            __syncthreads();
+            const double rJ = Vt[J + (size_t)N * k];
+            if (fabs(rJ) > 1e-15) {
+                S.gamma  = 1. / rJ;
+                S.J      = J;
+                S.status = kAcaNeedCol;
+            } else { // zero row (partialACA.hpp:149-156)
+                S.q -= 1;
+                if (S.q == 0)
+                    S.q = -1;
+                S.status = kAcaDone;
+            }
+        }
+    } else if (S.status == kAcaNeedCol) {
+        // ---- column J of the residual, scaled -> U_s[:, k]  (partialACA.hpp:108-124)
+        const int J = S.J;
+        const double gamma = S.gamma;
+        double piv2 = -1.;
+        int I2      = -1;
+        for (int i = tid; i < M; i += NT) {
+            double v = g[i];
+            for (int p = 0; p < k; p++)
+                v = fma(-Vt[J + (size_t)N * p], U[i + (size_t)M * p], v);
+            v                    = v * gamma;
+            U[i + (size_t)M * k] = v;
+            if (!vrow[i]) {
+                double a = fabs(v);
+                if (!(a < piv2)) {
+                    piv2 = a;
+                    I2   = i;
+                }
+            }
+        }
+        BlockReduce<NT>::argmax(piv2, I2, sv, si);
+        if (I2 < 0) { // no pivot row left (only with non-finite entries)
+            S.status = kAcaDone;
+        } else {
+            if (tid == 0)
+                vcol[J] = 1;
+            if (S.reqrank <= 0) {
+                // ---- Frobenius estimator (partialACA.hpp:127-141), as partial_aca_kernel
+                const int nd = 2 + 2 * k;
+                const int lane = tid & 31, warp = tid >> 5;
+                if (tid == 0)
+                    sacc[1] = 0.;
+                for (int d0 = 0; d0 < nd; d0 += kDotChunk) {
+                    const int dn = min(kDotChunk, nd - d0);
+                    for (int dd = 0; dd < dn; dd++) {
+                        const int d = d0 + dd;
+                        double s    = 0.;
+                        if (d == 0) {
+                            for (int i = tid; i < M; i += NT) {
+                                double c = U[i + (size_t)M * k];
+                                s        = s + c * c;
+                            }
+                        } else if (d == 1) {
+                            for (int j = tid; j < N; j += NT) {
+                                double r = Vt[j + (size_t)N * k];
+                                s        = s + r * r;
+                            }
+                        } else if (d & 1) {
+                            int p = (d - 2) >> 1;
+                            for (int j = tid; j < N; j += NT)
+                                s = s + Vt[j + (size_t)N * p] * Vt[j + (size_t)N * k];
+                        } else {
+                            int p = (d - 2) >> 1;
+                            for (int i = tid; i < M; i += NT)
+                                s = s + U[i + (size_t)M * p] * U[i + (size_t)M * k];
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1)
+                            s = s + __shfl_down_sync(0xffffffffu, s, o);
+                        if (lane == 0)
+                            sdot[warp][dd] = s;
+                    }
+                    __syncthreads();
+                    if (tid < dn) {
+                        double s = 0.;
+                        for (int w = 0; w < NT / 32; w++)
+                            s = s + sdot[w][tid];
+                        sres[tid] = s;
+                    }
+                    __syncthreads();
+                    if (tid == 0) {
+                        for (int dd = 0; dd < dn; dd++) {
+                            const int d = d0 + dd;
+                            if (d == 0)
+                                sacc[0] = fabs(sres[dd]);
+                            else if (d == 1)
+                                sacc[0] = sacc[0] * fabs(sres[dd]);
+                            else if (d & 1)
+                                sacc[1] = sacc[1] + sres[dd] * sacc[2];
+                            else
+                                sacc[2] = sres[dd];
+                        }
+                    }
+                    __syncthreads();
+                }
+                S.aux     = sacc[0];
+                double fa = sacc[1];
+                S.frob    = S.frob + (S.aux + 2 * fa);
+            }
+            S.I      = I2;
+            S.status = aca_next_cross(S, M, N, B.cap, eps) ? kAcaNeedRow : kAcaDone;
+        }
+    }
+    __syncthreads();
+    if (tid == 0)
+        state[b] = S;
+}
+
 __global__ void pack_factors_kernel(const PackItem *__restrict__ items, const double *__restrict__ scratch, double *__restrict__ arena) {
     const PackItem it = items[blockIdx.x];
     const long long nu = (long long)it.M * it.r, nv = (long long)it.N * it.r;
@@ -565,6 +788,21 @@ void launch_partial_aca(const AcaBlock *blocks, int nblocks, const double *xt, c
     if (nblocks <= 0)
         return;
     partial_aca_kernel<<<nblocks, kAcaThreads, 0, st>>>(blocks, xt, xs, perm_t, perm_s, kd, eps, scratch, flags, rank_out);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_aca_step_init(const AcaBlock *blocks, int nblocks, const double *xt, const int *perm_t, bool host_first_row, double eps, unsigned char *flags, AcaStep *state, cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    aca_step_init_kernel<<<nblocks, kAcaThreads, 0, st>>>(blocks, xt, perm_t, host_first_row ? 1 : 0, eps, flags, state);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_aca_step(const AcaBlock *blocks, const int *active, const long long *stage_off, int nactive, const double *stage, double eps, double *scratch, unsigned char *flags, AcaStep *state,
+                     cudaStream_t st) {
+    if (nactive <= 0)
+        return;
+    aca_step_kernel<<<nactive, kAcaThreads, 0, st>>>(blocks, active, stage_off, stage, eps, scratch, flags, state);
     HTGPU_CUDA(cudaGetLastError());
 }
 

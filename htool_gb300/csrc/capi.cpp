@@ -24,6 +24,10 @@ struct htgpu_batch_s {
     std::unique_ptr<htgpu::Batch> b;
 };
 
+struct htgpu_aca_s {
+    std::unique_ptr<htgpu::AcaSession> a;
+};
+
 namespace {
 thread_local std::string g_last_error;
 
@@ -211,6 +215,79 @@ int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, con
         kd.id    = kernel_id;
         kd.param = kernel_param;
         h->h->build(kd, xt, xs);
+    });
+}
+
+int htgpu_hmatrix_build_host(htgpu_hmatrix h, htgpu_generator_fn gen, void *ctx, const double *xt, const double *xs) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need((const void *)gen, "generator");
+        need(xt, "xt");
+        need(xs, "xs");
+        h->h->build_host(htgpu::HostGen{gen, ctx}, xt, xs);
+    });
+}
+
+int htgpu_hmatrix_build_host_sym(htgpu_hmatrix h, htgpu_generator_fn gen, void *ctx, const double *xt) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need((const void *)gen, "generator");
+        need(xt, "xt");
+        h->h->build_host(htgpu::HostGen{gen, ctx}, xt, xt, true);
+    });
+}
+
+int htgpu_aca_create(int device, htgpu_aca *out) {
+    return guarded([&] {
+        need(out, "out");
+        auto *a = new htgpu_aca_s;
+        try {
+            a->a.reset(new htgpu::AcaSession(device));
+        } catch (...) {
+            delete a;
+            throw;
+        }
+        *out = a;
+    });
+}
+
+int htgpu_aca_destroy(htgpu_aca a) {
+    return guarded([&] { delete a; });
+}
+
+int htgpu_aca_compress(htgpu_aca a, htgpu_generator_fn gen, void *ctx, double epsilon, int M, int N, const int *rows, const int *cols, const double *xt, const double *ctr, int reqrank, int *rank) {
+    return guarded([&] {
+        need(a, "aca");
+        need((const void *)gen, "generator");
+        need(rank, "rank");
+        htgpu::require(epsilon > 0 || reqrank > 0, "epsilon must be positive");
+        *rank = a->a->compress(htgpu::HostGen{gen, ctx}, epsilon, M, N, rows, cols, xt, ctr, reqrank);
+    });
+}
+
+int htgpu_aca_factors(htgpu_aca a, double *U, double *V) {
+    return guarded([&] {
+        need(a, "aca");
+        need(U, "U");
+        need(V, "V");
+        a->a->factors(U, V);
+    });
+}
+
+int htgpu_cluster_import(int n, const int *perm, int nnodes, const int *node_i, const double *node_d, htgpu_cluster *out) {
+    return guarded([&] {
+        need(perm, "perm");
+        need(node_i, "node_i");
+        need(node_d, "node_d");
+        need(out, "out");
+        auto *c = new htgpu_cluster_s;
+        try {
+            c->tree = std::make_shared<htgpu::ClusterTree>(htgpu::import_cluster(n, perm, nnodes, node_i, node_d));
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *out = c;
     });
 }
 

@@ -155,6 +155,17 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
         require(kd.id == 2, "a complex H-matrix needs the Helmholtz device generator (id 2)", 2);
     else
         require(kd.id == 0 || kd.id == 1, "device generator id must be 0 (1/(1e-5+r)) or 1 (Laplace) for a real H-matrix", 2);
+    build_impl(&kd, nullptr, xt, xs, force_sym);
+}
+
+void HMatrix::build_host(const HostGen &g, const double *xt, const double *xs, bool force_sym) {
+    require(g.fn != nullptr, "the generator callback is null");
+    require(!complex_, "a host generator builds real H-matrices only; complex H-matrices use the Helmholtz device generator", 2);
+    build_impl(nullptr, &g, xt, xs, force_sym);
+}
+
+void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double *xt, const double *xs, bool force_sym) {
+    const KernelDesc kd = kdp ? *kdp : KernelDesc{kHostKernelId, 0.};
     nlr_stored_ = ndn_stored_ = -1;
     // block tree and ACA on the trees of the points; a complex H-matrix is
     // stored in real form on doubled trees (T, S), its leaves scaled by f
@@ -348,20 +359,32 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
             st_.aca_peak_scratch_bytes = std::max(st_.aca_peak_scratch_bytes, 8 * sc);
             flags.alloc(fl);
             dranks.alloc(blocks.size());
-            if (complex_) {
-                if (n_direct > 0)
-                    launch_partial_aca_z(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
-                if ((int)blocks.size() > n_direct)
-                    launch_partial_aca_z(dblocks.p + n_direct, (int)blocks.size() - n_direct, dxs.p, dxt.p, aca_ps, aca_pt, kd, eps_, scratch.p, flags.p, dranks.p + n_direct, stream_);
-            } else {
-                if (n_direct > 0)
-                    launch_partial_aca(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
-                if ((int)blocks.size() > n_direct)
-                    launch_partial_aca(dblocks.p + n_direct, (int)blocks.size() - n_direct, dxs.p, dxt.p, aca_ps, aca_pt, kd, eps_, scratch.p, flags.p, dranks.p + n_direct, stream_);
-            }
             std::vector<int> ranks(blocks.size());
-            HTGPU_CUDA(cudaMemcpyAsync(ranks.data(), dranks.p, sizeof(int) * ranks.size(), cudaMemcpyDeviceToHost, stream_));
-            HTGPU_CUDA(cudaStreamSynchronize(stream_));
+            if (hg) {
+                // rows and columns in user numbering; a mirrored block reads
+                // the generator with the roles of the two trees exchanged
+                std::vector<const int *> ru(blocks.size()), cu(blocks.size());
+                for (std::size_t b = 0; b < blocks.size(); b++) {
+                    const bool mir = (int)b >= n_direct;
+                    ru[b]          = (mir ? Sa.perm.data() : Ta.perm.data()) + blocks[b].row_off;
+                    cu[b]          = (mir ? Ta.perm.data() : Sa.perm.data()) + blocks[b].col_off;
+                }
+                aca_host_batch(*hg, blocks, ru, cu, dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, nullptr, -1, eps_, scratch.p, flags.p, ranks, stream_);
+            } else {
+                if (complex_) {
+                    if (n_direct > 0)
+                        launch_partial_aca_z(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+                    if ((int)blocks.size() > n_direct)
+                        launch_partial_aca_z(dblocks.p + n_direct, (int)blocks.size() - n_direct, dxs.p, dxt.p, aca_ps, aca_pt, kd, eps_, scratch.p, flags.p, dranks.p + n_direct, stream_);
+                } else {
+                    if (n_direct > 0)
+                        launch_partial_aca(dblocks.p, n_direct, dxt.p, dxs.p, aca_pt, aca_ps, kd, eps_, scratch.p, flags.p, dranks.p, stream_);
+                    if ((int)blocks.size() > n_direct)
+                        launch_partial_aca(dblocks.p + n_direct, (int)blocks.size() - n_direct, dxs.p, dxt.p, aca_ps, aca_pt, kd, eps_, scratch.p, flags.p, dranks.p + n_direct, stream_);
+                }
+                HTGPU_CUDA(cudaMemcpyAsync(ranks.data(), dranks.p, sizeof(int) * ranks.size(), cudaMemcpyDeviceToHost, stream_));
+                HTGPU_CUDA(cudaStreamSynchronize(stream_));
+            }
             st_.aca_rounds++;
             st_.aca_blocks += (long long)blocks.size();
             // pack the accepted crosses of this slice
@@ -491,7 +514,38 @@ void HMatrix::build(const KernelDesc &kd, const double *xt, const double *xs, bo
     std::vector<const double *> bufs;
     for (auto &b : round_bufs)
         bufs.push_back(b->p);
-    finalize(bufs, lr_src, nullptr, &kd, dxt.p, dxs.p);
+    if (!hg) {
+        finalize(bufs, lr_src, nullptr, &kd, dxt.p, dxs.p);
+    } else {
+        // dense leaves from the host generator, one block per call, into
+        // one pinned buffer; the twins of a symmetric H-matrix read their
+        // stored block transposed
+        const int nd0 = n_dense();
+        std::vector<long long> doff(nd0 + 1, 0);
+        for (int d = 0; d < nd0; d++)
+            doff[d + 1] = doff[d] + (long long)dn_h[d].m * dn_h[d].n;
+        double *dh = nullptr;
+        HTGPU_CUDA(cudaMallocHost((void **)&dh, sizeof(double) * (std::size_t)std::max<long long>(doff[nd0], 1)));
+        std::unique_ptr<double, cudaError_t (*)(void *)> dh_guard(dh, cudaFreeHost);
+        host_parallel_for(nd0, [&](long long d) {
+            const DenseLeaf &D = dn_h[d];
+            call_generator(*hg, D.m, D.n, Ta.perm.data() + D.oi, Sa.perm.data() + D.oj, dh + doff[d]);
+        });
+        auto dbuf = std::unique_ptr<DevBuf<double>>(new DevBuf<double>());
+        dbuf->upload(dh, (std::size_t)std::max<long long>(doff[nd0], 1), stream_);
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+        const int bi = (int)bufs.size();
+        bufs.push_back(dbuf->p);
+        round_bufs.push_back(std::move(dbuf));
+        std::vector<LeafSrc> dn_src;
+        for (int d = 0; d < nd0; d++)
+            dn_src.push_back({bi, doff[d], 0, 0, 0});
+        for (int d = 0; d < nd0; d++)
+            if ((int)dn_h.size() > nd0 && dn_h[d].oi != dn_h[d].oj)
+                dn_src.push_back({bi, doff[d], 0, 0, 1});
+        require(dn_src.size() == dn_h.size(), "dense twins out of step with their blocks", 5);
+        finalize(bufs, lr_src, &dn_src, nullptr, nullptr, nullptr);
+    }
     st_.build_seconds = now() - t0;
 }
 

@@ -3,10 +3,58 @@
 #pragma once
 #include "kernels.hpp"
 
+#include <functional>
 #include <map>
 #include <memory>
 
 namespace htgpu {
+
+// A host generator: htool's VirtualGenerator<double>::copy_submatrix
+// (include/htool/types/virtual_generator.hpp:22) as a C callback filling
+// ptr[i + M j] = A(rows[i], cols[j]) (user numbering), nonzero on failure.
+// It is called concurrently from several host threads.
+struct HostGen {
+    int (*fn)(void *ctx, int M, int N, const int *rows, const int *cols, double *ptr);
+    void *ctx;
+};
+constexpr int kHostKernelId = 3; // kernel id of a host generator in the rank predictor's features
+
+int host_threads();
+void host_parallel_for(long long n, const std::function<void(long long)> &body);
+void call_generator(const HostGen &g, int M, int N, const int *rows, const int *cols, double *ptr);
+
+// partialACA of a batch of blocks fed by a host generator (hostgen.cpp):
+// blocks[b] with its user-numbered row / column index arrays; blocks from
+// n_direct on are mirrors (first pivot from the source points); first_rows
+// (optional) gives every block's first pivot row instead; ranks as
+// launch_partial_aca
+void aca_host_batch(const HostGen &g, const std::vector<AcaBlock> &blocks, const std::vector<const int *> &rows_user, const std::vector<const int *> &cols_user, const AcaBlock *dblocks, int n_direct,
+                    const double *dxt, const double *dxs, const int *dperm_t, const int *dperm_s, const std::vector<int> *first_rows, int reqrank, double eps, double *scratch, unsigned char *flags,
+                    std::vector<int> &ranks, cudaStream_t st);
+
+// One block compressed at a time, htool's VirtualLowRankGenerator<double>::
+// copy_low_rank_approximation (lrmat/virtual_lrmat_generator.hpp:15) with
+// partialACA's algorithm on the device and the rows / columns from a host
+// generator
+class AcaSession {
+  public:
+    explicit AcaSession(int device);
+    ~AcaSession();
+    // rank (htool's: -1 when the block is not worth compressing); xt / ctr
+    // (optional) choose the first row as partialACA does
+    int compress(const HostGen &g, double eps, int M, int N, const int *rows, const int *cols, const double *xt, const double *ctr, int reqrank);
+    // U (M x rank) and V (rank x N), column-major, of the last compression
+    void factors(double *U, double *V) const;
+    int rank() const { return rank_; }
+    int rows() const { return M_; }
+    int cols() const { return N_; }
+
+  private:
+    int device_;
+    cudaStream_t st_ = nullptr;
+    DevBuf<double> scratch_;
+    int rank_ = 0, M_ = 0, N_ = 0, cap_ = 0;
+};
 
 struct BuildStats {
     double block_tree_seconds = 0, build_seconds = 0, aca_seconds = 0;
@@ -37,6 +85,10 @@ class HMatrix {
     // build(gen, xt) (hmatrix.hpp:343-400), which always uses the symmetric
     // block tree
     void build(const KernelDesc &kd, const double *xt, const double *xs, bool force_sym = false);
+    // the same with a host generator (htool's VirtualGenerator): partialACA
+    // on the device fed row by row and column by column from the host, dense
+    // leaves filled by the generator (real H-matrices)
+    void build_host(const HostGen &g, const double *xt, const double *xs, bool force_sym = false);
 
     // HMatrix(t, s, eps, eta, symmetry, UPLO) (hmatrix.hpp:115-122): 'N'/'N'
     // or 'S' with 'U' or 'L' (one triangle stored, applied with its
@@ -158,6 +210,7 @@ class HMatrix {
         int tr  = 0; // dense: the leaf is the transpose of the block at su (D.n x D.m stored)
     };
     int dense_mode(int d) const; // DenseMode of the fill of dense leaf d
+    void build_impl(const KernelDesc *kd, const HostGen *hg, const double *xt, const double *xs, bool force_sym);
     void finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs);
     void assign_phase1_modes();
     void ensure_work(int mu);

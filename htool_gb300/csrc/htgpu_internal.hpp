@@ -219,6 +219,8 @@ std::vector<int> partition_rows(int nleaves, const long long *leaves, int nr, in
 // htool's CSV pair for cluster trees (cluster.hpp:433-583)
 void save_cluster(const ClusterTree &T, const std::string &name);
 ClusterTree read_cluster(const std::string &perm_file, const std::string &tree_file);
+// a tree given node by node in pre-order (the layout of htgpu_cluster_get_nodes)
+ClusterTree import_cluster(int n, const int *perm, int nnodes, const int *node_i, const double *node_d);
 
 // tree of the interleaved (re, im) real form of vectors on the points of T
 ClusterTree double_tree(const ClusterTree &T);

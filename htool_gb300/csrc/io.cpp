@@ -13,6 +13,8 @@
 //   is reloaded only onto the same cluster trees.
 #include "hmatrix.hpp"
 
+#include <functional>
+
 #include <cstdint>
 #include <cstring>
 #include <fstream>
@@ -153,6 +155,65 @@ ClusterTree read_cluster(const std::string &perm_file, const std::string &tree_f
         }
         T.max_depth = std::max(T.max_depth, d);
     }
+    return T;
+}
+
+ClusterTree import_cluster(int n, const int *perm, int nnodes, const int *node_i, const double *node_d) {
+    require(n > 0 && nnodes > 0, "a cluster tree needs points and nodes");
+    ClusterTree T;
+    T.n = n;
+    T.perm.assign(perm, perm + n);
+    std::vector<char> seen(n, 0);
+    for (int i = 0; i < n; i++) {
+        require(perm[i] >= 0 && perm[i] < n && !seen[perm[i]], "the permutation is not a permutation of 0..n-1");
+        seen[perm[i]] = 1;
+    }
+    auto fill = [&](ClusterNode &c, int k) {
+        c.depth   = node_i[6 * k + 0];
+        c.rank    = node_i[6 * k + 1];
+        c.offset  = node_i[6 * k + 2];
+        c.size    = node_i[6 * k + 3];
+        c.counter = node_i[6 * k + 5];
+        c.rad     = node_d[4 * k];
+        for (int d = 0; d < 3; d++)
+            c.ctr[d] = node_d[4 * k + 1 + d];
+        require(c.offset >= 0 && c.size > 0 && c.offset + c.size <= n, "cluster node " + std::to_string(k) + " is out of range");
+        return node_i[6 * k + 4];
+    };
+    // pre-order in, construction order out: every node's sons contiguous
+    T.nodes.emplace_back();
+    const int ns0 = fill(T.nodes[0], 0);
+    require(T.nodes[0].offset == 0 && T.nodes[0].size == n, "the root cluster must hold every point");
+    int next = 1; // next pre-order record
+    T.min_depth = 1 << 30;
+    T.max_depth = 0;
+    std::function<void(int, int)> grow = [&](int v, int ns) {
+        const int d = T.nodes[v].depth;
+        T.max_depth = std::max(T.max_depth, d);
+        if (ns == 0) {
+            T.min_depth = std::min(T.min_depth, d);
+            return;
+        }
+        require(ns > 0, "negative number of sons");
+        const int first      = (int)T.nodes.size();
+        T.nodes[v].nb_sons   = ns;
+        T.nodes[v].first_son = first;
+        for (int p = 0; p < ns; p++)
+            T.nodes.emplace_back();
+        int off = T.nodes[v].offset;
+        for (int p = 0; p < ns; p++) {
+            require(next < nnodes, "fewer nodes than the sons counts announce");
+            const int nsp = fill(T.nodes[first + p], next++);
+            ClusterNode &c = T.nodes[first + p];
+            c.parent       = v;
+            require(c.depth == d + 1 && c.offset == off, "the sons of a cluster must follow it in pre-order and tile its points");
+            off += c.size;
+            grow(first + p, nsp);
+        }
+        require(off == T.nodes[v].offset + T.nodes[v].size, "the sons of a cluster must tile its points");
+    };
+    grow(0, ns0);
+    require(next == nnodes, "more nodes than the sons counts announce");
     return T;
 }
 

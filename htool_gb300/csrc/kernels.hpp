@@ -23,6 +23,30 @@ struct AcaBlock {
 void launch_partial_aca(const AcaBlock *blocks, int nblocks, const double *xt, const double *xs, const int *perm_t, const int *perm_s, KernelDesc kd, double eps, double *scratch, unsigned char *flags,
                         int *rank_out, cudaStream_t st);
 
+// partialACA fed by a host generator (htool's VirtualGenerator::copy_submatrix,
+// include/htool/types/virtual_generator.hpp:22): the steps of the
+// adaptive loop (partialACA.hpp:68-158) run on the device one cross at a
+// time for a batch of blocks, and between steps the host fills the residual
+// row or column each block asks for.  state per block:
+constexpr int kAcaNeedRow = 0, kAcaNeedCol = 1, kAcaDone = 2;
+struct AcaStep {
+    int q;       // current rank (htool's q): the final rank, -1 rejected, -2 out of scratch, once done
+    int I, J;    // pivot row / column (block-local) the next step reads
+    int status;  // kAcaNeedRow / kAcaNeedCol / kAcaDone
+    int reqrank; // htool's rank argument: <= 0 adaptive, > 0 a required rank
+    int pad;
+    double frob, aux, gamma;
+};
+// flags cleared, first pivot row chosen (nearest the block's target centre,
+// from xt / perm_t as launch_partial_aca, unless host_first_row: then
+// state[b].I is already set), the loop's first test taken
+void launch_aca_step_init(const AcaBlock *blocks, int nblocks, const double *xt, const int *perm_t, bool host_first_row, double eps, unsigned char *flags, AcaStep *state, cudaStream_t st);
+// one step for the blocks active[a] (a < nactive): the generator's row
+// A(I, :) (status need-row) or column A(:, J) (need-column) of block
+// active[a] sits at stage + stage_off[a]
+void launch_aca_step(const AcaBlock *blocks, const int *active, const long long *stage_off, int nactive, const double *stage, double eps, double *scratch, unsigned char *flags, AcaStep *state,
+                     cudaStream_t st);
+
 struct PackItem {
     long long src_u, src_v, dst_u, dst_v;
     int M, N, r, pad;

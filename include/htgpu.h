@@ -60,6 +60,14 @@ int htgpu_version(int *major, int *minor);
 int htgpu_cluster_build(int n, const double *xyz, int minclustersize, int nb_sons, htgpu_cluster *out);
 int htgpu_cluster_destroy(htgpu_cluster c);
 
+/* A cluster tree built elsewhere, e.g. any htool VirtualCluster
+ * (include/htool/clustering/virtual_cluster.hpp:28-40) walked in pre-order:
+ * perm[n] (get_perm) and per node, sons in order, node_i[6 * k ...] =
+ * depth, rank, offset, size, nb_sons, counter and node_d[4 * k ...] = rad,
+ * ctr[0..2] (the layout of htgpu_cluster_get_nodes).  The sons of every
+ * node must tile its points. */
+int htgpu_cluster_import(int n, const int *perm, int nnodes, const int *node_i, const double *node_d, htgpu_cluster *out);
+
 /* Sizes: number of points, number of nodes, get_min_depth/get_max_depth
  * (cluster.hpp:277-278). */
 int htgpu_cluster_info(htgpu_cluster c, int *n, int *nnodes, int *min_depth, int *max_depth);
@@ -121,6 +129,46 @@ int htgpu_hmatrix_build(htgpu_hmatrix h, int kernel_id, double kernel_param, con
 /* HMatrix<double>::build(mat, xt) (hmatrix.hpp:343-400): one point array
  * for rows and columns and the symmetric block tree (force_sym). */
 int htgpu_hmatrix_build_sym(htgpu_hmatrix h, int kernel_id, double kernel_param, const double *xt);
+
+/* A host generator: VirtualGenerator<double>::copy_submatrix(M, N, rows,
+ * cols, ptr) (include/htool/types/virtual_generator.hpp:22) as a C callback:
+ * fill ptr[i + M * j] = A(rows[i], cols[j]) (user numbering, ptr column-major
+ * and owned by the library) and return 0, or nonzero to abort the build
+ * (the call then fails with HTGPU_ERR_INVALID).  As in htool, where
+ * HMatrix::build calls it from OpenMP threads (hmatrix.hpp:424-452), it is
+ * called concurrently from several host threads and must be thread-safe. */
+typedef int (*htgpu_generator_fn)(void *ctx, int M, int N, const int *rows, const int *cols, double *ptr);
+
+/* Replaces HMatrix<double>::build(mat, xt, xs) (hmatrix.hpp:286-341) for a
+ * user generator that lives on the host.  partialACA (lrmat/partialACA.hpp:
+ * 39-171) runs on the device for every admissible block at once, one cross
+ * per step: the library asks the generator for the residual row A(I, :) of
+ * every unfinished block, then for the column A(:, J), in batches; dense
+ * leaves are filled by one call each.  htool's rejection and recursion rules
+ * and the current compression (set_compression) apply; with a generator
+ * that returns the same entries the result equals htgpu_hmatrix_build's
+ * (leaves, ranks and factors).  Real H-matrices only. */
+int htgpu_hmatrix_build_host(htgpu_hmatrix h, htgpu_generator_fn gen, void *ctx, const double *xt, const double *xs);
+/* HMatrix<double>::build(mat, xt) (hmatrix.hpp:343-400) with a host generator. */
+int htgpu_hmatrix_build_host_sym(htgpu_hmatrix h, htgpu_generator_fn gen, void *ctx, const double *xt);
+
+/* partialACA of one block with a host generator, on the device: the
+ * counterpart of VirtualLowRankGenerator<double>::copy_low_rank_approximation
+ * (include/htool/lrmat/virtual_lrmat_generator.hpp:15) as partialACA
+ * implements it (lrmat/partialACA.hpp:39-171).  rows / cols: the block's
+ * M and N user indices; xt (points, 3 doubles each, indexed by rows) and ctr
+ * (the target cluster's centre) choose the first row as htool does (row 0
+ * when either is NULL); reqrank: htool's rank argument (-1 adaptive to
+ * epsilon, > 0 a required rank).  *rank: the rank, or -1 when the block is
+ * not worth compressing (q (M + N) > M N), as htool returns it.  One handle
+ * per host thread: a handle is not thread-safe. */
+typedef struct htgpu_aca_s *htgpu_aca;
+int htgpu_aca_create(int device, htgpu_aca *out);
+int htgpu_aca_destroy(htgpu_aca a);
+int htgpu_aca_compress(htgpu_aca a, htgpu_generator_fn gen, void *ctx, double epsilon, int M, int N, const int *rows, const int *cols, const double *xt, const double *ctr, int reqrank, int *rank);
+/* The last compression's factors in htool's layouts (lrmat.hpp:47-50): U
+ * (M x rank) and V (rank x N), column-major, into caller memory. */
+int htgpu_aca_factors(htgpu_aca a, double *U, double *V);
 
 /* Before a build: the symmetry and UPLO arguments of HMatrix's constructor
  * (hmatrix.hpp:115-122): 'N' with 'N', or 'S' / 'H' with 'U' / 'L' -- one
@@ -355,8 +403,9 @@ int htgpu_batch_create(int device, htgpu_batch *out);
 int htgpu_batch_destroy(htgpu_batch b);
 int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, int *index);
 /* The same with flags: HTGPU_CLUSTER_NUMBERING makes the entry a product in
- * cluster (local) numbering, htool's mvprod_local_to_local on one rank
- * (hmatrix.hpp:1185-1274): what HPDDM's GMV calls in a Krylov loop
+ * cluster (local) numbering, htool's mymvprod_local_to_local on one rank
+ * (hmatrix.hpp:980-996; mvprod_local_to_local after set_use_permutation(false),
+ * :1185-1274): what HPDDM's GMV calls in a Krylov loop
  * (wrappers/wrapper_hpddm.hpp:41-83). */
 int htgpu_batch_add_flags(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, int *index);
 int htgpu_batch_capture(htgpu_batch b, int nstreams, long long *graph_nodes);

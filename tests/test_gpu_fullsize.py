@@ -41,7 +41,7 @@ def case(port):
     return pts, ot, OH, t, GH
 
 
-def test_fullsize_assembly_and_products(case):
+def test_fullsize_assembly_and_products(case, port):
     pts, ot, OH, t, GH = case
     assert np.array_equal(t.get_perm(), ot.export()[0])
     glr, gdn = GH.get_leaves()
