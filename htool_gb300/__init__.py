@@ -119,6 +119,8 @@ def _load():
         "htgpu_aca_compress": (i, [vp, vp, vp, d, i, i, vp, vp, vp, vp, i, vp]),
         "htgpu_aca_factors": (i, [vp, vp, vp]),
         "htgpu_cluster_import": (i, [i, vp, i, vp, vp, vp]),
+        "htgpu_hmatrix_reset_status": (i, [vp]),
+        "htgpu_debug_set_waits": (i, [i, C.c_longlong, C.c_longlong]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -541,6 +543,9 @@ class HMatrix:
         v = C.c_int()
         _check(lib.htgpu_hmatrix_device_status(self.h, C.byref(v)))
         return v.value
+
+    def reset_status(self):
+        _check(lib.htgpu_hmatrix_reset_status(self.h))
 
     def autotune(self, mu=1, reps=5):
         """Pick the fastest launch shape (and FP64 split) for this H-matrix and

@@ -529,6 +529,24 @@ int htgpu_hmatrix_precision_info(htgpu_hmatrix h, int *policy, long long *stored
     });
 }
 
+int htgpu_hmatrix_reset_status(htgpu_hmatrix h) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->reset_status();
+    });
+}
+
+int htgpu_debug_set_waits(int device, long long cycles, long long skip_chunk) {
+    return guarded([&] {
+        htgpu::require(cycles > 0, "the wait limit must be positive");
+        int prev = 0;
+        HTGPU_CUDA(cudaGetDevice(&prev));
+        HTGPU_CUDA(cudaSetDevice(device));
+        htgpu::set_debug_waits(cycles, skip_chunk);
+        HTGPU_CUDA(cudaSetDevice(prev));
+    });
+}
+
 int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out, int mu, void *stream) {
     return guarded([&] {
         if (h == nullptr)

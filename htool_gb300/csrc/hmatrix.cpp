@@ -1041,6 +1041,14 @@ int HMatrix::device_status() {
     return v;
 }
 
+void HMatrix::reset_status() {
+    HTGPU_CUDA(cudaSetDevice(device_));
+    if (status_d.p) {
+        HTGPU_CUDA(cudaMemsetAsync(status_d.p, 0, sizeof(int), stream_));
+        HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    }
+}
+
 // phase 2 of a reduced-precision product: its dense blocks stay FP64, on
 // the DFMA pipe for p2m_n64_ / 1000 of their elements and emulated on the
 // FP32 pipe for the rest (error diffusion, chunk by chunk)

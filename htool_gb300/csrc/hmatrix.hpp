@@ -188,6 +188,7 @@ class HMatrix {
     // nonzero when a bounded device wait of a product ran out (1 producer,
     // 2 consumer, 3 drain); reading it synchronises the H-matrix's stream
     int device_status();
+    void reset_status(); // clears the status word (synchronises the handle's stream)
 
     // factor storage used by products: 0 FP64, 1 FP32, 2 FP32/BF16 per
     // column (BF16 where the column's bound is below tau * eps of the leaf),

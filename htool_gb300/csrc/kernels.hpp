@@ -47,6 +47,11 @@ void launch_aca_step_init(const AcaBlock *blocks, int nblocks, const double *xt,
 void launch_aca_step(const AcaBlock *blocks, const int *active, const long long *stage_off, int nactive, const double *stage, double eps, double *scratch, unsigned char *flags, AcaStep *state,
                      cudaStream_t st);
 
+// test support: the limit of every bounded wait of the product kernels (SM
+// clock cycles) and a chunk of the producer-fed phase 2 whose copies are
+// left out (-1 none), on the current device
+void set_debug_waits(long long cycles, long long skip_chunk);
+
 struct PackItem {
     long long src_u, src_v, dst_u, dst_v;
     int M, N, r, pad;

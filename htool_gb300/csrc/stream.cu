@@ -37,7 +37,12 @@ constexpr int kWarps     = kStreamWarpsPerCta;
 constexpr int kStages    = 3;  // per warp
 constexpr int kDataBuf   = kStreamStage + 32;
 constexpr int kIdxBuf    = kStreamCols * 4 + 32;
-constexpr long long kWaitCycles = 4000000000ll;
+// Limit of every bounded wait, in SM clock cycles (about 2 s by default),
+// and a chunk whose bulk copies the producer-fed phase 2 leaves out (-1:
+// none): the two knobs with which a test makes a wait run out on purpose
+// (htgpu_debug_set_waits).  Read once per kernel or on a wait's slow path.
+__device__ long long g_wait_cycles = 4000000000ll;
+__device__ long long g_skip_chunk  = -1;
 
 // floor(t / d) for 0 <= t < 128 and 1 <= d <= 32 as (t * r_d) >> 16 with
 // r_d = floor(65536 / d) + 1: the product overshoots t / d by less than
@@ -86,7 +91,7 @@ __device__ __forceinline__ bool warp_wait(unsigned long long *b, unsigned parity
             ok = mbar_sleep(b, parity, 20000);
             if (__all_sync(0xffffffffu, ok))
                 break;
-            if (__any_sync(0xffffffffu, clock64() - t0 > kWaitCycles))
+            if (__any_sync(0xffffffffu, clock64() - t0 > g_wait_cycles))
                 return false;
         }
     }
@@ -515,9 +520,9 @@ constexpr unsigned char kStreamStop = 0xFF; // descriptor kind: no more chunks
 __device__ __forceinline__ bool lane_wait(unsigned long long *b, unsigned parity) {
     if (mbar_sleep(b, parity, 20000))
         return true;
-    const long long t0 = clock64();
+    const long long t0 = clock64(), limit = g_wait_cycles;
     while (!mbar_sleep(b, parity, 20000))
-        if (clock64() - t0 > kWaitCycles)
+        if (clock64() - t0 > limit)
             return false;
     return true;
 }
@@ -566,6 +571,8 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
             return true;
         };
         more                           = claim_unit();
+        const long long wait_limit     = g_wait_cycles;
+        const long long skip           = g_skip_chunk;
         const unsigned long long pol   = evict_first_policy();
         long long idle0                = clock64();
         bool timed_out                 = false;
@@ -603,9 +610,11 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
                         const unsigned char *base = (dn.flags & kStreamPre) ? arena2 : (dn.flags & kStreamArena1) ? arena1 : arena0;
                         const long long a0 = dn.src & ~15LL, a1 = (dn.src + dn.bytes + 15) & ~15LL;
                         const long long i0 = (4LL * dn.a) & ~15LL, i1 = (4LL * (dn.a + dn.ncol) + 15) & ~15LL;
-                        mbar_arrive_tx(fullb(lane, s), (unsigned)(a1 - a0 + i1 - i0));
-                        bulk_load_stream(ring(lane) + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), fullb(lane, s), pol);
-                        bulk_load_stream(ring(lane) + L::kIdx + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), fullb(lane, s), pol);
+                        if (k != skip) { // a skipped chunk's stage never fills: its consumer's wait runs out
+                            mbar_arrive_tx(fullb(lane, s), (unsigned)(a1 - a0 + i1 - i0));
+                            bulk_load_stream(ring(lane) + (size_t)s * kDataBuf, base + a0, (unsigned)(a1 - a0), fullb(lane, s), pol);
+                            bulk_load_stream(ring(lane) + L::kIdx + (size_t)s * kIdxBuf, reinterpret_cast<const unsigned char *>(cidx) + i0, (unsigned)(i1 - i0), fullb(lane, s), pol);
+                        }
                         if (++k < e)
                             dn = chunks[k];
                     }
@@ -615,7 +624,7 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
             if (__any_sync(0xffffffffu, ready))
                 idle0 = clock64();
             else {
-                if (__any_sync(0xffffffffu, clock64() - idle0 > kWaitCycles)) { // no consumer released a stage for ~2 s
+                if (__any_sync(0xffffffffu, clock64() - idle0 > wait_limit)) { // no consumer released a stage for ~2 s
                     timed_out = true;
                     break;
                 }
@@ -1259,9 +1268,9 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
                     // every consumer is done with the stage's previous fill
                     const unsigned par = ((i / kP1Ring) - 1) & 1;
                     if (!mbar_sleep(&empt[s], par, 20000)) {
-                        const long long t0 = clock64();
+                        const long long t0 = clock64(), limit = g_wait_cycles;
                         while (!mbar_sleep(&empt[s], par, 20000))
-                            if (clock64() - t0 > kWaitCycles) {
+                            if (clock64() - t0 > limit) {
                                 okl = false;
                                 break;
                             }
@@ -1292,9 +1301,9 @@ __global__ void __launch_bounds__(32 * (p1_cons<KM>() + 1), 1)
             for (int i = max(0, issued - kP1Ring); i < issued; i++) {
                 const unsigned par = (i / kP1Ring) & 1;
                 if (!mbar_sleep(&full[i % kP1Ring], par, 20000)) {
-                    const long long t0 = clock64();
+                    const long long t0 = clock64(), limit = g_wait_cycles;
                     while (!mbar_sleep(&full[i % kP1Ring], par, 20000))
-                        if (clock64() - t0 > kWaitCycles) {
+                        if (clock64() - t0 > limit) {
                             atomicExch(status, 3);
                             break;
                         }
@@ -1676,6 +1685,12 @@ int stream2_units_target() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return 4 * (sms > 0 ? sms : 152) * 6; // ~6 units per CTA: balance through the ticket
+}
+
+void set_debug_waits(long long cycles, long long skip_chunk) {
+    HTGPU_CUDA(cudaMemcpyToSymbol(g_wait_cycles, &cycles, sizeof(cycles)));
+    HTGPU_CUDA(cudaMemcpyToSymbol(g_skip_chunk, &skip_chunk, sizeof(skip_chunk)));
+    HTGPU_CUDA(cudaDeviceSynchronize());
 }
 
 } // namespace htgpu

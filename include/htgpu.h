@@ -301,6 +301,18 @@ int htgpu_hmatrix_get_phase2_mode(htgpu_hmatrix h, int *mode);
  * valid).  Synchronises the H-matrix's stream.  Host-pointer products check
  * it themselves and fail.  No counterpart in the reference. */
 int htgpu_hmatrix_device_status(htgpu_hmatrix h, int *status);
+/* Clears the status word (after a reported expiry), synchronising the
+ * H-matrix's stream.  No counterpart in the reference. */
+int htgpu_hmatrix_reset_status(htgpu_hmatrix h);
+
+/* Test support, no counterpart in the reference: on CUDA device `device`,
+ * the limit of every bounded wait of the product kernels in SM clock cycles
+ * (default 4e9, about 2 s) and the index of one chunk of the producer-fed
+ * phase 2 (HTGPU_PHASE2_PRODUCER) whose bulk copies are left out, so that
+ * its consumer's wait runs out (-1, the default: none).  Lets a test see
+ * the kernels give up, report status 2 / 3 and return; restore the
+ * defaults afterwards. */
+int htgpu_debug_set_waits(int device, long long cycles, long long skip_chunk);
 
 /* Autotuner: times `reps` products with mu right-hand sides on this
  * H-matrix and keeps the fastest configuration for the current storage
