@@ -66,7 +66,8 @@ def parse():
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-predictor", action="store_true", help="skip the rank-predictor rebuild")
-    p.add_argument("--workload", default="sphere", choices=["sphere", "batched"], help="sphere: the one-H-matrix product; batched: 256 H-matrices in one graph launch")
+    p.add_argument("--workload", default="sphere", choices=["sphere", "batched", "helmholtz"],
+                   help="sphere: the one-H-matrix product; batched: 256 H-matrices in one graph launch; helmholtz: the complex cube with 64 right-hand sides")
     p.add_argument("--count", type=int, default=256, help="batched: number of H-matrices")
     # fixed configuration instead of the autotuner (e.g. to replay a tuned run under a profiler)
     p.add_argument("--fp64-split", default=None, help="phase-1,phase-2 DFMA per mille, e.g. 0,650")
@@ -534,6 +535,78 @@ def run_batched(args):
         print(json.dumps(line), flush=True)
 
 
+def run_helmholtz(args):
+    """Complex Helmholtz exp(ikr)/(4 pi r), k = 20, on N = 200 000 points of
+    the unit-cube surface (seeded), eta = 3, epsilon = 1e-5: products with 64
+    complex N(0,1) + i N(0,1) right-hand sides, FP64 (double-float kernels)
+    and mixed precision (both low-rank contractions on the tensor cores,
+    tcgen05 and the warp-level mma.sync kernels), errors against FP64."""
+    import torch
+
+    import htool_gb300 as H
+    from htool_gb300 import geometry as G
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    n = args.n if args.n != WORKLOAD["n"] else 200000
+    mu = 64
+    pts = G.cube_surface(n, seed=1)
+    t = H.Cluster().build(n, pts)
+    t0 = time.perf_counter()
+    hm = H.HMatrix(t, t, 1e-5, 3.0, device=local, dtype=np.complex128).build(H.HELMHOLTZ, pts, kernel_param=20.0)
+    build_s = time.perf_counter() - t0
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(n * mu) + 1j * rng.standard_normal(n * mu)
+    xd = torch.from_numpy(x.view(np.float64).copy()).cuda()
+    yd = torch.empty_like(xd)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def timed(steps):
+        for _ in range(max(args.warmup, 3)):
+            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), mu, 0, stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), mu, 0, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, yd.cpu().numpy().copy()
+
+    steps = max(1, min(args.steps, 20))
+    clocks = Clocks(local)
+    clocks.start()
+    ms64, y64 = timed(steps)
+    ph64 = hm.profile(mu, 3)
+    hm.set_precision("mixed", 1.0)
+    hm.set_tensor_core_mode("tcgen05")
+    ms_tc, y_tc = timed(steps)
+    ph_tc = hm.profile(mu, 3)
+    hm.set_tensor_core_mode("mma.sync")
+    ms_mma, y_mma = timed(steps)
+    ph_mma = hm.profile(mu, 3)
+    hm.set_tensor_core_mode("tcgen05")
+    ck = clocks.stop()
+    status = hm.device_status()
+    info = hm.get_infos()
+    err = lambda y: float(np.linalg.norm(y - y64) / np.linalg.norm(y64))
+    phases = lambda ph: {"gather": ph[0], "phase1": ph[1], "phase2": ph[2], "sums": ph[3], "total": ph[4]}
+    line = {
+        "metric": "complex H-matmat with 64 right-hand sides per second (H-matvec/s = 64 / time)", "value": world * mu / (ms_tc * 1e-3), "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_tc, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32/bf16 factors (per-column scaled), TF32x3 tensor-core contractions with FP32 accumulation, fp64 dense", "data": "synthetic (seeded points on the unit-cube surface)",
+        "config": {"workload": "helmholtz_cube", "n": n, "wavenumber": 20.0, "eta": 3.0, "epsilon": 1e-5, "mu": mu, "l2": "inputs larger than L2 (the stored H-matrix, tens of GB)"},
+        "mixed_tcgen05": {"ms": ms_tc, "rel_err_vs_fp64": err(y_tc), "phase_ms": phases(ph_tc)},
+        "mixed_mma_sync": {"ms": ms_mma, "rel_err_vs_fp64": err(y_mma), "phase_ms": phases(ph_mma)},
+        "fp64": {"ms": ms64, "phase_ms": phases(ph64)},
+        "build_seconds": build_s, "clocks": ck, "device_status": status,
+        "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_mean", "Compression_ratio")},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batched":
@@ -541,6 +614,11 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no reference arm in this script; the sphere workload carries it"}), flush=True)
             return
         run_batched(args)
+    elif args.workload == "helmholtz":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the complex workload has no reference arm in this script; the sphere workload carries it"}), flush=True)
+            return
+        run_helmholtz(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

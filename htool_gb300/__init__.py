@@ -120,6 +120,9 @@ def _load():
         "htgpu_aca_factors": (i, [vp, vp, vp]),
         "htgpu_cluster_import": (i, [i, vp, i, vp, vp, vp]),
         "htgpu_hmatrix_reset_status": (i, [vp]),
+        "htgpu_hmatrix_set_tensor_core_mode": (i, [vp, i]),
+        "htgpu_hmatrix_get_tensor_core_mode": (i, [vp, vp]),
+        "htgpu_debug_tc_gemm": (i, [i, vp, vp, vp]),
         "htgpu_debug_set_waits": (i, [i, C.c_longlong, C.c_longlong]),
     }
     for name, (res, args) in sig.items():
@@ -543,6 +546,16 @@ class HMatrix:
         v = C.c_int()
         _check(lib.htgpu_hmatrix_device_status(self.h, C.byref(v)))
         return v.value
+
+    def set_tensor_core_mode(self, mode):
+        """"mma.sync" / 0 or "tcgen05" / 1 (the default)"""
+        m = {"mma.sync": 0, "tcgen05": 1}[mode] if isinstance(mode, str) else int(mode)
+        _check(lib.htgpu_hmatrix_set_tensor_core_mode(self.h, m))
+
+    def get_tensor_core_mode(self):
+        m = C.c_int()
+        _check(lib.htgpu_hmatrix_get_tensor_core_mode(self.h, C.byref(m)))
+        return m.value
 
     def reset_status(self):
         _check(lib.htgpu_hmatrix_reset_status(self.h))

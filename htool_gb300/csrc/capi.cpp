@@ -529,6 +529,44 @@ int htgpu_hmatrix_precision_info(htgpu_hmatrix h, int *policy, long long *stored
     });
 }
 
+int htgpu_hmatrix_set_tensor_core_mode(htgpu_hmatrix h, int mode) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_tensor_core_mode(mode);
+    });
+}
+
+int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(mode, "mode");
+        *mode = h->h->tensor_core_mode();
+    });
+}
+
+int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d) {
+    return guarded([&] {
+        need(a, "a");
+        need(b, "b");
+        need(d, "d");
+        HTGPU_CUDA(cudaSetDevice(device));
+        htgpu::DevBuf<float> da, db, dd;
+        htgpu::DevBuf<int> st;
+        da.upload(a, 128 * 32, nullptr);
+        db.upload(b, 32 * 64, nullptr);
+        dd.alloc(128 * 64);
+        st.alloc(1);
+        HTGPU_CUDA(cudaMemset(st.p, 0, sizeof(int)));
+        HTGPU_CUDA(cudaMemset(dd.p, 0, sizeof(float) * 128 * 64));
+        htgpu::tc_selftest(da.p, db.p, dd.p, st.p, nullptr);
+        HTGPU_CUDA(cudaDeviceSynchronize());
+        int status = 0;
+        HTGPU_CUDA(cudaMemcpy(&status, st.p, sizeof(int), cudaMemcpyDeviceToHost));
+        htgpu::require(status == 0, "a wait of the tensor-core self-test ran out", 3);
+        HTGPU_CUDA(cudaMemcpy(d, dd.p, sizeof(float) * 128 * 64, cudaMemcpyDeviceToHost));
+    });
+}
+
 int htgpu_hmatrix_reset_status(htgpu_hmatrix h) {
     return guarded([&] {
         need(h, "hmatrix");

@@ -1310,6 +1310,44 @@ void HMatrix::set_precision(int policy, double tau) {
     }
     p1m_d.upload(p1m, stream_);
     n_p1m_ = (int)p1m.size();
+    {
+        // tensor-core phase 1: the tiles on the same x rows (the same source
+        // cluster slab) stacked, cut into blocks of at most 128 columns
+        std::map<std::pair<int, int>, std::vector<int>> on_rows; // (first x row, rows) -> tiles
+        for (std::size_t i = 0; i < p1m.size(); i++)
+            if (lr_h[p1m[i].leaf].r > 0)
+                on_rows[{lr_h[p1m[i].leaf].oj + p1m[i].j0, p1m[i].jlen}].push_back((int)i);
+        std::vector<TcSeg> segs;
+        std::vector<TcBlock> blks;
+        for (auto &g : on_rows) {
+            TcBlock b{(int)segs.size(), (int)segs.size(), g.first.first, g.first.second};
+            int rows = 0;
+            for (int i : g.second) {
+                const P1Item &m = p1m[i];
+                const LrLeaf &L = lr_h[m.leaf];
+                for (int c0 = 0; c0 < L.r;) {
+                    if (rows == 128) {
+                        b.s1 = (int)segs.size();
+                        blks.push_back(b);
+                        b.s0 = b.s1;
+                        rows = 0;
+                    }
+                    const int nc = std::min(L.r - c0, 128 - rows);
+                    segs.push_back({m.off, L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r + c0, m.pad, c0, nc, (int)L.a_off + c0});
+                    rows += nc;
+                    c0 += nc;
+                }
+            }
+            b.s1 = (int)segs.size();
+            if (b.s1 > b.s0)
+                blks.push_back(b);
+        }
+        // longest first, so the CTAs' shares even out
+        std::stable_sort(blks.begin(), blks.end(), [](const TcBlock &a, const TcBlock &b) { return a.jlen > b.jlen; });
+        tcseg_d.upload(segs, stream_);
+        tcblk_d.upload(blks, stream_);
+        n_tcblk_ = (int)blks.size();
+    }
     ch2_h_ = std::move(ch2);
     upload_mixed_phase2();
     cim.resize(cim.size() + 4, 0); // bulk copies read whole 16-byte words
@@ -1349,7 +1387,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
         } else if (n_p1m_ && mma) {
-            launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scalef_d.p, w_xs, mu, w_A, st);
+            if (tc_mode_ == 1 && n_tcblk_ > 0)
+                launch_phase1_tc(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, reinterpret_cast<float *>(w_A), status_d.p, st);
+            else
+                launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scalef_d.p, w_xs, mu, w_A, st);
             launches_ += 1;
         } else if (n_p1m_) {
             launch_phase1_mixed(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scale_d.p, w_xs, w_xexp, mu, w_A, st);
@@ -1431,6 +1472,12 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
     }
     launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
     launches_ += 1;
+}
+
+void HMatrix::set_tensor_core_mode(int mode) {
+    layout_gen_++; // captured products are stale
+    require(mode == 0 || mode == 1, "tensor-core mode must be 0 (mma.sync) or 1 (tcgen05)");
+    tc_mode_ = mode;
 }
 
 void HMatrix::set_phase2_mode(int mode) {

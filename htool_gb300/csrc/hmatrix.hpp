@@ -169,6 +169,10 @@ class HMatrix {
     long long presplit_bytes() const { return (long long)(((emu_fresh_ ? emu_.n : 0) + emu2_.n + emu3_.n) * sizeof(F2)); }
     void set_phase2_mode(int mode);
     int phase2_mode() const { return p2_mode_; }
+    // tensor-core kernels of reduced-precision products with many
+    // right-hand sides: 0 warp-level mma.sync, 1 tcgen05 (default)
+    void set_tensor_core_mode(int mode);
+    int tensor_core_mode() const { return tc_mode_; }
     bool emulation_allowed() const { return emu_ok_; }
     // time every candidate split on the current H-matrix and keep the fastest
     // FP64: phase-1 mode and the DFMA/emulation split; reduced precision:
@@ -304,6 +308,11 @@ class HMatrix {
     // reduced precision, many right-hand sides: first chunk of every row
     // chunk (tensor-core phase 2, then its dense chunks) and the dense chunk count
     DevBuf<int> p2rcm_d, p2rc_d; // and of the FP64 list
+    // tensor-core phase 1 (tc.cu): stacked blocks and their column segments
+    DevBuf<TcSeg> tcseg_d;
+    DevBuf<TcBlock> tcblk_d;
+    int n_tcblk_ = 0;
+    int tc_mode_ = 1; // many-RHS reduced-precision contractions: 0 warp-level mma.sync, 1 tcgen05
     int n_p2rc_m_ = 0, n_p2rc_ = 0;
     long long n_chunks_md_ = 0;
     // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced

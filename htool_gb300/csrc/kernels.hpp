@@ -188,6 +188,21 @@ constexpr double kMmaMinEps = 1e-5;
 // many-right-hand-side kernels (mrhs.cu)
 constexpr int kDfMinRhs = 8;
 void launch_phase1_mma(const P1Item *items, int nitems, const LrLeaf *lr, const unsigned char *mix, const float *scale, const F2 *xs, int mu, double *A, cudaStream_t st);
+// the same on the 5th-generation tensor cores (tc.cu): the V-side
+// contractions of every leaf on one source cluster stacked into GEMMs of at
+// most 128 columns sharing their x rows
+struct TcSeg { // columns col0 .. col0 + ncol of one reduced-precision tile
+    long long off;  // byte offset of the tile in the reduced arena
+    long long slot; // phase-1 sum slot of column col0
+    int c32, col0, ncol, sidx; // FP32 columns of the tile; first column; count; scale slot of col0
+};
+struct TcBlock { // segments [s0, s1), at most 128 columns in all, on x rows xrow .. xrow + jlen
+    int s0, s1, xrow, jlen;
+};
+void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, int *status, cudaStream_t st);
+// one 128 x 32 by 32 x 64 product (row-major a, b, d on the device) through
+// the tensor-core path's staging, descriptors and read-out
+void tc_selftest(const float *a, const float *b, float *d, int *status, cudaStream_t st);
 // phase 2 of a reduced-precision product with mu >= kMmaMinRhs: the FP32 /
 // BF16 chunks of every row chunk (rc: first chunk of row chunk i, nrc + 1
 // entries) on the tensor cores; writes the row chunk's z rows (the dense

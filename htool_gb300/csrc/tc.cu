@@ -1,0 +1,367 @@
+// Phase 1 of reduced-precision products with many right-hand sides on the
+// 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// htool applies a low-rank leaf as U (V^T x) (lrmat/lrmat.hpp:89-100), for mu
+// right-hand sides a gemm with the row-major right-hand sides
+// (types/matrix.hpp:346, 380).  Every leaf whose source cluster is s reads
+// the same rows of x, so the V-side contractions of all those leaves are one
+// GEMM with a shared operand:
+//
+//     D (stacked columns k of every leaf on s, x 64 right-hand sides)
+//       = [V_1 ... V_p]^T (stacked, x |s|)  *  X_s (|s| x 64)
+//
+// The host cuts these stacks into blocks of at most 128 columns (TcBlock,
+// TcSeg).  A CTA takes blocks in turn: its four warps stage 32 source rows of
+// the block's FP32 / BF16 columns and of x into shared memory -- each value
+// split once into TF32 hi and lo parts, written in the tensor cores'
+// canonical K-major layout -- while the previous slab is multiplied; one
+// thread issues tcgen05.mma (M = 128, N = 64, K = 8, kind::tf32: hi*hi +
+// hi*lo + lo*hi per step, FP32 accumulation in tensor memory) and commits
+// each slab to an mbarrier that frees its buffer; at the end of a block the
+// warps read the accumulator rows out of tensor memory (tcgen05.ld), scale
+// them by the columns' factors and write the phase-1 sums.
+//
+// Shared-memory operands use no swizzle: core matrices of 8 rows x 16 bytes,
+// 128 contiguous bytes each; the next 4 K-values of a row are the next core
+// matrix (leading byte offset 128), the next 8 rows are 8 core matrices
+// further (stride byte offset 1024 for a 32-deep slab).
+//
+// Every mbarrier wait is bounded; a wait that runs out records status 4 and
+// the CTA stops after freeing its tensor memory.
+#include "kernels.hpp"
+
+namespace htgpu {
+
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kTcK       = 32; // source rows (K) per staged slab
+constexpr int kTcM       = 128;
+constexpr int kTcN       = 64;
+constexpr int kTcLbo     = 128;                   // bytes between core matrices along K
+constexpr int kTcSbo     = (kTcK / 4) * 128;      // bytes between 8-row groups
+constexpr int kTcABytes  = kTcM * kTcK * 4;       // 16 KB: one TF32 part of A
+constexpr int kTcBBytes  = kTcN * kTcK * 4;       // 8 KB: one TF32 part of B
+constexpr int kTcBuf     = 2 * kTcABytes + 2 * kTcBBytes; // A hi, A lo, B hi, B lo
+constexpr int kTcSmem    = 2 * kTcBuf + 128;       // two buffers, barriers, tensor-memory slot
+constexpr unsigned kTcCols = 64;                   // tensor-memory columns: the 64 FP32 accumulators of a row
+constexpr long long kTcWait = 2000000000ll;        // about 1 s of SM clocks
+
+// instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator (bits
+// 4-5 = 1), A and B TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 =
+// 0), N / 8 at bits 17-22, M / 16 at bits 24-28
+constexpr unsigned kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kTcN >> 3) << 17) | ((unsigned)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// byte offset of element (row, k) of a slab in the canonical layout
+__device__ __forceinline__ int tc_off(int row, int k) { return (row >> 3) * kTcSbo + (k >> 2) * kTcLbo + (row & 7) * 16 + (k & 3) * 4; }
+
+// shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (all in 16-byte units), descriptor version 1, no swizzle
+__device__ __forceinline__ unsigned long long tc_desc(unsigned addr) {
+    unsigned long long d = (unsigned long long)((addr >> 4) & 0x3FFFu);
+    d |= (unsigned long long)((kTcLbo >> 4) & 0x3FFF) << 16;
+    d |= (unsigned long long)((kTcSbo >> 4) & 0x3FFF) << 32;
+    d |= 1ull << 46;
+    return d;
+}
+
+__device__ __forceinline__ void tc_mma(unsigned tmem_d, unsigned long long a, unsigned long long b, int accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d), "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate)
+                 : "memory");
+}
+
+// the mbarrier completes once every tcgen05 operation this thread issued so far has
+__device__ __forceinline__ void tc_commit(unsigned long long *bar) { asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+// shared-memory writes of this thread become visible to the tensor cores
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bar_init(unsigned long long *b) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory"); }
+
+// bounded wait for the completion of the phase of parity `parity`
+__device__ __forceinline__ bool bar_wait(unsigned long long *b, unsigned parity) {
+    const long long t0 = clock64();
+    while (true) {
+        unsigned ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_u32(b)), "r"(parity), "r"(20000u) : "memory");
+        if (ok)
+            return true;
+        if (clock64() - t0 > kTcWait)
+            return false;
+    }
+}
+
+// warp-wide tensor-memory allocation; the address lands in *slot
+__device__ __forceinline__ void tmem_alloc(unsigned *slot) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(kTcCols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(unsigned taddr) { asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTcCols) : "memory"); }
+
+// 16 consecutive FP32 columns of this thread's tensor-memory lane (lane =
+// 32 * warp + lane id), waited for
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_hi(float v) {
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+// four consecutive K-values of one row, split into TF32 hi and lo parts,
+// stored as one 16-byte word of each part
+__device__ __forceinline__ void put4(unsigned char *hi, unsigned char *lo, int row, int k, float a, float b, float c, float d) {
+    const float ha = tf32_hi(a), hb = tf32_hi(b), hc = tf32_hi(c), hd = tf32_hi(d);
+    *reinterpret_cast<float4 *>(hi + tc_off(row, k)) = make_float4(ha, hb, hc, hd);
+    *reinterpret_cast<float4 *>(lo + tc_off(row, k)) = make_float4(tf32_hi(a - ha), tf32_hi(b - hb), tf32_hi(c - hc), tf32_hi(d - hd));
+}
+
+__device__ __forceinline__ float bf16f(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
+
+// the three TF32 products of one slab (K = 32: four K-steps of 8)
+__device__ __forceinline__ void tc_slab(unsigned tmem, const unsigned char *buf, bool first) {
+    const unsigned a_hi = smem_u32(buf), a_lo = a_hi + kTcABytes, b_hi = a_lo + kTcABytes, b_lo = b_hi + kTcBBytes;
+#pragma unroll
+    for (int kk = 0; kk < kTcK / 8; kk++) {
+        const unsigned adv = kk * 2 * kTcLbo; // 8 K-values = two core matrices
+        tc_mma(tmem, tc_desc(a_hi + adv), tc_desc(b_hi + adv), !(first && kk == 0));
+        tc_mma(tmem, tc_desc(a_hi + adv), tc_desc(b_lo + adv), 1);
+        tc_mma(tmem, tc_desc(a_lo + adv), tc_desc(b_hi + adv), 1);
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 2) phase1_tc_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
+                                                                 const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, float *__restrict__ A, int *__restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf);
+    unsigned *tslot          = reinterpret_cast<unsigned *>(smem + 2 * kTcBuf + 64);
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        bar_init(&bars[0]);
+        bar_init(&bars[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+    int slabs  = 0; // slabs issued by this CTA: buffer slabs & 1, its (slabs >> 1)-th use
+    bool fail  = false;
+    for (int bi = blockIdx.x; bi < nblocks && !fail; bi += gridDim.x) {
+        const TcBlock B = blocks[bi];
+        // this thread's row of the stack: segment, column, FP32 or BF16
+        int m0 = 0, sg = -1;
+        for (int s = B.s0; s < B.s1; s++) {
+            const int nc = segs[s].ncol;
+            if (tid < m0 + nc) {
+                sg = s;
+                break;
+            }
+            m0 += nc;
+        }
+        const float *col32          = nullptr;
+        const unsigned short *col16 = nullptr;
+        long long out               = 0;
+        float sc                    = 0.f;
+        if (sg >= 0) {
+            const TcSeg S = segs[sg];
+            const int col = S.col0 + tid - m0;
+            const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
+            if (col < S.c32)
+                col32 = reinterpret_cast<const float *>(mix + S.off) + (long long)l32 * col;
+            else
+                col16 = reinterpret_cast<const unsigned short *>(mix + S.off + 4LL * l32 * S.c32) + (long long)l16 * (col - S.c32);
+            out = (S.slot + (long long)(tid - m0)) * mu;
+            sc  = scale[S.sidx + tid - m0];
+        }
+        const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
+        const F2 *X   = xs + (long long)B.xrow * mu;
+        for (int cb = 0; cb < mu && !fail; cb += kTcN) {
+            for (int ks = 0; ks < B.jlen; ks += kTcK) {
+                const int buf = slabs & 1, use = slabs >> 1;
+                unsigned char *bb = smem + (size_t)buf * kTcBuf;
+                if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1)) // the MMAs of two slabs ago read this buffer
+                    fail = true;
+                if (__syncthreads_or(fail)) {
+                    fail = true;
+                    break;
+                }
+                // A: row tid = one column of the stack, 32 source rows
+                unsigned char *ahi = bb, *alo = bb + kTcABytes;
+#pragma unroll
+                for (int k4 = 0; k4 < kTcK / 4; k4++) {
+                    const int j = ks + 4 * k4;
+                    float4 v    = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (col32 && j < l32)
+                        v = __ldg(reinterpret_cast<const float4 *>(col32 + j));
+                    else if (col16 && j < l16) {
+                        const uint2 w = __ldg(reinterpret_cast<const uint2 *>(col16 + j));
+                        v             = make_float4(bf16f((unsigned short)(w.x & 0xFFFFu)), bf16f((unsigned short)(w.x >> 16)), bf16f((unsigned short)(w.y & 0xFFFFu)), bf16f((unsigned short)(w.y >> 16)));
+                    }
+                    put4(ahi, alo, tid, 4 * k4, v.x, v.y, v.z, v.w);
+                }
+                // B: x rows ks .. ks + 32 of right-hand sides cb .. cb + 64,
+                // row n = right-hand side, 16 source rows per thread
+                {
+                    unsigned char *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
+                    const int n = tid & 63, k0 = (tid >> 6) * 16;
+                    const bool on = cb + n < mu;
+                    float v[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int j = ks + k0 + q;
+                        v[q]        = (on && j < B.jlen) ? X[(long long)j * mu + cb + n].hi : 0.f;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 16; q += 4)
+                        put4(bhi, blo, n, k0 + q, v[q], v[q + 1], v[q + 2], v[q + 3]);
+                }
+                proxy_fence();
+                __syncthreads();
+                if (tid == 0) {
+                    tc_fence_after();
+                    tc_slab(tmem, bb, ks == 0);
+                    tc_commit(&bars[buf]);
+                }
+                slabs++;
+            }
+            if (fail)
+                break;
+            // the block's sums: all its slabs' products are complete
+            const int last = slabs - 1;
+            if (!bar_wait(&bars[last & 1], (last >> 1) & 1))
+                fail = true;
+            if (__syncthreads_or(fail)) {
+                fail = true;
+                break;
+            }
+            tc_fence_after();
+#pragma unroll
+            for (int c16 = 0; c16 < kTcN / 16; c16++) {
+                float v[16];
+                tmem_ld16(tmem + ((unsigned)(32 * wid) << 16) + 16 * c16, v);
+                if (sg >= 0)
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int c = cb + 16 * c16 + q;
+                        if (c < mu)
+                            A[out + c] = v[q] * sc;
+                    }
+            }
+            tc_fence_before();
+            __syncthreads(); // the accumulator is read out before the next block overwrites it
+        }
+    }
+    if (fail && lane == 0)
+        atomicExch(status, 4);
+    // every issued product has completed (or a wait ran out) before the
+    // tensor memory is given back
+    if (!fail && slabs > 0 && tid == 0)
+        bar_wait(&bars[(slabs - 1) & 1], ((slabs - 1) >> 1) & 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (wid == 0)
+        tmem_free(tmem);
+}
+
+// One 128 x 32 by 32 x 64 product through the same staging, descriptors,
+// instructions and read-out: the check of the tensor-core path on its own
+__global__ void __launch_bounds__(kTcThreads) tc_selftest_kernel(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ d, int *__restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf);
+    unsigned *tslot          = reinterpret_cast<unsigned *>(smem + 2 * kTcBuf + 64);
+    const int tid = threadIdx.x, wid = tid >> 5;
+    if (tid == 0) {
+        bar_init(&bars[0]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+    unsigned char *ahi = smem, *alo = smem + kTcABytes, *bhi = smem + 2 * kTcABytes, *blo = bhi + kTcBBytes;
+    for (int k = 0; k < kTcK; k += 4)
+        put4(ahi, alo, tid, k, a[tid * kTcK + k], a[tid * kTcK + k + 1], a[tid * kTcK + k + 2], a[tid * kTcK + k + 3]);
+    {
+        const int n = tid & 63, k0 = (tid >> 6) * 16;
+        for (int q = 0; q < 16; q += 4)
+            put4(bhi, blo, n, k0 + q, b[(k0 + q) * kTcN + n], b[(k0 + q + 1) * kTcN + n], b[(k0 + q + 2) * kTcN + n], b[(k0 + q + 3) * kTcN + n]);
+    }
+    proxy_fence();
+    __syncthreads();
+    if (tid == 0) {
+        tc_fence_after();
+        tc_slab(tmem, smem, true);
+        tc_commit(&bars[0]);
+    }
+    const bool ok = bar_wait(&bars[0], 0);
+    const bool fail = __syncthreads_or(!ok);
+    if (!fail) {
+        tc_fence_after();
+        for (int c16 = 0; c16 < kTcN / 16; c16++) {
+            float v[16];
+            tmem_ld16(tmem + ((unsigned)(32 * wid) << 16) + 16 * c16, v);
+            for (int q = 0; q < 16; q++)
+                d[tid * kTcN + 16 * c16 + q] = v[q];
+        }
+    } else if (tid == 0)
+        atomicExch(status, 4);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (wid == 0)
+        tmem_free(tmem);
+}
+
+void tc_smem_limit(const void *fn) {
+    static unsigned long long done[2] = {0, 0}; // devices whose limit was raised, per kernel
+    const int which = fn == (const void *)phase1_tc_kernel ? 0 : 1;
+    int dev         = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done[which] >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+        if (dev < 64)
+            done[which] |= 1ull << dev;
+    }
+}
+
+} // namespace
+
+void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, int *status, cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    tc_smem_limit((const void *)phase1_tc_kernel);
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = std::min(nblocks, 2 * sms); // two CTAs an SM (96 KB of shared memory, 64 tensor-memory columns each)
+    phase1_tc_kernel<<<grid, kTcThreads, kTcSmem, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void tc_selftest(const float *a, const float *b, float *d, int *status, cudaStream_t st) {
+    tc_smem_limit((const void *)tc_selftest_kernel);
+    tc_selftest_kernel<<<1, kTcThreads, kTcSmem, st>>>(a, b, d, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+} // namespace htgpu

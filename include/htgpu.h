@@ -296,9 +296,27 @@ int htgpu_hmatrix_get_presplit(htgpu_hmatrix h, int *on, long long *bytes);
 int htgpu_hmatrix_set_phase2_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_phase2_mode(htgpu_hmatrix h, int *mode);
 
+/* Tensor-core kernels of reduced-precision products with at least 8
+ * right-hand sides on H-matrices with epsilon >= 1e-5: HTGPU_TC_MMA_SYNC
+ * (warp-level mma.sync TF32, one warp per tile or row chunk) or
+ * HTGPU_TC_TCGEN05 (the default: tcgen05.mma with tensor-memory
+ * accumulators; phase 1 stacks the tiles that share their x rows into GEMMs
+ * of up to 128 columns).  No counterpart in the reference. */
+#define HTGPU_TC_MMA_SYNC 0
+#define HTGPU_TC_TCGEN05 1
+int htgpu_hmatrix_set_tensor_core_mode(htgpu_hmatrix h, int mode);
+int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode);
+
+/* Test support, no counterpart in the reference: d (128 x 64) = a (128 x
+ * 32) b (32 x 64), row-major host arrays, computed on CUDA device `device`
+ * by the tcgen05 path of the tensor-core kernels (the same shared-memory
+ * layout, descriptors, three-term TF32 products and tensor-memory read-out),
+ * so that path can be checked on its own. */
+int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d);
+
 /* Status word of the product kernels' bounded waits: 0, or 1/2/3 when a
- * wait for a pipeline stage ran out (the product's result is then not
- * valid).  Synchronises the H-matrix's stream.  Host-pointer products check
+ * wait for a pipeline stage ran out, 4 when a wait of the tensor-core
+ * kernels did (the product's result is then not valid).  Synchronises the H-matrix's stream.  Host-pointer products check
  * it themselves and fail.  No counterpart in the reference. */
 int htgpu_hmatrix_device_status(htgpu_hmatrix h, int *status);
 /* Clears the status word (after a reported expiry), synchronising the
