@@ -419,7 +419,11 @@ def run_gpu(args):
                   "gpu_launches": launchesm * args.steps},
         "gpu_launches": launches64 * args.steps, "clocks": clk, "device_status": status,
         "rel_err_vs_dense_1000_rows": dense_err,
-        "aca_seconds": aca_seconds, "rank_predictor": predictor,
+        "aca_seconds": aca_seconds,
+        "assembly_breakdown_s": {"block_tree": float(info["GPU_block_tree_seconds"]), "aca_rounds": float(info["GPU_aca_seconds"]),
+                                 "layout_and_uploads": float(info["GPU_build_seconds"]) - float(info["GPU_aca_seconds"]) - float(info["GPU_block_tree_seconds"]),
+                                 "aca_blocks": int(info["GPU_aca_blocks"]), "aca_rounds_launched": int(float(info["GPU_aca_rounds"]))},
+        "rank_predictor": predictor,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},
     }
     if not args.no_cpu_baseline:

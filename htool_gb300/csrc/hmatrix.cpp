@@ -1403,7 +1403,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
         if (mma && n_p2rc_m_ > 0) { // low-rank part on the tensor cores, then the dense chunks added
-            launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
+            if (tc_mode_ == 1)
+                launch_phase2_tc(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, reinterpret_cast<const float *>(w_A), w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            else
+                launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
             launches_ += 1;
             if (n_chunks_md_ > 0) {
                 launch_phase2_df_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xs, w_xexp, mu,
@@ -1886,6 +1889,7 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["GPU_aca_blocks"]           = inum(st_.aca_blocks);
     m["GPU_aca_overflow_reruns"]  = num(st_.overflow_reruns);
     m["GPU_aca_seconds"]          = num(st_.aca_seconds);
+    m["GPU_block_tree_seconds"]   = num(st_.block_tree_seconds);
     m["GPU_build_seconds"]        = num(st_.build_seconds);
     m["GPU_stored_bytes"]         = inum(stored_bytes());
     m["GPU_phase1_items"]         = inum((long long)p1_h.size());

@@ -28,6 +28,7 @@
 //
 // Every mbarrier wait is bounded; a wait that runs out records status 4 and
 // the CTA stops after freeing its tensor memory.
+#include "df64.cuh"
 #include "kernels.hpp"
 
 namespace htgpu {
@@ -144,12 +145,25 @@ __device__ __forceinline__ void tc_slab(unsigned tmem, const unsigned char *buf,
     }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 2) phase1_tc_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
-                                                                 const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, float *__restrict__ A, int *__restrict__ status) {
+// Eight warps: thread t stages half a row of A (16 K-values of column
+// t mod 128) and 8 x values of B; the global loads of a block's next slab
+// are issued into registers right after the current slab is stored, so
+// they are in flight while the tensor cores work and the CTA syncs.
+constexpr int kTc1Threads = 256;
+
+struct P1Regs {
+    float4 a[4]; // 16 K-values of this thread's row of A
+    float b[8];  // 8 K-values of this thread's right-hand side of B
+};
+
+__global__ void __launch_bounds__(kTc1Threads, 2) phase1_tc_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
+                                                                   const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, float *__restrict__ A, int *__restrict__ status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf);
     unsigned *tslot          = reinterpret_cast<unsigned *>(smem + 2 * kTcBuf + 64);
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const int row = tid & 127, kh = (tid >> 7) * 16; // A: row and first K-value of this thread
+    const int bn = tid & 63, bk = (tid >> 6) * 8;     // B: right-hand side and first K-value
     if (tid == 0) {
         bar_init(&bars[0]);
         bar_init(&bars[1]);
@@ -161,77 +175,71 @@ __global__ void __launch_bounds__(kTcThreads, 2) phase1_tc_kernel(const TcBlock 
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = *tslot;
-    int slabs  = 0; // slabs issued by this CTA: buffer slabs & 1, its (slabs >> 1)-th use
-    bool fail  = false;
+    int slabs = 0; // slabs issued by this CTA: buffer slabs & 1, its (slabs >> 1)-th use
+    bool fail = false;
     for (int bi = blockIdx.x; bi < nblocks && !fail; bi += gridDim.x) {
         const TcBlock B = blocks[bi];
         // this thread's row of the stack: segment, column, FP32 or BF16
         int m0 = 0, sg = -1;
         for (int s = B.s0; s < B.s1; s++) {
             const int nc = segs[s].ncol;
-            if (tid < m0 + nc) {
+            if (row < m0 + nc) {
                 sg = s;
                 break;
             }
             m0 += nc;
         }
+        const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
         const float *col32          = nullptr;
         const unsigned short *col16 = nullptr;
-        long long out               = 0;
-        float sc                    = 0.f;
         if (sg >= 0) {
             const TcSeg S = segs[sg];
-            const int col = S.col0 + tid - m0;
-            const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
+            const int col = S.col0 + row - m0;
             if (col < S.c32)
                 col32 = reinterpret_cast<const float *>(mix + S.off) + (long long)l32 * col;
             else
                 col16 = reinterpret_cast<const unsigned short *>(mix + S.off + 4LL * l32 * S.c32) + (long long)l16 * (col - S.c32);
-            out = (S.slot + (long long)(tid - m0)) * mu;
-            sc  = scale[S.sidx + tid - m0];
         }
-        const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
-        const F2 *X   = xs + (long long)B.xrow * mu;
+        const F2 *X = xs + (long long)B.xrow * mu;
+        auto load = [&](int ks, int cb, P1Regs &r) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int j = ks + kh + 4 * q;
+                r.a[q]      = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (col32 && j < l32)
+                    r.a[q] = __ldg(reinterpret_cast<const float4 *>(col32 + j));
+                else if (col16 && j < l16) {
+                    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(col16 + j));
+                    r.a[q]        = make_float4(bf16f((unsigned short)(w.x & 0xFFFFu)), bf16f((unsigned short)(w.x >> 16)), bf16f((unsigned short)(w.y & 0xFFFFu)), bf16f((unsigned short)(w.y >> 16)));
+                }
+            }
+            const bool on = cb + bn < mu;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int j = ks + bk + q;
+                r.b[q]      = (on && j < B.jlen) ? X[(long long)j * mu + cb + bn].hi : 0.f;
+            }
+        };
         for (int cb = 0; cb < mu && !fail; cb += kTcN) {
+            P1Regs r;
+            load(0, cb, r);
             for (int ks = 0; ks < B.jlen; ks += kTcK) {
                 const int buf = slabs & 1, use = slabs >> 1;
                 unsigned char *bb = smem + (size_t)buf * kTcBuf;
-                if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1)) // the MMAs of two slabs ago read this buffer
+                if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1)) // the products of two slabs ago read this buffer
                     fail = true;
                 if (__syncthreads_or(fail)) {
                     fail = true;
                     break;
                 }
-                // A: row tid = one column of the stack, 32 source rows
-                unsigned char *ahi = bb, *alo = bb + kTcABytes;
+                unsigned char *ahi = bb, *alo = bb + kTcABytes, *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
 #pragma unroll
-                for (int k4 = 0; k4 < kTcK / 4; k4++) {
-                    const int j = ks + 4 * k4;
-                    float4 v    = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (col32 && j < l32)
-                        v = __ldg(reinterpret_cast<const float4 *>(col32 + j));
-                    else if (col16 && j < l16) {
-                        const uint2 w = __ldg(reinterpret_cast<const uint2 *>(col16 + j));
-                        v             = make_float4(bf16f((unsigned short)(w.x & 0xFFFFu)), bf16f((unsigned short)(w.x >> 16)), bf16f((unsigned short)(w.y & 0xFFFFu)), bf16f((unsigned short)(w.y >> 16)));
-                    }
-                    put4(ahi, alo, tid, 4 * k4, v.x, v.y, v.z, v.w);
-                }
-                // B: x rows ks .. ks + 32 of right-hand sides cb .. cb + 64,
-                // row n = right-hand side, 16 source rows per thread
-                {
-                    unsigned char *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
-                    const int n = tid & 63, k0 = (tid >> 6) * 16;
-                    const bool on = cb + n < mu;
-                    float v[16];
-#pragma unroll
-                    for (int q = 0; q < 16; q++) {
-                        const int j = ks + k0 + q;
-                        v[q]        = (on && j < B.jlen) ? X[(long long)j * mu + cb + n].hi : 0.f;
-                    }
-#pragma unroll
-                    for (int q = 0; q < 16; q += 4)
-                        put4(bhi, blo, n, k0 + q, v[q], v[q + 1], v[q + 2], v[q + 3]);
-                }
+                for (int q = 0; q < 4; q++)
+                    put4(ahi, alo, row, kh + 4 * q, r.a[q].x, r.a[q].y, r.a[q].z, r.a[q].w);
+                put4(bhi, blo, bn, bk, r.b[0], r.b[1], r.b[2], r.b[3]);
+                put4(bhi, blo, bn, bk + 4, r.b[4], r.b[5], r.b[6], r.b[7]);
+                if (ks + kTcK < B.jlen) // the next slab's loads fly while this one is multiplied
+                    load(ks + kTcK, cb, r);
                 proxy_fence();
                 __syncthreads();
                 if (tid == 0) {
@@ -252,17 +260,37 @@ __global__ void __launch_bounds__(kTcThreads, 2) phase1_tc_kernel(const TcBlock 
                 break;
             }
             tc_fence_after();
-#pragma unroll
-            for (int c16 = 0; c16 < kTcN / 16; c16++) {
-                float v[16];
-                tmem_ld16(tmem + ((unsigned)(32 * wid) << 16) + 16 * c16, v);
-                if (sg >= 0)
-#pragma unroll
-                    for (int q = 0; q < 16; q++) {
-                        const int c = cb + 16 * c16 + q;
-                        if (c < mu)
-                            A[out + c] = v[q] * sc;
+            {
+                // warp w reads lanes 32 (w mod 4) ..: the rows of those threads;
+                // warps 0-3 the first 32 columns, warps 4-7 the last 32
+                const int orow = 32 * (wid & 3) + lane, c0 = 32 * (wid >> 2);
+                int osg = -1, om0 = 0;
+                for (int s2 = B.s0; s2 < B.s1; s2++) {
+                    const int nc = segs[s2].ncol;
+                    if (orow < om0 + nc) {
+                        osg = s2;
+                        break;
                     }
+                    om0 += nc;
+                }
+                long long oo = 0;
+                float osc    = 0.f;
+                if (osg >= 0) {
+                    oo  = (segs[osg].slot + (long long)(orow - om0)) * mu;
+                    osc = scale[segs[osg].sidx + orow - om0];
+                }
+#pragma unroll
+                for (int c16 = 0; c16 < 2; c16++) {
+                    float v[16];
+                    tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + c0 + 16 * c16, v);
+                    if (osg >= 0)
+#pragma unroll
+                        for (int q = 0; q < 16; q++) {
+                            const int c = cb + c0 + 16 * c16 + q;
+                            if (c < mu)
+                                A[oo + c] = v[q] * osc;
+                        }
+                }
             }
             tc_fence_before();
             __syncthreads(); // the accumulator is read out before the next block overwrites it
@@ -270,10 +298,184 @@ __global__ void __launch_bounds__(kTcThreads, 2) phase1_tc_kernel(const TcBlock 
     }
     if (fail && lane == 0)
         atomicExch(status, 4);
-    // every issued product has completed (or a wait ran out) before the
-    // tensor memory is given back
-    if (!fail && slabs > 0 && tid == 0)
-        bar_wait(&bars[(slabs - 1) & 1], ((slabs - 1) >> 1) & 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (wid == 0)
+        tmem_free(tmem);
+}
+
+// Phase 2 (the U side) of the same products: per row chunk (h <= 32 rows)
+// Z (h x 64) = U (h x K) C (K x 64) over its FP32 / BF16 chunks, U the
+// chunks' columns as stored in lane order (column q = slice + S j of slice
+// q mod S, S = 32 / h: element ((j / V) S h + slice h + row) V + j mod V, V
+// = 4 FP32 or 8 BF16 values a 16-byte word) and C their coefficients (the
+// float phase-1 sums through the column indices).  Four row chunks share one
+// M = 128 accumulator, row chunk q in rows 32 q .. 32 q + 32: a slab of row
+// chunk q fills that band of A and leaves the other bands zero, so each
+// product only adds to its own rows.  The first product of a group starts
+// from zero (accumulate off) and so clears every row.  The z rows of the
+// group are written at the end; the dense FP64 chunks are added afterwards
+// by the double-float kernel.
+constexpr int kTcChunkBuf = kStreamStage; // one chunk's bytes
+
+__global__ void __launch_bounds__(kTcThreads, 2) phase2_tc_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ mix,
+                                                                 const int *__restrict__ cidx, const float *__restrict__ Af, const int *__restrict__ xexp, int mu, double *__restrict__ z,
+                                                                 int zlen, int *__restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf);
+    unsigned *tslot          = reinterpret_cast<unsigned *>(smem + 2 * kTcBuf + 64);
+    unsigned char *cbuf      = smem + 2 * kTcBuf + 128; // the current chunk's bytes
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        bar_init(&bars[0]);
+        bar_init(&bars[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot);
+    // both A buffers start zero: a slab writes only its band
+    for (int b = 0; b < 2; b++) // A hi and A lo of buffer b: the first 2 * kTcABytes of it
+        for (int e = tid; e < 2 * kTcABytes / 16; e += kTcThreads)
+            *reinterpret_cast<uint4 *>(smem + (size_t)b * kTcBuf + (size_t)e * 16) = make_uint4(0u, 0u, 0u, 0u);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+    const int shift     = max(*xexp, 1) - 1023;
+    int band[2]         = {-1, -1}; // the band each A buffer holds
+    int slabs           = 0;
+    bool fail           = false;
+    const int ngroups   = (nrc + 3) / 4;
+    for (int g = blockIdx.x; g < ngroups && !fail; g += gridDim.x) {
+        for (int cb = 0; cb < mu && !fail; cb += kTcN) {
+            int first = slabs; // slabs of this group start here
+            for (int q = 0; q < 4 && !fail; q++) {
+                const int w = 4 * g + q;
+                if (w >= nrc)
+                    break;
+                const int kb = rc[w], ke = rc[w + 1];
+                for (int k = kb; k < ke && !fail; k++) {
+                    const StreamChunk c = chunks[k];
+                    if (c.kind != kStreamF32 && c.kind != kStreamBf16)
+                        continue;
+                    // the chunk's bytes (16-byte words, <= 4 KB) into shared memory;
+                    // the previous chunk's band writes are done (barrier below)
+                    __syncthreads();
+                    for (int e = tid; e < (c.bytes >> 4); e += kTcThreads)
+                        reinterpret_cast<uint4 *>(cbuf)[e] = __ldg(reinterpret_cast<const uint4 *>(mix + c.src) + e);
+                    __syncthreads();
+                    const int h = c.h, S = 32 / h, Ln = S * h, lv = c.kind == kStreamF32 ? 2 : 3;
+                    for (int qs = 0; qs < c.ncol; qs += kTcK) {
+                        const int buf = slabs & 1, use = slabs >> 1;
+                        unsigned char *bb = smem + (size_t)buf * kTcBuf;
+                        if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1))
+                            fail = true;
+                        if (__syncthreads_or(fail)) {
+                            fail = true;
+                            break;
+                        }
+                        unsigned char *ahi = bb, *alo = bb + kTcABytes;
+                        // clear the band another row chunk left in this buffer
+                        if (band[buf] >= 0 && band[buf] != q) {
+                            const int row = 32 * band[buf] + (tid & 31), k0 = (tid >> 5) * 8;
+                            put4(ahi, alo, row, k0, 0.f, 0.f, 0.f, 0.f);
+                            put4(ahi, alo, row, k0 + 4, 0.f, 0.f, 0.f, 0.f);
+                        }
+                        band[buf] = q;
+                        // band q: row i = row i of the chunk (zero past h), eight K-values a thread
+                        {
+                            const int i = tid & 31, k0 = (tid >> 5) * 8;
+                            float v[8];
+#pragma unroll
+                            for (int t = 0; t < 8; t++) {
+                                const int col = qs + k0 + t;
+                                v[t]          = 0.f;
+                                if (i < h && col < c.ncol) {
+                                    const int j = col / S, sl = col - j * S;
+                                    const int e = (((j >> lv) * Ln + sl * h + i) << lv) + (j & ((1 << lv) - 1));
+                                    v[t]        = lv == 2 ? reinterpret_cast<const float *>(cbuf)[e] : bf16f(reinterpret_cast<const unsigned short *>(cbuf)[e]);
+                                }
+                            }
+                            put4(ahi, alo, 32 * q + i, k0, v[0], v[1], v[2], v[3]);
+                            put4(ahi, alo, 32 * q + i, k0 + 4, v[4], v[5], v[6], v[7]);
+                        }
+                        // B: the coefficients of the slab's columns, row n = right-hand side
+                        {
+                            unsigned char *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
+                            const int n = tid & 63, k0 = (tid >> 6) * 16;
+                            const bool on = cb + n < mu;
+                            float v[16];
+#pragma unroll
+                            for (int t = 0; t < 16; t++) {
+                                const int col = qs + k0 + t;
+                                v[t]          = 0.f;
+                                if (on && col < c.ncol) {
+                                    const int kx = __ldg(cidx + c.a + col);
+                                    if (kx >= 0)
+                                        v[t] = __ldg(Af + (long long)kx * mu + cb + n);
+                                }
+                            }
+#pragma unroll
+                            for (int t = 0; t < 16; t += 4)
+                                put4(bhi, blo, n, k0 + t, v[t], v[t + 1], v[t + 2], v[t + 3]);
+                        }
+                        proxy_fence();
+                        __syncthreads();
+                        if (tid == 0) {
+                            tc_fence_after();
+                            tc_slab(tmem, bb, slabs == first);
+                            tc_commit(&bars[buf]);
+                        }
+                        slabs++;
+                    }
+                }
+            }
+            if (fail)
+                break;
+            // z rows of the group's row chunks (zero where a row chunk has no
+            // reduced-precision columns: the dense chunks are added on top)
+            const bool any = slabs > first;
+            if (any) {
+                const int last = slabs - 1;
+                if (!bar_wait(&bars[last & 1], (last >> 1) & 1))
+                    fail = true;
+            }
+            if (__syncthreads_or(fail)) {
+                fail = true;
+                break;
+            }
+            tc_fence_after();
+            const int w = 4 * g + wid;
+            int h = 0, zrow = 0;
+            if (w < nrc) {
+                const StreamChunk head = chunks[rc[w]];
+                h                      = head.h;
+                zrow                   = head.b;
+            }
+#pragma unroll
+            for (int c16 = 0; c16 < kTcN / 16; c16++) {
+                float v[16];
+                if (any)
+                    tmem_ld16(tmem + ((unsigned)(32 * wid) << 16) + 16 * c16, v);
+                else
+#pragma unroll
+                    for (int t = 0; t < 16; t++)
+                        v[t] = 0.f;
+                if (lane < h)
+#pragma unroll
+                    for (int t = 0; t < 16; t++) {
+                        const int col = cb + 16 * c16 + t;
+                        if (col < mu)
+                            z[(long long)col * zlen + zrow + lane] = scale_pow2_safe((double)v[t], shift);
+                    }
+            }
+            tc_fence_before();
+            __syncthreads();
+        }
+    }
+    if (fail && lane == 0)
+        atomicExch(status, 4);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -354,7 +556,26 @@ void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, con
     HTGPU_CUDA(cudaGetDevice(&dev));
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int grid = std::min(nblocks, 2 * sms); // two CTAs an SM (96 KB of shared memory, 64 tensor-memory columns each)
-    phase1_tc_kernel<<<grid, kTcThreads, kTcSmem, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A, status);
+    phase1_tc_kernel<<<grid, kTc1Threads, kTcSmem, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase2_tc(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const float *Af, const int *xexp, int mu, double *z, int zlen, int *status,
+                      cudaStream_t st) {
+    if (nrc <= 0)
+        return;
+    static unsigned long long done = 0;
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem + kTcChunkBuf));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int ngroups = (nrc + 3) / 4;
+    const int grid    = std::min(ngroups, 2 * sms);
+    phase2_tc_kernel<<<grid, kTcThreads, kTcSmem + kTcChunkBuf, st>>>(chunks, rc, nrc, mix, cidx, Af, xexp, mu, z, zlen, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
