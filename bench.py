@@ -587,6 +587,9 @@ def run_helmholtz(args):
     hm.set_tensor_core_mode("tcgen05")
     ms_tc, y_tc = timed(steps)
     ph_tc = hm.profile(mu, 3)
+    hm.set_tensor_core_mode("tcgen05_both")
+    ms_both, y_both = timed(steps)
+    ph_both = hm.profile(mu, 3)
     hm.set_tensor_core_mode("mma.sync")
     ms_mma, y_mma = timed(steps)
     ph_mma = hm.profile(mu, 3)
@@ -601,7 +604,8 @@ def run_helmholtz(args):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_tc, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32/bf16 factors (per-column scaled), TF32x3 tensor-core contractions with FP32 accumulation, fp64 dense", "data": "synthetic (seeded points on the unit-cube surface)",
         "config": {"workload": "helmholtz_cube", "n": n, "wavenumber": 20.0, "eta": 3.0, "epsilon": 1e-5, "mu": mu, "l2": "inputs larger than L2 (the stored H-matrix, tens of GB)"},
-        "mixed_tcgen05": {"ms": ms_tc, "rel_err_vs_fp64": err(y_tc), "phase_ms": phases(ph_tc)},
+        "mixed_tcgen05": {"ms": ms_tc, "rel_err_vs_fp64": err(y_tc), "phase_ms": phases(ph_tc), "kernels": "phase 1 tcgen05, phase 2 mma.sync (the default)"},
+        "mixed_tcgen05_both": {"ms": ms_both, "rel_err_vs_fp64": err(y_both), "phase_ms": phases(ph_both)},
         "mixed_mma_sync": {"ms": ms_mma, "rel_err_vs_fp64": err(y_mma), "phase_ms": phases(ph_mma)},
         "fp64": {"ms": ms64, "phase_ms": phases(ph64)},
         "build_seconds": build_s, "clocks": ck, "device_status": status,

@@ -548,8 +548,9 @@ class HMatrix:
         return v.value
 
     def set_tensor_core_mode(self, mode):
-        """"mma.sync" / 0 or "tcgen05" / 1 (the default)"""
-        m = {"mma.sync": 0, "tcgen05": 1}[mode] if isinstance(mode, str) else int(mode)
+        """"mma.sync" / 0, "tcgen05" / 1 (phase 1 on tcgen05, the default) or
+        "tcgen05_both" / 2 (both phases on tcgen05)"""
+        m = {"mma.sync": 0, "tcgen05": 1, "tcgen05_both": 2}[mode] if isinstance(mode, str) else int(mode)
         _check(lib.htgpu_hmatrix_set_tensor_core_mode(self.h, m))
 
     def get_tensor_core_mode(self):

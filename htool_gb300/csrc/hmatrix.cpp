@@ -1387,7 +1387,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
         } else if (n_p1m_ && mma) {
-            if (tc_mode_ == 1 && n_tcblk_ > 0)
+            if (tc_mode_ >= 1 && n_tcblk_ > 0)
                 launch_phase1_tc(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, reinterpret_cast<float *>(w_A), status_d.p, st);
             else
                 launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scalef_d.p, w_xs, mu, w_A, st);
@@ -1403,7 +1403,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
         if (mma && n_p2rc_m_ > 0) { // low-rank part on the tensor cores, then the dense chunks added
-            if (tc_mode_ == 1)
+            if (tc_mode_ == 2)
                 launch_phase2_tc(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, reinterpret_cast<const float *>(w_A), w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
             else
                 launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
@@ -1479,7 +1479,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
 
 void HMatrix::set_tensor_core_mode(int mode) {
     layout_gen_++; // captured products are stale
-    require(mode == 0 || mode == 1, "tensor-core mode must be 0 (mma.sync) or 1 (tcgen05)");
+    require(mode >= 0 && mode <= 2, "tensor-core mode must be 0 (mma.sync), 1 (tcgen05 phase 1) or 2 (tcgen05 both phases)");
     tc_mode_ = mode;
 }
 

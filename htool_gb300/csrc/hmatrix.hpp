@@ -170,7 +170,8 @@ class HMatrix {
     void set_phase2_mode(int mode);
     int phase2_mode() const { return p2_mode_; }
     // tensor-core kernels of reduced-precision products with many
-    // right-hand sides: 0 warp-level mma.sync, 1 tcgen05 (default)
+    // right-hand sides: 0 warp-level mma.sync in both phases, 1 tcgen05
+    // phase 1 with the mma.sync phase 2 (default), 2 tcgen05 in both
     void set_tensor_core_mode(int mode);
     int tensor_core_mode() const { return tc_mode_; }
     bool emulation_allowed() const { return emu_ok_; }
@@ -312,7 +313,7 @@ class HMatrix {
     DevBuf<TcSeg> tcseg_d;
     DevBuf<TcBlock> tcblk_d;
     int n_tcblk_ = 0;
-    int tc_mode_ = 1; // many-RHS reduced-precision contractions: 0 warp-level mma.sync, 1 tcgen05
+    int tc_mode_ = 1; // many-RHS reduced-precision contractions: 0 mma.sync, 1 tcgen05 phase 1, 2 tcgen05 both phases
     int n_p2rc_m_ = 0, n_p2rc_ = 0;
     long long n_chunks_md_ = 0;
     // algorithmic bytes: phase-1 / phase-2 factor bytes (FP64 and reduced

@@ -298,12 +298,15 @@ int htgpu_hmatrix_get_phase2_mode(htgpu_hmatrix h, int *mode);
 
 /* Tensor-core kernels of reduced-precision products with at least 8
  * right-hand sides on H-matrices with epsilon >= 1e-5: HTGPU_TC_MMA_SYNC
- * (warp-level mma.sync TF32, one warp per tile or row chunk) or
- * HTGPU_TC_TCGEN05 (the default: tcgen05.mma with tensor-memory
- * accumulators; phase 1 stacks the tiles that share their x rows into GEMMs
- * of up to 128 columns).  No counterpart in the reference. */
+ * (warp-level mma.sync TF32 in both phases, one warp per tile or row chunk),
+ * HTGPU_TC_TCGEN05 (the default: phase 1 on tcgen05.mma with tensor-memory
+ * accumulators, the tiles that share their x rows stacked into GEMMs of up
+ * to 128 columns; phase 2 on mma.sync) or HTGPU_TC_TCGEN05_BOTH (phase 2 on
+ * tcgen05 as well, four row chunks to one 128-row accumulator).  Results
+ * agree within FP32 accumulation.  No counterpart in the reference. */
 #define HTGPU_TC_MMA_SYNC 0
 #define HTGPU_TC_TCGEN05 1
+#define HTGPU_TC_TCGEN05_BOTH 2
 int htgpu_hmatrix_set_tensor_core_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode);
 

@@ -65,9 +65,12 @@ def test_tcgen05_phase1_matches_mma_sync_and_fp64(mu):
     assert hm.device_status() == 0
     hm.set_tensor_core_mode("mma.sync")
     ymma = hm.mvprod_global_to_global(x, mu)
+    hm.set_tensor_core_mode("tcgen05_both")
+    yboth = hm.mvprod_global_to_global(x, mu)
+    assert hm.device_status() == 0
     hm.set_tensor_core_mode("tcgen05")
-    assert rel(ytc, ymma) < 2e-6
-    assert rel(ytc, y64) < 1e-5
+    assert rel(ytc, ymma) < 2e-6 and rel(yboth, ymma) < 2e-6
+    assert rel(ytc, y64) < 1e-5 and rel(yboth, y64) < 1e-5
     assert np.array_equal(hm.mvprod_global_to_global(x, mu), ytc)  # repeatable
 
 
@@ -81,5 +84,7 @@ def test_tcgen05_complex_many_rhs(golden):
     y64 = hm.mvprod_global_to_global(X, 64)
     hm.set_precision("mixed")
     ytc = hm.mvprod_global_to_global(X, 64)
+    hm.set_tensor_core_mode("tcgen05_both")
+    yboth = hm.mvprod_global_to_global(X, 64)
     assert hm.device_status() == 0
-    assert rel(ytc, y64) < 1e-5
+    assert rel(ytc, y64) < 1e-5 and rel(yboth, y64) < 1e-5
