@@ -1095,6 +1095,39 @@ void HMatrix::upload_mixed_phase2() {
         n_p2rc_m_ = (int)rc.size();
         rc.push_back((int)ch2.size());
         p2rcm_d.upload(rc, stream_);
+        // tcgen05 phase 2: slabs of 32 reduced columns per row chunk, four
+        // row chunks to a group
+        std::vector<Tc2Slab> slabs;
+        std::vector<int> gs;
+        for (int w = 0; w < n_p2rc_m_; w++) {
+            if (w % 4 == 0)
+                gs.push_back((int)slabs.size());
+            int k = rc[w];
+            while (k < rc[w + 1] && ch2[k].kind != kStreamF32 && ch2[k].kind != kStreamBf16)
+                k++; // the dense chunks come first
+            int col = 0;
+            while (k < rc[w + 1]) {
+                slabs.push_back({k, col, w % 4, 0});
+                int left = 32; // advance 32 columns
+                while (k < rc[w + 1] && left > 0) {
+                    const int room = ch2[k].ncol - col;
+                    if (room > left) {
+                        col += left;
+                        left = 0;
+                    } else {
+                        left -= room;
+                        col = 0;
+                        k++;
+                    }
+                }
+            }
+        }
+        gs.push_back((int)slabs.size());
+        n_tc2_groups_ = (int)gs.size() - 1;
+        tc2slab_d.upload(slabs, stream_);
+        if (slabs.empty())
+            tc2slab_d.alloc(1);
+        tc2g_d.upload(gs, stream_);
     }
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
@@ -1404,7 +1437,8 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
             HTGPU_CUDA(cudaEventRecord(marks[1], st));
         if (mma && n_p2rc_m_ > 0) { // low-rank part on the tensor cores, then the dense chunks added
             if (tc_mode_ == 2)
-                launch_phase2_tc(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, reinterpret_cast<const float *>(w_A), w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+                launch_phase2_tc(scm_d.p, p2rcm_d.p, n_p2rc_m_, tc2slab_d.p, tc2g_d.p, n_tc2_groups_, mix_.p, cidxm_d.p, reinterpret_cast<const float *>(w_A), w_xexp, mu, w_z, (int)zlen_,
+                                 status_d.p, st);
             else
                 launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
             launches_ += 1;

@@ -313,6 +313,9 @@ class HMatrix {
     DevBuf<TcSeg> tcseg_d;
     DevBuf<TcBlock> tcblk_d;
     int n_tcblk_ = 0;
+    DevBuf<Tc2Slab> tc2slab_d; // tensor-core phase 2: slabs and the first slab of each group of four row chunks
+    DevBuf<int> tc2g_d;
+    int n_tc2_groups_ = 0;
     int tc_mode_ = 1; // many-RHS reduced-precision contractions: 0 mma.sync, 1 tcgen05 phase 1, 2 tcgen05 both phases
     int n_p2rc_m_ = 0, n_p2rc_ = 0;
     long long n_chunks_md_ = 0;

@@ -200,11 +200,15 @@ struct TcBlock { // segments [s0, s1), at most 128 columns in all, on x rows xro
     int s0, s1, xrow, jlen;
 };
 void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, int *status, cudaStream_t st);
-// phase 2 of the same products on tcgen05: the FP32 / BF16 chunks of every
-// row chunk (rc as launch_phase2_mma), four row chunks to one 128-row
-// accumulator; writes the z rows (the dense chunks are added afterwards)
-void launch_phase2_tc(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const float *Af, const int *xexp, int mu, double *z, int zlen, int *status,
-                      cudaStream_t st);
+// phase 2 of the same products on tcgen05: the FP32 / BF16 columns of every
+// row chunk in slabs of 32 (rc as launch_phase2_mma), four row chunks
+// (a group) to one 128-row accumulator; writes the z rows (the dense chunks
+// are added afterwards)
+struct Tc2Slab { // first column of a slab: chunk and column in it; row chunk within its group
+    int chunk, col, band, pad;
+};
+void launch_phase2_tc(const StreamChunk *chunks, const int *rc, int nrc, const Tc2Slab *slabs, const int *gslab, int ngroups, const unsigned char *mix, const int *cidx, const float *Af,
+                      const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
 // one 128 x 32 by 32 x 64 product (row-major a, b, d on the device) through
 // the tensor-core path's staging, descriptors and read-out
 void tc_selftest(const float *a, const float *b, float *d, int *status, cudaStream_t st);

@@ -133,6 +133,11 @@ __device__ __forceinline__ void put4(unsigned char *hi, unsigned char *lo, int r
 
 __device__ __forceinline__ float bf16f(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
 
+// floor(t / d) for 0 <= t < 128, 1 <= d <= 32: (t * (floor(65536 / d) + 1)) >> 16
+// overshoots t / d by less than 128 / 65536, below the 1 / d gap to the next
+// integer (a run-time division costs tens of instructions)
+__device__ __forceinline__ int div_small32(int t, int d) { return (int)(((unsigned)t * (65536u / (unsigned)d + 1u)) >> 16); }
+
 // the three TF32 products of one slab (K = 32: four K-steps of 8)
 __device__ __forceinline__ void tc_slab(unsigned tmem, const unsigned char *buf, bool first) {
     const unsigned a_hi = smem_u32(buf), a_lo = a_hi + kTcABytes, b_hi = a_lo + kTcABytes, b_lo = b_hi + kTcBBytes;
@@ -311,22 +316,28 @@ __global__ void __launch_bounds__(kTc1Threads, 2) phase1_tc_kernel(const TcBlock
 // q mod S, S = 32 / h: element ((j / V) S h + slice h + row) V + j mod V, V
 // = 4 FP32 or 8 BF16 values a 16-byte word) and C their coefficients (the
 // float phase-1 sums through the column indices).  Four row chunks share one
-// M = 128 accumulator, row chunk q in rows 32 q .. 32 q + 32: a slab of row
-// chunk q fills that band of A and leaves the other bands zero, so each
-// product only adds to its own rows.  The first product of a group starts
-// from zero (accumulate off) and so clears every row.  The z rows of the
-// group are written at the end; the dense FP64 chunks are added afterwards
-// by the double-float kernel.
-constexpr int kTcChunkBuf = kStreamStage; // one chunk's bytes
+// M = 128 accumulator, row chunk q in rows 32 q .. 32 q + 32: a slab (32
+// consecutive reduced columns of one row chunk, across its chunks: Tc2Slab)
+// fills that band of A and leaves the other bands zero, so each product only
+// adds to its own rows; the first product of a group starts from zero and so
+// clears every row.  Eight warps; the next slab's values are loaded into
+// registers while the current one is multiplied.  The z rows of the group
+// are written at the end; the dense FP64 chunks are added afterwards by the
+// double-float kernel.
+struct P2Regs {
+    float a[4]; // this thread's row of the band, 4 K-values
+    float b[8]; // this thread's right-hand side of B, 8 K-values
+};
 
-__global__ void __launch_bounds__(kTcThreads, 2) phase2_tc_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ mix,
-                                                                 const int *__restrict__ cidx, const float *__restrict__ Af, const int *__restrict__ xexp, int mu, double *__restrict__ z,
-                                                                 int zlen, int *__restrict__ status) {
+__global__ void __launch_bounds__(kTc1Threads, 2) phase2_tc_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const Tc2Slab *__restrict__ slabs_in,
+                                                                   const int *__restrict__ gslab, int ngroups, const unsigned char *__restrict__ mix, const int *__restrict__ cidx,
+                                                                   const float *__restrict__ Af, const int *__restrict__ xexp, int mu, double *__restrict__ z, int zlen, int *__restrict__ status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf);
     unsigned *tslot          = reinterpret_cast<unsigned *>(smem + 2 * kTcBuf + 64);
-    unsigned char *cbuf      = smem + 2 * kTcBuf + 128; // the current chunk's bytes
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const int ai = tid & 31, ak = (tid >> 5) * 4; // A: band row, first K-value
+    const int bn = tid & 63, bk = (tid >> 6) * 8; // B: right-hand side, first K-value
     if (tid == 0) {
         bar_init(&bars[0]);
         bar_init(&bars[1]);
@@ -334,119 +345,110 @@ __global__ void __launch_bounds__(kTcThreads, 2) phase2_tc_kernel(const StreamCh
     }
     if (wid == 0)
         tmem_alloc(tslot);
-    // both A buffers start zero: a slab writes only its band
-    for (int b = 0; b < 2; b++) // A hi and A lo of buffer b: the first 2 * kTcABytes of it
-        for (int e = tid; e < 2 * kTcABytes / 16; e += kTcThreads)
+    for (int b = 0; b < 2; b++) // A hi and A lo of buffer b start zero: a slab writes only its band
+        for (int e = tid; e < 2 * kTcABytes / 16; e += kTc1Threads)
             *reinterpret_cast<uint4 *>(smem + (size_t)b * kTcBuf + (size_t)e * 16) = make_uint4(0u, 0u, 0u, 0u);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = *tslot;
     const int shift     = max(*xexp, 1) - 1023;
-    int band[2]         = {-1, -1}; // the band each A buffer holds
-    int slabs           = 0;
+    int band0 = -1, band1 = -1; // the band each A buffer holds
+    int nsl             = 0;        // slabs issued by this CTA
     bool fail           = false;
-    const int ngroups   = (nrc + 3) / 4;
+    // chunk and column of K-value k of a slab: walk the row chunk's reduced chunks
+    auto locate = [&](const Tc2Slab &S, int kend, int k, int &ch, int &col) {
+        ch  = S.chunk;
+        col = S.col + k;
+        while (ch < kend) {
+            const int nc = chunks[ch].ncol;
+            if (col < nc)
+                return true;
+            col -= nc;
+            ch++;
+        }
+        return false;
+    };
+    auto load = [&](int si, int g, int cb, P2Regs &r) {
+        const Tc2Slab S = slabs_in[si];
+        const int w     = 4 * g + S.band;
+        const int kend  = rc[w + 1];
+        const int h     = chunks[rc[w]].h;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            int ch, col;
+            r.a[t] = 0.f;
+            if (ai < h && locate(S, kend, ak + t, ch, col)) {
+                const StreamChunk c = chunks[ch];
+                const int S2 = 32 / h, lv = c.kind == kStreamF32 ? 2 : 3;
+                const int j  = div_small32(col, S2), sl = col - j * S2;
+                const int e  = (((j >> lv) * (S2 * h) + sl * h + ai) << lv) + (j & ((1 << lv) - 1));
+                r.a[t]       = lv == 2 ? __ldg(reinterpret_cast<const float *>(mix + c.src) + e) : bf16f(__ldg(reinterpret_cast<const unsigned short *>(mix + c.src) + e));
+            }
+        }
+        const bool on = cb + bn < mu;
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            int ch, col;
+            r.b[t] = 0.f;
+            if (on && locate(S, kend, bk + t, ch, col)) {
+                const int kx = __ldg(cidx + chunks[ch].a + col);
+                if (kx >= 0)
+                    r.b[t] = __ldg(Af + (long long)kx * mu + cb + bn);
+            }
+        }
+    };
     for (int g = blockIdx.x; g < ngroups && !fail; g += gridDim.x) {
+        const int s0 = gslab[g], s1 = gslab[g + 1];
         for (int cb = 0; cb < mu && !fail; cb += kTcN) {
-            int first = slabs; // slabs of this group start here
-            for (int q = 0; q < 4 && !fail; q++) {
-                const int w = 4 * g + q;
-                if (w >= nrc)
+            P2Regs r;
+            if (s0 < s1)
+                load(s0, g, cb, r);
+            for (int si = s0; si < s1; si++) {
+                const int q   = slabs_in[si].band;
+                const int buf = nsl & 1, use = nsl >> 1;
+                unsigned char *bb = smem + (size_t)buf * kTcBuf;
+                if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1))
+                    fail = true;
+                if (__syncthreads_or(fail)) {
+                    fail = true;
                     break;
-                const int kb = rc[w], ke = rc[w + 1];
-                for (int k = kb; k < ke && !fail; k++) {
-                    const StreamChunk c = chunks[k];
-                    if (c.kind != kStreamF32 && c.kind != kStreamBf16)
-                        continue;
-                    // the chunk's bytes (16-byte words, <= 4 KB) into shared memory;
-                    // the previous chunk's band writes are done (barrier below)
-                    __syncthreads();
-                    for (int e = tid; e < (c.bytes >> 4); e += kTcThreads)
-                        reinterpret_cast<uint4 *>(cbuf)[e] = __ldg(reinterpret_cast<const uint4 *>(mix + c.src) + e);
-                    __syncthreads();
-                    const int h = c.h, S = 32 / h, Ln = S * h, lv = c.kind == kStreamF32 ? 2 : 3;
-                    for (int qs = 0; qs < c.ncol; qs += kTcK) {
-                        const int buf = slabs & 1, use = slabs >> 1;
-                        unsigned char *bb = smem + (size_t)buf * kTcBuf;
-                        if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1))
-                            fail = true;
-                        if (__syncthreads_or(fail)) {
-                            fail = true;
-                            break;
-                        }
-                        unsigned char *ahi = bb, *alo = bb + kTcABytes;
-                        // clear the band another row chunk left in this buffer
-                        if (band[buf] >= 0 && band[buf] != q) {
-                            const int row = 32 * band[buf] + (tid & 31), k0 = (tid >> 5) * 8;
-                            put4(ahi, alo, row, k0, 0.f, 0.f, 0.f, 0.f);
-                            put4(ahi, alo, row, k0 + 4, 0.f, 0.f, 0.f, 0.f);
-                        }
-                        band[buf] = q;
-                        // band q: row i = row i of the chunk (zero past h), eight K-values a thread
-                        {
-                            const int i = tid & 31, k0 = (tid >> 5) * 8;
-                            float v[8];
-#pragma unroll
-                            for (int t = 0; t < 8; t++) {
-                                const int col = qs + k0 + t;
-                                v[t]          = 0.f;
-                                if (i < h && col < c.ncol) {
-                                    const int j = col / S, sl = col - j * S;
-                                    const int e = (((j >> lv) * Ln + sl * h + i) << lv) + (j & ((1 << lv) - 1));
-                                    v[t]        = lv == 2 ? reinterpret_cast<const float *>(cbuf)[e] : bf16f(reinterpret_cast<const unsigned short *>(cbuf)[e]);
-                                }
-                            }
-                            put4(ahi, alo, 32 * q + i, k0, v[0], v[1], v[2], v[3]);
-                            put4(ahi, alo, 32 * q + i, k0 + 4, v[4], v[5], v[6], v[7]);
-                        }
-                        // B: the coefficients of the slab's columns, row n = right-hand side
-                        {
-                            unsigned char *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
-                            const int n = tid & 63, k0 = (tid >> 6) * 16;
-                            const bool on = cb + n < mu;
-                            float v[16];
-#pragma unroll
-                            for (int t = 0; t < 16; t++) {
-                                const int col = qs + k0 + t;
-                                v[t]          = 0.f;
-                                if (on && col < c.ncol) {
-                                    const int kx = __ldg(cidx + c.a + col);
-                                    if (kx >= 0)
-                                        v[t] = __ldg(Af + (long long)kx * mu + cb + n);
-                                }
-                            }
-#pragma unroll
-                            for (int t = 0; t < 16; t += 4)
-                                put4(bhi, blo, n, k0 + t, v[t], v[t + 1], v[t + 2], v[t + 3]);
-                        }
-                        proxy_fence();
-                        __syncthreads();
-                        if (tid == 0) {
-                            tc_fence_after();
-                            tc_slab(tmem, bb, slabs == first);
-                            tc_commit(&bars[buf]);
-                        }
-                        slabs++;
-                    }
                 }
+                unsigned char *ahi = bb, *alo = bb + kTcABytes, *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
+                const int held = buf ? band1 : band0;
+                if (held >= 0 && held != q) // clear the band another row chunk left here
+                    put4(ahi, alo, 32 * held + ai, ak, 0.f, 0.f, 0.f, 0.f);
+                if (buf)
+                    band1 = q;
+                else
+                    band0 = q;
+                put4(ahi, alo, 32 * q + ai, ak, r.a[0], r.a[1], r.a[2], r.a[3]);
+                put4(bhi, blo, bn, bk, r.b[0], r.b[1], r.b[2], r.b[3]);
+                put4(bhi, blo, bn, bk + 4, r.b[4], r.b[5], r.b[6], r.b[7]);
+                if (si + 1 < s1) // the next slab's values fly while this one is multiplied
+                    load(si + 1, g, cb, r);
+                proxy_fence();
+                __syncthreads();
+                if (tid == 0) {
+                    tc_fence_after();
+                    tc_slab(tmem, bb, si == s0);
+                    tc_commit(&bars[buf]);
+                }
+                nsl++;
             }
             if (fail)
                 break;
-            // z rows of the group's row chunks (zero where a row chunk has no
-            // reduced-precision columns: the dense chunks are added on top)
-            const bool any = slabs > first;
-            if (any) {
-                const int last = slabs - 1;
-                if (!bar_wait(&bars[last & 1], (last >> 1) & 1))
-                    fail = true;
-            }
+            // the group's z rows (zero where a row chunk has no reduced columns:
+            // the dense chunks are added on top)
+            const bool any = s1 > s0;
+            if (any && !bar_wait(&bars[(nsl - 1) & 1], ((nsl - 1) >> 1) & 1))
+                fail = true;
             if (__syncthreads_or(fail)) {
                 fail = true;
                 break;
             }
             tc_fence_after();
-            const int w = 4 * g + wid;
+            const int w = 4 * g + (wid & 3), c0 = 32 * (wid >> 2);
             int h = 0, zrow = 0;
             if (w < nrc) {
                 const StreamChunk head = chunks[rc[w]];
@@ -454,10 +456,10 @@ __global__ void __launch_bounds__(kTcThreads, 2) phase2_tc_kernel(const StreamCh
                 zrow                   = head.b;
             }
 #pragma unroll
-            for (int c16 = 0; c16 < kTcN / 16; c16++) {
+            for (int c16 = 0; c16 < 2; c16++) {
                 float v[16];
                 if (any)
-                    tmem_ld16(tmem + ((unsigned)(32 * wid) << 16) + 16 * c16, v);
+                    tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + c0 + 16 * c16, v);
                 else
 #pragma unroll
                     for (int t = 0; t < 16; t++)
@@ -465,7 +467,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) phase2_tc_kernel(const StreamCh
                 if (lane < h)
 #pragma unroll
                     for (int t = 0; t < 16; t++) {
-                        const int col = cb + 16 * c16 + t;
+                        const int col = cb + c0 + 16 * c16 + t;
                         if (col < mu)
                             z[(long long)col * zlen + zrow + lane] = scale_pow2_safe((double)v[t], shift);
                     }
@@ -560,22 +562,21 @@ void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, con
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_phase2_tc(const StreamChunk *chunks, const int *rc, int nrc, const unsigned char *mix, const int *cidx, const float *Af, const int *xexp, int mu, double *z, int zlen, int *status,
-                      cudaStream_t st) {
-    if (nrc <= 0)
+void launch_phase2_tc(const StreamChunk *chunks, const int *rc, int nrc, const Tc2Slab *slabs, const int *gslab, int ngroups, const unsigned char *mix, const int *cidx, const float *Af,
+                      const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+    if (ngroups <= 0)
         return;
     static unsigned long long done = 0;
     int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
     if (dev >= 64 || !(done >> dev & 1)) {
-        HTGPU_CUDA(cudaFuncSetAttribute(phase2_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem + kTcChunkBuf));
+        HTGPU_CUDA(cudaFuncSetAttribute(phase2_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
         if (dev < 64)
             done |= 1ull << dev;
     }
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int ngroups = (nrc + 3) / 4;
-    const int grid    = std::min(ngroups, 2 * sms);
-    phase2_tc_kernel<<<grid, kTcThreads, kTcSmem + kTcChunkBuf, st>>>(chunks, rc, nrc, mix, cidx, Af, xexp, mu, z, zlen, status);
+    const int grid = std::min(ngroups, 2 * sms);
+    phase2_tc_kernel<<<grid, kTc1Threads, kTcSmem, st>>>(chunks, rc, nrc, slabs, gslab, ngroups, mix, cidx, Af, xexp, mu, z, zlen, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
