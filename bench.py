@@ -66,6 +66,7 @@ def parse():
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-predictor", action="store_true", help="skip the rank-predictor rebuild")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched workload (the `batched` key)")
     p.add_argument("--workload", default="sphere", choices=["sphere", "batched", "helmholtz"],
                    help="sphere: the one-H-matrix product; batched: 256 H-matrices in one graph launch; helmholtz: the complex cube with 64 right-hand sides")
     p.add_argument("--count", type=int, default=256, help="batched: number of H-matrices")
@@ -396,12 +397,19 @@ def run_gpu(args):
                      "rerun_rate": int(il["GPU_aca_overflow_reruns"]) / max(1, int(il["GPU_aca_predicted_blocks"])), "same_leaves": same}
         del hl
 
+    gpu_leaves = hm.get_leaves()
+    # the batched workload (256 H-matrices, one graph launch per step),
+    # measured in the same run
+    batched = None
+    if not args.no_batched:
+        hm.set_precision("fp64")
+        batched = batched_workload(local, args.steps, args.warmup, args.count, world)
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
     err_mixed_vs_fp64 = float(np.linalg.norm(ym - y64) / np.linalg.norm(y64))
-    gpu_leaves = hm.get_leaves()
     dense_err = {k: float(np.linalg.norm(v[rows] - dense_ref) / np.linalg.norm(dense_ref)) for k, v in (("fp64", y64), ("mixed", ym))}
     line = {
         "metric": METRIC, "value": value64, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step64, "higher_is_better": True,
@@ -425,6 +433,7 @@ def run_gpu(args):
                                  "aca_blocks": int(info["GPU_aca_blocks"]), "aca_rounds_launched": int(float(info["GPU_aca_rounds"]))},
         "rank_predictor": predictor,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},
+        "batched": batched,
     }
     if not args.no_cpu_baseline:
         cb, y_ref, ref_leaves = cpu_reference(n, reps=5, single_thread_reps=1, x=x)
@@ -451,89 +460,140 @@ def batched_items(count, seed=4):
     return out
 
 
-def run_batched(args):
-    """256 H-matrices, one graph launch per step (replicas under torchrun)"""
+def batched_workload(local, steps, warmup, count=256, world=1, sample_parity=True):
+    """The batched workload: every H-matrix of `batched_items(count)` is a
+    member of one forest per right-hand-side count (a block-diagonal
+    H-matrix built by one device assembly and applied by one product), and
+    the forests' products are captured as one CUDA graph: one launch per
+    step.  FP64 then mixed precision, each forest autotuned (kernel modes,
+    FP64 split, right-hand-side bucket).  Returns the measurements."""
     import torch
+
     import htool_gb300 as H
     from htool_gb300 import geometry as G
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    items = batched_items(args.count)
+    eps, eta = WORKLOAD["epsilon"], WORKLOAD["eta"]
+    items = batched_items(count)
+    buckets = {}
+    for k, (_, _, mu) in enumerate(items):
+        buckets.setdefault(mu, []).append(k)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    hms, bufs = [], []
-    batch = H.HBatch(local)
-    total_mu = 0
-    nbytes = 0
-    for k, (n, axes, mu) in enumerate(items):
-        pts = G.ellipsoid(n, axes, seed=100 + k)
-        t = H.Cluster().build(n, pts)
-        hm = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).build(H.LAPLACE, pts)
-        x = torch.from_numpy(G.rhs(n, mu, seed=10 + k)).cuda()
-        y = torch.zeros(n * mu, dtype=torch.float64, device="cuda")
-        batch.add(hm, x.data_ptr(), y.data_ptr(), mu, keep=(x, y))
-        hms.append(hm)
-        bufs.append((x, y))
-        total_mu += mu
-        nbytes += sum(hm.phase_bytes(mu))
+    forests = []
+    for mu in sorted(buckets):
+        ks = buckets[mu]
+        trees, pts, ns = [], [], []
+        for k in ks:
+            n, axes, _ = items[k]
+            p = G.ellipsoid(n, axes, seed=100 + k)
+            trees.append(H.Cluster().build(n, p))
+            pts.append(p)
+            ns.append(n)
+        F = H.Cluster.forest(trees)
+        hm = H.HMatrix(F, F, eps, eta, device=local).build(H.LAPLACE, np.concatenate(pts))
+        xs = [G.rhs(n, mu, seed=10 + k) for n, k in zip(ns, ks)]
+        cat = np.concatenate([np.concatenate([x[c * n:(c + 1) * n] for x, n in zip(xs, ns)]) for c in range(mu)])
+        N = int(sum(ns))
+        forests.append(dict(mu=mu, ks=ks, ns=ns, N=N, hm=hm, pts=pts, x=torch.from_numpy(cat).cuda(), y=torch.zeros(N * mu, dtype=torch.float64, device="cuda")))
+    torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
-    free_b, total_b = torch.cuda.mem_get_info()
+    total_mu = sum(mu for _, _, mu in items)
     stream = torch.cuda.current_stream()
 
-    def timed_batch():
-        """(ms per graph launch over the timed steps, ms of the products one by one)"""
-        batch.capture(nstreams=8)
-        for _ in range(max(args.warmup, 3)):
+    def members(f, y):
+        cols = y.reshape(f["mu"], f["N"])
+        out, off = [], 0
+        for n in f["ns"]:
+            out.append(np.ascontiguousarray(cols[:, off:off + n]).reshape(-1))
+            off += n
+        return out
+
+    def timed(policy):
+        tune = {}
+        for f in forests:
+            if policy == "fp64":
+                f["hm"].set_precision("fp64")
+            else:
+                f["hm"].set_precision(policy, 1.0)
+            tune[f["mu"]] = f["hm"].autotune(f["mu"], 3)
+        batch = H.HBatch(local)
+        for f in forests:
+            batch.add(f["hm"], f["x"].data_ptr(), f["y"].data_ptr(), f["mu"], keep=(f["x"], f["y"]))
+        nodes = batch.capture(nstreams=len(forests))
+        for _ in range(max(warmup, 3)):
             batch.launch(stream.cuda_stream)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for hm, (x, y), (n, _, mu) in zip(hms, bufs, items):
-            hm.mvprod_ptr(x.data_ptr(), y.data_ptr(), mu, 0, stream.cuda_stream)
+        for _ in range(steps):
+            batch.launch(stream.cuda_stream)
         e1.record(stream)
         torch.cuda.synchronize()
-        single = e0.elapsed_time(e1)
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        for _ in range(args.steps):
-            batch.launch(stream.cuda_stream)
-        s1.record(stream)
-        torch.cuda.synchronize()
-        return s0.elapsed_time(s1) / args.steps, single
+        ms = e0.elapsed_time(e1) / steps
+        nbytes = sum(sum(f["hm"].phase_bytes(f["mu"])) for f in forests)
+        ys = [f["y"].cpu().numpy().copy() for f in forests]
+        info = {"bucket_run": {str(f["mu"]): f["hm"].get_rhs_bucket(f["mu"]) for f in forests}, "autotune_ms": {str(k): v for k, v in tune.items()}, "graph_nodes": nodes}
+        del batch
+        return ms, nbytes, ys, info
 
-    ms64, single64 = timed_batch()
-    y64 = [y.clone() for _, y in bufs]
-    nbytes64 = nbytes
-    for hm in hms:
-        hm.set_precision("mixed", 1.0)
-    nbytes = sum(sum(hm.phase_bytes(mu)) for hm, (_, _, mu) in zip(hms, items))
     clocks = Clocks(local)
     clocks.start()
-    ms, single_ms = timed_batch()
+    ms64, bytes64, ys64, info64 = timed("fp64")
+    msm, bytesm, ysm, infom = timed("mixed")
     ck = clocks.stop()
-    err = max(float(torch.linalg.norm(y - r) / torch.linalg.norm(r)) for (_, y), r in zip(bufs, y64))
+    err = 0.0
+    for f, a, b in zip(forests, ysm, ys64):
+        for ym, y6 in zip(members(f, a), members(f, b)):
+            err = max(err, float(np.linalg.norm(ym - y6) / np.linalg.norm(y6)))
+    parity = None
+    if sample_parity:
+        # the oracle's own build and product of one member per forest (its
+        # smallest), against that member's rows of both products
+        from oracle.oracle import Oracle, build_port
+
+        build_port()
+        O = Oracle("port")
+        O.set_num_threads(host_cores())
+        worst = {"fp64": 0.0, "mixed": 0.0}
+        for f, a, b in zip(forests, ysm, ys64):
+            q = int(np.argmin(f["ns"]))
+            p = f["pts"][q]
+            ot = O.cluster(p)
+            oh = O.hmatrix(ot, ot, p, p, 1, eps, eta)
+            yo = oh.mvprod(G.rhs(f["ns"][q], f["mu"], seed=10 + f["ks"][q]), f["mu"])
+            for key, y in (("fp64", b), ("mixed", a)):
+                worst[key] = max(worst[key], float(np.linalg.norm(members(f, y)[q] - yo) / np.linalg.norm(yo)))
+        parity = {"max_rel_err": worst, "members_checked": len(forests), "reference": "the CPU oracle's build and product of the smallest member of every forest (oracle/htool_oracle.c, pinned to upstream htool)"}
     peak, peak_src = measured_peaks()
+    free_b, total_b = torch.cuda.mem_get_info()
+    out = {
+        "value": world * total_mu / (msm * 1e-3), "ms_per_step": msm, "fp64_value": world * total_mu / (ms64 * 1e-3), "fp64_ms_per_step": ms64, "mixed_speedup_vs_fp64": ms64 / msm,
+        "max_rel_err_mixed_vs_fp64": err, "rel_err_vs_reference": parity,
+        "whole_batch": {"mixed": {"bytes": bytesm, "GB_per_s": bytesm / (msm * 1e-3) / 1e9, "frac_of_hbm_peak": bytesm / (msm * 1e-3) / 1e9 / peak},
+                        "fp64": {"bytes": bytes64, "GB_per_s": bytes64 / (ms64 * 1e-3) / 1e9, "frac_of_hbm_peak": bytes64 / (ms64 * 1e-3) / 1e9 / peak}, "peak_source": peak_src},
+        "forests": {str(f["mu"]): {"members": len(f["ks"]), "points": f["N"]} for f in forests}, "tuning": {"fp64": info64, "mixed": infom},
+        "count": len(items), "n_total": int(sum(i[0] for i in items)), "rhs_total": total_mu, "build_seconds": build_s, "device_gb_in_use": (total_b - free_b) / 1e9, "clocks": ck,
+    }
+    for f in forests:
+        del f["hm"]
+    return out
+
+
+def run_batched(args):
+    """256 H-matrices in one forest per right-hand-side count, one graph
+    launch per step (replicas under torchrun)"""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    b = batched_workload(local, args.steps, args.warmup, args.count, world)
     line = {
-        "metric": "H-matvec/s over a batch of %d H-matrices (one graph launch per step), mixed vs plain FP64" % len(items),
-        "value": world * total_mu / (ms * 1e-3),
-        "unit": UNIT,
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": max(args.warmup, 3),
-        "ms_per_step": ms,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32/bf16 factors, f64 dense",
-        "data": "synthetic (seeded ellipsoids)",
-        "config": {"workload": "batched_laplace_ellipsoids", "count": len(items), "n_total": int(sum(i[0] for i in items)), "rhs_total": total_mu, "epsilon": WORKLOAD["epsilon"], "eta": WORKLOAD["eta"], "tau": 1.0, "l2": "inputs larger than L2 (%.1f GB per step)" % (nbytes / 1e9)},
-        "max_rel_err_vs_fp64": err,
-        "one_by_one_ms": single_ms,
-        "whole_batch": {"bytes": nbytes, "GB_per_s": nbytes / (ms * 1e-3) / 1e9, "frac_of_hbm_peak": nbytes / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_src},
-        "fp64": {"value": world * total_mu / (ms64 * 1e-3), "ms_per_step": ms64, "one_by_one_ms": single64, "bytes": nbytes64, "GB_per_s": nbytes64 / (ms64 * 1e-3) / 1e9},
-        "build_seconds": build_s,
-        "device_gb_in_use": (total_b - free_b) / 1e9,
-        "clocks": ck,
+        "metric": "H-matvec/s over a batch of %d H-matrices (one graph launch per step), mixed vs plain FP64" % b["count"],
+        "value": b["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/bf16 factors, f64 dense", "data": "synthetic (seeded ellipsoids)",
+        "config": {"workload": "batched_laplace_ellipsoids", "count": b["count"], "n_total": b["n_total"], "rhs_total": b["rhs_total"], "epsilon": WORKLOAD["epsilon"], "eta": WORKLOAD["eta"], "tau": 1.0,
+                   "l2": "inputs larger than L2 (%.1f GB per step)" % (b["whole_batch"]["mixed"]["bytes"] / 1e9)},
+        "batched": b, "clocks": b["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

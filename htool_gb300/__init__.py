@@ -28,6 +28,7 @@ KERNELS = {"inv_r_eps": INV_R_EPS, "laplace": LAPLACE, "helmholtz": HELMHOLTZ}
 
 HOST_PTRS = 1
 CLUSTER_NUMBERING = 2
+GLOBAL_TO_LOCAL = 4  # in: the whole input in cluster numbering; out: the local rows of the handle's rank
 
 PREC_FP64, PREC_FP32, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
 PHASE1_TILES, PHASE1_STREAM = 0, 1
@@ -124,6 +125,16 @@ def _load():
         "htgpu_hmatrix_get_tensor_core_mode": (i, [vp, vp]),
         "htgpu_debug_tc_gemm": (i, [i, vp, vp, vp]),
         "htgpu_debug_set_waits": (i, [i, C.c_longlong, C.c_longlong]),
+        "htgpu_cluster_build_world": (i, [i, vp, i, i, i, vp]),
+        "htgpu_cluster_masteroffset": (i, [vp, vp, vp]),
+        "htgpu_cluster_forest": (i, [i, vp, vp]),
+        "htgpu_hmatrix_set_rhs_bucket": (i, [vp, i, i]),
+        "htgpu_hmatrix_get_rhs_bucket": (i, [vp, i, vp]),
+        "htgpu_cluster_forest_offsets": (i, [vp, vp, vp]),
+        "htgpu_block_tasks_rank": (i, [vp, vp, d, i, vp, vp]),
+        "htgpu_hmatrix_set_local_rank": (i, [vp, i]),
+        "htgpu_hmatrix_local": (i, [vp, vp, vp, vp]),
+        "htgpu_hmatrix_mvprod_global_to_local": (i, [vp, vp, vp, i, u, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -168,15 +179,51 @@ class Cluster:
             raise ValueError("[Htool error] MinClusterSize parameter cannot be zero")
         self.minclustersize = int(m)
 
-    def build(self, nb_pt, x, nb_sons=-1):
+    def build(self, nb_pt, x, nb_sons=-1, size_world=1):
+        """Cluster::build (cluster.hpp:57-92); size_world > 1 builds the tree
+        of a run of that many MPI ranks (the root split into one son per
+        rank, pca.hpp:28), whichever rank calls it."""
         self.points = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
         if self.points.shape[0] != nb_pt:
             raise ValueError("[Htool error] point array does not hold nb_pt points")
         h = C.c_void_p()
-        _check(lib.htgpu_cluster_build(nb_pt, _ptr(self.points), self.minclustersize, nb_sons, C.byref(h)))
+        _check(lib.htgpu_cluster_build_world(nb_pt, _ptr(self.points), self.minclustersize, nb_sons, int(size_world), C.byref(h)))
         self._free()
         self.h = h
         return self
+
+    @classmethod
+    def forest(cls, members):
+        """k independent trees side by side (points concatenated in order):
+        an H-matrix on forests is the block-diagonal union of the members'
+        H-matrices, built and applied at once (no counterpart in htool)."""
+        arr = (C.c_void_p * len(members))(*[m.h for m in members])
+        h = C.c_void_p()
+        _check(lib.htgpu_cluster_forest(len(members), arr, C.byref(h)))
+        f = cls()
+        f.h = h
+        f.members = list(members)
+        f.points = np.concatenate([m.points for m in members])
+        return f
+
+    def get_forest_offsets(self):
+        """the k + 1 point offsets of a forest's members (empty otherwise)"""
+        k = C.c_int()
+        _check(lib.htgpu_cluster_forest_offsets(self.h, C.byref(k), None))
+        if k.value == 0:
+            return np.zeros(0, np.int32)
+        off = np.empty(k.value + 1, np.int32)
+        _check(lib.htgpu_cluster_forest_offsets(self.h, C.byref(k), _ptr(off)))
+        return off
+
+    def get_masteroffset(self):
+        """int[size_world, 2]: (offset, size) of every rank's cluster
+        (cluster.hpp:42, virtual_cluster.hpp:61-62)."""
+        n = C.c_int()
+        _check(lib.htgpu_cluster_masteroffset(self.h, C.byref(n), None))
+        mo = np.empty((n.value, 2), np.int32)
+        _check(lib.htgpu_cluster_masteroffset(self.h, C.byref(n), _ptr(mo)))
+        return mo
 
     def _info(self):
         n, nn, mn, mx = C.c_int(), C.c_int(), C.c_int(), C.c_int()
@@ -250,6 +297,41 @@ def block_tasks(t, s, eta, UPLO="N", force_sym=False):
     _check(lib.htgpu_block_tasks_sym(t.h, s.h, eta, u, int(force_sym), C.byref(n), None))
     out = np.empty((n.value, 5), np.int32)
     _check(lib.htgpu_block_tasks_sym(t.h, s.h, eta, u, int(force_sym), C.byref(n), _ptr(out)))
+    return out
+
+
+def gather_source(x_local, masteroffset, mu=1, group=None):
+    """local_to_global_source (hmatrix.hpp:963-977): every rank's part of an
+    input (its MasterOffset rows in cluster numbering, column-major per
+    right-hand side; a torch tensor) all-gathered over `group`
+    (torch.distributed, the run's ranks in rank order) into the whole input
+    in cluster numbering, column-major.  One rank: the part itself."""
+    import torch
+
+    P = len(masteroffset)
+    sizes = [int(masteroffset[p][1]) * mu for p in range(P)]
+    if P == 1:
+        parts = [x_local.reshape(-1)]
+    else:
+        import torch.distributed as dist
+
+        # parts padded to the largest (gloo gathers equal sizes only)
+        width = max(sizes)
+        mine = torch.zeros(width, dtype=x_local.dtype, device=x_local.device)
+        mine[:x_local.numel()] = x_local.reshape(-1)
+        buf = [torch.empty(width, dtype=x_local.dtype, device=x_local.device) for _ in range(P)]
+        dist.all_gather(buf, mine, group=group)
+        parts = [buf[p][:sizes[p]] for p in range(P)]
+    return torch.cat([torch.cat([parts[p].reshape(mu, -1)[c] for p in range(P)]) for c in range(mu)])
+
+
+def block_tasks_rank(t, s, eta, rank):
+    """Local tasks of MPI rank `rank` on trees of a multi-rank run
+    (blocks.hpp:251-277): int[n,5] as block_tasks."""
+    n = C.c_int()
+    _check(lib.htgpu_block_tasks_rank(t.h, s.h, eta, int(rank), C.byref(n), None))
+    out = np.empty((n.value, 5), np.int32)
+    _check(lib.htgpu_block_tasks_rank(t.h, s.h, eta, int(rank), C.byref(n), _ptr(out)))
     return out
 
 
@@ -616,6 +698,72 @@ class HMatrix:
     def __matmul__(self, x):
         return self.mvprod_global_to_global(x, 1)
 
+    def set_rhs_bucket(self, mu, mu_run):
+        """products with mu (1..8) right-hand sides run padded with zero
+        columns to mu_run (0: unpadded); autotune(mu) picks the faster"""
+        _check(lib.htgpu_hmatrix_set_rhs_bucket(self.h, int(mu), int(mu_run)))
+
+    def get_rhs_bucket(self, mu):
+        v = C.c_int()
+        _check(lib.htgpu_hmatrix_get_rhs_bucket(self.h, int(mu), C.byref(v)))
+        return v.value
+
+    # -- a rank of a multi-rank run (htool's local products) ----------------
+    def set_local_rank(self, rank):
+        """Hold the local rows of MPI rank `rank` of the run the cluster trees
+        were built for (Cluster.build(..., size_world=P)); before build."""
+        _check(lib.htgpu_hmatrix_set_local_rank(self.h, int(rank)))
+        return self
+
+    def get_local_rank(self):
+        return self._local()[0]
+
+    def get_local_offset(self):
+        return self._local()[1]
+
+    def get_local_size(self):
+        return self._local()[2]
+
+    def _local(self):
+        r, o, n = C.c_int(), C.c_int(), C.c_int()
+        _check(lib.htgpu_hmatrix_local(self.h, C.byref(r), C.byref(o), C.byref(n)))
+        return r.value, o.value, n.value
+
+    def mymvprod_global_to_local(self, x, mu=1):
+        """mymvprod_global_to_local (hmatrix.hpp:844-911) on host arrays: x
+        the whole input in cluster numbering (column-major, mu right-hand
+        sides), the local rows out."""
+        nr, nc, _, _ = self.sizes()
+        ls = self.get_local_size()
+        dt = np.complex128 if self.complex else np.float64
+        f = 2 if self.complex else 1
+        x = np.ascontiguousarray(x, dtype=dt)
+        if f * x.size != nc * mu:
+            raise ValueError("[Htool error] input has %d entries, expected %d" % (x.size, nc * mu // f))
+        y = np.empty(ls * mu, dt)
+        _check(lib.htgpu_hmatrix_mvprod_global_to_local(self.h, _ptr(x), _ptr(y), mu, HOST_PTRS, None))
+        return y
+
+    def mymvprod_local_to_local(self, x_local, mu=1, group=None):
+        """mymvprod_local_to_local (hmatrix.hpp:980-996), what HPDDM's GMV
+        calls: this rank's part of the input (cluster numbering, column-major)
+        is all-gathered over `group` (torch.distributed; the ranks of the run
+        in rank order), then the product of the local rows is taken.  Host
+        arrays in and out; torch tensors also work (then on their device)."""
+        import torch
+
+        if not torch.is_tensor(x_local):
+            x_local = torch.from_numpy(np.ascontiguousarray(x_local))
+        xg = gather_source(x_local, self.s.get_masteroffset(), mu, group)
+        if xg.is_cuda:
+            ls = self.get_local_size()
+            y = torch.empty(ls * mu, dtype=xg.dtype, device=xg.device)
+            xr = torch.view_as_real(xg) if xg.is_complex() else xg
+            yr = torch.view_as_real(y) if y.is_complex() else y
+            _check(lib.htgpu_hmatrix_mvprod_global_to_local(self.h, C.c_void_p(xr.data_ptr()), C.c_void_p(yr.data_ptr()), mu, 0, C.c_void_p(torch.cuda.current_stream(xg.device).cuda_stream or 1)))
+            return y
+        return torch.from_numpy(self.mymvprod_global_to_local(xg.numpy(), mu))
+
     def save(self, path):
         """Binary dump of the leaves and factors (reloadable with load)."""
         _check(lib.htgpu_hmatrix_save(self.h, str(path).encode()))
@@ -743,7 +891,8 @@ class HBatch:
 
     def add(self, hmatrix, x_ptr, y_ptr, mu=1, keep=None, flags=0):
         """y = H x on device pointers (CLUSTER_NUMBERING in flags: cluster
-        numbering); `keep` (e.g. the tensors) is held alive."""
+        numbering; GLOBAL_TO_LOCAL: a rank's local rows); `keep` (e.g. the
+        tensors) is held alive."""
         idx = C.c_int()
         _check(lib.htgpu_batch_add_flags(self.h, hmatrix.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), int(mu), int(flags), C.byref(idx)))
         self._keep.append((hmatrix, keep))

@@ -26,11 +26,11 @@ void Batch::release() {
     streams_.clear();
 }
 
-int Batch::add(HMatrix *h, const double *x, double *y, int mu, bool cluster_numbering) {
+int Batch::add(HMatrix *h, const double *x, double *y, int mu, int numbering) {
     require(h != nullptr && x != nullptr && y != nullptr, "batch entries need an H-matrix and device input and output");
     require(mu >= 1, "number of right-hand sides must be positive");
     require(h->device() == device_, "H-matrix on another device than the batch");
-    entries_.push_back({h, x, y, mu, cluster_numbering, 0});
+    entries_.push_back({h, x, y, mu, numbering, 0});
     release(); // a new entry invalidates the captured graph
     return (int)entries_.size() - 1;
 }
@@ -43,7 +43,7 @@ void Batch::capture(int nstreams) {
     // one product per entry outside the capture: work buffers and first-use
     // settings are in place before any launch is recorded
     for (auto &e : entries_)
-        e.h->mvprod(e.x, e.y, e.mu, false, e.cluster, nullptr);
+        e.h->mvprod(e.x, e.y, e.mu, false, e.numbering, nullptr);
     for (auto &e : entries_)
         e.h->sync();
     nstreams = std::min<int>(nstreams, (int)entries_.size());
@@ -66,7 +66,7 @@ void Batch::capture(int nstreams) {
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return entries_[a].h->stored_bytes() * entries_[a].mu > entries_[b].h->stored_bytes() * entries_[b].mu; });
     for (std::size_t i = 0; i < order.size(); i++) {
         const Entry &e = entries_[order[i]];
-        e.h->mvprod(e.x, e.y, e.mu, false, e.cluster, streams_[1 + i % nstreams]);
+        e.h->mvprod(e.x, e.y, e.mu, false, e.numbering, streams_[1 + i % nstreams]);
     }
     for (int k = 1; k <= nstreams; k++) {
         HTGPU_CUDA(cudaEventRecord(events_[k], streams_[k]));

@@ -13,10 +13,10 @@ class Batch {
     ~Batch();
     Batch(const Batch &)            = delete;
     Batch &operator=(const Batch &) = delete;
-    // y = H x with mu right-hand sides (device memory, user numbering, or
-    // cluster numbering with cluster_numbering); the H-matrix and the
-    // buffers must outlive the batch's launches
-    int add(HMatrix *h, const double *x, double *y, int mu, bool cluster_numbering = false);
+    // y = H x with mu right-hand sides (device memory; numbering as
+    // HMatrix::mvprod: user, cluster, or global-to-local); the H-matrix and
+    // the buffers must outlive the batch's launches
+    int add(HMatrix *h, const double *x, double *y, int mu, int numbering = kUserNumbering);
     // record every product (on up to nstreams concurrent streams) as one graph
     void capture(int nstreams);
     void launch(cudaStream_t st); // NULL: the batch's own stream
@@ -31,7 +31,7 @@ class Batch {
         const double *x;
         double *y;
         int mu;
-        bool cluster; // cluster numbering
+        int numbering; // as HMatrix::mvprod
         unsigned long long gen; // layout generation at capture
     };
     int device_;

@@ -75,6 +75,58 @@ int htgpu_cluster_build(int n, const double *xyz, int minclustersize, int nb_son
     });
 }
 
+int htgpu_cluster_build_world(int n, const double *xyz, int minclustersize, int nb_sons, int size_world, htgpu_cluster *out) {
+    return guarded([&] {
+        need(xyz, "xyz");
+        need(out, "out");
+        htgpu::require(n >= 2, "a cluster tree needs at least two points");
+        auto *c = new htgpu_cluster_s;
+        c->tree = std::make_shared<htgpu::ClusterTree>(htgpu::build_cluster_tree(n, xyz, minclustersize, nb_sons, size_world));
+        *out    = c;
+    });
+}
+
+int htgpu_cluster_forest(int k, const htgpu_cluster *members, htgpu_cluster *out) {
+    return guarded([&] {
+        need(members, "members");
+        need(out, "out");
+        htgpu::require(k >= 1, "a forest needs at least one tree");
+        std::vector<const htgpu::ClusterTree *> m(k);
+        for (int q = 0; q < k; q++) {
+            need(members[q], "member cluster");
+            m[q] = members[q]->tree.get();
+        }
+        auto *c = new htgpu_cluster_s;
+        c->tree = std::make_shared<htgpu::ClusterTree>(htgpu::build_forest(m));
+        *out    = c;
+    });
+}
+
+int htgpu_cluster_forest_offsets(htgpu_cluster c, int *k, int *offsets) {
+    return guarded([&] {
+        need(c, "cluster");
+        need(k, "k");
+        const auto &T = *c->tree;
+        *k            = (int)T.forest_roots.size();
+        if (offsets)
+            std::copy(T.forest_offsets.begin(), T.forest_offsets.end(), offsets);
+    });
+}
+
+int htgpu_cluster_masteroffset(htgpu_cluster c, int *size_world, int *mo) {
+    return guarded([&] {
+        need(c, "cluster");
+        need(size_world, "size_world");
+        const auto &T = *c->tree;
+        *size_world   = T.size_world();
+        if (mo)
+            for (int p = 0; p < T.size_world(); p++) {
+                mo[2 * p]     = T.rank_cluster(p).offset;
+                mo[2 * p + 1] = T.rank_cluster(p).size;
+            }
+    });
+}
+
 int htgpu_cluster_destroy(htgpu_cluster c) {
     return guarded([&] { delete c; });
 }
@@ -125,7 +177,8 @@ int htgpu_cluster_get_nodes(htgpu_cluster c, int *node_i, double *node_d) {
 
 int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks, int *out) { return htgpu_block_tasks_sym(t, s, eta, 'N', 0, ntasks, out); }
 
-int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char uplo, int force_sym, int *ntasks, int *out) {
+namespace {
+int block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, char uplo, int force_sym, int rank, int *ntasks, int *out) {
     return guarded([&] {
         need(t, "target cluster");
         need(s, "source cluster");
@@ -134,6 +187,7 @@ int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char upl
         htgpu::BlockTreeParams p;
         p.eta      = eta;
         p.uplo     = uplo;
+        p.rank     = rank;
         p.sym_tree = uplo != 'N' || force_sym != 0;
         auto tasks = htgpu::build_local_tasks(*t->tree, *s->tree, p);
         *ntasks    = (int)tasks.size();
@@ -149,6 +203,11 @@ int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char upl
             }
     });
 }
+} // namespace
+
+int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char uplo, int force_sym, int *ntasks, int *out) { return block_tasks(t, s, eta, uplo, force_sym, 0, ntasks, out); }
+
+int htgpu_block_tasks_rank(htgpu_cluster t, htgpu_cluster s, double eta, int rank, int *ntasks, int *out) { return block_tasks(t, s, eta, 'N', 0, rank, ntasks, out); }
 
 int htgpu_hmatrix_create(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out) {
     return guarded([&] {
@@ -342,10 +401,62 @@ int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const
     });
 }
 
+namespace {
+int numbering_of(unsigned int flags) {
+    htgpu::require((flags & ~(HTGPU_HOST_PTRS | HTGPU_CLUSTER_NUMBERING | HTGPU_GLOBAL_TO_LOCAL)) == 0, "unknown product flags");
+    htgpu::require(!((flags & HTGPU_CLUSTER_NUMBERING) && (flags & HTGPU_GLOBAL_TO_LOCAL)), "HTGPU_CLUSTER_NUMBERING and HTGPU_GLOBAL_TO_LOCAL exclude each other");
+    return (flags & HTGPU_GLOBAL_TO_LOCAL) ? htgpu::kGlobalToLocal : (flags & HTGPU_CLUSTER_NUMBERING) ? htgpu::kClusterNumbering : htgpu::kUserNumbering;
+}
+} // namespace
+
 int htgpu_hmatrix_mvprod(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream) {
     return guarded([&] {
         need(h, "hmatrix");
-        h->h->mvprod(in, out, mu, (flags & HTGPU_HOST_PTRS) != 0, (flags & HTGPU_CLUSTER_NUMBERING) != 0, (cudaStream_t)stream);
+        h->h->mvprod(in, out, mu, (flags & HTGPU_HOST_PTRS) != 0, numbering_of(flags), (cudaStream_t)stream);
+    });
+}
+
+int htgpu_hmatrix_mvprod_global_to_local(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        htgpu::require((flags & ~HTGPU_HOST_PTRS) == 0, "the global-to-local product takes HTGPU_HOST_PTRS only");
+        h->h->mvprod(in, out, mu, (flags & HTGPU_HOST_PTRS) != 0, htgpu::kGlobalToLocal, (cudaStream_t)stream);
+    });
+}
+
+int htgpu_hmatrix_set_local_rank(htgpu_hmatrix h, int rank) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_local_rank(rank);
+    });
+}
+
+int htgpu_hmatrix_set_rhs_bucket(htgpu_hmatrix h, int mu, int mu_run) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_rhs_bucket(mu, mu_run);
+    });
+}
+
+int htgpu_hmatrix_get_rhs_bucket(htgpu_hmatrix h, int mu, int *mu_run) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(mu_run, "mu_run");
+        htgpu::require(mu >= 1, "number of right-hand sides must be positive");
+        *mu_run = h->h->rhs_run(mu);
+    });
+}
+
+int htgpu_hmatrix_local(htgpu_hmatrix h, int *rank, int *local_offset, int *local_size) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        const int f = h->h->is_complex() ? 2 : 1; // complex handles count complex rows
+        if (rank)
+            *rank = h->h->local_rank();
+        if (local_offset)
+            *local_offset = h->h->local_row_offset() / f;
+        if (local_size)
+            *local_size = h->h->local_row_count() / f;
     });
 }
 
@@ -728,8 +839,8 @@ int htgpu_batch_add_flags(htgpu_batch b, htgpu_hmatrix h, const double *in, doub
     return guarded([&] {
         need(b, "batch");
         need(h, "hmatrix");
-        htgpu::require((flags & ~HTGPU_CLUSTER_NUMBERING) == 0, "batch entries take device pointers; the only flag is HTGPU_CLUSTER_NUMBERING");
-        const int i = b->b->add(h->h.get(), in, out, mu, (flags & HTGPU_CLUSTER_NUMBERING) != 0);
+        htgpu::require((flags & HTGPU_HOST_PTRS) == 0, "batch entries take device pointers");
+        const int i = b->b->add(h->h.get(), in, out, mu, numbering_of(flags));
         if (index)
             *index = i;
     });

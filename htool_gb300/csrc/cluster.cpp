@@ -112,8 +112,8 @@ struct Pending {
 
 // Assign each point of `pts` to a son.  Two sons: the sign of the
 // projection on `dir` relative to the centre.  Other counts: equal-width
-// slabs between the extreme projections (only the single-son root split
-// of a one-rank run takes that branch).
+// slabs between the extreme projections (the root split into one son per
+// MPI rank, or nb_sons > 2).
 bool split_points(const double *x, const std::vector<int> &pts, const double *ctr, const double *dir, int nsons, std::vector<int> &son) {
     const int n = (int)pts.size();
     son.assign(n, 0);
@@ -174,12 +174,13 @@ std::vector<int> ClusterTree::preorder() const {
     return order;
 }
 
-ClusterTree build_cluster_tree(int n, const double *x, int minclustersize, int nb_sons) {
+ClusterTree build_cluster_tree(int n, const double *x, int minclustersize, int nb_sons, int size_world) {
     require(n > 0, "cluster tree needs at least one point");
     require(minclustersize > 0, "MinClusterSize parameter cannot be zero");
     if (nb_sons == -1)
         nb_sons = 2;
     require(nb_sons >= 2, "Impossible value for nb_sons:" + std::to_string(nb_sons));
+    require(size_world >= 1 && size_world <= n, "the number of MPI ranks must be between 1 and the number of points");
     ClusterTree T;
     T.n              = n;
     T.minclustersize = minclustersize;
@@ -199,7 +200,7 @@ ClusterTree build_cluster_tree(int n, const double *x, int minclustersize, int n
         stack.pop_back();
         const int v     = cur.node;
         const int np    = (int)cur.pts.size();
-        const int nsons = T.nodes[v].depth == 0 ? 1 : nb_sons; // one rank
+        const int nsons = T.nodes[v].depth == 0 ? size_world : nb_sons; // the root: one son per rank
         // centre: (sum of unit masses * x) * (1 / total mass)
         double mass = 0.;
         for (int j = 0; j < np; j++)
@@ -379,19 +380,80 @@ struct BlockBuilder {
 };
 } // namespace
 
+ClusterTree build_forest(const std::vector<const ClusterTree *> &members) {
+    require(!members.empty(), "a forest needs at least one tree");
+    ClusterTree F;
+    const int k = (int)members.size();
+    int n = 0, nn = 2 + k;
+    for (auto *m : members) {
+        require(m != nullptr && !m->nodes.empty(), "a forest member is empty");
+        require(m->forest_roots.empty(), "a forest member cannot be a forest itself");
+        require(m->size_world() == 1, "forest members must be one-rank trees");
+        F.forest_offsets.push_back(n);
+        n += m->n;
+        nn += (int)m->nodes.size() - 1;
+    }
+    F.forest_offsets.push_back(n);
+    F.n              = n;
+    F.minclustersize = members[0]->minclustersize;
+    F.perm.resize(n);
+    F.nodes.resize(nn);
+    ClusterNode &root = F.nodes[0];
+    root.rank = -1, root.depth = 0, root.offset = 0, root.size = n, root.nb_sons = 1, root.first_son = 1;
+    ClusterNode &all = F.nodes[1];
+    all.rank = 0, all.depth = 1, all.offset = 0, all.size = n, all.nb_sons = k, all.first_son = 2, all.parent = 0;
+    int base = 2 + k;
+    for (int q = 0; q < k; q++) {
+        const ClusterTree &m = *members[q];
+        const int off        = F.forest_offsets[q];
+        // member node v -> forest node: the root to 2 + q, the others to base + v - 1
+        auto map = [&](int v) { return v == 0 ? 2 + q : base + v - 1; };
+        for (int v = 0; v < (int)m.nodes.size(); v++) {
+            ClusterNode c = m.nodes[v];
+            c.offset += off;
+            c.first_son = c.nb_sons > 0 ? map(c.first_son) : -1;
+            c.parent    = v == 0 ? 1 : map(c.parent);
+            F.nodes[map(v)] = c;
+        }
+        for (int i = 0; i < m.n; i++)
+            F.perm[off + i] = m.perm[i] + off;
+        F.forest_roots.push_back(2 + q);
+        F.min_depth = F.min_depth < 0 ? m.min_depth : std::min(F.min_depth, m.min_depth);
+        F.max_depth = std::max(F.max_depth, m.max_depth);
+        base += (int)m.nodes.size() - 1;
+    }
+    return F;
+}
+
 std::vector<BlockTask> build_local_tasks(const ClusterTree &T, const ClusterTree &S, const BlockTreeParams &p) {
     BlockBuilder B{T, S, p, {}};
-    bool adm = admissible(T.nodes[0], S.nodes[0], p.eta);
-    if (p.sym_tree ? B.visit_sym(0, 0, adm) : B.visit(0, 0, adm))
-        B.tasks.push_back({0, 0, adm});
-    // local tasks of the single rank: targets of rank 0 (in the triangle
-    // UPLO names), ordered by offsets (blocks.hpp:251-277)
+    require(T.forest_roots.size() == S.forest_roots.size(), "a forest's H-matrix needs forests of as many trees on both sides");
+    if (T.forest_roots.empty()) {
+        bool adm = admissible(T.nodes[0], S.nodes[0], p.eta);
+        if (p.sym_tree ? B.visit_sym(0, 0, adm) : B.visit(0, 0, adm))
+            B.tasks.push_back({0, 0, adm});
+    } else {
+        // a forest: member k's block tree on its own pair of trees only
+        for (std::size_t q = 0; q < T.forest_roots.size(); q++) {
+            const int rt = T.forest_roots[q], rs = S.forest_roots[q];
+            bool adm = admissible(T.nodes[rt], S.nodes[rs], p.eta);
+            if (p.sym_tree ? B.visit_sym(rt, rs, adm) : B.visit(rt, rs, adm))
+                B.tasks.push_back({rt, rs, adm});
+        }
+    }
+    // local tasks of rank p.rank: targets of that rank (in the triangle
+    // UPLO names, sources beyond the local rows always kept), ordered by
+    // offsets (blocks.hpp:251-277)
+    require(p.rank >= 0 && p.rank < T.size_world(), "rank outside the cluster tree's MPI ranks");
+    const int loff = T.rank_cluster(p.rank).offset, lend = loff + T.rank_cluster(p.rank).size;
     std::vector<BlockTask> local;
     for (auto &b : B.tasks) {
-        if (T.nodes[b.t].rank != 0)
+        if (T.nodes[b.t].rank != p.rank)
             continue;
         const int to = T.nodes[b.t].offset, so = S.nodes[b.s].offset;
-        if ((p.uplo == 'L' && so > to) || (p.uplo == 'U' && so < to))
+        if (p.uplo == 'L' && !(so <= to || so >= lend))
+            continue;
+        if (p.uplo == 'U' && !(so >= to || so < loff))
             continue;
         local.push_back(b);
     }
@@ -420,6 +482,8 @@ ClusterTree double_tree(const ClusterTree &T) {
         c.offset *= 2;
         c.size *= 2;
     }
+    for (auto &o : D.forest_offsets)
+        o *= 2;
     return D;
 }
 

@@ -101,6 +101,13 @@ void HMatrix::set_symmetry(char symmetry, char uplo) {
     uplo_     = uplo;
 }
 
+void HMatrix::set_local_rank(int rank) {
+    require(rank >= 0 && rank < T->size_world(), "rank " + std::to_string(rank) + " outside the " + std::to_string(T->size_world()) + " MPI ranks the target cluster tree was built for");
+    require(S->size_world() == T->size_world(), "target and source cluster trees built for different numbers of MPI ranks");
+    require(lr_h.empty() && dn_h.empty(), "the local rank must be set before the H-matrix is built");
+    bp.rank = rank;
+}
+
 // the fill of dense leaf d: complex Hermitian H-matrices conjugate the twins
 // of the stored off-diagonal blocks (B^H of a symmetric generator's B is
 // conj(B^T)) and complete the diagonal blocks from their UPLO triangle with
@@ -177,6 +184,7 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
     samples_y_.clear();
     const double t0 = now();
     bp.eta          = eta_;
+    require(T->size_world() == 1 || (symmetry_ == 'N' && !force_sym), "symmetric H-matrices of multi-rank runs are not built here: their twins cross the ranks' rows");
     bp.sym_tree     = uplo_ != 'N' || force_sym; // Block::build (blocks.hpp:237-246)
     bp.uplo         = uplo_;
     std::vector<BlockTask> tasks = build_local_tasks(Ta, Sa, bp);
@@ -764,7 +772,8 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     // z sums: target rows cut at every group boundary into atoms; every atom
     // lists the z bases of the groups covering it, largest group first
     {
-        std::vector<int> cuts{0, nr};
+        const int loff = local_row_offset(), lend = loff + local_row_count();
+        std::vector<int> cuts{0, nr, loff, lend}; // the local rows are whole atoms
         for (auto &gk : groups) {
             cuts.push_back(gk.first);
             cuts.push_back(gk.first + gk.second);
@@ -793,6 +802,13 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
             zsum_reads_ += (long long)zi.h * (zi.lend - zi.lbeg);
             zi_h.push_back(zi);
         }
+        // the atoms of the local rows (global-to-local products write only these)
+        zloc0_ = zloc1_ = 0;
+        while (zloc0_ < natoms && cuts[zloc0_] < loff)
+            zloc0_++;
+        zloc1_ = zloc0_;
+        while (zloc1_ < natoms && cuts[zloc1_] < lend)
+            zloc1_++;
     }
     arena_len = off;
     fac.alloc(std::max<long long>(off, 2));
@@ -862,23 +878,25 @@ void HMatrix::ensure_work(int mu) {
     mu_cap = mu;
 }
 
-void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, bool cluster_numbering, cudaStream_t st) {
+void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, int numbering, cudaStream_t st) {
     require(mu >= 1, "number of right-hand sides must be positive");
     require(in != nullptr && out != nullptr, "null input or output");
+    require(numbering >= kUserNumbering && numbering <= kGlobalToLocal, "unknown product numbering");
     HTGPU_CUDA(cudaSetDevice(device_));
     if (!st)
         st = stream_;
-    ensure_work(mu);
+    ensure_work(rhs_run(mu));
     const double *x = in;
     double *y       = out;
+    const std::size_t nout = (std::size_t)(numbering == kGlobalToLocal ? local_row_count() : nr) * mu;
     if (host_ptrs) {
         HTGPU_CUDA(cudaMemcpyAsync(xstage.p, in, sizeof(double) * (std::size_t)nc * mu, cudaMemcpyHostToDevice, st));
         x = xstage.p;
         y = ystage.p;
     }
-    launch_product(x, y, mu, cluster_numbering, st);
+    launch_product(x, y, mu, numbering, st);
     if (host_ptrs) {
-        HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * (std::size_t)nr * mu, cudaMemcpyDeviceToHost, st));
+        HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * nout, cudaMemcpyDeviceToHost, st));
         HTGPU_CUDA(cudaStreamSynchronize(st));
         int status = 0;
         HTGPU_CUDA(cudaMemcpy(&status, status_d.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1155,7 +1173,16 @@ void HMatrix::get_fp64_split(int *p1, int *n64) const {
     *n64 = emu_ok_ ? p2_n64_ : 1000;
 }
 
-void HMatrix::launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st) { launch_product_with(x, y, mu, cluster_numbering, st, xp.p, xs.p, xexp.p, A.p, z.p); }
+void HMatrix::launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st) { launch_product_with(x, y, mu, numbering, st, xp.p, xs.p, xexp.p, A.p, z.p, nullptr, rhs_run(mu)); }
+
+int HMatrix::rhs_run(int mu) const { return mu < (int)rhs_pad_.size() && rhs_pad_[mu] > mu ? rhs_pad_[mu] : mu; }
+
+void HMatrix::set_rhs_bucket(int mu, int mu_run) {
+    require(mu >= 1 && mu < (int)rhs_pad_.size(), "right-hand-side buckets cover 1 to " + std::to_string(rhs_pad_.size() - 1) + " right-hand sides");
+    require(mu_run == 0 || (mu_run >= mu && mu_run < (int)rhs_pad_.size()), "a bucket runs at least the product's right-hand sides and at most " + std::to_string(rhs_pad_.size() - 1));
+    rhs_pad_[mu] = mu_run;
+    layout_gen_++; // captured products are stale
+}
 
 // Reduced-precision copy of the low-rank factors (see mixed.cu): column
 // maxima from the FP64 blocks, per-column precision on the host, then one
@@ -1405,11 +1432,15 @@ void HMatrix::set_precision(int policy, double tau) {
 // The phase-1 tiles on the FP64 pipe and those on the emulation run as two
 // kernels on two streams at once (fork/join through events), so each keeps
 // its own register budget and both pipe families work together.
-void HMatrix::launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks) {
+void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks,
+                                  int mu_run) {
+    // a product padded up to its right-hand-side bucket runs mu columns, the
+    // ones past mu_out zero, and writes mu_out
+    const int mu     = std::max(mu_out, mu_run);
     const int groups = rhs_groups(mu);
     launches_        = 0;
-    launch_xexp(x, (long long)nc * mu, w_xexp, st);
-    launch_gather_split(x, nc, cluster_numbering ? nullptr : perm_s.p, nc, mu, w_xexp, w_xp, w_xs, st);
+    launch_xexp(x, (long long)nc * mu_out, w_xexp, st);
+    launch_gather_split(x, nc, numbering == kUserNumbering ? perm_s.p : nullptr, nc, mu, w_xexp, w_xp, w_xs, st, mu_out);
     launches_ += 2;
     if (marks)
         HTGPU_CUDA(cudaEventRecord(marks[0], st));
@@ -1455,7 +1486,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
                                  (int)zlen_, status_d.p, st);
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
-        launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
+        launch_sums(y, mu_out, numbering, w_z, st);
         launches_ += groups + 1;
         return;
     }
@@ -1507,8 +1538,17 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu, bool clust
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
     }
-    launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, cluster_numbering ? nullptr : perm_t.p, y, nr, st);
+    launch_sums(y, mu_out, numbering, w_z, st);
     launches_ += 1;
+}
+
+// the per-cluster sums into y: every row in user or cluster numbering, or
+// (global-to-local products) the local rows only, at y[i - local offset]
+void HMatrix::launch_sums(double *y, int mu, int numbering, const double *w_z, cudaStream_t st) {
+    if (numbering == kGlobalToLocal)
+        launch_zsum(zi_d.p + zloc0_, zloc1_ - zloc0_, zl_d.p, w_z, (int)zlen_, mu, nullptr, y, local_row_count(), st, local_row_offset());
+    else
+        launch_zsum(zi_d.p, (int)zi_h.size(), zl_d.p, w_z, (int)zlen_, mu, numbering == kUserNumbering ? perm_t.p : nullptr, y, nr, st);
 }
 
 void HMatrix::set_tensor_core_mode(int mode) {
@@ -1542,7 +1582,11 @@ void HMatrix::set_presplit(bool on) {
 
 void HMatrix::autotune(int mu, int reps, float *best_ms) {
     HTGPU_CUDA(cudaSetDevice(device_));
-    ensure_work(mu);
+    int bucket = 1; // the power of two a product with mu right-hand sides may be padded to
+    while (bucket < mu)
+        bucket <<= 1;
+    const bool try_bucket = mu < (int)rhs_pad_.size() && bucket != mu;
+    ensure_work(try_bucket ? bucket : std::max(mu, rhs_run(mu)));
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
     cudaEvent_t e0, e1;
     HTGPU_CUDA(cudaEventCreate(&e0));
@@ -1622,6 +1666,18 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         best     = b2;
         layout_gen_++;
     }
+    // the right-hand-side bucket: 3, 5, 6 or 7 right-hand sides run in
+    // groups of 4, 2 and 1 (one pass over the factors each), or in one pass
+    // padded with zero columns up to the next power of two; the faster stays
+    if (try_bucket) {
+        rhs_pad_[mu]        = 0;
+        const float t_split = timed();
+        rhs_pad_[mu]        = bucket;
+        const float t_pad   = timed();
+        rhs_pad_[mu]        = t_pad < t_split ? bucket : 0;
+        best                = std::min(t_split, t_pad);
+        layout_gen_++;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_ms)
@@ -1630,7 +1686,7 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
 
 void HMatrix::profile(int mu, int reps, float *ms) {
     HTGPU_CUDA(cudaSetDevice(device_));
-    ensure_work(mu);
+    ensure_work(rhs_run(mu));
     cudaEvent_t ev[5];
     for (auto &e : ev)
         HTGPU_CUDA(cudaEventCreate(&e));
@@ -1638,7 +1694,7 @@ void HMatrix::profile(int mu, int reps, float *ms) {
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
     for (int r = 0; r < reps; r++) {
         HTGPU_CUDA(cudaEventRecord(ev[0], stream_));
-        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1);
+        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1, rhs_run(mu));
         HTGPU_CUDA(cudaEventRecord(ev[4], stream_));
         HTGPU_CUDA(cudaEventSynchronize(ev[4]));
         float t;

@@ -19,6 +19,9 @@ struct HostGen {
 };
 constexpr int kHostKernelId = 3; // kernel id of a host generator in the rank predictor's features
 
+// numbering of a product's input and output
+constexpr int kUserNumbering = 0, kClusterNumbering = 1, kGlobalToLocal = 2;
+
 int host_threads();
 void host_parallel_for(long long n, const std::function<void(long long)> &body);
 void call_generator(const HostGen &g, int M, int N, const int *rows, const int *cols, double *ptr);
@@ -120,8 +123,12 @@ class HMatrix {
 
     // y = H x for mu right-hand sides (column-major, leading dims nc / nr).
     // host_ptrs: in/out are host memory (copied through device staging);
-    // cluster_numbering: in/out are already in cluster order.
-    void mvprod(const double *in, double *out, int mu, bool host_ptrs, bool cluster_numbering, cudaStream_t st);
+    // numbering: kUserNumbering (htool's mvprod_global_to_global),
+    // kClusterNumbering (in/out already in cluster order), kGlobalToLocal
+    // (in: the whole input in cluster numbering; out: the local rows of
+    // this H-matrix's rank, leading dim local_row_count(); htool's
+    // mymvprod_global_to_local, hmatrix.hpp:844-911)
+    void mvprod(const double *in, double *out, int mu, bool host_ptrs, int numbering, cudaStream_t st);
     // per-launch timing of reps products (ms[0..3]: gather, phase 1, phase 2, total)
     void profile(int mu, int reps, float *ms);
     // the product with device pointers whose working memory is a fixed array
@@ -131,6 +138,14 @@ class HMatrix {
 
     int nb_rows() const { return nr; }
     int nb_cols() const { return nc; }
+    // rank of a multi-rank run whose local rows this H-matrix holds (htool's
+    // local tasks, blocks.hpp:258-273): must be set before the build; the
+    // target tree's depth-1 cluster of that rank gives the local rows
+    // (htool's local_offset / local_size, hmatrix.hpp:320-321)
+    void set_local_rank(int rank);
+    int local_rank() const { return bp.rank; }
+    int local_row_offset() const { return T->rank_cluster(bp.rank).offset; }
+    int local_row_count() const { return T->rank_cluster(bp.rank).size; }
     // htool's leaves: a symmetric H-matrix also applies transposed twins of
     // its off-diagonal leaves, kept after these in lr_h / dn_h
     int n_lowrank() const { return nlr_stored_ >= 0 ? nlr_stored_ : (int)lr_h.size(); }
@@ -174,6 +189,12 @@ class HMatrix {
     // phase 1 with the mma.sync phase 2 (default), 2 tcgen05 in both
     void set_tensor_core_mode(int mode);
     int tensor_core_mode() const { return tc_mode_; }
+    // right-hand-side buckets: a product with mu right-hand sides (1 to 8)
+    // runs padded with zero columns to mu_run (one pass over the factors
+    // instead of one per group of 4, 2, 1); 0 runs it unpadded.  The
+    // autotuner chooses.
+    void set_rhs_bucket(int mu, int mu_run);
+    int rhs_run(int mu) const;
     bool emulation_allowed() const { return emu_ok_; }
     // time every candidate split on the current H-matrix and keep the fastest
     // FP64: phase-1 mode and the DFMA/emulation split; reduced precision:
@@ -257,8 +278,11 @@ class HMatrix {
     std::vector<StreamChunk> ch2_h_; // their phase-2 chunks
     void upload_mixed_phase2();
     bool emu_ok_ = false;
-    void launch_product(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st);
-    void launch_product_with(const double *x, double *y, int mu, bool cluster_numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr);
+    void launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st);
+    // mu_run > mu: padded to that many right-hand sides (zero columns)
+    void launch_product_with(const double *x, double *y, int mu, int numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr,
+                             int mu_run = 0);
+    void launch_sums(double *y, int mu, int numbering, const double *w_z, cudaStream_t st);
     void upload_phase1_lists();
     DevBuf<P1Item> p1e_d; // phase-1 tiles on the emulation (p1_d: on DFMA)
     DevBuf<F2> emu_;          // (hi, lo) split of the phase-1 region of fac, for an all-emulated streamed phase 1 (FP64 products)
@@ -327,6 +351,8 @@ class HMatrix {
     int n_p1_ranges_ = 0, n_p1m_ranges_ = 0;
     int p1_kinds_ = 0, p1m_kinds_ = 1; // element kinds of those chunk lists
     int mu_cap = 0;
+    int zloc0_ = 0, zloc1_ = 0; // the z-sum atoms of the local rows
+    std::vector<int> rhs_pad_ = std::vector<int>(9, 0); // right-hand-side bucket of 1..8 right-hand sides (0: unpadded)
     int launches_ = 0;
     BuildStats st_;
 };

@@ -49,9 +49,27 @@ struct ClusterTree {
     std::vector<ClusterNode> nodes; // construction order; sons contiguous
     int min_depth = -1, max_depth = 0;
     std::vector<int> preorder() const;
+    // MPI ranks the tree was built for: the root has one son per rank, son
+    // p (depth 1) holds rank p's points (htool's MasterOffset[p] = its
+    // offset and size)
+    int size_world() const { return nodes.empty() ? 0 : nodes[0].nb_sons; }
+    const ClusterNode &rank_cluster(int p) const { return nodes[nodes[0].first_son + p]; }
+    // a forest: several independent trees side by side (a batch of
+    // H-matrices stored and applied as one block-diagonal H-matrix).  Node 0
+    // covers every point and has one son, node 1, whose sons are the member
+    // roots (their node indices here, in order); member k's points are
+    // forest_offsets[k] .. forest_offsets[k + 1], and its nodes, ranks and
+    // depths are those of its own tree.  Empty for an ordinary tree.
+    std::vector<int> forest_roots;
+    std::vector<int> forest_offsets;
 };
 
-ClusterTree build_cluster_tree(int n, const double *xyz, int minclustersize, int nb_sons);
+// the forest of the member trees, in order (points concatenated)
+ClusterTree build_forest(const std::vector<const ClusterTree *> &members);
+
+// size_world: the MPI ranks htool's Cluster::build would see (pca.hpp:28:
+// the root is split into one son per rank); 1 for a one-rank run
+ClusterTree build_cluster_tree(int n, const double *xyz, int minclustersize, int nb_sons, int size_world = 1);
 
 // ---------------------------------------------------------------------------
 // block tree (host).  Same algorithm as htool's Block::build (UPLO 'N').
@@ -67,6 +85,7 @@ struct BlockTreeParams {
     std::size_t maxblocksize = 1000000;
     bool sym_tree = false; // Block::build_sym_block_tree (blocks.hpp:140-235)
     char uplo     = 'N';   // local tasks of one triangle: 'U' s.offset >= t.offset, 'L' s.offset <= t.offset
+    int rank      = 0;     // local tasks of this MPI rank: targets inside its depth-1 cluster
 };
 
 bool admissible(const ClusterNode &t, const ClusterNode &s, double eta);

@@ -81,7 +81,9 @@ void launch_xexp(const double *x, long long total, int *xexp, cudaStream_t st);
 void launch_presplit(const double *in, long long n, F2 *out, cudaStream_t st);
 // the same for runs of doubles into a compact mirror
 void launch_presplit_segs(const double *in, const SplitSeg *segs, int nsegs, F2 *out, cudaStream_t st);
-void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st);
+// mu_src >= 0: only the first mu_src columns come from x, the others are
+// zero (a product padded up to a right-hand-side bucket)
+void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st, int mu_src = -1);
 void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, const double *factors, const double *xp, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st);
 void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st);
 // complex conjugate of n interleaved (re, im) doubles (dst may be src)
@@ -89,8 +91,9 @@ void launch_conj(const double *src, double *dst, long long n, cudaStream_t st);
 // the same over float phase-1 sums (reduced-precision products)
 void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st);
 void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st);
-// y[c * ldy + perm[i]] = sum of the partial sums z of the clusters covering row i
-void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st);
+// y[c * ldy + perm[i]] = sum of the partial sums z of the clusters covering
+// row i; without perm, y[c * ldy + i - shift]
+void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st, int shift = 0);
 
 // ---- streamed phase 2 (stream.cu) ------------------------------------------
 // warps claim the chunk ranges rbeg[r] .. rbeg[r+1] (r < nranges) through

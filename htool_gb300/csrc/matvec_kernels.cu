@@ -48,14 +48,16 @@ __global__ void xexp_kernel(const double *__restrict__ x, long long total, int *
         atomicMax(xexp, m);
 }
 
-// xp[j*mu + c] = x[c*ldx + perm[j]] and xs = split(xp * 2^(1023 - xexp))
-__global__ void gather_split_kernel(const double *__restrict__ x, int ldx, const int *__restrict__ perm, int n, int mu, const int *__restrict__ xexp, double *__restrict__ xp, F2 *__restrict__ xs) {
+// xp[j*mu + c] = x[c*ldx + perm[j]] and xs = split(xp * 2^(1023 - xexp));
+// columns c >= mu_src (padding up to a right-hand-side bucket) are zero
+__global__ void gather_split_kernel(const double *__restrict__ x, int ldx, const int *__restrict__ perm, int n, int mu, int mu_src, const int *__restrict__ xexp, double *__restrict__ xp,
+                                    F2 *__restrict__ xs) {
     const long long total = (long long)n * mu;
     const int shift       = 1023 - max(*xexp, 1);
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
         int j = (int)(e / mu), c = (int)(e % mu);
         int src        = perm ? perm[j] : j;
-        const double v = x[(long long)c * ldx + src];
+        const double v = c < mu_src ? x[(long long)c * ldx + src] : 0.;
         xp[e]          = v;
         const int ex   = (int)(((unsigned)__double2hiint(v) >> 20) & 0x7FFu);
         xs[e]          = (ex == 0 || ex + shift < 1) ? F2{0.f, 0.f} : split64(scale_pow2(v, shift));
@@ -288,9 +290,10 @@ __global__ void block_copy_kernel(const BlockCopy *__restrict__ items, const dou
     }
 }
 
-// y[c * ldy + perm[i]] = sum over the covering clusters (largest first) of z
+// y[c * ldy + perm[i]] (no perm: i - shift) = sum over the covering
+// clusters (largest first) of z
 __global__ void zsum_kernel(const ZItem *__restrict__ items, int nitems, const int *__restrict__ zl, const double *__restrict__ z, int zlen, int mu, const int *__restrict__ perm,
-                            double *__restrict__ y, int ldy) {
+                            double *__restrict__ y, int ldy, int shift) {
     const int w    = blockIdx.x * 8 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= nitems)
@@ -298,7 +301,7 @@ __global__ void zsum_kernel(const ZItem *__restrict__ items, int nitems, const i
     const ZItem it = items[w];
     for (int r = lane; r < it.h; r += 32) {
         const int i   = it.row0 + r;
-        const int dst = perm ? perm[i] : i;
+        const int dst = perm ? perm[i] : i - shift;
         for (int c = 0; c < mu; c++) {
             double s = 0.;
             for (int l = it.lbeg; l < it.lend; l++)
@@ -387,12 +390,12 @@ void launch_presplit(const double *in, long long n, F2 *out, cudaStream_t st) {
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st) {
+void launch_gather_split(const double *x, int ldx, const int *perm, int n, int mu, const int *xexp, double *xp, F2 *xs, cudaStream_t st, int mu_src) {
     long long total = (long long)n * mu;
     if (total <= 0)
         return;
     int blocks = (int)std::min<long long>((total + 255) / 256, (long long)sm_count() * 16);
-    gather_split_kernel<<<blocks, 256, 0, st>>>(x, ldx, perm, n, mu, xexp, xp, xs);
+    gather_split_kernel<<<blocks, 256, 0, st>>>(x, ldx, perm, n, mu, mu_src < 0 ? mu : mu_src, xexp, xp, xs);
     HTGPU_CUDA(cudaGetLastError());
 }
 
@@ -444,10 +447,10 @@ void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int m
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st) {
+void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z, int zlen, int mu, const int *perm, double *y, int ldy, cudaStream_t st, int shift) {
     if (nitems <= 0)
         return;
-    zsum_kernel<<<(nitems + 7) / 8, 256, 0, st>>>(items, nitems, zl, z, zlen, mu, perm, y, ldy);
+    zsum_kernel<<<(nitems + 7) / 8, 256, 0, st>>>(items, nitems, zl, z, zlen, mu, perm, y, ldy, shift);
     HTGPU_CUDA(cudaGetLastError());
 }
 

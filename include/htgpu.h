@@ -30,6 +30,7 @@ extern "C" {
 /* flags of the product entry points */
 #define HTGPU_HOST_PTRS 1u         /* in/out are host memory; the call is synchronous */
 #define HTGPU_CLUSTER_NUMBERING 2u /* in/out are in cluster (permuted) order: no permutation */
+#define HTGPU_GLOBAL_TO_LOCAL 4u   /* in: the whole input in cluster order; out: the local rows of the handle's MPI rank */
 
 /* built-in device generators (the device-generator variant of
  * VirtualGenerator<T>::copy_submatrix, include/htool/types/virtual_generator.hpp:22) */
@@ -59,6 +60,32 @@ int htgpu_version(int *major, int *minor);
  * centres and radii are bit-identical to htool's. */
 int htgpu_cluster_build(int n, const double *xyz, int minclustersize, int nb_sons, htgpu_cluster *out);
 int htgpu_cluster_destroy(htgpu_cluster c);
+
+/* The same build as rank `rank` of a run of size_world MPI ranks would do it
+ * (cluster.hpp:57-92 with MPI_Comm_size = size_world): the root is split
+ * into one son per rank (pca.hpp:28), son p holding rank p's points
+ * (pca.hpp:93-99).  The tree does not depend on the rank, which only picks
+ * the local cluster; htgpu_hmatrix_set_local_rank gives it to an H-matrix.
+ * size_world = 1 is htgpu_cluster_build. */
+int htgpu_cluster_build_world(int n, const double *xyz, int minclustersize, int nb_sons, int size_world, htgpu_cluster *out);
+
+/* A forest (no counterpart in the reference): k independent cluster trees
+ * side by side, their points concatenated in order (member q's points are
+ * offsets[q] .. offsets[q + 1]).  An H-matrix on forests holds the
+ * block-diagonal union of the members' H-matrices: each member's block tree
+ * is htool's on its own pair of trees (no block couples two members), so a
+ * build, a product or a batch launch handles every member at once.  Inputs
+ * and outputs are the members' vectors concatenated (user numbering of each
+ * member shifted by its offset).  Members must be one-rank trees. */
+int htgpu_cluster_forest(int k, const htgpu_cluster *members, htgpu_cluster *out);
+/* *k and, when offsets != NULL, the k + 1 member offsets of a forest (k = 0
+ * for an ordinary tree). */
+int htgpu_cluster_forest_offsets(htgpu_cluster c, int *k, int *offsets);
+
+/* get_masteroffset (cluster.hpp:42, virtual_cluster.hpp:61-62):
+ * *size_world, and when mo != NULL, mo[2 p] = offset and mo[2 p + 1] =
+ * size of rank p's cluster (cluster numbering). */
+int htgpu_cluster_masteroffset(htgpu_cluster c, int *size_world, int *mo);
 
 /* A cluster tree built elsewhere, e.g. any htool VirtualCluster
  * (include/htool/clustering/virtual_cluster.hpp:28-40) walked in pre-order:
@@ -90,6 +117,11 @@ int htgpu_block_tasks(htgpu_cluster t, htgpu_cluster s, double eta, int *ntasks,
  * uplo != 'N' or force_sym the tree is build_sym_block_tree's
  * (blocks.hpp:140-235). */
 int htgpu_block_tasks_sym(htgpu_cluster t, htgpu_cluster s, double eta, char uplo, int force_sym, int *ntasks, int *out);
+
+/* Block::build(UPLO = 'N') local task list of MPI rank `rank` of the run
+ * the trees were built for (blocks.hpp:251-277: tasks whose target cluster
+ * belongs to that rank, sorted by offsets). */
+int htgpu_block_tasks_rank(htgpu_cluster t, htgpu_cluster s, double eta, int rank, int *ntasks, int *out);
 
 /* ---------------------------------------------------------------------------
  * H-matrices (double precision, non-symmetric storage)
@@ -211,6 +243,35 @@ int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const
  * handle's own stream; cudaStreamLegacy / cudaStreamPerThread select the
  * default streams) and returns at once. */
 int htgpu_hmatrix_mvprod(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream);
+
+/* The H-matrix of rank `rank` of a multi-rank run: on trees from
+ * htgpu_cluster_build_world, the build keeps that rank's local tasks only
+ * (htool's HMatrix::build on rank `rank`, hmatrix.hpp:286-341 with
+ * blocks.hpp:258-273).  Call before the build; symmetry 'N' only.  Its
+ * local rows are the rank's target cluster (get_local_offset /
+ * get_local_size, hmatrix.hpp:175-176, set at :320-321). */
+int htgpu_hmatrix_set_local_rank(htgpu_hmatrix h, int rank);
+
+/* Right-hand-side buckets (no counterpart in the reference): products with
+ * mu right-hand sides (1 <= mu <= 8) run padded with zero columns to
+ * mu_run (mu <= mu_run <= 8), one pass over the factors, instead of one
+ * pass per group of 4, 2 and 1; mu_run = 0 runs them unpadded.
+ * htgpu_hmatrix_autotune(h, mu, ...) sets the faster for mu. */
+int htgpu_hmatrix_set_rhs_bucket(htgpu_hmatrix h, int mu, int mu_run);
+int htgpu_hmatrix_get_rhs_bucket(htgpu_hmatrix h, int mu, int *mu_run);
+int htgpu_hmatrix_local(htgpu_hmatrix h, int *rank, int *local_offset, int *local_size);
+
+/* Replaces HMatrix::mymvprod_global_to_local(in, out, mu)
+ * (hmatrix.hpp:844-911), the product behind mymvprod_local_to_local
+ * (:980-996) and HPDDM's GMV (wrappers/wrapper_hpddm.hpp:41-83): `in` is
+ * the whole input in cluster numbering (nb_cols x mu, column-major: what
+ * local_to_global_source all-gathers from the ranks' local parts,
+ * hmatrix.hpp:963-977), `out` the handle's local rows (local_size x mu,
+ * column-major).  The same as htgpu_hmatrix_mvprod with
+ * HTGPU_GLOBAL_TO_LOCAL; flags may add HTGPU_HOST_PTRS.  htool's buffers
+ * are row-major for mu > 1; these are column-major like every product
+ * here (include/htool_gpu.hpp transposes for htool's callers). */
+int htgpu_hmatrix_mvprod_global_to_local(htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, void *stream);
 
 /* nb_rows / nb_cols, get_nlrmat / get_ndmat (hmatrix.hpp:173-187). */
 int htgpu_hmatrix_sizes(htgpu_hmatrix h, int *nr, int *nc, int *nlr, int *ndense);
@@ -439,7 +500,9 @@ int htgpu_batch_add(htgpu_batch b, htgpu_hmatrix h, const double *in, double *ou
  * cluster (local) numbering, htool's mymvprod_local_to_local on one rank
  * (hmatrix.hpp:980-996; mvprod_local_to_local after set_use_permutation(false),
  * :1185-1274): what HPDDM's GMV calls in a Krylov loop
- * (wrappers/wrapper_hpddm.hpp:41-83). */
+ * (wrappers/wrapper_hpddm.hpp:41-83); HTGPU_GLOBAL_TO_LOCAL the product of
+ * htgpu_hmatrix_mvprod_global_to_local (a rank's part of a multi-rank
+ * product, its input already gathered).  Device pointers only. */
 int htgpu_batch_add_flags(htgpu_batch b, htgpu_hmatrix h, const double *in, double *out, int mu, unsigned int flags, int *index);
 int htgpu_batch_capture(htgpu_batch b, int nstreams, long long *graph_nodes);
 int htgpu_batch_launch(htgpu_batch b, void *stream);

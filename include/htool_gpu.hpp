@@ -14,12 +14,20 @@
  * exceptions: HTGPU_ERR_INVALID as std::invalid_argument, everything else as
  * std::logic_error, with the library's "[Htool error] ..." message.
  *
- * Scope: one MPI rank (a communicator of size one: local and global
- * numberings coincide), real (double) H-matrices.  Clusters of any
- * VirtualCluster type are handed over node by node.  The generator passed to
- * build() is called from several threads at once, as htool's own build
- * does.  Compressors: partialACA, sympartialACA and DeviceACA select the
- * device partialACA; any other compressor is refused.
+ * Scope: real (double) H-matrices, one GPU per MPI rank.  On a
+ * communicator of P ranks each rank's GpuHMatrix holds the leaves of its
+ * local tasks (the cluster trees must be htool's trees of that run, with one
+ * son of the root per rank) and the products exchange what htool's do: an
+ * MPI_Allgatherv of the local inputs (local_to_global_source) or of the
+ * local outputs, an MPI_Allreduce for transposed products.  Symmetric
+ * storage needs one rank.  Clusters of any VirtualCluster type are handed
+ * over node by node.  The generator passed to build() is called from
+ * several threads at once, as htool's own build does.  Compressors:
+ * partialACA, sympartialACA and DeviceACA select the device partialACA; any
+ * other compressor is refused.  htool's "my" products take right-hand sides
+ * row by row (in[j * mu + c], hmatrix.hpp:867) and the public ones column by
+ * column; the C ABI is column-major throughout, so the "my" products
+ * transpose around it for mu > 1.
  */
 #ifndef HTOOL_GPU_HPP
 #define HTOOL_GPU_HPP
@@ -142,14 +150,16 @@ class GpuHMatrix : public htool::VirtualHMatrix<double> {
         : t_(t), s_(s), epsilon_(epsilon), eta_(eta), symmetry_(symmetry), uplo_(UPLO), device_(device), comm_(comm) {
         if (!t_ || !s_)
             throw std::invalid_argument("[Htool error] cluster trees are needed");
-        int size = 1;
-        MPI_Comm_size(comm_, &size);
-        if (size != 1)
-            throw std::invalid_argument("[Htool error] GpuHMatrix runs on one MPI rank (one GPU); use a communicator of size one");
+        MPI_Comm_size(comm_, &size_);
+        MPI_Comm_rank(comm_, &rank_);
         if (!(symmetry_ == 'N' && uplo_ == 'N') && !((symmetry_ == 'S' || symmetry_ == 'H') && (uplo_ == 'U' || uplo_ == 'L')))
             throw std::invalid_argument("[Htool error] Invalid arguments to create HMatrix"); // hmatrix.hpp:117-121
         if (symmetry_ == 'H')
             throw std::invalid_argument("[Htool error] Hermitian storage needs a complex H-matrix; GpuHMatrix is real");
+        if ((int)t_->get_masteroffset().size() != size_ || (int)s_->get_masteroffset().size() != size_)
+            throw std::invalid_argument("[Htool error] the cluster trees were not built for this communicator's ranks");
+        if (size_ > 1 && symmetry_ != 'N')
+            throw std::invalid_argument("[Htool error] GpuHMatrix stores symmetric H-matrices on one MPI rank only");
         tc_ = import_cluster(*t_);
         sc_ = t_ == s_ ? tc_ : import_cluster(*s_);
     }
@@ -168,10 +178,10 @@ class GpuHMatrix : public htool::VirtualHMatrix<double> {
     int nb_rows() const override { return t_->get_size(); }
     int nb_cols() const override { return s_->get_size(); }
     MPI_Comm get_comm() const override { return comm_; }
-    int get_rankworld() const override { return 0; }
-    int get_sizeworld() const override { return 1; }
-    int get_local_size() const override { return nb_rows(); }
-    int get_local_offset() const override { return 0; }
+    int get_rankworld() const override { return rank_; }
+    int get_sizeworld() const override { return size_; }
+    int get_local_size() const override { return t_->get_masteroffset(rank_).second; }
+    int get_local_offset() const override { return t_->get_masteroffset(rank_).first; }
     char get_symmetry_type() const override { return symmetry_; }
     char get_storage_type() const override { return uplo_; }
     const htool::VirtualCluster *get_target_cluster() const override { return t_.get(); }
@@ -204,32 +214,143 @@ class GpuHMatrix : public htool::VirtualHMatrix<double> {
     void build(htool::VirtualGenerator<double> &mat, const double *const xt, const double *const xs) override { do_build(mat, xt, xs, false); }
     void build(htool::VirtualGenerator<double> &mat, const double *const xt) override { do_build(mat, xt, xt, true); }
 
-    // ---- products (hmatrix.hpp:844-1455).  On one rank the local part is
-    // the whole matrix: the public products take user numbering (cluster
-    // numbering after set_use_permutation(false)), the "my" products, which
-    // HPDDM's GMV calls (wrappers/wrapper_hpddm.hpp:41-83), cluster numbering
+    // ---- products (hmatrix.hpp:844-1455).  The public products take user
+    // numbering (cluster numbering after set_use_permutation(false)), the
+    // "my" products, which HPDDM's GMV calls (wrappers/wrapper_hpddm.hpp:
+    // 41-83), cluster numbering with the right-hand sides row by row
     void mvprod_global_to_global(const double *const in, double *const out, const int &mu = 1) const override {
-        check(htgpu_hmatrix_mvprod(built(), in, out, mu, HTGPU_HOST_PTRS | (use_permutation_ ? 0u : HTGPU_CLUSTER_NUMBERING), nullptr));
-    }
-    void mvprod_local_to_local(const double *const in, double *const out, const int &mu = 1, double * = nullptr) const override { mvprod_global_to_global(in, out, mu); }
-    void mymvprod_local_to_local(const double *const in, double *const out, const int &mu = 1, double * = nullptr) const override {
-        check(htgpu_hmatrix_mvprod(built(), in, out, mu, HTGPU_HOST_PTRS | HTGPU_CLUSTER_NUMBERING, nullptr));
-    }
-    void mymvprod_global_to_local(const double *const in, double *const out, const int &mu = 1) const override { mymvprod_local_to_local(in, out, mu); }
-    void mvprod_transp_global_to_global(const double *const in, double *const out, const int &mu = 1) const override {
+        if (size_ == 1) {
+            check(htgpu_hmatrix_mvprod(built(), in, out, mu, HTGPU_HOST_PTRS | (use_permutation_ ? 0u : HTGPU_CLUSTER_NUMBERING), nullptr));
+            return;
+        }
+        // hmatrix.hpp:1074-1182: the whole input in cluster numbering, the
+        // local rows on this rank, all-gathered, back to user numbering
+        const int nr = nb_rows(), nc = nb_cols(), ls = get_local_size();
+        std::vector<double> xc((std::size_t)nc * mu), yl((std::size_t)ls * mu), yc(nr);
         if (use_permutation_)
-            check(htgpu_hmatrix_mvprod_transp(built(), in, out, mu, HTGPU_HOST_PTRS, nullptr));
+            to_cluster(*s_, in, xc.data(), mu);
         else
-            mymvprod_transp_local_to_local(in, out, mu);
+            std::copy(in, in + (std::size_t)nc * mu, xc.begin());
+        check(htgpu_hmatrix_mvprod_global_to_local(built(), xc.data(), yl.data(), mu, HTGPU_HOST_PTRS, nullptr));
+        for (int c = 0; c < mu; c++) {
+            gather_rows(*t_, yl.data() + (std::size_t)c * ls, yc.data(), 1);
+            if (use_permutation_)
+                to_user(*t_, yc.data(), out + (std::size_t)c * nr, 1);
+            else
+                std::copy(yc.begin(), yc.end(), out + (std::size_t)c * nr);
+        }
     }
-    void mvprod_transp_local_to_local(const double *const in, double *const out, const int &mu = 1, double * = nullptr) const override { mvprod_transp_global_to_global(in, out, mu); }
-    void mymvprod_transp_local_to_local(const double *const in, double *const out, const int &mu = 1, double * = nullptr) const override {
-        std::vector<double> xin((std::size_t)nb_rows() * mu), xout((std::size_t)nb_cols() * mu);
-        to_user(*t_, in, xin.data(), mu);
-        check(htgpu_hmatrix_mvprod_transp(built(), xin.data(), xout.data(), mu, HTGPU_HOST_PTRS, nullptr));
-        to_cluster(*s_, xout.data(), out, mu);
+    void mvprod_local_to_local(const double *const in, double *const out, const int &mu = 1, double *work = nullptr) const override {
+        if (size_ == 1) {
+            mvprod_global_to_global(in, out, mu);
+            return;
+        }
+        // hmatrix.hpp:1185-1274: local permutations need local trees
+        const int lss = s_->get_masteroffset(rank_).second, ls = get_local_size();
+        if (use_permutation_ && (!s_->IsLocal() || !t_->IsLocal()))
+            throw std::logic_error("[Htool error] Permutation is not local, mvprod_local_to_local cannot be used");
+        std::vector<double> xr((std::size_t)lss * mu), yr((std::size_t)ls * mu);
+        for (int c = 0; c < mu; c++)
+            for (int j = 0; j < lss; j++)
+                xr[(std::size_t)j * mu + c] = in[(std::size_t)c * lss + (use_permutation_ ? local_perm(*s_, j) : j)];
+        mymvprod_local_to_local(xr.data(), yr.data(), mu, work);
+        for (int c = 0; c < mu; c++)
+            for (int i = 0; i < ls; i++)
+                out[(std::size_t)c * ls + (use_permutation_ ? local_perm(*t_, i) : i)] = yr[(std::size_t)i * mu + c];
     }
-    void mymvprod_transp_local_to_global(const double *const in, double *const out, const int &mu = 1) const override { mymvprod_transp_local_to_local(in, out, mu); }
+    void mymvprod_local_to_local(const double *const in, double *const out, const int &mu = 1, double *work = nullptr) const override {
+        // hmatrix.hpp:980-996: local_to_global_source, then the local rows
+        std::vector<double> own;
+        if (size_ > 1 && work == nullptr) {
+            own.resize((std::size_t)nb_cols() * mu);
+            work = own.data();
+        }
+        const double *global = in;
+        if (size_ > 1) {
+            local_to_global_source(in, work, mu);
+            global = work;
+        }
+        mymvprod_global_to_local(global, out, mu);
+    }
+    void mymvprod_global_to_local(const double *const in, double *const out, const int &mu = 1) const override {
+        const int nc = nb_cols(), ls = get_local_size();
+        if (mu == 1) {
+            check(htgpu_hmatrix_mvprod_global_to_local(built(), in, out, 1, HTGPU_HOST_PTRS, nullptr));
+            return;
+        }
+        std::vector<double> xc((std::size_t)nc * mu), yc((std::size_t)ls * mu);
+        rows_to_cols(in, xc.data(), nc, mu);
+        check(htgpu_hmatrix_mvprod_global_to_local(built(), xc.data(), yc.data(), mu, HTGPU_HOST_PTRS, nullptr));
+        cols_to_rows(yc.data(), out, ls, mu);
+    }
+    void mvprod_transp_global_to_global(const double *const in, double *const out, const int &mu = 1) const override {
+        if (size_ == 1) {
+            if (use_permutation_)
+                check(htgpu_hmatrix_mvprod_transp(built(), in, out, mu, HTGPU_HOST_PTRS, nullptr));
+            else
+                transp_cluster(in, out, mu);
+            return;
+        }
+        // hmatrix.hpp:1277-1455: the local rows of the input, the ranks'
+        // transposed contributions summed
+        const int nr = nb_rows(), nc = nb_cols(), ls = get_local_size(), lo = get_local_offset();
+        std::vector<double> xc((std::size_t)nr), xr((std::size_t)ls * mu), yr((std::size_t)nc * mu);
+        for (int c = 0; c < mu; c++) {
+            if (use_permutation_)
+                to_cluster(*t_, in + (std::size_t)c * nr, xc.data(), 1);
+            else
+                std::copy(in + (std::size_t)c * nr, in + (std::size_t)(c + 1) * nr, xc.begin());
+            for (int i = 0; i < ls; i++)
+                xr[(std::size_t)i * mu + c] = xc[lo + i];
+        }
+        mymvprod_transp_local_to_global(xr.data(), yr.data(), mu);
+        std::vector<double> yc((std::size_t)nc * mu);
+        rows_to_cols(yr.data(), yc.data(), nc, mu);
+        if (use_permutation_)
+            to_user(*s_, yc.data(), out, mu);
+        else
+            std::copy(yc.begin(), yc.end(), out);
+    }
+    void mvprod_transp_local_to_local(const double *const in, double *const out, const int &mu = 1, double *work = nullptr) const override {
+        if (size_ == 1) {
+            mvprod_transp_global_to_global(in, out, mu);
+            return;
+        }
+        const int ls = get_local_size(), lss = s_->get_masteroffset(rank_).second;
+        if (use_permutation_ && (!s_->IsLocal() || !t_->IsLocal()))
+            throw std::logic_error("[Htool error] Permutation is not local, mvprod_transp_local_to_local cannot be used");
+        std::vector<double> xr((std::size_t)ls * mu), yr((std::size_t)lss * mu);
+        for (int c = 0; c < mu; c++)
+            for (int i = 0; i < ls; i++)
+                xr[(std::size_t)i * mu + c] = in[(std::size_t)c * ls + (use_permutation_ ? local_perm(*t_, i) : i)];
+        mymvprod_transp_local_to_local(xr.data(), yr.data(), mu, work);
+        for (int c = 0; c < mu; c++)
+            for (int j = 0; j < lss; j++)
+                out[(std::size_t)c * lss + (use_permutation_ ? local_perm(*s_, j) : j)] = yr[(std::size_t)j * mu + c];
+    }
+    void mymvprod_transp_local_to_local(const double *const in, double *const out, const int &mu = 1, double *work = nullptr) const override {
+        // hmatrix.hpp:999-1071: the summed transposed product's local source rows
+        std::vector<double> own;
+        if (work == nullptr) {
+            own.resize((std::size_t)nb_cols() * mu);
+            work = own.data();
+        }
+        mymvprod_transp_local_to_global(in, work, mu);
+        const int off = s_->get_masteroffset(rank_).first, lss = s_->get_masteroffset(rank_).second;
+        std::copy(work + (std::size_t)off * mu, work + (std::size_t)(off + lss) * mu, out);
+    }
+    void mymvprod_transp_local_to_global(const double *const in, double *const out, const int &mu = 1) const override {
+        // hmatrix.hpp:914-944: this rank's leaves transposed, summed over ranks
+        const int nr = nb_rows(), nc = nb_cols(), ls = get_local_size(), lo = get_local_offset();
+        std::vector<double> xc((std::size_t)nr * mu, 0.), yc((std::size_t)nc * mu);
+        for (int c = 0; c < mu; c++)
+            for (int i = 0; i < ls; i++)
+                xc[(std::size_t)c * nr + lo + i] = in[(std::size_t)i * mu + c];
+        transp_cluster(xc.data(), yc.data(), mu);
+        cols_to_rows(yc.data(), out, nc, mu);
+        if (size_ > 1)
+            MPI_Allreduce(MPI_IN_PLACE, out, nc * mu, MPI_DOUBLE, MPI_SUM, comm_);
+    }
     void mvprod_subrhs(const double *const, double *const, const int &, const int &, const int &, const int &) const override {
         throw std::logic_error("[Htool error] mvprod_subrhs (the DDM sub-domain product) is not supported by GpuHMatrix");
     }
@@ -346,6 +467,7 @@ class GpuHMatrix : public htool::VirtualHMatrix<double> {
         h_ = nullptr;
         cache_.reset();
         check(htgpu_hmatrix_create(tc_, sc_, epsilon_, eta_, device_, &h_));
+        check(htgpu_hmatrix_set_local_rank(h_, rank_)); // this rank's local tasks (blocks.hpp:258-273)
         if (symmetry_ != 'N')
             check(htgpu_hmatrix_set_symmetry(h_, symmetry_, uplo_));
         check(htgpu_hmatrix_set_compression(h_, compression_));
@@ -422,6 +544,38 @@ class GpuHMatrix : public htool::VirtualHMatrix<double> {
                 }
     }
 
+    // the transposed product in cluster numbering (column-major)
+    void transp_cluster(const double *in, double *out, int mu) const {
+        std::vector<double> xin((std::size_t)nb_rows() * mu), xout((std::size_t)nb_cols() * mu);
+        to_user(*t_, in, xin.data(), mu);
+        check(htgpu_hmatrix_mvprod_transp(built(), xin.data(), xout.data(), mu, HTGPU_HOST_PTRS, nullptr));
+        to_cluster(*s_, xout.data(), out, mu);
+    }
+    // local_to_global_source (hmatrix.hpp:963-977): every rank's rows (row
+    // by row, mu per row) gathered in rank order
+    void local_to_global_source(const double *in, double *out, int mu) const { gather_rows(*s_, in, out, mu); }
+    void gather_rows(const htool::VirtualCluster &c, const double *in, double *out, int mu) const {
+        std::vector<int> counts(size_), displs(size_);
+        for (int p = 0; p < size_; p++) {
+            counts[p] = c.get_masteroffset(p).second * mu;
+            displs[p] = c.get_masteroffset(p).first * mu;
+        }
+        MPI_Allgatherv(in, counts[rank_], MPI_DOUBLE, out, counts.data(), displs.data(), MPI_DOUBLE, comm_);
+    }
+    // local_cluster_to_local / local_to_local_cluster (virtual_cluster.hpp:
+    // 103-124): local index i of this rank's cluster <-> its local user index
+    int local_perm(const htool::VirtualCluster &c, int i) const { return c.get_perm(c.get_masteroffset(rank_).first + i) - c.get_masteroffset(rank_).first; }
+    static void rows_to_cols(const double *in, double *out, int n, int mu) {
+        for (int c = 0; c < mu; c++)
+            for (int j = 0; j < n; j++)
+                out[(std::size_t)c * n + j] = in[(std::size_t)j * mu + c];
+    }
+    static void cols_to_rows(const double *in, double *out, int n, int mu) {
+        for (int c = 0; c < mu; c++)
+            for (int j = 0; j < n; j++)
+                out[(std::size_t)j * mu + c] = in[(std::size_t)c * n + j];
+    }
+
     static void to_user(const htool::VirtualCluster &c, const double *in, double *out, int mu) {
         const std::vector<int> &p = c.get_perm();
         const std::size_t n       = p.size();
@@ -442,6 +596,7 @@ class GpuHMatrix : public htool::VirtualHMatrix<double> {
     char symmetry_, uplo_;
     int device_;
     MPI_Comm comm_;
+    int size_ = 1, rank_ = 0; // the communicator's ranks and this one
     htgpu_cluster tc_ = nullptr, sc_ = nullptr;
     htgpu_hmatrix h_  = nullptr;
     int compression_ = HTGPU_COMPRESSION_PARTIAL_ACA;

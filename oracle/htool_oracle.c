@@ -264,8 +264,10 @@ typedef struct {
 } orc_item;
 
 /* Cluster::build (cluster.hpp:57-92) + PCA::recursive_build (pca.hpp:15-128)
- * for one MPI rank: the root has a single son at depth 1. */
-void *orc_cluster_build(int n, const double *x, int minclustersize, int nb_sons) {
+ * in a run of size_world MPI ranks: the root has size_world sons at depth 1
+ * (pca.hpp:28), son p holding the points of rank p (pca.hpp:93-99); one rank
+ * gives the root a single son. */
+void *orc_cluster_build_world(int n, const double *x, int minclustersize, int nb_sons, int size_world) {
     if (nb_sons == -1)
         nb_sons = 2;
     orc_tree *T       = (orc_tree *)calloc(1, sizeof(orc_tree));
@@ -288,7 +290,7 @@ void *orc_cluster_build(int n, const double *x, int minclustersize, int nb_sons)
         orc_item it = st[--top];
         orc_node *c = &T->nodes[it.node];
         int np      = c->size;
-        int nsons   = c->depth == 0 ? 1 : nb_sons;
+        int nsons   = c->depth == 0 ? size_world : nb_sons;
         /* centre: sum of g*x with g = 1, times 1/G (pca.hpp:30-46) */
         double G = 0;
         for (int j = 0; j < np; j++)
@@ -383,6 +385,21 @@ void *orc_cluster_build(int n, const double *x, int minclustersize, int nb_sons)
     }
     free(st);
     return T;
+}
+
+void *orc_cluster_build(int n, const double *x, int minclustersize, int nb_sons) { return orc_cluster_build_world(n, x, minclustersize, nb_sons, 1); }
+
+/* MasterOffset (cluster.hpp:42, pca.hpp:98): (offset, size) of the depth-1
+ * cluster of every rank; returns the number of ranks */
+int orc_cluster_masteroffset(void *p, int *out) {
+    orc_tree *T = (orc_tree *)p;
+    orc_node *r = &T->nodes[0];
+    if (out)
+        for (int q = 0; q < r->nb_sons; q++) {
+            out[2 * q]     = T->nodes[r->first_son + q].offset;
+            out[2 * q + 1] = T->nodes[r->first_son + q].size;
+        }
+    return r->nb_sons;
 }
 
 void orc_cluster_free(void *p) {
@@ -525,9 +542,9 @@ static int orc_task_cmp(const void *a, const void *b) {
 }
 
 /* Block::build with UPLO 'N' (blocks.hpp:237-278): tasks, then the local
- * filter (every task whose target has rank 0) and the (t.offset, s.offset)
- * sort. */
-static orc_tasks orc_block_build(orc_tree *T, orc_tree *S, double eta) {
+ * filter (every task whose target cluster belongs to `rank`) and the
+ * (t.offset, s.offset) sort. */
+static orc_tasks orc_block_build(orc_tree *T, orc_tree *S, double eta, int rank) {
     orc_bt B;
     memset(&B, 0, sizeof(B));
     B.T            = T;
@@ -537,11 +554,11 @@ static orc_tasks orc_block_build(orc_tree *T, orc_tree *S, double eta) {
     int adm        = orc_admissible(&T->nodes[0], &S->nodes[0], eta);
     if (orc_bt_rec(&B, 0, 0, adm))
         orc_push_task(&B.tasks, 0, 0, adm);
-    /* local cluster = the depth-1 son, rank 0 */
+    /* local cluster = the depth-1 son of `rank` */
     orc_tasks L;
     memset(&L, 0, sizeof(L));
     for (int b = 0; b < B.tasks.n; b++)
-        if (T->nodes[B.tasks.v[b].t].rank == 0)
+        if (T->nodes[B.tasks.v[b].t].rank == rank)
             orc_push_task(&L, B.tasks.v[b].t, B.tasks.v[b].s, B.tasks.v[b].adm);
     free(B.tasks.v);
     orc_cmp_T = T;
@@ -550,9 +567,9 @@ static orc_tasks orc_block_build(orc_tree *T, orc_tree *S, double eta) {
     return L;
 }
 
-int orc_block_tasks(void *ct, void *cs, double eta, int *out) {
+int orc_block_tasks_rank(void *ct, void *cs, double eta, int rank, int *out) {
     orc_tree *T = (orc_tree *)ct, *S = (orc_tree *)cs;
-    orc_tasks L = orc_block_build(T, S, eta);
+    orc_tasks L = orc_block_build(T, S, eta, rank);
     if (out)
         for (int b = 0; b < L.n; b++) {
             out[5 * b + 0] = T->nodes[L.v[b].t].offset;
@@ -565,6 +582,8 @@ int orc_block_tasks(void *ct, void *cs, double eta, int *out) {
     free(L.v);
     return n;
 }
+
+int orc_block_tasks(void *ct, void *cs, double eta, int *out) { return orc_block_tasks_rank(ct, cs, eta, 0, out); }
 
 /* ------------------------------------------------------------------ */
 /* partialACA                                                          */
@@ -720,6 +739,7 @@ typedef struct {
 typedef struct {
     orc_tree *T, *S;
     int nr, nc, kernel;
+    int rank, loff, lsize; /* local target rows of `rank` (local_offset, local_size) */
     double eps, eta;
     const double *xt, *xs;
     orc_leafset L;
@@ -817,11 +837,21 @@ static double orc_now(void) {
 }
 
 /* HMatrix(t, s, eps, eta, 'N', 'N') with partialACA, then build(gen, xt, xs)
- * (hmatrix.hpp:115, 286-341, 423-501).  OpenMP over local tasks as upstream. */
-void *orc_hmatrix_build(void *ct, void *cs, int nr, const double *xt, int nc, const double *xs, int kernel, double eps, double eta) {
+ * (hmatrix.hpp:115, 286-341, 423-501) as rank `rank` of the run the cluster
+ * trees were built for: the leaves of its local tasks only, local rows
+ * (local_offset, local_size) = its depth-1 target cluster
+ * (hmatrix.hpp:320-321).  OpenMP over local tasks as upstream. */
+void *orc_hmatrix_build_rank(void *ct, void *cs, int nr, const double *xt, int nc, const double *xs, int kernel, double eps, double eta, int rank) {
     orc_hmat *H = (orc_hmat *)calloc(1, sizeof(orc_hmat));
     H->T        = (orc_tree *)ct;
     H->S        = (orc_tree *)cs;
+    {
+        orc_node *root = &H->T->nodes[0];
+        orc_node *loc  = &H->T->nodes[root->first_son + rank];
+        H->rank        = rank;
+        H->loff        = loc->offset;
+        H->lsize       = loc->size;
+    }
     H->nr       = nr;
     H->nc       = nc;
     H->kernel   = kernel;
@@ -830,7 +860,7 @@ void *orc_hmatrix_build(void *ct, void *cs, int nr, const double *xt, int nc, co
     H->xt       = xt;
     H->xs       = xs;
     double t0   = orc_now();
-    orc_tasks tasks = orc_block_build(H->T, H->S, eta);
+    orc_tasks tasks = orc_block_build(H->T, H->S, eta, rank);
     int ntask       = tasks.n;
     orc_leafset *per = (orc_leafset *)calloc(ntask ? ntask : 1, sizeof(orc_leafset));
 #pragma omp parallel for schedule(guided)
@@ -862,6 +892,16 @@ void *orc_hmatrix_build(void *ct, void *cs, int nr, const double *xt, int nc, co
     qsort(H->L.dn, H->L.ndn, sizeof(orc_dense), orc_dn_cmp);
     H->build_seconds = orc_now() - t0;
     return H;
+}
+
+void *orc_hmatrix_build(void *ct, void *cs, int nr, const double *xt, int nc, const double *xs, int kernel, double eps, double eta) {
+    return orc_hmatrix_build_rank(ct, cs, nr, xt, nc, xs, kernel, eps, eta, 0);
+}
+
+void orc_hmatrix_local(void *p, int *offset, int *size) {
+    orc_hmat *H = (orc_hmat *)p;
+    *offset     = H->loff;
+    *size       = H->lsize;
 }
 
 void orc_hmatrix_free(void *p) {
@@ -935,24 +975,22 @@ void orc_hmatrix_factors(void *p, double *uv, double *dense) {
  * buffer (hmatrix.hpp:844-911; LowRankMatrix::add_mvprod_row_major =
  * V-gemv then U-gemv, lrmat.hpp:89-100), reduce, scatter through the target
  * permutation.  x and y hold mu column-major right-hand sides. */
-void orc_hmatrix_mvprod(void *p, const double *x, double *y, int mu) {
-    orc_hmat *H = (orc_hmat *)p;
-    int nr = H->nr, nc = H->nc;
-    double *xp = (double *)malloc(sizeof(double) * (size_t)nc * mu);
-    double *yp = (double *)calloc((size_t)nr * mu, sizeof(double));
-    for (int c = 0; c < mu; c++)
-        for (int i = 0; i < nc; i++)
-            xp[(size_t)c * nc + i] = x[(size_t)c * nc + H->S->perm[i]];
+/* the leaf loop of mymvprod_global_to_local (hmatrix.hpp:844-911): xp is
+ * the input in cluster numbering (nc per right-hand side), yp receives rows
+ * row0 .. row0 + nrows (nrows per right-hand side, zeroed here) */
+static void orc_apply_leaves(orc_hmat *H, const double *xp, double *yp, int mu, int row0, int nrows) {
+    int nc = H->nc;
+    memset(yp, 0, sizeof(double) * (size_t)nrows * mu);
     int nlr = H->L.nlr, ndn = H->L.ndn;
 #pragma omp parallel
     {
-        double *tmp = (double *)calloc((size_t)nr * mu, sizeof(double));
+        double *tmp = (double *)calloc((size_t)nrows * mu + 1, sizeof(double));
         double a[4096];
 #pragma omp for schedule(guided) nowait
         for (int b = 0; b < nlr + ndn; b++) {
             for (int c = 0; c < mu; c++) {
                 const double *xs = xp + (size_t)c * nc;
-                double *ys       = tmp + (size_t)c * nr;
+                double *ys       = tmp + (size_t)c * nrows;
                 if (b < nlr) {
                     orc_lr *v = &H->L.lr[b];
                     int r     = v->rank;
@@ -969,7 +1007,7 @@ void orc_hmatrix_mvprod(void *p, const double *x, double *y, int mu) {
                         const double *col = v->U + (size_t)v->m * k;
                         double ak         = ap[k];
                         for (int i = 0; i < v->m; i++)
-                            ys[v->oi + i] += col[i] * ak;
+                            ys[v->oi - row0 + i] += col[i] * ak;
                     }
                     if (ap != a)
                         free(ap);
@@ -979,23 +1017,48 @@ void orc_hmatrix_mvprod(void *p, const double *x, double *y, int mu) {
                         double xj         = xs[v->oj + j];
                         const double *col = v->D + (size_t)v->m * j;
                         for (int i = 0; i < v->m; i++)
-                            ys[v->oi + i] += col[i] * xj;
+                            ys[v->oi - row0 + i] += col[i] * xj;
                     }
                 }
             }
         }
 #pragma omp critical
         {
-            for (size_t i = 0; i < (size_t)nr * mu; i++)
+            for (size_t i = 0; i < (size_t)nrows * mu; i++)
                 yp[i] += tmp[i];
         }
         free(tmp);
     }
+}
+
+/* mvprod_global_to_global (hmatrix.hpp:1074-1182) for one rank: gather x
+ * through the source permutation, accumulate every leaf into a per-thread
+ * buffer (hmatrix.hpp:844-911; LowRankMatrix::add_mvprod_row_major =
+ * V-gemv then U-gemv, lrmat.hpp:89-100), reduce, scatter through the target
+ * permutation.  x and y hold mu column-major right-hand sides. */
+void orc_hmatrix_mvprod(void *p, const double *x, double *y, int mu) {
+    orc_hmat *H = (orc_hmat *)p;
+    int nr = H->nr, nc = H->nc;
+    double *xp = (double *)malloc(sizeof(double) * (size_t)nc * mu);
+    double *yp = (double *)malloc(sizeof(double) * (size_t)nr * mu + 8);
+    for (int c = 0; c < mu; c++)
+        for (int i = 0; i < nc; i++)
+            xp[(size_t)c * nc + i] = x[(size_t)c * nc + H->S->perm[i]];
+    orc_apply_leaves(H, xp, yp, mu, 0, nr);
     for (int c = 0; c < mu; c++)
         for (int i = 0; i < nr; i++)
             y[(size_t)c * nr + H->T->perm[i]] = yp[(size_t)c * nr + i];
     free(xp);
     free(yp);
+}
+
+/* mymvprod_global_to_local (hmatrix.hpp:844-911): x is the whole input in
+ * cluster numbering (what local_to_global_source all-gathers,
+ * hmatrix.hpp:963-977), y the rank's local target rows local_offset ..
+ * local_offset + local_size; both column-major per right-hand side */
+void orc_hmatrix_mvprod_global_to_local(void *p, const double *x, double *y, int mu) {
+    orc_hmat *H = (orc_hmat *)p;
+    orc_apply_leaves(H, x, y, mu, H->loff, H->lsize);
 }
 
 /* median wall time of reps products after one warm-up */

@@ -179,6 +179,14 @@ class Oracle:
             L.orc_partial_aca.argtypes = [_i, _vp, _vp, _d, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]
             L.orc_dense_rows_mvprod.argtypes = [_i, _i, _vp, _vp, _i, _vp, _vp, _vp]
             L.orc_set_num_threads.argtypes = [_i]
+            L.orc_cluster_build_world.restype = _vp
+            L.orc_cluster_build_world.argtypes = [_i, _vp, _i, _i, _i]
+            L.orc_cluster_masteroffset.argtypes = [_vp, _vp]
+            L.orc_block_tasks_rank.argtypes = [_vp, _vp, _d, _i, _vp]
+            L.orc_hmatrix_build_rank.restype = _vp
+            L.orc_hmatrix_build_rank.argtypes = [_vp, _vp, _i, _vp, _i, _vp, _i, _d, _d, _i]
+            L.orc_hmatrix_local.argtypes = [_vp, _vp, _vp]
+            L.orc_hmatrix_mvprod_global_to_local.argtypes = [_vp, _vp, _vp, _i]
         elif kind == "reference":
             if not os.path.exists(REF_SO):
                 raise FileNotFoundError(REF_SO)
@@ -211,6 +219,10 @@ class Oracle:
             L.ref_hmatrix_infos_d.argtypes = [_vp, C.c_char_p, _i]
             L.ref_lrmat_partialACA.argtypes = [_vp, _vp, _i, _vp, _i, _vp, _i, _i, _d, _i, _vp, _vp, _vp]
             L.ref_last_error.restype = C.c_char_p
+            L.ref_set_world.argtypes = [_i, _i]
+            L.ref_cluster_masteroffset.argtypes = [_vp, _vp]
+            L.ref_hmatrix_mvprod_global_to_local_d.argtypes = [_vp, _vp, _vp, _i]
+            L.ref_hmatrix_local_d.argtypes = [_vp, _vp, _vp]
         else:
             raise ValueError(kind)
         self._bind()
@@ -261,11 +273,77 @@ class Oracle:
         else:
             os.environ["OMP_NUM_THREADS"] = str(n)
 
-    def cluster(self, points, minclustersize=10, nb_sons=2):
+    def cluster(self, points, minclustersize=10, nb_sons=2, size_world=1, rank=0):
+        """Cluster tree; size_world > 1 builds it as rank `rank` of a run of
+        size_world MPI ranks (the root then has one son per rank)."""
         pts = np.ascontiguousarray(points, dtype=np.float64)
         n = pts.shape[0]
-        f = self._L.orc_cluster_build if self.kind == "port" else self._L.ref_cluster_build
-        return Cluster(self, f(n, _ptr(pts), minclustersize, nb_sons), n, pts)
+        if self.kind == "port":
+            h = self._L.orc_cluster_build_world(n, _ptr(pts), minclustersize, nb_sons, size_world)
+        else:
+            self._L.ref_set_world(size_world, rank)
+            try:
+                h = self._L.ref_cluster_build(n, _ptr(pts), minclustersize, nb_sons)
+            finally:
+                self._L.ref_set_world(1, 0)
+        c = Cluster(self, h, n, pts)
+        c.size_world, c.rank = size_world, rank
+        return c
+
+    def masteroffset(self, ct):
+        """(offset, size) of every rank's depth-1 cluster"""
+        f = self._L.orc_cluster_masteroffset if self.kind == "port" else self._L.ref_cluster_masteroffset
+        n = f(ct.h, None)
+        out = np.empty((n, 2), np.int32)
+        f(ct.h, _ptr(out))
+        return out
+
+    def block_tasks_rank(self, ct, cs, eta, rank):
+        """Local tasks of `rank` (trees of a multi-rank run)"""
+        if self.kind == "port":
+            n = self._L.orc_block_tasks_rank(ct.h, cs.h, eta, rank, None)
+            out = np.empty((n, 5), np.int32)
+            self._L.orc_block_tasks_rank(ct.h, cs.h, eta, rank, _ptr(out))
+            return out
+        self._L.ref_set_world(ct.size_world, rank)
+        try:
+            n = self._L.ref_block_tasks(ct.h, cs.h, eta, b"N", 0, None)
+            out = np.empty((n, 5), np.int32)
+            self._L.ref_block_tasks(ct.h, cs.h, eta, b"N", 0, _ptr(out))
+        finally:
+            self._L.ref_set_world(1, 0)
+        return out
+
+    def hmatrix_rank(self, ct, cs, xt, xs, kernel, eps, eta, rank):
+        """H-matrix of rank `rank` of a multi-rank run (non-symmetric,
+        partialACA): the leaves of its local tasks"""
+        xt = np.ascontiguousarray(xt, dtype=np.float64)
+        xs = np.ascontiguousarray(xs, dtype=np.float64)
+        nr, nc = xt.shape[0], xs.shape[0]
+        if self.kind == "port":
+            h = self._L.orc_hmatrix_build_rank(ct.h, cs.h, nr, _ptr(xt), nc, _ptr(xs), kernel, eps, eta, rank)
+        else:
+            self._L.ref_set_world(ct.size_world, rank)
+            try:
+                h = self._L.ref_hmatrix_build_d(ct.h, cs.h, nr, _ptr(xt), nc, _ptr(xs), kernel, eps, eta, 0, b"N", b"N", 0)
+            finally:
+                self._L.ref_set_world(1, 0)
+            if not h:
+                raise RuntimeError(self._L.ref_last_error().decode())
+        hm = HMat(self, h, nr, nc, (xt, xs, ct, cs))
+        a, b = C.c_int(), C.c_int()
+        (self._L.orc_hmatrix_local if self.kind == "port" else self._L.ref_hmatrix_local_d)(h, C.byref(a), C.byref(b))
+        hm.local_offset, hm.local_size = a.value, b.value
+        return hm
+
+    def mvprod_global_to_local(self, hm, x_cluster, mu=1):
+        """mymvprod_global_to_local: the whole input in cluster numbering in,
+        the local rows out (column-major per right-hand side)"""
+        x = np.ascontiguousarray(x_cluster, dtype=np.float64)
+        y = np.empty(hm.local_size * mu, np.float64)
+        f = self._L.orc_hmatrix_mvprod_global_to_local if self.kind == "port" else self._L.ref_hmatrix_mvprod_global_to_local_d
+        f(hm.h, _ptr(x), _ptr(y), mu)
+        return y
 
     def block_tasks(self, ct, cs, eta):
         """Local tasks (t.offset, t.size, s.offset, s.size, admissible)."""

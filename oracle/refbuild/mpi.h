@@ -8,6 +8,12 @@
  * encoded as their size in bytes so the copies know how much to move.  The
  * symbol set is exactly what htool's hmatrix.hpp, cluster.hpp,
  * wrapper_mpi.hpp and blocks.hpp call.
+ *
+ * htgpu_stub_set_world(P, p) makes MPI_Comm_size / MPI_Comm_rank report a
+ * world of P ranks seen from rank p, so that one process can replay what
+ * rank p of a P-rank run computes locally (its cluster tree, local tasks,
+ * leaves and mymvprod_global_to_local).  The collectives stay local copies:
+ * only the rank-local steps are meaningful in that mode.
  */
 #ifndef HTGPU_ORACLE_MPI_STUB_H
 #define HTGPU_ORACLE_MPI_STUB_H
@@ -49,12 +55,17 @@ typedef struct {
 
 static inline int MPI_Init(int *, char ***) { return MPI_SUCCESS; }
 static inline int MPI_Finalize(void) { return MPI_SUCCESS; }
+static int htgpu_stub_world_size = 1, htgpu_stub_world_rank = 0;
+static inline void htgpu_stub_set_world(int size, int rank) {
+    htgpu_stub_world_size = size;
+    htgpu_stub_world_rank = rank;
+}
 static inline int MPI_Comm_size(MPI_Comm, int *size) {
-    *size = 1;
+    *size = htgpu_stub_world_size;
     return MPI_SUCCESS;
 }
 static inline int MPI_Comm_rank(MPI_Comm, int *rank) {
-    *rank = 0;
+    *rank = htgpu_stub_world_rank;
     return MPI_SUCCESS;
 }
 static inline double MPI_Wtime(void) {

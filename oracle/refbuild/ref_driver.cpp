@@ -143,6 +143,45 @@ void ref_cluster_export(void *p, int *perm, int *node_i, double *node_d) {
     });
 }
 
+// World of P ranks seen from rank p for the calls that follow (the MPI stub
+// reports it): rank p's cluster tree, local tasks, H-matrix and
+// mymvprod_global_to_local, replayed in one process
+void ref_set_world(int size, int rank) { htgpu_stub_set_world(size, rank); }
+
+// MasterOffset of a cluster tree (cluster.hpp:42, pca.hpp:93-99): per rank
+// (offset, size) of its depth-1 cluster; returns the number of ranks
+int ref_cluster_masteroffset(void *p, int *out) {
+    const auto &mo = ((RefCluster *)p)->c->get_masteroffset();
+    if (out)
+        for (size_t r = 0; r < mo.size(); r++) {
+            out[2 * r]     = mo[r].first;
+            out[2 * r + 1] = mo[r].second;
+        }
+    return (int)mo.size();
+}
+
+// HMatrix::mymvprod_global_to_local (hmatrix.hpp:844-911): x is the whole
+// input in cluster numbering, y the local target rows; both column-major
+// per right-hand side here (htool's are row-major for mu > 1: transposed
+// around the call)
+void ref_hmatrix_mvprod_global_to_local_d(void *p, const double *x, double *y, int mu) {
+    auto &h    = *((RefHMat<double> *)p)->h;
+    const int nc = h.nb_cols(), ls = h.get_local_size();
+    std::vector<double> xr((size_t)nc * mu), yr((size_t)ls * mu);
+    for (int c = 0; c < mu; c++)
+        for (int j = 0; j < nc; j++)
+            xr[(size_t)j * mu + c] = x[(size_t)c * nc + j];
+    h.mymvprod_global_to_local(xr.data(), yr.data(), mu);
+    for (int c = 0; c < mu; c++)
+        for (int i = 0; i < ls; i++)
+            y[(size_t)c * ls + i] = yr[(size_t)i * mu + c];
+}
+void ref_hmatrix_local_d(void *p, int *offset, int *size) {
+    auto &h = *((RefHMat<double> *)p)->h;
+    *offset = h.get_local_offset();
+    *size   = h.get_local_size();
+}
+
 // HMatrix::save_plot (hmatrix.hpp:1696-1712)
 void ref_hmatrix_save_plot_d(void *p, const char *name) { ((RefHMat<double> *)p)->h->save_plot(name); }
 void ref_hmatrix_save_plot_z(void *p, const char *name) { ((RefHMat<std::complex<double>> *)p)->h->save_plot(name); }

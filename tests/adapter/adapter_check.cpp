@@ -124,6 +124,60 @@ int main(int argc, char **argv) {
         htgpu_cluster_destroy(hc);
     }
 
+    // rank r of a two-rank run, replayed in this process (the MPI stub
+    // reports the world): htool's tree of that run handed over, its
+    // MasterOffset and rank r's local tasks as htool's Block::build keeps them
+    for (int r = 0; r < 2; r++) {
+        htgpu_stub_set_world(2, r);
+        auto t2 = std::make_shared<Cluster<PCAGeometricClustering>>(3);
+        t2->build(n, pts.data(), 2);
+        htgpu_cluster h2 = htool_gpu::import_cluster(*t2);
+        int P = 0;
+        std::vector<int> mo(4);
+        htool_gpu::check(htgpu_cluster_masteroffset(h2, &P, mo.data()));
+        CHECK(P == 2);
+        for (int q = 0; q < 2; q++)
+            CHECK(mo[2 * q] == t2->get_masteroffset(q).first && mo[2 * q + 1] == t2->get_masteroffset(q).second);
+        int ntasks = 0;
+        htool_gpu::check(htgpu_block_tasks_rank(h2, h2, 10.0, r, &ntasks, nullptr));
+        std::vector<int> tasks(5 * (size_t)ntasks);
+        htool_gpu::check(htgpu_block_tasks_rank(h2, h2, 10.0, r, &ntasks, tasks.data()));
+        RjasanowSteinbach adm2;
+        Block B2(&adm2, *t2, *t2);
+        B2.set_eta(10.0);
+        B2.build('N', false);
+        std::vector<std::array<int, 5>> up, ours;
+        for (auto *b : B2.get_local_tasks())
+            up.push_back({b->get_target_cluster().get_offset(), b->get_target_cluster().get_size(), b->get_source_cluster().get_offset(), b->get_source_cluster().get_size(), b->IsAdmissible() ? 1 : 0});
+        for (int q = 0; q < ntasks; q++)
+            ours.push_back({tasks[5 * q], tasks[5 * q + 1], tasks[5 * q + 2], tasks[5 * q + 3], tasks[5 * q + 4]});
+        CHECK(ours == up && !up.empty());
+        htool_gpu::GpuHMatrix H2(t2, t2, 1e-6, 10.0);
+        CHECK(H2.get_sizeworld() == 2 && H2.get_rankworld() == r);
+        CHECK(H2.get_local_offset() == t2->get_masteroffset(r).first && H2.get_local_size() == t2->get_masteroffset(r).second);
+        bool sym_refused = false;
+        try {
+            htool_gpu::GpuHMatrix S2(t2, t2, 1e-6, 10.0, 'S', 'U');
+        } catch (const std::invalid_argument &) {
+            sym_refused = true;
+        }
+        CHECK(sym_refused);
+        htgpu_cluster_destroy(h2);
+        htgpu_stub_set_world(1, 0);
+    }
+    {
+        // a one-rank tree on a two-rank communicator is refused
+        htgpu_stub_set_world(2, 0);
+        bool refused = false;
+        try {
+            htool_gpu::GpuHMatrix bad(t, t, 1e-6, 10.0);
+        } catch (const std::invalid_argument &e) {
+            refused = std::strstr(e.what(), "not built for this communicator") != nullptr;
+        }
+        CHECK(refused);
+        htgpu_stub_set_world(1, 0);
+    }
+
     // the adapters are concrete implementations of htool's interfaces
     std::unique_ptr<VirtualHMatrix<double>> H(new htool_gpu::GpuHMatrix(t, t, 1e-6, 10.0));
     std::shared_ptr<VirtualLowRankGenerator<double>> dev = std::make_shared<htool_gpu::DeviceACA>(0);

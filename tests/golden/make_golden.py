@@ -21,6 +21,7 @@ Usage (needs the upstream sources, i.e. only in the build container):
     python tests/golden/make_golden.py ztransp  # transposed products of the Helmholtz fixture
     python tests/golden/make_golden.py zsym     # symmetric / Hermitian complex H-matrices
     python tests/golden/make_golden.py zleaves  # upstream's complex leaves and their products
+    python tests/golden/make_golden.py ranks    # multi-rank trees, local tasks, leaves, local products
 """
 import ctypes as C
 import hashlib
@@ -354,6 +355,48 @@ def plot_cases():
     L.ref_hmatrix_save_plot_z(h, os.path.join(OUT, "helmholtz_cube2000_plot").encode())
     L.ref_hmatrix_free_z(h)
 
+def ranks_case(R, name, pts, kernel, eps, eta, worlds=(2, 3, 4), mus=(1, 2)):
+    """What rank r of a run of P MPI ranks computes locally, replayed in one
+    process (the MPI stub reports P ranks seen from r): the cluster tree with
+    one son of the root per rank and its MasterOffset (pca.hpp:28, 93-99),
+    rank r's local task list (blocks.hpp:258-273), the leaves of its
+    HMatrix::build and mymvprod_global_to_local (hmatrix.hpp:844-911) of
+    seeded right-hand sides given in cluster numbering"""
+    n = pts.shape[0]
+    data = dict(points=pts)
+    meta = dict(kernel=kernel, eps=eps, eta=eta, minclustersize=10, nb_sons=2, worlds=list(worlds), mus=list(mus), ranks={})
+    for P in worlds:
+        for r in range(P):
+            ct = R.cluster(pts, size_world=P, rank=r)
+            perm, ni, nd = ct.export()
+            if r == 0:
+                data["perm_P%d" % P] = perm
+                data["nodes_i_P%d" % P] = ni
+                data["nodes_d_P%d" % P] = nd
+                data["masteroffset_P%d" % P] = R.masteroffset(ct)
+                for mu in mus:
+                    x = G.rhs(n, mu, seed=2)
+                    data["x_P%d_mu%d" % (P, mu)] = np.concatenate([x[c * n:(c + 1) * n][perm] for c in range(mu)])
+            tag = "P%d_r%d" % (P, r)
+            data["tasks_" + tag] = R.block_tasks_rank(ct, ct, eta, r)
+            H = R.hmatrix_rank(ct, ct, pts, pts, kernel, eps, eta, r)
+            lr, dn, uv, dd = H.factors()
+            data["lr_" + tag] = lr
+            data["dense_" + tag] = dn
+            for mu in mus:
+                data["y_%s_mu%d" % (tag, mu)] = R.mvprod_global_to_local(H, data["x_P%d_mu%d" % (P, mu)], mu)
+            meta["ranks"][tag] = dict(local_offset=H.local_offset, local_size=H.local_size, sha_uv=sha(uv), sha_dense=sha(dd))
+            print(name, tag, "local", H.local_offset, H.local_size, "leaves", lr.shape[0], dn.shape[0])
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
+    with open(os.path.join(OUT, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
+def rank_cases():
+    R = Oracle("reference")
+    ranks_case(R, "cyl4000_k0_ranks", G.cylinder(4000, seed=1), 0, 1e-6, 10.0)
+    ranks_case(R, "sphere6000_k1_ranks", G.sphere(6000, seed=1), 1, 1e-6, 10.0, worlds=(2, 3))
+
 
 if __name__ == "__main__":
     if sys.argv[1:] == ["plot"]:
@@ -366,5 +409,7 @@ if __name__ == "__main__":
         zsym_cases()
     elif sys.argv[1:] == ["zleaves"]:
         zleaves_case()
+    elif sys.argv[1:] == ["ranks"]:
+        rank_cases()
     else:
         main()

@@ -86,3 +86,102 @@ def test_batch_errors():
         batch.launch()
     with pytest.raises(ValueError):
         batch.capture()
+
+
+def _forest_inputs(members, mu, seed):
+    """every member's right-hand sides (n_k x mu, column-major) and their
+    concatenation in the forest's layout (sum n_k rows, column-major)"""
+    xs = [G.rhs(n, mu, seed=seed + k) for k, (_, n) in enumerate(members)]
+    cat = np.concatenate([np.concatenate([x[c * n:(c + 1) * n] for x, (_, n) in zip(xs, members)]) for c in range(mu)])
+    return xs, cat
+
+
+def _split(y, members, mu):
+    N = sum(n for _, n in members)
+    cols = y.reshape(mu, N)
+    out, off = [], 0
+    for _, n in members:
+        out.append(cols[:, off:off + n].reshape(-1))
+        off += n
+    return out
+
+
+def test_forest_is_the_block_diagonal_batch(port):
+    """a forest of independent trees: one H-matrix holding every member's
+    leaves (the same leaves as the members built alone, offsets shifted),
+    one product for all of them, each member's rows equal to the oracle's
+    product of that member (FP64 1e-12, mixed 1e-6)"""
+    rng = np.random.default_rng(7)
+    members, trees, pts, oracle, alone = [], [], [], [], []
+    for k in range(6):
+        n = int(round(np.exp(rng.uniform(np.log(1500), np.log(6000)))))
+        p = G.ellipsoid(n, rng.uniform(0.5, 2.0, 3), seed=200 + k)
+        t = H.Cluster().build(n, p)
+        members.append((t, n))
+        trees.append(t)
+        pts.append(p)
+        ot = port.cluster(p)
+        oracle.append(port.hmatrix(ot, ot, p, p, H.LAPLACE, 1e-6, 10.0))
+        alone.append(H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, p))
+    F = H.Cluster.forest(trees)
+    off = F.get_forest_offsets()
+    hf = H.HMatrix(F, F, 1e-6, 10.0).build(H.LAPLACE, np.concatenate(pts))
+    lr, dn = hf.get_leaves()
+    for k, h in enumerate(alone):
+        lk, dk = h.get_leaves()
+        sel = (lr[:, 0] >= off[k]) & (lr[:, 0] < off[k + 1])
+        shifted = lk.copy()
+        shifted[:, :2] += off[k]
+        assert np.array_equal(lr[sel], shifted), k
+        seld = (dn[:, 0] >= off[k]) & (dn[:, 0] < off[k + 1])
+        shiftd = dk.copy()
+        shiftd[:, :2] += off[k]
+        assert np.array_equal(dn[seld], shiftd), k
+    for mu in (1, 3):
+        xs, cat = _forest_inputs(members, mu, seed=30)
+        ys = _split(hf.mvprod_global_to_global(cat, mu), members, mu)
+        for k in range(len(members)):
+            yo = oracle[k].mvprod(xs[k], mu)
+            assert np.linalg.norm(ys[k] - yo) / np.linalg.norm(yo) < TOL["fp64"], (k, mu)
+    hf.set_precision("mixed")
+    xs, cat = _forest_inputs(members, 2, seed=60)
+    ys = _split(hf.mvprod_global_to_global(cat, 2), members, 2)
+    for k in range(len(members)):
+        yo = oracle[k].mvprod(xs[k], 2)
+        assert np.linalg.norm(ys[k] - yo) / np.linalg.norm(yo) < TOL["mixed"], k
+    assert hf.device_status() == 0
+
+
+def test_rhs_buckets_pad_to_one_pass(port):
+    """3, 5, 6 and 7 right-hand sides padded with zero columns to 4 or 8
+    (one pass over the factors) give the unpadded product (FP64 within
+    1e-12 -- 8 columns take the many-right-hand-side kernels; mixed within
+    1e-6 of the oracle)"""
+    pts = G.sphere(5000, seed=11)
+    t = H.Cluster().build(5000, pts)
+    hm = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+    ot = port.cluster(pts)
+    oh = port.hmatrix(ot, ot, pts, pts, H.LAPLACE, 1e-6, 10.0)
+    for policy in ("fp64", "mixed"):
+        hm.set_precision(policy)
+        for mu, up in ((3, 4), (5, 8), (6, 8), (7, 8)):
+            x = G.rhs(5000, mu, seed=70 + mu)
+            hm.set_rhs_bucket(mu, 0)
+            y0 = hm.mvprod_global_to_global(x, mu)
+            hm.set_rhs_bucket(mu, up)
+            assert hm.get_rhs_bucket(mu) == up
+            y1 = hm.mvprod_global_to_global(x, mu)
+            yo = oh.mvprod(x, mu)
+            assert np.linalg.norm(y1 - yo) / np.linalg.norm(yo) < TOL[policy], (policy, mu)
+            if policy == "fp64":
+                assert np.linalg.norm(y1 - y0) / np.linalg.norm(y0) < 1e-12, mu
+        hm.autotune(5, 2)
+        assert hm.get_rhs_bucket(5) in (5, 8)
+        x = G.rhs(5000, 5, seed=99)
+        yo = oh.mvprod(x, 5)
+        assert np.linalg.norm(hm.mvprod_global_to_global(x, 5) - yo) / np.linalg.norm(yo) < TOL[policy]
+    with pytest.raises(ValueError):
+        hm.set_rhs_bucket(3, 2)
+    with pytest.raises(ValueError):
+        hm.set_rhs_bucket(9, 16)
+    assert hm.device_status() == 0
