@@ -1450,6 +1450,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
+        } else if (n_p1m_ && mu >= 3 && !mma && p1_mode_ == 1 && n_tcblk_ > 0) {
+            // the stacked blocks on the CUDA cores (phase-1 mode 1 with 3 or more right-hand sides)
+            launch_phase1_stack(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, reinterpret_cast<float *>(w_A), st);
+            launches_ += 1;
         } else if (n_p1m_ && mma) {
             if (tc_mode_ >= 1 && n_tcblk_ > 0)
                 launch_phase1_tc(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, reinterpret_cast<float *>(w_A), status_d.p, st);

@@ -203,6 +203,10 @@ struct TcBlock { // segments [s0, s1), at most 128 columns in all, on x rows xro
     int s0, s1, xrow, jlen;
 };
 void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, int *status, cudaStream_t st);
+// the same stacked blocks on the CUDA cores (mixed.cu), products with 3 or
+// more right-hand sides at any epsilon: one thread per stacked column, FP32
+// FMA, float sums into A
+void launch_phase1_stack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, cudaStream_t st);
 // phase 2 of the same products on tcgen05: the FP32 / BF16 columns of every
 // row chunk in slabs of 32 (rc as launch_phase2_mma), four row chunks
 // (a group) to one 128-row accumulator; writes the z rows (the dense chunks

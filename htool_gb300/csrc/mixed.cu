@@ -194,6 +194,120 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
     }
 }
 
+// ---------------------------------------------------------------------------
+// Phase 1 of reduced-precision products with 3 or more right-hand sides on
+// the CUDA cores.  The tiles on the same x rows are stacked into blocks of at
+// most 128 columns (TcBlock / TcSeg, the blocks of the tensor-core phase 1);
+// thread t of the CTA owns stacked column t.  Per 32-row slab the CTA stages
+// the block's columns (a warp copies one column's 32 rows at a time,
+// coalesced, BF16 widened to float) and the slab's x rows for MU
+// right-hand sides in shared memory; each thread then walks its column down
+// the slab, MU FMAs per element, and at the end writes its phase-1 sums times
+// the column's scale.  The contraction runs along each thread's own column,
+// so no shuffles are needed; sums are FP32 over a tile (at most 256 rows),
+// as in the other reduced-precision kernels.
+constexpr int kStkThreads = 128, kStkSlab = 32, kStkLd = 33;
+
+template <int MU>
+__global__ void __launch_bounds__(kStkThreads) phase1_stack_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
+                                                                  const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, float *__restrict__ A) {
+    static_assert(MU % 4 == 0, "x rows are read four right-hand sides at a time");
+    __shared__ float sv[kStkThreads * kStkLd];       // [stacked column][row of the slab]
+    __shared__ __align__(16) float sx[kStkSlab * MU]; // [row of the slab][right-hand side]
+    __shared__ long long cp[kStkThreads];            // byte offset of every stacked column in the reduced arena
+    __shared__ int ck[kStkThreads];                  // its kind: 0 none, 1 FP32, 2 BF16
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int bi = blockIdx.x; bi < nblocks; bi += gridDim.x) {
+        const TcBlock B = blocks[bi];
+        const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
+        int m0 = 0, sg = -1;
+        for (int s = B.s0; s < B.s1; s++) {
+            const int nc = segs[s].ncol;
+            if (tid < m0 + nc) {
+                sg = s;
+                break;
+            }
+            m0 += nc;
+        }
+        long long off = 0, oslot = 0;
+        int kind      = 0;
+        float osc     = 0.f;
+        if (sg >= 0) {
+            const TcSeg S = segs[sg];
+            const int col = S.col0 + tid - m0;
+            if (col < S.c32) {
+                off  = S.off + 4LL * l32 * col;
+                kind = 1;
+            } else {
+                off  = S.off + 4LL * l32 * S.c32 + 2LL * l16 * (col - S.c32);
+                kind = 2;
+            }
+            oslot = S.slot + (tid - m0);
+            osc   = scale[S.sidx + tid - m0];
+        }
+        __syncthreads(); // the previous block's column table is no longer read
+        cp[tid]       = off;
+        ck[tid]       = kind;
+        const F2 *X   = xs + (long long)B.xrow * mu;
+        for (int cb = 0; cb < mu; cb += MU) {
+            float acc[MU];
+#pragma unroll
+            for (int c = 0; c < MU; c++)
+                acc[c] = 0.f;
+            for (int js = 0; js < B.jlen; js += kStkSlab) {
+                const int nj = min(kStkSlab, B.jlen - js);
+                __syncthreads(); // the column table is written; the previous slab is read out
+                // the block's columns: warp w copies columns w + 4 q, lane = row, eight loads in flight
+#pragma unroll 1
+                for (int q0 = 0; q0 < kStkThreads / 4; q0 += 8) {
+                    float v[8];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const int cc = wid + 4 * (q0 + q);
+                        const int kd = ck[cc];
+                        v[q]         = 0.f;
+                        if (lane < nj) {
+                            if (kd == 1)
+                                v[q] = __ldg(reinterpret_cast<const float *>(mix + cp[cc]) + js + lane);
+                            else if (kd == 2)
+                                v[q] = bf16_to_f32(__ldg(reinterpret_cast<const unsigned short *>(mix + cp[cc]) + js + lane));
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; q++)
+                        sv[(wid + 4 * (q0 + q)) * kStkLd + lane] = v[q];
+                }
+                // the slab's x rows for right-hand sides cb .. cb + MU
+                for (int e = tid; e < kStkSlab * MU; e += kStkThreads) {
+                    const int j = e / MU, c = e % MU;
+                    sx[e]       = (j < nj && cb + c < mu) ? __ldg(&X[(long long)(js + j) * mu + cb + c].hi) : 0.f;
+                }
+                __syncthreads();
+                if (kind) {
+                    const float *colv = sv + tid * kStkLd;
+                    for (int j = 0; j < nj; j++) {
+                        const float v     = colv[j];
+                        const float4 *xr = reinterpret_cast<const float4 *>(sx + j * MU);
+#pragma unroll
+                        for (int q = 0; q < MU / 4; q++) {
+                            const float4 xv  = xr[q];
+                            acc[4 * q]     = fmaf(v, xv.x, acc[4 * q]);
+                            acc[4 * q + 1] = fmaf(v, xv.y, acc[4 * q + 1]);
+                            acc[4 * q + 2] = fmaf(v, xv.z, acc[4 * q + 2]);
+                            acc[4 * q + 3] = fmaf(v, xv.w, acc[4 * q + 3]);
+                        }
+                    }
+                }
+            }
+            if (kind)
+#pragma unroll
+                for (int c = 0; c < MU; c++)
+                    if (cb + c < mu)
+                        A[oslot * mu + cb + c] = acc[c] * osc;
+        }
+    }
+}
+
 template <typename F>
 void rhs_groups_each(int mu, F f) {
     int c0 = 0;
@@ -566,6 +680,22 @@ void launch_phase1_mixed(const P1Item *items, int nitems, const LrLeaf *lr, cons
         }
         HTGPU_CUDA(cudaGetLastError());
     });
+}
+
+void launch_phase1_stack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = std::min(nblocks, 8 * sms);
+    if (mu <= 4)
+        phase1_stack_kernel<4><<<grid, kStkThreads, 0, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A);
+    else if (mu <= 8)
+        phase1_stack_kernel<8><<<grid, kStkThreads, 0, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A);
+    else
+        phase1_stack_kernel<16><<<grid, kStkThreads, 0, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A);
+    HTGPU_CUDA(cudaGetLastError());
 }
 
 } // namespace htgpu

@@ -327,9 +327,12 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int
  * right-hand sides: HTGPU_PHASE1_TILES (one warp per tile, DFMA and emulated
  * tiles as two concurrent kernels) or HTGPU_PHASE1_STREAM (consecutive tile
  * chunks staged into shared memory by a producer warp with bulk copies and
- * shared by the CTA's consumer warps, the default).  Results agree within
- * the FP64 tolerance; the autotuner picks one.  No counterpart in the
- * reference. */
+ * shared by the CTA's consumer warps, the default).  Reduced-precision
+ * products with 3 or more right-hand sides off the tensor cores take, in
+ * HTGPU_PHASE1_STREAM, the tiles on the same x rows stacked into blocks of
+ * 128 columns with one thread per column.  Results agree within the
+ * storage policy's tolerance; the autotuner picks one.  No counterpart in
+ * the reference. */
 #define HTGPU_PHASE1_TILES 0
 #define HTGPU_PHASE1_STREAM 1
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);

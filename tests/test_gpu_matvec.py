@@ -367,6 +367,28 @@ def test_many_rhs(golden, eps):
     assert GH.device_status() == 0
 
 
+def test_stacked_phase1_matches_tile_kernels(golden):
+    """Reduced-precision products with 3 to 16 right-hand sides: phase-1
+    mode 1 (the tiles on the same x rows stacked, one thread per column)
+    and mode 0 (one warp per tile) agree within the reduced-precision
+    tolerance, and both stay within 1e-6 of the FP64 product."""
+    g, meta = golden("sphere6000_k1")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    X = {mu: G.rhs(n, mu, seed=40 + mu) for mu in (3, 4, 5, 8, 11, 16)}
+    y64 = {mu: GH.mvprod_global_to_global(X[mu], mu) for mu in X}
+    GH.set_precision("mixed")
+    for mu in X:
+        out = []
+        for mode in (H.PHASE1_STREAM, H.PHASE1_TILES):
+            GH.set_phase1_mode(mode)
+            out.append(GH.mvprod_global_to_global(X[mu], mu))
+        assert rel(out[0], out[1]) < 1e-6, mu
+        assert rel(out[0], y64[mu]) < 1e-6 and rel(out[1], y64[mu]) < 1e-6, mu
+    assert GH.device_status() == 0
+
+
 def test_autotune_keeps_parity(golden):
     g, meta = golden("sphere6000_k1")
     t = H.Cluster().build(g["xt"].shape[0], g["xt"])
