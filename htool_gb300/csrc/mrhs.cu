@@ -4,9 +4,10 @@
 // element meets mu coefficients.  These kernels keep one warp on one work
 // item (a phase-1 tile, a phase-2 row chunk), stage its operands in the
 // warp's shared memory with every load of a stage issued before the first
-// use, and apply each element to 16 right-hand sides per pass in the
-// double-float arithmetic of df64.cuh on the FP32 pipe (FP64-accurate, the
-// same arithmetic as the streamed kernels' emulated chunks).
+// use, and apply each element to 16 right-hand sides per pass (8 for a
+// product with at most 8) in the double-float arithmetic of df64.cuh on the
+// FP32 pipe (FP64-accurate, the same arithmetic as the streamed kernels'
+// emulated chunks).
 //
 //   phase1_df_mrhs_kernel   A = V^T X of the FP64 tiles (lane = tile column)
 //   phase2_df_mrhs_kernel   z = U A + D x over the FP64 chunks of a row chunk
@@ -20,7 +21,7 @@ namespace htgpu {
 namespace {
 
 constexpr int kDfWarps = 4;  // warps per CTA, one work item each
-constexpr int kDfRhs   = 16; // right-hand sides per pass
+constexpr int kDfRhs   = 16; // right-hand sides per pass at most (8 when a product has 8 or fewer)
 
 // ---------------------------------------------------------------------------
 // phase 1: per tile (jlen <= 256 rows x r columns, column-major, ld jlen),
@@ -30,6 +31,7 @@ constexpr int kP1DfSlab = 32, kP1DfLd = 33;
 constexpr int kP1DfWarp = 8 * kP1DfSlab * kP1DfLd + 8 * kP1DfSlab * kDfRhs;
 constexpr int kP1DfSmem = kDfWarps * kP1DfWarp;
 
+template <int R>
 __global__ void __launch_bounds__(32 * kDfWarps) phase1_df_mrhs_kernel(const P1Item *__restrict__ items, int nitems, const LrLeaf *__restrict__ lr, const double *__restrict__ fac,
                                                                        const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, double *__restrict__ A) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -47,11 +49,11 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase1_df_mrhs_kernel(const P1I
         const long long slot = L.a_off + (long long)(it.chunk & ~kEmuBit) * r;
         for (int kb = 0; kb < r; kb += 32) {
             const int k = kb + lane; // this lane's column
-            for (int cb = 0; cb < mu; cb += kDfRhs) {
-                const int nn = min(kDfRhs, mu - cb);
-                DF acc[kDfRhs];
+            for (int cb = 0; cb < mu; cb += R) {
+                const int nn = min(R, mu - cb);
+                DF acc[R];
 #pragma unroll
-                for (int cc = 0; cc < kDfRhs; cc++)
+                for (int cc = 0; cc < R; cc++)
                     df_zero(acc[cc]);
                 for (int js = 0; js < jlen; js += kP1DfSlab) {
                     const int nj = min(kP1DfSlab, jlen - js);
@@ -71,23 +73,23 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase1_df_mrhs_kernel(const P1I
                     }
                     // x slab: rows js .. js + nj, right-hand sides cb .. cb + 16
                     {
-                        float2 v[kP1DfSlab * kDfRhs / 32];
+                        float2 v[kP1DfSlab * R / 32];
 #pragma unroll
-                        for (int i = 0; i < kP1DfSlab * kDfRhs / 32; i++) {
-                            const int e = lane + 32 * i, j = e / kDfRhs, cc = e % kDfRhs;
+                        for (int i = 0; i < kP1DfSlab * R / 32; i++) {
+                            const int e = lane + 32 * i, j = e / R, cc = e % R;
                             v[i]        = (j < nj && cc < nn) ? __ldg(reinterpret_cast<const float2 *>(X) + (long long)(js + j) * mu + cb + cc) : make_float2(0.f, 0.f);
                         }
 #pragma unroll
-                        for (int i = 0; i < kP1DfSlab * kDfRhs / 32; i++)
+                        for (int i = 0; i < kP1DfSlab * R / 32; i++)
                             sx[lane + 32 * i] = v[i];
                     }
                     __syncwarp();
                     if (k < r)
                         for (int j = 0; j < nj; j++) {
                             const F2 u        = split64(sv[lane * kP1DfLd + j]);
-                            const float4 *xr = reinterpret_cast<const float4 *>(sx + j * kDfRhs);
+                            const float4 *xr = reinterpret_cast<const float4 *>(sx + j * R);
 #pragma unroll
-                            for (int q = 0; q < kDfRhs / 2; q++) {
+                            for (int q = 0; q < R / 2; q++) {
                                 const float4 xv = xr[q]; // the pairs of right-hand sides 2q, 2q + 1
                                 F2 b;
                                 b.hi = xv.x;
@@ -100,12 +102,12 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase1_df_mrhs_kernel(const P1I
                         }
                     if (k < r)
 #pragma unroll
-                        for (int cc = 0; cc < kDfRhs; cc++)
+                        for (int cc = 0; cc < R; cc++)
                             df_renorm(acc[cc]);
                 }
                 if (k < r)
 #pragma unroll
-                    for (int cc = 0; cc < kDfRhs; cc++)
+                    for (int cc = 0; cc < R; cc++)
                         if (cc < nn)
                             A[(slot + k) * mu + cb + cc] = scale_pow2_safe(df_to_double(acc[cc]), shift);
             }
@@ -120,6 +122,7 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase1_df_mrhs_kernel(const P1I
 constexpr int kP2DfWarp = kStreamStage + kStreamCols * kDfRhs * 8;
 constexpr int kP2DfSmem = kDfWarps * kP2DfWarp;
 
+template <int R>
 __global__ void __launch_bounds__(32 * kDfWarps) phase2_df_mrhs_kernel(const StreamChunk *__restrict__ chunks, const int *__restrict__ rc, int nrc, const unsigned char *__restrict__ fac,
                                                                        const unsigned char *__restrict__ pre, const int *__restrict__ cidx, const double *__restrict__ A,
                                                                        const F2 *__restrict__ xs, const int *__restrict__ xexp, int mu, double *__restrict__ z, int zlen, int add) {
@@ -138,11 +141,11 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase2_df_mrhs_kernel(const Str
             continue;
         const StreamChunk head = chunks[kb];
         const int h = head.h, zrow = head.b;
-        for (int cb = 0; cb < mu; cb += kDfRhs) {
-            const int nn = min(kDfRhs, mu - cb);
-            DF acc[kDfRhs];
+        for (int cb = 0; cb < mu; cb += R) {
+            const int nn = min(R, mu - cb);
+            DF acc[R];
 #pragma unroll
-            for (int cc = 0; cc < kDfRhs; cc++)
+            for (int cc = 0; cc < R; cc++)
                 df_zero(acc[cc]);
             for (int k = kb; k < ke; k++) {
                 const StreamChunk c = chunks[k];
@@ -155,12 +158,12 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase2_df_mrhs_kernel(const Str
                 {
                     // pairs [column][rhs]: a phase-1 sum (slot kx >= 0, FP64, brought to
                     // the units of the split x) or x (row ~kx, already split)
-                    float2 v[kStreamCols * kDfRhs / 32];
+                    float2 v[kStreamCols * R / 32];
 #pragma unroll
-                    for (int i = 0; i < kStreamCols * kDfRhs / 32; i++) {
-                        const int e = lane + 32 * i, tcol = e / kDfRhs, cc = e % kDfRhs;
-                        // columns 2i and 2i + 1 in this step: both below 32 or both above
-                        const int kh = 2 * i < 32 ? k0 : k1;
+                    for (int i = 0; i < kStreamCols * R / 32; i++) {
+                        const int e = lane + 32 * i, tcol = e / R, cc = e % R;
+                        // the 32 / R columns of this step: all below 32 or all above
+                        const int kh = 32 * i / R < 32 ? k0 : k1;
                         const int kx = __shfl_sync(0xffffffffu, kh, tcol & 31);
                         v[i]         = make_float2(0.f, 0.f);
                         if (tcol < c.ncol && cc < nn) {
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase2_df_mrhs_kernel(const Str
                         }
                     }
 #pragma unroll
-                    for (int i = 0; i < kStreamCols * kDfRhs / 32; i++)
+                    for (int i = 0; i < kStreamCols * R / 32; i++)
                         sx[lane + 32 * i] = v[i];
                 }
                 {
@@ -200,9 +203,9 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase2_df_mrhs_kernel(const Str
                         } else {
                             u = split64(reinterpret_cast<const double *>(sd)[lane + h * tcol]);
                         }
-                        const float4 *xr = reinterpret_cast<const float4 *>(sx + tcol * kDfRhs);
+                        const float4 *xr = reinterpret_cast<const float4 *>(sx + tcol * R);
 #pragma unroll
-                        for (int q = 0; q < kDfRhs / 2; q++) {
+                        for (int q = 0; q < R / 2; q++) {
                             const float4 xv = xr[q]; // the pairs of right-hand sides 2q, 2q + 1
                             F2 b;
                             b.hi = xv.x;
@@ -214,13 +217,13 @@ __global__ void __launch_bounds__(32 * kDfWarps) phase2_df_mrhs_kernel(const Str
                         }
                     }
 #pragma unroll
-                    for (int cc = 0; cc < kDfRhs; cc++)
+                    for (int cc = 0; cc < R; cc++)
                         df_renorm(acc[cc]);
                 }
             }
             if (lane < h)
 #pragma unroll
-                for (int cc = 0; cc < kDfRhs; cc++)
+                for (int cc = 0; cc < R; cc++)
                     if (cc < nn) {
                         double *zp     = z + (long long)(cb + cc) * zlen + zrow + lane;
                         const double v = scale_pow2_safe(df_to_double(acc[cc]), xe - 1023);
@@ -246,10 +249,15 @@ void raise_smem(K kernel, int bytes, unsigned long long &done) {
 void launch_phase1_df_mrhs(const P1Item *items, int nitems, const LrLeaf *lr, const double *factors, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;
-    static unsigned long long done = 0; // devices whose shared-memory limit was raised
-    raise_smem(phase1_df_mrhs_kernel, kP1DfSmem, done);
+    static unsigned long long done8 = 0, done16 = 0; // devices whose shared-memory limit was raised
     const int blocks = (nitems + kDfWarps - 1) / kDfWarps; // one warp per tile
-    phase1_df_mrhs_kernel<<<blocks, 32 * kDfWarps, kP1DfSmem, st>>>(items, nitems, lr, factors, xs, xexp, mu, A);
+    if (mu <= 8) { // one pass of 8 right-hand sides
+        raise_smem(phase1_df_mrhs_kernel<8>, kP1DfSmem, done8);
+        phase1_df_mrhs_kernel<8><<<blocks, 32 * kDfWarps, kP1DfSmem, st>>>(items, nitems, lr, factors, xs, xexp, mu, A);
+    } else {
+        raise_smem(phase1_df_mrhs_kernel<16>, kP1DfSmem, done16);
+        phase1_df_mrhs_kernel<16><<<blocks, 32 * kDfWarps, kP1DfSmem, st>>>(items, nitems, lr, factors, xs, xexp, mu, A);
+    }
     HTGPU_CUDA(cudaGetLastError());
 }
 
@@ -257,10 +265,15 @@ void launch_phase2_df_mrhs(const StreamChunk *chunks, const int *rc, int nrc, co
                            int mu, double *z, int zlen, bool add, cudaStream_t st) {
     if (nrc <= 0)
         return;
-    static unsigned long long done = 0;
-    raise_smem(phase2_df_mrhs_kernel, kP2DfSmem, done);
+    static unsigned long long done8 = 0, done16 = 0;
     const int blocks = (nrc + kDfWarps - 1) / kDfWarps; // one warp per row chunk
-    phase2_df_mrhs_kernel<<<blocks, 32 * kDfWarps, kP2DfSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, A, xs, xexp, mu, z, zlen, add ? 1 : 0);
+    if (mu <= 8) {
+        raise_smem(phase2_df_mrhs_kernel<8>, kP2DfSmem, done8);
+        phase2_df_mrhs_kernel<8><<<blocks, 32 * kDfWarps, kP2DfSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, A, xs, xexp, mu, z, zlen, add ? 1 : 0);
+    } else {
+        raise_smem(phase2_df_mrhs_kernel<16>, kP2DfSmem, done16);
+        phase2_df_mrhs_kernel<16><<<blocks, 32 * kDfWarps, kP2DfSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, A, xs, xexp, mu, z, zlen, add ? 1 : 0);
+    }
     HTGPU_CUDA(cudaGetLastError());
 }
 
