@@ -430,6 +430,8 @@ def run_gpu(args):
         "aca_seconds": aca_seconds,
         "assembly_breakdown_s": {"block_tree": float(info["GPU_block_tree_seconds"]), "aca_rounds": float(info["GPU_aca_seconds"]),
                                  "layout_and_uploads": float(info["GPU_build_seconds"]) - float(info["GPU_aca_seconds"]) - float(info["GPU_block_tree_seconds"]),
+                                 "layout_host_lists": float(info.get("GPU_layout_host_seconds", 0)), "layout_device_copies": float(info.get("GPU_layout_device_seconds", 0)),
+                                 "layout_launch_lists": float(info.get("GPU_layout_lists_seconds", 0)),
                                  "aca_blocks": int(info["GPU_aca_blocks"]), "aca_rounds_launched": int(float(info["GPU_aca_rounds"]))},
         "rank_predictor": predictor,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Number_of_false_positive", "Rank_max", "Rank_mean", "Compression_ratio")},

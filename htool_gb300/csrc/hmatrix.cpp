@@ -649,6 +649,7 @@ void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, 
 //  The arena holds all phase-1 tiles (item order), then all phase-2 blocks
 //  (item order), each block 16-byte aligned.
 void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vector<LeafSrc> &lr_src, const std::vector<LeafSrc> *dn_src, const KernelDesc *kd, const double *dxt, const double *dxs) {
+    const double tl0 = now();
     layout_gen_++; // buffers or launch lists change: captured products are stale
     transp_.reset();
     auto even = [](long long v) { return (v + 1) & ~1LL; };
@@ -810,7 +811,8 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
         while (zloc1_ < natoms && cuts[zloc1_] < lend)
             zloc1_++;
     }
-    arena_len = off;
+    const double tl1 = now();
+    arena_len        = off;
     fac.alloc(std::max<long long>(off, 2));
     HTGPU_CUDA(cudaMemsetAsync(fac.p, 0, sizeof(double) * (std::size_t)std::max<long long>(off, 2), stream_));
     for (std::size_t b = 0; b < bufs.size(); b++) {
@@ -844,6 +846,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
         HTGPU_CUDA(cudaStreamSynchronize(stream_));
         emu_ok_ = ef < 1023 + 60;
     }
+    const double tl2 = now();
     assign_phase1_modes();
     emu_fresh_ = false; // fac was rewritten
     upload_phase1_lists();
@@ -860,6 +863,9 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     if (lr_h.empty())
         lr_d.alloc(1);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    st_.layout_host_seconds   = tl1 - tl0;
+    st_.layout_device_seconds = tl2 - tl1;
+    st_.layout_lists_seconds  = now() - tl2;
     mu_cap     = 0;
     precision_ = 0;
 }
@@ -1985,6 +1991,9 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["GPU_aca_seconds"]          = num(st_.aca_seconds);
     m["GPU_block_tree_seconds"]   = num(st_.block_tree_seconds);
     m["GPU_build_seconds"]        = num(st_.build_seconds);
+    m["GPU_layout_host_seconds"]   = num(st_.layout_host_seconds);
+    m["GPU_layout_device_seconds"] = num(st_.layout_device_seconds);
+    m["GPU_layout_lists_seconds"]  = num(st_.layout_lists_seconds);
     m["GPU_stored_bytes"]         = inum(stored_bytes());
     m["GPU_phase1_items"]         = inum((long long)p1_h.size());
     m["GPU_phase2_items"]         = inum((long long)p2_h.size());

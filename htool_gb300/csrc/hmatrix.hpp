@@ -65,6 +65,9 @@ struct BuildStats {
     long long aca_blocks = 0;
     long long aca_scratch_bytes = 0, aca_peak_scratch_bytes = 0; // summed / largest slice of ACA scratch
     long long predicted_blocks = 0;                              // first attempts sized by the rank predictor
+    // the layout after the ACA rounds: host lists, device copies and fills
+    // (with the arena's allocation), launch lists and their uploads
+    double layout_host_seconds = 0, layout_device_seconds = 0, layout_lists_seconds = 0;
 };
 
 class Mlp;

@@ -198,43 +198,77 @@ __global__ void __launch_bounds__(32 * kMixWarps) phase1_mixed_kernel(const P1It
 // Phase 1 of reduced-precision products with 3 or more right-hand sides on
 // the CUDA cores.  The tiles on the same x rows are stacked into blocks of at
 // most 128 columns (TcBlock / TcSeg, the blocks of the tensor-core phase 1);
-// thread t of the CTA owns stacked column t.  Per 32-row slab the CTA stages
-// the block's columns (a warp copies one column's 32 rows at a time,
-// coalesced, BF16 widened to float) and the slab's x rows for MU
-// right-hand sides in shared memory; each thread then walks its column down
-// the slab, MU FMAs per element, and at the end writes its phase-1 sums times
-// the column's scale.  The contraction runs along each thread's own column,
-// so no shuffles are needed; sums are FP32 over a tile (at most 256 rows),
-// as in the other reduced-precision kernels.
+// thread t of the CTA owns stacked column t.  The block's segment table is
+// read once, in parallel, into shared memory.  The block's columns and x rows
+// go through shared memory in 32-row slabs by asynchronous copies (cp.async,
+// 4 bytes a lane: one FP32 row or two BF16 rows): a slab's copies are all in
+// flight at once and need no registers, so the CTA stays small (one buffer,
+// few registers) and many CTAs share an SM, each multiplying while others
+// wait for their copies.  Each thread walks its own column down the slab,
+// MU FMAs per element, and at the end writes its phase-1 sums times its
+// column's scale.  No shuffles; sums are FP32 over a tile (at most 256
+// rows), as in the other reduced-precision kernels.
 constexpr int kStkThreads = 128, kStkSlab = 32, kStkLd = 33;
 
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 template <int MU>
-__global__ void __launch_bounds__(kStkThreads) phase1_stack_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
+__global__ void __launch_bounds__(kStkThreads, 8) phase1_stack_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
                                                                   const float *__restrict__ scale, const F2 *__restrict__ xs, int mu, float *__restrict__ A) {
     static_assert(MU % 4 == 0, "x rows are read four right-hand sides at a time");
-    __shared__ float sv[kStkThreads * kStkLd];       // [stacked column][row of the slab]
-    __shared__ __align__(16) float sx[kStkSlab * MU]; // [row of the slab][right-hand side]
-    __shared__ long long cp[kStkThreads];            // byte offset of every stacked column in the reduced arena
-    __shared__ int ck[kStkThreads];                  // its kind: 0 none, 1 FP32, 2 BF16
+    __shared__ float sv[1][kStkThreads * kStkLd];        // [stacked column][row]: FP32, or BF16 pairs
+    __shared__ __align__(16) float sx[1][kStkSlab * MU]; // [row][right-hand side]
+    __shared__ TcSeg sseg[kStkThreads];                  // the block's segments (at most one per column)
+    __shared__ int sstart[kStkThreads + 1];              // first stacked column of every segment
+    __shared__ long long cp[kStkThreads];                // byte offset of every stacked column in the arena
+    __shared__ int ck[kStkThreads];                      // its kind: 0 none, 1 FP32, 2 BF16
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int bi = blockIdx.x; bi < nblocks; bi += gridDim.x) {
         const TcBlock B = blocks[bi];
+        const int nseg  = B.s1 - B.s0; // <= 128: every segment holds a column
         const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
-        int m0 = 0, sg = -1;
-        for (int s = B.s0; s < B.s1; s++) {
-            const int nc = segs[s].ncol;
-            if (tid < m0 + nc) {
-                sg = s;
-                break;
+        __syncthreads(); // the previous block's tables and buffers are no longer read
+        if (tid < nseg)
+            sseg[tid] = segs[B.s0 + tid];
+        __syncthreads();
+        if (wid == 0) { // first stacked column of every segment: a scan over four segments a lane
+            int part[4], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int sg = 4 * lane + q;
+                part[q]      = sum;
+                sum += sg < nseg ? sseg[sg].ncol : 0;
             }
-            m0 += nc;
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += v;
+            }
+            const int excl = incl - sum;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                sstart[4 * lane + q] = excl + part[q];
+            if (lane == 31)
+                sstart[kStkThreads] = incl;
         }
+        __syncthreads();
         long long off = 0, oslot = 0;
         int kind      = 0;
         float osc     = 0.f;
-        if (sg >= 0) {
-            const TcSeg S = segs[sg];
-            const int col = S.col0 + tid - m0;
+        if (tid < sstart[nseg]) {
+            int sg = 0;
+            while (sstart[sg + 1] <= tid)
+                sg++;
+            const TcSeg &S = sseg[sg];
+            const int k    = tid - sstart[sg];
+            const int col  = S.col0 + k;
             if (col < S.c32) {
                 off  = S.off + 4LL * l32 * col;
                 kind = 1;
@@ -242,62 +276,78 @@ __global__ void __launch_bounds__(kStkThreads) phase1_stack_kernel(const TcBlock
                 off  = S.off + 4LL * l32 * S.c32 + 2LL * l16 * (col - S.c32);
                 kind = 2;
             }
-            oslot = S.slot + (tid - m0);
-            osc   = scale[S.sidx + tid - m0];
+            oslot = S.slot + k;
+            osc   = scale[S.sidx + k];
         }
-        __syncthreads(); // the previous block's column table is no longer read
-        cp[tid]       = off;
-        ck[tid]       = kind;
-        const F2 *X   = xs + (long long)B.xrow * mu;
+        cp[tid] = off;
+        ck[tid] = kind;
+        __syncthreads();
+        const int ncols = sstart[nseg];
+        const F2 *X     = xs + (long long)B.xrow * mu;
+        // the copies of one slab into buffer b: warp w copies columns w + 4 q
+        // (lane = row, or pair of rows for BF16), every thread x elements
+        // (row, rhs) = tid + 128 i; rows past the tile and right-hand sides
+        // past mu are not copied (never read)
+        auto issue = [&](int js, int cb, int b) {
+            const int nj = min(kStkSlab, B.jlen - js);
+            for (int cc = wid; cc < ncols; cc += 4) {
+                float *dst = sv[b] + cc * kStkLd;
+                if (ck[cc] == 1) {
+                    if (lane < nj)
+                        cp_async4(dst + lane, reinterpret_cast<const float *>(mix + cp[cc]) + js + lane);
+                } else if (2 * lane < nj) {
+                    cp_async4(dst + lane, reinterpret_cast<const unsigned short *>(mix + cp[cc]) + js + 2 * lane);
+                }
+            }
+            for (int e = tid; e < kStkSlab * MU; e += kStkThreads) {
+                const int j = e / MU, c = e % MU;
+                if (j < nj && cb + c < mu)
+                    cp_async4(sx[b] + e, &X[(long long)(js + j) * mu + cb + c].hi);
+            }
+            cp_async_commit();
+        };
         for (int cb = 0; cb < mu; cb += MU) {
             float acc[MU];
 #pragma unroll
             for (int c = 0; c < MU; c++)
                 acc[c] = 0.f;
+            const int b = 0;
             for (int js = 0; js < B.jlen; js += kStkSlab) {
                 const int nj = min(kStkSlab, B.jlen - js);
-                __syncthreads(); // the column table is written; the previous slab is read out
-                // the block's columns: warp w copies columns w + 4 q, lane = row, eight loads in flight
-#pragma unroll 1
-                for (int q0 = 0; q0 < kStkThreads / 4; q0 += 8) {
-                    float v[8];
-#pragma unroll
-                    for (int q = 0; q < 8; q++) {
-                        const int cc = wid + 4 * (q0 + q);
-                        const int kd = ck[cc];
-                        v[q]         = 0.f;
-                        if (lane < nj) {
-                            if (kd == 1)
-                                v[q] = __ldg(reinterpret_cast<const float *>(mix + cp[cc]) + js + lane);
-                            else if (kd == 2)
-                                v[q] = bf16_to_f32(__ldg(reinterpret_cast<const unsigned short *>(mix + cp[cc]) + js + lane));
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < 8; q++)
-                        sv[(wid + 4 * (q0 + q)) * kStkLd + lane] = v[q];
-                }
-                // the slab's x rows for right-hand sides cb .. cb + MU
-                for (int e = tid; e < kStkSlab * MU; e += kStkThreads) {
-                    const int j = e / MU, c = e % MU;
-                    sx[e]       = (j < nj && cb + c < mu) ? __ldg(&X[(long long)(js + j) * mu + cb + c].hi) : 0.f;
-                }
+                issue(js, cb, b);
+                cp_async_wait<0>();
                 __syncthreads();
-                if (kind) {
-                    const float *colv = sv + tid * kStkLd;
+                const float *xsb = sx[b];
+                if (kind == 1) {
+                    const float *colv = sv[b] + tid * kStkLd;
                     for (int j = 0; j < nj; j++) {
-                        const float v     = colv[j];
-                        const float4 *xr = reinterpret_cast<const float4 *>(sx + j * MU);
+                        const float u    = colv[j];
+                        const float4 *xr = reinterpret_cast<const float4 *>(xsb + j * MU);
 #pragma unroll
                         for (int q = 0; q < MU / 4; q++) {
-                            const float4 xv  = xr[q];
-                            acc[4 * q]     = fmaf(v, xv.x, acc[4 * q]);
-                            acc[4 * q + 1] = fmaf(v, xv.y, acc[4 * q + 1]);
-                            acc[4 * q + 2] = fmaf(v, xv.z, acc[4 * q + 2]);
-                            acc[4 * q + 3] = fmaf(v, xv.w, acc[4 * q + 3]);
+                            const float4 x4  = xr[q];
+                            acc[4 * q]     = fmaf(u, x4.x, acc[4 * q]);
+                            acc[4 * q + 1] = fmaf(u, x4.y, acc[4 * q + 1]);
+                            acc[4 * q + 2] = fmaf(u, x4.z, acc[4 * q + 2]);
+                            acc[4 * q + 3] = fmaf(u, x4.w, acc[4 * q + 3]);
+                        }
+                    }
+                } else if (kind == 2) {
+                    const unsigned short *colh = reinterpret_cast<const unsigned short *>(sv[b] + tid * kStkLd);
+                    for (int j = 0; j < nj; j++) {
+                        const float u    = bf16_to_f32(colh[j]);
+                        const float4 *xr = reinterpret_cast<const float4 *>(xsb + j * MU);
+#pragma unroll
+                        for (int q = 0; q < MU / 4; q++) {
+                            const float4 x4  = xr[q];
+                            acc[4 * q]     = fmaf(u, x4.x, acc[4 * q]);
+                            acc[4 * q + 1] = fmaf(u, x4.y, acc[4 * q + 1]);
+                            acc[4 * q + 2] = fmaf(u, x4.z, acc[4 * q + 2]);
+                            acc[4 * q + 3] = fmaf(u, x4.w, acc[4 * q + 3]);
                         }
                     }
                 }
+                __syncthreads(); // the slab is read out before the next one's copies
             }
             if (kind)
 #pragma unroll
