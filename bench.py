@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--n", type=int, default=WORKLOAD["n"])
+    p.add_argument("--mu", type=int, default=WORKLOAD["mu"], help="sphere workload: right-hand sides per product")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-predictor", action="store_true", help="skip the rank-predictor rebuild")
     p.add_argument("--no-batched", action="store_true", help="skip the batched workload (the `batched` key)")
@@ -153,7 +154,7 @@ class Clocks:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference(n, reps, single_thread_reps=1, x=None, warmup=1):
+def cpu_reference(n, reps, single_thread_reps=1, x=None, warmup=1, mu=1):
     """The CPU restatement of htool's product (oracle/htool_oracle.c, pinned
     to upstream htool) on the same workload: its assembly (HMatrix::build
     with partialACA, timed), then `reps` products on all host cores (median
@@ -172,22 +173,22 @@ def cpu_reference(n, reps, single_thread_reps=1, x=None, warmup=1):
     H = O.hmatrix(t, t, pts, pts, 1, WORKLOAD["epsilon"], WORKLOAD["eta"])
     build_s = time.perf_counter() - t0
     if x is None:
-        x = G.rhs(n, 1, seed=2)
+        x = G.rhs(n, mu, seed=2)
     for _ in range(max(0, warmup - 1)):  # time_mvprod warms up once more itself
-        H.mvprod(x, 1)
-    sec = H.time_mvprod(x, 1, reps)
-    y = H.mvprod(x, 1)
-    out = {"value": 1.0 / sec, "unit": UNIT, "cores": threads, "kind": "port",
+        H.mvprod(x, mu)
+    sec = H.time_mvprod(x, mu, reps)
+    y = H.mvprod(x, mu)
+    out = {"value": mu / sec, "unit": UNIT, "cores": threads, "kind": "port",
            "sample": "%d products (median, after %d warm-up) of the N=%d Laplace-sphere H-matrix on %d threads; its assembly (%.2f s) not in the figure" % (reps, max(1, warmup), n, threads, build_s),
            "build_seconds": build_s, "threads": threads}
     if single_thread_reps:
         O.set_num_threads(1)
         t1 = time.perf_counter()
         for _ in range(single_thread_reps):
-            H.mvprod(x, 1)
+            H.mvprod(x, mu)
         st = (time.perf_counter() - t1) / single_thread_reps
         O.set_num_threads(threads)
-        out["single_thread"] = {"value": 1.0 / st, "unit": UNIT, "cores": 1, "sample": "%d product(s), one thread" % single_thread_reps}
+        out["single_thread"] = {"value": mu / st, "unit": UNIT, "cores": 1, "sample": "%d product(s), one thread" % single_thread_reps}
     lr, dn = H.leaves()
     return out, y, (lr, dn)
 
@@ -196,9 +197,9 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    cb, _, _ = cpu_reference(args.n, reps=max(args.steps, 3), single_thread_reps=0, warmup=args.warmup)
+    cb, _, _ = cpu_reference(args.n, reps=max(args.steps, 3), single_thread_reps=0, warmup=args.warmup, mu=args.mu)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)", "config": dict(WORKLOAD, n=args.n),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)", "config": dict(WORKLOAD, n=args.n, mu=args.mu),
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "aca_seconds": cb["build_seconds"]}
     print(json.dumps(line), flush=True)
@@ -256,9 +257,10 @@ def run_gpu(args):
     aca_seconds = time.perf_counter() - t0
     info = hm.get_infos()
 
-    x = G.rhs(n, 1, seed=2)
+    mu = args.mu
+    x = G.rhs(n, mu, seed=2)
     xd = torch.from_numpy(x).cuda()
-    yd = torch.empty(n, dtype=torch.float64, device="cuda")
+    yd = torch.empty(n * mu, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
@@ -266,12 +268,12 @@ def run_gpu(args):
 
     def timed_products():
         for _ in range(args.warmup):
-            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
+            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), mu, 0, sp)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), 1, 0, sp)
+            hm.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), mu, 0, sp)
         e1.record(stream)
         barrier()
         return max_over_ranks(e0.elapsed_time(e1)), hm.last_launches()
@@ -280,15 +282,15 @@ def run_gpu(args):
         """the product through the C ABI with host buffers: pinned x copied
         in, y copied out, inside the timed region, every step"""
         xh = torch.from_numpy(x).pin_memory()
-        yh = torch.empty(n, dtype=torch.float64).pin_memory()
+        yh = torch.empty(n * mu, dtype=torch.float64).pin_memory()
         for _ in range(max(2, args.warmup)):
-            hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
+            hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), mu, H.HOST_PTRS, None)
         barrier()
         w0 = time.perf_counter()
         for _ in range(args.steps):
-            hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), 1, H.HOST_PTRS, None)
+            hm.mvprod_ptr(xh.data_ptr(), yh.data_ptr(), mu, H.HOST_PTRS, None)
         e2e_s = max_over_ranks(time.perf_counter() - w0)
-        return {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n}
+        return {"value": world * args.steps * mu / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n * mu, "d2h_bytes_per_step": 8 * n * mu}
 
     def profiled_traffic(kernel, precision, algorithmic):
         """DRAM bytes per launch of `kernel` from the committed ncu summaries
@@ -313,9 +315,18 @@ def run_gpu(args):
     def describe(ms_total, precision):
         """per-step numbers, phase breakdown and the dominant kernel's roofline"""
         ms_step = ms_total / args.steps
-        ph = hm.profile(1, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
-        pb = hm.phase_bytes(1)
-        names = ["gather_split_kernel", "phase 1 (tile kernels)" if hm.get_phase1_mode() == 0 else "phase1_cta_kernel", "phase2_warp_kernel" if hm.get_phase2_mode() == 0 else "phase2_ws_kernel", "zsum_kernel"]
+        ph = hm.profile(mu, max(3, args.steps // 3))  # gather, phase 1, phase 2, sums, total
+        pb = hm.phase_bytes(mu)
+        mode1 = hm.get_phase1_mode()
+        run = hm.get_rhs_bucket(mu) if mu <= 8 else mu
+        if run <= 2:
+            p1 = "phase 1 (tile kernels)" if mode1 == 0 else "phase1_cta_kernel"
+        elif precision != "fp64":
+            p1 = "phase1_mixed_kernel" if mode1 == 0 else "phase1_stack_kernel"
+        else:
+            p1 = "phase1_df_mrhs_kernel" if run >= 8 else "phase 1 (tile kernels)"
+        p2 = "phase2_df_mrhs_kernel" if (precision == "fp64" and run >= 8) else ("phase2_warp_kernel" if hm.get_phase2_mode() == 0 else "phase2_ws_kernel")
+        names = ["gather_split_kernel", p1, p2, "zsum_kernel"]
         k = max(range(4), key=lambda i: ph[i])
         achieved = pb[k] / (ph[k] / 1e3) / 1e9
         total_bytes = sum(pb)
@@ -343,7 +354,7 @@ def run_gpu(args):
             hm.set_phase2_mode(args.phase2_mode)
         tune64 = None
     else:
-        tune64 = hm.autotune(1, 5)
+        tune64 = hm.autotune(mu, 5)
     split = hm.get_fp64_split()
     p1mode64, p2mode64 = hm.get_phase1_mode(), hm.get_phase2_mode()
     ms64, launches64 = timed_products()
@@ -362,7 +373,7 @@ def run_gpu(args):
             hm.set_phase2_mode(args.mixed_phase2_mode)
         tunem = None
     else:
-        tunem = hm.autotune(1, 5)
+        tunem = hm.autotune(mu, 5)
     splitm = hm.get_fp64_split()[1]
     msm, launchesm = timed_products()
     ym = yd.cpu().numpy().copy()
@@ -370,11 +381,11 @@ def run_gpu(args):
     e2em = timed_e2e()
     pinfo = hm.precision_info()
     clk = clocks.stop()
-    value64 = world * args.steps / (ms64 / 1e3)
-    valuem = world * args.steps / (msm / 1e3)
+    value64 = world * args.steps * mu / (ms64 / 1e3)
+    valuem = world * args.steps * mu / (msm / 1e3)
     status = hm.device_status()
     hm.set_precision("fp64")
-    rows, dense_ref = sampled_dense_rows(pts, x)
+    rows, dense_ref = sampled_dense_rows(pts, x[:n])  # the first right-hand side
 
     # learned rank predictor: trained on the (geometry, crosses) pairs this
     # build's partialACA produced, then the same mesh re-assembled with it
@@ -410,12 +421,12 @@ def run_gpu(args):
             torch.distributed.destroy_process_group()
         return
     err_mixed_vs_fp64 = float(np.linalg.norm(ym - y64) / np.linalg.norm(y64))
-    dense_err = {k: float(np.linalg.norm(v[rows] - dense_ref) / np.linalg.norm(dense_ref)) for k, v in (("fp64", y64), ("mixed", ym))}
+    dense_err = {k: float(np.linalg.norm(v[:n][rows] - dense_ref) / np.linalg.norm(dense_ref)) for k, v in (("fp64", y64), ("mixed", ym))}
     line = {
         "metric": METRIC, "value": value64, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step64, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
         "data": "synthetic (seeded points on the unit sphere, N(0,1) right-hand side)",
-        "config": dict(WORKLOAD, n=n),
+        "config": dict(WORKLOAD, n=n, mu=mu),
         "run": {"precision": "fp64", "parallelism": "replicas" if world > 1 else "single", "stored_gb": {"fp64": d64["whole_product"]["bytes"] / 1e9, "mixed": dm["whole_product"]["bytes"] / 1e9}},
         "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
         "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64, "phase1_mode": p1mode64, "phase2_mode": p2mode64},
@@ -438,7 +449,7 @@ def run_gpu(args):
         "batched": batched,
     }
     if not args.no_cpu_baseline:
-        cb, y_ref, ref_leaves = cpu_reference(n, reps=5, single_thread_reps=1, x=x)
+        cb, y_ref, ref_leaves = cpu_reference(n, reps=5, single_thread_reps=1, x=x, mu=mu)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread")}
         line["cpu_aca_seconds"] = cb["build_seconds"]
         line["rel_err_vs_reference"] = {
