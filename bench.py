@@ -294,8 +294,9 @@ def run_gpu(args):
 
     def profiled_traffic(kernel, precision, algorithmic):
         """DRAM bytes per launch of `kernel` from the committed ncu summaries
-        (lines "traffic: kernel=K precision=P n=N bytes_per_launch=B
-        algorithmic=A"): the captured launch's DRAM bytes scaled to this
+        (lines "traffic: kernel=K precision=P n=N [mu=M] bytes_per_launch=B
+        algorithmic=A", mu 1 when absent; the same kernel, storage and
+        right-hand sides): the captured launch's DRAM bytes scaled to this
         launch by its algorithmic bytes (traffic grows with the bytes
         streamed); None when no capture covers the kernel"""
         pdir = os.path.join(ROOT, "profiles")
@@ -307,7 +308,7 @@ def run_gpu(args):
             for line in open(os.path.join(pdir, name)):
                 if line.startswith("traffic:"):
                     kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
-                    if kv.get("kernel") == kernel and kv.get("precision") == precision and "algorithmic" in kv:
+                    if kv.get("kernel") == kernel and kv.get("precision") == precision and kv.get("mu", "1") == str(mu) and "algorithmic" in kv:
                         ratio = int(kv["bytes_per_launch"]) / int(kv["algorithmic"])
                         return int(round(ratio * algorithmic)), "profiles/%s (n=%s capture, DRAM/algorithmic %.3f, scaled to this launch)" % (name, kv.get("n"), ratio)
         return None, None

@@ -279,10 +279,47 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
     std::vector<Accepted> acc;
     std::vector<std::unique_ptr<DevBuf<double>>> round_bufs;
     const double ta = now();
+    // first attempts sized by the rank predictor (when one is set): the
+    // blocks' features in parallel, one inference launch
+    auto predict_caps = [&](const std::vector<int> &fresh) {
+        if (fresh.empty())
+            return;
+        std::vector<float> fx(fresh.size() * kMlpIn), fy(fresh.size());
+        host_parallel_chunks((long long)fresh.size(), 4096, [&](long long lo, long long hi) {
+            for (long long i = lo; i < hi; i++) {
+                const ClusterNode &tn = Ta.nodes[reqs[fresh[i]].t], &sn = Sa.nodes[reqs[fresh[i]].s];
+                block_features(tn.size, sn.size, tn.rad, sn.rad, tn.ctr, sn.ctr, eps_, kd.id, &fx[i * kMlpIn]);
+            }
+        });
+        predictor_->predict(fx.data(), (int)fresh.size(), fy.data());
+        for (std::size_t i = 0; i < fresh.size(); i++) {
+            Req &r         = reqs[fresh[i]];
+            const int qmax = max_profitable_rank(Ta.nodes[r.t].size, Sa.nodes[r.s].size);
+            const float pr = fy[i];
+            const int want = pr >= 60.f ? qmax : (int)std::ceil(std::max(pr, 0.f) * (1.0 + margin_)) + 2;
+            r.cap          = std::max(1, std::min(qmax, std::max(want, 4)));
+            st_.predicted_blocks++;
+        }
+    };
     while (!pending.empty()) {
+        // the work of a block is about (M + N) generator entries per cross:
+        // with a predictor, blocks are taken in the order of their predicted
+        // work (the largest first, so the CTAs of a launch finish together),
+        // otherwise by size
+        if (predictor_) {
+            std::vector<int> fresh;
+            for (int id : pending)
+                if (reqs[id].cap == 0)
+                    fresh.push_back(id);
+            predict_caps(fresh);
+        }
         std::sort(pending.begin(), pending.end(), [&](int a, int b) {
             long long ca = (long long)Ta.nodes[reqs[a].t].size + Sa.nodes[reqs[a].s].size;
             long long cb = (long long)Ta.nodes[reqs[b].t].size + Sa.nodes[reqs[b].s].size;
+            if (predictor_) {
+                ca *= reqs[a].cap;
+                cb *= reqs[b].cap;
+            }
             return ca != cb ? ca > cb : a < b;
         });
         std::size_t free_b = 0, total_b = 0;
@@ -298,22 +335,7 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
                 for (std::size_t k = pos; k < pending.size(); k++)
                     if (reqs[pending[k]].cap == 0)
                         fresh.push_back(pending[k]);
-                if (!fresh.empty()) {
-                    std::vector<float> fx(fresh.size() * kMlpIn), fy(fresh.size());
-                    for (std::size_t i = 0; i < fresh.size(); i++) {
-                        const ClusterNode &tn = Ta.nodes[reqs[fresh[i]].t], &sn = Sa.nodes[reqs[fresh[i]].s];
-                        block_features(tn.size, sn.size, tn.rad, sn.rad, tn.ctr, sn.ctr, eps_, kd.id, &fx[i * kMlpIn]);
-                    }
-                    predictor_->predict(fx.data(), (int)fresh.size(), fy.data());
-                    for (std::size_t i = 0; i < fresh.size(); i++) {
-                        Req &r         = reqs[fresh[i]];
-                        const int qmax = max_profitable_rank(Ta.nodes[r.t].size, Sa.nodes[r.s].size);
-                        const float pr = fy[i];
-                        const int want = pr >= 60.f ? qmax : (int)std::ceil(std::max(pr, 0.f) * (1.0 + margin_)) + 2;
-                        r.cap          = std::max(1, std::min(qmax, std::max(want, 4)));
-                        st_.predicted_blocks++;
-                    }
-                }
+                predict_caps(fresh);
             }
             // a slice of requests whose scratch fits the budget.  With
             // sympartialACA a block whose target comes before its source is
@@ -685,25 +707,28 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     // every group owns a slice of the partial-sum vector z (|tau| rows), cut
     // into balanced chunks of <= kRowChunk rows, one phase-2 item each,
     // listing the group's leaves (dense, then low-rank, each by offset_j)
-    std::map<std::pair<int, int>, int> gid;
     std::vector<std::pair<int, int>> groups; // (offset_i, m)
     std::vector<std::vector<int>> members;   // ~d for dense leaf d, l for low-rank leaf l
-    auto group_of = [&](int oi, int m) {
-        auto key = std::make_pair(oi, m);
-        auto f   = gid.find(key);
-        if (f != gid.end())
-            return f->second;
-        int g    = (int)groups.size();
-        gid[key] = g;
-        groups.push_back(key);
-        members.emplace_back();
-        return g;
-    };
-    for (int d = 0; d < (int)dn_h.size(); d++)
-        members[group_of(dn_h[d].oi, dn_h[d].m)].push_back(~d);
-    for (int l = 0; l < (int)lr_h.size(); l++)
-        if (lr_h[l].r > 0)
-            members[group_of(lr_h[l].oi, lr_h[l].m)].push_back(l);
+    {
+        // leaves sorted by (offset_i, m), dense first, each kind in its own
+        // order: the groups and their members without a map lookup per leaf
+        std::vector<std::pair<std::pair<int, int>, long long>> keyed; // ((oi, m), order)
+        keyed.reserve(dn_h.size() + lr_h.size());
+        for (int d = 0; d < (int)dn_h.size(); d++)
+            keyed.push_back({{dn_h[d].oi, dn_h[d].m}, (long long)d});
+        for (int l = 0; l < (int)lr_h.size(); l++)
+            if (lr_h[l].r > 0)
+                keyed.push_back({{lr_h[l].oi, lr_h[l].m}, (long long)dn_h.size() + l});
+        std::stable_sort(keyed.begin(), keyed.end(), [](const std::pair<std::pair<int, int>, long long> &a, const std::pair<std::pair<int, int>, long long> &b) { return a.first < b.first; });
+        for (std::size_t k = 0; k < keyed.size(); k++) {
+            if (k == 0 || keyed[k].first != keyed[k - 1].first) {
+                groups.push_back(keyed[k].first);
+                members.emplace_back();
+            }
+            const long long o = keyed[k].second;
+            members.back().push_back(o < (long long)dn_h.size() ? ~(int)o : (int)(o - (long long)dn_h.size()));
+        }
+    }
     std::vector<int> gorder(groups.size());
     std::iota(gorder.begin(), gorder.end(), 0);
     std::sort(gorder.begin(), gorder.end(), [&](int a, int b) { return groups[a].first != groups[b].first ? groups[a].first < groups[b].first : groups[a].second > groups[b].second; });
@@ -713,62 +738,103 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
         zbase[g] = zlen_ - groups[g].first; // z index of cluster row i is i + zbase
         zlen_ += groups[g].second;
     }
-    p2_h.clear();
-    c_h.clear();
-    c_leaf.clear();
-    p2_row_h.clear();
-    pan_h.clear();
-    cidx_h.clear();
-    for (int g : gorder) {
-        const int oi = groups[g].first, m = groups[g].second;
+    // sizes of every group's row chunks (first pass), then every list filled
+    // at its own positions in parallel (second pass)
+    const std::size_t ng = gorder.size();
+    std::vector<long long> g_off(ng + 1, 0), g_c(ng + 1, 0), g_q(ng + 1, 0), g_p(ng + 1, 0);
+    for (std::size_t gi = 0; gi < ng; gi++) {
+        const int g = gorder[gi], m = groups[g].second;
         const int nchunk = (m + kRowChunk - 1) / kRowChunk;
+        long long width = 0;
+        for (int leaf : members[g])
+            width += leaf >= 0 ? lr_h[leaf].r : dn_h[~leaf].n;
+        long long bytes = 0;
         for (int q = 0; q < nchunk; q++) {
             const int lo = (int)((long long)m * q / nchunk), hi = (int)((long long)m * (q + 1) / nchunk);
-            P2Item it;
-            it.row0 = (int)(oi + lo + zbase[g]); // z index of the chunk's first row
-            it.h    = hi - lo;
-            it.cbeg = (int)c_h.size();
-            PanelItem pi;
-            pi.off  = off;
-            pi.row0 = it.row0;
-            pi.h    = it.h;
-            pi.q0   = (int)cidx_h.size();
-            long long col = 0;
-            for (int leaf : members[g]) { // dense leaves come first in members
-                P2Contrib pc;
-                pc.off = off + (long long)it.h * col;
-                if (leaf >= 0) {
-                    const LrLeaf &L = lr_h[leaf];
-                    pc.w            = L.r;
-                    pc.aux          = (int)L.a_off;
-                    copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + lo, pc.off, it.h, L.r, L.m, lr_src[leaf].neg ? 1 | (lo & 1) << 1 : 0});
-                    for (int k = 0; k < L.r; k++)
-                        cidx_h.push_back((int)L.a_off + k);
-                } else {
-                    const DenseLeaf &D = dn_h[~leaf];
-                    pc.w               = D.n;
-                    pc.aux             = ~D.oj;
-                    const LeafSrc *ds = dn_src ? &(*dn_src)[~leaf] : nullptr;
-                    if (ds && ds->tr) // rows lo.. of the transposed block: columns lo.. of the stored one (D.n x D.m)
-                        copies[ds->buf].push_back({ds->su + (long long)D.n * lo, pc.off, it.h, D.n, D.n, (ds->neg ? 1 | (lo & 1) << 1 : 0) | 4});
-                    else if (ds)
-                        copies[ds->buf].push_back({ds->su + lo, pc.off, it.h, D.n, D.m, ds->neg ? 1 | (lo & 1) << 1 : 0});
-                    else
-                        fills.push_back({pc.off, oi + lo, it.h, D.oj, D.n, dense_mode(~leaf), 0});
-                    for (int j = 0; j < D.n; j++)
-                        cidx_h.push_back(~(D.oj + j));
-                }
-                col += pc.w;
-                c_h.push_back(pc);
-                c_leaf.push_back(leaf);
-            }
-            pi.ncol = (int)col;
-            off += even((long long)it.h * col);
-            it.cend = (int)c_h.size();
-            p2_h.push_back(it);
-            p2_row_h.push_back(oi + lo);
-            pan_h.push_back(pi);
+            bytes += even((long long)(hi - lo) * width);
         }
+        g_off[gi + 1] = g_off[gi] + bytes;
+        g_c[gi + 1]   = g_c[gi] + (long long)nchunk * (long long)members[g].size();
+        g_q[gi + 1]   = g_q[gi] + (long long)nchunk * width;
+        g_p[gi + 1]   = g_p[gi] + nchunk;
+    }
+    p2_h.assign((std::size_t)g_p[ng], P2Item{});
+    p2_row_h.assign((std::size_t)g_p[ng], 0);
+    pan_h.assign((std::size_t)g_p[ng], PanelItem{});
+    c_h.assign((std::size_t)g_c[ng], P2Contrib{});
+    c_leaf.assign((std::size_t)g_c[ng], 0);
+    cidx_h.assign((std::size_t)g_q[ng], 0);
+    const long long off_p2 = off;
+    constexpr long long kGroupGrain = 512;
+    const long long nranges = ((long long)ng + kGroupGrain - 1) / kGroupGrain;
+    std::vector<std::vector<std::vector<BlockCopy>>> rcopies((std::size_t)nranges, std::vector<std::vector<BlockCopy>>(bufs.size()));
+    std::vector<std::vector<DenseChunk>> rfills((std::size_t)nranges);
+    host_parallel_for(nranges, [&](long long rg) {
+        auto &my_copies = rcopies[(std::size_t)rg];
+        auto &my_fills  = rfills[(std::size_t)rg];
+        const std::size_t g_end = std::min<std::size_t>(ng, (std::size_t)((rg + 1) * kGroupGrain));
+        for (std::size_t gi = (std::size_t)(rg * kGroupGrain); gi < g_end; gi++) {
+            const int g = gorder[gi];
+            const int oi = groups[g].first, m = groups[g].second;
+            const int nchunk = (m + kRowChunk - 1) / kRowChunk;
+            long long poff = off_p2 + g_off[gi];
+            long long cpos = g_c[gi], qpos = g_q[gi], ppos = g_p[gi];
+            for (int q = 0; q < nchunk; q++) {
+                const int lo = (int)((long long)m * q / nchunk), hi = (int)((long long)m * (q + 1) / nchunk);
+                P2Item it;
+                it.row0 = (int)(oi + lo + zbase[g]); // z index of the chunk's first row
+                it.h    = hi - lo;
+                it.cbeg = (int)cpos;
+                PanelItem pi;
+                pi.off  = poff;
+                pi.row0 = it.row0;
+                pi.h    = it.h;
+                pi.q0   = (int)qpos;
+                long long col = 0;
+                for (int leaf : members[g]) { // dense leaves come first in members
+                    P2Contrib pc;
+                    pc.off = poff + (long long)it.h * col;
+                    if (leaf >= 0) {
+                        const LrLeaf &L = lr_h[leaf];
+                        pc.w            = L.r;
+                        pc.aux          = (int)L.a_off;
+                        my_copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + lo, pc.off, it.h, L.r, L.m, lr_src[leaf].neg ? 1 | (lo & 1) << 1 : 0});
+                        for (int k = 0; k < L.r; k++)
+                            cidx_h[(std::size_t)qpos++] = (int)L.a_off + k;
+                    } else {
+                        const DenseLeaf &D = dn_h[~leaf];
+                        pc.w               = D.n;
+                        pc.aux             = ~D.oj;
+                        const LeafSrc *ds = dn_src ? &(*dn_src)[~leaf] : nullptr;
+                        if (ds && ds->tr) // rows lo.. of the transposed block: columns lo.. of the stored one (D.n x D.m)
+                            my_copies[ds->buf].push_back({ds->su + (long long)D.n * lo, pc.off, it.h, D.n, D.n, (ds->neg ? 1 | (lo & 1) << 1 : 0) | 4});
+                        else if (ds)
+                            my_copies[ds->buf].push_back({ds->su + lo, pc.off, it.h, D.n, D.m, ds->neg ? 1 | (lo & 1) << 1 : 0});
+                        else
+                            my_fills.push_back({pc.off, oi + lo, it.h, D.oj, D.n, dense_mode(~leaf), 0});
+                        for (int j = 0; j < D.n; j++)
+                            cidx_h[(std::size_t)qpos++] = ~(D.oj + j);
+                    }
+                    col += pc.w;
+                    c_h[(std::size_t)cpos]    = pc;
+                    c_leaf[(std::size_t)cpos] = leaf;
+                    cpos++;
+                }
+                pi.ncol = (int)col;
+                poff += even((long long)it.h * col);
+                it.cend                    = (int)cpos;
+                p2_h[(std::size_t)ppos]     = it;
+                p2_row_h[(std::size_t)ppos] = oi + lo;
+                pan_h[(std::size_t)ppos]    = pi;
+                ppos++;
+            }
+        }
+    });
+    off = off_p2 + g_off[ng];
+    for (long long rg = 0; rg < nranges; rg++) {
+        for (std::size_t b = 0; b < bufs.size(); b++)
+            copies[b].insert(copies[b].end(), rcopies[(std::size_t)rg][b].begin(), rcopies[(std::size_t)rg][b].end());
+        fills.insert(fills.end(), rfills[(std::size_t)rg].begin(), rfills[(std::size_t)rg].end());
     }
     // z sums: target rows cut at every group boundary into atoms; every atom
     // lists the z bases of the groups covering it, largest group first
@@ -1006,20 +1072,42 @@ void HMatrix::upload_phase1_lists() {
     std::vector<StreamChunk> ch;
     n_p2_dfma_ = n_p2_emu_ = 0;
     p2_bytes_ = n_cols_ = 0;
+    {
+        // every panel's chunks, generated in parallel over ranges of panels
+        // and concatenated in panel order
+        constexpr long long kPanelGrain = 4096;
+        const long long npan            = (long long)pan_h.size();
+        const long long nranges         = (npan + kPanelGrain - 1) / kPanelGrain;
+        std::vector<std::vector<StreamChunk>> part((std::size_t)nranges);
+        host_parallel_for(nranges, [&](long long rg) {
+            const long long e = std::min(npan, (rg + 1) * kPanelGrain);
+            for (long long q = rg * kPanelGrain; q < e; q++) {
+                const PanelItem &pi     = pan_h[(std::size_t)q];
+                auto &out               = part[(std::size_t)rg];
+                const std::size_t first = out.size();
+                stream_section(out, 8 * pi.off, 8, pi.h, pi.ncol, pi.q0, pi.row0, kStreamDfma, 0);
+                out[first].flags |= kStreamFirst;
+                out.back().flags |= kStreamLast;
+            }
+        });
+        std::size_t total = 0;
+        for (auto &pv : part)
+            total += pv.size();
+        ch.reserve(total + 1);
+        for (auto &pv : part)
+            ch.insert(ch.end(), pv.begin(), pv.end());
+    }
+    for (std::size_t k = 0; k < ch.size(); k++) {
+        const long long e = (long long)ch[k].h * ch[k].ncol;
+        seen += e;
+        if (target >= 1.0 || (double)dfma < target * (double)seen)
+            dfma += e;
+        else
+            ch[k].kind = kStreamEmu;
+        if (ch[k].flags & kStreamFirst)
+            (ch[k].kind == kStreamDfma ? n_p2_dfma_ : n_p2_emu_)++;
+    }
     for (auto &pi : pan_h) {
-        const std::size_t first = ch.size();
-        stream_section(ch, 8 * pi.off, 8, pi.h, pi.ncol, pi.q0, pi.row0, kStreamDfma, 0);
-        for (std::size_t k = first; k < ch.size(); k++) {
-            const long long e = (long long)ch[k].h * ch[k].ncol;
-            seen += e;
-            if (target >= 1.0 || (double)dfma < target * (double)seen)
-                dfma += e;
-            else
-                ch[k].kind = kStreamEmu;
-        }
-        ch[first].flags |= kStreamFirst;
-        ch.back().flags |= kStreamLast;
-        (ch[first].kind == kStreamDfma ? n_p2_dfma_ : n_p2_emu_)++;
         p2_bytes_ += 8LL * pi.h * pi.ncol;
         n_cols_ += pi.ncol;
     }
@@ -1490,10 +1578,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
             }
         } else if (p2_mode_ == 1)
             launch_phase2_producer(scm_d.p, sum_d.p, n_units_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
-                                   (int)zlen_, status_d.p, st);
+                                   (int)zlen_, status_d.p, st, p2_gmax_);
         else
             launch_phase2_stream(scm_d.p, srm_d.p, n_ranges_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
-                                 (int)zlen_, status_d.p, st);
+                                 (int)zlen_, status_d.p, st, p2_gmax_);
         if (marks)
             HTGPU_CUDA(cudaEventRecord(marks[2], st));
         launch_sums(y, mu_out, numbering, w_z, st);
@@ -1539,10 +1627,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
             launch_phase2_df_mrhs(sc_d.p, p2rc_d.p, n_p2rc_, arena, pre, cidx_d.p, w_A, w_xs, w_xexp, mu, w_z, (int)zlen_, false, st);
             launches_ += 1;
         } else if (p2_mode_ == 1) {
-            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_producer(sc_d.p, su_d.p, n_units_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st, p2_gmax_);
             launches_ += groups;
         } else {
-            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_stream(sc_d.p, sr_d.p, n_ranges_, tickets_d.p, arena, arena, pre, cidx_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z, (int)zlen_, status_d.p, st, p2_gmax_);
             launches_ += groups;
         }
         if (marks)
@@ -1687,6 +1775,21 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         rhs_pad_[mu]        = t_pad < t_split ? bucket : 0;
         best                = std::min(t_split, t_pad);
         layout_gen_++;
+    }
+    // the streamed phase 2 with 8 or more right-hand sides (reduced
+    // precision off the tensor cores): passes of 8, or of 4
+    {
+        const int run  = rhs_run(mu);
+        const bool tcs = run >= kMmaMinRhs && eps_ >= kMmaMinEps;
+        if (precision_ != 0 && run >= 8 && !tcs) {
+            p2_gmax_         = 8;
+            const float t8   = timed();
+            p2_gmax_         = 4;
+            const float t4   = timed();
+            p2_gmax_         = t4 < t8 ? 4 : 8;
+            best             = std::min(t4, t8);
+            layout_gen_++;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

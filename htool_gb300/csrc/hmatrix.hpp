@@ -24,6 +24,8 @@ constexpr int kUserNumbering = 0, kClusterNumbering = 1, kGlobalToLocal = 2;
 
 int host_threads();
 void host_parallel_for(long long n, const std::function<void(long long)> &body);
+// the same over ranges [lo, hi) of at most `grain` indices (few atomics for fine-grained loops)
+void host_parallel_chunks(long long n, long long grain, const std::function<void(long long, long long)> &body);
 void call_generator(const HostGen &g, int M, int N, const int *rows, const int *cols, double *ptr);
 
 // partialACA of a batch of blocks fed by a host generator (hostgen.cpp):
@@ -356,6 +358,7 @@ class HMatrix {
     int mu_cap = 0;
     int zloc0_ = 0, zloc1_ = 0; // the z-sum atoms of the local rows
     std::vector<int> rhs_pad_ = std::vector<int>(9, 0); // right-hand-side bucket of 1..8 right-hand sides (0: unpadded)
+    int p2_gmax_              = 8;                      // largest right-hand-side group of a streamed phase-2 pass (8 or 4)
     int launches_ = 0;
     BuildStats st_;
 };

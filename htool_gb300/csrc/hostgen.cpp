@@ -89,6 +89,14 @@ void host_parallel_for(long long n, const std::function<void(long long)> &body) 
         std::rethrow_exception(err);
 }
 
+void host_parallel_chunks(long long n, long long grain, const std::function<void(long long, long long)> &body) {
+    if (n <= 0)
+        return;
+    grain                  = std::max(1LL, grain);
+    const long long chunks = (n + grain - 1) / grain;
+    host_parallel_for(chunks, [&](long long c) { body(c * grain, std::min(n, (c + 1) * grain)); });
+}
+
 void call_generator(const HostGen &g, int M, int N, const int *rows, const int *cols, double *ptr) {
     const int rc = g.fn(g.ctx, M, N, rows, cols, ptr);
     if (rc != 0)

@@ -103,14 +103,18 @@ void launch_zsum(const ZItem *items, int nitems, const int *zl, const double *z,
 constexpr int kStreamWarpsPerCta = 4;
 int stream_ctas(); // CTAs per launch (all resident)
 void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
-                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
+                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st, int gmax = 8);
 // phase-2 mode 1: CTAs of one producer warp and consumer warps; the producer
 // claims units of whole row chunks (stream_units: nunits + 1 unit bounds in
 // row chunks, then the first chunk of every row chunk and the end) and feeds
 // its consumers
 constexpr int kUnitRowChunks = 31; // row chunks per unit at most
+// both phase-2 launchers take the right-hand sides in groups of 8, 4, 2 and
+// 1; gmax = 4 caps the groups at 4 (two passes of 4 instead of one of 8:
+// the 8-wide kernel's code and registers can cost more than the second
+// pass over the data)
 void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx,
-                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st);
+                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st, int gmax = 8);
 std::vector<int> stream_units(const std::vector<StreamChunk> &chunks, int target, int *nunits);
 int stream2_units_target(); // units for a product launch on this device
 // phase 1 with one or two right-hand sides from stages of tile chunks

@@ -1595,7 +1595,7 @@ void reduced_tile_chunks(std::vector<StreamChunk> &out, long long src, int jlen,
 }
 
 void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nranges, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx, const double *A,
-                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+                          const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st, int gmax) {
     if (nranges <= 0)
         return;
     HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
@@ -1605,7 +1605,7 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
     int c0 = 0, g = 0;
     while (c0 < mu) {
         const int left = mu - c0;
-        const int n    = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        const int n    = left >= 8 && gmax >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
         int *t         = tickets + std::min(g, 7);
         if (g >= 7 && c0 > 0)
             HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
@@ -1621,14 +1621,14 @@ void launch_phase2_stream(const StreamChunk *chunks, const int *rbeg, int nrange
 }
 
 void launch_phase2_producer(const StreamChunk *chunks, const int *units, int nunits, int *tickets, const unsigned char *arena0, const unsigned char *arena1, const unsigned char *arena2, const int *cidx,
-                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+                            const double *A, const double *xp, const F2 *xs, const int *xexp, int mu, double *z, int zlen, int *status, cudaStream_t st, int gmax) {
     if (nunits <= 0)
         return;
     HTGPU_CUDA(cudaMemsetAsync(tickets, 0, sizeof(int) * 8, st));
     int c0 = 0, g = 0;
     while (c0 < mu) {
         const int left = mu - c0;
-        const int n    = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        const int n    = left >= 8 && gmax >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
         int *t         = tickets + std::min(g, 7);
         if (g >= 7 && c0 > 0)
             HTGPU_CUDA(cudaMemsetAsync(t, 0, sizeof(int), st));
