@@ -407,7 +407,24 @@ def run_gpu(args):
                      "aca_seconds": {"fixed_first_attempt": aca_seconds, "predicted_first_attempt": aca_learned},
                      "scratch_bytes": {"fixed_first_attempt": int(info["GPU_aca_scratch_bytes"]), "predicted_first_attempt": int(il["GPU_aca_scratch_bytes"])},
                      "rerun_rate": int(il["GPU_aca_overflow_reruns"]) / max(1, int(il["GPU_aca_predicted_blocks"])), "same_leaves": same}
+        # what pre-sizing buys when memory is short: both builds under the
+        # same ACA scratch budget (1.1 x what the predicted first attempts
+        # take), where the fixed first attempts need more slices
+        budget = int(1.1 * int(il["GPU_aca_scratch_bytes"]))
         del hl
+        under = {"budget_bytes": budget, "aca_seconds": {}, "aca_slices": {}, "same_leaves": True}
+        for name, use in (("fixed_first_attempt", False), ("predicted_first_attempt", True)):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            hb = H.HMatrix(t, t, WORKLOAD["epsilon"], WORKLOAD["eta"], device=local).set_aca_budget(budget)
+            if use:
+                hb.set_rank_predictor(mlp)
+            hb.build(H.LAPLACE, pts)
+            under["aca_seconds"][name] = time.perf_counter() - t1
+            under["aca_slices"][name] = int(float(hb.get_infos()["GPU_aca_rounds"]))
+            under["same_leaves"] = under["same_leaves"] and bool(np.array_equal(hb.get_leaves()[0], hm.get_leaves()[0]))
+            del hb
+        predictor["under_scratch_budget"] = under
 
     gpu_leaves = hm.get_leaves()
     # the batched workload (256 H-matrices, one graph launch per step),

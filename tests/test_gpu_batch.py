@@ -180,6 +180,11 @@ def test_rhs_buckets_pad_to_one_pass(port):
         x = G.rhs(5000, 5, seed=99)
         yo = oh.mvprod(x, 5)
         assert np.linalg.norm(hm.mvprod_global_to_global(x, 5) - yo) / np.linalg.norm(yo) < TOL[policy]
+        # 8 right-hand sides: the autotuner also picks passes of 8 or of 4 in phase 2
+        hm.autotune(8, 2)
+        x = G.rhs(5000, 8, seed=98)
+        yo = oh.mvprod(x, 8)
+        assert np.linalg.norm(hm.mvprod_global_to_global(x, 8) - yo) / np.linalg.norm(yo) < TOL[policy]
     with pytest.raises(ValueError):
         hm.set_rhs_bucket(3, 2)
     with pytest.raises(ValueError):
