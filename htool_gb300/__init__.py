@@ -130,6 +130,8 @@ def _load():
         "htgpu_cluster_forest": (i, [i, vp, vp]),
         "htgpu_hmatrix_set_rhs_bucket": (i, [vp, i, i]),
         "htgpu_hmatrix_get_rhs_bucket": (i, [vp, i, vp]),
+        "htgpu_hmatrix_set_phase2_dense_split": (i, [vp, i]),
+        "htgpu_hmatrix_get_phase2_dense_split": (i, [vp, vp]),
         "htgpu_cluster_forest_offsets": (i, [vp, vp, vp]),
         "htgpu_block_tasks_rank": (i, [vp, vp, d, i, vp, vp]),
         "htgpu_hmatrix_set_local_rank": (i, [vp, i]),
@@ -702,6 +704,17 @@ class HMatrix:
         """products with mu (1..8) right-hand sides run padded with zero
         columns to mu_run (0: unpadded); autotune(mu) picks the faster"""
         _check(lib.htgpu_hmatrix_set_rhs_bucket(self.h, int(mu), int(mu_run)))
+
+    def set_phase2_dense_split(self, on):
+        """reduced precision, 4+ right-hand sides: dense chunks first in the
+        double-float kernel, the FP32 / BF16 chunks after them (True), or
+        every chunk in the streamed kernel (False)"""
+        _check(lib.htgpu_hmatrix_set_phase2_dense_split(self.h, int(bool(on))))
+
+    def get_phase2_dense_split(self):
+        v = C.c_int()
+        _check(lib.htgpu_hmatrix_get_phase2_dense_split(self.h, C.byref(v)))
+        return bool(v.value)
 
     def get_rhs_bucket(self, mu):
         v = C.c_int()

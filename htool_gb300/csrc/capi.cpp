@@ -447,6 +447,21 @@ int htgpu_hmatrix_get_rhs_bucket(htgpu_hmatrix h, int mu, int *mu_run) {
     });
 }
 
+int htgpu_hmatrix_set_phase2_dense_split(htgpu_hmatrix h, int on) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_phase2_dense_split(on != 0);
+    });
+}
+
+int htgpu_hmatrix_get_phase2_dense_split(htgpu_hmatrix h, int *on) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(on, "on");
+        *on = h->h->phase2_dense_split() ? 1 : 0;
+    });
+}
+
 int htgpu_hmatrix_local(htgpu_hmatrix h, int *rank, int *local_offset, int *local_size) {
     return guarded([&] {
         need(h, "hmatrix");

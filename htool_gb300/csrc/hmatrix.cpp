@@ -1017,9 +1017,15 @@ void HMatrix::presplit_chunks(std::vector<StreamChunk> &ch, DevBuf<F2> &mirror) 
     if (segs.empty())
         return;
     mirror.alloc((std::size_t)cur + 2); // stage copies end on a 16-byte boundary
+    // runs cut into pieces so that every warp of the launch has a share
+    constexpr long long kSplitPiece = 4096;
+    std::vector<SplitSeg> pieces;
+    for (const SplitSeg &g : segs)
+        for (long long o = 0; o < g.n; o += kSplitPiece)
+            pieces.push_back({g.src + o, g.dst + o, std::min(kSplitPiece, g.n - o)});
     DevBuf<SplitSeg> sd;
-    sd.upload(segs, stream_);
-    launch_presplit_segs(fac.p, sd.p, (int)segs.size(), mirror.p, stream_);
+    sd.upload(pieces, stream_);
+    launch_presplit_segs(fac.p, sd.p, (int)pieces.size(), mirror.p, stream_);
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -1207,6 +1213,31 @@ void HMatrix::upload_mixed_phase2() {
         n_p2rc_m_ = (int)rc.size();
         rc.push_back((int)ch2.size());
         p2rcm_d.upload(rc, stream_);
+        // the FP32 / BF16 chunks alone, each row chunk's last one adding onto
+        // z: the streamed phase 2 of products whose dense chunks the
+        // double-float kernel takes first (many right-hand sides)
+        std::vector<StreamChunk> red;
+        for (int w = 0; w < n_p2rc_m_; w++) {
+            const std::size_t first = red.size();
+            for (int k = rc[w]; k < rc[w + 1]; k++)
+                if (ch2[k].kind == kStreamF32 || ch2[k].kind == kStreamBf16) {
+                    StreamChunk c = ch2[k];
+                    c.flags &= (unsigned char)~(kStreamFirst | kStreamLast);
+                    red.push_back(c);
+                }
+            if (red.size() > first) {
+                red[first].flags |= kStreamFirst;
+                red.back().flags |= (unsigned char)(kStreamLast | kStreamAdd);
+            }
+        }
+        n_chunks_r_ = (long long)red.size();
+        scr_d.upload(red, stream_);
+        if (red.empty())
+            scr_d.alloc(1);
+        const std::vector<int> rr = stream_ranges(red, n_sctas_);
+        n_ranges_r_               = (int)rr.size() - 1;
+        srr_d.upload(rr, stream_);
+        sur_d.upload(stream_units(red, stream2_units_target(), &n_units_r_), stream_);
         // tcgen05 phase 2: slabs of 32 reduced columns per row chunk, four
         // row chunks to a group
         std::vector<Tc2Slab> slabs;
@@ -1576,6 +1607,20 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
                                       w_z, (int)zlen_, true, st);
                 launches_ += 1;
             }
+        } else if (split_dense_ && mu >= 4 && n_chunks_md_ > 0 && n_chunks_r_ > 0) {
+            // many right-hand sides: the dense FP64 chunks in the double-float
+            // kernel (z cleared first, every row chunk added), then the
+            // FP32 / BF16 chunks in the streamed kernel, adding onto z
+            HTGPU_CUDA(cudaMemsetAsync(w_z, 0, sizeof(double) * (std::size_t)zlen_ * mu, st));
+            launch_phase2_df_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xs, w_xexp, mu, w_z,
+                                  (int)zlen_, true, st);
+            if (p2_mode_ == 1)
+                launch_phase2_producer(scr_d.p, sur_d.p, n_units_r_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu,
+                                       w_z, (int)zlen_, status_d.p, st, p2_gmax_);
+            else
+                launch_phase2_stream(scr_d.p, srr_d.p, n_ranges_r_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
+                                     (int)zlen_, status_d.p, st, p2_gmax_);
+            launches_ += 1;
         } else if (p2_mode_ == 1)
             launch_phase2_producer(scm_d.p, sum_d.p, n_units_m_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu, w_z,
                                    (int)zlen_, status_d.p, st, p2_gmax_);
@@ -1788,6 +1833,17 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
             const float t4   = timed();
             p2_gmax_         = t4 < t8 ? 4 : 8;
             best             = std::min(t4, t8);
+            layout_gen_++;
+        }
+        // and, from 4 right-hand sides on, the dense chunks in the
+        // double-float kernel or in the streamed one
+        if (precision_ != 0 && run >= 4 && !tcs) {
+            split_dense_       = false;
+            const float t_one  = timed();
+            split_dense_       = true;
+            const float t_two  = timed();
+            split_dense_       = t_two < t_one;
+            best               = std::min(t_one, t_two);
             layout_gen_++;
         }
     }

@@ -200,6 +200,15 @@ class HMatrix {
     // autotuner chooses.
     void set_rhs_bucket(int mu, int mu_run);
     int rhs_run(int mu) const;
+    // reduced-precision products with 4 or more right-hand sides off the
+    // tensor cores: the dense FP64 chunks in the streamed phase-2 kernel
+    // (false) or first in the double-float many-right-hand-side kernel, the
+    // streamed one then adding the FP32 / BF16 chunks (true); autotuned
+    void set_phase2_dense_split(bool on) {
+        split_dense_ = on;
+        layout_gen_++;
+    }
+    bool phase2_dense_split() const { return split_dense_; }
     bool emulation_allowed() const { return emu_ok_; }
     // time every candidate split on the current H-matrix and keep the fastest
     // FP64: phase-1 mode and the DFMA/emulation split; reduced precision:
@@ -359,6 +368,11 @@ class HMatrix {
     int zloc0_ = 0, zloc1_ = 0; // the z-sum atoms of the local rows
     std::vector<int> rhs_pad_ = std::vector<int>(9, 0); // right-hand-side bucket of 1..8 right-hand sides (0: unpadded)
     int p2_gmax_              = 8;                      // largest right-hand-side group of a streamed phase-2 pass (8 or 4)
+    bool split_dense_         = false;                  // reduced precision, 4+ right-hand sides: dense chunks in the double-float kernel
+    DevBuf<StreamChunk> scr_d;                          // the reduced-precision chunks alone (split_dense_)
+    DevBuf<int> srr_d, sur_d;                           // their ranges and units
+    int n_ranges_r_ = 0, n_units_r_ = 0;
+    long long n_chunks_r_ = 0;
     int launches_ = 0;
     BuildStats st_;
 };

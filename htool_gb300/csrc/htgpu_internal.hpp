@@ -133,7 +133,9 @@ struct PanelItem { // z rows row0 .. row0+h += panel (h x ncol, column-major, ld
 enum StreamKind : unsigned char { kStreamDfma = 0, kStreamEmu = 1, kStreamF32 = 2, kStreamBf16 = 3 };
 // first / last chunk of a row chunk (phase 2) or tile (phase 1); data in the
 // second arena; an emulated chunk whose data are (hi, lo) float pairs
-enum StreamFlag : unsigned char { kStreamFirst = 1, kStreamLast = 2, kStreamArena1 = 4, kStreamPre = 8 };
+// kStreamAdd (on a row chunk's last chunk): add the row chunk's sums onto z
+// instead of writing them (another kernel wrote the rest of the row first)
+enum StreamFlag : unsigned char { kStreamFirst = 1, kStreamLast = 2, kStreamArena1 = 4, kStreamPre = 8, kStreamAdd = 16 };
 
 // one run of doubles copied as (hi, lo) float pairs: n values from double
 // index src of the arena to pair index dst of a pre-split mirror

@@ -375,6 +375,7 @@ __global__ void presplit_segs_kernel(const double *__restrict__ in, const SplitS
 }
 
 void launch_presplit_segs(const double *in, const SplitSeg *segs, int nsegs, F2 *out, cudaStream_t st) {
+    // segs: runs cut into pieces of a few thousand doubles, one warp each
     if (nsegs <= 0)
         return;
     int blocks = std::min((nsegs + 7) / 8, sm_count() * 8);

@@ -26,12 +26,20 @@ __device__ __forceinline__ float bf16_to_f32(unsigned short h) { return __uint_a
 // max |entry| per (leaf, column) for U (from phase-2 chunk blocks) and for
 // Vt (from phase-1 tiles); positive floats order like their bit patterns
 __global__ void colmax_kernel(const ColMaxJob *__restrict__ jobs, const double *__restrict__ fac, unsigned *__restrict__ cmax) {
+    // one warp per column of the job: lanes over its rows, a warp maximum,
+    // one atomic per column and job
     const ColMaxJob J = jobs[blockIdx.x];
-    const long long n = (long long)J.rows * J.cols;
-    for (long long e = threadIdx.x; e < n; e += blockDim.x) {
-        const int k   = (int)(e / J.rows);
-        const float a = (float)fabs(fac[J.off + e]);
-        atomicMax(cmax + J.slot + k, __float_as_uint(a));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = wid; k < J.cols; k += nw) {
+        const double *col = fac + J.off + (long long)J.rows * k;
+        float m           = 0.f;
+        for (int i = lane; i < J.rows; i += 32)
+            m = fmaxf(m, (float)fabs(col[i]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0)
+            atomicMax(cmax + J.slot + k, __float_as_uint(m));
     }
 }
 
@@ -43,15 +51,20 @@ __global__ void convert_kernel(const ConvertJob *__restrict__ jobs, const double
     const long long n32 = (long long)l32 * J.c32, n = n32 + (long long)l16 * (J.cols - J.c32);
     float *f32          = reinterpret_cast<float *>(mix + J.dst32);
     __nv_bfloat16 *b16  = reinterpret_cast<__nv_bfloat16 *>(mix + J.dst16);
+    int kprev  = -1;
+    double inv = 0.; // 1 / (the column's maximum), formed once per column a thread meets
     for (long long e = threadIdx.x; e < n; e += blockDim.x) {
         const bool is32 = e < n32;
         const int k     = is32 ? (int)(e / l32) : J.c32 + (int)((e - n32) / l16);
         const int i     = is32 ? (int)(e % l32) : (int)((e - n32) % l16);
         double nv       = 0.; // zero rows past the tile
         if (i < J.rows) {
-            const float mx = __uint_as_float(cmax[J.slot + k]);
-            const double v = fac[J.src + (long long)k * J.rows + i];
-            nv             = mx > 0.f ? v / (double)mx : 0.;
+            if (k != kprev) {
+                const float mx = __uint_as_float(cmax[J.slot + k]);
+                inv            = mx > 0.f ? 1.0 / (double)mx : 0.;
+                kprev          = k;
+            }
+            nv = fac[J.src + (long long)k * J.rows + i] * inv;
         }
         if (is32)
             f32[e] = (float)nv;

@@ -439,10 +439,14 @@ __global__ void __launch_bounds__(32 * kWarps, MU >= 8 ? 2 : MU >= 4 ? 3 : 4)
                     if (slice == 0)
                         v[cc] += vv;
                 }
-            if (slice == 0)
+            if (slice == 0) {
+                const bool add = (c.flags & kStreamAdd) != 0;
 #pragma unroll
-                for (int cc = 0; cc < MU; cc++)
-                    z[(long long)(c0 + cc) * zlen + c.b + row] = v[cc];
+                for (int cc = 0; cc < MU; cc++) {
+                    double *zp = z + (long long)(c0 + cc) * zlen + c.b + row;
+                    *zp        = add ? *zp + v[cc] : v[cc];
+                }
+            }
 #pragma unroll
             for (int cc = 0; cc < MU; cc++) {
                 dacc[cc] = 0.;
@@ -853,10 +857,14 @@ __global__ void __launch_bounds__(32 * (WsCfg<MU>::kCons + 1), WsCfg<MU>::kCtas)
                     if (slice == 0)
                         v[cc] += vv;
                 }
-            if (slice == 0)
+            if (slice == 0) {
+                const bool add = (c.flags & kStreamAdd) != 0;
 #pragma unroll
-                for (int cc = 0; cc < MU; cc++)
-                    z[(long long)(c0 + cc) * zlen + c.b + row] = v[cc];
+                for (int cc = 0; cc < MU; cc++) {
+                    double *zp = z + (long long)(c0 + cc) * zlen + c.b + row;
+                    *zp        = add ? *zp + v[cc] : v[cc];
+                }
+            }
 #pragma unroll
             for (int cc = 0; cc < MU; cc++) {
                 dacc[cc] = 0.;

@@ -259,6 +259,15 @@ int htgpu_hmatrix_set_local_rank(htgpu_hmatrix h, int rank);
  * htgpu_hmatrix_autotune(h, mu, ...) sets the faster for mu. */
 int htgpu_hmatrix_set_rhs_bucket(htgpu_hmatrix h, int mu, int mu_run);
 int htgpu_hmatrix_get_rhs_bucket(htgpu_hmatrix h, int mu, int *mu_run);
+
+/* Reduced-precision products with 4 or more right-hand sides off the tensor
+ * cores: on != 0 applies the dense FP64 chunks first in the double-float
+ * many-right-hand-side kernel and the FP32 / BF16 chunks after them in the
+ * streamed phase-2 kernel; 0 streams every chunk through the one kernel.
+ * Results agree within the storage policy's tolerance; the autotuner picks.
+ * No counterpart in the reference. */
+int htgpu_hmatrix_set_phase2_dense_split(htgpu_hmatrix h, int on);
+int htgpu_hmatrix_get_phase2_dense_split(htgpu_hmatrix h, int *on);
 int htgpu_hmatrix_local(htgpu_hmatrix h, int *rank, int *local_offset, int *local_size);
 
 /* Replaces HMatrix::mymvprod_global_to_local(in, out, mu)

@@ -386,6 +386,14 @@ def test_stacked_phase1_matches_tile_kernels(golden):
             out.append(GH.mvprod_global_to_global(X[mu], mu))
         assert rel(out[0], out[1]) < 1e-6, mu
         assert rel(out[0], y64[mu]) < 1e-6 and rel(out[1], y64[mu]) < 1e-6, mu
+        # phase 2 with the dense chunks first in the double-float kernel,
+        # both phase-2 kernels after them
+        GH.set_phase2_dense_split(True)
+        for mode in ("producer", "warp"):
+            GH.set_phase2_mode(mode)
+            assert rel(GH.mvprod_global_to_global(X[mu], mu), y64[mu]) < 1e-6, (mu, mode)
+        GH.set_phase2_dense_split(False)
+        GH.set_phase2_mode("producer")
     assert GH.device_status() == 0
 
 
