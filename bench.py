@@ -78,6 +78,7 @@ def parse():
     p.add_argument("--mixed-phase1-mode", type=int, default=None, help="mixed precision: 0 tile kernels, 1 streamed")
     p.add_argument("--phase2-mode", type=int, default=None, help="FP64: 0 per-warp streams, 1 producer-fed")
     p.add_argument("--mixed-phase2-mode", type=int, default=None, help="mixed precision: 0 per-warp streams, 1 producer-fed")
+    p.add_argument("--mixed-dense-split", type=int, default=None, help="mixed precision, 4+ right-hand sides: 1 dense chunks first in the double-float kernel")
     return p.parse_args()
 
 
@@ -340,7 +341,7 @@ def run_gpu(args):
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
         }
 
-    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode))
+    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode, args.mixed_dense_split))
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.5)  # let the sampler start before the timed regions
@@ -372,6 +373,8 @@ def run_gpu(args):
             hm.set_phase1_mode(args.mixed_phase1_mode)
         if args.mixed_phase2_mode is not None:
             hm.set_phase2_mode(args.mixed_phase2_mode)
+        if args.mixed_dense_split is not None:
+            hm.set_phase2_dense_split(bool(args.mixed_dense_split))
         tunem = None
     else:
         tunem = hm.autotune(mu, 5)

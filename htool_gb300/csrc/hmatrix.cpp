@@ -1836,14 +1836,26 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
             layout_gen_++;
         }
         // and, from 4 right-hand sides on, the dense chunks in the
-        // double-float kernel or in the streamed one
+        // double-float kernel or in the streamed one, with either phase-2
+        // kernel for the rest
         if (precision_ != 0 && run >= 4 && !tcs) {
-            split_dense_       = false;
-            const float t_one  = timed();
-            split_dense_       = true;
-            const float t_two  = timed();
-            split_dense_       = t_two < t_one;
-            best               = std::min(t_one, t_two);
+            float tbest   = 1e30f;
+            bool arg_sp   = false;
+            int arg_mode  = p2_mode_;
+            for (bool sp : {false, true})
+                for (int m : {0, 1}) {
+                    split_dense_  = sp;
+                    p2_mode_      = m;
+                    const float t = timed();
+                    if (t < tbest) {
+                        tbest    = t;
+                        arg_sp   = sp;
+                        arg_mode = m;
+                    }
+                }
+            split_dense_ = arg_sp;
+            p2_mode_     = arg_mode;
+            best         = tbest;
             layout_gen_++;
         }
     }

@@ -4,8 +4,8 @@
 // element meets mu coefficients.  These kernels keep one warp on one work
 // item (a phase-1 tile, a phase-2 row chunk), stage its operands in the
 // warp's shared memory with every load of a stage issued before the first
-// use, and apply each element to 16 right-hand sides per pass (8 for a
-// product with at most 8) in the double-float arithmetic of df64.cuh on the
+// use, and apply each element to 16 right-hand sides per pass (4 or 8 for
+// a product with at most 4 or 8) in the double-float arithmetic of df64.cuh on the
 // FP32 pipe (FP64-accurate, the same arithmetic as the streamed kernels'
 // emulated chunks).
 //
@@ -249,9 +249,12 @@ void raise_smem(K kernel, int bytes, unsigned long long &done) {
 void launch_phase1_df_mrhs(const P1Item *items, int nitems, const LrLeaf *lr, const double *factors, const F2 *xs, const int *xexp, int mu, double *A, cudaStream_t st) {
     if (nitems <= 0)
         return;
-    static unsigned long long done8 = 0, done16 = 0; // devices whose shared-memory limit was raised
+    static unsigned long long done4 = 0, done8 = 0, done16 = 0; // devices whose shared-memory limit was raised
     const int blocks = (nitems + kDfWarps - 1) / kDfWarps; // one warp per tile
-    if (mu <= 8) { // one pass of 8 right-hand sides
+    if (mu <= 4) { // one pass of 4 right-hand sides
+        raise_smem(phase1_df_mrhs_kernel<4>, kP1DfSmem, done4);
+        phase1_df_mrhs_kernel<4><<<blocks, 32 * kDfWarps, kP1DfSmem, st>>>(items, nitems, lr, factors, xs, xexp, mu, A);
+    } else if (mu <= 8) { // one pass of 8 right-hand sides
         raise_smem(phase1_df_mrhs_kernel<8>, kP1DfSmem, done8);
         phase1_df_mrhs_kernel<8><<<blocks, 32 * kDfWarps, kP1DfSmem, st>>>(items, nitems, lr, factors, xs, xexp, mu, A);
     } else {
@@ -265,9 +268,12 @@ void launch_phase2_df_mrhs(const StreamChunk *chunks, const int *rc, int nrc, co
                            int mu, double *z, int zlen, bool add, cudaStream_t st) {
     if (nrc <= 0)
         return;
-    static unsigned long long done8 = 0, done16 = 0;
+    static unsigned long long done4 = 0, done8 = 0, done16 = 0;
     const int blocks = (nrc + kDfWarps - 1) / kDfWarps; // one warp per row chunk
-    if (mu <= 8) {
+    if (mu <= 4) {
+        raise_smem(phase2_df_mrhs_kernel<4>, kP2DfSmem, done4);
+        phase2_df_mrhs_kernel<4><<<blocks, 32 * kDfWarps, kP2DfSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, A, xs, xexp, mu, z, zlen, add ? 1 : 0);
+    } else if (mu <= 8) {
         raise_smem(phase2_df_mrhs_kernel<8>, kP2DfSmem, done8);
         phase2_df_mrhs_kernel<8><<<blocks, 32 * kDfWarps, kP2DfSmem, st>>>(chunks, rc, nrc, fac, pre, cidx, A, xs, xexp, mu, z, zlen, add ? 1 : 0);
     } else {
