@@ -688,6 +688,12 @@ def run_helmholtz(args):
     ms_mma, y_mma = timed(steps)
     ph_mma = hm.profile(mu, 3)
     hm.set_tensor_core_mode("tcgen05")
+    # the tcgen05 phase 1 from the factors' pre-laid-out copy
+    hm.set_tensor_core_arena(True)
+    arena_bytes = hm.get_tensor_core_arena()[1]
+    ms_arena, y_arena = timed(steps)
+    ph_arena = hm.profile(mu, 3)
+    hm.set_tensor_core_arena(False)
     ck = clocks.stop()
     status = hm.device_status()
     info = hm.get_infos()
@@ -701,6 +707,7 @@ def run_helmholtz(args):
         "mixed_tcgen05": {"ms": ms_tc, "rel_err_vs_fp64": err(y_tc), "phase_ms": phases(ph_tc), "kernels": "phase 1 tcgen05, phase 2 mma.sync (the default)"},
         "mixed_tcgen05_both": {"ms": ms_both, "rel_err_vs_fp64": err(y_both), "phase_ms": phases(ph_both)},
         "mixed_mma_sync": {"ms": ms_mma, "rel_err_vs_fp64": err(y_mma), "phase_ms": phases(ph_mma)},
+        "mixed_tcgen05_arena": {"ms": ms_arena, "phase_ms": phases(ph_arena), "arena_bytes": arena_bytes, "bitwise_equal_to_tcgen05": bool(np.array_equal(y_arena, y_tc))},
         "fp64": {"ms": ms64, "phase_ms": phases(ph64)},
         "build_seconds": build_s, "clocks": ck, "device_status": status,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_mean", "Compression_ratio")},

@@ -31,7 +31,7 @@ CLUSTER_NUMBERING = 2
 GLOBAL_TO_LOCAL = 4  # in: the whole input in cluster numbering; out: the local rows of the handle's rank
 
 PREC_FP64, PREC_FP32, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
-PHASE1_TILES, PHASE1_STREAM = 0, 1
+PHASE1_TILES, PHASE1_STREAM, PHASE1_TENSOR = 0, 1, 2
 PHASE2_WARP, PHASE2_PRODUCER = 0, 1
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED, "bf16": PREC_BF16}
 
@@ -123,6 +123,8 @@ def _load():
         "htgpu_hmatrix_reset_status": (i, [vp]),
         "htgpu_hmatrix_set_tensor_core_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_tensor_core_mode": (i, [vp, vp]),
+        "htgpu_hmatrix_set_tensor_core_arena": (i, [vp, i]),
+        "htgpu_hmatrix_get_tensor_core_arena": (i, [vp, vp, vp]),
         "htgpu_debug_tc_gemm": (i, [i, vp, vp, vp]),
         "htgpu_debug_set_waits": (i, [i, C.c_longlong, C.c_longlong]),
         "htgpu_cluster_build_world": (i, [i, vp, i, i, i, vp]),
@@ -591,8 +593,10 @@ class HMatrix:
         return {"policy": p.value, "stored_bytes": b.value, "fp32_columns": f.value, "bf16_columns": h.value}
 
     def set_phase1_mode(self, mode):
-        """Phase 1 with one or two right-hand sides: 'tiles' or 'stream'."""
-        m = {"tiles": PHASE1_TILES, "stream": PHASE1_STREAM}[mode] if isinstance(mode, str) else int(mode)
+        """Phase 1: 'tiles', 'stream', or 'tensor' (as 'stream', and
+        reduced-precision products with 8+ right-hand sides on tcgen05 at any
+        epsilon)."""
+        m = {"tiles": PHASE1_TILES, "stream": PHASE1_STREAM, "tensor": PHASE1_TENSOR}[mode] if isinstance(mode, str) else int(mode)
         _check(lib.htgpu_hmatrix_set_phase1_mode(self.h, m))
         return self
 
@@ -641,6 +645,18 @@ class HMatrix:
         m = C.c_int()
         _check(lib.htgpu_hmatrix_get_tensor_core_mode(self.h, C.byref(m)))
         return m.value
+
+    def set_tensor_core_arena(self, on):
+        """the tcgen05 phase 1 reading a copy of the factors laid out for the
+        tensor cores (bitwise the same sums, more memory)"""
+        _check(lib.htgpu_hmatrix_set_tensor_core_arena(self.h, int(bool(on))))
+        return self
+
+    def get_tensor_core_arena(self):
+        """(on, bytes of the copy)"""
+        on, b = C.c_int(), C.c_longlong()
+        _check(lib.htgpu_hmatrix_get_tensor_core_arena(self.h, C.byref(on), C.byref(b)))
+        return bool(on.value), b.value
 
     def reset_status(self):
         _check(lib.htgpu_hmatrix_reset_status(self.h))

@@ -670,6 +670,23 @@ int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode) {
     });
 }
 
+int htgpu_hmatrix_set_tensor_core_arena(htgpu_hmatrix h, int on) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_tensor_core_arena(on != 0);
+    });
+}
+
+int htgpu_hmatrix_get_tensor_core_arena(htgpu_hmatrix h, int *on, long long *bytes) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        if (on)
+            *on = h->h->tensor_core_arena() ? 1 : 0;
+        if (bytes)
+            *bytes = h->h->tensor_core_arena_bytes();
+    });
+}
+
 int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d) {
     return guarded([&] {
         need(a, "a");

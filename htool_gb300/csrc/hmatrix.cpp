@@ -1321,6 +1321,8 @@ void HMatrix::set_precision(int policy, double tau) {
     tau_       = tau;
     if (policy == 0) {
         emu3_.release(); // the reduced-precision products' mirror
+        tca_d.release();  // and the tensor cores' copy of the factors
+        tcoff_d.release();
         if (fp64_lists_stale_) // FP64 chunk lists and pre-split mirrors back
             upload_phase1_lists();
         return;
@@ -1532,6 +1534,7 @@ void HMatrix::set_precision(int policy, double tau) {
         tcseg_d.upload(segs, stream_);
         tcblk_d.upload(blks, stream_);
         n_tcblk_ = (int)blks.size();
+        tcblk_h_ = std::move(blks);
     }
     ch2_h_ = std::move(ch2);
     upload_mixed_phase2();
@@ -1552,6 +1555,27 @@ void HMatrix::set_precision(int policy, double tau) {
         launch_swizzle(dz.p, (int)swz.size(), fac.p, dso.p, cidxm_d.p, cmax.p, mix_.p, stream_);
         HTGPU_CUDA(cudaStreamSynchronize(stream_));
     }
+    build_tc_arena();
+}
+
+void HMatrix::build_tc_arena() {
+    tca_d.release();
+    tcoff_d.release();
+    if (!tc_arena_ || precision_ == 0 || n_tcblk_ == 0)
+        return;
+    std::vector<long long> off(tcblk_h_.size());
+    const long long bytes = tc_arena_bytes(tcblk_h_.data(), n_tcblk_, off.data());
+    tcoff_d.upload(off, stream_);
+    tca_d.alloc(bytes);
+    launch_tc_pack(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, tcoff_d.p, tca_d.p, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void HMatrix::set_tensor_core_arena(bool on) {
+    HTGPU_CUDA(cudaSetDevice(device_));
+    layout_gen_++; // captured products are stale
+    tc_arena_ = on;
+    build_tc_arena();
 }
 
 // The phase-1 tiles on the FP64 pipe and those on the emulation run as two
@@ -1572,16 +1596,22 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
     // many right-hand sides on the tensor cores when epsilon leaves room for their FP32 sums
     const bool mma = mu >= kMmaMinRhs && eps_ >= kMmaMinEps;
     if (precision_ != 0) {
-        if (n_p1m_ && mu <= 2 && p1_mode_ == 1) {
+        if (n_p1m_ && mu <= 2 && p1_mode_ >= 1) {
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
-        } else if (n_p1m_ && mu >= 3 && !mma && p1_mode_ == 1 && n_tcblk_ > 0) {
+        } else if (n_p1m_ && mu >= 8 && !mma && p1_mode_ == 2 && tc_mode_ >= 1 && n_tcblk_ > 0) {
+            // phase-1 mode 2: the stacked blocks on tcgen05 at any epsilon
+            // (each stacked sum runs over at most 256 rows in FP32, as on the
+            // CUDA cores; phase 2 stays on the CUDA cores)
+            phase1_tc(w_xs, mu, w_A, st);
+            launches_ += 1;
+        } else if (n_p1m_ && mu >= 3 && !mma && p1_mode_ >= 1 && n_tcblk_ > 0) {
             // the stacked blocks on the CUDA cores (phase-1 mode 1 with 3 or more right-hand sides)
             launch_phase1_stack(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, reinterpret_cast<float *>(w_A), st);
             launches_ += 1;
         } else if (n_p1m_ && mma) {
             if (tc_mode_ >= 1 && n_tcblk_ > 0)
-                launch_phase1_tc(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, reinterpret_cast<float *>(w_A), status_d.p, st);
+                phase1_tc(w_xs, mu, w_A, st);
             else
                 launch_phase1_mma(p1m_d.p, n_p1m_, lr_d.p, mix_.p, scalef_d.p, w_xs, mu, w_A, st);
             launches_ += 1;
@@ -1638,7 +1668,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         launch_phase1_df_mrhs(p1_d.p, n_p1_dfma_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
         launch_phase1_df_mrhs(p1e_d.p, n_p1_emu_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
         launches_ += (n_p1_dfma_ > 0) + (n_p1_emu_ > 0);
-    } else if (!p1_h.empty() && mu <= 2 && p1_mode_ == 1) {
+    } else if (!p1_h.empty() && mu <= 2 && p1_mode_ >= 1) {
         if (emu_fresh_)
             launch_phase1_stream(p1r_d.p, n_p1_ranges_, p1c_d.p, p1_kinds_, reinterpret_cast<const unsigned char *>(emu_.p), w_xp, w_xs, nullptr, w_xexp, mu, w_A, status_d.p, st, true);
         else
@@ -1687,6 +1717,14 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
 
 // the per-cluster sums into y: every row in user or cluster numbering, or
 // (global-to-local products) the local rows only, at y[i - local offset]
+void HMatrix::phase1_tc(const F2 *w_xs, int mu, double *w_A, cudaStream_t st) {
+    float *Af = reinterpret_cast<float *>(w_A);
+    if (tca_d.p)
+        launch_phase1_tc_pre(tcblk_d.p, n_tcblk_, tcseg_d.p, tca_d.p, tcoff_d.p, scalef_d.p, w_xs, mu, Af, status_d.p, st);
+    else
+        launch_phase1_tc(tcblk_d.p, n_tcblk_, tcseg_d.p, mix_.p, scalef_d.p, w_xs, mu, Af, status_d.p, st);
+}
+
 void HMatrix::launch_sums(double *y, int mu, int numbering, const double *w_z, cudaStream_t st) {
     if (numbering == kGlobalToLocal)
         launch_zsum(zi_d.p + zloc0_, zloc1_ - zloc0_, zl_d.p, w_z, (int)zlen_, mu, nullptr, y, local_row_count(), st, local_row_offset());
@@ -1708,7 +1746,7 @@ void HMatrix::set_phase2_mode(int mode) {
 
 void HMatrix::set_phase1_mode(int mode) {
     layout_gen_++; // buffers or launch lists change: captured products are stale
-    require(mode == 0 || mode == 1, "phase-1 mode must be 0 (tile kernels) or 1 (streamed chunks)");
+    require(mode >= 0 && mode <= 2, "phase-1 mode must be 0 (tile kernels), 1 (streamed chunks) or 2 (tensor cores for reduced-precision products with 8 or more right-hand sides)");
     p1_mode_ = mode;
 }
 
@@ -1750,7 +1788,9 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         // phase-1 modes with the dense blocks' DFMA / emulation split
         int arg_mode = p1_mode_, arg_split = p2m_n64_;
         const std::vector<int> shares = emu_ok_ ? std::vector<int>{0, 350, 650, 1000} : std::vector<int>{1000};
-        for (int mode : {0, 1})
+        // mode 2 (tcgen05 phase 1 at any epsilon) where it applies
+        const std::vector<int> modes = (mu >= 8 && tc_mode_ >= 1 && n_tcblk_ > 0 && !(mu >= kMmaMinRhs && eps_ >= kMmaMinEps)) ? std::vector<int>{0, 1, 2} : std::vector<int>{0, 1};
+        for (int mode : modes)
             for (int q2 : shares) {
                 p1_mode_ = mode;
                 p2m_n64_ = q2;
@@ -1765,6 +1805,26 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         p1_mode_ = arg_mode;
         p2m_n64_ = arg_split;
         upload_mixed_phase2();
+        // the tcgen05 phase 1 from its pre-laid-out copy of the factors,
+        // where that phase 1 runs and the copy fits in half the free memory
+        const int run   = rhs_run(mu);
+        const bool tcs  = run >= kMmaMinRhs && eps_ >= kMmaMinEps;
+        const bool tc1  = n_tcblk_ > 0 && tc_mode_ >= 1 && (tcs || (run >= 8 && p1_mode_ == 2));
+        if (tc1) {
+            std::vector<long long> off(tcblk_h_.size());
+            const long long need = tc_arena_bytes(tcblk_h_.data(), n_tcblk_, off.data());
+            std::size_t fr = 0, tot = 0;
+            HTGPU_CUDA(cudaMemGetInfo(&fr, &tot));
+            const bool was = tc_arena_;
+            if (tca_d.p || (std::size_t)need < fr / 2) {
+                set_tensor_core_arena(!was);
+                const float ms = timed();
+                if (ms < best)
+                    best = ms;
+                else
+                    set_tensor_core_arena(was);
+            }
+        }
     } else {
         // every phase-1 mode with every DFMA/emulation split
         std::vector<std::pair<int, int>> splits;

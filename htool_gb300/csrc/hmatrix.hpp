@@ -194,6 +194,13 @@ class HMatrix {
     // phase 1 with the mma.sync phase 2 (default), 2 tcgen05 in both
     void set_tensor_core_mode(int mode);
     int tensor_core_mode() const { return tc_mode_; }
+    // the tcgen05 phase 1 reading its A operand from a copy of the factors
+    // laid out for the tensor cores (one bulk copy a slab, no staging by the
+    // threads) at the price of that copy's memory (tensor_core_arena_bytes);
+    // off by default, autotuned
+    void set_tensor_core_arena(bool on);
+    bool tensor_core_arena() const { return tc_arena_; }
+    long long tensor_core_arena_bytes() const { return (long long)tca_d.n; }
     // right-hand-side buckets: a product with mu right-hand sides (1 to 8)
     // runs padded with zero columns to mu_run (one pass over the factors
     // instead of one per group of 4, 2, 1); 0 runs it unpadded.  The
@@ -351,6 +358,15 @@ class HMatrix {
     DevBuf<TcSeg> tcseg_d;
     DevBuf<TcBlock> tcblk_d;
     int n_tcblk_ = 0;
+    std::vector<TcBlock> tcblk_h_;
+    // the blocks' A operands laid out once for the tensor cores (TF32 hi and
+    // lo parts, 32 KB a slab) and each block's byte offset; built while
+    // tc_arena_ is on and the factors are in reduced precision
+    bool tc_arena_ = false;
+    DevBuf<unsigned char> tca_d;
+    DevBuf<long long> tcoff_d;
+    void build_tc_arena();
+    void phase1_tc(const F2 *w_xs, int mu, double *w_A, cudaStream_t st); // the tcgen05 phase 1, from the arena when there is one
     DevBuf<Tc2Slab> tc2slab_d; // tensor-core phase 2: slabs and the first slab of each group of four row chunks
     DevBuf<int> tc2g_d;
     int n_tc2_groups_ = 0;

@@ -207,6 +207,15 @@ struct TcBlock { // segments [s0, s1), at most 128 columns in all, on x rows xro
     int s0, s1, xrow, jlen;
 };
 void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const float *scale, const F2 *xs, int mu, float *A, int *status, cudaStream_t st);
+// the A operand of every block laid out once (tc.cu): per 32-row slab its
+// TF32 hi and lo parts in the tensor cores' canonical layout, 32 KB a slab;
+// tc_arena_bytes fills tcoff_h (each block's byte offset) and returns the
+// size, launch_tc_pack writes it, launch_phase1_tc_pre is the phase 1 that
+// brings each slab in by one bulk copy
+long long tc_arena_bytes(const TcBlock *blocks_h, int nblocks, long long *tcoff_h);
+void launch_tc_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const long long *tcoff, unsigned char *arena, cudaStream_t st);
+void launch_phase1_tc_pre(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *tca, const long long *tcoff, const float *scale, const F2 *xs, int mu, float *A, int *status,
+                          cudaStream_t st);
 // the same stacked blocks on the CUDA cores (mixed.cu), products with 3 or
 // more right-hand sides at any epsilon: one thread per stacked column, FP32
 // FMA, float sums into A

@@ -310,6 +310,202 @@ __global__ void __launch_bounds__(kTc1Threads, 2) phase1_tc_kernel(const TcBlock
         tmem_free(tmem);
 }
 
+// ---------------------------------------------------------------------------
+// The A operand of phase 1 laid out once: for every stacked block and 32-row
+// slab, the TF32 hi then lo parts of its 128 x 32 slab in the canonical
+// layout the MMAs read (32 KB a slab, zero past the block's columns and
+// rows).  tc_pack_kernel writes it (one CTA per block, the staging code of
+// the kernel above, to global memory); phase1_tc_pre_kernel then brings a
+// slab into shared memory by one bulk copy (cp.async.bulk, completion on an
+// mbarrier) issued by one thread, and the threads only stage the x slab.
+constexpr int kTcSlabBytes = 2 * kTcABytes;
+
+__global__ void __launch_bounds__(kTc1Threads) tc_pack_kernel(const TcBlock *__restrict__ blocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ mix,
+                                                              const long long *__restrict__ tcoff, unsigned char *__restrict__ arena) {
+    const int tid = threadIdx.x;
+    const int row = tid & 127, kh = (tid >> 7) * 16;
+    const TcBlock B = blocks[blockIdx.x];
+    int m0 = 0, sg = -1;
+    for (int s = B.s0; s < B.s1; s++) {
+        const int nc = segs[s].ncol;
+        if (row < m0 + nc) {
+            sg = s;
+            break;
+        }
+        m0 += nc;
+    }
+    const int l32 = ld_f32(B.jlen), l16 = ld_bf16(B.jlen);
+    const float *col32          = nullptr;
+    const unsigned short *col16 = nullptr;
+    if (sg >= 0) {
+        const TcSeg S = segs[sg];
+        const int col = S.col0 + row - m0;
+        if (col < S.c32)
+            col32 = reinterpret_cast<const float *>(mix + S.off) + (long long)l32 * col;
+        else
+            col16 = reinterpret_cast<const unsigned short *>(mix + S.off + 4LL * l32 * S.c32) + (long long)l16 * (col - S.c32);
+    }
+    for (int ks = 0, slab = 0; ks < B.jlen; ks += kTcK, slab++) {
+        unsigned char *hi = arena + tcoff[blockIdx.x] + (long long)slab * kTcSlabBytes, *lo = hi + kTcABytes;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int j = ks + kh + 4 * q;
+            float4 a    = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (col32 && j < l32)
+                a = __ldg(reinterpret_cast<const float4 *>(col32 + j));
+            else if (col16 && j < l16) {
+                const uint2 w = __ldg(reinterpret_cast<const uint2 *>(col16 + j));
+                a             = make_float4(bf16f((unsigned short)(w.x & 0xFFFFu)), bf16f((unsigned short)(w.x >> 16)), bf16f((unsigned short)(w.y & 0xFFFFu)), bf16f((unsigned short)(w.y >> 16)));
+            }
+            put4(hi, lo, row, kh + 4 * q, a.x, a.y, a.z, a.w);
+        }
+    }
+}
+
+__device__ __forceinline__ void bar_expect_tx(unsigned long long *b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(kTc1Threads, 2) phase1_tc_pre_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ tca,
+                                                                       const long long *__restrict__ tcoff, const float *__restrict__ scale, const F2 *__restrict__ xs, int mu,
+                                                                       float *__restrict__ A, int *__restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *bars  = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf);      // products of a buffer done
+    unsigned long long *fulls = reinterpret_cast<unsigned long long *>(smem + 2 * kTcBuf + 16); // a buffer's A slab landed
+    unsigned *tslot           = reinterpret_cast<unsigned *>(smem + 2 * kTcBuf + 64);
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const int bn = tid & 63, bk = (tid >> 6) * 8; // B: right-hand side and first K-value
+    if (tid == 0) {
+        bar_init(&bars[0]);
+        bar_init(&bars[1]);
+        bar_init(&fulls[0]);
+        bar_init(&fulls[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+    int slabs  = 0; // slabs issued by this CTA: buffer slabs & 1, its (slabs >> 1)-th use
+    int copies = 0; // A copies issued (thread 0), one per slab
+    bool fail  = false;
+    for (int bi = blockIdx.x; bi < nblocks && !fail; bi += gridDim.x) {
+        const TcBlock B = blocks[bi];
+        const F2 *X     = xs + (long long)B.xrow * mu;
+        const unsigned char *ablk = tca + tcoff[bi];
+        auto loadb = [&](int ks, int cb, float (&b)[8]) {
+            const bool on = cb + bn < mu;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int j = ks + bk + q;
+                b[q]        = (on && j < B.jlen) ? X[(long long)j * mu + cb + bn].hi : 0.f;
+            }
+        };
+        for (int cb = 0; cb < mu && !fail; cb += kTcN) {
+            float b[8];
+            loadb(0, cb, b);
+            for (int ks = 0; ks < B.jlen; ks += kTcK) {
+                const int buf = slabs & 1, use = slabs >> 1;
+                unsigned char *bb = smem + (size_t)buf * kTcBuf;
+                if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1)) // the products of two slabs ago read this buffer
+                    fail = true;
+                if (__syncthreads_or(fail)) {
+                    fail = true;
+                    break;
+                }
+                if (tid == 0) { // this slab's A parts, one bulk copy
+                    bar_expect_tx(&fulls[buf], kTcSlabBytes);
+                    bulk_g2s(bb, ablk + (long long)(ks / kTcK) * kTcSlabBytes, kTcSlabBytes, &fulls[buf]);
+                    copies++;
+                }
+                unsigned char *bhi = bb + 2 * kTcABytes, *blo = bhi + kTcBBytes;
+                put4(bhi, blo, bn, bk, b[0], b[1], b[2], b[3]);
+                put4(bhi, blo, bn, bk + 4, b[4], b[5], b[6], b[7]);
+                if (ks + kTcK < B.jlen) // the next slab's x values fly while this one is multiplied
+                    loadb(ks + kTcK, cb, b);
+                proxy_fence();
+                __syncthreads();
+                if (tid == 0) {
+                    if (bar_wait(&fulls[buf], use & 1)) {
+                        tc_fence_after();
+                        tc_slab(tmem, bb, ks == 0);
+                        tc_commit(&bars[buf]);
+                    } else {
+                        fail = true; // spreads at the next barrier
+                    }
+                }
+                slabs++;
+            }
+            if (__syncthreads_or(fail)) {
+                fail = true;
+                break;
+            }
+            // the block's sums: all its slabs' products are complete
+            const int last = slabs - 1;
+            if (!bar_wait(&bars[last & 1], (last >> 1) & 1))
+                fail = true;
+            if (__syncthreads_or(fail)) {
+                fail = true;
+                break;
+            }
+            tc_fence_after();
+            {
+                const int orow = 32 * (wid & 3) + lane, c0 = 32 * (wid >> 2);
+                int osg = -1, om0 = 0;
+                for (int s2 = B.s0; s2 < B.s1; s2++) {
+                    const int nc = segs[s2].ncol;
+                    if (orow < om0 + nc) {
+                        osg = s2;
+                        break;
+                    }
+                    om0 += nc;
+                }
+                long long oo = 0;
+                float osc    = 0.f;
+                if (osg >= 0) {
+                    oo  = (segs[osg].slot + (long long)(orow - om0)) * mu;
+                    osc = scale[segs[osg].sidx + orow - om0];
+                }
+#pragma unroll
+                for (int c16 = 0; c16 < 2; c16++) {
+                    float v[16];
+                    tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + c0 + 16 * c16, v);
+                    if (osg >= 0)
+#pragma unroll
+                        for (int q = 0; q < 16; q++) {
+                            const int c = cb + c0 + 16 * c16 + q;
+                            if (c < mu)
+                                A[oo + c] = v[q] * osc;
+                        }
+                }
+            }
+            tc_fence_before();
+            __syncthreads(); // the accumulator is read out before the next block overwrites it
+        }
+    }
+    if (fail) {
+        if (lane == 0)
+            atomicExch(status, 4);
+        // the A copies this CTA issued land before the CTA leaves: every one
+        // completed the phase of its buffer's full barrier
+        if (tid == 0)
+            for (int p = 0; p < 2 && p < copies; p++) {
+                const int last_use = (copies - 1 - p) >> 1; // uses of buffer (copies - 1 - p) & 1
+                bar_wait(&fulls[(copies - 1 - p) & 1], last_use & 1);
+            }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (wid == 0)
+        tmem_free(tmem);
+}
+
 // Phase 2 (the U side) of the same products: per row chunk (h <= 32 rows)
 // Z (h x 64) = U (h x K) C (K x 64) over its FP32 / BF16 chunks, U the
 // chunks' columns as stored in lane order (column q = slice + S j of slice
@@ -559,6 +755,40 @@ void launch_phase1_tc(const TcBlock *blocks, int nblocks, const TcSeg *segs, con
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int grid = std::min(nblocks, 2 * sms); // two CTAs an SM (96 KB of shared memory, 64 tensor-memory columns each)
     phase1_tc_kernel<<<grid, kTc1Threads, kTcSmem, st>>>(blocks, nblocks, segs, mix, scale, xs, mu, A, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+long long tc_arena_bytes(const TcBlock *blocks_h, int nblocks, long long *tcoff_h) {
+    long long off = 0;
+    for (int b = 0; b < nblocks; b++) {
+        tcoff_h[b] = off;
+        off += (long long)((blocks_h[b].jlen + kTcK - 1) / kTcK) * kTcSlabBytes;
+    }
+    return off;
+}
+
+void launch_tc_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *mix, const long long *tcoff, unsigned char *arena, cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    tc_pack_kernel<<<nblocks, kTc1Threads, 0, st>>>(blocks, segs, mix, tcoff, arena);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase1_tc_pre(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *tca, const long long *tcoff, const float *scale, const F2 *xs, int mu, float *A, int *status,
+                          cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    static unsigned long long done = 0;
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase1_tc_pre_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = std::min(nblocks, 2 * sms);
+    phase1_tc_pre_kernel<<<grid, kTc1Threads, kTcSmem, st>>>(blocks, nblocks, segs, tca, tcoff, scale, xs, mu, A, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 

@@ -344,6 +344,10 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int
  * the reference. */
 #define HTGPU_PHASE1_TILES 0
 #define HTGPU_PHASE1_STREAM 1
+/* as HTGPU_PHASE1_STREAM, and reduced-precision products with 8 or more
+ * right-hand sides take the tcgen05 phase 1 at any epsilon (the tensor-core
+ * phase 2 stays reserved to epsilon >= 1e-5) */
+#define HTGPU_PHASE1_TENSOR 2
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode);
 
@@ -382,6 +386,18 @@ int htgpu_hmatrix_get_phase2_mode(htgpu_hmatrix h, int *mode);
 #define HTGPU_TC_TCGEN05_BOTH 2
 int htgpu_hmatrix_set_tensor_core_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode);
+
+/* The tcgen05 phase 1 reading its A operand from a second copy of the
+ * low-rank factors, laid out once for the tensor cores (per block of up to
+ * 128 stacked columns and 32 source rows: the TF32 hi and lo parts in the
+ * MMA's shared-memory layout, 32 KB), brought into shared memory by one bulk
+ * copy a slab instead of being decoded and split by the threads.  Costs the
+ * copy's memory (*bytes, 0 while off or in FP64); bitwise the same sums.
+ * Off by default; htgpu_hmatrix_autotune tries it where the tcgen05 phase 1
+ * runs and the copy fits in half the free memory.  No counterpart in the
+ * reference. */
+int htgpu_hmatrix_set_tensor_core_arena(htgpu_hmatrix h, int on);
+int htgpu_hmatrix_get_tensor_core_arena(htgpu_hmatrix h, int *on, long long *bytes);
 
 /* Test support, no counterpart in the reference: d (128 x 64) = a (128 x
  * 32) b (32 x 64), row-major host arrays, computed on CUDA device `device`

@@ -251,7 +251,7 @@ def test_phase1_modes_parity(golden, mode):
         assert rel(GH.mvprod_global_to_global(x2, 2), ref2) < 1e-6
     GH.set_precision("fp64")
     with pytest.raises(ValueError):
-        GH.set_phase1_mode(2)
+        GH.set_phase1_mode(3)
     assert GH.device_status() == 0
 
 
@@ -394,6 +394,31 @@ def test_stacked_phase1_matches_tile_kernels(golden):
             assert rel(GH.mvprod_global_to_global(X[mu], mu), y64[mu]) < 1e-6, (mu, mode)
         GH.set_phase2_dense_split(False)
         GH.set_phase2_mode("producer")
+    assert GH.device_status() == 0
+
+
+def test_tensor_core_phase1_at_small_epsilon(golden):
+    """Phase-1 mode 2: the tcgen05 phase 1 of reduced-precision products at
+    epsilon 1e-6 (its stacked FP32 sums run over at most 256 rows, like the
+    CUDA-core kernels'), the CUDA-core phase 2 after it: within 1e-6 of the
+    FP64 product for 8 to 64 right-hand sides, and close to the CUDA-core
+    phase 1's result"""
+    g, meta = golden("sphere6000_k1")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    GH = H.HMatrix(t, t, meta["eps"], meta["eta"]).build(meta["kernel"], g["xt"])
+    assert meta["eps"] < 1e-5
+    X = {mu: G.rhs(n, mu, seed=60 + mu) for mu in (8, 24, 64)}
+    y64 = {mu: GH.mvprod_global_to_global(X[mu], mu) for mu in X}
+    GH.set_precision("mixed")
+    for mu in X:
+        GH.set_phase1_mode("tensor")
+        assert GH.get_phase1_mode() == H.PHASE1_TENSOR
+        yt = GH.mvprod_global_to_global(X[mu], mu)
+        GH.set_phase1_mode("stream")
+        ys = GH.mvprod_global_to_global(X[mu], mu)
+        assert rel(yt, y64[mu]) < 1e-6, mu
+        assert rel(yt, ys) < 1e-6, mu
     assert GH.device_status() == 0
 
 

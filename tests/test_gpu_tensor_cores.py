@@ -9,6 +9,8 @@ many right-hand sides.
   80 right-hand sides) on tcgen05 against the warp-level mma.sync kernels
   and against the FP64 product; config 3's complex Helmholtz matrix (real
   form) with 64 right-hand sides likewise.
+* The tcgen05 phase 1 reading the factors' pre-laid-out copy (one bulk copy
+  a slab): bitwise the products of the staged kernel.
 The reference computes these contractions as BLAS gemm calls with the
 row-major right-hand sides (types/matrix.hpp:346, 380)."""
 import ctypes as C
@@ -88,3 +90,37 @@ def test_tcgen05_complex_many_rhs(golden):
     yboth = hm.mvprod_global_to_global(X, 64)
     assert hm.device_status() == 0
     assert rel(ytc, y64) < 1e-5 and rel(yboth, y64) < 1e-5
+
+
+@pytest.mark.parametrize("eps,mus", [(1e-5, (64, 80)), (1e-6, (8, 40))])
+def test_tcgen05_arena_bitwise(eps, mus):
+    """The A operand laid out once for the tensor cores gives the staged
+    kernel's sums bit for bit (the same TF32 splits of the same values), for
+    the tensor-core products (epsilon 1e-5) and for phase-1 mode 2 (1e-6);
+    the copy follows precision changes and is dropped in FP64"""
+    n = 6000
+    pts = G.sphere(n, seed=43)
+    t = H.Cluster().build(n, pts)
+    hm = H.HMatrix(t, t, eps, 10.0).build(H.LAPLACE, pts)
+    X = {mu: G.rhs(n, mu, seed=44 + mu) for mu in mus}
+    hm.set_precision("mixed", 1.0)
+    if eps < 1e-5:
+        hm.set_phase1_mode("tensor")
+    staged = {mu: hm.mvprod_global_to_global(X[mu], mu) for mu in mus}
+    assert hm.get_tensor_core_arena() == (False, 0)
+    hm.set_tensor_core_arena(True)
+    on, nbytes = hm.get_tensor_core_arena()
+    assert on and nbytes > 0 and nbytes % 32768 == 0
+    for mu in mus:
+        assert np.array_equal(hm.mvprod_global_to_global(X[mu], mu), staged[mu]), mu
+    assert hm.device_status() == 0
+    hm.set_precision("fp32", 1.0)  # the copy is rebuilt from the new factors
+    assert hm.get_tensor_core_arena()[1] > 0
+    y32 = hm.mvprod_global_to_global(X[mus[0]], mus[0])
+    hm.set_tensor_core_arena(False)
+    assert hm.get_tensor_core_arena() == (False, 0)
+    assert np.array_equal(hm.mvprod_global_to_global(X[mus[0]], mus[0]), y32)
+    hm.set_tensor_core_arena(True)
+    hm.set_precision("fp64")
+    assert hm.get_tensor_core_arena() == (True, 0)
+    assert hm.device_status() == 0
