@@ -1788,8 +1788,12 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         // phase-1 modes with the dense blocks' DFMA / emulation split
         int arg_mode = p1_mode_, arg_split = p2m_n64_;
         const std::vector<int> shares = emu_ok_ ? std::vector<int>{0, 350, 650, 1000} : std::vector<int>{1000};
-        // mode 2 (tcgen05 phase 1 at any epsilon) where it applies
-        const std::vector<int> modes = (mu >= 8 && tc_mode_ >= 1 && n_tcblk_ > 0 && !(mu >= kMmaMinRhs && eps_ >= kMmaMinEps)) ? std::vector<int>{0, 1, 2} : std::vector<int>{0, 1};
+        // mode 2 (the TF32 tcgen05 phase 1 below epsilon 1e-5) is never
+        // picked here, only kept when set: the tensor cores' FP32
+        // accumulation puts single right-hand sides of a 400 000-point sphere
+        // 1.4e-6 from FP64 at epsilon 1e-6, beyond the epsilon a
+        // reduced-precision product keeps
+        const std::vector<int> modes = p1_mode_ == 2 ? std::vector<int>{2} : std::vector<int>{0, 1};
         for (int mode : modes)
             for (int q2 : shares) {
                 p1_mode_ = mode;

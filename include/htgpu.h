@@ -345,8 +345,11 @@ int htgpu_hmatrix_get_fp64_split(htgpu_hmatrix h, int *phase1_dfma_permille, int
 #define HTGPU_PHASE1_TILES 0
 #define HTGPU_PHASE1_STREAM 1
 /* as HTGPU_PHASE1_STREAM, and reduced-precision products with 8 or more
- * right-hand sides take the tcgen05 phase 1 at any epsilon (the tensor-core
- * phase 2 stays reserved to epsilon >= 1e-5) */
+ * right-hand sides take the TF32 tcgen05 phase 1 at any epsilon (the
+ * tensor-core phase 2 stays reserved to epsilon >= 1e-5).  Below epsilon
+ * 1e-5 the tensor cores' FP32 accumulation can put a right-hand side beyond
+ * epsilon from FP64 (1.4e-6 on a 400 000-point sphere at 1e-6), so the
+ * autotuner never picks this mode; it keeps it when set. */
 #define HTGPU_PHASE1_TENSOR 2
 int htgpu_hmatrix_set_phase1_mode(htgpu_hmatrix h, int mode);
 int htgpu_hmatrix_get_phase1_mode(htgpu_hmatrix h, int *mode);
