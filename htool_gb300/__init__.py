@@ -123,6 +123,9 @@ def _load():
         "htgpu_hmatrix_reset_status": (i, [vp]),
         "htgpu_hmatrix_set_tensor_core_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_tensor_core_mode": (i, [vp, vp]),
+        "htgpu_debug_oz_gemm": (i, [i, i, i, i, vp, vp, vp]),
+        "htgpu_hmatrix_set_digit_planes": (i, [vp, i]),
+        "htgpu_hmatrix_get_digit_planes": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_tensor_core_arena": (i, [vp, i]),
         "htgpu_hmatrix_get_tensor_core_arena": (i, [vp, vp, vp]),
         "htgpu_debug_tc_gemm": (i, [i, vp, vp, vp]),
@@ -656,6 +659,18 @@ class HMatrix:
         """(on, bytes of the copy)"""
         on, b = C.c_int(), C.c_longlong()
         _check(lib.htgpu_hmatrix_get_tensor_core_arena(self.h, C.byref(on), C.byref(b)))
+        return bool(on.value), b.value
+
+    def set_digit_planes(self, on):
+        """phase 1 of products with 8+ right-hand sides on the BF16 tensor
+        cores by exact digit slicing (FP64-grade for FP64 storage)"""
+        _check(lib.htgpu_hmatrix_set_digit_planes(self.h, int(bool(on))))
+        return self
+
+    def get_digit_planes(self):
+        """(on, bytes of the digit planes)"""
+        on, b = C.c_int(), C.c_longlong()
+        _check(lib.htgpu_hmatrix_get_digit_planes(self.h, C.byref(on), C.byref(b)))
         return bool(on.value), b.value
 
     def reset_status(self):

@@ -35,7 +35,7 @@ def _sources():
 def _compile(src, verbose):
     name = os.path.basename(src)
     obj = os.path.join(BUILD, name + ".o")
-    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".hpp")] + [os.path.join(os.path.dirname(HERE), "include", "htgpu.h")]
+    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".hpp", ".cuh"))] + [os.path.join(os.path.dirname(HERE), "include", "htgpu.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     if src.endswith(".cu"):

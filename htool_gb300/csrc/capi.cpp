@@ -687,6 +687,23 @@ int htgpu_hmatrix_get_tensor_core_arena(htgpu_hmatrix h, int *on, long long *byt
     });
 }
 
+int htgpu_hmatrix_set_digit_planes(htgpu_hmatrix h, int on) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_digit_planes(on != 0);
+    });
+}
+
+int htgpu_hmatrix_get_digit_planes(htgpu_hmatrix h, int *on, long long *bytes) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        if (on)
+            *on = h->h->digit_planes() ? 1 : 0;
+        if (bytes)
+            *bytes = h->h->digit_plane_bytes();
+    });
+}
+
 int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d) {
     return guarded([&] {
         need(a, "a");
@@ -707,6 +724,49 @@ int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d) {
         HTGPU_CUDA(cudaMemcpy(&status, st.p, sizeof(int), cudaMemcpyDeviceToHost));
         htgpu::require(status == 0, "a wait of the tensor-core self-test ran out", 3);
         HTGPU_CUDA(cudaMemcpy(d, dd.p, sizeof(float) * 128 * 64, cudaMemcpyDeviceToHost));
+    });
+}
+
+int htgpu_debug_oz_gemm(int device, int S, int K, int mu, const double *a, const double *b, double *d) {
+    return guarded([&] {
+        need(a, "a");
+        need(b, "b");
+        need(d, "d");
+        htgpu::require(S == 4 || S == 8, "digit planes: S must be 4 or 8");
+        htgpu::require(K >= 1 && K <= 256, "K must be in [1, 256]");
+        htgpu::require(mu >= 1 && mu <= 1024, "mu must be in [1, 1024]");
+        HTGPU_CUDA(cudaSetDevice(device));
+        // one stacked block: the 128 rows of a as columns of a K-row tile
+        const htgpu::TcBlock blk{0, 1, 0, K};
+        const htgpu::TcSeg seg{0, 0, 0, 0, 128, 0};
+        long long off = 0;
+        const long long bytes = htgpu::oz_arena_bytes(&blk, 1, S, &off);
+        htgpu::DevBuf<double> da, db, dd;
+        htgpu::DevBuf<htgpu::TcBlock> dblk;
+        htgpu::DevBuf<htgpu::TcSeg> dseg;
+        htgpu::DevBuf<long long> doff;
+        htgpu::DevBuf<int> rexp, gexp, st;
+        htgpu::DevBuf<unsigned char> arena;
+        da.upload(a, (std::size_t)128 * K, nullptr);
+        db.upload(b, (std::size_t)K * mu, nullptr);
+        dd.alloc((std::size_t)128 * mu);
+        dblk.upload(&blk, 1, nullptr);
+        dseg.upload(&seg, 1, nullptr);
+        doff.upload(&off, 1, nullptr);
+        rexp.alloc(128);
+        gexp.alloc((std::size_t)((K + 31) / 32) * mu);
+        arena.alloc(bytes);
+        st.alloc(1);
+        HTGPU_CUDA(cudaMemset(st.p, 0, sizeof(int)));
+        HTGPU_CUDA(cudaMemset(dd.p, 0, sizeof(double) * 128 * mu));
+        htgpu::launch_oz_pack(dblk.p, 1, dseg.p, da.p, nullptr, S, doff.p, rexp.p, arena.p, nullptr);
+        htgpu::launch_oz_xgroups(db.p, K, mu, gexp.p, nullptr);
+        htgpu::launch_phase1_oz(dblk.p, 1, dseg.p, S, arena.p, doff.p, rexp.p, nullptr, db.p, gexp.p, nullptr, mu, dd.p, st.p, nullptr);
+        HTGPU_CUDA(cudaDeviceSynchronize());
+        int status = 0;
+        HTGPU_CUDA(cudaMemcpy(&status, st.p, sizeof(int), cudaMemcpyDeviceToHost));
+        htgpu::require(status == 0, "a wait of the digit-plane product ran out", 3);
+        HTGPU_CUDA(cudaMemcpy(d, dd.p, sizeof(double) * 128 * mu, cudaMemcpyDeviceToHost));
     });
 }
 

@@ -25,6 +25,42 @@ namespace htgpu {
 
 namespace {
 
+// The phase-1 tiles on the same x rows (the same source cluster slab)
+// stacked and cut into blocks of at most 128 columns, longest first so the
+// CTAs' shares even out: the operands of the tensor-core phase-1 kernels.
+// Segment offsets are the tiles' (bytes of the reduced arena, or elements of
+// the FP64 one).
+void stack_tiles(const std::vector<P1Item> &items, const std::vector<LrLeaf> &lr, std::vector<TcSeg> &segs, std::vector<TcBlock> &blks) {
+    std::map<std::pair<int, int>, std::vector<int>> on_rows; // (first x row, rows) -> tiles
+    for (std::size_t i = 0; i < items.size(); i++)
+        if (lr[items[i].leaf].r > 0)
+            on_rows[{lr[items[i].leaf].oj + items[i].j0, items[i].jlen}].push_back((int)i);
+    for (auto &g : on_rows) {
+        TcBlock b{(int)segs.size(), (int)segs.size(), g.first.first, g.first.second};
+        int rows = 0;
+        for (int i : g.second) {
+            const P1Item &m = items[i];
+            const LrLeaf &L = lr[m.leaf];
+            for (int c0 = 0; c0 < L.r;) {
+                if (rows == 128) {
+                    b.s1 = (int)segs.size();
+                    blks.push_back(b);
+                    b.s0 = b.s1;
+                    rows = 0;
+                }
+                const int nc = std::min(L.r - c0, 128 - rows);
+                segs.push_back({m.off, L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r + c0, m.pad, c0, nc, (int)L.a_off + c0});
+                rows += nc;
+                c0 += nc;
+            }
+        }
+        b.s1 = (int)segs.size();
+        if (b.s1 > b.s0)
+            blks.push_back(b);
+    }
+    std::stable_sort(blks.begin(), blks.end(), [](const TcBlock &a, const TcBlock &b) { return a.jlen > b.jlen; });
+}
+
 double now() { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
 
 // largest q with q * (M + N) <= M * N in htool's 32-bit int arithmetic
@@ -934,6 +970,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     st_.layout_lists_seconds  = now() - tl2;
     mu_cap     = 0;
     precision_ = 0;
+    build_oz_arena(); // the digit planes follow new factors (none while off)
 }
 
 void HMatrix::ensure_work(int mu) {
@@ -947,6 +984,7 @@ void HMatrix::ensure_work(int mu) {
     z.alloc((std::size_t)std::max<long long>(zlen_, 1) * mu);
     xstage.alloc((std::size_t)nc * mu);
     ystage.alloc((std::size_t)nr * mu);
+    ozg.alloc((std::size_t)((nc + 31) / 32) * mu + 1);
     mu_cap = mu;
 }
 
@@ -1298,7 +1336,9 @@ void HMatrix::get_fp64_split(int *p1, int *n64) const {
     *n64 = emu_ok_ ? p2_n64_ : 1000;
 }
 
-void HMatrix::launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st) { launch_product_with(x, y, mu, numbering, st, xp.p, xs.p, xexp.p, A.p, z.p, nullptr, rhs_run(mu)); }
+void HMatrix::launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st) {
+    launch_product_with(x, y, mu, numbering, st, xp.p, xs.p, xexp.p, A.p, z.p, nullptr, rhs_run(mu), ozg.p);
+}
 
 int HMatrix::rhs_run(int mu) const { return mu < (int)rhs_pad_.size() && rhs_pad_[mu] > mu ? rhs_pad_[mu] : mu; }
 
@@ -1325,6 +1365,8 @@ void HMatrix::set_precision(int policy, double tau) {
         tcoff_d.release();
         if (fp64_lists_stale_) // FP64 chunk lists and pre-split mirrors back
             upload_phase1_lists();
+        if (oz_on_)
+            build_oz_arena(); // the FP64 planes
         return;
     }
     if (emu_.p || emu2_.p) { // the reduced-precision products need no FP64 mirrors
@@ -1498,39 +1540,10 @@ void HMatrix::set_precision(int policy, double tau) {
     p1m_d.upload(p1m, stream_);
     n_p1m_ = (int)p1m.size();
     {
-        // tensor-core phase 1: the tiles on the same x rows (the same source
-        // cluster slab) stacked, cut into blocks of at most 128 columns
-        std::map<std::pair<int, int>, std::vector<int>> on_rows; // (first x row, rows) -> tiles
-        for (std::size_t i = 0; i < p1m.size(); i++)
-            if (lr_h[p1m[i].leaf].r > 0)
-                on_rows[{lr_h[p1m[i].leaf].oj + p1m[i].j0, p1m[i].jlen}].push_back((int)i);
+        // tensor-core phase 1: the reduced tiles stacked
         std::vector<TcSeg> segs;
         std::vector<TcBlock> blks;
-        for (auto &g : on_rows) {
-            TcBlock b{(int)segs.size(), (int)segs.size(), g.first.first, g.first.second};
-            int rows = 0;
-            for (int i : g.second) {
-                const P1Item &m = p1m[i];
-                const LrLeaf &L = lr_h[m.leaf];
-                for (int c0 = 0; c0 < L.r;) {
-                    if (rows == 128) {
-                        b.s1 = (int)segs.size();
-                        blks.push_back(b);
-                        b.s0 = b.s1;
-                        rows = 0;
-                    }
-                    const int nc = std::min(L.r - c0, 128 - rows);
-                    segs.push_back({m.off, L.a_off + (long long)(m.chunk & ~kEmuBit) * L.r + c0, m.pad, c0, nc, (int)L.a_off + c0});
-                    rows += nc;
-                    c0 += nc;
-                }
-            }
-            b.s1 = (int)segs.size();
-            if (b.s1 > b.s0)
-                blks.push_back(b);
-        }
-        // longest first, so the CTAs' shares even out
-        std::stable_sort(blks.begin(), blks.end(), [](const TcBlock &a, const TcBlock &b) { return a.jlen > b.jlen; });
+        stack_tiles(p1m, lr_h, segs, blks);
         tcseg_d.upload(segs, stream_);
         tcblk_d.upload(blks, stream_);
         n_tcblk_ = (int)blks.size();
@@ -1556,6 +1569,7 @@ void HMatrix::set_precision(int policy, double tau) {
         HTGPU_CUDA(cudaStreamSynchronize(stream_));
     }
     build_tc_arena();
+    build_oz_arena();
 }
 
 void HMatrix::build_tc_arena() {
@@ -1578,11 +1592,71 @@ void HMatrix::set_tensor_core_arena(bool on) {
     build_tc_arena();
 }
 
+long long HMatrix::oz_arena_need() {
+    std::vector<TcBlock> blks;
+    if (precision_ == 0) {
+        std::vector<TcSeg> segs;
+        stack_tiles(p1_h, lr_h, segs, blks);
+    } else {
+        blks = tcblk_h_;
+    }
+    std::vector<long long> off(blks.size());
+    return oz_arena_bytes(blks.data(), (int)blks.size(), precision_ == 0 ? 8 : 4, off.data());
+}
+
+void HMatrix::build_oz_arena() {
+    oza_d.release();
+    ozoff_d.release();
+    ozrexp_d.release();
+    ozseg64_d.release();
+    ozblk64_d.release();
+    n_ozblk64_ = 0;
+    oz_S_      = 0;
+    if (!oz_on_ || !fac.p)
+        return;
+    std::vector<TcBlock> blks;
+    const TcBlock *bd;
+    const TcSeg *sd;
+    if (precision_ == 0) { // FP64 tiles, eight planes
+        std::vector<TcSeg> segs;
+        stack_tiles(p1_h, lr_h, segs, blks);
+        if (blks.empty())
+            return;
+        ozseg64_d.upload(segs, stream_);
+        ozblk64_d.upload(blks, stream_);
+        n_ozblk64_ = (int)blks.size();
+        bd         = ozblk64_d.p;
+        sd         = ozseg64_d.p;
+    } else { // the reduced tiles' stacked blocks, four planes
+        if (n_tcblk_ == 0)
+            return;
+        blks = tcblk_h_;
+        bd   = tcblk_d.p;
+        sd   = tcseg_d.p;
+    }
+    const int S = precision_ == 0 ? 8 : 4;
+    std::vector<long long> off(blks.size());
+    const long long bytes = oz_arena_bytes(blks.data(), (int)blks.size(), S, off.data());
+    ozoff_d.upload(off, stream_);
+    ozrexp_d.alloc(blks.size() * 128);
+    oza_d.alloc(bytes);
+    launch_oz_pack(bd, (int)blks.size(), sd, precision_ == 0 ? fac.p : nullptr, precision_ == 0 ? nullptr : mix_.p, S, ozoff_d.p, ozrexp_d.p, oza_d.p, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    oz_S_ = S;
+}
+
+void HMatrix::set_digit_planes(bool on) {
+    HTGPU_CUDA(cudaSetDevice(device_));
+    layout_gen_++; // captured products are stale
+    oz_on_ = on;
+    build_oz_arena();
+}
+
 // The phase-1 tiles on the FP64 pipe and those on the emulation run as two
 // kernels on two streams at once (fork/join through events), so each keeps
 // its own register budget and both pipe families work together.
 void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks,
-                                  int mu_run) {
+                                  int mu_run, int *w_gexp) {
     // a product padded up to its right-hand-side bucket runs mu columns, the
     // ones past mu_out zero, and writes mu_out
     const int mu     = std::max(mu_out, mu_run);
@@ -1599,6 +1673,11 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         if (n_p1m_ && mu <= 2 && p1_mode_ >= 1) {
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
+        } else if (n_p1m_ && mu >= kMmaMinRhs && oz_S_ == 4 && w_gexp && n_tcblk_ > 0) {
+            // the stacked blocks on the BF16 tensor cores, four digit planes
+            launch_oz_xgroups(w_xp, nc, mu, w_gexp, st);
+            launch_phase1_oz(tcblk_d.p, n_tcblk_, tcseg_d.p, 4, oza_d.p, ozoff_d.p, ozrexp_d.p, scalef_d.p, w_xp, w_gexp, w_xexp, mu, w_A, status_d.p, st);
+            launches_ += 2;
         } else if (n_p1m_ && mu >= 8 && !mma && p1_mode_ == 2 && tc_mode_ >= 1 && n_tcblk_ > 0) {
             // phase-1 mode 2: the stacked blocks on tcgen05 at any epsilon
             // (each stacked sum runs over at most 256 rows in FP32, as on the
@@ -1664,7 +1743,12 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         return;
     }
     const bool many = mu >= kDfMinRhs; // many right-hand sides: double-float kernels over 16 per pass
-    if (many) {
+    if (many && oz_S_ == 8 && w_gexp && n_ozblk64_ > 0) {
+        // the stacked FP64 tiles on the BF16 tensor cores, eight digit planes
+        launch_oz_xgroups(w_xp, nc, mu, w_gexp, st);
+        launch_phase1_oz(ozblk64_d.p, n_ozblk64_, ozseg64_d.p, 8, oza_d.p, ozoff_d.p, ozrexp_d.p, nullptr, w_xp, w_gexp, nullptr, mu, w_A, status_d.p, st);
+        launches_ += 2;
+    } else if (many) {
         launch_phase1_df_mrhs(p1_d.p, n_p1_dfma_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
         launch_phase1_df_mrhs(p1e_d.p, n_p1_emu_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
         launches_ += (n_p1_dfma_ > 0) + (n_p1_emu_ > 0);
@@ -1784,6 +1868,24 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
         return ms / reps;
     };
     float best = 1e30f;
+    // the digit-plane phase 1 (products with 8 or more right-hand sides),
+    // where its planes fit in half the free memory; `best` is the time of
+    // the current configuration
+    auto try_digit_planes = [&]() {
+        const bool was = oz_on_;
+        if (!was) {
+            std::size_t fr = 0, tot = 0;
+            HTGPU_CUDA(cudaMemGetInfo(&fr, &tot));
+            if ((std::size_t)oz_arena_need() >= fr / 2)
+                return;
+        }
+        set_digit_planes(!was);
+        const float ms = timed();
+        if (ms < best)
+            best = ms;
+        else
+            set_digit_planes(was);
+    };
     if (precision_ != 0) {
         // phase-1 modes with the dense blocks' DFMA / emulation split
         int arg_mode = p1_mode_, arg_split = p2m_n64_;
@@ -1829,6 +1931,8 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
                     set_tensor_core_arena(was);
             }
         }
+        if (run >= kMmaMinRhs && n_tcblk_ > 0)
+            try_digit_planes();
     } else {
         // every phase-1 mode with every DFMA/emulation split
         std::vector<std::pair<int, int>> splits;
@@ -1853,6 +1957,8 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
             }
         p1_mode_ = arg_mode;
         set_fp64_split(arg.first, arg.second);
+        if (rhs_run(mu) >= kDfMinRhs)
+            try_digit_planes();
     }
     // then the phase-2 kernel for the chosen configuration
     {
@@ -1939,7 +2045,7 @@ void HMatrix::profile(int mu, int reps, float *ms) {
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
     for (int r = 0; r < reps; r++) {
         HTGPU_CUDA(cudaEventRecord(ev[0], stream_));
-        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1, rhs_run(mu));
+        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1, rhs_run(mu), ozg.p);
         HTGPU_CUDA(cudaEventRecord(ev[4], stream_));
         HTGPU_CUDA(cudaEventSynchronize(ev[4]));
         float t;

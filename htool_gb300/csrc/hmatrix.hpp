@@ -201,6 +201,14 @@ class HMatrix {
     void set_tensor_core_arena(bool on);
     bool tensor_core_arena() const { return tc_arena_; }
     long long tensor_core_arena_bytes() const { return (long long)tca_d.n; }
+    // products with 8 or more right-hand sides: phase 1 on the BF16 tensor
+    // cores by exact digit slicing (oz.cu) -- FP64 storage with 8 digit
+    // planes (FP64-grade sums), reduced storage with 4 (exact FP32-grade
+    // sums at any epsilon) -- from a copy of the factors cut into planes
+    // (digit_plane_bytes); off by default, autotuned
+    void set_digit_planes(bool on);
+    bool digit_planes() const { return oz_on_; }
+    long long digit_plane_bytes() const { return (long long)oza_d.n; }
     // right-hand-side buckets: a product with mu right-hand sides (1 to 8)
     // runs padded with zero columns to mu_run (one pass over the factors
     // instead of one per group of 4, 2, 1); 0 runs it unpadded.  The
@@ -301,8 +309,9 @@ class HMatrix {
     bool emu_ok_ = false;
     void launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st);
     // mu_run > mu: padded to that many right-hand sides (zero columns)
+    // w_gexp: scratch of the digit-plane phase 1 (none: that phase 1 is not used)
     void launch_product_with(const double *x, double *y, int mu, int numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr,
-                             int mu_run = 0);
+                             int mu_run = 0, int *w_gexp = nullptr);
     void launch_sums(double *y, int mu, int numbering, const double *w_z, cudaStream_t st);
     void upload_phase1_lists();
     DevBuf<P1Item> p1e_d; // phase-1 tiles on the emulation (p1_d: on DFMA)
@@ -366,6 +375,20 @@ class HMatrix {
     DevBuf<unsigned char> tca_d;
     DevBuf<long long> tcoff_d;
     void build_tc_arena();
+    // the digit planes of the current storage (oz.cu): the stacked blocks of
+    // the FP64 tiles (the reduced ones reuse tcblk_d), the planes, each
+    // block's offset and row exponents; S of the planes built (0: none)
+    bool oz_on_ = false;
+    int oz_S_   = 0;
+    DevBuf<TcSeg> ozseg64_d;
+    DevBuf<TcBlock> ozblk64_d;
+    int n_ozblk64_ = 0;
+    DevBuf<unsigned char> oza_d;
+    DevBuf<long long> ozoff_d;
+    DevBuf<int> ozrexp_d;
+    DevBuf<int> ozg; // per product: the input's exponent groups (ceil(nc / 32) x mu)
+    void build_oz_arena();
+    long long oz_arena_need(); // bytes the planes of the current storage take
     void phase1_tc(const F2 *w_xs, int mu, double *w_A, cudaStream_t st); // the tcgen05 phase 1, from the arena when there is one
     DevBuf<Tc2Slab> tc2slab_d; // tensor-core phase 2: slabs and the first slab of each group of four row chunks
     DevBuf<int> tc2g_d;

@@ -1,0 +1,556 @@
+// Phase 1 of products with many right-hand sides on the BF16 tensor cores,
+// at FP64 accuracy (FP64 storage) or FP32 accuracy (reduced storage), by
+// exact digit slicing (the Ozaki scheme: K. Ozaki, T. Ogita, S. Oishi,
+// S. M. Rump, "Error-free transformations of matrix multiplication by using
+// fast routines of matrix multiplication and its applications", Numer.
+// Algorithms 59, 2012).
+//
+// htool applies a low-rank leaf as U (V^T x) (lrmat/lrmat.hpp:89-100), for mu
+// right-hand sides one gemm with the row-major right-hand sides
+// (types/matrix.hpp:346, 380).  The tiles on the same x rows are stacked into
+// blocks of at most 128 columns (TcBlock / TcSeg, as for the TF32 kernels of
+// tc.cu): D (128 x 64) = [V_1 .. V_p]^T (128 x K, K <= 256) * X (K x 64).
+//
+// GB300's FP64 pipe is about 1/1800 of its BF16 tensor rate, so FP64 work is
+// cast as exact integer products.  Every row of A (a factor column) is
+// scaled by a power of two 2^-ea at least its largest magnitude, every
+// column of B (a right-hand side over the block's x rows) by 2^-eb, and
+// rounded to the integer Q = round(v 2^T), |Q| <= 2^T, T = 6 + 7 (S - 1).
+// Q is cut into S balanced base-128 digits d_0 (top, |d_0| <= 65) ..
+// d_{S-1} (|d| <= 64), each exact in BF16:
+//
+//     Q = sum_i d_i 2^(7 (S - 1 - i)).
+//
+// The products of digit planes i of A and j of B with i + j = D share the
+// weight 2^(7 (2S - 2 - D)); pairs with i + j >= S are dropped (they weigh
+// less than 2^-(7S - 7) of the leading term).  Each plane product is an
+// ordinary BF16 MMA with FP32 accumulation, and it is exact: a product of
+// two digits is below 2^12.1, a diagonal holds at most S pairs, K <= 256, so
+// every partial sum stays an integer below 2^24.  The S diagonals accumulate
+// in S tensor-memory accumulators of 64 columns; the read-out combines them
+// exactly in 128-bit integers and converts once (integer arithmetic only:
+// the FP64 pipe is not used anywhere).  With S = 8 (T = 55) the result carries the
+// rounding of the inputs to 55 bits relative to the block's row / column
+// maxima (FP64-grade); with S = 4 (T = 27) of reduced-precision factors it
+// keeps their FP32 accuracy and accumulates exactly, unlike the TF32
+// products of tc.cu whose FP32 tensor-core sums round.
+//
+// Data: the A digit planes are laid out once per H-matrix (oz_pack_kernel:
+// per block and 32-row slab, S planes of 128 x 32 BF16 in the canonical
+// no-swizzle K-major layout, 8 KB each, with each row's exponent beside),
+// brought into shared memory by one bulk copy per slab; the B planes are cut
+// by the threads from the FP64 gathered input, with exponents per group of
+// 32 x rows and right-hand side (oz_xgroup_kernel, once per product).  One
+// thread issues the MMAs (kind::f16, M 128, N 64, K 16) and commits each slab
+// to an mbarrier; every wait is bounded (status 4 on expiry, copies in flight
+// waited for, tensor memory freed).
+#include "df64.cuh"
+#include "kernels.hpp"
+#include "tcgen05.cuh"
+
+namespace htgpu {
+
+namespace {
+
+using namespace tc5;
+
+constexpr int kOzThreads = 256;
+constexpr int kOzK       = 32;  // K rows per slab
+constexpr int kOzM       = 128; // stacked columns per block (MMA M)
+constexpr int kOzN       = 64;  // right-hand sides per pass (MMA N)
+constexpr int kOzPlaneA  = kOzM * kOzK * 2; // 8 KB: one BF16 digit plane of A
+constexpr int kOzPlaneB  = kOzN * kOzK * 2; // 4 KB: one of B
+constexpr int kOzLbo     = 128;             // bytes between core matrices along K (8 BF16 values)
+constexpr int kOzSbo     = (kOzK / 8) * 128; // bytes between 8-row groups
+
+template <int S>
+struct OzCfg {
+    static constexpr int kT      = 6 + 7 * (S - 1);        // bits of the fixed-point values
+    static constexpr int kBuf    = S * (kOzPlaneA + kOzPlaneB); // one stage: A planes, B planes
+    static constexpr int kSmem   = 2 * kBuf + 128 + 4 * kOzN;   // two stages, barriers, exponents
+    static constexpr unsigned kCols = S * kOzN <= 256 ? (S * kOzN <= 128 ? 128u : 256u) : 512u; // a power of two
+    static constexpr int kSlab   = S * kOzPlaneA;           // arena bytes per slab
+};
+
+// instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits
+// 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both K-major, N / 8 at bits
+// 17-22, M / 16 at bits 24-28
+constexpr unsigned kOzIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(kOzN >> 3) << 17) | ((unsigned)(kOzM >> 4) << 24);
+
+// byte offset of BF16 element (row, k) of a 32-deep plane in the canonical layout
+__device__ __forceinline__ int oz_off(int row, int k) { return (row >> 3) * kOzSbo + (k >> 3) * kOzLbo + (row & 7) * 16 + (k & 7) * 2; }
+
+__device__ __forceinline__ unsigned long long oz_desc(unsigned addr) {
+    unsigned long long d = (unsigned long long)((addr >> 4) & 0x3FFFu);
+    d |= (unsigned long long)((kOzLbo >> 4) & 0x3FFF) << 16;
+    d |= (unsigned long long)((kOzSbo >> 4) & 0x3FFF) << 32;
+    d |= 1ull << 46;
+    return d;
+}
+
+__device__ __forceinline__ void oz_mma(unsigned tmem_d, unsigned long long a, unsigned long long b, int accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d), "l"(a), "l"(b), "r"(kOzIdesc), "r"(accumulate) : "memory");
+}
+
+// biased exponent field of |v| (0 for zero and subnormals)
+__device__ __forceinline__ int oz_ebits(double v) { return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF); }
+
+// round(v 2^(T + 1022 - emax)) for |v| < 2^(emax - 1022): integer operations
+// on the bits of v (subnormals count as zero)
+template <int T>
+__device__ __forceinline__ long long oz_fixed(double v, int emax) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e                = (int)((b >> 52) & 0x7FF);
+    if (e == 0)
+        return 0;
+    const long long M = (long long)((b & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+    const int sh      = e - emax + T - 53;
+    long long q;
+    if (sh >= 0)
+        q = M << sh;
+    else if (sh > -60)
+        q = (M + (1ll << (-sh - 1))) >> (-sh);
+    else
+        q = 0;
+    return (b >> 63) ? -q : q;
+}
+
+// balanced base-128 digits of q, d[0] the top one
+template <int S>
+__device__ __forceinline__ void oz_digits(long long q, int (&d)[S]) {
+#pragma unroll
+    for (int i = S - 1; i >= 1; i--) {
+        int lo = (int)(q & 127);
+        lo     = lo >= 64 ? lo - 128 : lo;
+        d[i]   = lo;
+        q      = (q - lo) >> 7;
+    }
+    d[0] = (int)q;
+}
+
+__device__ __forceinline__ unsigned oz_bf2(int a, int b) { // two small integers as BF16 (exact)
+    unsigned r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"((float)b), "f"((float)a));
+    return r;
+}
+
+// eight consecutive K values of one row, cut into S digit planes, one
+// 16-byte store per plane
+template <int S, int T>
+__device__ __forceinline__ void oz_put8(unsigned char *planes, int plane_bytes, int row, int k, const double (&v)[8], int emax) {
+    int d[8][S];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        oz_digits<S>(oz_fixed<T>(v[q], emax), d[q]);
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        uint4 w;
+        w.x = oz_bf2(d[0][s], d[1][s]);
+        w.y = oz_bf2(d[2][s], d[3][s]);
+        w.z = oz_bf2(d[4][s], d[5][s]);
+        w.w = oz_bf2(d[6][s], d[7][s]);
+        *reinterpret_cast<uint4 *>(planes + (size_t)s * plane_bytes + oz_off(row, k)) = w;
+    }
+}
+
+// |I| normalised: the leading bit at 127, its position, the sign
+struct OzNorm {
+    unsigned long long hi, lo;
+    int top; // bit index of the leading one in |I|
+    bool neg;
+};
+__device__ __forceinline__ OzNorm oz_norm(__int128 I) {
+    OzNorm n;
+    n.neg                  = I < 0;
+    unsigned __int128 u    = n.neg ? (unsigned __int128)(-I) : (unsigned __int128)I;
+    unsigned long long hi  = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
+    const int lz           = hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
+    u <<= lz;
+    n.hi  = (unsigned long long)(u >> 64);
+    n.lo  = (unsigned long long)u;
+    n.top = 127 - lz;
+    return n;
+}
+
+// I 2^k as a double, integer operations only (round to nearest even)
+__device__ __forceinline__ double oz_i2d(__int128 I, int k) {
+    if (I == 0)
+        return 0.;
+    const OzNorm n        = oz_norm(I);
+    unsigned long long m  = n.hi >> 11; // 53 bits
+    const unsigned rem    = (unsigned)(n.hi & 0x7FF);
+    int ex                = 1023 + n.top + k;
+    if (rem > 0x400u || (rem == 0x400u && (n.lo != 0 || (m & 1))))
+        m++;
+    if (m >> 53) {
+        m >>= 1;
+        ex++;
+    }
+    if (ex <= 0)
+        return 0.;
+    return __longlong_as_double((long long)((n.neg ? 1ull << 63 : 0ull) | ((unsigned long long)ex << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
+
+// I 2^k as a float (round to nearest even)
+__device__ __forceinline__ float oz_i2f(__int128 I, int k) {
+    if (I == 0)
+        return 0.f;
+    const OzNorm n               = oz_norm(I);
+    unsigned m                   = (unsigned)(n.hi >> 40); // 24 bits
+    const unsigned long long rem = n.hi & 0xFFFFFFFFFFull;
+    int ex                       = 127 + n.top + k;
+    if (rem > 0x8000000000ull || (rem == 0x8000000000ull && (n.lo != 0 || (m & 1))))
+        m++;
+    if (m >> 24) {
+        m >>= 1;
+        ex++;
+    }
+    const unsigned sgn = n.neg ? 1u << 31 : 0u;
+    if (ex <= 0)
+        return 0.f;
+    if (ex >= 255)
+        return __uint_as_float(sgn | 0x7F800000u);
+    return __uint_as_float(sgn | ((unsigned)ex << 23) | (m & 0x7FFFFFu));
+}
+
+__device__ __forceinline__ float bf16f_oz(unsigned short h) { return __uint_as_float((unsigned)h << 16); }
+
+// the value of row `row` (stacked column) of block B at source row j
+struct OzSrc {
+    const double *f64;        // FP64 tiles (jlen x r column-major, ld jlen) at element offset seg.off
+    const unsigned char *mix; // or reduced tiles at byte offset seg.off: c32 FP32 columns, then BF16
+};
+
+__device__ __forceinline__ void oz_column(const OzSrc &src, const TcBlock &B, const TcSeg &S, int col, const double *&c64, const float *&c32, const unsigned short *&c16) {
+    c64 = nullptr;
+    c32 = nullptr;
+    c16 = nullptr;
+    if (src.f64)
+        c64 = src.f64 + S.off + (long long)B.jlen * col;
+    else if (col < S.c32)
+        c32 = reinterpret_cast<const float *>(src.mix + S.off) + (long long)ld_f32(B.jlen) * col;
+    else
+        c16 = reinterpret_cast<const unsigned short *>(src.mix + S.off + 4LL * ld_f32(B.jlen) * S.c32) + (long long)ld_bf16(B.jlen) * (col - S.c32);
+}
+
+__device__ __forceinline__ double oz_value(const double *c64, const float *c32, const unsigned short *c16, int j) {
+    if (c64)
+        return c64[j];
+    if (c32)
+        return (double)c32[j];
+    if (c16)
+        return (double)bf16f_oz(c16[j]);
+    return 0.;
+}
+
+// one CTA per block: each row's exponent, then its digit planes slab by slab
+template <int S>
+__global__ void __launch_bounds__(kOzThreads) oz_pack_kernel(const TcBlock *__restrict__ blocks, const TcSeg *__restrict__ segs, OzSrc src, const long long *__restrict__ ozoff,
+                                                             int *__restrict__ rexp, unsigned char *__restrict__ arena) {
+    __shared__ int se[2][kOzM];
+    const int tid = threadIdx.x, row = tid & 127, half = tid >> 7;
+    const TcBlock B = blocks[blockIdx.x];
+    int m0 = 0, sg = -1;
+    for (int s = B.s0; s < B.s1; s++) {
+        const int nc = segs[s].ncol;
+        if (row < m0 + nc) {
+            sg = s;
+            break;
+        }
+        m0 += nc;
+    }
+    const double *c64          = nullptr;
+    const float *c32           = nullptr;
+    const unsigned short *c16  = nullptr;
+    if (sg >= 0) {
+        const TcSeg Sg = segs[sg];
+        oz_column(src, B, Sg, Sg.col0 + row - m0, c64, c32, c16);
+    }
+    int e = 0;
+    for (int j = half; j < B.jlen; j += 2)
+        e = max(e, oz_ebits(oz_value(c64, c32, c16, j)));
+    se[half][row] = e;
+    __syncthreads();
+    const int emax = max(se[0][row], se[1][row]);
+    if (half == 0)
+        rexp[(long long)blockIdx.x * kOzM + row] = emax;
+    const int kh = half * 16;
+    for (int ks = 0, slab = 0; ks < B.jlen; ks += kOzK, slab++) {
+        unsigned char *planes = arena + ozoff[blockIdx.x] + (long long)slab * OzCfg<S>::kSlab;
+#pragma unroll
+        for (int q8 = 0; q8 < 2; q8++) {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int j = ks + kh + 8 * q8 + q;
+                v[q]        = j < B.jlen ? oz_value(c64, c32, c16, j) : 0.;
+            }
+            oz_put8<S, OzCfg<S>::kT>(planes, kOzPlaneA, row, kh + 8 * q8, v, emax);
+        }
+    }
+}
+
+// exponent field maxima of the gathered input per group of 32 rows and right-hand side
+__global__ void oz_xgroup_kernel(const double *__restrict__ xp, int nrows, int mu, int *__restrict__ gexp) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ng      = (nrows + 31) >> 5;
+    if (t >= (long long)ng * mu)
+        return;
+    const int g = (int)(t / mu), c = (int)(t - (long long)g * mu);
+    int e       = 0;
+    const int j1 = min(nrows, 32 * g + 32);
+    for (int j = 32 * g; j < j1; j++)
+        e = max(e, oz_ebits(xp[(long long)j * mu + c]));
+    gexp[t] = e;
+}
+
+// Eight warps; thread t cuts 8 K values of right-hand side t mod 64 into
+// digit planes; thread 0 issues the copies and the MMAs.  OUT64: FP64 sums
+// (FP64 storage); else FP32 sums times the columns' scales.
+template <int S, bool OUT64>
+__global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ arena,
+                                                                  const long long *__restrict__ ozoff, const int *__restrict__ rexp, const float *__restrict__ scale,
+                                                                  const double *__restrict__ xp, const int *__restrict__ gexp, const int *__restrict__ xexp, int mu, void *__restrict__ Aout,
+                                                                  int *__restrict__ status) {
+    using C = OzCfg<S>;
+    constexpr int T = C::kT;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *bars  = reinterpret_cast<unsigned long long *>(smem + 2 * C::kBuf);      // products of a stage done
+    unsigned long long *fulls = reinterpret_cast<unsigned long long *>(smem + 2 * C::kBuf + 16); // a stage's A planes landed
+    unsigned *tslot           = reinterpret_cast<unsigned *>(smem + 2 * C::kBuf + 64);
+    int *sE                   = reinterpret_cast<int *>(smem + 2 * C::kBuf + 128); // the pass's right-hand-side exponents
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const int bn = tid & 63, bk = (tid >> 6) * 8; // B: right-hand side and first K value
+    if (tid == 0) {
+        bar_init(&bars[0]);
+        bar_init(&bars[1]);
+        bar_init(&fulls[0]);
+        bar_init(&fulls[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot, C::kCols);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tmem = *tslot;
+    // FP32 sums are kept in the units of the split input, x 2^(1023 - xexp)
+    const int kunits = OUT64 ? 0 : 1023 - max(*xexp, 1);
+    int slabs  = 0; // slabs issued by this CTA: stage slabs & 1, its (slabs >> 1)-th use
+    int copies = 0; // A copies issued (thread 0)
+    bool fail  = false;
+    for (int bi = blockIdx.x; bi < nblocks && !fail; bi += gridDim.x) {
+        const TcBlock B = blocks[bi];
+        const double *X = xp + (long long)B.xrow * mu;
+        const unsigned char *ablk = arena + ozoff[bi];
+        const int g0 = B.xrow >> 5, g1 = (B.xrow + B.jlen - 1) >> 5;
+        for (int cb = 0; cb < mu && !fail; cb += kOzN) {
+            const bool on = cb + bn < mu;
+            int eb        = 0; // exponent of this thread's right-hand side over the block's rows
+            if (on)
+                for (int g = g0; g <= g1; g++)
+                    eb = max(eb, gexp[(long long)g * mu + cb + bn]);
+            if (tid < kOzN)
+                sE[tid] = eb;
+            double b[8];
+            auto loadb = [&](int ks) {
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int j = ks + bk + q;
+                    b[q]        = (on && j < B.jlen) ? X[(long long)j * mu + cb + bn] : 0.;
+                }
+            };
+            loadb(0);
+            for (int ks = 0; ks < B.jlen; ks += kOzK) {
+                const int buf = slabs & 1, use = slabs >> 1;
+                unsigned char *stage = smem + (size_t)buf * C::kBuf;
+                if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1)) // the products of two slabs ago read this stage
+                    fail = true;
+                if (__syncthreads_or(fail)) {
+                    fail = true;
+                    break;
+                }
+                if (tid == 0) { // this slab's A planes, one bulk copy
+                    bar_expect_tx(&fulls[buf], C::kSlab);
+                    bulk_g2s(stage, ablk + (long long)(ks / kOzK) * C::kSlab, C::kSlab, &fulls[buf]);
+                    copies++;
+                }
+                oz_put8<S, T>(stage + S * kOzPlaneA, kOzPlaneB, bn, bk, b, eb);
+                if (ks + kOzK < B.jlen) // the next slab's x values fly while this one is multiplied
+                    loadb(ks + kOzK);
+                proxy_fence();
+                __syncthreads();
+                if (tid == 0) {
+                    if (bar_wait(&fulls[buf], use & 1)) {
+                        fence_after();
+                        const unsigned a0 = smem_u32(stage), b0 = a0 + S * kOzPlaneA;
+#pragma unroll
+                        for (int kk = 0; kk < kOzK / 16; kk++)
+#pragma unroll
+                            for (int D = 0; D < S; D++)
+#pragma unroll
+                                for (int i = 0; i <= D; i++)
+                                    oz_mma(tmem + (unsigned)(D * kOzN), oz_desc(a0 + i * kOzPlaneA + kk * 2 * kOzLbo), oz_desc(b0 + (D - i) * kOzPlaneB + kk * 2 * kOzLbo),
+                                           !(ks == 0 && kk == 0 && i == 0));
+                        commit(&bars[buf]);
+                    } else {
+                        fail = true; // spreads at the next barrier
+                    }
+                }
+                slabs++;
+            }
+            if (__syncthreads_or(fail)) {
+                fail = true;
+                break;
+            }
+            const int last = slabs - 1;
+            if (!bar_wait(&bars[last & 1], (last >> 1) & 1))
+                fail = true;
+            if (__syncthreads_or(fail)) {
+                fail = true;
+                break;
+            }
+            fence_after();
+            {
+                // warp w reads lanes 32 (w mod 4) ..: the rows of those
+                // threads; warps 0-3 the first 32 right-hand sides, 4-7 the last 32
+                const int orow = 32 * (wid & 3) + lane, c0 = 32 * (wid >> 2);
+                int osg = -1, om0 = 0;
+                for (int s2 = B.s0; s2 < B.s1; s2++) {
+                    const int nc = segs[s2].ncol;
+                    if (orow < om0 + nc) {
+                        osg = s2;
+                        break;
+                    }
+                    om0 += nc;
+                }
+                long long oo = 0;
+                float osc    = 1.f;
+                if (osg >= 0) {
+                    oo = (segs[osg].slot + (long long)(orow - om0)) * mu;
+                    if (!OUT64)
+                        osc = scale[segs[osg].sidx + orow - om0];
+                }
+                const int er = rexp[(long long)bi * kOzM + orow];
+                // sum_D acc_D 2^(7 (2S - 2 - D)) = 2^(7 (S - 1)) I with
+                // I = sum_D acc_D 2^(7 (S - 1 - D)), exact in 128 bits;
+                // value = that 2^(er - 1022 - T) 2^(eb - 1022 - T)
+                const int kr = 7 * (S - 1) + er - 2044 - 2 * T + kunits;
+#pragma unroll
+                for (int c16 = 0; c16 < 2; c16++) {
+                    __int128 I[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        I[q] = 0;
+#pragma unroll
+                    for (int D = 0; D < S; D++) {
+                        unsigned r[16];
+                        tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + (unsigned)(D * kOzN + c0 + 16 * c16), r);
+#pragma unroll
+                        for (int q = 0; q < 16; q++)
+                            I[q] += (__int128)__float2int_rn(__uint_as_float(r[q])) << (7 * (S - 1 - D));
+                    }
+                    if (osg >= 0)
+#pragma unroll
+                        for (int q = 0; q < 16; q++) {
+                            const int cl = c0 + 16 * c16 + q, c = cb + cl;
+                            if (c < mu) {
+                                if (OUT64)
+                                    reinterpret_cast<double *>(Aout)[oo + c] = oz_i2d(I[q], kr + sE[cl]);
+                                else
+                                    reinterpret_cast<float *>(Aout)[oo + c] = oz_i2f(I[q], kr + sE[cl]) * osc;
+                            }
+                        }
+                }
+            }
+            fence_before();
+            __syncthreads(); // the accumulators are read out (and sE) before the next pass overwrites them
+        }
+    }
+    if (fail) {
+        if (lane == 0)
+            atomicExch(status, 4);
+        // the A copies this CTA issued land before it leaves
+        if (tid == 0)
+            for (int p = 0; p < 2 && p < copies; p++) {
+                const int c = copies - 1 - p;
+                bar_wait(&fulls[c & 1], (c >> 1) & 1);
+            }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (wid == 0)
+        tmem_free(tmem, C::kCols);
+}
+
+template <int S, bool OUT64>
+void oz_launch(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *arena, const long long *ozoff, const int *rexp, const float *scale, const double *xp, const int *gexp,
+               const int *xexp, int mu, void *A, int *status, cudaStream_t st) {
+    static unsigned long long done = 0;
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        HTGPU_CUDA(cudaFuncSetAttribute(phase1_oz_kernel<S, OUT64>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzCfg<S>::kSmem));
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int per_sm = OzCfg<S>::kSmem * 2 <= 227 * 1024 ? 2 : 1;
+    const int grid   = std::min(nblocks, per_sm * sms);
+    phase1_oz_kernel<S, OUT64><<<grid, kOzThreads, OzCfg<S>::kSmem, st>>>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+} // namespace
+
+long long oz_arena_bytes(const TcBlock *blocks_h, int nblocks, int S, long long *ozoff_h) {
+    long long off = 0;
+    for (int b = 0; b < nblocks; b++) {
+        ozoff_h[b] = off;
+        off += (long long)((blocks_h[b].jlen + kOzK - 1) / kOzK) * S * kOzPlaneA;
+    }
+    return off;
+}
+
+void launch_oz_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const double *f64, const unsigned char *mix, int S, const long long *ozoff, int *rexp, unsigned char *arena,
+                    cudaStream_t st) {
+    if (nblocks <= 0)
+        return;
+    OzSrc src{f64, mix};
+    if (S == 8)
+        oz_pack_kernel<8><<<nblocks, kOzThreads, 0, st>>>(blocks, segs, src, ozoff, rexp, arena);
+    else if (S == 4)
+        oz_pack_kernel<4><<<nblocks, kOzThreads, 0, st>>>(blocks, segs, src, ozoff, rexp, arena);
+    else
+        throw Error(1, "[Htool error] digit planes: S must be 4 or 8");
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_oz_xgroups(const double *xp, int nrows, int mu, int *gexp, cudaStream_t st) {
+    const long long n = (long long)((nrows + 31) >> 5) * mu;
+    if (n <= 0)
+        return;
+    oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xp, nrows, mu, gexp);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase1_oz(const TcBlock *blocks, int nblocks, const TcSeg *segs, int S, const unsigned char *arena, const long long *ozoff, const int *rexp, const float *scale, const double *xp,
+                      const int *gexp, const int *xexp, int mu, void *A, int *status, cudaStream_t st) {
+    if (scale && !xexp)
+        throw Error(1, "[Htool error] digit planes: FP32 sums need the input's exponent");
+    if (nblocks <= 0)
+        return;
+    if (S == 8 && !scale)
+        oz_launch<8, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+    else if (S == 4 && scale)
+        oz_launch<4, false>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+    else if (S == 8)
+        oz_launch<8, false>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+    else if (S == 4)
+        oz_launch<4, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+    else
+        throw Error(1, "[Htool error] digit planes: S must be 4 or 8");
+}
+
+} // namespace htgpu

@@ -30,6 +30,7 @@
 // the CTA stops after freeing its tensor memory.
 #include "df64.cuh"
 #include "kernels.hpp"
+#include "tcgen05.cuh"
 
 namespace htgpu {
 
@@ -46,14 +47,12 @@ constexpr int kTcBBytes  = kTcN * kTcK * 4;       // 8 KB: one TF32 part of B
 constexpr int kTcBuf     = 2 * kTcABytes + 2 * kTcBBytes; // A hi, A lo, B hi, B lo
 constexpr int kTcSmem    = 2 * kTcBuf + 128;       // two buffers, barriers, tensor-memory slot
 constexpr unsigned kTcCols = 64;                   // tensor-memory columns: the 64 FP32 accumulators of a row
-constexpr long long kTcWait = 2000000000ll;        // about 1 s of SM clocks
 
 // instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator (bits
 // 4-5 = 1), A and B TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 =
 // 0), N / 8 at bits 17-22, M / 16 at bits 24-28
 constexpr unsigned kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kTcN >> 3) << 17) | ((unsigned)(kTcM >> 4) << 24);
 
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 // byte offset of element (row, k) of a slab in the canonical layout
 __device__ __forceinline__ int tc_off(int row, int k) { return (row >> 3) * kTcSbo + (k >> 2) * kTcLbo + (row & 7) * 16 + (k & 3) * 4; }
@@ -73,45 +72,27 @@ __device__ __forceinline__ void tc_mma(unsigned tmem_d, unsigned long long a, un
                  : "memory");
 }
 
-// the mbarrier completes once every tcgen05 operation this thread issued so far has
-__device__ __forceinline__ void tc_commit(unsigned long long *bar) { asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-// shared-memory writes of this thread become visible to the tensor cores
-__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__device__ __forceinline__ void bar_init(unsigned long long *b) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory"); }
 
-// bounded wait for the completion of the phase of parity `parity`
-__device__ __forceinline__ bool bar_wait(unsigned long long *b, unsigned parity) {
-    const long long t0 = clock64();
-    while (true) {
-        unsigned ok;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_u32(b)), "r"(parity), "r"(20000u) : "memory");
-        if (ok)
-            return true;
-        if (clock64() - t0 > kTcWait)
-            return false;
-    }
-}
 
-// warp-wide tensor-memory allocation; the address lands in *slot
-__device__ __forceinline__ void tmem_alloc(unsigned *slot) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(kTcCols) : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_free(unsigned taddr) { asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTcCols) : "memory"); }
+
+using tc5::bar_expect_tx;
+using tc5::bar_init;
+using tc5::bar_wait;
+using tc5::bulk_g2s;
+using tc5::proxy_fence;
+using tc5::smem_u32;
+__device__ __forceinline__ void tc_commit(unsigned long long *bar) { tc5::commit(bar); }
+__device__ __forceinline__ void tc_fence_after() { tc5::fence_after(); }
+__device__ __forceinline__ void tc_fence_before() { tc5::fence_before(); }
+__device__ __forceinline__ void tmem_alloc(unsigned *slot) { tc5::tmem_alloc(slot, kTcCols); }
+__device__ __forceinline__ void tmem_free(unsigned taddr) { tc5::tmem_free(taddr, kTcCols); }
 
 // 16 consecutive FP32 columns of this thread's tensor-memory lane (lane =
 // 32 * warp + lane id), waited for
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
     unsigned r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
-                 "tcgen05.wait::ld.sync.aligned;"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                   "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr)
-                 : "memory");
+    tc5::tmem_ld16(taddr, r);
 #pragma unroll
     for (int i = 0; i < 16; i++)
         v[i] = __uint_as_float(r[i]);
@@ -360,13 +341,6 @@ __global__ void __launch_bounds__(kTc1Threads) tc_pack_kernel(const TcBlock *__r
             put4(hi, lo, row, kh + 4 * q, a.x, a.y, a.z, a.w);
         }
     }
-}
-
-__device__ __forceinline__ void bar_expect_tx(unsigned long long *b, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
 __global__ void __launch_bounds__(kTc1Threads, 2) phase1_tc_pre_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ tca,

@@ -1,0 +1,65 @@
+// Primitives of the tcgen05 kernels (tc.cu, oz.cu): 5th-generation tensor
+// core MMAs with tensor-memory accumulators, mbarriers with bounded waits,
+// bulk copies global -> shared memory.  Inline PTX for sm_103a.
+#pragma once
+
+namespace htgpu {
+namespace tc5 {
+
+constexpr long long kWaitCycles = 2000000000ll; // about 1 s of SM clocks
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// the mbarrier completes once every tcgen05 operation this thread issued so far has
+__device__ __forceinline__ void commit(unsigned long long *bar) { asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+// shared-memory writes of this thread become visible to the tensor cores
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bar_init(unsigned long long *b) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory"); }
+
+// bounded wait for the completion of the phase of parity `parity`
+__device__ __forceinline__ bool bar_wait(unsigned long long *b, unsigned parity) {
+    const long long t0 = clock64();
+    while (true) {
+        unsigned ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_u32(b)), "r"(parity), "r"(20000u) : "memory");
+        if (ok)
+            return true;
+        if (clock64() - t0 > kWaitCycles)
+            return false;
+    }
+}
+
+// this thread's arrival, expecting `bytes` of asynchronous copies on the barrier
+__device__ __forceinline__ void bar_expect_tx(unsigned long long *b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+// bytes (a multiple of 16, both addresses 16-byte aligned) global -> shared,
+// completing on the barrier
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// warp-wide tensor-memory allocation of ncols (a power of two >= 32)
+// columns; the address lands in *slot
+__device__ __forceinline__ void tmem_alloc(unsigned *slot, unsigned ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(unsigned taddr, unsigned ncols) { asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory"); }
+
+// 16 consecutive 32-bit columns of this thread's tensor-memory lane (lane =
+// 32 * (warp mod 4) + lane id), waited for
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+}
+
+} // namespace tc5
+} // namespace htgpu

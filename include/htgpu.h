@@ -402,12 +402,35 @@ int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode);
 int htgpu_hmatrix_set_tensor_core_arena(htgpu_hmatrix h, int on);
 int htgpu_hmatrix_get_tensor_core_arena(htgpu_hmatrix h, int *on, long long *bytes);
 
+/* Phase 1 of products with 8 or more right-hand sides on the BF16 tensor
+ * cores by exact digit slicing (the Ozaki scheme): every factor column and
+ * right-hand side is scaled by a power of two and cut into base-128 digits
+ * (8 planes for FP64 storage: 55 bits, FP64-grade sums; 4 for reduced
+ * storage: 27 bits, at any epsilon), the plane products are exact integer
+ * MMAs, the read-out sums them exactly in 128-bit integers.  Replaces the
+ * double-float FP64 phase 1 and the reduced-precision phase-1 kernels of
+ * those products.  Costs a copy of the factors cut into planes (*bytes; 0
+ * while off); on after a build follows it and precision changes.  Off by
+ * default; htgpu_hmatrix_autotune tries it where the planes fit in half the
+ * free memory.  No counterpart in the reference (its gemm calls,
+ * types/matrix.hpp:346, 380). */
+int htgpu_hmatrix_set_digit_planes(htgpu_hmatrix h, int on);
+int htgpu_hmatrix_get_digit_planes(htgpu_hmatrix h, int *on, long long *bytes);
+
 /* Test support, no counterpart in the reference: d (128 x 64) = a (128 x
  * 32) b (32 x 64), row-major host arrays, computed on CUDA device `device`
  * by the tcgen05 path of the tensor-core kernels (the same shared-memory
  * layout, descriptors, three-term TF32 products and tensor-memory read-out),
  * so that path can be checked on its own. */
 int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d);
+
+/* Test support, no counterpart in the reference: d (128 x mu) = a (128 x K)
+ * b (K x mu), row-major FP64 host arrays, K <= 256, computed on CUDA device
+ * `device` by the digit-plane path of the tensor-core phase 1 (the FP64
+ * products cut into S = 8 or 4 BF16 digit planes, exact MMA sums, integer
+ * read-out): one stacked block through the plane packing, the input's
+ * exponent groups and the phase-1 kernel. */
+int htgpu_debug_oz_gemm(int device, int S, int K, int mu, const double *a, const double *b, double *d);
 
 /* Status word of the product kernels' bounded waits: 0, or 1/2/3 when a
  * wait for a pipeline stage ran out, 4 when a wait of the tensor-core
