@@ -79,6 +79,7 @@ def parse():
     p.add_argument("--phase2-mode", type=int, default=None, help="FP64: 0 per-warp streams, 1 producer-fed")
     p.add_argument("--mixed-phase2-mode", type=int, default=None, help="mixed precision: 0 per-warp streams, 1 producer-fed")
     p.add_argument("--mixed-dense-split", type=int, default=None, help="mixed precision, 4+ right-hand sides: 1 dense chunks first in the double-float kernel")
+    p.add_argument("--digit-planes", type=int, default=None, help="8+ right-hand sides: 1 phase 1 on the BF16 tensor cores by exact digit slicing, 0 not")
     return p.parse_args()
 
 
@@ -323,8 +324,10 @@ def run_gpu(args):
         run = hm.get_rhs_bucket(mu) if mu <= 8 else mu
         if run <= 2:
             p1 = "phase 1 (tile kernels)" if mode1 == 0 else "phase1_cta_kernel"
+        elif run >= 8 and hm.get_digit_planes()[0]:
+            p1 = "phase1_oz_kernel"
         elif precision != "fp64":
-            p1 = "phase1_mixed_kernel" if mode1 == 0 else "phase1_stack_kernel"
+            p1 = "phase1_mixed_kernel" if mode1 == 0 else ("phase1_tc_kernel" if mode1 == 2 and run >= 8 else "phase1_stack_kernel")
         else:
             p1 = "phase1_df_mrhs_kernel" if run >= 8 else "phase 1 (tile kernels)"
         p2 = "phase2_df_mrhs_kernel" if (precision == "fp64" and run >= 8) else ("phase2_warp_kernel" if hm.get_phase2_mode() == 0 else "phase2_ws_kernel")
@@ -341,7 +344,7 @@ def run_gpu(args):
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
         }
 
-    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode, args.mixed_dense_split))
+    fixed = any(v is not None for v in (args.fp64_split, args.phase1_mode, args.mixed_split, args.mixed_phase1_mode, args.phase2_mode, args.mixed_phase2_mode, args.mixed_dense_split, args.digit_planes))
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.5)  # let the sampler start before the timed regions
@@ -354,11 +357,14 @@ def run_gpu(args):
             hm.set_phase1_mode(args.phase1_mode)
         if args.phase2_mode is not None:
             hm.set_phase2_mode(args.phase2_mode)
+        if args.digit_planes is not None:
+            hm.set_digit_planes(bool(args.digit_planes))
         tune64 = None
     else:
         tune64 = hm.autotune(mu, 5)
     split = hm.get_fp64_split()
     p1mode64, p2mode64 = hm.get_phase1_mode(), hm.get_phase2_mode()
+    planes64 = hm.get_digit_planes()[0]
     ms64, launches64 = timed_products()
     y64 = yd.cpu().numpy().copy()
     step64, d64 = describe(ms64, "fp64")
@@ -375,6 +381,8 @@ def run_gpu(args):
             hm.set_phase2_mode(args.mixed_phase2_mode)
         if args.mixed_dense_split is not None:
             hm.set_phase2_dense_split(bool(args.mixed_dense_split))
+        if args.digit_planes is not None:
+            hm.set_digit_planes(bool(args.digit_planes))
         tunem = None
     else:
         tunem = hm.autotune(mu, 5)
@@ -450,12 +458,12 @@ def run_gpu(args):
         "config": dict(WORKLOAD, n=n, mu=mu),
         "run": {"precision": "fp64", "parallelism": "replicas" if world > 1 else "single", "stored_gb": {"fp64": d64["whole_product"]["bytes"] / 1e9, "mixed": dm["whole_product"]["bytes"] / 1e9}},
         "roofline": d64["roofline"], "whole_product": d64["whole_product"], "phase_ms": d64["phase_ms"], "phase_bytes": d64["phase_bytes"],
-        "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64, "phase1_mode": p1mode64, "phase2_mode": p2mode64},
+        "fp64_split": {"phase1_dfma_permille": split[0], "phase2_dfma_permille": split[1], "autotune_ms": tune64, "phase1_mode": p1mode64, "phase2_mode": p2mode64, "digit_planes": planes64},
         "e2e": e2e64,
         "mixed": {"value": valuem, "unit": UNIT, "ms_per_step": stepm, "speedup_vs_fp64": valuem / value64, "rel_err_vs_fp64": err_mixed_vs_fp64, "tau": tau,
                   "dtype": "fp32/bf16 factors (per-column scaled), fp64 dense, fp32+fp64 accumulation", "e2e": e2em,
                   "roofline": dm["roofline"], "whole_product": dm["whole_product"], "phase_ms": dm["phase_ms"], "phase_bytes": dm["phase_bytes"],
-                  "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "phase2_mode": hm.get_phase2_mode(), "dense_dfma_permille": splitm},
+                  "precision": {"fp32_columns": pinfo["fp32_columns"], "bf16_columns": pinfo["bf16_columns"], "stored_bytes": pinfo["stored_bytes"], "autotune_ms": tunem, "phase1_mode": hm.get_phase1_mode(), "phase2_mode": hm.get_phase2_mode(), "dense_dfma_permille": splitm, "digit_planes": hm.get_digit_planes()[0]},
                   "gpu_launches": launchesm * args.steps},
         "gpu_launches": launches64 * args.steps, "clocks": clk, "device_status": status,
         "rel_err_vs_dense_1000_rows": dense_err,

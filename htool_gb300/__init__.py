@@ -123,7 +123,7 @@ def _load():
         "htgpu_hmatrix_reset_status": (i, [vp]),
         "htgpu_hmatrix_set_tensor_core_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_tensor_core_mode": (i, [vp, vp]),
-        "htgpu_debug_oz_gemm": (i, [i, i, i, i, vp, vp, vp]),
+        "htgpu_debug_oz_gemm": (i, [i, i, i, i, i, vp, vp, vp]),
         "htgpu_hmatrix_set_digit_planes": (i, [vp, i]),
         "htgpu_hmatrix_get_digit_planes": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_tensor_core_arena": (i, [vp, i]),

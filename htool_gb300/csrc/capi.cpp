@@ -727,7 +727,7 @@ int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d) {
     });
 }
 
-int htgpu_debug_oz_gemm(int device, int S, int K, int mu, const double *a, const double *b, double *d) {
+int htgpu_debug_oz_gemm(int device, int S, int K, int mu, int staged, const double *a, const double *b, double *d) {
     return guarded([&] {
         need(a, "a");
         need(b, "b");
@@ -745,8 +745,8 @@ int htgpu_debug_oz_gemm(int device, int S, int K, int mu, const double *a, const
         htgpu::DevBuf<htgpu::TcBlock> dblk;
         htgpu::DevBuf<htgpu::TcSeg> dseg;
         htgpu::DevBuf<long long> doff;
-        htgpu::DevBuf<int> rexp, gexp, st;
-        htgpu::DevBuf<unsigned char> arena;
+        htgpu::DevBuf<int> rexp, gexp, ecol, st;
+        htgpu::DevBuf<unsigned char> arena, xplanes;
         da.upload(a, (std::size_t)128 * K, nullptr);
         db.upload(b, (std::size_t)K * mu, nullptr);
         dd.alloc((std::size_t)128 * mu);
@@ -755,13 +755,20 @@ int htgpu_debug_oz_gemm(int device, int S, int K, int mu, const double *a, const
         doff.upload(&off, 1, nullptr);
         rexp.alloc(128);
         gexp.alloc((std::size_t)((K + 31) / 32) * mu);
+        ecol.alloc((std::size_t)mu + 1);
+        xplanes.alloc((std::size_t)htgpu::oz_xplanes_bytes(K, mu, S));
         arena.alloc(bytes);
         st.alloc(1);
         HTGPU_CUDA(cudaMemset(st.p, 0, sizeof(int)));
         HTGPU_CUDA(cudaMemset(dd.p, 0, sizeof(double) * 128 * mu));
+        const htgpu::OzScratch sc{gexp.p, ecol.p, xplanes.p};
         htgpu::launch_oz_pack(dblk.p, 1, dseg.p, da.p, nullptr, S, doff.p, rexp.p, arena.p, nullptr);
-        htgpu::launch_oz_xgroups(db.p, K, mu, gexp.p, nullptr);
-        htgpu::launch_phase1_oz(dblk.p, 1, dseg.p, S, arena.p, doff.p, rexp.p, nullptr, db.p, gexp.p, nullptr, mu, dd.p, st.p, nullptr);
+        htgpu::launch_oz_prepare(db.p, K, mu, S, sc, nullptr);
+        if (staged) { // the kernel of wide inputs (exponents per block)
+            const int one = 1;
+            HTGPU_CUDA(cudaMemcpy(ecol.p + mu, &one, sizeof(int), cudaMemcpyHostToDevice));
+        }
+        htgpu::launch_phase1_oz(dblk.p, 1, dseg.p, S, arena.p, doff.p, rexp.p, nullptr, db.p, sc, nullptr, mu, dd.p, st.p, nullptr);
         HTGPU_CUDA(cudaDeviceSynchronize());
         int status = 0;
         HTGPU_CUDA(cudaMemcpy(&status, st.p, sizeof(int), cudaMemcpyDeviceToHost));

@@ -984,8 +984,8 @@ void HMatrix::ensure_work(int mu) {
     z.alloc((std::size_t)std::max<long long>(zlen_, 1) * mu);
     xstage.alloc((std::size_t)nc * mu);
     ystage.alloc((std::size_t)nr * mu);
-    ozg.alloc((std::size_t)((nc + 31) / 32) * mu + 1);
     mu_cap = mu;
+    ensure_oz_work(mu);
 }
 
 void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, int numbering, cudaStream_t st) {
@@ -1337,7 +1337,7 @@ void HMatrix::get_fp64_split(int *p1, int *n64) const {
 }
 
 void HMatrix::launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st) {
-    launch_product_with(x, y, mu, numbering, st, xp.p, xs.p, xexp.p, A.p, z.p, nullptr, rhs_run(mu), ozg.p);
+    launch_product_with(x, y, mu, numbering, st, xp.p, xs.p, xexp.p, A.p, z.p, nullptr, rhs_run(mu), oz_scratch(rhs_run(mu)));
 }
 
 int HMatrix::rhs_run(int mu) const { return mu < (int)rhs_pad_.size() && rhs_pad_[mu] > mu ? rhs_pad_[mu] : mu; }
@@ -1650,13 +1650,40 @@ void HMatrix::set_digit_planes(bool on) {
     layout_gen_++; // captured products are stale
     oz_on_ = on;
     build_oz_arena();
+    ensure_oz_work(mu_cap);
+}
+
+// the per-product scratch of the digit-plane phase 1 for up to mu
+// right-hand sides (8 planes: enough for either storage)
+void HMatrix::ensure_oz_work(int mu) {
+    if (!oz_on_ || mu <= 0) {
+        ozg.release();
+        ozc.release();
+        ozx.release();
+        ozx_mu_ = 0;
+        return;
+    }
+    if (mu <= ozx_mu_)
+        return;
+    layout_gen_++; // scratch moves: captured products are stale
+    ozg.alloc((std::size_t)((nc + 31) / 32) * mu + 1);
+    ozc.alloc((std::size_t)mu + 1);
+    ozx.alloc((std::size_t)oz_xplanes_bytes(nc, mu, 8));
+    ozx_mu_ = mu;
+}
+
+const OzScratch *HMatrix::oz_scratch(int mu) {
+    if (!oz_on_ || mu > ozx_mu_ || !ozx.p)
+        return nullptr;
+    ozs_ = OzScratch{ozg.p, ozc.p, ozx.p};
+    return &ozs_;
 }
 
 // The phase-1 tiles on the FP64 pipe and those on the emulation run as two
 // kernels on two streams at once (fork/join through events), so each keeps
 // its own register budget and both pipe families work together.
 void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks,
-                                  int mu_run, int *w_gexp) {
+                                  int mu_run, const OzScratch *w_oz) {
     // a product padded up to its right-hand-side bucket runs mu columns, the
     // ones past mu_out zero, and writes mu_out
     const int mu     = std::max(mu_out, mu_run);
@@ -1673,11 +1700,11 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         if (n_p1m_ && mu <= 2 && p1_mode_ >= 1) {
             launch_phase1_stream(p1rm_d.p, n_p1m_ranges_, p1cm_d.p, p1m_kinds_, mix_.p, w_xp, w_xs, scalef_d.p, w_xexp, mu, w_A, status_d.p, st);
             launches_ += 1;
-        } else if (n_p1m_ && mu >= kMmaMinRhs && oz_S_ == 4 && w_gexp && n_tcblk_ > 0) {
+        } else if (n_p1m_ && mu >= kMmaMinRhs && oz_S_ == 4 && w_oz && n_tcblk_ > 0) {
             // the stacked blocks on the BF16 tensor cores, four digit planes
-            launch_oz_xgroups(w_xp, nc, mu, w_gexp, st);
-            launch_phase1_oz(tcblk_d.p, n_tcblk_, tcseg_d.p, 4, oza_d.p, ozoff_d.p, ozrexp_d.p, scalef_d.p, w_xp, w_gexp, w_xexp, mu, w_A, status_d.p, st);
-            launches_ += 2;
+            launch_oz_prepare(w_xp, nc, mu, 4, *w_oz, st);
+            launch_phase1_oz(tcblk_d.p, n_tcblk_, tcseg_d.p, 4, oza_d.p, ozoff_d.p, ozrexp_d.p, scalef_d.p, w_xp, *w_oz, w_xexp, mu, w_A, status_d.p, st);
+            launches_ += 5;
         } else if (n_p1m_ && mu >= 8 && !mma && p1_mode_ == 2 && tc_mode_ >= 1 && n_tcblk_ > 0) {
             // phase-1 mode 2: the stacked blocks on tcgen05 at any epsilon
             // (each stacked sum runs over at most 256 rows in FP32, as on the
@@ -1743,11 +1770,11 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         return;
     }
     const bool many = mu >= kDfMinRhs; // many right-hand sides: double-float kernels over 16 per pass
-    if (many && oz_S_ == 8 && w_gexp && n_ozblk64_ > 0) {
+    if (many && oz_S_ == 8 && w_oz && n_ozblk64_ > 0) {
         // the stacked FP64 tiles on the BF16 tensor cores, eight digit planes
-        launch_oz_xgroups(w_xp, nc, mu, w_gexp, st);
-        launch_phase1_oz(ozblk64_d.p, n_ozblk64_, ozseg64_d.p, 8, oza_d.p, ozoff_d.p, ozrexp_d.p, nullptr, w_xp, w_gexp, nullptr, mu, w_A, status_d.p, st);
-        launches_ += 2;
+        launch_oz_prepare(w_xp, nc, mu, 8, *w_oz, st);
+        launch_phase1_oz(ozblk64_d.p, n_ozblk64_, ozseg64_d.p, 8, oza_d.p, ozoff_d.p, ozrexp_d.p, nullptr, w_xp, *w_oz, nullptr, mu, w_A, status_d.p, st);
+        launches_ += 5;
     } else if (many) {
         launch_phase1_df_mrhs(p1_d.p, n_p1_dfma_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
         launch_phase1_df_mrhs(p1e_d.p, n_p1_emu_, lr_d.p, fac.p, w_xs, w_xexp, mu, w_A, st);
@@ -2045,7 +2072,7 @@ void HMatrix::profile(int mu, int reps, float *ms) {
     HTGPU_CUDA(cudaMemsetAsync(xstage.p, 0, sizeof(double) * (std::size_t)nc * mu, stream_));
     for (int r = 0; r < reps; r++) {
         HTGPU_CUDA(cudaEventRecord(ev[0], stream_));
-        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1, rhs_run(mu), ozg.p);
+        launch_product_with(xstage.p, ystage.p, mu, false, stream_, xp.p, xs.p, xexp.p, A.p, z.p, ev + 1, rhs_run(mu), oz_scratch(rhs_run(mu)));
         HTGPU_CUDA(cudaEventRecord(ev[4], stream_));
         HTGPU_CUDA(cudaEventSynchronize(ev[4]));
         float t;

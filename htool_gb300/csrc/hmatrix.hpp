@@ -309,9 +309,10 @@ class HMatrix {
     bool emu_ok_ = false;
     void launch_product(const double *x, double *y, int mu, int numbering, cudaStream_t st);
     // mu_run > mu: padded to that many right-hand sides (zero columns)
-    // w_gexp: scratch of the digit-plane phase 1 (none: that phase 1 is not used)
+    // w_oz: scratch of the digit-plane phase 1 (none: that phase 1 is not used)
     void launch_product_with(const double *x, double *y, int mu, int numbering, cudaStream_t st, double *w_xp, F2 *w_xs, int *w_xexp, double *w_A, double *w_z, cudaEvent_t *marks = nullptr,
-                             int mu_run = 0, int *w_gexp = nullptr);
+                             int mu_run = 0, const OzScratch *w_oz = nullptr);
+    const OzScratch *oz_scratch(int mu); // the H-matrix's own, when it holds mu right-hand sides
     void launch_sums(double *y, int mu, int numbering, const double *w_z, cudaStream_t st);
     void upload_phase1_lists();
     DevBuf<P1Item> p1e_d; // phase-1 tiles on the emulation (p1_d: on DFMA)
@@ -386,7 +387,11 @@ class HMatrix {
     DevBuf<unsigned char> oza_d;
     DevBuf<long long> ozoff_d;
     DevBuf<int> ozrexp_d;
-    DevBuf<int> ozg; // per product: the input's exponent groups (ceil(nc / 32) x mu)
+    DevBuf<int> ozg, ozc;     // per product: the input's exponents per 32-row group and per right-hand side (+ flag)
+    DevBuf<unsigned char> ozx; // and its digit planes
+    int ozx_mu_ = 0;           // right-hand sides the plane scratch holds
+    OzScratch ozs_{};
+    void ensure_oz_work(int mu);
     void build_oz_arena();
     long long oz_arena_need(); // bytes the planes of the current storage take
     void phase1_tc(const F2 *w_xs, int mu, double *w_A, cudaStream_t st); // the tcgen05 phase 1, from the arena when there is one

@@ -218,20 +218,27 @@ void launch_phase1_tc_pre(const TcBlock *blocks, int nblocks, const TcSeg *segs,
                           cudaStream_t st);
 // the stacked blocks on the BF16 tensor cores by exact digit slicing (oz.cu):
 // oz_arena_bytes fills ozoff_h (each block's byte offset in the digit-plane
-// arena, S planes of 8 KB per 32-row slab) and returns its size;
-// launch_oz_pack writes the planes and each block row's exponent (rexp,
-// 128 a block) from FP64 tiles (f64, element offsets in the segments) or
-// reduced ones (mix); launch_oz_xgroups writes the exponent maxima of the
-// gathered input per 32 rows and right-hand side (gexp, ceil(nrows / 32) x
-// mu); launch_phase1_oz writes the phase-1 sums, FP64 when scale is null,
-// else FP32 times the columns' scales in the units of the split input
-// (x 2^(1023 - *xexp)).  S = 8 (FP64-grade) or 4.
+// arena, S planes of 8 KB per 32-row slab, the slabs aligned to the input's
+// 32-row groups) and returns its size; launch_oz_pack writes the planes and
+// each block row's exponent (rexp, 128 a block) from FP64 tiles (f64,
+// element offsets in the segments) or reduced ones (mix).  Per product,
+// launch_oz_prepare writes the input's exponents (per 32-row group and
+// right-hand side, per right-hand side, a wide-input flag) and its digit
+// planes into the scratch; launch_phase1_oz then writes the phase-1 sums,
+// FP64 when scale is null, else FP32 times the columns' scales in the units
+// of the split input (x 2^(1023 - *xexp)).  S = 8 (FP64-grade) or 4.
+struct OzScratch {
+    int *gexp;              // ceil(nrows / 32) x mu
+    int *ecol;              // mu + 1: per right-hand side, then the wide flag
+    unsigned char *xplanes; // oz_xplanes_bytes
+};
 long long oz_arena_bytes(const TcBlock *blocks_h, int nblocks, int S, long long *ozoff_h);
+long long oz_xplanes_bytes(int nrows, int mu, int S);
 void launch_oz_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const double *f64, const unsigned char *mix, int S, const long long *ozoff, int *rexp, unsigned char *arena,
                     cudaStream_t st);
-void launch_oz_xgroups(const double *xp, int nrows, int mu, int *gexp, cudaStream_t st);
+void launch_oz_prepare(const double *xp, int nrows, int mu, int S, const OzScratch &sc, cudaStream_t st);
 void launch_phase1_oz(const TcBlock *blocks, int nblocks, const TcSeg *segs, int S, const unsigned char *arena, const long long *ozoff, const int *rexp, const float *scale, const double *xp,
-                      const int *gexp, const int *xexp, int mu, void *A, int *status, cudaStream_t st);
+                      const OzScratch &sc, const int *xexp, int mu, void *A, int *status, cudaStream_t st);
 // the same stacked blocks on the CUDA cores (mixed.cu), products with 3 or
 // more right-hand sides at any epsilon: one thread per stacked column, FP32
 // FMA, float sums into A

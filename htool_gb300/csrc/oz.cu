@@ -36,14 +36,18 @@
 // products of tc.cu whose FP32 tensor-core sums round.
 //
 // Data: the A digit planes are laid out once per H-matrix (oz_pack_kernel:
-// per block and 32-row slab, S planes of 128 x 32 BF16 in the canonical
-// no-swizzle K-major layout, 8 KB each, with each row's exponent beside),
-// brought into shared memory by one bulk copy per slab; the B planes are cut
-// by the threads from the FP64 gathered input, with exponents per group of
-// 32 x rows and right-hand side (oz_xgroup_kernel, once per product).  One
-// thread issues the MMAs (kind::f16, M 128, N 64, K 16) and commits each slab
-// to an mbarrier; every wait is bounded (status 4 on expiry, copies in flight
-// waited for, tensor memory freed).
+// per block and 16-row slab, S planes of 128 x 16 BF16 in the canonical
+// no-swizzle K-major layout, 4 KB each, with each row's exponent beside; the
+// slabs aligned to the input's 16-row groups).  Per product the input is
+// cut into planes once (oz_xplanes_kernel: per 16-row group and 64
+// right-hand sides, S planes of 2 KB, relative to each right-hand side's
+// maximum) and phase1_ozb_kernel brings both operands of every slab in by
+// bulk copies, four stages deep, one thread issuing the MMAs (kind::f16,
+// M 128, N 64, K 16), eight warps reading the accumulators out.  An input
+// with a 32-row group more than kOzWide binades below its right-hand side's
+// maximum takes phase1_oz_kernel instead, whose threads cut the input per
+// block relative to the block's own maxima.  Every wait is bounded (status 4
+// on expiry, copies in flight waited for, tensor memory freed).
 #include "df64.cuh"
 #include "kernels.hpp"
 #include "tcgen05.cuh"
@@ -55,21 +59,24 @@ namespace {
 using namespace tc5;
 
 constexpr int kOzThreads = 256;
-constexpr int kOzK       = 32;  // K rows per slab
+constexpr int kOzK       = 16;  // K rows per slab (one MMA)
 constexpr int kOzM       = 128; // stacked columns per block (MMA M)
 constexpr int kOzN       = 64;  // right-hand sides per pass (MMA N)
-constexpr int kOzPlaneA  = kOzM * kOzK * 2; // 8 KB: one BF16 digit plane of A
-constexpr int kOzPlaneB  = kOzN * kOzK * 2; // 4 KB: one of B
+constexpr int kOzPlaneA  = kOzM * kOzK * 2; // 4 KB: one BF16 digit plane of A
+constexpr int kOzPlaneB  = kOzN * kOzK * 2; // 2 KB: one of B
 constexpr int kOzLbo     = 128;             // bytes between core matrices along K (8 BF16 values)
 constexpr int kOzSbo     = (kOzK / 8) * 128; // bytes between 8-row groups
 
 template <int S>
 struct OzCfg {
     static constexpr int kT      = 6 + 7 * (S - 1);        // bits of the fixed-point values
-    static constexpr int kBuf    = S * (kOzPlaneA + kOzPlaneB); // one stage: A planes, B planes
-    static constexpr int kSmem   = 2 * kBuf + 128 + 4 * kOzN;   // two stages, barriers, exponents
-    static constexpr unsigned kCols = S * kOzN <= 256 ? (S * kOzN <= 128 ? 128u : 256u) : 512u; // a power of two
     static constexpr int kSlab   = S * kOzPlaneA;           // arena bytes per slab
+    static constexpr int kBslab  = S * kOzPlaneB;           // input plane bytes per slab
+    static constexpr int kBuf    = kSlab + kBslab;          // one stage: A planes, B planes
+    static constexpr int kSmem   = 2 * kBuf + 128 + 4 * kOzN; // staged kernel: two stages, barriers, exponents
+    static constexpr int kStages = 4;                        // plane kernel: stages in flight
+    static constexpr int kFastSmem = kStages * kBuf + 128;
+    static constexpr unsigned kCols = S * kOzN <= 256 ? (S * kOzN <= 128 ? 128u : 256u) : 512u; // a power of two
 };
 
 // instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits
@@ -274,53 +281,319 @@ __global__ void __launch_bounds__(kOzThreads) oz_pack_kernel(const TcBlock *__re
     const int emax = max(se[0][row], se[1][row]);
     if (half == 0)
         rexp[(long long)blockIdx.x * kOzM + row] = emax;
-    const int kh = half * 16;
-    for (int ks = 0, slab = 0; ks < B.jlen; ks += kOzK, slab++) {
+    // K index k of the planes is x row (xrow & ~15) + k: the slabs line up
+    // with the 16-row groups of the input's planes
+    const int kh = half * 8, off = B.xrow & (kOzK - 1);
+    for (int ks = 0, slab = 0; ks < off + B.jlen; ks += kOzK, slab++) {
         unsigned char *planes = arena + ozoff[blockIdx.x] + (long long)slab * OzCfg<S>::kSlab;
+        double v[8];
 #pragma unroll
-        for (int q8 = 0; q8 < 2; q8++) {
-            double v[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int j = ks + kh + 8 * q8 + q;
-                v[q]        = j < B.jlen ? oz_value(c64, c32, c16, j) : 0.;
-            }
-            oz_put8<S, OzCfg<S>::kT>(planes, kOzPlaneA, row, kh + 8 * q8, v, emax);
+        for (int q = 0; q < 8; q++) {
+            const int j = ks + kh + q - off;
+            v[q]        = (j >= 0 && j < B.jlen) ? oz_value(c64, c32, c16, j) : 0.;
         }
+        oz_put8<S, OzCfg<S>::kT>(planes, kOzPlaneA, row, kh, v, emax);
     }
 }
 
-// exponent field maxima of the gathered input per group of 32 rows and right-hand side
-__global__ void oz_xgroup_kernel(const double *__restrict__ xp, int nrows, int mu, int *__restrict__ gexp) {
+// exponent field maxima of the gathered input per group of 32 rows and
+// right-hand side; the wide-input flag ecol[mu] cleared
+__global__ void oz_xgroup_kernel(const double *__restrict__ xp, int nrows, int mu, int *__restrict__ gexp, int *__restrict__ ecol) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int ng      = (nrows + 31) >> 5;
+    if (t == 0)
+        ecol[mu] = 0;
+    const int ng = (nrows + 31) >> 5;
     if (t >= (long long)ng * mu)
         return;
     const int g = (int)(t / mu), c = (int)(t - (long long)g * mu);
-    int e       = 0;
+    int e        = 0;
     const int j1 = min(nrows, 32 * g + 32);
     for (int j = 32 * g; j < j1; j++)
         e = max(e, oz_ebits(xp[(long long)j * mu + c]));
     gexp[t] = e;
 }
 
-// Eight warps; thread t cuts 8 K values of right-hand side t mod 64 into
-// digit planes; thread 0 issues the copies and the MMAs.  OUT64: FP64 sums
-// (FP64 storage); else FP32 sums times the columns' scales.
+// Inputs with a group of 32 rows whose largest value is more than this many
+// binades below its right-hand side's maximum take the staged kernel
+// (exponents per block); the others are cut into planes once, relative to
+// each right-hand side's maximum, and keep at least T - kOzWide bits.
+constexpr int kOzWide = 10;
+
+// each right-hand side's exponent maximum (one CTA per right-hand side),
+// then the wide-input flag
+__global__ void oz_xcol_kernel(const int *__restrict__ gexp, int ng, int mu, int *__restrict__ ecol) {
+    __shared__ int red[8];
+    __shared__ int emax;
+    const int c = blockIdx.x;
+    int e       = 0;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x)
+        e = max(e, gexp[(long long)g * mu + c]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            e = max(e, red[w]);
+        e       = max(e, red[0]);
+        ecol[c] = e;
+        emax    = e;
+    }
+    __syncthreads();
+    bool wide = false;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const int eg = gexp[(long long)g * mu + c];
+        wide |= eg > 0 && emax - eg > kOzWide;
+    }
+    if (__syncthreads_or(wide) && threadIdx.x == 0)
+        atomicOr(&ecol[mu], 1);
+}
+
+// the input cut into digit planes once per product: for 16-row group g
+// (blockIdx.x) and pass p of 64 right-hand sides (blockIdx.y), S planes of
+// 64 x 16 BF16 in the canonical layout (S x 2 KB, contiguous), relative to
+// each right-hand side's maximum
+template <int S>
+__global__ void __launch_bounds__(128) oz_xplanes_kernel(const double *__restrict__ xp, int nrows, int mu, const int *__restrict__ ecol, unsigned char *__restrict__ xplanes) {
+    const int g = blockIdx.x, p = blockIdx.y, npass = gridDim.y;
+    const int n = threadIdx.x & 63, k0 = (threadIdx.x >> 6) * 8, c = kOzN * p + n;
+    const bool on = c < mu;
+    const int e   = on ? ecol[c] : 0;
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int j = kOzK * g + k0 + q;
+        v[q]        = (on && j < nrows) ? xp[(long long)j * mu + c] : 0.;
+    }
+    oz_put8<S, OzCfg<S>::kT>(xplanes + ((long long)g * npass + p) * OzCfg<S>::kBslab, kOzPlaneB, n, k0, v, e);
+}
+
+// Warp-specialised phase 1 for inputs cut into planes once.  One thread of
+// warp 0 runs ahead issuing, per 16-row slab, the bulk copies of the block's
+// A planes and of the input group's B planes into a ring of four stages,
+// and, as the slabs land, their MMAs; warps 1-8 read the accumulators out
+// after the last slab of each block and pass (tensor-memory lanes 32 (warp
+// mod 4) .., warps 1-4 the first 32 right-hand sides, 5-8 the last 32),
+// while the next block's copies already fly.
+constexpr int kOzFastThreads = 288;
+
+template <int S, bool OUT64>
+__global__ void __launch_bounds__(kOzFastThreads, 1) phase1_ozb_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs,
+                                                                       const unsigned char *__restrict__ arena, const long long *__restrict__ ozoff, const int *__restrict__ rexp,
+                                                                       const float *__restrict__ scale, const unsigned char *__restrict__ xplanes, const int *__restrict__ ecol,
+                                                                       const int *__restrict__ xexp, int mu, void *__restrict__ Aout, int *__restrict__ status) {
+    using C           = OzCfg<S>;
+    constexpr int T   = C::kT;
+    constexpr int NST = C::kStages;
+    if (ecol[mu] != 0) // a wide input: the staged kernel takes it
+        return;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *full  = reinterpret_cast<unsigned long long *>(smem + NST * C::kBuf); // [NST] a stage's planes landed
+    unsigned long long *empty = full + NST;                                                   // [NST] a stage's MMAs done
+    unsigned long long *accf  = full + 2 * NST;                                               // a pass's accumulators complete
+    unsigned long long *acce  = accf + 1;                                                     // and read out
+    unsigned *tslot           = reinterpret_cast<unsigned *>(smem + NST * C::kBuf + 96);
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const int npass = (mu + kOzN - 1) / kOzN;
+    if (tid == 0) {
+        for (int k = 0; k < NST; k++) {
+            bar_init(&full[k]);
+            bar_init(&empty[k]);
+        }
+        bar_init(accf);
+        bar_init_n(acce, 8); // one arrival per read-out warp
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot, C::kCols);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tmem = *tslot;
+    bool fail           = false;
+    if (wid == 0) {
+        if (lane == 0) {
+            // two cursors over (block, pass, slab): copies run up to NST
+            // slabs ahead of the MMAs
+            struct Cursor {
+                int bi, p, s, nsl, g0;
+                long long aoff;
+            };
+            auto load = [&](Cursor &c) {
+                if (c.bi < nblocks) {
+                    const TcBlock B = blocks[c.bi];
+                    c.nsl           = ((B.xrow & (kOzK - 1)) + B.jlen + kOzK - 1) / kOzK;
+                    c.g0            = B.xrow / kOzK;
+                    c.aoff          = ozoff[c.bi];
+                }
+            };
+            auto advance = [&](Cursor &c) {
+                if (++c.s == c.nsl) {
+                    c.s = 0;
+                    if (++c.p == npass) {
+                        c.p = 0;
+                        c.bi += gridDim.x;
+                        load(c);
+                    }
+                }
+            };
+            Cursor cc{(int)blockIdx.x, 0, 0, 0, 0, 0};
+            load(cc);
+            Cursor mc = cc;
+            int ci = 0, mi = 0, np = 0; // copies issued, slabs multiplied, passes completed
+            while (mc.bi < nblocks && !fail) {
+                while (cc.bi < nblocks && ci < mi + NST) {
+                    const int stg = ci % NST, use = ci / NST;
+                    if (use > 0 && !bar_wait(&empty[stg], (use - 1) & 1)) { // the MMAs of slab ci - NST read this stage
+                        fail = true;
+                        break;
+                    }
+                    unsigned char *stage = smem + (size_t)stg * C::kBuf;
+                    bar_expect_tx(&full[stg], C::kBuf);
+                    bulk_g2s(stage, arena + cc.aoff + (long long)cc.s * C::kSlab, C::kSlab, &full[stg]);
+                    bulk_g2s(stage + C::kSlab, xplanes + ((long long)(cc.g0 + cc.s) * npass + cc.p) * C::kBslab, C::kBslab, &full[stg]);
+                    ci++;
+                    advance(cc);
+                }
+                if (fail)
+                    break;
+                const int stg = mi % NST, use = mi / NST;
+                // the read-out of the previous pass is done with the accumulators
+                if (mc.s == 0 && np > 0 && !bar_wait(acce, (np - 1) & 1)) {
+                    fail = true;
+                    break;
+                }
+                if (!bar_wait(&full[stg], use & 1)) {
+                    fail = true;
+                    break;
+                }
+                fence_after();
+                const unsigned a0 = smem_u32(smem + (size_t)stg * C::kBuf), b0 = a0 + C::kSlab;
+#pragma unroll
+                for (int D = 0; D < S; D++)
+#pragma unroll
+                    for (int i = 0; i <= D; i++)
+                        oz_mma(tmem + (unsigned)(D * kOzN), oz_desc(a0 + i * kOzPlaneA), oz_desc(b0 + (D - i) * kOzPlaneB), !(mc.s == 0 && i == 0));
+                commit(&empty[stg]);
+                mi++;
+                const bool last = mc.s == mc.nsl - 1;
+                advance(mc);
+                if (last) {
+                    commit(accf);
+                    np++;
+                }
+            }
+            if (fail) {
+                atomicExch(status, 4);
+                for (int k = mi; k < ci; k++) // the copies in flight land before the CTA leaves
+                    bar_wait(&full[k % NST], (k / NST) & 1);
+            }
+        }
+    } else {
+        const int orow = 32 * (wid & 3) + lane, c0 = 32 * ((wid - 1) >> 2);
+        const int kunits = OUT64 ? 0 : 1023 - max(*xexp, 1); // FP32 sums in the units of the split input
+        int np = 0;
+        for (int bi = blockIdx.x; bi < nblocks && !fail; bi += gridDim.x) {
+            const TcBlock B = blocks[bi];
+            int osg = -1, om0 = 0;
+            for (int s2 = B.s0; s2 < B.s1; s2++) {
+                const int nc = segs[s2].ncol;
+                if (orow < om0 + nc) {
+                    osg = s2;
+                    break;
+                }
+                om0 += nc;
+            }
+            long long oo = 0;
+            float osc    = 1.f;
+            if (osg >= 0) {
+                oo = (segs[osg].slot + (long long)(orow - om0)) * mu;
+                if (!OUT64)
+                    osc = scale[segs[osg].sidx + orow - om0];
+            }
+            const int kr = 7 * (S - 1) + rexp[(long long)bi * kOzM + orow] - 2044 - 2 * T + kunits;
+            for (int p = 0; p < npass; p++) {
+                if (!bar_wait(accf, np & 1)) {
+                    fail = true;
+                    break;
+                }
+                fence_after();
+                // the accumulators out of tensor memory first, into two exact
+                // 64-bit partial sums per column (diagonals D < S/2 and the
+                // rest: I = hi 2^(7 S/2) + lo); tensor memory is released
+                // before the conversions, so the next block's MMAs overlap them
+                long long hi[32], lo[32];
+#pragma unroll
+                for (int q = 0; q < 32; q++)
+                    hi[q] = lo[q] = 0;
+#pragma unroll
+                for (int D = 0; D < S; D++)
+#pragma unroll
+                    for (int c16 = 0; c16 < 2; c16++) {
+                        unsigned r[16];
+                        tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + (unsigned)(D * kOzN + c0 + 16 * c16), r);
+#pragma unroll
+                        for (int q = 0; q < 16; q++) {
+                            const long long a = (long long)__float2int_rn(__uint_as_float(r[q]));
+                            if (D < S / 2)
+                                hi[16 * c16 + q] += a << (7 * (S / 2 - 1 - D));
+                            else
+                                lo[16 * c16 + q] += a << (7 * (S - 1 - D));
+                        }
+                    }
+                fence_before();
+                __syncwarp();
+                if (lane == 0)
+                    bar_arrive(acce);
+                if (osg >= 0)
+#pragma unroll
+                    for (int q = 0; q < 32; q++) {
+                        const int c = kOzN * p + c0 + q;
+                        if (c < mu) {
+                            const __int128 I = ((__int128)hi[q] << (7 * (S / 2))) + lo[q];
+                            if (OUT64)
+                                reinterpret_cast<double *>(Aout)[oo + c] = oz_i2d(I, kr + __ldg(ecol + c));
+                            else
+                                reinterpret_cast<float *>(Aout)[oo + c] = oz_i2f(I, kr + __ldg(ecol + c)) * osc;
+                        }
+                    }
+                np++;
+            }
+        }
+        if (fail && lane == 0)
+            atomicExch(status, 4);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (wid == 0)
+        tmem_free(tmem, C::kCols);
+}
+
+// The staged kernel, for wide inputs: exponents per block and right-hand
+// side (from the 32-row group maxima), eight warps; threads 0-127 cut 8 K
+// values of right-hand side t mod 64 into digit planes each slab, thread 0
+// issues the A copy and the MMAs.  OUT64: FP64 sums (FP64 storage); else
+// FP32 sums times the columns' scales.
 template <int S, bool OUT64>
 __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(const TcBlock *__restrict__ blocks, int nblocks, const TcSeg *__restrict__ segs, const unsigned char *__restrict__ arena,
                                                                   const long long *__restrict__ ozoff, const int *__restrict__ rexp, const float *__restrict__ scale,
-                                                                  const double *__restrict__ xp, const int *__restrict__ gexp, const int *__restrict__ xexp, int mu, void *__restrict__ Aout,
-                                                                  int *__restrict__ status) {
+                                                                  const double *__restrict__ xp, const int *__restrict__ gexp, const int *__restrict__ ecol, const int *__restrict__ xexp, int mu,
+                                                                  void *__restrict__ Aout, int *__restrict__ status) {
     using C = OzCfg<S>;
     constexpr int T = C::kT;
+    if (ecol[mu] == 0) // not a wide input: the plane kernel took it
+        return;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned long long *bars  = reinterpret_cast<unsigned long long *>(smem + 2 * C::kBuf);      // products of a stage done
     unsigned long long *fulls = reinterpret_cast<unsigned long long *>(smem + 2 * C::kBuf + 16); // a stage's A planes landed
     unsigned *tslot           = reinterpret_cast<unsigned *>(smem + 2 * C::kBuf + 64);
     int *sE                   = reinterpret_cast<int *>(smem + 2 * C::kBuf + 128); // the pass's right-hand-side exponents
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-    const int bn = tid & 63, bk = (tid >> 6) * 8; // B: right-hand side and first K value
+    const int bn = tid & 63, bk = ((tid >> 6) & 1) * 8; // B: right-hand side and first K value
+    const bool stager = tid < 2 * kOzN;
     if (tid == 0) {
         bar_init(&bars[0]);
         bar_init(&bars[1]);
@@ -341,11 +614,12 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
     bool fail  = false;
     for (int bi = blockIdx.x; bi < nblocks && !fail; bi += gridDim.x) {
         const TcBlock B = blocks[bi];
-        const double *X = xp + (long long)B.xrow * mu;
+        const int off   = B.xrow & (kOzK - 1), kend = off + B.jlen; // K index k is x row (xrow & ~15) + k
+        const double *X = xp + (long long)(B.xrow - off) * mu;
         const unsigned char *ablk = arena + ozoff[bi];
         const int g0 = B.xrow >> 5, g1 = (B.xrow + B.jlen - 1) >> 5;
         for (int cb = 0; cb < mu && !fail; cb += kOzN) {
-            const bool on = cb + bn < mu;
+            const bool on = stager && cb + bn < mu;
             int eb        = 0; // exponent of this thread's right-hand side over the block's rows
             if (on)
                 for (int g = g0; g <= g1; g++)
@@ -357,11 +631,11 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
                     const int j = ks + bk + q;
-                    b[q]        = (on && j < B.jlen) ? X[(long long)j * mu + cb + bn] : 0.;
+                    b[q]        = (on && j >= off && j < kend) ? X[(long long)j * mu + cb + bn] : 0.;
                 }
             };
             loadb(0);
-            for (int ks = 0; ks < B.jlen; ks += kOzK) {
+            for (int ks = 0; ks < kend; ks += kOzK) {
                 const int buf = slabs & 1, use = slabs >> 1;
                 unsigned char *stage = smem + (size_t)buf * C::kBuf;
                 if (use > 0 && !bar_wait(&bars[buf], (use - 1) & 1)) // the products of two slabs ago read this stage
@@ -375,9 +649,11 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
                     bulk_g2s(stage, ablk + (long long)(ks / kOzK) * C::kSlab, C::kSlab, &fulls[buf]);
                     copies++;
                 }
-                oz_put8<S, T>(stage + S * kOzPlaneA, kOzPlaneB, bn, bk, b, eb);
-                if (ks + kOzK < B.jlen) // the next slab's x values fly while this one is multiplied
-                    loadb(ks + kOzK);
+                if (stager) {
+                    oz_put8<S, T>(stage + S * kOzPlaneA, kOzPlaneB, bn, bk, b, eb);
+                    if (ks + kOzK < kend) // the next slab's x values fly while this one is multiplied
+                        loadb(ks + kOzK);
+                }
                 proxy_fence();
                 __syncthreads();
                 if (tid == 0) {
@@ -484,21 +760,30 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
         tmem_free(tmem, C::kCols);
 }
 
+template <typename K>
+void oz_smem_attr(K kernel, int bytes) {
+    HTGPU_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
 template <int S, bool OUT64>
-void oz_launch(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *arena, const long long *ozoff, const int *rexp, const float *scale, const double *xp, const int *gexp,
+void oz_launch(const TcBlock *blocks, int nblocks, const TcSeg *segs, const unsigned char *arena, const long long *ozoff, const int *rexp, const float *scale, const double *xp, const OzScratch &sc,
                const int *xexp, int mu, void *A, int *status, cudaStream_t st) {
     static unsigned long long done = 0;
     int dev = 0, sms = 0;
     HTGPU_CUDA(cudaGetDevice(&dev));
+    using C = OzCfg<S>;
     if (dev >= 64 || !(done >> dev & 1)) {
-        HTGPU_CUDA(cudaFuncSetAttribute(phase1_oz_kernel<S, OUT64>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzCfg<S>::kSmem));
+        oz_smem_attr(phase1_oz_kernel<S, OUT64>, C::kSmem);
+        oz_smem_attr(phase1_ozb_kernel<S, OUT64>, C::kFastSmem);
         if (dev < 64)
             done |= 1ull << dev;
     }
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int per_sm = OzCfg<S>::kSmem * 2 <= 227 * 1024 ? 2 : 1;
-    const int grid   = std::min(nblocks, per_sm * sms);
-    phase1_oz_kernel<S, OUT64><<<grid, kOzThreads, OzCfg<S>::kSmem, st>>>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status);
+    // one of the two does the work: the plane kernel unless the input is wide
+    phase1_ozb_kernel<S, OUT64><<<std::min(nblocks, sms), kOzFastThreads, C::kFastSmem, st>>>(blocks, nblocks, segs, arena, ozoff, rexp, scale, sc.xplanes, sc.ecol, xexp, mu, A, status);
+    HTGPU_CUDA(cudaGetLastError());
+    const int per_sm = C::kSmem * 2 <= 227 * 1024 ? 2 : 1;
+    phase1_oz_kernel<S, OUT64><<<std::min(nblocks, per_sm * sms), kOzThreads, C::kSmem, st>>>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, sc.gexp, sc.ecol, xexp, mu, A, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 
@@ -508,10 +793,12 @@ long long oz_arena_bytes(const TcBlock *blocks_h, int nblocks, int S, long long 
     long long off = 0;
     for (int b = 0; b < nblocks; b++) {
         ozoff_h[b] = off;
-        off += (long long)((blocks_h[b].jlen + kOzK - 1) / kOzK) * S * kOzPlaneA;
+        off += (long long)(((blocks_h[b].xrow & (kOzK - 1)) + blocks_h[b].jlen + kOzK - 1) / kOzK) * S * kOzPlaneA;
     }
     return off;
 }
+
+long long oz_xplanes_bytes(int nrows, int mu, int S) { return (long long)((nrows + kOzK - 1) / kOzK) * ((mu + kOzN - 1) / kOzN) * S * kOzPlaneB; }
 
 void launch_oz_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const double *f64, const unsigned char *mix, int S, const long long *ozoff, int *rexp, unsigned char *arena,
                     cudaStream_t st) {
@@ -527,28 +814,39 @@ void launch_oz_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const
     HTGPU_CUDA(cudaGetLastError());
 }
 
-void launch_oz_xgroups(const double *xp, int nrows, int mu, int *gexp, cudaStream_t st) {
-    const long long n = (long long)((nrows + 31) >> 5) * mu;
-    if (n <= 0)
+void launch_oz_prepare(const double *xp, int nrows, int mu, int S, const OzScratch &sc, cudaStream_t st) {
+    const int ng = (nrows + 31) >> 5;
+    if (ng <= 0 || mu <= 0)
         return;
-    oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xp, nrows, mu, gexp);
+    const long long n = (long long)ng * mu;
+    oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xp, nrows, mu, sc.gexp, sc.ecol);
+    HTGPU_CUDA(cudaGetLastError());
+    oz_xcol_kernel<<<mu, 256, 0, st>>>(sc.gexp, ng, mu, sc.ecol);
+    HTGPU_CUDA(cudaGetLastError());
+    const dim3 grid((nrows + kOzK - 1) / kOzK, (mu + kOzN - 1) / kOzN);
+    if (S == 8)
+        oz_xplanes_kernel<8><<<grid, 128, 0, st>>>(xp, nrows, mu, sc.ecol, sc.xplanes);
+    else if (S == 4)
+        oz_xplanes_kernel<4><<<grid, 128, 0, st>>>(xp, nrows, mu, sc.ecol, sc.xplanes);
+    else
+        throw Error(1, "[Htool error] digit planes: S must be 4 or 8");
     HTGPU_CUDA(cudaGetLastError());
 }
 
 void launch_phase1_oz(const TcBlock *blocks, int nblocks, const TcSeg *segs, int S, const unsigned char *arena, const long long *ozoff, const int *rexp, const float *scale, const double *xp,
-                      const int *gexp, const int *xexp, int mu, void *A, int *status, cudaStream_t st) {
+                      const OzScratch &sc, const int *xexp, int mu, void *A, int *status, cudaStream_t st) {
     if (scale && !xexp)
         throw Error(1, "[Htool error] digit planes: FP32 sums need the input's exponent");
     if (nblocks <= 0)
         return;
     if (S == 8 && !scale)
-        oz_launch<8, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+        oz_launch<8, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, sc, xexp, mu, A, status, st);
     else if (S == 4 && scale)
-        oz_launch<4, false>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+        oz_launch<4, false>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, sc, xexp, mu, A, status, st);
     else if (S == 8)
-        oz_launch<8, false>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+        oz_launch<8, false>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, sc, xexp, mu, A, status, st);
     else if (S == 4)
-        oz_launch<4, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, gexp, xexp, mu, A, status, st);
+        oz_launch<4, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, sc, xexp, mu, A, status, st);
     else
         throw Error(1, "[Htool error] digit planes: S must be 4 or 8");
 }

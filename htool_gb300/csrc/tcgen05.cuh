@@ -18,6 +18,9 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void bar_init(unsigned long long *b) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory"); }
+// a barrier whose phase completes after `count` arrivals
+__device__ __forceinline__ void bar_init_n(unsigned long long *b, unsigned count) { asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory"); }
+__device__ __forceinline__ void bar_arrive(unsigned long long *b) { asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory"); }
 
 // bounded wait for the completion of the phase of parity `parity`
 __device__ __forceinline__ bool bar_wait(unsigned long long *b, unsigned parity) {

@@ -429,8 +429,9 @@ int htgpu_debug_tc_gemm(int device, const float *a, const float *b, float *d);
  * `device` by the digit-plane path of the tensor-core phase 1 (the FP64
  * products cut into S = 8 or 4 BF16 digit planes, exact MMA sums, integer
  * read-out): one stacked block through the plane packing, the input's
- * exponent groups and the phase-1 kernel. */
-int htgpu_debug_oz_gemm(int device, int S, int K, int mu, const double *a, const double *b, double *d);
+ * exponents and planes and the phase-1 kernel -- the one for inputs cut into
+ * planes once, or (staged != 0) the one of wide inputs. */
+int htgpu_debug_oz_gemm(int device, int S, int K, int mu, int staged, const double *a, const double *b, double *d);
 
 /* Status word of the product kernels' bounded waits: 0, or 1/2/3 when a
  * wait for a pipeline stage ran out, 4 when a wait of the tensor-core

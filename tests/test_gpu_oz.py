@@ -53,29 +53,30 @@ def model(a, b, S):
     return np.vectorize(lambda i, kk: float(i) * 2.0 ** int(kk))(acc, k).astype(np.float64)
 
 
-def oz_gemm(a, b, S):
+def oz_gemm(a, b, S, staged=False):
     a = np.ascontiguousarray(a, dtype=np.float64)
     b = np.ascontiguousarray(b, dtype=np.float64)
     K, mu = b.shape
     assert a.shape == (128, K)
     d = np.empty((128, mu), np.float64)
-    H._check(H.lib.htgpu_debug_oz_gemm(0, S, K, mu, H._ptr(a), H._ptr(b), H._ptr(d)))
+    H._check(H.lib.htgpu_debug_oz_gemm(0, S, K, mu, int(staged), H._ptr(a), H._ptr(b), H._ptr(d)))
     return d
 
 
+@pytest.mark.parametrize("staged", [False, True])
 @pytest.mark.parametrize("S", [8, 4])
-def test_integer_operands_exact(S):
+def test_integer_operands_exact(S, staged):
     rng = np.random.default_rng(11)
     a = rng.integers(-1000, 1001, (128, 256)).astype(np.float64)
     b = rng.integers(-1000, 1001, (256, 64)).astype(np.float64)
-    d = oz_gemm(a, b, S)
+    d = oz_gemm(a, b, S, staged)
     ref = a.astype(np.int64) @ b.astype(np.int64)
     assert np.array_equal(d, ref.astype(np.float64))
     # a single 1 per row picks one row of b: the layout of both operands
     e = np.zeros((128, 32))
     e[np.arange(128), (7 * np.arange(128)) % 32] = 1.0
     bb = np.arange(32 * 64, dtype=np.float64).reshape(32, 64) - 1000.0
-    assert np.array_equal(oz_gemm(e, bb, S), e @ bb)
+    assert np.array_equal(oz_gemm(e, bb, S, staged), e @ bb)
 
 
 @pytest.mark.parametrize("S,bits", [(8, 55), (4, 27)])
@@ -100,15 +101,17 @@ def test_fp64_operands_within_bound(S, bits, K, mu):
         assert np.linalg.norm(d - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("staged", [False, True])
 @pytest.mark.parametrize("S", [8, 4])
-def test_matches_integer_model_bitwise(S):
-    """the kernel computes the scheme exactly as stated: bit for bit the
-    numpy restatement (ragged K, two passes of right-hand sides)"""
+def test_matches_integer_model_bitwise(S, staged):
+    """both kernels compute the scheme exactly as stated: bit for bit the
+    numpy restatement (ragged K, two passes of right-hand sides; one block,
+    so the staged kernel's per-block exponents are the columns' maxima)"""
     rng = np.random.default_rng(70 + S)
     K, mu = 77, 100
     a = rng.standard_normal((128, K)) * np.exp2(rng.integers(-12, 12, (128, K)))
     b = rng.standard_normal((K, mu)) * np.exp2(rng.integers(-12, 12, (1, mu)))
-    assert np.array_equal(oz_gemm(a, b, S), model(a, b, S))
+    assert np.array_equal(oz_gemm(a, b, S, staged), model(a, b, S))
 
 
 def rel(a, b):
@@ -132,11 +135,20 @@ def test_hmatrix_fp64_digit_planes(golden):
     assert hm.get_digit_planes() == (False, 0)
     hm.set_digit_planes(True)
     on, nbytes = hm.get_digit_planes()
-    assert on and nbytes > 0 and nbytes % 65536 == 0  # 8 planes of 8 KB a slab
+    assert on and nbytes > 0 and nbytes % 32768 == 0  # 8 planes of 4 KB a slab
     for mu in X:
         y = hm.mvprod_global_to_global(X[mu], mu)
         assert rel(y, base[mu]) < 1e-13, mu
         assert np.array_equal(y, hm.mvprod_global_to_global(X[mu], mu))  # repeatable
+    # a wide input (a quarter of the rows 1e-9 of the rest) takes the staged
+    # kernel, with exponents per block
+    xw = X[16].copy().reshape(16, n)
+    xw[:, : n // 4] *= 1e-9
+    xw = xw.reshape(-1)
+    hm.set_digit_planes(False)
+    yw = hm.mvprod_global_to_global(xw, 16)
+    hm.set_digit_planes(True)
+    assert rel(hm.mvprod_global_to_global(xw, 16), yw) < 1e-13
     y16 = hm.mvprod_global_to_global(X[16], 16)
     ones = np.concatenate([hm.mvprod_global_to_global(X[16][c * n:(c + 1) * n].copy(), 1) for c in range(16)])
     assert rel(y16, ones) < 1e-13
@@ -147,7 +159,7 @@ def test_hmatrix_fp64_digit_planes(golden):
     assert hm.device_status() == 0
     hm.set_precision("mixed")  # four planes of the reduced factors
     on, nb4 = hm.get_digit_planes()
-    assert on and nb4 > 0 and nb4 % 32768 == 0
+    assert on and nb4 > 0 and nb4 % 16384 == 0
     hm.set_precision("fp64")
     assert hm.get_digit_planes()[1] == nbytes
     hm.set_digit_planes(False)
