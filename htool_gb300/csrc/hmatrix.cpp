@@ -1594,14 +1594,20 @@ void HMatrix::set_tensor_core_arena(bool on) {
 
 long long HMatrix::oz_arena_need() {
     std::vector<TcBlock> blks;
+    long long panels = 0;
     if (precision_ == 0) {
         std::vector<TcSeg> segs;
         stack_tiles(p1_h, lr_h, segs, blks);
+        std::vector<OzPanel> pans;
+        for (const PanelItem &pi : pan_h)
+            pans.push_back(OzPanel{pi.off, 0, pi.row0, pi.h, pi.q0, pi.ncol});
+        std::vector<long long> poff(pans.size());
+        panels = oz_panel_bytes(pans.data(), (int)pans.size(), 8, poff.data());
     } else {
         blks = tcblk_h_;
     }
     std::vector<long long> off(blks.size());
-    return oz_arena_bytes(blks.data(), (int)blks.size(), precision_ == 0 ? 8 : 4, off.data());
+    return oz_arena_bytes(blks.data(), (int)blks.size(), precision_ == 0 ? 8 : 4, off.data()) + panels;
 }
 
 void HMatrix::build_oz_arena() {
@@ -1610,7 +1616,12 @@ void HMatrix::build_oz_arena() {
     ozrexp_d.release();
     ozseg64_d.release();
     ozblk64_d.release();
+    ozpan_d.release();
+    ozpa_d.release();
+    ozprexp_d.release();
+    ozgrp_d.release();
     n_ozblk64_ = 0;
+    n_ozpan_   = 0;
     oz_S_      = 0;
     if (!oz_on_ || !fac.p)
         return;
@@ -1641,6 +1652,41 @@ void HMatrix::build_oz_arena() {
     ozrexp_d.alloc(blks.size() * 128);
     oza_d.alloc(bytes);
     launch_oz_pack(bd, (int)blks.size(), sd, precision_ == 0 ? fac.p : nullptr, precision_ == 0 ? nullptr : mix_.p, S, ozoff_d.p, ozrexp_d.p, oza_d.p, stream_);
+    if (precision_ == 0 && !pan_h.empty()) {
+        // phase 2: every row chunk's panel, the widest first
+        std::vector<OzPanel> pans;
+        pans.reserve(pan_h.size());
+        for (const PanelItem &pi : pan_h)
+            if (pi.ncol > 0)
+                pans.push_back(OzPanel{pi.off, 0, pi.row0, pi.h, pi.q0, pi.ncol, 0, 0});
+        std::stable_sort(pans.begin(), pans.end(), [](const OzPanel &a, const OzPanel &b) { return a.ncol > b.ncol; });
+        std::vector<long long> poff(pans.size());
+        const long long pbytes = oz_panel_bytes(pans.data(), (int)pans.size(), 8, poff.data());
+        // each panel's exponent groups: the 32-slot groups of its phase-1
+        // sums (g) and the 32-row groups of its input rows (-1 - g)
+        std::vector<int> grp;
+        for (std::size_t q = 0; q < pans.size(); q++) {
+            pans[q].poff = poff[q];
+            std::vector<int> gs;
+            gs.reserve(pans[q].ncol);
+            for (int c = 0; c < pans[q].ncol; c++) {
+                const int kx = cidx_h[(std::size_t)pans[q].q0 + c];
+                gs.push_back(kx >= 0 ? kx >> 5 : -1 - ((~kx) >> 5));
+            }
+            std::sort(gs.begin(), gs.end());
+            gs.erase(std::unique(gs.begin(), gs.end()), gs.end());
+            pans[q].gofs = (int)grp.size();
+            pans[q].ngrp = (int)gs.size();
+            grp.insert(grp.end(), gs.begin(), gs.end());
+        }
+        grp.push_back(0);
+        ozgrp_d.upload(grp, stream_);
+        ozpan_d.upload(pans, stream_);
+        ozprexp_d.alloc(pans.size() * 32);
+        ozpa_d.alloc(pbytes);
+        n_ozpan_ = (int)pans.size();
+        launch_oz_panel_pack(ozpan_d.p, n_ozpan_, fac.p, ozprexp_d.p, ozpa_d.p, stream_);
+    }
     HTGPU_CUDA(cudaStreamSynchronize(stream_));
     oz_S_ = S;
 }
@@ -1660,6 +1706,8 @@ void HMatrix::ensure_oz_work(int mu) {
         ozg.release();
         ozc.release();
         ozx.release();
+        ozag.release();
+        ozpe.release();
         ozx_mu_ = 0;
         return;
     }
@@ -1669,13 +1717,15 @@ void HMatrix::ensure_oz_work(int mu) {
     ozg.alloc((std::size_t)((nc + 31) / 32) * mu + 1);
     ozc.alloc((std::size_t)mu + 1);
     ozx.alloc((std::size_t)oz_xplanes_bytes(nc, mu, 8));
+    ozag.alloc((std::size_t)((a_slots + 31) / 32) * mu + 1);
+    ozpe.alloc((std::size_t)std::max<std::size_t>(pan_h.size(), 1) * mu);
     ozx_mu_ = mu;
 }
 
 const OzScratch *HMatrix::oz_scratch(int mu) {
     if (!oz_on_ || mu > ozx_mu_ || !ozx.p)
         return nullptr;
-    ozs_ = OzScratch{ozg.p, ozc.p, ozx.p};
+    ozs_ = OzScratch{ozg.p, ozc.p, ozx.p, ozag.p, ozpe.p};
     return &ozs_;
 }
 
@@ -1809,7 +1859,11 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
     {
         const unsigned char *arena = reinterpret_cast<const unsigned char *>(fac.p);
         const unsigned char *pre   = reinterpret_cast<const unsigned char *>(emu2_.p); // kStreamPre chunks
-        if (many) {
+        if (many && oz_S_ == 8 && w_oz && n_ozpan_ > 0) {
+            // the panels on the BF16 tensor cores
+            launch_phase2_oz(ozpan_d.p, n_ozpan_, ozgrp_d.p, ozpa_d.p, ozprexp_d.p, cidx_d.p, w_A, (int)a_slots, w_xp, *w_oz, mu, w_z, (int)zlen_, status_d.p, st);
+            launches_ += 2;
+        } else if (many) {
             launch_phase2_df_mrhs(sc_d.p, p2rc_d.p, n_p2rc_, arena, pre, cidx_d.p, w_A, w_xs, w_xexp, mu, w_z, (int)zlen_, false, st);
             launches_ += 1;
         } else if (p2_mode_ == 1) {

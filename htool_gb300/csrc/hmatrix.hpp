@@ -208,7 +208,7 @@ class HMatrix {
     // (digit_plane_bytes); off by default, autotuned
     void set_digit_planes(bool on);
     bool digit_planes() const { return oz_on_; }
-    long long digit_plane_bytes() const { return (long long)oza_d.n; }
+    long long digit_plane_bytes() const { return (long long)(oza_d.n + ozpa_d.n); }
     // right-hand-side buckets: a product with mu right-hand sides (1 to 8)
     // runs padded with zero columns to mu_run (one pass over the factors
     // instead of one per group of 4, 2, 1); 0 runs it unpadded.  The
@@ -387,7 +387,13 @@ class HMatrix {
     DevBuf<unsigned char> oza_d;
     DevBuf<long long> ozoff_d;
     DevBuf<int> ozrexp_d;
+    DevBuf<OzPanel> ozpan_d; // FP64 phase 2: the row chunks' panels, their planes and row exponents
+    DevBuf<unsigned char> ozpa_d;
+    DevBuf<int> ozprexp_d;
+    DevBuf<int> ozgrp_d; // the panels' exponent groups
+    int n_ozpan_ = 0;
     DevBuf<int> ozg, ozc;     // per product: the input's exponents per 32-row group and per right-hand side (+ flag)
+    DevBuf<int> ozag, ozpe;   // and the phase-1 sums' group table, the panels' exponent bounds
     DevBuf<unsigned char> ozx; // and its digit planes
     int ozx_mu_ = 0;           // right-hand sides the plane scratch holds
     OzScratch ozs_{};

@@ -79,10 +79,6 @@ struct OzCfg {
     static constexpr unsigned kCols = S * kOzN <= 256 ? (S * kOzN <= 128 ? 128u : 256u) : 512u; // a power of two
 };
 
-// instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits
-// 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both K-major, N / 8 at bits
-// 17-22, M / 16 at bits 24-28
-constexpr unsigned kOzIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(kOzN >> 3) << 17) | ((unsigned)(kOzM >> 4) << 24);
 
 // byte offset of BF16 element (row, k) of a 32-deep plane in the canonical layout
 __device__ __forceinline__ int oz_off(int row, int k) { return (row >> 3) * kOzSbo + (k >> 3) * kOzLbo + (row & 7) * 16 + (k & 7) * 2; }
@@ -95,8 +91,28 @@ __device__ __forceinline__ unsigned long long oz_desc(unsigned addr) {
     return d;
 }
 
-__device__ __forceinline__ void oz_mma(unsigned tmem_d, unsigned long long a, unsigned long long b, int accumulate) {
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d), "l"(a), "l"(b), "r"(kOzIdesc), "r"(accumulate) : "memory");
+
+__device__ __forceinline__ void oz_mma_i(unsigned tmem_d, unsigned long long a, unsigned long long b, unsigned idesc, int accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+// The S (S + 1) / 2 plane products of one slab in few MMAs: A plane i times
+// the B planes j = 0 .. S - 1 - i side by side along N lands in the
+// accumulators of the diagonals i + j, which lie side by side in tensor
+// memory (plane rows nb each, at most 256 columns a MMA).  The instruction
+// descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits 4-5 = 1), A
+// and B BF16 (bits 7-9, 10-12 = 1), both K-major, N / 8 at bits 17-22,
+// M / 16 at bits 24-28.
+template <int S>
+__device__ __forceinline__ void oz_slab_mmas(unsigned tmem, unsigned a0, unsigned b0, int nb, bool first) {
+    const int per = 256 / nb; // B planes a MMA
+#pragma unroll
+    for (int i = 0; i < S; i++)
+        for (int j0 = 0; j0 < S - i; j0 += per) {
+            const int cnt        = min(per, S - i - j0);
+            const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)((cnt * nb) >> 3) << 17) | ((unsigned)(kOzM >> 4) << 24);
+            oz_mma_i(tmem + (unsigned)((i + j0) * nb), oz_desc(a0 + i * kOzPlaneA), oz_desc(b0 + j0 * nb * 32), idesc, !(first && i == 0));
+        }
 }
 
 // biased exponent field of |v| (0 for zero and subnormals)
@@ -158,6 +174,18 @@ __device__ __forceinline__ void oz_put8(unsigned char *planes, int plane_bytes, 
         w.w = oz_bf2(d[6][s], d[7][s]);
         *reinterpret_cast<uint4 *>(planes + (size_t)s * plane_bytes + oz_off(row, k)) = w;
     }
+}
+
+// four consecutive K values (k a multiple of 4), one 8-byte store per plane
+template <int S, int T>
+__device__ __forceinline__ void oz_put4(unsigned char *planes, int plane_bytes, int row, int k, const double (&v)[4], const int (&emax)[4]) {
+    int d[4][S];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        oz_digits<S>(oz_fixed<T>(v[q], emax[q]), d[q]);
+#pragma unroll
+    for (int s = 0; s < S; s++)
+        *reinterpret_cast<uint2 *>(planes + (size_t)s * plane_bytes + oz_off(row, k)) = make_uint2(oz_bf2(d[0][s], d[1][s]), oz_bf2(d[2][s], d[3][s]));
 }
 
 // |I| normalised: the leading bit at 127, its position, the sign
@@ -296,12 +324,13 @@ __global__ void __launch_bounds__(kOzThreads) oz_pack_kernel(const TcBlock *__re
     }
 }
 
-// exponent field maxima of the gathered input per group of 32 rows and
-// right-hand side; the wide-input flag ecol[mu] cleared
-__global__ void oz_xgroup_kernel(const double *__restrict__ xp, int nrows, int mu, int *__restrict__ gexp, int *__restrict__ ecol) {
+// exponent field maxima of v (nrows x mu, row-major: the gathered input, or
+// the phase-1 sums) per group of 32 rows and right-hand side; *reset (a
+// wide-input flag) cleared
+__global__ void oz_xgroup_kernel(const double *__restrict__ v, int nrows, int mu, int *__restrict__ gexp, int *__restrict__ reset) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0)
-        ecol[mu] = 0;
+    if (t == 0 && reset)
+        *reset = 0;
     const int ng = (nrows + 31) >> 5;
     if (t >= (long long)ng * mu)
         return;
@@ -309,25 +338,27 @@ __global__ void oz_xgroup_kernel(const double *__restrict__ xp, int nrows, int m
     int e        = 0;
     const int j1 = min(nrows, 32 * g + 32);
     for (int j = 32 * g; j < j1; j++)
-        e = max(e, oz_ebits(xp[(long long)j * mu + c]));
+        e = max(e, oz_ebits(v[(long long)j * mu + c]));
     gexp[t] = e;
 }
 
 // Inputs with a group of 32 rows whose largest value is more than this many
 // binades below its right-hand side's maximum take the staged kernel
-// (exponents per block); the others are cut into planes once, relative to
-// each right-hand side's maximum, and keep at least T - kOzWide bits.
+// (exponents per block); the others are cut into planes relative to each
+// right-hand side's maximum, and keep at least T - kOzWide bits.
 constexpr int kOzWide = 10;
 
-// each right-hand side's exponent maximum (one CTA per right-hand side),
-// then the wide-input flag
-__global__ void oz_xcol_kernel(const int *__restrict__ gexp, int ng, int mu, int *__restrict__ ecol) {
+// each right-hand side's exponent maximum over one or two group tables (one
+// CTA per right-hand side), then the wide flag ecol[mu]
+__global__ void oz_xcol_kernel(const int *__restrict__ g1, int ng1, const int *__restrict__ g2, int ng2, int mu, int *__restrict__ ecol) {
     __shared__ int red[8];
     __shared__ int emax;
     const int c = blockIdx.x;
     int e       = 0;
-    for (int g = threadIdx.x; g < ng; g += blockDim.x)
-        e = max(e, gexp[(long long)g * mu + c]);
+    for (int g = threadIdx.x; g < ng1; g += blockDim.x)
+        e = max(e, g1[(long long)g * mu + c]);
+    for (int g = threadIdx.x; g < ng2; g += blockDim.x)
+        e = max(e, g2[(long long)g * mu + c]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
         e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
@@ -343,8 +374,12 @@ __global__ void oz_xcol_kernel(const int *__restrict__ gexp, int ng, int mu, int
     }
     __syncthreads();
     bool wide = false;
-    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-        const int eg = gexp[(long long)g * mu + c];
+    for (int g = threadIdx.x; g < ng1; g += blockDim.x) {
+        const int eg = g1[(long long)g * mu + c];
+        wide |= eg > 0 && emax - eg > kOzWide;
+    }
+    for (int g = threadIdx.x; g < ng2; g += blockDim.x) {
+        const int eg = g2[(long long)g * mu + c];
         wide |= eg > 0 && emax - eg > kOzWide;
     }
     if (__syncthreads_or(wide) && threadIdx.x == 0)
@@ -471,11 +506,7 @@ __global__ void __launch_bounds__(kOzFastThreads, 1) phase1_ozb_kernel(const TcB
                 }
                 fence_after();
                 const unsigned a0 = smem_u32(smem + (size_t)stg * C::kBuf), b0 = a0 + C::kSlab;
-#pragma unroll
-                for (int D = 0; D < S; D++)
-#pragma unroll
-                    for (int i = 0; i <= D; i++)
-                        oz_mma(tmem + (unsigned)(D * kOzN), oz_desc(a0 + i * kOzPlaneA), oz_desc(b0 + (D - i) * kOzPlaneB), !(mc.s == 0 && i == 0));
+                oz_slab_mmas<S>(tmem, a0, b0, kOzN, mc.s == 0);
                 commit(&empty[stg]);
                 mi++;
                 const bool last = mc.s == mc.nsl - 1;
@@ -660,14 +691,7 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
                     if (bar_wait(&fulls[buf], use & 1)) {
                         fence_after();
                         const unsigned a0 = smem_u32(stage), b0 = a0 + S * kOzPlaneA;
-#pragma unroll
-                        for (int kk = 0; kk < kOzK / 16; kk++)
-#pragma unroll
-                            for (int D = 0; D < S; D++)
-#pragma unroll
-                                for (int i = 0; i <= D; i++)
-                                    oz_mma(tmem + (unsigned)(D * kOzN), oz_desc(a0 + i * kOzPlaneA + kk * 2 * kOzLbo), oz_desc(b0 + (D - i) * kOzPlaneB + kk * 2 * kOzLbo),
-                                           !(ks == 0 && kk == 0 && i == 0));
+                        oz_slab_mmas<S>(tmem, a0, b0, kOzN, ks == 0);
                         commit(&bars[buf]);
                     } else {
                         fail = true; // spreads at the next barrier
@@ -760,6 +784,338 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
         tmem_free(tmem, C::kCols);
 }
 
+// ---------------------------------------------------------------------------
+// Phase 2 of FP64 products with many right-hand sides on the same planes.
+// A row chunk (panel: h <= 32 rows of z, ncol columns -- the U columns of
+// the leaves on its target cluster and its dense columns, each times a
+// coefficient: a phase-1 sum or an x row) is one transposed product
+//
+//     z^T (mu x h) = C^T (mu x ncol) P^T (ncol x h),
+//
+// M = 128 right-hand-side rows (64 used per pass, the rest zero), N = h
+// rounded up to 16 or 32, K = 16 columns a slab.  The panel's planes (B,
+// N x 16 a slab) are laid out once (oz_panel_pack_kernel); the threads cut
+// the coefficients into planes (A) relative to a bound on the panel's
+// largest coefficient for each right-hand side (the maxima of the 32-row
+// groups of phase-1 sums and input rows its columns lie in: the trailing
+// columns of a leaf's sums are epsilon below its leading ones, so one
+// exponent per right-hand side for the whole product would not do).  The
+// accumulators restart every 256 columns so their FP32 sums stay exact
+// integers; the rounds add up exactly in the read-out's 64-bit registers.
+constexpr int kOzRound = 256 / kOzK; // slabs per accumulation round
+
+template <int S>
+__global__ void __launch_bounds__(kOzThreads) oz_panel_pack_kernel(const OzPanel *__restrict__ panels, const double *__restrict__ f64, int *__restrict__ prexp,
+                                                                   unsigned char *__restrict__ parena) {
+    __shared__ int se[8][32];
+    const OzPanel P = panels[blockIdx.x];
+    const int tid = threadIdx.x, N = P.h <= 16 ? 16 : 32, nsl = (P.ncol + kOzK - 1) / kOzK;
+    const double *src = f64 + P.off; // h x ncol, column-major
+    {
+        const int n = tid & 31, cg = tid >> 5;
+        int e = 0;
+        if (n < P.h)
+            for (int q = cg; q < P.ncol; q += 8)
+                e = max(e, oz_ebits(src[(long long)q * P.h + n]));
+        se[cg][n] = e;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        int e = 0;
+#pragma unroll
+        for (int g = 0; g < 8; g++)
+            e = max(e, se[g][tid]);
+        se[0][tid]                                = e;
+        prexp[(long long)blockIdx.x * 32 + tid] = e;
+    }
+    __syncthreads();
+    const int plane = 32 * N; // N x 16 BF16
+    for (int it = tid; it < nsl * N * 2; it += blockDim.x) {
+        const int sl = it / (2 * N), r = it - sl * 2 * N, n = r >> 1, kh = (r & 1) * 8;
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int col = kOzK * sl + kh + q;
+            v[q]          = (n < P.h && col < P.ncol) ? src[(long long)col * P.h + n] : 0.;
+        }
+        oz_put8<S, OzCfg<S>::kT>(parena + P.poff + (long long)sl * S * plane, plane, n, kh, v, se[0][n & 31]);
+    }
+}
+
+
+// the exponent bound of right-hand side rhs over a panel's coefficients:
+// the largest of its groups' maxima
+__device__ __forceinline__ int oz_panel_exp(const OzPanel &P, const int *__restrict__ groups, const int *__restrict__ gexp, const int *__restrict__ agexp, int mu, int rhs) {
+    int e = 0;
+    for (int k = 0; k < P.ngrp; k++) {
+        const int g = __ldg(groups + P.gofs + k);
+        e           = max(e, g >= 0 ? __ldg(agexp + (long long)g * mu + rhs) : __ldg(gexp + (long long)(-1 - g) * mu + rhs));
+    }
+    return e;
+}
+
+// each panel's exponent bound per right-hand side (pexp: npanels x mu):
+// one warp per panel and 32 right-hand sides, lanes over the right-hand sides
+__global__ void oz_panel_exp_kernel(const OzPanel *__restrict__ panels, int npanels, const int *__restrict__ groups, const int *__restrict__ gexp, const int *__restrict__ agexp, int mu,
+                                    int *__restrict__ pexp) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane    = threadIdx.x & 31, nq = (mu + 31) >> 5;
+    if (w >= (long long)npanels * nq)
+        return;
+    const int q = (int)(w / nq), rhs = 32 * (int)(w - (long long)q * nq) + lane;
+    if (rhs < mu)
+        pexp[(long long)q * mu + rhs] = oz_panel_exp(panels[q], groups, gexp, agexp, mu, rhs);
+}
+
+template <int S>
+struct Oz2Cfg {
+    static constexpr int kA      = S * kOzPlaneA;   // 128 x 16 per plane (rows 64-127 zero)
+    static constexpr int kB      = S * 32 * 32;     // N <= 32 rows x 16 per plane
+    static constexpr int kStage  = kA + kB;
+    static constexpr int kStages = 4;
+    static constexpr int kSmem   = kStages * kStage + 256;
+    static constexpr unsigned kCols = S * 32 <= 128 ? 128u : 256u;
+};
+
+// Thirteen warps in three roles over the same sequence of (panel, pass of
+// 64 right-hand sides, 16-column slab): warps 2 and 6-12 cut each slab's
+// coefficients into planes (thread t: right-hand side t mod 64, 4 columns;
+// the next slab's coefficients loaded while the current one is cut) into a
+// ring of four stages; lane 0 of warp 3 copies the panel's planes in and
+// issues the MMAs as both halves of a stage are ready; warps 0, 1, 4, 5
+// (tensor-memory lanes 0-63: the right-hand sides) add each round's
+// accumulators into exact 64-bit sums and write the z rows at the end of a
+// pass.  The exponent bounds come from pexp (oz_panel_exp_kernel).
+constexpr int kOz2Threads = 416;
+
+template <int S>
+__global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel *__restrict__ panels, int npanels, const int *__restrict__ groups, const unsigned char *__restrict__ parena,
+                                                                   const int *__restrict__ prexp, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp,
+                                                                   const int *__restrict__ pexp, int mu, double *__restrict__ z, int zlen, int *__restrict__ status) {
+    using C           = Oz2Cfg<S>;
+    constexpr int T   = OzCfg<S>::kT;
+    constexpr int NST = C::kStages;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long *fulla = reinterpret_cast<unsigned long long *>(smem + NST * C::kStage); // [NST] coefficients cut (256 arrivals)
+    unsigned long long *fullb = fulla + NST;                                                    // [NST] panel planes landed
+    unsigned long long *empty = fulla + 2 * NST;                                                // [NST] a stage's MMAs done
+    unsigned long long *accf  = fulla + 3 * NST;                                                // a round's accumulators complete
+    unsigned long long *acce  = accf + 1;                                                       // and added up by the readers (4 arrivals)
+    unsigned *tslot           = reinterpret_cast<unsigned *>(smem + NST * C::kStage + 128);
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const int npass = (mu + kOzN - 1) / kOzN;
+    for (int i = tid; i < NST * C::kA / 16; i += blockDim.x) { // the A planes' rows 64-127 stay zero
+        const int st = i / (C::kA / 16), w = i - st * (C::kA / 16);
+        reinterpret_cast<uint4 *>(smem + (size_t)st * C::kStage)[w] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    proxy_fence();
+    if (tid == 0) {
+        for (int k = 0; k < NST; k++) {
+            bar_init_n(&fulla[k], 256);
+            bar_init(&fullb[k]);
+            bar_init(&empty[k]);
+        }
+        bar_init(accf);
+        bar_init_n(acce, 4);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (wid == 0)
+        tmem_alloc(tslot, C::kCols);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tmem = *tslot;
+    bool fail           = false;
+    // a cursor over (panel, pass, slab)
+    struct Cur {
+        int bi, p, s, nsl;
+    };
+    auto load = [&](Cur &c) {
+        if (c.bi < npanels)
+            c.nsl = (panels[c.bi].ncol + kOzK - 1) / kOzK;
+    };
+    auto advance = [&](Cur &c) {
+        if (++c.s == c.nsl) {
+            c.s = 0;
+            if (++c.p == npass) {
+                c.p = 0;
+                c.bi += gridDim.x;
+                load(c);
+            }
+        }
+    };
+    if (wid == 3) {
+        if (lane == 0) { // copies and MMAs
+            Cur cc{(int)blockIdx.x, 0, 0, 0};
+            load(cc);
+            Cur mc = cc;
+            int ci = 0, mi = 0, rounds = 0, inround = 0;
+            while (mc.bi < npanels && !fail) {
+                while (cc.bi < npanels && ci < mi + NST) {
+                    const int stg = ci % NST, use = ci / NST;
+                    if (use > 0 && !bar_wait(&empty[stg], (use - 1) & 1)) {
+                        fail = true;
+                        break;
+                    }
+                    const OzPanel P = panels[cc.bi];
+                    const int bytes = S * 32 * (P.h <= 16 ? 16 : 32);
+                    bar_expect_tx(&fullb[stg], bytes);
+                    bulk_g2s(smem + (size_t)stg * C::kStage + C::kA, parena + P.poff + (long long)cc.s * bytes, bytes, &fullb[stg]);
+                    ci++;
+                    advance(cc);
+                }
+                if (fail)
+                    break;
+                const int stg = mi % NST, use = mi / NST;
+                if (inround == 0 && rounds > 0 && !bar_wait(acce, (rounds - 1) & 1)) { // the readers hold the last round
+                    fail = true;
+                    break;
+                }
+                if (!bar_wait(&fullb[stg], use & 1) || !bar_wait(&fulla[stg], use & 1)) {
+                    fail = true;
+                    break;
+                }
+                fence_after();
+                const int N       = panels[mc.bi].h <= 16 ? 16 : 32;
+                const unsigned a0 = smem_u32(smem + (size_t)stg * C::kStage), b0 = a0 + C::kA;
+                oz_slab_mmas<S>(tmem, a0, b0, N, inround == 0);
+                commit(&empty[stg]);
+                mi++;
+                const bool end = mc.s == mc.nsl - 1 || inround == kOzRound - 1;
+                advance(mc);
+                inround++;
+                if (end) {
+                    commit(accf);
+                    rounds++;
+                    inround = 0;
+                }
+            }
+            if (fail) {
+                atomicExch(status, 4);
+                for (int k = mi; k < ci; k++) // the copies in flight land before the CTA leaves
+                    bar_wait(&fullb[k % NST], (k / NST) & 1);
+            }
+        }
+    } else if (wid == 2 || wid >= 6) { // coefficient stagers
+        const int t = 32 * (wid == 2 ? 0 : wid - 5) + lane, n = t & 63, k0 = (t >> 6) * 4;
+        Cur c{(int)blockIdx.x, 0, 0, 0};
+        load(c);
+        double v[4];
+        auto loadc = [&](const Cur &k) {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                v[q] = 0.;
+            if (k.bi >= npanels)
+                return;
+            const OzPanel P = panels[k.bi];
+            const int rhs   = kOzN * k.p + n;
+            if (rhs >= mu)
+                return;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int col = kOzK * k.s + k0 + q;
+                if (col < P.ncol) {
+                    const int kx = __ldg(cidx + P.q0 + col);
+                    v[q]         = kx >= 0 ? __ldg(A + (long long)kx * mu + rhs) : __ldg(xp + (long long)(~kx) * mu + rhs);
+                }
+            }
+        };
+        loadc(c);
+        int it = 0;
+        while (c.bi < npanels && !fail) {
+            const int stg = it % NST, use = it / NST;
+            if (use > 0 && !bar_wait(&empty[stg], (use - 1) & 1)) {
+                fail = true;
+                break;
+            }
+            const int rhs = kOzN * c.p + n;
+            const int e   = rhs < mu ? __ldg(pexp + (long long)c.bi * mu + rhs) : 0;
+            const int E[4] = {e, e, e, e};
+            double cur[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                cur[q] = v[q];
+            Cur nx = c;
+            advance(nx);
+            loadc(nx); // the next slab's coefficients fly while this one is cut
+            oz_put4<S, T>(smem + (size_t)stg * C::kStage, kOzPlaneA, n, k0, cur, E);
+            proxy_fence();
+            bar_arrive(&fulla[stg]);
+            c = nx;
+            it++;
+        }
+        if (fail && lane == 0)
+            atomicExch(status, 4);
+    } else { // readers: warps 0, 1 (columns 0-15), 4, 5 (16-31)
+        const int m = 32 * (wid & 3) + lane, ch = wid >> 2;
+        Cur c{(int)blockIdx.x, 0, 0, 0};
+        load(c);
+        int rounds = 0;
+        long long hi[16], lo[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++)
+            hi[q] = lo[q] = 0;
+        while (c.bi < npanels && !fail) {
+            const OzPanel P = panels[c.bi];
+            const int N     = P.h <= 16 ? 16 : 32;
+            // this round: slabs c.s .. end of round or of the pass
+            const int last = min(c.nsl - 1, c.s + kOzRound - 1);
+            if (!bar_wait(accf, rounds & 1)) {
+                fail = true;
+                break;
+            }
+            fence_after();
+            if (16 * ch < N) {
+#pragma unroll
+                for (int D = 0; D < S; D++) {
+                    unsigned r[16];
+                    tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + (unsigned)(D * N + 16 * ch), r);
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const long long a = (long long)__float2int_rn(__uint_as_float(r[q]));
+                        if (D < S / 2)
+                            hi[q] += a << (7 * (S / 2 - 1 - D));
+                        else
+                            lo[q] += a << (7 * (S - 1 - D));
+                    }
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0)
+                bar_arrive(acce);
+            rounds++;
+            const bool pass_end = last == c.nsl - 1;
+            const int bi = c.bi, p = c.p;
+            c.s = last; // the cursor past this round
+            advance(c);
+            if (pass_end) {
+                const int rhs = kOzN * p + m;
+                if (16 * ch < N && rhs < mu) {
+                    const int k = 7 * (S - 1) + __ldg(pexp + (long long)bi * mu + rhs) - 2044 - 2 * T;
+                    double *zc  = z + (long long)rhs * zlen + P.row0;
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int r = 16 * ch + q;
+                        if (r < P.h)
+                            zc[r] = oz_i2d(((__int128)hi[q] << (7 * (S / 2))) + lo[q], k + __ldg(prexp + (long long)bi * 32 + r));
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 16; q++)
+                    hi[q] = lo[q] = 0;
+            }
+        }
+        if (fail && lane == 0)
+            atomicExch(status, 4);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (wid == 0)
+        tmem_free(tmem, C::kCols);
+}
+
 template <typename K>
 void oz_smem_attr(K kernel, int bytes) {
     HTGPU_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -819,9 +1175,9 @@ void launch_oz_prepare(const double *xp, int nrows, int mu, int S, const OzScrat
     if (ng <= 0 || mu <= 0)
         return;
     const long long n = (long long)ng * mu;
-    oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xp, nrows, mu, sc.gexp, sc.ecol);
+    oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xp, nrows, mu, sc.gexp, sc.ecol + mu);
     HTGPU_CUDA(cudaGetLastError());
-    oz_xcol_kernel<<<mu, 256, 0, st>>>(sc.gexp, ng, mu, sc.ecol);
+    oz_xcol_kernel<<<mu, 256, 0, st>>>(sc.gexp, ng, nullptr, 0, mu, sc.ecol);
     HTGPU_CUDA(cudaGetLastError());
     const dim3 grid((nrows + kOzK - 1) / kOzK, (mu + kOzN - 1) / kOzN);
     if (S == 8)
@@ -849,6 +1205,52 @@ void launch_phase1_oz(const TcBlock *blocks, int nblocks, const TcSeg *segs, int
         oz_launch<4, true>(blocks, nblocks, segs, arena, ozoff, rexp, scale, xp, sc, xexp, mu, A, status, st);
     else
         throw Error(1, "[Htool error] digit planes: S must be 4 or 8");
+}
+
+long long oz_panel_bytes(const OzPanel *panels_h, int npanels, int S, long long *poff_h) {
+    long long off = 0;
+    for (int q = 0; q < npanels; q++) {
+        const int N = panels_h[q].h <= 16 ? 16 : 32;
+        poff_h[q]   = off;
+        off += (long long)((panels_h[q].ncol + kOzK - 1) / kOzK) * S * 32 * N;
+    }
+    return off;
+}
+
+void launch_oz_panel_pack(const OzPanel *panels, int npanels, const double *f64, int *prexp, unsigned char *parena, cudaStream_t st) {
+    if (npanels <= 0)
+        return;
+    oz_panel_pack_kernel<8><<<npanels, kOzThreads, 0, st>>>(panels, f64, prexp, parena);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_phase2_oz(const OzPanel *panels, int npanels, const int *groups, const unsigned char *parena, const int *prexp, const int *cidx, const double *A, int aslots, const double *xp,
+                      const OzScratch &sc, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+    if (npanels <= 0)
+        return;
+    // the phase-1 sums' exponent table (the input's was written by launch_oz_prepare)
+    const int nga = (aslots + 31) >> 5;
+    if (nga > 0) {
+        const long long n = (long long)nga * mu;
+        oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(A, aslots, mu, sc.agexp, nullptr);
+        HTGPU_CUDA(cudaGetLastError());
+    }
+    {
+        const long long warps = (long long)npanels * ((mu + 31) >> 5);
+        oz_panel_exp_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(panels, npanels, groups, sc.gexp, sc.agexp, mu, sc.pexp);
+        HTGPU_CUDA(cudaGetLastError());
+    }
+    static unsigned long long done = 0;
+    int dev = 0, sms = 0;
+    HTGPU_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(done >> dev & 1)) {
+        oz_smem_attr(phase2_oz_kernel<8>, Oz2Cfg<8>::kSmem);
+        if (dev < 64)
+            done |= 1ull << dev;
+    }
+    HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    phase2_oz_kernel<8><<<std::min(npanels, sms), kOz2Threads, Oz2Cfg<8>::kSmem, st>>>(panels, npanels, groups, parena, prexp, cidx, A, xp, sc.pexp, mu, z, zlen, status);
+    HTGPU_CUDA(cudaGetLastError());
 }
 
 } // namespace htgpu
