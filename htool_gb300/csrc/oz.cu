@@ -15,25 +15,29 @@
 // cast as exact integer products.  Every row of A (a factor column) is
 // scaled by a power of two 2^-ea at least its largest magnitude, every
 // column of B (a right-hand side over the block's x rows) by 2^-eb, and
-// rounded to the integer Q = round(v 2^T), |Q| <= 2^T, T = 6 + 7 (S - 1).
-// Q is cut into S balanced base-128 digits d_0 (top, |d_0| <= 65) ..
+// rounded to the integer Q = round(v 2^T), |Q| <= 2^T, T = 5 + 7 (S - 1).
+// Q is cut into S balanced base-128 digits d_0 (top, |d_0| <= 33) ..
 // d_{S-1} (|d| <= 64), each exact in BF16:
 //
 //     Q = sum_i d_i 2^(7 (S - 1 - i)).
 //
 // The products of digit planes i of A and j of B with i + j = D share the
 // weight 2^(7 (2S - 2 - D)); pairs with i + j >= S are dropped (they weigh
-// less than 2^-(7S - 7) of the leading term).  Each plane product is an
-// ordinary BF16 MMA with FP32 accumulation, and it is exact: a product of
-// two digits is below 2^12.1, a diagonal holds at most S pairs, K <= 256, so
-// every partial sum stays an integer below 2^24.  The S diagonals accumulate
-// in S tensor-memory accumulators of 64 columns; the read-out combines them
+// less than 2^-(7S - 8) of the leading term).  Each plane product is an
+// ordinary BF16 MMA with FP32 accumulation, and it is exact: a diagonal
+// holds at most S pairs, two of them with a top digit, so a column adds at
+// most 2 * 33 * 64 + 6 * 64 * 64 = 28 800 and K <= 271 rows (256 and the
+// alignment to the input's 16-row groups) keep every partial sum below
+// 2^23, where the tensor cores' FP32 sums were measured exact (an
+// adversarial test drives them to 7.3 M; 7-bit fields of one sign, whose
+// sums reach 2^24, lost bits).  The S diagonals accumulate in S
+// tensor-memory accumulators of 64 columns; the read-out combines them
 // exactly in 128-bit integers and converts once (integer arithmetic only:
-// the FP64 pipe is not used anywhere).  With S = 8 (T = 55) the result carries the
-// rounding of the inputs to 55 bits relative to the block's row / column
-// maxima (FP64-grade); with S = 4 (T = 27) of reduced-precision factors it
-// keeps their FP32 accuracy and accumulates exactly, unlike the TF32
-// products of tc.cu whose FP32 tensor-core sums round.
+// the FP64 pipe is not used anywhere).  With S = 8 (T = 54) the result
+// carries the rounding of the inputs to 54 bits relative to the block's row
+// / column maxima (FP64-grade); with S = 4 (T = 26) of reduced-precision
+// factors it keeps their FP32 accuracy and accumulates exactly, unlike the
+// TF32 products of tc.cu whose FP32 tensor-core sums round.
 //
 // Data: the A digit planes are laid out once per H-matrix (oz_pack_kernel:
 // per block and 16-row slab, S planes of 128 x 16 BF16 in the canonical
@@ -69,7 +73,7 @@ constexpr int kOzSbo     = (kOzK / 8) * 128; // bytes between 8-row groups
 
 template <int S>
 struct OzCfg {
-    static constexpr int kT      = 6 + 7 * (S - 1);        // bits of the fixed-point values
+    static constexpr int kT      = 5 + 7 * (S - 1);        // bits of the fixed-point values
     static constexpr int kSlab   = S * kOzPlaneA;           // arena bytes per slab
     static constexpr int kBslab  = S * kOzPlaneB;           // input plane bytes per slab
     static constexpr int kBuf    = kSlab + kBslab;          // one stage: A planes, B planes
@@ -176,7 +180,11 @@ __device__ __forceinline__ void oz_put8(unsigned char *planes, int plane_bytes, 
     }
 }
 
-// four consecutive K values (k a multiple of 4), one 8-byte store per plane
+// four consecutive K values (k a multiple of 4), one 8-byte store per plane.
+// (Two's-complement 7-bit fields would take fewer operations than the
+// balanced digits, but their products are all of one sign and up to
+// 33 * 127: the MMA sums then grow past 2^23, where the measured products
+// lost bits.)
 template <int S, int T>
 __device__ __forceinline__ void oz_put4(unsigned char *planes, int plane_bytes, int row, int k, const double (&v)[4], const int (&emax)[4]) {
     int d[4][S];
@@ -802,7 +810,9 @@ __global__ void __launch_bounds__(kOzThreads, S <= 4 ? 2 : 1) phase1_oz_kernel(c
 // exponent per right-hand side for the whole product would not do).  The
 // accumulators restart every 256 columns so their FP32 sums stay exact
 // integers; the rounds add up exactly in the read-out's 64-bit registers.
-constexpr int kOzRound = 256 / kOzK; // slabs per accumulation round
+// slabs per accumulation round: 256 columns keep a diagonal's sums below
+// 2^23 (at most 28 800 a column, as in phase 1)
+constexpr int kOzRound = 256 / kOzK;
 
 template <int S>
 __global__ void __launch_bounds__(kOzThreads) oz_panel_pack_kernel(const OzPanel *__restrict__ panels, const double *__restrict__ f64, int *__restrict__ prexp,

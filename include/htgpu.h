@@ -405,8 +405,8 @@ int htgpu_hmatrix_get_tensor_core_arena(htgpu_hmatrix h, int *on, long long *byt
 /* Phase 1 of products with 8 or more right-hand sides on the BF16 tensor
  * cores by exact digit slicing (the Ozaki scheme): every factor column and
  * right-hand side is scaled by a power of two and cut into base-128 digits
- * (8 planes for FP64 storage: 55 bits, FP64-grade sums; 4 for reduced
- * storage: 27 bits, at any epsilon), the plane products are exact integer
+ * (8 planes for FP64 storage: 54 bits, FP64-grade sums; 4 for reduced
+ * storage: 26 bits, at any epsilon), the plane products are exact integer
  * MMAs, the read-out sums them exactly in 128-bit integers.  Replaces the
  * double-float FP64 phase 1 and the reduced-precision phase-1 kernels of
  * those products.  Costs a copy of the factors cut into planes (*bytes; 0

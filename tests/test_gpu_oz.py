@@ -4,9 +4,11 @@ cut into BF16 digit planes whose MMA sums are exact integers.
 * Integer operands: the products are exact, bit for bit, with S = 8 and 4.
 * Random FP64 operands over a wide range of magnitudes, ragged K and mu
   (several passes of 64 right-hand sides), zero rows and columns: within
-  the error bound of the scheme (each input rounded to T = 55 (S = 8) or
-  27 (S = 4) fraction bits of its row's or column's maximum) against the
+  the error bound of the scheme (each input rounded to T = 54 (S = 8) or
+  26 (S = 4) fraction bits of its row's or column's maximum) against the
   float64 product.
+* Digits all of one sign and near their bound: the tensor cores' FP32 sums
+  of the plane products (up to 7.3 M) stay exact.
 The reference computes these contractions as BLAS gemm calls with the
 row-major right-hand sides (types/matrix.hpp:346, 380)."""
 import numpy as np
@@ -21,7 +23,7 @@ def model(a, b, S):
     """The scheme restated with numpy integers (one block, the exponents of
     whole rows of a and columns of b): digits, exact plane products, the
     pairs i + j < S, the exact sum, one rounding to float64."""
-    T = 6 + 7 * (S - 1)
+    T = 5 + 7 * (S - 1)
     eb = lambda v: ((v.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
     er, ec = eb(a).max(1), eb(b).max(0)
 
@@ -79,7 +81,7 @@ def test_integer_operands_exact(S, staged):
     assert np.array_equal(oz_gemm(e, bb, S, staged), e @ bb)
 
 
-@pytest.mark.parametrize("S,bits", [(8, 55), (4, 27)])
+@pytest.mark.parametrize("S,bits", [(8, 54), (4, 26)])
 @pytest.mark.parametrize("K,mu", [(256, 64), (77, 100), (5, 3), (200, 130)])
 def test_fp64_operands_within_bound(S, bits, K, mu):
     rng = np.random.default_rng(K * 1000 + mu)
@@ -208,3 +210,18 @@ def test_autotune_with_digit_planes(golden):
     assert hm.autotune(32, 2) > 0
     assert rel(hm.mvprod_global_to_global(X, 32), y) < 1e-6
     assert hm.device_status() == 0
+
+
+@pytest.mark.parametrize("staged", [False, True])
+def test_accumulation_exact_near_2_23(staged):
+    """operands whose digits are all of one sign and at their bound (top -31,
+    the others -64): every plane product is positive and the FP32 sums of
+    the last diagonal reach 7.3 M over 256 rows; the result is still bit
+    for bit the integer restatement's"""
+    S = 8
+    Q = -31 * 2**49 - 64 * ((2**49 - 1) // 127)  # balanced digits -31, -64, ..., -64
+    v = Q / 2.0**53  # |Q| in [2^53, 2^54): the fixed point of T = 54 bits
+    assert v * 2.0**53 == Q
+    a = np.full((128, 256), v)
+    b = np.full((256, 64), v)
+    assert np.array_equal(oz_gemm(a, b, S, staged), model(a, b, S))
