@@ -702,6 +702,16 @@ def run_helmholtz(args):
     ms_arena, y_arena = timed(steps)
     ph_arena = hm.profile(mu, 3)
     hm.set_tensor_core_arena(False)
+    # phase 1 on the BF16 tensor cores by exact digit slicing (4 planes)
+    hm.set_digit_planes(True)
+    ms_dpm, y_dpm = timed(steps)
+    ph_dpm = hm.profile(mu, 3)
+    # FP64 with 8 planes in both phases
+    hm.set_precision("fp64")
+    planes64 = hm.get_digit_planes()[1]
+    ms_dp64, y_dp64 = timed(steps)
+    ph_dp64 = hm.profile(mu, 3)
+    hm.set_digit_planes(False)
     ck = clocks.stop()
     status = hm.device_status()
     info = hm.get_infos()
@@ -716,6 +726,8 @@ def run_helmholtz(args):
         "mixed_tcgen05_both": {"ms": ms_both, "rel_err_vs_fp64": err(y_both), "phase_ms": phases(ph_both)},
         "mixed_mma_sync": {"ms": ms_mma, "rel_err_vs_fp64": err(y_mma), "phase_ms": phases(ph_mma)},
         "mixed_tcgen05_arena": {"ms": ms_arena, "phase_ms": phases(ph_arena), "arena_bytes": arena_bytes, "bitwise_equal_to_tcgen05": bool(np.array_equal(y_arena, y_tc))},
+        "mixed_digit_planes": {"ms": ms_dpm, "rel_err_vs_fp64": err(y_dpm), "phase_ms": phases(ph_dpm), "kernels": "phase 1 on 4 BF16 digit planes (exact sums), phase 2 mma.sync"},
+        "fp64_digit_planes": {"ms": ms_dp64, "rel_err_vs_fp64": err(y_dp64), "phase_ms": phases(ph_dp64), "plane_bytes": planes64, "kernels": "both phases on 8 BF16 digit planes (exact sums)"},
         "fp64": {"ms": ms64, "phase_ms": phases(ph64)},
         "build_seconds": build_s, "clocks": ck, "device_status": status,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_mean", "Compression_ratio")},
