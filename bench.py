@@ -716,11 +716,15 @@ def run_helmholtz(args):
     status = hm.device_status()
     info = hm.get_infos()
     err = lambda y: float(np.linalg.norm(y - y64) / np.linalg.norm(y64))
+    # the headline: the fastest reduced-precision variant within epsilon of FP64
+    variants = {"mixed_tcgen05": (ms_tc, y_tc), "mixed_tcgen05_arena": (ms_arena, y_arena), "mixed_digit_planes": (ms_dpm, y_dpm), "mixed_mma_sync": (ms_mma, y_mma), "mixed_tcgen05_both": (ms_both, y_both)}
+    best_name = min((k for k in variants if err(variants[k][1]) <= 1e-5), key=lambda k: variants[k][0])
+    ms_best = variants[best_name][0]
     phases = lambda ph: {"gather": ph[0], "phase1": ph[1], "phase2": ph[2], "sums": ph[3], "total": ph[4]}
     line = {
-        "metric": "complex H-matmat with 64 right-hand sides per second (H-matvec/s = 64 / time)", "value": world * mu / (ms_tc * 1e-3), "unit": UNIT, "n_gpus": world, "steps": steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms_tc, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32/bf16 factors (per-column scaled), TF32x3 tensor-core contractions with FP32 accumulation, fp64 dense", "data": "synthetic (seeded points on the unit-cube surface)",
+        "metric": "complex H-matmat with 64 right-hand sides per second (H-matvec/s = 64 / time)", "value": world * mu / (ms_best * 1e-3), "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_best, "headline_variant": best_name, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32/bf16 factors (per-column scaled), fp64 dense; tensor-core contractions (TF32x3 with FP32 accumulation, or exact BF16 digit planes: headline_variant)", "data": "synthetic (seeded points on the unit-cube surface)",
         "config": {"workload": "helmholtz_cube", "n": n, "wavenumber": 20.0, "eta": 3.0, "epsilon": 1e-5, "mu": mu, "l2": "inputs larger than L2 (the stored H-matrix, tens of GB)"},
         "mixed_tcgen05": {"ms": ms_tc, "rel_err_vs_fp64": err(y_tc), "phase_ms": phases(ph_tc), "kernels": "phase 1 tcgen05, phase 2 mma.sync (the default)"},
         "mixed_tcgen05_both": {"ms": ms_both, "rel_err_vs_fp64": err(y_both), "phase_ms": phases(ph_both)},

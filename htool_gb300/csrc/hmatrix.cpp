@@ -1594,18 +1594,25 @@ void HMatrix::set_tensor_core_arena(bool on) {
 
 long long HMatrix::oz_arena_need() {
     std::vector<TcBlock> blks;
-    long long panels = 0;
     if (precision_ == 0) {
         std::vector<TcSeg> segs;
         stack_tiles(p1_h, lr_h, segs, blks);
-        std::vector<OzPanel> pans;
-        for (const PanelItem &pi : pan_h)
-            pans.push_back(OzPanel{pi.off, 0, pi.row0, pi.h, pi.q0, pi.ncol});
-        std::vector<long long> poff(pans.size());
-        panels = oz_panel_bytes(pans.data(), (int)pans.size(), 8, poff.data());
     } else {
         blks = tcblk_h_;
     }
+    // phase 2: the whole panels (FP64 storage) or their dense columns
+    std::vector<OzPanel> pans;
+    for (const PanelItem &pi : pan_h) {
+        int ncol = pi.ncol;
+        if (precision_ != 0) {
+            ncol = 0;
+            while (ncol < pi.ncol && cidx_h[(std::size_t)pi.q0 + ncol] < 0)
+                ncol++;
+        }
+        pans.push_back(OzPanel{pi.off, 0, pi.row0, pi.h, pi.q0, ncol, 0, 0});
+    }
+    std::vector<long long> poff(pans.size());
+    const long long panels = oz_panel_bytes(pans.data(), (int)pans.size(), 8, poff.data());
     std::vector<long long> off(blks.size());
     return oz_arena_bytes(blks.data(), (int)blks.size(), precision_ == 0 ? 8 : 4, off.data()) + panels;
 }
@@ -1652,13 +1659,22 @@ void HMatrix::build_oz_arena() {
     ozrexp_d.alloc(blks.size() * 128);
     oza_d.alloc(bytes);
     launch_oz_pack(bd, (int)blks.size(), sd, precision_ == 0 ? fac.p : nullptr, precision_ == 0 ? nullptr : mix_.p, S, ozoff_d.p, ozrexp_d.p, oza_d.p, stream_);
-    if (precision_ == 0 && !pan_h.empty()) {
-        // phase 2: every row chunk's panel, the widest first
+    if (!pan_h.empty()) {
+        // phase 2: every row chunk's panel (FP64 storage), or its dense
+        // columns alone (reduced storage: they stay FP64 and come first in
+        // the FP64 panel, their coefficients input rows), the widest first
         std::vector<OzPanel> pans;
         pans.reserve(pan_h.size());
-        for (const PanelItem &pi : pan_h)
-            if (pi.ncol > 0)
-                pans.push_back(OzPanel{pi.off, 0, pi.row0, pi.h, pi.q0, pi.ncol, 0, 0});
+        for (const PanelItem &pi : pan_h) {
+            int ncol = pi.ncol;
+            if (precision_ != 0) {
+                ncol = 0;
+                while (ncol < pi.ncol && cidx_h[(std::size_t)pi.q0 + ncol] < 0)
+                    ncol++;
+            }
+            if (ncol > 0)
+                pans.push_back(OzPanel{pi.off, 0, pi.row0, pi.h, pi.q0, ncol, 0, 0});
+        }
         std::stable_sort(pans.begin(), pans.end(), [](const OzPanel &a, const OzPanel &b) { return a.ncol > b.ncol; });
         std::vector<long long> poff(pans.size());
         const long long pbytes = oz_panel_bytes(pans.data(), (int)pans.size(), 8, poff.data());
@@ -1789,8 +1805,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
                 launch_phase2_mma(scm_d.p, p2rcm_d.p, n_p2rc_m_, mix_.p, cidxm_d.p, w_A, w_xexp, mu, w_z, (int)zlen_, st);
             launches_ += 1;
             if (n_chunks_md_ > 0) {
-                launch_phase2_df_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xs, w_xexp, mu,
-                                      w_z, (int)zlen_, true, st);
+                dense_mrhs(w_xp, w_xs, w_xexp, w_A, w_z, mu, w_oz, st);
                 launches_ += 1;
             }
         } else if (split_dense_ && mu >= 4 && n_chunks_md_ > 0 && n_chunks_r_ > 0) {
@@ -1798,8 +1813,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
             // kernel (z cleared first, every row chunk added), then the
             // FP32 / BF16 chunks in the streamed kernel, adding onto z
             HTGPU_CUDA(cudaMemsetAsync(w_z, 0, sizeof(double) * (std::size_t)zlen_ * mu, st));
-            launch_phase2_df_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xs, w_xexp, mu, w_z,
-                                  (int)zlen_, true, st);
+            dense_mrhs(w_xp, w_xs, w_xexp, w_A, w_z, mu, w_oz, st);
             if (p2_mode_ == 1)
                 launch_phase2_producer(scr_d.p, sur_d.p, n_units_r_, tickets_d.p, mix_.p, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xp, w_xs, w_xexp, mu,
                                        w_z, (int)zlen_, status_d.p, st, p2_gmax_);
@@ -1861,7 +1875,7 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         const unsigned char *pre   = reinterpret_cast<const unsigned char *>(emu2_.p); // kStreamPre chunks
         if (many && oz_S_ == 8 && w_oz && n_ozpan_ > 0) {
             // the panels on the BF16 tensor cores
-            launch_phase2_oz(ozpan_d.p, n_ozpan_, ozgrp_d.p, ozpa_d.p, ozprexp_d.p, cidx_d.p, w_A, (int)a_slots, w_xp, *w_oz, mu, w_z, (int)zlen_, status_d.p, st);
+            launch_phase2_oz(ozpan_d.p, n_ozpan_, ozgrp_d.p, ozpa_d.p, ozprexp_d.p, cidx_d.p, w_A, (int)a_slots, w_xp, *w_oz, mu, w_z, (int)zlen_, false, status_d.p, st);
             launches_ += 2;
         } else if (many) {
             launch_phase2_df_mrhs(sc_d.p, p2rc_d.p, n_p2rc_, arena, pre, cidx_d.p, w_A, w_xs, w_xexp, mu, w_z, (int)zlen_, false, st);
@@ -1882,6 +1896,17 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
 
 // the per-cluster sums into y: every row in user or cluster numbering, or
 // (global-to-local products) the local rows only, at y[i - local offset]
+// the dense FP64 chunks of a reduced-precision product with many right-hand
+// sides, added onto z: on the digit planes (their phase 1 on the planes wrote
+// the input's exponent table) or in the double-float kernel
+void HMatrix::dense_mrhs(const double *w_xp, const F2 *w_xs, const int *w_xexp, const double *w_A, double *w_z, int mu, const OzScratch *w_oz, cudaStream_t st) {
+    if (oz_S_ == 4 && w_oz && n_ozpan_ > 0 && mu >= kMmaMinRhs && n_tcblk_ > 0)
+        launch_phase2_oz(ozpan_d.p, n_ozpan_, ozgrp_d.p, ozpa_d.p, ozprexp_d.p, cidx_d.p, nullptr, 0, w_xp, *w_oz, mu, w_z, (int)zlen_, true, status_d.p, st);
+    else
+        launch_phase2_df_mrhs(scm_d.p, p2rcm_d.p, n_p2rc_m_, reinterpret_cast<const unsigned char *>(fac.p), reinterpret_cast<const unsigned char *>(emu3_.p), cidxm_d.p, w_A, w_xs, w_xexp, mu, w_z,
+                              (int)zlen_, true, st);
+}
+
 void HMatrix::phase1_tc(const F2 *w_xs, int mu, double *w_A, cudaStream_t st) {
     float *Af = reinterpret_cast<float *>(w_A);
     if (tca_d.p)

@@ -401,6 +401,7 @@ class HMatrix {
     void build_oz_arena();
     long long oz_arena_need(); // bytes the planes of the current storage take
     void phase1_tc(const F2 *w_xs, int mu, double *w_A, cudaStream_t st); // the tcgen05 phase 1, from the arena when there is one
+    void dense_mrhs(const double *w_xp, const F2 *w_xs, const int *w_xexp, const double *w_A, double *w_z, int mu, const OzScratch *w_oz, cudaStream_t st);
     DevBuf<Tc2Slab> tc2slab_d; // tensor-core phase 2: slabs and the first slab of each group of four row chunks
     DevBuf<int> tc2g_d;
     int n_tc2_groups_ = 0;

@@ -240,7 +240,9 @@ struct OzScratch {
 // its planes, 8 planes of (h <= 16 ? 16 : 32) x 16 per 16 columns;
 // coefficients cidx[q0 ..]); oz_panel_bytes fills poff_h and returns the
 // planes' size, launch_oz_panel_pack writes them and each row's exponent
-// (prexp, 32 a panel), launch_phase2_oz writes the z rows of every panel,
+// (prexp, 32 a panel), launch_phase2_oz writes (add: adds onto) the z rows
+// of every panel (A null: panels whose coefficients are all input rows, the
+// dense blocks of reduced-precision products),
 // the coefficients cut into planes relative to each panel's and right-hand
 // side's maximum (from the group tables of the input and of the phase-1
 // sums over the panel's groups).
@@ -252,7 +254,7 @@ struct OzPanel {
 long long oz_panel_bytes(const OzPanel *panels_h, int npanels, int S, long long *poff_h);
 void launch_oz_panel_pack(const OzPanel *panels, int npanels, const double *f64, int *prexp, unsigned char *parena, cudaStream_t st);
 void launch_phase2_oz(const OzPanel *panels, int npanels, const int *groups, const unsigned char *parena, const int *prexp, const int *cidx, const double *A, int aslots, const double *xp,
-                      const OzScratch &sc, int mu, double *z, int zlen, int *status, cudaStream_t st);
+                      const OzScratch &sc, int mu, double *z, int zlen, bool add, int *status, cudaStream_t st);
 long long oz_arena_bytes(const TcBlock *blocks_h, int nblocks, int S, long long *ozoff_h);
 long long oz_xplanes_bytes(int nrows, int mu, int S);
 void launch_oz_pack(const TcBlock *blocks, int nblocks, const TcSeg *segs, const double *f64, const unsigned char *mix, int S, const long long *ozoff, int *rexp, unsigned char *arena,

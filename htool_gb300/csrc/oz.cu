@@ -901,7 +901,7 @@ constexpr int kOz2Threads = 416;
 template <int S>
 __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel *__restrict__ panels, int npanels, const int *__restrict__ groups, const unsigned char *__restrict__ parena,
                                                                    const int *__restrict__ prexp, const int *__restrict__ cidx, const double *__restrict__ A, const double *__restrict__ xp,
-                                                                   const int *__restrict__ pexp, int mu, double *__restrict__ z, int zlen, int *__restrict__ status) {
+                                                                   const int *__restrict__ pexp, int mu, double *__restrict__ z, int zlen, int add, int *__restrict__ status) {
     using C           = Oz2Cfg<S>;
     constexpr int T   = OzCfg<S>::kT;
     constexpr int NST = C::kStages;
@@ -1107,8 +1107,10 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
 #pragma unroll
                     for (int q = 0; q < 16; q++) {
                         const int r = 16 * ch + q;
-                        if (r < P.h)
-                            zc[r] = oz_i2d(((__int128)hi[q] << (7 * (S / 2))) + lo[q], k + __ldg(prexp + (long long)bi * 32 + r));
+                        if (r < P.h) {
+                            const double v = oz_i2d(((__int128)hi[q] << (7 * (S / 2))) + lo[q], k + __ldg(prexp + (long long)bi * 32 + r));
+                            zc[r]          = add ? zc[r] + v : v;
+                        }
                     }
                 }
 #pragma unroll
@@ -1235,11 +1237,12 @@ void launch_oz_panel_pack(const OzPanel *panels, int npanels, const double *f64,
 }
 
 void launch_phase2_oz(const OzPanel *panels, int npanels, const int *groups, const unsigned char *parena, const int *prexp, const int *cidx, const double *A, int aslots, const double *xp,
-                      const OzScratch &sc, int mu, double *z, int zlen, int *status, cudaStream_t st) {
+                      const OzScratch &sc, int mu, double *z, int zlen, bool add, int *status, cudaStream_t st) {
     if (npanels <= 0)
         return;
-    // the phase-1 sums' exponent table (the input's was written by launch_oz_prepare)
-    const int nga = (aslots + 31) >> 5;
+    // the phase-1 sums' exponent table (the input's was written by
+    // launch_oz_prepare); panels of input rows alone (A null) need none
+    const int nga = A ? (aslots + 31) >> 5 : 0;
     if (nga > 0) {
         const long long n = (long long)nga * mu;
         oz_xgroup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(A, aslots, mu, sc.agexp, nullptr);
@@ -1259,7 +1262,7 @@ void launch_phase2_oz(const OzPanel *panels, int npanels, const int *groups, con
             done |= 1ull << dev;
     }
     HTGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    phase2_oz_kernel<8><<<std::min(npanels, sms), kOz2Threads, Oz2Cfg<8>::kSmem, st>>>(panels, npanels, groups, parena, prexp, cidx, A, xp, sc.pexp, mu, z, zlen, status);
+    phase2_oz_kernel<8><<<std::min(npanels, sms), kOz2Threads, Oz2Cfg<8>::kSmem, st>>>(panels, npanels, groups, parena, prexp, cidx, A, xp, sc.pexp, mu, z, zlen, add ? 1 : 0, status);
     HTGPU_CUDA(cudaGetLastError());
 }
 

@@ -137,7 +137,7 @@ def test_hmatrix_fp64_digit_planes(golden):
     assert hm.get_digit_planes() == (False, 0)
     hm.set_digit_planes(True)
     on, nbytes = hm.get_digit_planes()
-    assert on and nbytes > 0 and nbytes % 32768 == 0  # 8 planes of 4 KB a slab
+    assert on and nbytes > 0 and nbytes % 4096 == 0  # planes of 4 KB (blocks) and 512 B (panels) a slab
     for mu in X:
         y = hm.mvprod_global_to_global(X[mu], mu)
         assert rel(y, base[mu]) < 1e-13, mu
@@ -161,7 +161,7 @@ def test_hmatrix_fp64_digit_planes(golden):
     assert hm.device_status() == 0
     hm.set_precision("mixed")  # four planes of the reduced factors
     on, nb4 = hm.get_digit_planes()
-    assert on and nb4 > 0 and nb4 % 16384 == 0
+    assert on and nb4 > 0 and nb4 % 4096 == 0
     hm.set_precision("fp64")
     assert hm.get_digit_planes()[1] == nbytes
     hm.set_digit_planes(False)
@@ -190,8 +190,15 @@ def test_hmatrix_mixed_digit_planes_within_epsilon(golden):
         cols = [rel(yp[c * n:(c + 1) * n], y64[c * n:(c + 1) * n]) for c in range(mu)]
         assert max(cols) < 1e-6, (mu, max(cols))
         assert rel(yp, ys) < 1e-6
-        assert hm.device_status() == 0
+        # the dense FP64 blocks first, on the planes (eight digits), against
+        # the same phase 1 with the dense blocks in the streamed kernel
+        # (FP64): the same product to FP64 accuracy
+        hm.set_phase2_dense_split(True)
+        yd = hm.mvprod_global_to_global(X, mu)
+        assert rel(yd, yp) < 1e-12, mu
+        hm.set_phase2_dense_split(False)
         hm.set_digit_planes(False)
+        assert hm.device_status() == 0
         hm.set_precision("fp64")
 
 
@@ -225,3 +232,25 @@ def test_accumulation_exact_near_2_23(staged):
     a = np.full((128, 256), v)
     b = np.full((256, 64), v)
     assert np.array_equal(oz_gemm(a, b, S, staged), model(a, b, S))
+
+
+def test_tensor_core_products_with_dense_planes():
+    """epsilon 1e-5, 64 right-hand sides: phase 1 on 4 digit planes, the
+    low-rank phase 2 on the tensor cores, the dense FP64 blocks added from 8
+    digit planes; within 1e-5 of FP64 like the default tcgen05 / mma.sync /
+    double-float path, and its dense part to FP64 accuracy"""
+    from htool_gb300 import geometry as G
+
+    n, mu = 6000, 64
+    pts = G.sphere(n, seed=47)
+    t = H.Cluster().build(n, pts)
+    hm = H.HMatrix(t, t, 1e-5, 10.0).build(H.LAPLACE, pts)
+    X = G.rhs(n, mu, seed=48)
+    y64 = hm.mvprod_global_to_global(X, mu)
+    hm.set_precision("mixed", 1.0)
+    ytc = hm.mvprod_global_to_global(X, mu)
+    hm.set_digit_planes(True)
+    yp = hm.mvprod_global_to_global(X, mu)
+    assert hm.device_status() == 0
+    assert rel(ytc, y64) < 1e-5 and rel(yp, y64) < 1e-5
+    assert rel(yp, ytc) < 2e-6
