@@ -2133,6 +2133,10 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
             p2_mode_     = arg_mode;
             best         = tbest;
             layout_gen_++;
+            // the digit planes again, now that the dense blocks may come
+            // first (on the planes when they are on)
+            if (run >= kMmaMinRhs && n_tcblk_ > 0)
+                try_digit_planes();
         }
     }
     cudaEventDestroy(e0);
