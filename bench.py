@@ -333,7 +333,7 @@ def run_gpu(args):
         if precision == "fp64" and run >= 8:
             p2 = "phase2_oz_kernel" if hm.get_digit_planes()[0] else "phase2_df_mrhs_kernel"
         else:
-            p2 = "phase2_warp_kernel" if hm.get_phase2_mode() == 0 else "phase2_ws_kernel
+            p2 = "phase2_warp_kernel" if hm.get_phase2_mode() == 0 else "phase2_ws_kernel"
         names = ["gather_split_kernel", p1, p2, "zsum_kernel"]
         k = max(range(4), key=lambda i: ph[i])
         achieved = pb[k] / (ph[k] / 1e3) / 1e9
