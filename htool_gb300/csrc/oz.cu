@@ -142,17 +142,23 @@ __device__ __forceinline__ long long oz_fixed(double v, int emax) {
     return (b >> 63) ? -q : q;
 }
 
-// balanced base-128 digits of q, d[0] the top one
+// balanced base-128 digits of q, d[0] the top one, without a carry chain:
+// adding 64 to every lower digit position (the constant 64 * (1 + 128 +
+// ... + 128^(S-2))) turns the balanced digits d in [-64, 63] into the plain
+// 7-bit fields d + 64 of q + bias, and the top digit into its arithmetic
+// shift -- the same digits as the sequential split, a shift, a mask and a
+// subtraction each
 template <int S>
 __device__ __forceinline__ void oz_digits(long long q, int (&d)[S]) {
+    long long bias = 0;
 #pragma unroll
-    for (int i = S - 1; i >= 1; i--) {
-        int lo = (int)(q & 127);
-        lo     = lo >= 64 ? lo - 128 : lo;
-        d[i]   = lo;
-        q      = (q - lo) >> 7;
-    }
-    d[0] = (int)q;
+    for (int i = 0; i < S - 1; i++)
+        bias |= 64ll << (7 * i);
+    const long long u = q + bias;
+    d[0]              = (int)(u >> (7 * (S - 1)));
+#pragma unroll
+    for (int i = 1; i < S; i++)
+        d[i] = (int)((u >> (7 * (S - 1 - i))) & 127) - 64;
 }
 
 __device__ __forceinline__ unsigned oz_bf2(int a, int b) { // two small integers as BF16 (exact)
