@@ -79,6 +79,7 @@ def parse():
     p.add_argument("--phase2-mode", type=int, default=None, help="FP64: 0 per-warp streams, 1 producer-fed")
     p.add_argument("--mixed-phase2-mode", type=int, default=None, help="mixed precision: 0 per-warp streams, 1 producer-fed")
     p.add_argument("--mixed-dense-split", type=int, default=None, help="mixed precision, 4+ right-hand sides: 1 dense chunks first in the double-float kernel")
+    p.add_argument("--tau", type=float, default=1.0, help="mixed precision: BF16 columns from the first whose storage bound is below tau * epsilon")
     p.add_argument("--digit-planes", type=int, default=None, help="8+ right-hand sides: 1 phase 1 on the BF16 tensor cores by exact digit slicing, 0 not")
     return p.parse_args()
 
@@ -373,7 +374,7 @@ def run_gpu(args):
     step64, d64 = describe(ms64, "fp64")
     e2e64 = timed_e2e()
     # mixed precision
-    tau = 1.0
+    tau = args.tau
     hm.set_precision("mixed", tau)
     if fixed:
         if args.mixed_split is not None:

@@ -254,3 +254,53 @@ def test_tensor_core_products_with_dense_planes():
     assert hm.device_status() == 0
     assert rel(ytc, y64) < 1e-5 and rel(yp, y64) < 1e-5
     assert rel(yp, ytc) < 2e-6
+
+
+def _planes_agree(hm, n, mu, seed, tol, dtype=np.float64):
+    """a product with the digit planes against the same H-matrix without"""
+    from htool_gb300 import geometry as G
+
+    X = G.rhs(n, mu, seed=seed, dtype=dtype)
+    hm.set_digit_planes(False)
+    ref = hm.mvprod_global_to_global(X, mu)
+    hm.set_digit_planes(True)
+    y = hm.mvprod_global_to_global(X, mu)
+    assert hm.device_status() == 0
+    hm.set_digit_planes(False)
+    return rel(y, ref)
+
+
+def test_digit_planes_symmetric_complex_and_rank_local(golden):
+    """the planes follow every storage the product supports: a symmetric
+    H-matrix (its twins are ordinary tiles and panel columns), the complex
+    Helmholtz H-matrix (real form, 64 right-hand sides), and the local
+    tasks of one of three MPI ranks (global-to-local product)"""
+    g, meta = golden("cyl4000_k0_symU")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    hs = H.HMatrix(t, t, meta["eps"], meta["eta"], symmetry=meta["symmetry"], UPLO=meta["uplo"])
+    hs.set_compression(meta["compressor"])
+    if meta["one_array_build"]:
+        hs.build_sym(meta["kernel"], g["xt"])
+    else:
+        hs.build(meta["kernel"], g["xt"], g["xt"])
+    # kernel 1/(1e-5 + r): dense rows span 2^17 between the diagonal and the
+    # rest, which the 54-bit row scaling costs; still the 1e-12 FP64 bar
+    assert _planes_agree(hs, n, 16, 3, 1e-12) < 1e-12
+    g, meta = golden("helmholtz_cube2000")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    hz = H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128).build(H.HELMHOLTZ, g["xt"], kernel_param=meta["wavenumber"])
+    assert _planes_agree(hz, n, 64, 4, 1e-12, dtype=np.complex128) < 1e-12
+    g, meta = golden("cyl4000_k0_ranks")
+    pts = g["points"]
+    n = pts.shape[0]
+    t = H.Cluster().build(n, pts, size_world=3)
+    hr = H.HMatrix(t, t, meta["eps"], meta["eta"]).set_local_rank(1).build(meta["kernel"], pts)
+    from htool_gb300 import geometry as G
+
+    X = G.rhs(n, 16, seed=5)
+    y0 = hr.mymvprod_global_to_local(X, 16)
+    hr.set_digit_planes(True)
+    y1 = hr.mymvprod_global_to_local(X, 16)
+    assert rel(y1, y0) < 1e-13 and hr.device_status() == 0
