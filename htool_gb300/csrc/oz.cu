@@ -186,6 +186,17 @@ __device__ __forceinline__ void oz_put8(unsigned char *planes, int plane_bytes, 
     }
 }
 
+// two consecutive K values (k even), one 4-byte store per plane
+template <int S, int T>
+__device__ __forceinline__ void oz_put2(unsigned char *planes, int plane_bytes, int row, int k, const double (&v)[2], int emax) {
+    int d[2][S];
+    oz_digits<S>(oz_fixed<T>(v[0], emax), d[0]);
+    oz_digits<S>(oz_fixed<T>(v[1], emax), d[1]);
+#pragma unroll
+    for (int s = 0; s < S; s++)
+        *reinterpret_cast<unsigned *>(planes + (size_t)s * plane_bytes + oz_off(row, k)) = oz_bf2(d[0][s], d[1][s]);
+}
+
 // four consecutive K values (k a multiple of 4), one 8-byte store per plane.
 // (Two's-complement 7-bit fields would take fewer operations than the
 // balanced digits, but their products are all of one sign and up to
@@ -889,20 +900,23 @@ struct Oz2Cfg {
     static constexpr int kB      = S * 32 * 32;     // N <= 32 rows x 16 per plane
     static constexpr int kStage  = kA + kB;
     static constexpr int kStages = 4;
-    static constexpr int kSmem   = kStages * kStage + 256;
+    static constexpr int kAcc    = 4 * 16 * 32 * 16; // the readers' 64-bit partial sums (hi, lo) between rounds
+    static constexpr int kSmem   = kStages * kStage + 256 + kAcc;
     static constexpr unsigned kCols = S * 32 <= 128 ? 128u : 256u;
 };
 
-// Thirteen warps in three roles over the same sequence of (panel, pass of
-// 64 right-hand sides, 16-column slab): warps 2 and 6-12 cut each slab's
-// coefficients into planes (thread t: right-hand side t mod 64, 4 columns;
+// Twenty-one warps in three roles over the same sequence of (panel, pass of
+// 64 right-hand sides, 16-column slab): warps 2 and 6-20 cut each slab's
+// coefficients into planes (thread t: right-hand side t mod 64, 2 columns;
 // the next slab's coefficients loaded while the current one is cut) into a
-// ring of four stages; lane 0 of warp 3 copies the panel's planes in and
-// issues the MMAs as both halves of a stage are ready; warps 0, 1, 4, 5
-// (tensor-memory lanes 0-63: the right-hand sides) add each round's
-// accumulators into exact 64-bit sums and write the z rows at the end of a
-// pass.  The exponent bounds come from pexp (oz_panel_exp_kernel).
-constexpr int kOz2Threads = 416;
+// ring of four stages -- many warps, few registers each, to hide the
+// latency of the gathered coefficients; lane 0 of warp 3 copies the panel's
+// planes in and issues the MMAs as both halves of a stage are ready; warps
+// 0, 1, 4, 5 (tensor-memory lanes 0-63: the right-hand sides) add each
+// round's accumulators into exact 64-bit sums kept in shared memory and
+// write the z rows at the end of a pass.  The exponent bounds come from
+// pexp (oz_panel_exp_kernel).
+constexpr int kOz2Threads = 672;
 
 template <int S>
 __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel *__restrict__ panels, int npanels, const int *__restrict__ groups, const unsigned char *__restrict__ parena,
@@ -912,7 +926,7 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
     constexpr int T   = OzCfg<S>::kT;
     constexpr int NST = C::kStages;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned long long *fulla = reinterpret_cast<unsigned long long *>(smem + NST * C::kStage); // [NST] coefficients cut (256 arrivals)
+    unsigned long long *fulla = reinterpret_cast<unsigned long long *>(smem + NST * C::kStage); // [NST] coefficients cut (512 arrivals)
     unsigned long long *fullb = fulla + NST;                                                    // [NST] panel planes landed
     unsigned long long *empty = fulla + 2 * NST;                                                // [NST] a stage's MMAs done
     unsigned long long *accf  = fulla + 3 * NST;                                                // a round's accumulators complete
@@ -927,7 +941,7 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
     proxy_fence();
     if (tid == 0) {
         for (int k = 0; k < NST; k++) {
-            bar_init_n(&fulla[k], 256);
+            bar_init_n(&fulla[k], 512);
             bar_init(&fullb[k]);
             bar_init(&empty[k]);
         }
@@ -1013,13 +1027,13 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
             }
         }
     } else if (wid == 2 || wid >= 6) { // coefficient stagers
-        const int t = 32 * (wid == 2 ? 0 : wid - 5) + lane, n = t & 63, k0 = (t >> 6) * 4;
+        const int t = 32 * (wid == 2 ? 0 : wid - 5) + lane, n = t & 63, k0 = (t >> 6) * 2;
         Cur c{(int)blockIdx.x, 0, 0, 0};
         load(c);
-        double v[4];
+        double v[2];
         auto loadc = [&](const Cur &k) {
 #pragma unroll
-            for (int q = 0; q < 4; q++)
+            for (int q = 0; q < 2; q++)
                 v[q] = 0.;
             if (k.bi >= npanels)
                 return;
@@ -1028,7 +1042,7 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
             if (rhs >= mu)
                 return;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
+            for (int q = 0; q < 2; q++) {
                 const int col = kOzK * k.s + k0 + q;
                 if (col < P.ncol) {
                     const int kx = __ldg(cidx + P.q0 + col);
@@ -1046,15 +1060,11 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
             }
             const int rhs = kOzN * c.p + n;
             const int e   = rhs < mu ? __ldg(pexp + (long long)c.bi * mu + rhs) : 0;
-            const int E[4] = {e, e, e, e};
-            double cur[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                cur[q] = v[q];
-            Cur nx = c;
+            double cur[2] = {v[0], v[1]};
+            Cur nx        = c;
             advance(nx);
             loadc(nx); // the next slab's coefficients fly while this one is cut
-            oz_put4<S, T>(smem + (size_t)stg * C::kStage, kOzPlaneA, n, k0, cur, E);
+            oz_put2<S, T>(smem + (size_t)stg * C::kStage, kOzPlaneA, n, k0, cur, e);
             proxy_fence();
             bar_arrive(&fulla[stg]);
             c = nx;
@@ -1063,14 +1073,16 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
         if (fail && lane == 0)
             atomicExch(status, 4);
     } else { // readers: warps 0, 1 (columns 0-15), 4, 5 (16-31)
-        const int m = 32 * (wid & 3) + lane, ch = wid >> 2;
+        const int m = 32 * (wid & 3) + lane, ch = wid >> 2, rw = 2 * ch + (wid & 3);
+        // this thread's 64-bit partial sums: hi of column q at sacc[q][lane],
+        // lo at sacc[16 + q][lane], in its warp's block
+        long long *sacc = reinterpret_cast<long long *>(smem + NST * C::kStage + 256) + (size_t)rw * 32 * 32;
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+            sacc[q * 32 + lane] = 0;
         Cur c{(int)blockIdx.x, 0, 0, 0};
         load(c);
         int rounds = 0;
-        long long hi[16], lo[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++)
-            hi[q] = lo[q] = 0;
         while (c.bi < npanels && !fail) {
             const OzPanel P = panels[c.bi];
             const int N     = P.h <= 16 ? 16 : 32;
@@ -1083,16 +1095,28 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
             fence_after();
             if (16 * ch < N) {
 #pragma unroll
-                for (int D = 0; D < S; D++) {
-                    unsigned r[16];
-                    tmem_ld16(tmem + ((unsigned)(32 * (wid & 3)) << 16) + (unsigned)(D * N + 16 * ch), r);
+                for (int h8 = 0; h8 < 2; h8++) {
+                    long long hi[8], lo[8];
 #pragma unroll
-                    for (int q = 0; q < 16; q++) {
-                        const long long a = (long long)__float2int_rn(__uint_as_float(r[q]));
-                        if (D < S / 2)
-                            hi[q] += a << (7 * (S / 2 - 1 - D));
-                        else
-                            lo[q] += a << (7 * (S - 1 - D));
+                    for (int q = 0; q < 8; q++)
+                        hi[q] = lo[q] = 0;
+#pragma unroll
+                    for (int D = 0; D < S; D++) {
+                        unsigned r[8];
+                        tmem_ld8(tmem + ((unsigned)(32 * (wid & 3)) << 16) + (unsigned)(D * N + 16 * ch + 8 * h8), r);
+#pragma unroll
+                        for (int q = 0; q < 8; q++) {
+                            const long long a = (long long)__float2int_rn(__uint_as_float(r[q]));
+                            if (D < S / 2)
+                                hi[q] += a << (7 * (S / 2 - 1 - D));
+                            else
+                                lo[q] += a << (7 * (S - 1 - D));
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        sacc[(8 * h8 + q) * 32 + lane] += hi[q];
+                        sacc[(16 + 8 * h8 + q) * 32 + lane] += lo[q];
                     }
                 }
             }
@@ -1110,18 +1134,19 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
                 if (16 * ch < N && rhs < mu) {
                     const int k = 7 * (S - 1) + __ldg(pexp + (long long)bi * mu + rhs) - 2044 - 2 * T;
                     double *zc  = z + (long long)rhs * zlen + P.row0;
-#pragma unroll
+#pragma unroll 4
                     for (int q = 0; q < 16; q++) {
                         const int r = 16 * ch + q;
                         if (r < P.h) {
-                            const double v = oz_i2d(((__int128)hi[q] << (7 * (S / 2))) + lo[q], k + __ldg(prexp + (long long)bi * 32 + r));
-                            zc[r]          = add ? zc[r] + v : v;
+                            const __int128 I = ((__int128)sacc[q * 32 + lane] << (7 * (S / 2))) + sacc[(16 + q) * 32 + lane];
+                            const double v   = oz_i2d(I, k + __ldg(prexp + (long long)bi * 32 + r));
+                            zc[r]            = add ? zc[r] + v : v;
                         }
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < 16; q++)
-                    hi[q] = lo[q] = 0;
+                for (int q = 0; q < 32; q++)
+                    sacc[q * 32 + lane] = 0;
             }
         }
         if (fail && lane == 0)
