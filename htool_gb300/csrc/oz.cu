@@ -1031,16 +1031,19 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
         Cur c{(int)blockIdx.x, 0, 0, 0};
         load(c);
         double v[2];
+        int ve = 0; // the slab's exponent bound, loaded with its coefficients
         auto loadc = [&](const Cur &k) {
 #pragma unroll
             for (int q = 0; q < 2; q++)
                 v[q] = 0.;
+            ve = 0;
             if (k.bi >= npanels)
                 return;
             const OzPanel P = panels[k.bi];
             const int rhs   = kOzN * k.p + n;
             if (rhs >= mu)
                 return;
+            ve = __ldg(pexp + (long long)k.bi * mu + rhs);
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const int col = kOzK * k.s + k0 + q;
@@ -1058,8 +1061,7 @@ __global__ void __launch_bounds__(kOz2Threads, 1) phase2_oz_kernel(const OzPanel
                 fail = true;
                 break;
             }
-            const int rhs = kOzN * c.p + n;
-            const int e   = rhs < mu ? __ldg(pexp + (long long)c.bi * mu + rhs) : 0;
+            const int e   = ve;
             double cur[2] = {v[0], v[1]};
             Cur nx        = c;
             advance(nx);
