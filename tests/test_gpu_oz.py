@@ -304,3 +304,34 @@ def test_digit_planes_symmetric_complex_and_rank_local(golden):
     hr.set_digit_planes(True)
     y1 = hr.mymvprod_global_to_local(X, 16)
     assert rel(y1, y0) < 1e-13 and hr.device_status() == 0
+
+
+def test_digit_planes_in_a_captured_batch():
+    """products on the digit planes captured into one CUDA graph (HBatch)
+    and replayed: bit for bit the direct products, FP64 and reduced"""
+    torch = pytest.importorskip("torch")
+    from htool_gb300 import geometry as G
+
+    items = []
+    for k, prec in enumerate(("fp64", "mixed")):
+        n = 3000 + 500 * k
+        pts = G.sphere(n, seed=80 + k)
+        t = H.Cluster().build(n, pts)
+        hm = H.HMatrix(t, t, 1e-6, 10.0).build(H.LAPLACE, pts)
+        hm.set_precision(prec)
+        hm.set_digit_planes(True)
+        items.append((hm, n, 16))
+    b = H.HBatch()
+    bufs = []
+    for k, (hm, n, mu) in enumerate(items):
+        x = torch.from_numpy(G.rhs(n, mu, seed=90 + k)).cuda()
+        y = torch.zeros(n * mu, dtype=torch.float64, device="cuda")
+        b.add(hm, x.data_ptr(), y.data_ptr(), mu, keep=(x, y))
+        bufs.append((x, y))
+    b.capture(nstreams=2)
+    b.launch()
+    b.sync()
+    for k, (hm, n, mu) in enumerate(items):
+        ref = hm.mvprod_global_to_global(bufs[k][0].cpu().numpy(), mu)
+        assert np.array_equal(bufs[k][1].cpu().numpy(), ref), k
+        assert hm.device_status() == 0
