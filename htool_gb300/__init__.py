@@ -662,8 +662,9 @@ class HMatrix:
         return bool(on.value), b.value
 
     def set_digit_planes(self, on):
-        """phase 1 of products with 8+ right-hand sides on the BF16 tensor
-        cores by exact digit slicing (FP64-grade for FP64 storage)"""
+        """products with 8+ right-hand sides on the BF16 tensor cores by
+        exact digit slicing: both phases of FP64 products (FP64-grade),
+        phase 1 and the dense blocks of reduced-precision ones"""
         _check(lib.htgpu_hmatrix_set_digit_planes(self.h, int(bool(on))))
         return self
 

@@ -201,11 +201,12 @@ class HMatrix {
     void set_tensor_core_arena(bool on);
     bool tensor_core_arena() const { return tc_arena_; }
     long long tensor_core_arena_bytes() const { return (long long)tca_d.n; }
-    // products with 8 or more right-hand sides: phase 1 on the BF16 tensor
-    // cores by exact digit slicing (oz.cu) -- FP64 storage with 8 digit
-    // planes (FP64-grade sums), reduced storage with 4 (exact FP32-grade
-    // sums at any epsilon) -- from a copy of the factors cut into planes
-    // (digit_plane_bytes); off by default, autotuned
+    // products with 8 or more right-hand sides on the BF16 tensor cores by
+    // exact digit slicing (oz.cu) -- FP64 storage: both phases on 8 digit
+    // planes (FP64-grade sums); reduced storage: phase 1 on 4 (exact
+    // FP32-grade sums at any epsilon) and the dense FP64 blocks on 8 -- from
+    // a copy of the factors cut into planes (digit_plane_bytes); off by
+    // default, autotuned
     void set_digit_planes(bool on);
     bool digit_planes() const { return oz_on_; }
     long long digit_plane_bytes() const { return (long long)(oza_d.n + ozpa_d.n); }

@@ -402,18 +402,19 @@ int htgpu_hmatrix_get_tensor_core_mode(htgpu_hmatrix h, int *mode);
 int htgpu_hmatrix_set_tensor_core_arena(htgpu_hmatrix h, int on);
 int htgpu_hmatrix_get_tensor_core_arena(htgpu_hmatrix h, int *on, long long *bytes);
 
-/* Phase 1 of products with 8 or more right-hand sides on the BF16 tensor
- * cores by exact digit slicing (the Ozaki scheme): every factor column and
- * right-hand side is scaled by a power of two and cut into base-128 digits
- * (8 planes for FP64 storage: 54 bits, FP64-grade sums; 4 for reduced
- * storage: 26 bits, at any epsilon), the plane products are exact integer
- * MMAs, the read-out sums them exactly in 128-bit integers.  Replaces the
- * double-float FP64 phase 1 and the reduced-precision phase-1 kernels of
- * those products.  Costs a copy of the factors cut into planes (*bytes; 0
- * while off); on after a build follows it and precision changes.  Off by
- * default; htgpu_hmatrix_autotune tries it where the planes fit in half the
- * free memory.  No counterpart in the reference (its gemm calls,
- * types/matrix.hpp:346, 380). */
+/* Products with 8 or more right-hand sides on the BF16 tensor cores by
+ * exact digit slicing (the Ozaki scheme): every factor column, panel row,
+ * right-hand side and coefficient set is scaled by a power of two and cut
+ * into base-128 digits (8 planes for FP64 data: 54 bits, FP64-grade sums;
+ * 4 for reduced-precision factors: 26 bits, at any epsilon), the plane
+ * products are exact integer MMAs, the read-out sums them exactly in
+ * 128-bit integers.  FP64 storage: both phases (replacing the double-float
+ * kernels); reduced storage: phase 1, and the dense FP64 blocks of phase 2
+ * where the dense blocks go first.  Costs a copy of the factors cut into
+ * planes (*bytes; 0 while off); on after a build follows it and precision
+ * changes.  Off by default; htgpu_hmatrix_autotune tries it where the
+ * planes fit in half the free memory.  No counterpart in the reference (its
+ * gemm calls, types/matrix.hpp:346, 380). */
 int htgpu_hmatrix_set_digit_planes(htgpu_hmatrix h, int on);
 int htgpu_hmatrix_get_digit_planes(htgpu_hmatrix h, int *on, long long *bytes);
 
