@@ -716,6 +716,42 @@ def run_helmholtz(args):
     ms_dp64, y_dp64 = timed(steps)
     ph_dp64 = hm.profile(mu, 3)
     hm.set_digit_planes(False)
+    # the native complex layout (entries at 16 bytes instead of the real
+    # form's 32) against the real form, FP64 and autotuned: one right-hand
+    # side (bandwidth-bound) and 64 (the double-float kernels; the digit
+    # planes serve the real form only)
+    def timed_on(h, m, k):
+        for _ in range(max(args.warmup, 3)):
+            h.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), m, 0, stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            h.mvprod_ptr(xd.data_ptr(), yd.data_ptr(), m, 0, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k, yd[: 2 * n * m].cpu().numpy().copy()
+
+    peak, peak_kind = measured_peaks()
+    t0 = time.perf_counter()
+    hz = H.HMatrix(t, t, 1e-5, 3.0, device=local, dtype=np.complex128, complex_layout="native").build(H.HELMHOLTZ, pts, kernel_param=20.0)
+    build_native_s = time.perf_counter() - t0
+    single = {}
+    for name, h in (("real_form", hm), ("native", hz)):
+        h.autotune(1, 5)
+        ms1, y1 = timed_on(h, 1, max(steps, 10))
+        ph1 = h.profile(1, 5)
+        b = h.precision_info()["stored_bytes"]
+        single[name] = {"ms": ms1, "stored_bytes": b, "GB_per_s_stored": b / (ms1 * 1e-3) / 1e9, "frac_of_hbm_peak": b / (ms1 * 1e-3) / 1e9 / peak, "peak": peak_kind,
+                        "phase_ms": {"gather": ph1[0], "phase1": ph1[1], "phase2": ph1[2], "sums": ph1[3], "total": ph1[4]}, "y": y1}
+    single["native"]["rel_err_vs_real_form"] = float(np.linalg.norm(single["native"]["y"] - single["real_form"]["y"]) / np.linalg.norm(single["real_form"]["y"]))
+    for v in single.values():
+        del v["y"]
+    ms64n, y64n = timed_on(hz, mu, min(steps, 3))
+    native = {"build_seconds": build_native_s, "one_rhs": single, "speedup_one_rhs": single["real_form"]["ms"] / single["native"]["ms"],
+              "fp64_64rhs": {"ms": ms64n, "rel_err_vs_fp64": float(np.linalg.norm(y64n - y64) / np.linalg.norm(y64))},
+              "status": hz.device_status()}
+    del hz
     ck = clocks.stop()
     status = hm.device_status()
     info = hm.get_infos()
@@ -737,6 +773,7 @@ def run_helmholtz(args):
         "mixed_digit_planes": {"ms": ms_dpm, "rel_err_vs_fp64": err(y_dpm), "phase_ms": phases(ph_dpm), "kernels": "phase 1 on 4 BF16 digit planes (exact sums), phase 2 mma.sync"},
         "fp64_digit_planes": {"ms": ms_dp64, "rel_err_vs_fp64": err(y_dp64), "phase_ms": phases(ph_dp64), "plane_bytes": planes64, "kernels": "both phases on 8 BF16 digit planes (exact sums)"},
         "fp64": {"ms": ms64, "phase_ms": phases(ph64)},
+        "fp64_native_complex_layout": native,
         "build_seconds": build_s, "clocks": ck, "device_status": status,
         "hmatrix": {k: info[k] for k in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_mean", "Compression_ratio")},
     }

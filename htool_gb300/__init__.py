@@ -124,6 +124,8 @@ def _load():
         "htgpu_hmatrix_set_tensor_core_mode": (i, [vp, i]),
         "htgpu_hmatrix_get_tensor_core_mode": (i, [vp, vp]),
         "htgpu_debug_oz_gemm": (i, [i, i, i, i, i, vp, vp, vp]),
+        "htgpu_hmatrix_set_complex_layout": (i, [vp, i]),
+        "htgpu_hmatrix_get_complex_layout": (i, [vp, vp]),
         "htgpu_hmatrix_set_digit_planes": (i, [vp, i]),
         "htgpu_hmatrix_get_digit_planes": (i, [vp, vp, vp]),
         "htgpu_hmatrix_set_tensor_core_arena": (i, [vp, i]),
@@ -441,13 +443,18 @@ class HMatrix:
     partialACA compression unless set_compression says otherwise; symmetry
     'S' with UPLO 'U' or 'L' stores one triangle."""
 
-    def __init__(self, cluster_tree_t, cluster_tree_s, epsilon=1e-6, eta=10.0, symmetry="N", UPLO="N", device=0, dtype=np.float64):
+    def __init__(self, cluster_tree_t, cluster_tree_s, epsilon=1e-6, eta=10.0, symmetry="N", UPLO="N", device=0, dtype=np.float64, complex_layout="real"):
         self.t, self.s = cluster_tree_t, cluster_tree_s
         self.complex = np.dtype(dtype) == np.complex128
+        if complex_layout not in ("real", "native"):
+            raise ValueError("complex_layout must be 'real' or 'native'")
         h = C.c_void_p()
         create = lib.htgpu_hmatrix_create_complex if self.complex else lib.htgpu_hmatrix_create
         _check(create(cluster_tree_t.h, cluster_tree_s.h, float(epsilon), float(eta), int(device), C.byref(h)))
         self.h = h
+        if complex_layout == "native":
+            # complex factors at 16 bytes an entry instead of the real form's 32
+            _check(lib.htgpu_hmatrix_set_complex_layout(self.h, 1))
         self.epsilon, self.eta = epsilon, eta
         if symmetry != "N" or UPLO != "N":
             _check(lib.htgpu_hmatrix_set_symmetry(self.h, symmetry.encode(), UPLO.encode()))
@@ -660,6 +667,12 @@ class HMatrix:
         on, b = C.c_int(), C.c_longlong()
         _check(lib.htgpu_hmatrix_get_tensor_core_arena(self.h, C.byref(on), C.byref(b)))
         return bool(on.value), b.value
+
+    def get_complex_layout(self):
+        """'native' (complex entries at 16 bytes) or 'real' (the real form)."""
+        v = C.c_int()
+        _check(lib.htgpu_hmatrix_get_complex_layout(self.h, C.byref(v)))
+        return "native" if v.value else "real"
 
     def set_digit_planes(self, on):
         """products with 8+ right-hand sides on the BF16 tensor cores by

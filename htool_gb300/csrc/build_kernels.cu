@@ -757,12 +757,42 @@ __global__ void pack_z_kernel(const PackItem *__restrict__ items, const double *
     }
 }
 
+// complex crosses -> the native complex layout: Re U and Im U (M x r each,
+// column-major) at dst_u, and at dst_v the 2N x r tile whose rows 2j and
+// 2j + 1 hold the real and imaginary parts of Vt[j, :]
+__global__ void pack_zn_kernel(const PackItem *__restrict__ items, const double *__restrict__ scratch, double *__restrict__ arena) {
+    const PackItem it = items[blockIdx.x];
+    const int M = it.M, N = it.N, r = it.r; // complex sizes
+    const zd *U = reinterpret_cast<const zd *>(scratch + it.src_u);
+    const zd *V = reinterpret_cast<const zd *>(scratch + it.src_v);
+    double *Ur = arena + it.dst_u, *Ui = Ur + (size_t)M * r, *V2 = arena + it.dst_v;
+    for (long long e = threadIdx.x; e < (long long)M * r; e += blockDim.x) {
+        const zd u = U[e];
+        Ur[e]      = u.re;
+        Ui[e]      = u.im;
+    }
+    for (long long e = threadIdx.x; e < 2LL * N * r; e += blockDim.x) {
+        const int row = (int)(e % (2 * N)), k = (int)(e / (2 * N));
+        const zd v    = V[row / 2 + (size_t)N * k];
+        V2[e]         = (row & 1) ? v.im : v.re;
+    }
+}
+
 // dense leaves of a complex matrix in real form: rows / columns are indices
 // of the doubled numbering, whose permutation keeps the component (2p + c)
 __global__ void dense_fill_z_kernel(const DenseChunk *__restrict__ chunks, const double *__restrict__ xt, const double *__restrict__ xs, const int *__restrict__ perm_t, const int *__restrict__ perm_s,
                                     KernelDesc kd, double *__restrict__ arena) {
     const DenseChunk C = chunks[blockIdx.x];
     const int hn       = C.h * C.n;
+    if (C.mode == kDenseNative) { // rows of the points, columns of the doubled numbering
+        for (int e = threadIdx.x; e < hn; e += blockDim.x) {
+            const int i = e % C.h, j = e / C.h;
+            const int pi = perm_t[C.row0 + i], pj = perm_s[C.oj + j];
+            const zd z   = kernel_entry_z(kd, xt + 3 * (size_t)pi, xs + 3 * (size_t)(pj >> 1));
+            arena[C.dst + e] = (pj & 1) ? z.im : z.re;
+        }
+        return;
+    }
     for (int e = threadIdx.x; e < hn; e += blockDim.x) {
         const int i = e % C.h, j = e / C.h;
         const int pi = perm_t[C.row0 + i], pj = perm_s[C.oj + j];
@@ -835,6 +865,13 @@ void launch_pack_z(const PackItem *items, int nitems, const double *scratch, dou
     if (nitems <= 0)
         return;
     pack_z_kernel<<<nitems, 128, 0, st>>>(items, scratch, arena);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_pack_zn(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st) {
+    if (nitems <= 0)
+        return;
+    pack_zn_kernel<<<nitems, 128, 0, st>>>(items, scratch, arena);
     HTGPU_CUDA(cudaGetLastError());
 }
 

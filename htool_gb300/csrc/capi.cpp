@@ -241,6 +241,21 @@ int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilo
     });
 }
 
+int htgpu_hmatrix_set_complex_layout(htgpu_hmatrix h, int native) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        h->h->set_complex_layout(native != 0);
+    });
+}
+
+int htgpu_hmatrix_get_complex_layout(htgpu_hmatrix h, int *native) {
+    return guarded([&] {
+        need(h, "hmatrix");
+        need(native, "native");
+        *native = h->h->complex_native() ? 1 : 0;
+    });
+}
+
 int htgpu_hmatrix_destroy(htgpu_hmatrix h) {
     return guarded([&] { delete h; });
 }
@@ -465,7 +480,7 @@ int htgpu_hmatrix_get_phase2_dense_split(htgpu_hmatrix h, int *on) {
 int htgpu_hmatrix_local(htgpu_hmatrix h, int *rank, int *local_offset, int *local_size) {
     return guarded([&] {
         need(h, "hmatrix");
-        const int f = h->h->is_complex() ? 2 : 1; // complex handles count complex rows
+        const int f = h->h->is_complex() && !h->h->complex_native() ? 2 : 1; // complex handles count complex rows
         if (rank)
             *rank = h->h->local_rank();
         if (local_offset)
@@ -478,8 +493,8 @@ int htgpu_hmatrix_local(htgpu_hmatrix h, int *rank, int *local_offset, int *loca
 int htgpu_hmatrix_sizes(htgpu_hmatrix h, int *nr, int *nc, int *nlr, int *ndense) {
     return guarded([&] {
         need(h, "hmatrix");
-        if (nr)
-            *nr = h->h->nb_rows();
+        if (nr) // the native complex layout's rows are the points: twice that many doubles
+            *nr = h->h->nb_rows() * (h->h->complex_native() ? 2 : 1);
         if (nc)
             *nc = h->h->nb_cols();
         if (nlr)
@@ -799,6 +814,8 @@ int htgpu_hmatrix_mvprod_noalloc(htgpu_hmatrix h, const double *in, double *out,
     return guarded([&] {
         if (h == nullptr)
             throw htgpu::Error(HTGPU_ERR_INVALID, "[Htool error] hmatrix is null");
+        if (h->h->complex_native())
+            throw htgpu::Error(HTGPU_ERR_UNSUPPORTED, "[Htool error] the allocation-free product is not available with the native complex layout");
         h->h->mvprod_noalloc(in, out, mu, (cudaStream_t)stream);
     });
 }

@@ -132,6 +132,8 @@ void HMatrix::set_symmetry(char symmetry, char uplo) {
             "Invalid arguments to create HMatrix: symmetry must be 'N' with UPLO 'N', or 'S'/'H' with UPLO 'U' or 'L'");
     require(symmetry != 'H' || complex_, "Hermitian H-matrices ('H') need a complex type", 2);
     if (symmetry != 'N')
+        require_real_form("a symmetric H-matrix");
+    if (symmetry != 'N')
         require(T->n == S->n && T->perm == S->perm, "a symmetric H-matrix needs the same target and source cluster tree");
     symmetry_ = symmetry;
     uplo_     = uplo;
@@ -149,6 +151,8 @@ void HMatrix::set_local_rank(int rank) {
 // conj(B^T)) and complete the diagonal blocks from their UPLO triangle with
 // a real diagonal, as hemv / hemm read them (matrix.hpp:386-447)
 int HMatrix::dense_mode(int d) const {
+    if (znative_)
+        return kDenseNative;
     if (!complex_ || symmetry_ != 'H')
         return kDenseAsIs;
     const DenseLeaf &D = dn_h[d];
@@ -159,8 +163,27 @@ int HMatrix::dense_mode(int d) const {
 
 void HMatrix::set_compression(int compressor) {
     require(compressor == 0 || compressor == 1, "compression must be 0 (partialACA) or 1 (sympartialACA)");
+    if (compressor != 0)
+        require_real_form("sympartialACA");
     compression_ = compressor;
 }
+
+void HMatrix::set_complex_layout(bool native) {
+    require(complex_ || !native, "the native complex layout needs a complex H-matrix", 2);
+    if (native == znative_)
+        return;
+    require(lr_h.empty() && dn_h.empty(), "the complex layout is chosen before the H-matrix is built", 2);
+    require(!native || (symmetry_ == 'N' && compression_ == 0), "the native complex layout holds non-symmetric H-matrices compressed by partialACA", 2);
+    HTGPU_CUDA(cudaSetDevice(device_));
+    znative_ = native;
+    T        = native ? Tz_ : std::make_shared<const ClusterTree>(double_tree(*Tz_));
+    nr       = T->n;
+    perm_t.upload(T->perm, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    mu_cap = 0; // the work buffers follow the row count
+}
+
+void HMatrix::require_real_form(const char *what) const { require(!znative_, std::string(what) + " is not available with the native complex layout", 2); }
 
 // transposed twins of the off-diagonal leaves of a symmetric H-matrix,
 // after htool's own leaves: the twin of a low-rank leaf reads the same
@@ -211,9 +234,15 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
     const KernelDesc kd = kdp ? *kdp : KernelDesc{kHostKernelId, 0.};
     nlr_stored_ = ndn_stored_ = -1;
     // block tree and ACA on the trees of the points; a complex H-matrix is
-    // stored in real form on doubled trees (T, S), its leaves scaled by f
+    // stored in real form on doubled trees (T, S), its leaves scaled by f,
+    // or in the native layout on the points' target tree (rows and ranks
+    // scaled by ft = 1) and the doubled source tree
     const ClusterTree &Ta = complex_ ? *Tz_ : *T, &Sa = complex_ ? *Sz_ : *S;
     const int f           = complex_ ? 2 : 1;
+    const int ft          = znative_ ? 1 : f;
+    const long long fu    = znative_ ? 2 : (long long)f * f; // stored doubles per complex factor entry
+    if (znative_)
+        require(symmetry_ == 'N' && compression_ == 0, "the native complex layout holds non-symmetric H-matrices compressed by partialACA", 2);
     HTGPU_CUDA(cudaSetDevice(device_));
     st_             = BuildStats();
     samples_x_.clear();
@@ -476,9 +505,9 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
                     it.N     = blocks[b].N;
                     it.r     = r;
                     it.pad   = 0;
-                    it.dst_u = packed; // real form: f M x f r and f N x f r
-                    it.dst_v = packed + (long long)f * f * it.M * r;
-                    packed += (long long)f * f * r * (it.M + it.N);
+                    it.dst_u = packed; // real form: f M x f r and f N x f r; native: 2 M x r and 2 N x r
+                    it.dst_v = packed + fu * it.M * r;
+                    packed += fu * r * (it.M + it.N);
                     items.push_back(it);
                     if ((int)b < n_direct)
                         acc.push_back({id, round, r, it.dst_u, it.dst_v, 0});
@@ -503,7 +532,9 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
             if (!items.empty()) {
                 DevBuf<PackItem> ditems;
                 ditems.upload(items, stream_);
-                if (complex_)
+                if (znative_)
+                    launch_pack_zn(ditems.p, (int)items.size(), scratch.p, buf->p, stream_);
+                else if (complex_)
                     launch_pack_z(ditems.p, (int)items.size(), scratch.p, buf->p, stream_);
                 else
                     launch_pack_factors(ditems.p, (int)items.size(), scratch.p, buf->p, stream_);
@@ -556,11 +587,11 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
     for (auto &a : acc) {
         const ClusterNode &tn = Ta.nodes[reqs[a.req].t], &sn = Sa.nodes[reqs[a.req].s];
         LrLeaf L;
-        L.oi    = f * tn.offset;
+        L.oi    = ft * tn.offset;
         L.oj    = f * sn.offset;
-        L.m     = f * tn.size;
+        L.m     = ft * tn.size;
         L.n     = f * sn.size;
-        L.r     = f * a.r;
+        L.r     = ft * a.r;
         L.nch   = 0;
         L.a_off = 0;
         lr_h.push_back(L);
@@ -574,7 +605,7 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
     });
     dn_h.clear();
     for (auto &d : dense_ts)
-        dn_h.push_back({f * Ta.nodes[d.first].offset, f * Sa.nodes[d.second].offset, f * Ta.nodes[d.first].size, f * Sa.nodes[d.second].size});
+        dn_h.push_back({ft * Ta.nodes[d.first].offset, f * Sa.nodes[d.second].offset, ft * Ta.nodes[d.first].size, f * Sa.nodes[d.second].size});
     if (symmetry_ != 'N')
         add_symmetric_twins(lr_src);
     std::vector<const double *> bufs;
@@ -616,6 +647,7 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
 }
 
 void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dn) {
+    require_real_form("adopting leaves");
     nlr_stored_ = ndn_stored_ = -1;
     HTGPU_CUDA(cudaSetDevice(device_));
     lr_h.clear();
@@ -714,8 +746,10 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     long long off = 0;
     std::vector<std::vector<BlockCopy>> copies(bufs.size());
     std::vector<DenseChunk> fills;
-    // phase-1 tiles
+    // phase-1 tiles; in the native complex layout every leaf's sums a are
+    // followed by r slots for i a (filled between the phases; Im U applies them)
     p1_h.clear();
+    rot_h.clear();
     a_slots = 0;
     for (int l = 0; l < (int)lr_h.size(); l++) {
         LrLeaf &L = lr_h[l];
@@ -726,6 +760,11 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
         L.nch   = (L.n + kPhase1Chunk - 1) / kPhase1Chunk;
         L.a_off = a_slots;
         a_slots += (long long)L.nch * L.r;
+        if (znative_) {
+            for (int k = 0; k < L.r; k++)
+                rot_h.push_back(make_int2((int)(L.a_off + k), (int)(a_slots + k)));
+            a_slots += L.r;
+        }
         for (int ch = 0; ch < L.nch; ch++) {
             P1Item it;
             it.j0    = ch * kPhase1Chunk;
@@ -775,22 +814,26 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
         zlen_ += groups[g].second;
     }
     // sizes of every group's row chunks (first pass), then every list filled
-    // at its own positions in parallel (second pass)
+    // at its own positions in parallel (second pass); a low-rank leaf of the
+    // native complex layout gives two contributions (Re U on a, Im U on i a)
     const std::size_t ng = gorder.size();
+    const int lr_parts   = znative_ ? 2 : 1;
     std::vector<long long> g_off(ng + 1, 0), g_c(ng + 1, 0), g_q(ng + 1, 0), g_p(ng + 1, 0);
     for (std::size_t gi = 0; gi < ng; gi++) {
         const int g = gorder[gi], m = groups[g].second;
         const int nchunk = (m + kRowChunk - 1) / kRowChunk;
-        long long width = 0;
-        for (int leaf : members[g])
-            width += leaf >= 0 ? lr_h[leaf].r : dn_h[~leaf].n;
+        long long width = 0, ncontrib = 0;
+        for (int leaf : members[g]) {
+            width += leaf >= 0 ? lr_parts * lr_h[leaf].r : dn_h[~leaf].n;
+            ncontrib += leaf >= 0 ? lr_parts : 1;
+        }
         long long bytes = 0;
         for (int q = 0; q < nchunk; q++) {
             const int lo = (int)((long long)m * q / nchunk), hi = (int)((long long)m * (q + 1) / nchunk);
             bytes += even((long long)(hi - lo) * width);
         }
         g_off[gi + 1] = g_off[gi] + bytes;
-        g_c[gi + 1]   = g_c[gi] + (long long)nchunk * (long long)members[g].size();
+        g_c[gi + 1]   = g_c[gi] + (long long)nchunk * ncontrib;
         g_q[gi + 1]   = g_q[gi] + (long long)nchunk * width;
         g_p[gi + 1]   = g_p[gi] + nchunk;
     }
@@ -832,11 +875,21 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
                     pc.off = poff + (long long)it.h * col;
                     if (leaf >= 0) {
                         const LrLeaf &L = lr_h[leaf];
-                        pc.w            = L.r;
-                        pc.aux          = (int)L.a_off;
-                        my_copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + lo, pc.off, it.h, L.r, L.m, lr_src[leaf].neg ? 1 | (lo & 1) << 1 : 0});
-                        for (int k = 0; k < L.r; k++)
-                            cidx_h[(std::size_t)qpos++] = (int)L.a_off + k;
+                        for (int part = 0; part < lr_parts; part++) {
+                            const long long slot = part ? L.a_off + (long long)L.nch * L.r : L.a_off; // i a after the tiles' sums
+                            pc.off               = poff + (long long)it.h * col;
+                            pc.w                 = L.r;
+                            pc.aux               = (int)slot;
+                            my_copies[lr_src[leaf].buf].push_back({lr_src[leaf].su + (long long)part * L.m * L.r + lo, pc.off, it.h, L.r, L.m, lr_src[leaf].neg ? 1 | (lo & 1) << 1 : 0});
+                            for (int k = 0; k < L.r; k++)
+                                cidx_h[(std::size_t)qpos++] = (int)slot + k;
+                            if (part + 1 < lr_parts) { // the last part is recorded below
+                                col += pc.w;
+                                c_h[(std::size_t)cpos]    = pc;
+                                c_leaf[(std::size_t)cpos] = leaf;
+                                cpos++;
+                            }
+                        }
                     } else {
                         const DenseLeaf &D = dn_h[~leaf];
                         pc.w               = D.n;
@@ -953,6 +1006,7 @@ void HMatrix::finalize(const std::vector<const double *> &bufs, const std::vecto
     emu_fresh_ = false; // fac was rewritten
     upload_phase1_lists();
     lr_d.upload(lr_h, stream_);
+    rot_d.upload(rot_h, stream_);
     {
         std::vector<int> padded = cidx_h; // bulk copies read whole 16-byte words
         padded.resize(cidx_h.size() + 4, 0);
@@ -984,6 +1038,10 @@ void HMatrix::ensure_work(int mu) {
     z.alloc((std::size_t)std::max<long long>(zlen_, 1) * mu);
     xstage.alloc((std::size_t)nc * mu);
     ystage.alloc((std::size_t)nr * mu);
+    if (znative_) { // the real form of a complex input and output (mu real columns)
+        zw_.alloc((std::size_t)nc * mu);
+        zy_.alloc((std::size_t)nr * mu);
+    }
     mu_cap = mu;
     ensure_oz_work(mu);
 }
@@ -995,6 +1053,31 @@ void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, int 
     HTGPU_CUDA(cudaSetDevice(device_));
     if (!st)
         st = stream_;
+    if (znative_) {
+        // complex x (nc / 2 points) -> its real form w, the real product with
+        // 2 mu right-hand sides, its output -> complex y (nr points)
+        require(numbering == kUserNumbering, "the native complex layout takes products in user numbering", 2);
+        ensure_work(rhs_run(2 * mu));
+        const double *x = in;
+        double *y       = out;
+        if (host_ptrs) {
+            HTGPU_CUDA(cudaMemcpyAsync(xstage.p, in, sizeof(double) * (std::size_t)nc * mu, cudaMemcpyHostToDevice, st));
+            x = xstage.p;
+            y = ystage.p;
+        }
+        launch_zin(x, nc / 2, mu, zw_.p, st);
+        launch_product(zw_.p, zy_.p, 2 * mu, kUserNumbering, st);
+        launch_zout(zy_.p, nr, mu, y, st);
+        launches_ += 2;
+        if (host_ptrs) {
+            HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * 2 * (std::size_t)nr * mu, cudaMemcpyDeviceToHost, st));
+            HTGPU_CUDA(cudaStreamSynchronize(st));
+            int status = 0;
+            HTGPU_CUDA(cudaMemcpy(&status, status_d.p, sizeof(int), cudaMemcpyDeviceToHost));
+            require(status == 0, "a device wait of the product ran out (status " + std::to_string(status) + ")", 3);
+        }
+        return;
+    }
     ensure_work(rhs_run(mu));
     const double *x = in;
     double *y       = out;
@@ -1355,6 +1438,8 @@ void HMatrix::set_rhs_bucket(int mu, int mu_run) {
 void HMatrix::set_precision(int policy, double tau) {
     layout_gen_++; // buffers or launch lists change: captured products are stale
     require(policy >= 0 && policy <= 3, "precision policy must be 0 (FP64), 1 (FP32), 2 (FP32/BF16) or 3 (BF16)");
+    if (policy != 0)
+        require_real_form("reduced-precision storage");
     require(tau > 0, "tau must be positive");
     HTGPU_CUDA(cudaSetDevice(device_));
     precision_ = policy;
@@ -1708,6 +1793,8 @@ void HMatrix::build_oz_arena() {
 }
 
 void HMatrix::set_digit_planes(bool on) {
+    if (on)
+        require_real_form("the digit planes");
     HTGPU_CUDA(cudaSetDevice(device_));
     layout_gen_++; // captured products are stale
     oz_on_ = on;
@@ -1868,6 +1955,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         launch_reduce_tiles(lr_d.p, multi_d.p, (int)multi_h.size(), mu, w_A, st);
         launches_++;
     }
+    if (!rot_h.empty()) { // native complex layout: i times the sums, which Im U applies
+        launch_rotate_slots(rot_d.p, (long long)rot_h.size(), mu, w_A, st);
+        launches_++;
+    }
     if (marks)
         HTGPU_CUDA(cudaEventRecord(marks[1], st));
     {
@@ -1953,6 +2044,8 @@ void HMatrix::set_presplit(bool on) {
 
 void HMatrix::autotune(int mu, int reps, float *best_ms) {
     HTGPU_CUDA(cudaSetDevice(device_));
+    if (znative_)
+        mu *= 2; // the real product behind mu complex right-hand sides
     int bucket = 1; // the power of two a product with mu right-hand sides may be padded to
     while (bucket < mu)
         bucket <<= 1;
@@ -1978,6 +2071,8 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
     // where its planes fit in half the free memory; `best` is the time of
     // the current configuration
     auto try_digit_planes = [&]() {
+        if (znative_)
+            return;
         const bool was = oz_on_;
         if (!was) {
             std::size_t fr = 0, tot = 0;
@@ -2147,6 +2242,8 @@ void HMatrix::autotune(int mu, int reps, float *best_ms) {
 
 void HMatrix::profile(int mu, int reps, float *ms) {
     HTGPU_CUDA(cudaSetDevice(device_));
+    if (znative_)
+        mu *= 2; // the real product behind mu complex right-hand sides (without the complex input / output steps)
     ensure_work(rhs_run(mu));
     cudaEvent_t ev[5];
     for (auto &e : ev)
@@ -2181,6 +2278,7 @@ void HMatrix::phase_bytes(int mu, long long *b) const {
 }
 
 void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st) {
+    require_real_form("the transposed product");
     if (symmetry_ == 'S') { // H^T = H
         mvprod(in, out, mu, host_ptrs, false, st);
         return;
@@ -2291,6 +2389,7 @@ void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {
 
 // inverse of the final layout, into htool's layouts
 void HMatrix::export_factors(double *uv, double *dn) {
+    require_real_form("exporting the factors");
     HTGPU_CUDA(cudaSetDevice(device_));
     std::vector<double> host(std::max<long long>(arena_len, 1));
     if (arena_len)
@@ -2344,8 +2443,8 @@ void HMatrix::export_factors(double *uv, double *dn) {
 
 long long HMatrix::stored_bytes() const {
     long long b = 0;
-    for (auto &L : lr_h)
-        b += 8LL * L.r * (L.m + L.n);
+    for (auto &L : lr_h) // the native complex layout stores Re U and Im U
+        b += 8LL * L.r * ((znative_ ? 2 : 1) * (long long)L.m + L.n);
     for (auto &D : dn_h)
         b += 8LL * D.m * D.n;
     return b;
@@ -2359,10 +2458,11 @@ std::map<std::string, std::string> HMatrix::infos() const {
 
     std::map<std::string, std::string> m;
     // a complex H-matrix reports its complex sizes and ranks (stored in real
-    // form: every size doubled, every block four times larger)
-    const int f = complex_ ? 2 : 1;
+    // form: every size and rank doubled; in the native layout: the source
+    // sizes doubled): target, source and rank factors
+    const int ft = complex_ && !znative_ ? 2 : 1, fs = complex_ ? 2 : 1, fr = ft;
     const ClusterTree &Ti = complex_ ? *Tz_ : *T, &Si = complex_ ? *Sz_ : *S;
-    const int nri = nr / f, nci = nc / f;
+    const int nri = nr / ft, nci = nc / fs;
     const std::size_t big = (std::size_t)std::max(nr, nc);
     std::size_t dmax = 0, dmin = big, lmax = 0, lmin = big, rmax = 0, rmin = big;
     double dmean = 0, lmean = 0, rmean = 0;
@@ -2370,13 +2470,13 @@ std::map<std::string, std::string> HMatrix::infos() const {
     const std::vector<DenseLeaf> dns(dn_h.begin(), dn_h.begin() + n_dense());
     const std::vector<LrLeaf> lrs(lr_h.begin(), lr_h.begin() + n_lowrank());
     for (auto &D : dns) {
-        std::size_t s = (std::size_t)D.m * D.n / (f * f);
+        std::size_t s = (std::size_t)(D.m / ft) * (D.n / fs);
         dmax          = std::max(dmax, s);
         dmin          = std::min(dmin, s);
         dmean += s;
     }
     for (auto &L : lrs) {
-        std::size_t s = (std::size_t)L.m * L.n / (f * f), r = (std::size_t)L.r / f;
+        std::size_t s = (std::size_t)(L.m / ft) * (L.n / fs), r = (std::size_t)L.r / fr;
         lmax          = std::max(lmax, s);
         lmin          = std::min(lmin, s);
         lmean += s;
@@ -2388,14 +2488,15 @@ std::map<std::string, std::string> HMatrix::infos() const {
     dmean = nd ? dmean / nd : 0;
     lmean = nl ? lmean / nl : 0;
     rmean = nl ? rmean / nl : 0;
+    // entries in complex units for a complex H-matrix
     double compressed = 0;
     for (auto &L : lrs)
-        compressed += (double)L.r * ((double)L.m + (double)L.n);
+        compressed += (double)(L.r / fr) * ((double)(L.m / ft) + (double)(L.n / fs));
     for (auto &D : dns) { // a symmetric H-matrix counts its square diagonal blocks once (hmatrix.hpp:1615-1619)
-        const double dm = (double)(D.m / f), dn = (double)(D.n / f); // complex sizes
-        compressed += f * f * ((symmetry_ != 'N' && D.oi == D.oj && D.m == D.n) ? dm * (dn + 1) / 2 : dm * dn);
+        const double dm = (double)(D.m / ft), dn = (double)(D.n / fs);
+        compressed += (symmetry_ != 'N' && D.oi == D.oj && D.m == D.n) ? dm * (dn + 1) / 2 : dm * dn;
     }
-    const double uncompressed = (double)((long)nr) * nc;
+    const double uncompressed = (double)nri * nci;
     m["Source_size"]              = inum(nci);
     m["Target_size"]              = inum(nri);
     m["Dimension"]                = "1";
@@ -2429,10 +2530,10 @@ std::map<std::string, std::string> HMatrix::infos() const {
     m["Blocks_max"]               = num(st_.build_seconds - st_.block_tree_seconds);
     m["Blocks_mean"]              = num(st_.build_seconds - st_.block_tree_seconds);
     m["Number_of_MPI_tasks"]      = "1";
-    m["Local_size_max"]           = inum(nr / (complex_ ? 2 : 1));
-    m["Local_size_mean"]          = num(nr / (complex_ ? 2 : 1));
-    m["Local_size_min"]           = inum(nr / (complex_ ? 2 : 1));
-    m["GPU_complex"]              = inum(complex_ ? 1 : 0);
+    m["Local_size_max"]           = inum(nri);
+    m["Local_size_mean"]          = num(nri);
+    m["Local_size_min"]           = inum(nri);
+    m["GPU_complex"]              = inum(complex_ ? (znative_ ? 2 : 1) : 0);
     m["GPU_aca_rounds"]           = num(st_.aca_rounds);
     m["GPU_aca_scratch_bytes"]      = inum(st_.aca_scratch_bytes);
     m["GPU_aca_peak_scratch_bytes"] = inum(st_.aca_peak_scratch_bytes);

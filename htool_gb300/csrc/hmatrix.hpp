@@ -86,6 +86,16 @@ class HMatrix {
     // entry z -> [[re, -im], [im, re]]; vectors as interleaved re, im)
     HMatrix(std::shared_ptr<const ClusterTree> t, std::shared_ptr<const ClusterTree> s, double eps, double eta, int device, bool complex = false);
     bool is_complex() const { return complex_; }
+    // the layout of a complex H-matrix, chosen before its build: false the
+    // real form above (every storage policy, symmetric H-matrices,
+    // transposed products); true the native complex layout at half the
+    // bytes: the target rows are the points, the source rows doubled (point
+    // p as x_p and i x_p), a leaf U Vt^T stored as Re U, Im U and one tile of
+    // (Re, Im) Vt row pairs, a dense block D as its (Re, Im) column pairs, and
+    // a product with mu right-hand sides runs as the real one with 2 mu
+    // (FP64 storage, 'N' symmetry, partialACA, user numbering)
+    void set_complex_layout(bool native);
+    bool complex_native() const { return znative_; }
     ~HMatrix();
 
     // HMatrix::build(gen, xt, xs) with a built-in device generator
@@ -342,6 +352,13 @@ class HMatrix {
     unsigned long long layout_gen_ = 0;
     bool complex_ = false;
     std::shared_ptr<const ClusterTree> Tz_, Sz_; // complex: the trees of the points
+    // native complex layout: the (sums, i times the sums) slot pairs filled
+    // between the phases, and the products' complex input / output in real form
+    bool znative_ = false;
+    std::vector<int2> rot_h;
+    DevBuf<int2> rot_d;
+    DevBuf<double> zw_, zy_;
+    void require_real_form(const char *what) const;
     std::unique_ptr<HMatrix> transp_; // transposed twin, built on first use
     long long aca_budget_ = 0;
     Mlp *predictor_       = nullptr;

@@ -188,8 +188,10 @@ struct BlockCopy {
 
 // complex dense fills of symmetric H-matrices: the entries as generated, their
 // conjugates (the twin of a Hermitian block), or the Hermitian completion of
-// a diagonal block from its lower ('L') / upper ('U') triangle
-enum DenseMode : int { kDenseAsIs = 0, kDenseConj = 1, kDenseHermL = 2, kDenseHermU = 3 };
+// a diagonal block from its lower ('L') / upper ('U') triangle; kDenseNative:
+// the native complex layout (rows: points; columns: the doubled source
+// numbering, column 2j + c holding the real (c = 0) or imaginary part of D(i, j))
+enum DenseMode : int { kDenseAsIs = 0, kDenseConj = 1, kDenseHermL = 2, kDenseHermU = 3, kDenseNative = 4 };
 
 struct DenseChunk { // dense rows row0 .. row0+h (cluster numbering) x columns oj .. oj+n
     long long dst;

@@ -223,6 +223,7 @@ ClusterTree import_cluster(int n, const int *perm, int nnodes, const int *node_i
 // and their factors in the set_leaves layout.  Version 1 (no symmetry
 // record) still loads.
 void HMatrix::save(const std::string &path) {
+    require_real_form("saving");
     HTGPU_CUDA(cudaSetDevice(device_));
     std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
@@ -259,6 +260,7 @@ void HMatrix::save(const std::string &path) {
 // (rank -1), each list in htool's order; a complex H-matrix reports its
 // complex sizes and ranks (the real form doubles them)
 void HMatrix::save_plot(const std::string &outputname) const {
+    require_real_form("the leaf map");
     std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
     const int f = complex_ ? 2 : 1;
@@ -274,6 +276,7 @@ void HMatrix::save_plot(const std::string &outputname) const {
 }
 
 void HMatrix::load(const std::string &path) {
+    require_real_form("loading");
     std::ifstream f(path, std::ios::binary);
     require((bool)f, "cannot open " + path);
     char magic[8];

@@ -67,6 +67,9 @@ void launch_partial_aca_z(const AcaBlock *blocks, int nblocks, const double *xt,
 // complex crosses (PackItem sizes complex, offsets in doubles) -> real form
 // U2 (2M x 2r) at dst_u and Vt2 (2N x 2r) at dst_v
 void launch_pack_z(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st);
+// the same -> the native complex layout: Re U, Im U (M x r each) at dst_u,
+// the 2N x r tile of (Re, Im) Vt row pairs at dst_v
+void launch_pack_zn(const PackItem *items, int nitems, const double *scratch, double *arena, cudaStream_t st);
 
 // D[dst + i + h j] = G(perm_t[row0 + i], perm_s[oj + j]) for every chunk
 // (kd.id 2: the real form of the complex kernel, on doubled numberings)
@@ -88,6 +91,15 @@ void launch_phase1(const P1Item *items, int nitems, bool emu, const LrLeaf *lr, 
 void launch_reduce_tiles(const LrLeaf *lr, const int *multi, int nmulti, int mu, double *A, cudaStream_t st);
 // complex conjugate of n interleaved (re, im) doubles (dst may be src)
 void launch_conj(const double *src, double *dst, long long n, cudaStream_t st);
+// the native complex layout's three steps around the real product with 2 mu
+// right-hand sides: complex x (n points x mu, interleaved (re, im), ld n)
+// -> w (2n x 2mu, ld 2n) with rows 2p, 2p + 1 holding x_p and i x_p (each
+// complex right-hand side c as the real columns 2c, 2c + 1); i times the
+// phase-1 sums of every (src, dst) slot pair (A rows of mu values, mu even);
+// y (m x 2mu, ld m) -> complex out (m x mu, interleaved)
+void launch_zin(const double *x, int n, int mu, double *w, cudaStream_t st);
+void launch_rotate_slots(const int2 *rows, long long nrows, int mu, double *A, cudaStream_t st);
+void launch_zout(const double *y, int m, int mu, double *out, cudaStream_t st);
 // the same over float phase-1 sums (reduced-precision products)
 void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st);
 void launch_block_copy(const BlockCopy *items, int nitems, const double *src, double *dst, cudaStream_t st);

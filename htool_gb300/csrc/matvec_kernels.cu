@@ -441,6 +441,67 @@ void launch_conj(const double *src, double *dst, long long n, cudaStream_t st) {
     HTGPU_CUDA(cudaGetLastError());
 }
 
+// the native complex layout (a complex leaf U Vt^T applied as Re U times
+// the sums a = Vt^T x plus Im U times i a): input rows, the rotated sums,
+// the output
+__global__ void zin_kernel(const double *__restrict__ x, int n, int mu, double *__restrict__ w) {
+    const long long total = (long long)n * mu, ld = 2LL * n;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long p = e % n, c = e / n;
+        const double re = x[2 * e], im = x[2 * e + 1]; // e = c n + p
+        double *w0      = w + 2 * p + ld * 2 * c;
+        w0[0]           = re;
+        w0[ld]          = im;
+        w0[1]           = -im;
+        w0[ld + 1]      = re;
+    }
+}
+
+__global__ void rotate_slots_kernel(const int2 *__restrict__ rows, long long nrows, int mu, double *__restrict__ A) {
+    const int half        = mu >> 1;
+    const long long total = nrows * half;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int2 p    = rows[e / half];
+        const int c     = 2 * (int)(e % half);
+        const double re = A[(long long)p.x * mu + c], im = A[(long long)p.x * mu + c + 1];
+        A[(long long)p.y * mu + c]     = -im;
+        A[(long long)p.y * mu + c + 1] = re;
+    }
+}
+
+__global__ void zout_kernel(const double *__restrict__ y, int m, int mu, double *__restrict__ out) {
+    const long long total = (long long)m * mu;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long i = e % m, c = e / m;
+        out[2 * e]        = y[i + (long long)m * 2 * c];
+        out[2 * e + 1]    = y[i + (long long)m * (2 * c + 1)];
+    }
+}
+
+void launch_zin(const double *x, int n, int mu, double *w, cudaStream_t st) {
+    const long long total = (long long)n * mu;
+    if (total <= 0)
+        return;
+    zin_kernel<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(x, n, mu, w);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_rotate_slots(const int2 *rows, long long nrows, int mu, double *A, cudaStream_t st) {
+    const long long total = nrows * (mu >> 1);
+    if (total <= 0)
+        return;
+    rotate_slots_kernel<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(rows, nrows, mu, A);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_zout(const double *y, int m, int mu, double *out, cudaStream_t st) {
+    const long long total = (long long)m * mu;
+    if (total <= 0)
+        return;
+    zout_kernel<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(y, m, mu, out);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
 void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st) {
     if (nmulti <= 0)
         return;

@@ -145,6 +145,23 @@ int htgpu_hmatrix_destroy(htgpu_hmatrix h);
  * htgpu_hmatrix_mvprod_transp gives the plain transpose (htool's op 'T'). */
 int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilon, double eta, int device, htgpu_hmatrix *out);
 
+/* The storage of a complex handle, chosen before its build: 0 (default) the
+ * real form above; 1 the native complex layout, at half the factor and
+ * dense bytes of the real form (htool's own std::complex<double> storage:
+ * U, V and dense blocks at 16 bytes an entry, lrmat/lrmat.hpp:89-100): a
+ * leaf U V is stored as Re U, Im U and one tile holding the (Re, Im) pairs
+ * of V's entries, a dense block as the (Re, Im) pairs of its entries; a
+ * product runs the real kernels with twice the right-hand sides (the input
+ * as x and i x, the tiles' sums a followed by i a).  The native layout takes
+ * FP64 storage, symmetry 'N', partialACA and products in user numbering
+ * (htgpu_hmatrix_mvprod, batches, autotune); reduced precision, the digit
+ * planes, symmetric handles, transposed products, the allocation-free and
+ * global-to-local products, adopted leaves, factor exports and dumps return
+ * HTGPU_ERR_UNSUPPORTED.  htgpu_hmatrix_get_leaves describes the stored
+ * form (rows of points, source columns and ranks as stored). */
+int htgpu_hmatrix_set_complex_layout(htgpu_hmatrix h, int native);
+int htgpu_hmatrix_get_complex_layout(htgpu_hmatrix h, int *native);
+
 /* set_maxblocksize / set_mintargetdepth / set_minsourcedepth (hmatrix.hpp:213-215). */
 int htgpu_hmatrix_set_maxblocksize(htgpu_hmatrix h, unsigned int maxblocksize);
 int htgpu_hmatrix_set_mintargetdepth(htgpu_hmatrix h, unsigned int depth);

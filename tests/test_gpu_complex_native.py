@@ -1,0 +1,120 @@
+"""The native complex layout of a complex H-matrix (entries at 16 bytes, as
+htool's std::complex<double> leaves, lrmat/lrmat.hpp:89-100): Re U, Im U and
+one tile of the (Re, Im) pairs of V, dense blocks as (Re, Im) column pairs,
+a product run as the real one with twice the right-hand sides.  Checked
+against upstream htool's complex products (Helmholtz exp(i k r)/(4 pi r),
+k = 20, unit cube surface, eta 3, eps 1e-5) and against the real-form
+layout of the same H-matrix."""
+import numpy as np
+import pytest
+
+import htool_gb300 as H
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def pair(golden):
+    g, meta = golden("helmholtz_cube2000")
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+
+    def make(layout):
+        hm = H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128, complex_layout=layout)
+        return hm.build(H.HELMHOLTZ, g["xt"], kernel_param=meta["wavenumber"])
+
+    return g, meta, t, make("native"), make("real")
+
+
+def test_native_leaves_infos_and_bytes(pair):
+    g, meta, t, hn, hr = pair
+    assert hn.get_complex_layout() == "native" and hr.get_complex_layout() == "real"
+    # the stored form: rows and ranks of the points, source columns doubled
+    lr, dn = hn.get_leaves()
+    assert np.array_equal(lr[:, [0, 2, 4]], g["lr"][:, [0, 2, 4]])
+    assert np.array_equal(lr[:, [1, 3]], 2 * g["lr"][:, [1, 3]])
+    assert np.array_equal(dn[:, [0, 2]], g["dense"][:, [0, 2]])
+    assert np.array_equal(dn[:, [1, 3]], 2 * g["dense"][:, [1, 3]])
+    # htool's infos in complex units, as the real form reports them
+    inn, inr = hn.get_infos(), hr.get_infos()
+    for k in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_min", "Target_size", "Source_size", "Compression_ratio", "Dense_block_size_max", "Low_rank_block_size_max", "Local_size_max"):
+        assert inn[k] == inr[k], k
+    assert inn["GPU_complex"] == "2" and inr["GPU_complex"] == "1"
+    # every factor and dense entry at 16 bytes instead of 32
+    bn, br = hn.precision_info()["stored_bytes"], hr.precision_info()["stored_bytes"]
+    assert 2 * bn == br
+    nr, nc, _, _ = hn.sizes()
+    assert (nr, nc) == hr.sizes()[:2]
+
+
+def test_native_products_match_upstream(pair):
+    g, meta, t, hn, hr = pair
+    for mu in (1, 3):
+        x = g["x_mu%d" % mu]
+        y = hn.mvprod_global_to_global(x, mu)
+        assert y.dtype == np.complex128
+        assert rel(y, g["y_mu%d" % mu]) < 1e-10
+        # the same factors as the real form's, summed in another order
+        assert rel(y, hr.mvprod_global_to_global(x, mu)) < 1e-12
+    assert hn.device_status() == 0
+
+
+def test_native_many_right_hand_sides(pair):
+    """16 complex right-hand sides: the double-float kernels over 32 real
+    ones, against the real form and the single products."""
+    g, meta, t, hn, hr = pair
+    n = g["xt"].shape[0]
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal(n * 16) + 1j * rng.standard_normal(n * 16)
+    yn = hn.mvprod_global_to_global(X, 16)
+    assert rel(yn, hr.mvprod_global_to_global(X, 16)) < 1e-12
+    for c in (0, 7, 15):
+        col = slice(c * n, (c + 1) * n)
+        assert rel(yn[col], hn.mvprod_global_to_global(X[col].copy())) < 1e-12
+    assert hn.device_status() == 0
+
+
+def test_native_autotune_and_captured_batch(pair):
+    torch = pytest.importorskip("torch")
+    g, meta, t, hn, hr = pair
+    assert hn.autotune(1, reps=2) > 0
+    assert hn.autotune(3, reps=2) > 0
+    for mu in (1, 3):
+        assert rel(hn.mvprod_global_to_global(g["x_mu%d" % mu], mu), g["y_mu%d" % mu]) < 1e-10
+    x = torch.from_numpy(g["x_mu3"].copy()).cuda()
+    y = torch.zeros_like(x)
+    b = H.HBatch()
+    b.add(hn, torch.view_as_real(x).data_ptr(), torch.view_as_real(y).data_ptr(), 3, keep=(x, y))
+    b.capture(1)
+    y.zero_()
+    b.launch()
+    b.sync()
+    assert rel(y.cpu().numpy(), g["y_mu3"]) < 1e-10
+
+
+def test_native_refusals(pair, tmp_path):
+    g, meta, t, hn, hr = pair
+    with pytest.raises(NotImplementedError):  # a real H-matrix has no complex layout
+        H.HMatrix(t, t, 1e-5, 3.0, complex_layout="native")
+    with pytest.raises(NotImplementedError):
+        H.HMatrix(t, t, meta["eps"], meta["eta"], symmetry="S", UPLO="L", dtype=np.complex128, complex_layout="native")
+    with pytest.raises(NotImplementedError):  # chosen before the build
+        H._check(H.lib.htgpu_hmatrix_set_complex_layout(hn.h, 0))
+    refused = [
+        lambda: hn.set_precision("mixed"),
+        lambda: hn.set_digit_planes(True),
+        lambda: hn.mvprod_transp_global_to_global(g["x_mu1"]),
+        lambda: hn.get_factors(),
+        lambda: hn.save(str(tmp_path / "native.bin")),
+        lambda: hn.mymvprod_global_to_local(g["x_mu1"]),
+    ]
+    for call in refused:
+        with pytest.raises(NotImplementedError):
+            call()
+    # the handle is intact after the refusals
+    assert rel(hn.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-10
+    assert hn.device_status() == 0
