@@ -509,8 +509,10 @@ class HMatrix:
     def set_leaves(self, lr_desc, uv, dense_desc, dense):
         lr_desc = np.ascontiguousarray(lr_desc, dtype=np.int32)
         dense_desc = np.ascontiguousarray(dense_desc, dtype=np.int32)
-        uv = np.ascontiguousarray(uv, dtype=np.float64)
-        dense = np.ascontiguousarray(dense, dtype=np.float64)
+        # complex leaves (a handle in the native complex layout) go over as
+        # their interleaved (re, im) doubles
+        uv = np.ascontiguousarray(uv, dtype=np.complex128).view(np.float64) if np.iscomplexobj(uv) else np.ascontiguousarray(uv, dtype=np.float64)
+        dense = np.ascontiguousarray(dense, dtype=np.complex128).view(np.float64) if np.iscomplexobj(dense) else np.ascontiguousarray(dense, dtype=np.float64)
         _check(lib.htgpu_hmatrix_set_leaves(self.h, lr_desc.shape[0], _ptr(lr_desc), _ptr(uv), dense_desc.shape[0], _ptr(dense_desc), _ptr(dense)))
         return self
 

@@ -646,8 +646,76 @@ void HMatrix::build_impl(const KernelDesc *kdp, const HostGen *hg, const double 
     st_.build_seconds = now() - t0;
 }
 
+// the native complex layout: htool's complex leaves as they are (offsets,
+// sizes and ranks of the points; U m x r and V r x n column-major, dense
+// blocks m x n column-major, every entry interleaved (re, im)) -> Re U,
+// Im U, the tile of (Re, Im) pairs of V's columns (2n x r), the dense
+// blocks' (Re, Im) column pairs (m x 2n)
+void HMatrix::set_leaves_native(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dn) {
+    const int npts = nc / 2;
+    lr_h.clear();
+    dn_h.clear();
+    std::vector<LeafSrc> lr_src, dn_src;
+    long long total = 0;
+    for (int b = 0; b < nlr; b++) {
+        const int oi = lr_desc[5 * b], oj = lr_desc[5 * b + 1], m = lr_desc[5 * b + 2], n = lr_desc[5 * b + 3], r = lr_desc[5 * b + 4];
+        require(oi >= 0 && m > 0 && oi + m <= nr && oj >= 0 && n > 0 && oj + n <= npts && r >= 0, "low-rank leaf " + std::to_string(b) + " is out of range");
+        lr_h.push_back({oi, 2 * oj, m, 2 * n, r, 0, 0});
+        lr_src.push_back({0, total, total + 2LL * m * r});
+        total += 2LL * r * (m + n);
+    }
+    for (int b = 0; b < nd; b++) {
+        const int oi = d_desc[4 * b], oj = d_desc[4 * b + 1], m = d_desc[4 * b + 2], n = d_desc[4 * b + 3];
+        require(oi >= 0 && m > 0 && oi + m <= nr && oj >= 0 && n > 0 && oj + n <= npts, "dense leaf " + std::to_string(b) + " is out of range");
+        dn_h.push_back({oi, 2 * oj, m, 2 * n});
+        dn_src.push_back({0, total, 0});
+        total += 2LL * m * n;
+    }
+    std::vector<double> host(std::max<long long>(total, 1));
+    long long src = 0; // complex entries read
+    for (std::size_t l = 0; l < lr_h.size(); l++) {
+        const LrLeaf &L = lr_h[l];
+        const int m = L.m, n = L.n / 2, r = L.r;
+        const long long su = lr_src[l].su, sv = lr_src[l].sv;
+        for (long long e = 0; e < (long long)m * r; e++) { // U(i, k) at i + m k
+            host[su + e]                 = uv[2 * (src + e)];
+            host[su + (long long)m * r + e] = uv[2 * (src + e) + 1];
+        }
+        src += (long long)m * r;
+        for (int j = 0; j < n; j++) // V(k, j) at k + r j -> tile rows 2j, 2j + 1 of column k
+            for (int k = 0; k < r; k++) {
+                const long long e                         = src + k + (long long)r * j;
+                host[sv + 2 * j + 2LL * n * k]     = uv[2 * e];
+                host[sv + 2 * j + 1 + 2LL * n * k] = uv[2 * e + 1];
+            }
+        src += (long long)r * n;
+    }
+    long long dsrc = 0;
+    for (std::size_t d = 0; d < dn_h.size(); d++) {
+        const int m = dn_h[d].m, n = dn_h[d].n / 2;
+        const long long su = dn_src[d].su;
+        for (int j = 0; j < n; j++) // D(i, j) at i + m j -> columns 2j, 2j + 1
+            for (int i = 0; i < m; i++) {
+                const long long e                     = dsrc + i + (long long)m * j;
+                host[su + i + (long long)m * 2 * j]       = dn[2 * e];
+                host[su + i + (long long)m * (2 * j + 1)] = dn[2 * e + 1];
+            }
+        dsrc += (long long)m * n;
+    }
+    DevBuf<double> staging;
+    staging.upload(host, stream_);
+    HTGPU_CUDA(cudaStreamSynchronize(stream_));
+    st_ = BuildStats();
+    finalize({staging.p}, lr_src, &dn_src, nullptr, nullptr, nullptr);
+}
+
 void HMatrix::set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dn) {
-    require_real_form("adopting leaves");
+    HTGPU_CUDA(cudaSetDevice(device_));
+    if (znative_) {
+        nlr_stored_ = ndn_stored_ = -1;
+        set_leaves_native(nlr, lr_desc, uv, nd, d_desc, dn);
+        return;
+    }
     nlr_stored_ = ndn_stored_ = -1;
     HTGPU_CUDA(cudaSetDevice(device_));
     lr_h.clear();

@@ -133,7 +133,9 @@ class HMatrix {
     const std::vector<float> &aca_labels() const { return samples_y_; }
 
     // adopt leaves computed elsewhere (reference layout: U m x r col-major,
-    // V r x n col-major, dense m x n col-major), e.g. exported from htool
+    // V r x n col-major, dense m x n col-major), e.g. exported from htool;
+    // the native complex layout takes htool's complex leaves (sizes of the
+    // points, entries interleaved (re, im))
     void set_leaves(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dense);
 
     // y = H x for mu right-hand sides (column-major, leading dims nc / nr).
@@ -359,6 +361,7 @@ class HMatrix {
     DevBuf<int2> rot_d;
     DevBuf<double> zw_, zy_;
     void require_real_form(const char *what) const;
+    void set_leaves_native(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dense);
     std::unique_ptr<HMatrix> transp_; // transposed twin, built on first use
     long long aca_budget_ = 0;
     Mlp *predictor_       = nullptr;

@@ -156,8 +156,9 @@ int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilo
  * FP64 storage, symmetry 'N', partialACA and products in user numbering
  * (htgpu_hmatrix_mvprod, batches, autotune); reduced precision, the digit
  * planes, symmetric handles, transposed products, the allocation-free and
- * global-to-local products, adopted leaves, factor exports and dumps return
- * HTGPU_ERR_UNSUPPORTED.  htgpu_hmatrix_get_leaves describes the stored
+ * global-to-local products, factor exports and dumps return
+ * HTGPU_ERR_UNSUPPORTED; htgpu_hmatrix_set_leaves takes htool's complex
+ * leaves.  htgpu_hmatrix_get_leaves describes the stored
  * form (rows of points, source columns and ranks as stored). */
 int htgpu_hmatrix_set_complex_layout(htgpu_hmatrix h, int native);
 int htgpu_hmatrix_get_complex_layout(htgpu_hmatrix h, int *native);
@@ -248,7 +249,11 @@ int htgpu_hmatrix_set_compression(htgpu_hmatrix h, int compressor);
  * dense = each dense leaf m x n column-major.  Host memory; copied.  On a
  * handle with symmetry 'S' / 'H' the leaves are one triangle (diagonal
  * blocks dense and square, no block together with its mirror) and the
- * product adds every off-diagonal leaf's (conjugate) transpose. */
+ * product adds every off-diagonal leaf's (conjugate) transpose.  A complex
+ * handle in real form takes the leaves of the real form (every offset, size
+ * and rank doubled, entries z as [[re, -im], [im, re]]); one in the native
+ * complex layout takes htool's complex leaves as they are (sizes of the
+ * points, uv and dense as interleaved (re, im) doubles). */
 int htgpu_hmatrix_set_leaves(htgpu_hmatrix h, int nlr, const int *lr_desc, const double *uv, int ndense, const int *d_desc, const double *dense);
 
 /* Replaces HMatrix<double>::mvprod_global_to_global(in, out, mu)

@@ -13,8 +13,9 @@ separates the product's error from the assembly's (whose complex factors
 differ from upstream's in the last bits).
 
 The library stores a complex H-matrix in real form on doubled trees
-(entry z -> [[re, -im], [im, re]]); the leaves are handed over in that
-form through htgpu_hmatrix_set_leaves.
+(entry z -> [[re, -im], [im, re]]), whose leaves are handed over in that
+form through htgpu_hmatrix_set_leaves, or in the native complex layout
+(16 bytes an entry), which takes upstream's complex leaves as they are.
 """
 import os
 
@@ -147,3 +148,29 @@ def test_gpu_products_over_upstreams_complex_leaves():
         assert rel(y, g["y_mu%d" % mu]) < FP64_TOL, mu
         assert rel(hm.mvprod_transp_global_to_global(x, mu), g["yT_mu%d" % mu]) < FP64_TOL, mu
     assert hm.device_status() == 0
+
+
+@pytest.mark.gpu
+def test_gpu_native_layout_over_upstreams_complex_leaves():
+    """the native complex layout given upstream's complex leaves as they
+    are: products within the FP64 tolerance of upstream's (mu = 1, 3, and
+    after autotuning), at half the real form's stored bytes"""
+    import htool_gb300 as H
+
+    g = load()
+    n = g["xt"].shape[0]
+    t = H.Cluster().build(n, g["xt"])
+    hn = H.HMatrix(t, t, 1e-5, 3.0, dtype=np.complex128, complex_layout="native")
+    hn.set_leaves(g["lr"], g["uv"], g["dense"], g["dd"])
+    lr, dn = hn.get_leaves()  # the stored form: source columns doubled
+    assert np.array_equal(lr[:, [0, 2, 4]], g["lr"][:, [0, 2, 4]]) and np.array_equal(lr[:, [1, 3]], 2 * g["lr"][:, [1, 3]])
+    assert np.array_equal(dn[:, [0, 2]], g["dense"][:, [0, 2]]) and np.array_equal(dn[:, [1, 3]], 2 * g["dense"][:, [1, 3]])
+    for mu in (1, 3):
+        y = hn.mvprod_global_to_global(g["x_mu%d" % mu], mu)
+        assert rel(y, g["y_mu%d" % mu]) < FP64_TOL, mu
+    hr = H.HMatrix(t, t, 1e-5, 3.0, dtype=np.complex128)
+    hr.set_leaves(*real_form_leaves(g))
+    assert 2 * hn.precision_info()["stored_bytes"] == hr.precision_info()["stored_bytes"]
+    hn.autotune(1, reps=2)
+    assert rel(hn.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < FP64_TOL
+    assert hn.device_status() == 0
