@@ -544,8 +544,10 @@ class HMatrix:
         lr, dn = self.get_leaves()
         nuv = int(np.sum(lr[:, 4].astype(np.int64) * (lr[:, 2] + lr[:, 3])))
         nd = int(np.sum(dn[:, 2].astype(np.int64) * dn[:, 3]))
-        uv = np.empty(max(nuv, 1))
-        dd = np.empty(max(nd, 1))
+        # the native complex layout exports htool's complex leaves
+        dt = np.complex128 if self.complex and self.get_complex_layout() == "native" else np.float64
+        uv = np.empty(max(nuv, 1), dt)
+        dd = np.empty(max(nd, 1), dt)
         _check(lib.htgpu_hmatrix_get_factors(self.h, _ptr(uv), _ptr(dd)))
         return lr, dn, uv[:nuv], dd[:nd]
 

@@ -2346,7 +2346,58 @@ void HMatrix::phase_bytes(int mu, long long *b) const {
 }
 
 void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptrs, cudaStream_t st) {
-    require_real_form("the transposed product");
+    if (znative_) {
+        // the native complex layout: a twin holding the plain transpose
+        // (U' = V^T, V' = U^T, D' = D^T; htool's op 'T') in the same layout
+        require(mu >= 1, "number of right-hand sides must be positive");
+        HTGPU_CUDA(cudaSetDevice(device_));
+        if (!transp_) {
+            const int nl = n_lowrank(), nd = n_dense();
+            std::vector<int> lr(5 * (std::size_t)nl), dn(4 * (std::size_t)nd);
+            leaf_descriptors(lr.data(), dn.data());
+            long long nuv = 0, ndd = 0; // complex entries
+            for (int b = 0; b < nl; b++)
+                nuv += (long long)lr[5 * b + 4] * (lr[5 * b + 2] + lr[5 * b + 3]);
+            for (int b = 0; b < nd; b++)
+                ndd += (long long)dn[4 * b + 2] * dn[4 * b + 3];
+            std::vector<double> uv(2 * std::max<long long>(nuv, 1)), dd(2 * std::max<long long>(ndd, 1)), uvt(uv.size()), ddt(dd.size());
+            export_native(uv.data(), dd.data());
+            long long o = 0;
+            for (int b = 0; b < nl; b++) {
+                const int m = lr[5 * b + 2], n = lr[5 * b + 3], r = lr[5 * b + 4];
+                const long long U = o, V = o + (long long)m * r, Ut = o, Vt = o + (long long)n * r;
+                for (int c = 0; c < 2; c++) {
+                    for (int k = 0; k < r; k++)
+                        for (int j = 0; j < n; j++)
+                            uvt[2 * (Ut + j + (long long)n * k) + c] = uv[2 * (V + k + (long long)r * j) + c]; // U' = V^T (n x r)
+                    for (int i = 0; i < m; i++)
+                        for (int k = 0; k < r; k++)
+                            uvt[2 * (Vt + k + (long long)r * i) + c] = uv[2 * (U + i + (long long)m * k) + c]; // V' = U^T (r x m)
+                }
+                std::swap(lr[5 * b], lr[5 * b + 1]);
+                std::swap(lr[5 * b + 2], lr[5 * b + 3]);
+                o += (long long)r * (m + n);
+            }
+            o = 0;
+            for (int b = 0; b < nd; b++) {
+                const int m = dn[4 * b + 2], n = dn[4 * b + 3];
+                for (int c = 0; c < 2; c++)
+                    for (int j = 0; j < n; j++)
+                        for (int i = 0; i < m; i++)
+                            ddt[2 * (o + j + (long long)n * i) + c] = dd[2 * (o + i + (long long)m * j) + c];
+                std::swap(dn[4 * b], dn[4 * b + 1]);
+                std::swap(dn[4 * b + 2], dn[4 * b + 3]);
+                o += (long long)m * n;
+            }
+            auto t = std::unique_ptr<HMatrix>(new HMatrix(Sz_, Tz_, eps_, eta_, device_, true));
+            t->set_complex_layout(true);
+            t->set_leaves(nl, lr.data(), uvt.data(), nd, dn.data(), ddt.data());
+            t->set_fp64_split(p1_permille_, p2_n64_);
+            transp_ = std::move(t);
+        }
+        transp_->mvprod(in, out, mu, host_ptrs, kUserNumbering, st);
+        return;
+    }
     if (symmetry_ == 'S') { // H^T = H
         mvprod(in, out, mu, host_ptrs, false, st);
         return;
@@ -2440,24 +2491,79 @@ void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptr
 }
 
 void HMatrix::leaf_descriptors(int *lr_desc, int *d_desc) const {
+    const int fs = znative_ ? 2 : 1; // the native complex layout describes htool's complex leaves
     for (int b = 0; b < n_lowrank(); b++) {
         lr_desc[5 * b]     = lr_h[b].oi;
-        lr_desc[5 * b + 1] = lr_h[b].oj;
+        lr_desc[5 * b + 1] = lr_h[b].oj / fs;
         lr_desc[5 * b + 2] = lr_h[b].m;
-        lr_desc[5 * b + 3] = lr_h[b].n;
+        lr_desc[5 * b + 3] = lr_h[b].n / fs;
         lr_desc[5 * b + 4] = lr_h[b].r;
     }
     for (int b = 0; b < n_dense(); b++) {
         d_desc[4 * b]     = dn_h[b].oi;
-        d_desc[4 * b + 1] = dn_h[b].oj;
+        d_desc[4 * b + 1] = dn_h[b].oj / fs;
         d_desc[4 * b + 2] = dn_h[b].m;
-        d_desc[4 * b + 3] = dn_h[b].n;
+        d_desc[4 * b + 3] = dn_h[b].n / fs;
+    }
+}
+
+// the inverse of the native complex layout: htool's complex leaves, every
+// entry as interleaved (re, im) doubles
+void HMatrix::export_native(double *uv, double *dn) {
+    std::vector<double> host(std::max<long long>(arena_len, 1));
+    if (arena_len)
+        HTGPU_CUDA(cudaMemcpy(host.data(), fac.p, sizeof(double) * arena_len, cudaMemcpyDeviceToHost));
+    std::vector<long long> u_at(lr_h.size()), v_at(lr_h.size()), d_at(dn_h.size()); // in complex entries
+    long long o = 0;
+    for (std::size_t l = 0; l < lr_h.size(); l++) {
+        u_at[l] = o;
+        o += (long long)lr_h[l].m * lr_h[l].r;
+        v_at[l] = o;
+        o += (long long)(lr_h[l].n / 2) * lr_h[l].r;
+    }
+    o = 0;
+    for (std::size_t d = 0; d < dn_h.size(); d++) {
+        d_at[d] = o;
+        o += (long long)dn_h[d].m * (dn_h[d].n / 2);
+    }
+    if (uv)
+        for (auto &it : p1_h) { // tile rows 2j + c: part c of V(k, j)
+            const LrLeaf &L = lr_h[it.leaf];
+            for (int k = 0; k < L.r; k++)
+                for (int jj = 0; jj < it.jlen; jj++) {
+                    const int row = it.j0 + jj;
+                    uv[2 * (v_at[it.leaf] + k + (long long)L.r * (row >> 1)) + (row & 1)] = host[it.off + jj + (long long)it.jlen * k];
+                }
+        }
+    for (std::size_t q = 0; q < p2_h.size(); q++) {
+        const P2Item &it = p2_h[q];
+        const int row0   = p2_row_h[q];
+        for (int c = it.cbeg; c < it.cend; c++) {
+            const int leaf      = c_leaf[c];
+            const P2Contrib &pc = c_h[c];
+            if (leaf >= 0 && uv) { // Re U on the sums, Im U on i times the sums
+                const LrLeaf &L = lr_h[leaf];
+                const int part  = pc.aux == (int)L.a_off ? 0 : 1;
+                for (int k = 0; k < L.r; k++)
+                    for (int i = 0; i < it.h; i++)
+                        uv[2 * (u_at[leaf] + (row0 - L.oi + i) + (long long)L.m * k) + part] = host[pc.off + i + (long long)it.h * k];
+            } else if (leaf < 0 && dn) { // column 2j + c: part c of D(:, j)
+                const DenseLeaf &D = dn_h[~leaf];
+                for (int j = 0; j < D.n; j++)
+                    for (int i = 0; i < it.h; i++)
+                        dn[2 * (d_at[~leaf] + (row0 - D.oi + i) + (long long)D.m * (j >> 1)) + (j & 1)] = host[pc.off + i + (long long)it.h * j];
+            }
+        }
     }
 }
 
 // inverse of the final layout, into htool's layouts
 void HMatrix::export_factors(double *uv, double *dn) {
-    require_real_form("exporting the factors");
+    if (znative_) {
+        HTGPU_CUDA(cudaSetDevice(device_));
+        export_native(uv, dn);
+        return;
+    }
     HTGPU_CUDA(cudaSetDevice(device_));
     std::vector<double> host(std::max<long long>(arena_len, 1));
     if (arena_len)

@@ -362,6 +362,7 @@ class HMatrix {
     DevBuf<double> zw_, zy_;
     void require_real_form(const char *what) const;
     void set_leaves_native(int nlr, const int *lr_desc, const double *uv, int nd, const int *d_desc, const double *dense);
+    void export_native(double *uv, double *dense);
     std::unique_ptr<HMatrix> transp_; // transposed twin, built on first use
     long long aca_budget_ = 0;
     Mlp *predictor_       = nullptr;

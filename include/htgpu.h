@@ -154,12 +154,13 @@ int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilo
  * product runs the real kernels with twice the right-hand sides (the input
  * as x and i x, the tiles' sums a followed by i a).  The native layout takes
  * FP64 storage, symmetry 'N', partialACA and products in user numbering
- * (htgpu_hmatrix_mvprod, batches, autotune); reduced precision, the digit
- * planes, symmetric handles, transposed products, the allocation-free and
- * global-to-local products, factor exports and dumps return
- * HTGPU_ERR_UNSUPPORTED; htgpu_hmatrix_set_leaves takes htool's complex
- * leaves.  htgpu_hmatrix_get_leaves describes the stored
- * form (rows of points, source columns and ranks as stored). */
+ * (htgpu_hmatrix_mvprod, htgpu_hmatrix_mvprod_transp: the plain transpose
+ * from a twin in the same layout, batches, autotune); reduced precision,
+ * the digit planes, symmetric handles, the allocation-free and
+ * global-to-local products and dumps return HTGPU_ERR_UNSUPPORTED.
+ * htgpu_hmatrix_set_leaves / get_leaves / get_factors take and give
+ * htool's complex leaves (sizes of the points, entries as interleaved
+ * (re, im) doubles). */
 int htgpu_hmatrix_set_complex_layout(htgpu_hmatrix h, int native);
 int htgpu_hmatrix_get_complex_layout(htgpu_hmatrix h, int *native);
 

@@ -153,8 +153,9 @@ def test_gpu_products_over_upstreams_complex_leaves():
 @pytest.mark.gpu
 def test_gpu_native_layout_over_upstreams_complex_leaves():
     """the native complex layout given upstream's complex leaves as they
-    are: products within the FP64 tolerance of upstream's (mu = 1, 3, and
-    after autotuning), at half the real form's stored bytes"""
+    are: exported back bit for bit, products and transposed products within
+    the FP64 tolerance of upstream's (mu = 1, 3, and after autotuning), at
+    half the real form's stored bytes"""
     import htool_gb300 as H
 
     g = load()
@@ -162,12 +163,13 @@ def test_gpu_native_layout_over_upstreams_complex_leaves():
     t = H.Cluster().build(n, g["xt"])
     hn = H.HMatrix(t, t, 1e-5, 3.0, dtype=np.complex128, complex_layout="native")
     hn.set_leaves(g["lr"], g["uv"], g["dense"], g["dd"])
-    lr, dn = hn.get_leaves()  # the stored form: source columns doubled
-    assert np.array_equal(lr[:, [0, 2, 4]], g["lr"][:, [0, 2, 4]]) and np.array_equal(lr[:, [1, 3]], 2 * g["lr"][:, [1, 3]])
-    assert np.array_equal(dn[:, [0, 2]], g["dense"][:, [0, 2]]) and np.array_equal(dn[:, [1, 3]], 2 * g["dense"][:, [1, 3]])
+    lr, dn, uv, dd = hn.get_factors()  # given back bit for bit
+    assert np.array_equal(lr, g["lr"]) and np.array_equal(dn, g["dense"])
+    assert np.array_equal(uv, g["uv"]) and np.array_equal(dd, g["dd"])
     for mu in (1, 3):
         y = hn.mvprod_global_to_global(g["x_mu%d" % mu], mu)
         assert rel(y, g["y_mu%d" % mu]) < FP64_TOL, mu
+        assert rel(hn.mvprod_transp_global_to_global(g["x_mu%d" % mu], mu), g["yT_mu%d" % mu]) < FP64_TOL, mu
     hr = H.HMatrix(t, t, 1e-5, 3.0, dtype=np.complex128)
     hr.set_leaves(*real_form_leaves(g))
     assert 2 * hn.precision_info()["stored_bytes"] == hr.precision_info()["stored_bytes"]

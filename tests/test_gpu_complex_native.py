@@ -5,6 +5,8 @@ a product run as the real one with twice the right-hand sides.  Checked
 against upstream htool's complex products (Helmholtz exp(i k r)/(4 pi r),
 k = 20, unit cube surface, eta 3, eps 1e-5) and against the real-form
 layout of the same H-matrix."""
+import os
+
 import numpy as np
 import pytest
 
@@ -33,12 +35,11 @@ def pair(golden):
 def test_native_leaves_infos_and_bytes(pair):
     g, meta, t, hn, hr = pair
     assert hn.get_complex_layout() == "native" and hr.get_complex_layout() == "real"
-    # the stored form: rows and ranks of the points, source columns doubled
+    # upstream's complex leaves (the real form's, halved)
     lr, dn = hn.get_leaves()
-    assert np.array_equal(lr[:, [0, 2, 4]], g["lr"][:, [0, 2, 4]])
-    assert np.array_equal(lr[:, [1, 3]], 2 * g["lr"][:, [1, 3]])
-    assert np.array_equal(dn[:, [0, 2]], g["dense"][:, [0, 2]])
-    assert np.array_equal(dn[:, [1, 3]], 2 * g["dense"][:, [1, 3]])
+    assert np.array_equal(lr, g["lr"]) and np.array_equal(dn, g["dense"])
+    lr2, dn2 = hr.get_leaves()
+    assert np.array_equal(lr2 // 2, lr) and np.array_equal(dn2 // 2, dn)
     # htool's infos in complex units, as the real form reports them
     inn, inr = hn.get_infos(), hr.get_infos()
     for k in ("Number_of_lrmat", "Number_of_dmat", "Rank_max", "Rank_min", "Target_size", "Source_size", "Compression_ratio", "Dense_block_size_max", "Low_rank_block_size_max", "Local_size_max"):
@@ -107,8 +108,6 @@ def test_native_refusals(pair, tmp_path):
     refused = [
         lambda: hn.set_precision("mixed"),
         lambda: hn.set_digit_planes(True),
-        lambda: hn.mvprod_transp_global_to_global(g["x_mu1"]),
-        lambda: hn.get_factors(),
         lambda: hn.save(str(tmp_path / "native.bin")),
         lambda: hn.mymvprod_global_to_local(g["x_mu1"]),
     ]
@@ -117,4 +116,26 @@ def test_native_refusals(pair, tmp_path):
             call()
     # the handle is intact after the refusals
     assert rel(hn.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-10
+    assert hn.device_status() == 0
+
+
+def test_native_transposed_products_and_factor_round_trip(pair):
+    """htool's op 'T' from the native twin against upstream's transposed
+    products; the exported complex factors, adopted by a new native handle,
+    give the same products"""
+    g, meta, t, hn, hr = pair
+    gt = np.load(os.path.join(os.path.dirname(__file__), "golden", "helmholtz_cube2000_transp.npz"))
+    for mu in (1, 3):
+        yt = hn.mvprod_transp_global_to_global(gt["xT_mu%d" % mu], mu)
+        assert rel(yt, gt["yT_mu%d" % mu]) < 1e-10
+        assert rel(yt, hr.mvprod_transp_global_to_global(gt["xT_mu%d" % mu], mu)) < 1e-12
+    lr, dn, uv, dd = hn.get_factors()
+    assert uv.dtype == np.complex128 and dd.dtype == np.complex128
+    h2 = H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128, complex_layout="native")
+    h2.set_leaves(lr, uv, dn, dd)
+    lr2, dn2, uv2, dd2 = h2.get_factors()
+    assert np.array_equal(uv2, uv) and np.array_equal(dd2, dd)
+    # the same leaves (hn runs its autotuned kernels, h2 the defaults)
+    y = hn.mvprod_global_to_global(g["x_mu3"], 3)
+    assert rel(h2.mvprod_global_to_global(g["x_mu3"], 3), y) < 1e-13
     assert hn.device_status() == 0
