@@ -223,15 +223,17 @@ ClusterTree import_cluster(int n, const int *perm, int nnodes, const int *node_i
 // and their factors in the set_leaves layout.  Version 1 (no symmetry
 // record) still loads.
 void HMatrix::save(const std::string &path) {
-    require_real_form("saving");
     HTGPU_CUDA(cudaSetDevice(device_));
     std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
+    // doubles of the set_leaves layout (the native complex layout: htool's
+    // complex leaves, two doubles an entry)
+    const long long fe = znative_ ? 2 : 1;
     long long nuv = 0, ndd = 0;
     for (int l = 0; l < n_lowrank(); l++)
-        nuv += (long long)lr_h[l].r * (lr_h[l].m + lr_h[l].n);
+        nuv += fe * lr[5 * l + 4] * ((long long)lr[5 * l + 2] + lr[5 * l + 3]);
     for (int d = 0; d < n_dense(); d++)
-        ndd += (long long)dn_h[d].m * dn_h[d].n;
+        ndd += fe * dn[4 * d + 2] * (long long)dn[4 * d + 3];
     std::vector<double> uv(std::max<long long>(nuv, 1)), dd(std::max<long long>(ndd, 1));
     export_factors(uv.data(), dd.data());
     std::ofstream f(path, std::ios::binary);
@@ -240,7 +242,7 @@ void HMatrix::save(const std::string &path) {
     const std::int64_t hdr[4]   = {nr, nc, (std::int64_t)n_lowrank(), (std::int64_t)n_dense()};
     const double par[2]         = {eps_, eta_};
     const std::uint64_t hash[2] = {fnv1a(T->perm), fnv1a(S->perm)};
-    const char sym[8]           = {symmetry_, uplo_, (char)(complex_ ? 1 : 0), 0, 0, 0, 0, 0};
+    const char sym[8]           = {symmetry_, uplo_, (char)(complex_ ? 1 : 0), (char)(znative_ ? 1 : 0), 0, 0, 0, 0};
     f.write(kMagic, 8);
     f.write((const char *)&version, 4);
     f.write((const char *)hdr, sizeof(hdr));
@@ -260,14 +262,14 @@ void HMatrix::save(const std::string &path) {
 // (rank -1), each list in htool's order; a complex H-matrix reports its
 // complex sizes and ranks (the real form doubles them)
 void HMatrix::save_plot(const std::string &outputname) const {
-    require_real_form("the leaf map");
     std::vector<int> lr(5 * (std::size_t)n_lowrank()), dn(4 * (std::size_t)n_dense());
     leaf_descriptors(lr.data(), dn.data());
-    const int f = complex_ ? 2 : 1;
+    // the real form's descriptors are doubled, the native layout's complex
+    const int f = complex_ && !znative_ ? 2 : 1;
     const std::string path = outputname + "_0.csv";
     std::ofstream out(path);
     require((bool)out, "cannot write " + path, 3);
-    out << nr / f << "," << nc / f << "\n";
+    out << nr / f << "," << nc / (complex_ ? 2 : 1) << "\n";
     for (int d = 0; d < n_dense(); d++)
         out << dn[4 * d] / f << "," << dn[4 * d + 2] / f << "," << dn[4 * d + 1] / f << "," << dn[4 * d + 3] / f << "," << -1 << "\n";
     for (int l = 0; l < n_lowrank(); l++)
@@ -276,7 +278,6 @@ void HMatrix::save_plot(const std::string &outputname) const {
 }
 
 void HMatrix::load(const std::string &path) {
-    require_real_form("loading");
     std::ifstream f(path, std::ios::binary);
     require((bool)f, "cannot open " + path);
     char magic[8];
@@ -296,6 +297,8 @@ void HMatrix::load(const std::string &path) {
         f.read(sym, 8);
     require((bool)f, path + " is truncated");
     require((sym[2] != 0) == complex_, path + (complex_ ? " holds a real H-matrix" : " holds a complex H-matrix"));
+    require((sym[3] != 0) == znative_, path + (znative_ ? " holds a complex H-matrix in real form" : " holds a complex H-matrix in the native layout"));
+    const long long fe = znative_ ? 2 : 1; // doubles an entry
     set_symmetry(sym[0], sym[1]); // the dump's storage (checks the combination and the trees)
     const std::int64_t nlr = hdr[2], nd = hdr[3];
     require(nlr >= 0 && nd >= 0 && nlr < (1LL << 31) && nd < (1LL << 31), path + ": bad leaf counts");
@@ -305,9 +308,9 @@ void HMatrix::load(const std::string &path) {
     require((bool)f, path + " is truncated");
     long long nuv = 0, ndd = 0;
     for (std::int64_t b = 0; b < nlr; b++)
-        nuv += (long long)lr[5 * b + 4] * (lr[5 * b + 2] + lr[5 * b + 3]);
+        nuv += fe * lr[5 * b + 4] * ((long long)lr[5 * b + 2] + lr[5 * b + 3]);
     for (std::int64_t b = 0; b < nd; b++)
-        ndd += (long long)dn[4 * b + 2] * dn[4 * b + 3];
+        ndd += fe * dn[4 * b + 2] * (long long)dn[4 * b + 3];
     std::vector<double> uv(std::max<long long>(nuv, 1)), dd(std::max<long long>(ndd, 1));
     f.read((char *)uv.data(), sizeof(double) * nuv);
     f.read((char *)dd.data(), sizeof(double) * ndd);

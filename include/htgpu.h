@@ -157,7 +157,8 @@ int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilo
  * (htgpu_hmatrix_mvprod, htgpu_hmatrix_mvprod_transp: the plain transpose
  * from a twin in the same layout, batches, autotune); reduced precision,
  * the digit planes, symmetric handles, the allocation-free and
- * global-to-local products and dumps return HTGPU_ERR_UNSUPPORTED.
+ * global-to-local products return HTGPU_ERR_UNSUPPORTED; dumps record the
+ * layout and reload into a handle of the same layout.
  * htgpu_hmatrix_set_leaves / get_leaves / get_factors take and give
  * htool's complex leaves (sizes of the points, entries as interleaved
  * (re, im) doubles). */

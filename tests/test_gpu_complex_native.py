@@ -108,7 +108,6 @@ def test_native_refusals(pair, tmp_path):
     refused = [
         lambda: hn.set_precision("mixed"),
         lambda: hn.set_digit_planes(True),
-        lambda: hn.save(str(tmp_path / "native.bin")),
         lambda: hn.mymvprod_global_to_local(g["x_mu1"]),
     ]
     for call in refused:
@@ -139,3 +138,18 @@ def test_native_transposed_products_and_factor_round_trip(pair):
     y = hn.mvprod_global_to_global(g["x_mu3"], 3)
     assert rel(h2.mvprod_global_to_global(g["x_mu3"], 3), y) < 1e-13
     assert hn.device_status() == 0
+
+
+def test_native_dump_and_leaf_map(pair, tmp_path):
+    """a dump of a native handle reloads into a native handle (and only
+    there); its leaf map is the real form's"""
+    g, meta, t, hn, hr = pair
+    hn.save(str(tmp_path / "native.bin"))
+    h2 = H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128, complex_layout="native").load(str(tmp_path / "native.bin"))
+    assert np.array_equal(h2.get_factors()[2], hn.get_factors()[2])
+    assert rel(h2.mvprod_global_to_global(g["x_mu1"]), g["y_mu1"]) < 1e-10
+    with pytest.raises(ValueError):
+        H.HMatrix(t, t, meta["eps"], meta["eta"], dtype=np.complex128).load(str(tmp_path / "native.bin"))
+    hn.save_plot(str(tmp_path / "native"))
+    hr.save_plot(str(tmp_path / "real"))
+    assert open(tmp_path / "native_0.csv").read() == open(tmp_path / "real_0.csv").read()
