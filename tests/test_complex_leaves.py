@@ -118,6 +118,44 @@ def test_real_form_is_a_product_homomorphism():
     assert np.allclose(real_form(U) @ real_form(V), real_form(U @ V), rtol=0, atol=1e-14 * np.abs(U @ V).max())
 
 
+def native_input(x):
+    """the native layout's real input (2n x 2mu) of complex x (n x mu): rows
+    2p, 2p + 1 hold x_p and i x_p, complex column c as real columns 2c, 2c + 1"""
+    n, mu = x.shape
+    W = np.empty((2 * n, 2 * mu))
+    W[0::2, 0::2], W[0::2, 1::2] = x.real, x.imag
+    W[1::2, 0::2], W[1::2, 1::2] = -x.imag, x.real
+    return W
+
+
+def test_native_layout_applies_the_complex_leaves():
+    """CPU: the native complex layout's real product with twice the
+    right-hand sides -- a tile of (Re, Im) pairs of V's columns summed over
+    (x, i x), Re U applied to those sums a and Im U to i a, dense blocks as
+    (Re, Im) column pairs -- is the complex product of upstream's leaves"""
+    g = load()
+    lrs, dns = split_leaves(g)
+    rng = np.random.default_rng(3)
+    for _, _, U, V in lrs[:: max(1, len(lrs) // 7)]:
+        m, r = U.shape
+        n = V.shape[1]
+        x = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+        tile = np.empty((2 * n, r))
+        tile[0::2], tile[1::2] = V.T.real, V.T.imag
+        a = tile.T @ native_input(x)  # r x 2mu: the complex sums as (re, im) columns
+        ia = np.empty_like(a)
+        ia[:, 0::2], ia[:, 1::2] = -a[:, 1::2], a[:, 0::2]
+        Y = U.real @ a + U.imag @ ia
+        assert np.allclose(Y[:, 0::2] + 1j * Y[:, 1::2], U @ (V @ x), rtol=0, atol=1e-13 * np.abs(U @ (V @ x)).max())
+    for _, _, D in dns[:: max(1, len(dns) // 7)]:
+        m, n = D.shape
+        x = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+        Dn = np.empty((m, 2 * n))
+        Dn[:, 0::2], Dn[:, 1::2] = D.real, D.imag
+        Y = Dn @ native_input(x)
+        assert np.allclose(Y[:, 0::2] + 1j * Y[:, 1::2], D @ x, rtol=0, atol=1e-13 * np.abs(D @ x).max())
+
+
 def test_cluster_tree_is_upstreams():
     """CPU: this library's cluster tree of the fixture's points has
     upstream's permutation, so the leaves land in the same numbering"""
