@@ -1506,8 +1506,6 @@ void HMatrix::set_rhs_bucket(int mu, int mu_run) {
 void HMatrix::set_precision(int policy, double tau) {
     layout_gen_++; // buffers or launch lists change: captured products are stale
     require(policy >= 0 && policy <= 3, "precision policy must be 0 (FP64), 1 (FP32), 2 (FP32/BF16) or 3 (BF16)");
-    if (policy != 0)
-        require_real_form("reduced-precision storage");
     require(tau > 0, "tau must be positive");
     HTGPU_CUDA(cudaSetDevice(device_));
     precision_ = policy;
@@ -1535,7 +1533,7 @@ void HMatrix::set_precision(int policy, double tau) {
     for (auto &it : p2_h)
         for (int c = it.cbeg; c < it.cend; c++)
             if (c_leaf[c] >= 0)
-                jobs.push_back({c_h[c].off, it.h, lr_h[c_leaf[c]].r, (int)lr_h[c_leaf[c]].a_off, 0});
+                jobs.push_back({c_h[c].off, it.h, lr_h[c_leaf[c]].r, c_h[c].aux, 0}); // the contribution's slots (native complex: Im U at i a's)
     DevBuf<unsigned> cmax;
     cmax.alloc(2 * std::max<long long>(a_slots, 1));
     HTGPU_CUDA(cudaMemsetAsync(cmax.p, 0, sizeof(unsigned) * cmax.n, stream_));
@@ -1547,6 +1545,15 @@ void HMatrix::set_precision(int policy, double tau) {
     }
     std::vector<unsigned> cm(cmax.n);
     HTGPU_CUDA(cudaMemcpy(cm.data(), cmax.p, sizeof(unsigned) * cm.size(), cudaMemcpyDeviceToHost));
+    if (znative_) {
+        // one scale for the Re U and Im U columns of a complex column (both
+        // multiply the same sums, a and i a): the larger maximum, for both
+        for (const int2 &p : rot_h) {
+            const unsigned u = std::max(cm[p.x], cm[p.y]); // non-negative floats order as their bits
+            cm[p.x] = cm[p.y] = u;
+        }
+        HTGPU_CUDA(cudaMemcpy(cmax.p, cm.data(), sizeof(unsigned) * cm.size(), cudaMemcpyHostToDevice));
+    }
     auto asf = [](unsigned u) {
         float f;
         std::memcpy(&f, &u, 4);
@@ -1630,7 +1637,7 @@ void HMatrix::set_precision(int policy, double tau) {
                     const LrLeaf &L = lr_h[c_leaf[c]];
                     const int k0 = part == 0 ? 0 : c32[c_leaf[c]], k1 = part == 0 ? c32[c_leaf[c]] : L.r;
                     for (int k = k0; k < k1; k++) {
-                        cim.push_back((int)L.a_off + k);
+                        cim.push_back(c_h[c].aux + k);
                         srcoff.push_back(c_h[c].off + (long long)h * k);
                     }
                 }
@@ -1663,8 +1670,8 @@ void HMatrix::set_precision(int policy, double tau) {
         n_cols_m_ += n64;
         mixed_bytes_ += 8LL * h * n64;
     }
-    for (std::size_t l = 0; l < lr_h.size(); l++)
-        mixed_bytes_ += (4LL * c32[l] + 2LL * (lr_h[l].r - c32[l])) * (lr_h[l].m + lr_h[l].n);
+    for (std::size_t l = 0; l < lr_h.size(); l++) // the native complex layout stores Re U and Im U
+        mixed_bytes_ += (4LL * c32[l] + 2LL * (lr_h[l].r - c32[l])) * ((znative_ ? 2LL : 1LL) * lr_h[l].m + lr_h[l].n);
     mix_.alloc(std::max<long long>(off, 16));
     scale_d.upload(scale, stream_);
     {
@@ -1948,6 +1955,10 @@ void HMatrix::launch_product_with(const double *x, double *y, int mu_out, int nu
         }
         if (!multi_h.empty()) {
             launch_reduce_tiles_f(lr_d.p, multi_d.p, (int)multi_h.size(), mu, reinterpret_cast<float *>(w_A), st); // float sums
+            launches_++;
+        }
+        if (!rot_h.empty()) { // native complex layout: i times the (float) sums
+            launch_rotate_slots_f(rot_d.p, (long long)rot_h.size(), mu, reinterpret_cast<float *>(w_A), st);
             launches_++;
         }
         if (marks)
@@ -2395,6 +2406,8 @@ void HMatrix::mvprod_transp(const double *in, double *out, int mu, bool host_ptr
             t->set_fp64_split(p1_permille_, p2_n64_);
             transp_ = std::move(t);
         }
+        if (transp_->precision() != precision_ || (precision_ != 0 && transp_->tau_ != tau_))
+            transp_->set_precision(precision_, tau_);
         transp_->mvprod(in, out, mu, host_ptrs, kUserNumbering, st);
         return;
     }

@@ -99,6 +99,7 @@ void launch_conj(const double *src, double *dst, long long n, cudaStream_t st);
 // y (m x 2mu, ld m) -> complex out (m x mu, interleaved)
 void launch_zin(const double *x, int n, int mu, double *w, cudaStream_t st);
 void launch_rotate_slots(const int2 *rows, long long nrows, int mu, double *A, cudaStream_t st);
+void launch_rotate_slots_f(const int2 *rows, long long nrows, int mu, float *A, cudaStream_t st); // float sums
 void launch_zout(const double *y, int m, int mu, double *out, cudaStream_t st);
 // the same over float phase-1 sums (reduced-precision products)
 void launch_reduce_tiles_f(const LrLeaf *lr, const int *multi, int nmulti, int mu, float *A, cudaStream_t st);

@@ -457,13 +457,15 @@ __global__ void zin_kernel(const double *__restrict__ x, int n, int mu, double *
     }
 }
 
-__global__ void rotate_slots_kernel(const int2 *__restrict__ rows, long long nrows, int mu, double *__restrict__ A) {
+// T: double sums (FP64 storage) or float sums (reduced precision)
+template <typename T>
+__global__ void rotate_slots_kernel(const int2 *__restrict__ rows, long long nrows, int mu, T *__restrict__ A) {
     const int half        = mu >> 1;
     const long long total = nrows * half;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-        const int2 p    = rows[e / half];
-        const int c     = 2 * (int)(e % half);
-        const double re = A[(long long)p.x * mu + c], im = A[(long long)p.x * mu + c + 1];
+        const int2 p = rows[e / half];
+        const int c  = 2 * (int)(e % half);
+        const T re = A[(long long)p.x * mu + c], im = A[(long long)p.x * mu + c + 1];
         A[(long long)p.y * mu + c]     = -im;
         A[(long long)p.y * mu + c + 1] = re;
     }
@@ -490,7 +492,15 @@ void launch_rotate_slots(const int2 *rows, long long nrows, int mu, double *A, c
     const long long total = nrows * (mu >> 1);
     if (total <= 0)
         return;
-    rotate_slots_kernel<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(rows, nrows, mu, A);
+    rotate_slots_kernel<double><<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(rows, nrows, mu, A);
+    HTGPU_CUDA(cudaGetLastError());
+}
+
+void launch_rotate_slots_f(const int2 *rows, long long nrows, int mu, float *A, cudaStream_t st) {
+    const long long total = nrows * (mu >> 1);
+    if (total <= 0)
+        return;
+    rotate_slots_kernel<float><<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, st>>>(rows, nrows, mu, A);
     HTGPU_CUDA(cudaGetLastError());
 }
 

@@ -106,7 +106,6 @@ def test_native_refusals(pair, tmp_path):
     with pytest.raises(NotImplementedError):  # chosen before the build
         H._check(H.lib.htgpu_hmatrix_set_complex_layout(hn.h, 0))
     refused = [
-        lambda: hn.set_precision("mixed"),
         lambda: hn.set_digit_planes(True),
         lambda: hn.mymvprod_global_to_local(g["x_mu1"]),
     ]
@@ -153,3 +152,29 @@ def test_native_dump_and_leaf_map(pair, tmp_path):
     hn.save_plot(str(tmp_path / "native"))
     hr.save_plot(str(tmp_path / "real"))
     assert open(tmp_path / "native_0.csv").read() == open(tmp_path / "real_0.csv").read()
+
+
+def test_native_reduced_precision(pair):
+    """FP32/BF16 factors in the native layout (one scale for the Re U and
+    Im U columns of a complex column): 1 and 3 right-hand sides on the CUDA
+    cores, 16 on the tensor cores, and the transposed product, within
+    epsilon of the FP64 products, at about half the real form's bytes"""
+    g, meta, t, hn, hr = pair
+    n = g["xt"].shape[0]
+    rng = np.random.default_rng(17)
+    X = rng.standard_normal(n * 16) + 1j * rng.standard_normal(n * 16)
+    y64 = {mu: hn.mvprod_global_to_global(X[: n * mu].copy(), mu) for mu in (1, 3, 16)}
+    yt64 = hn.mvprod_transp_global_to_global(X[:n].copy())
+    try:
+        hn.set_precision("mixed")
+        hr.set_precision("mixed")
+        assert hn.precision_info()["stored_bytes"] < 0.6 * hr.precision_info()["stored_bytes"]
+        for mu in (1, 3, 16):
+            assert rel(hn.mvprod_global_to_global(X[: n * mu].copy(), mu), y64[mu]) < meta["eps"], mu
+        assert rel(hn.mvprod_transp_global_to_global(X[:n].copy()), yt64) < meta["eps"]
+        assert hn.autotune(1, reps=2) > 0
+        assert rel(hn.mvprod_global_to_global(X[:n].copy()), y64[1]) < meta["eps"]
+        assert hn.device_status() == 0
+    finally:
+        hn.set_precision("fp64")
+        hr.set_precision("fp64")
