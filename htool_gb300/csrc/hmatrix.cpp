@@ -1123,9 +1123,11 @@ void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, int 
         st = stream_;
     if (znative_) {
         // complex x (nc / 2 points) -> its real form w, the real product with
-        // 2 mu right-hand sides, its output -> complex y (nr points)
-        require(numbering == kUserNumbering, "the native complex layout takes products in user numbering", 2);
+        // 2 mu right-hand sides, its output -> complex y (nr points, or the
+        // local rows); the point order of x and y is the numbering's, and
+        // the doubled rows of w keep it
         ensure_work(rhs_run(2 * mu));
+        const int mout = numbering == kGlobalToLocal ? local_row_count() : nr;
         const double *x = in;
         double *y       = out;
         if (host_ptrs) {
@@ -1134,11 +1136,11 @@ void HMatrix::mvprod(const double *in, double *out, int mu, bool host_ptrs, int 
             y = ystage.p;
         }
         launch_zin(x, nc / 2, mu, zw_.p, st);
-        launch_product(zw_.p, zy_.p, 2 * mu, kUserNumbering, st);
-        launch_zout(zy_.p, nr, mu, y, st);
+        launch_product(zw_.p, zy_.p, 2 * mu, numbering, st);
+        launch_zout(zy_.p, mout, mu, y, st);
         launches_ += 2;
         if (host_ptrs) {
-            HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * 2 * (std::size_t)nr * mu, cudaMemcpyDeviceToHost, st));
+            HTGPU_CUDA(cudaMemcpyAsync(out, ystage.p, sizeof(double) * 2 * (std::size_t)mout * mu, cudaMemcpyDeviceToHost, st));
             HTGPU_CUDA(cudaStreamSynchronize(st));
             int status = 0;
             HTGPU_CUDA(cudaMemcpy(&status, status_d.p, sizeof(int), cudaMemcpyDeviceToHost));

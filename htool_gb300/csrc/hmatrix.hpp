@@ -93,7 +93,7 @@ class HMatrix {
     // p as x_p and i x_p), a leaf U Vt^T stored as Re U, Im U and one tile of
     // (Re, Im) Vt row pairs, a dense block D as its (Re, Im) column pairs, and
     // a product with mu right-hand sides runs as the real one with 2 mu
-    // ('N' symmetry, partialACA, user numbering)
+    // ('N' symmetry, partialACA)
     void set_complex_layout(bool native);
     bool complex_native() const { return znative_; }
     ~HMatrix();

@@ -153,12 +153,13 @@ int htgpu_hmatrix_create_complex(htgpu_cluster t, htgpu_cluster s, double epsilo
  * of V's entries, a dense block as the (Re, Im) pairs of its entries; a
  * product runs the real kernels with twice the right-hand sides (the input
  * as x and i x, the tiles' sums a followed by i a).  The native layout takes
- * symmetry 'N', partialACA and products in user numbering
- * (htgpu_hmatrix_mvprod, htgpu_hmatrix_mvprod_transp: the plain transpose
- * from a twin in the same layout, batches, autotune), FP64 or reduced
- * precision (one column scale for the Re U and Im U columns of a complex
- * column); the digit planes, symmetric handles, the allocation-free and
- * global-to-local products return HTGPU_ERR_UNSUPPORTED; dumps record the
+ * symmetry 'N' and partialACA, FP64 or reduced precision (one column
+ * scale for the Re U and Im U columns of a complex column), and every
+ * product but the allocation-free one (htgpu_hmatrix_mvprod in any
+ * numbering, htgpu_hmatrix_mvprod_global_to_local,
+ * htgpu_hmatrix_mvprod_transp: the plain transpose from a twin in the same
+ * layout, batches, autotune); the digit planes, symmetric handles and the
+ * allocation-free product return HTGPU_ERR_UNSUPPORTED; dumps record the
  * layout and reload into a handle of the same layout.
  * htgpu_hmatrix_set_leaves / get_leaves / get_factors take and give
  * htool's complex leaves (sizes of the points, entries as interleaved

@@ -107,7 +107,6 @@ def test_native_refusals(pair, tmp_path):
         H._check(H.lib.htgpu_hmatrix_set_complex_layout(hn.h, 0))
     refused = [
         lambda: hn.set_digit_planes(True),
-        lambda: hn.mymvprod_global_to_local(g["x_mu1"]),
     ]
     for call in refused:
         with pytest.raises(NotImplementedError):
@@ -178,3 +177,24 @@ def test_native_reduced_precision(pair):
     finally:
         hn.set_precision("fp64")
         hr.set_precision("fp64")
+
+
+def test_native_cluster_numbering_and_global_to_local(pair):
+    """products with input and output in cluster numbering, and htool's
+    mymvprod_global_to_local (one rank: every row local), in the native
+    layout: the user-numbering product permuted"""
+    torch = pytest.importorskip("torch")
+    g, meta, t, hn, hr = pair
+    n = g["xt"].shape[0]
+    perm = t.get_perm()
+    X = g["x_mu3"].reshape(3, n)
+    Y = hn.mvprod_global_to_global(g["x_mu3"], 3).reshape(3, n)
+    Xc = np.ascontiguousarray(X[:, perm]).ravel()  # cluster numbering
+    yl = hn.mymvprod_global_to_local(Xc, 3).reshape(3, n)
+    assert rel(yl, Y[:, perm]) < 1e-13
+    xd = torch.from_numpy(Xc.copy()).cuda()
+    yd = torch.zeros_like(xd)
+    hn.mvprod_ptr(torch.view_as_real(xd).data_ptr(), torch.view_as_real(yd).data_ptr(), 3, H.CLUSTER_NUMBERING, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rel(yd.cpu().numpy().reshape(3, n), Y[:, perm]) < 1e-13
+    assert hn.device_status() == 0
