@@ -2351,6 +2351,8 @@ void HMatrix::profile(int mu, int reps, float *ms) {
 }
 
 void HMatrix::phase_bytes(int mu, long long *b) const {
+    if (znative_)
+        mu *= 2; // the real product behind mu complex right-hand sides
     const bool red = precision_ != 0;
     b[0]           = 8LL * nc * mu * 4 + 4LL * nc;                                          // x twice (exponent, gather), xp and xs, perm
     b[1]           = (red ? p1_bytes_m_ : p1_bytes_) + 8LL * a_slots * mu;                  // V-side factors, partial sums
@@ -2639,7 +2641,9 @@ long long HMatrix::stored_bytes() const {
     return b;
 }
 
-long long HMatrix::product_bytes(int mu) const { return stored_bytes() + 8LL * mu * (nr + nc) + 4LL * (nr + nc); }
+long long HMatrix::product_bytes(int mu) const { // the native complex layout's rows are points: 16 bytes an output entry
+    return stored_bytes() + 8LL * mu * ((znative_ ? 2LL : 1LL) * nr + nc) + 4LL * (nr + nc);
+}
 
 // HMatrix::ComputeInfos keys (hmatrix.hpp:739-841) for one rank, plus
 // GPU assembly counters
